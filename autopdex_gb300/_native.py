@@ -1,0 +1,114 @@
+"""ctypes binding of libautopdex_gb300 (C ABI in include/autopdex_gb300.h).
+
+The library is loaded from the package's ``_lib`` folder.  There is no fallback: if the
+shared library is missing or fails to load, every entry point raises.
+"""
+import ctypes as C
+import os
+import re
+
+from . import build as _build
+
+AGX_OK = 0
+AGX_NOT_CONVERGED = 1
+AGX_DIVERGED = 2
+
+AGX_QUAD4, AGX_HEX8, AGX_LINE2 = 0, 1, 2
+AGX_MODEL_POISSON_SINCOS = 0
+AGX_MODEL_HEAT_POTENTIAL = 1
+AGX_MODEL_NEO_HOOKE = 2
+AGX_MODEL_NEUMANN = 3
+AGX_MODEL_HEAT_BE = 4
+AGX_F64, AGX_F32 = 0, 1
+AGX_PCG, AGX_PCG_MIXED, AGX_BICGSTAB, AGX_FCG_MIXED = 0, 1, 2, 3
+
+PRECOND_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p)
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("method", C.c_int), ("rtol", C.c_double), ("atol", C.c_double), ("maxiter", C.c_int),
+                ("check_every", C.c_int)]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("rel_residual", C.c_double), ("status", C.c_int)]
+
+
+class NewtonOpts(C.Structure):
+    _fields_ = [("newton_tol", C.c_double), ("newton_rtol", C.c_double), ("maxiter", C.c_int), ("damping", C.c_double),
+                ("tangent_dtype", C.c_int), ("krylov", SolveOpts), ("reuse_tangent", C.c_int),
+                ("verbose", C.c_int)]
+
+
+class NewtonInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("res_norm", C.c_double), ("res0", C.c_double), ("diverged", C.c_int),
+                ("krylov_iterations", C.c_int), ("n_history", C.c_int),
+                ("res_history", C.c_double * 64), ("krylov_history", C.c_int * 64)]
+
+
+_P = C.c_void_p
+_SIGNATURES = {
+    "agx_create": (C.c_int, [C.POINTER(_P), _P]),
+    "agx_destroy": (C.c_int, [_P]),
+    "agx_last_error": (C.c_char_p, [_P]),
+    "agx_set_nodes": (C.c_int, [_P, C.c_int64, C.c_int, _P, C.c_int]),
+    "agx_add_element_set": (C.c_int, [_P, C.c_int, C.c_int64, C.c_int, _P, C.POINTER(C.c_int)]),
+    "agx_set_dirichlet": (C.c_int, [_P, _P]),
+    "agx_finalize": (C.c_int, [_P]),
+    "agx_set_model": (C.c_int, [_P, C.c_int, C.c_int, _P, C.c_int]),
+    "agx_set_element_field": (C.c_int, [_P, C.c_int, _P]),
+    "agx_set_node_field": (C.c_int, [_P, C.c_int, _P]),
+    "agx_assemble": (C.c_int, [_P, _P, _P, C.c_int]),
+    "agx_get_matrix": (C.c_int, [_P, C.c_int, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(C.c_int64)]),
+    "agx_copy_matrix": (C.c_int, [_P, C.c_int, _P, _P, _P]),
+    "agx_spmv": (C.c_int, [_P, C.c_int, _P, _P]),
+    "agx_solve": (C.c_int, [_P, _P, _P, C.POINTER(SolveOpts), C.POINTER(SolveInfo)]),
+    "agx_newton": (C.c_int, [_P, _P, _P, C.POINTER(NewtonOpts), C.POINTER(NewtonInfo)]),
+    "agx_set_preconditioner": (C.c_int, [_P, PRECOND_FN, _P]),
+    "agx_get_sizes": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
+}
+
+_lib = None
+
+
+def header_symbols():
+    """Function names declared in include/autopdex_gb300.h."""
+    path = os.path.join(_build.INCLUDE, "autopdex_gb300.h")
+    with open(path) as fh:
+        txt = fh.read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(agx_\w+)\s*\(", txt, re.M)))
+
+
+def lib_path():
+    return _build.lib_path()
+
+
+def load(path=None):
+    """Load the shared library (building it first when it is absent or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if path is None:
+        path = _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError(f"libautopdex_gb300 not found at {path}; run autopdex_gb300.build.build()")
+    lib = C.CDLL(path)
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class NativeError(RuntimeError):
+    def __init__(self, fn, code, msg):
+        super().__init__(f"{fn} failed with status {code}: {msg}")
+        self.code = code
+
+
+def check(ctx, fn, code):
+    if code < 0:
+        msg = load().agx_last_error(ctx).decode(errors="replace") if ctx else ""
+        raise NativeError(fn, code, msg)
+    return code

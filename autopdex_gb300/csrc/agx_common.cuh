@@ -1,0 +1,137 @@
+// Shared declarations of the GB300 solve backend: context layout, error handling and
+// small device helpers.  Everything here is internal; the public C ABI lives in
+// include/autopdex_gb300.h.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/autopdex_gb300.h"
+
+#define AGX_MAX_PARAMS 16
+#define AGX_MAX_HISTORY 64
+
+// Threads per block for every streaming kernel; grids are multiples of the SM count.
+#define AGX_BLOCK 256
+
+struct agx_element_set {
+  int elem_type = -1;        // AGX_QUAD4 / AGX_HEX8 / AGX_LINE2
+  int nen = 0;               // nodes per element
+  int64_t n_elem = 0;
+  int32_t* d_conn = nullptr; // n_elem * nen
+  int32_t* d_epos = nullptr; // n_elem * nen * nen node-block positions in the BSR pattern
+  std::vector<int32_t> h_conn;
+  int model = -1;
+  int n_params = 0;
+  double params[AGX_MAX_PARAMS] = {0};
+  double* d_elem_field = nullptr;        // one value per element (owned)
+  const double* d_node_field = nullptr;  // one value per DOF (caller-owned device pointer)
+};
+
+// Scalars of one Krylov solve, kept in device memory so that iterations need no host
+// round trip.  Written only by the last block of a reduction kernel.
+struct agx_krylov_scalars {
+  double rz;         // (r, z) of the current iterate
+  double rr;         // (r, r)
+  double pq;         // (p, A p)
+  double alpha, beta;
+  double rr_stop;    // stop when rr <= rr_stop
+  double omega, rho, rhat_v, ts, tt;  // BiCGStab scalars
+  double rz_old;     // flexible CG: (r_old, z_old)
+  double extra[4];
+  int converged;     // 1: tolerance met, 2: breakdown (zero or non-finite denominator)
+  int iters;         // iterations completed
+  int pad[2];
+};
+
+struct agx_context {
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int device = 0;
+  int sm_count = 152;
+
+  // nodes and DOFs
+  int64_t n_nodes = 0;
+  int dim = 0;
+  int ndof = 0;            // DOFs per node (BSR block size)
+  int64_t n_dofs = 0;
+  double* d_coords = nullptr;   // n_nodes * dim
+  std::vector<agx_element_set> sets;
+
+  // Dirichlet DOFs
+  std::vector<uint8_t> h_dmask;          // n_dofs
+  uint8_t* d_dmask_node = nullptr;       // n_nodes, bit c set if component c is prescribed
+  uint8_t* d_dmask_dof = nullptr;        // n_dofs, 1 if prescribed
+  int32_t* d_dir_dofs = nullptr;         // list of prescribed DOFs
+  int64_t n_dir = 0;
+
+  // BSR pattern (node blocks of ndof x ndof)
+  bool pattern_ready = false;
+  int64_t nnzb = 0;
+  int32_t* d_rowptr = nullptr;  // n_nodes + 1
+  int32_t* d_col = nullptr;     // nnzb
+  int32_t* d_diagpos = nullptr; // n_nodes
+  double* d_vals64 = nullptr;   // nnzb * ndof^2
+  float* d_vals32 = nullptr;
+  double* d_dinv64 = nullptr;   // inverse diagonal (Jacobi)
+  float* d_dinv32 = nullptr;
+  int tangent_valid = -1;       // dtype of the last assembled tangent, -1 none
+
+  // Newton / Krylov work vectors (double)
+  double *d_R = nullptr, *d_b = nullptr, *d_dx = nullptr;
+  double *d_r = nullptr, *d_z = nullptr, *d_p = nullptr, *d_q = nullptr;
+  double *d_s = nullptr, *d_t = nullptr, *d_rhat = nullptr, *d_v = nullptr;
+  // single-precision Krylov vectors (mixed precision inner solve)
+  float *f_x = nullptr, *f_r = nullptr, *f_z = nullptr, *f_p = nullptr, *f_q = nullptr, *f_rold = nullptr;
+
+  // reductions
+  int red_blocks = 0;
+  double* d_partials = nullptr;          // red_blocks * 4
+  unsigned int* d_counter = nullptr;
+  agx_krylov_scalars* d_scal = nullptr;
+  agx_krylov_scalars* h_scal = nullptr;  // pinned
+  double* d_norm = nullptr;              // 4 doubles
+  double* h_norm = nullptr;              // pinned
+
+  // learned preconditioner hook (set by the host layer; null = Jacobi)
+  agx_precond_fn precond = nullptr;
+  void* precond_user = nullptr;
+};
+
+// ------------------------------------------------------------------------------------
+// error handling: every entry point returns an int status and records a message
+// ------------------------------------------------------------------------------------
+int agx_fail(agx_context* ctx, int code, const char* fmt, ...);
+
+#define AGX_CUDA(ctx, call)                                                          \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess)                                                           \
+      return agx_fail((ctx), AGX_ERR_CUDA, "%s failed: %s (%s:%d)", #call,           \
+                      cudaGetErrorString(e_), __FILE__, __LINE__);                   \
+  } while (0)
+
+#define AGX_CHECK_LAUNCH(ctx) AGX_CUDA((ctx), cudaGetLastError())
+
+// internal entry points shared across translation units
+int agx_build_pattern(agx_context* ctx);
+int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, int tangent_dtype);
+int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_solve_opts* opts,
+                    agx_solve_info* info);
+int agx_residual_norm(agx_context* ctx, const double* R, double* norm2, double* nonfinite);
+void agx_launch_masked_scale(agx_context* ctx, const double* src, double* dst, double s);
+void agx_launch_set_dirichlet(agx_context* ctx, double* dofs, const double* values);
+void agx_launch_newton_update(agx_context* ctx, double* dofs, const double* dx, const double* values,
+                              double damping);
+void agx_launch_negate_free(agx_context* ctx, const double* R, double* b);
+int agx_spmv_impl(agx_context* ctx, int dtype, const void* x, void* y);
+
+static inline int agx_grid(const agx_context* ctx, int64_t n, int per_sm = 8) {
+  int64_t want = (n + AGX_BLOCK - 1) / AGX_BLOCK;
+  int64_t cap = (int64_t)ctx->sm_count * per_sm;
+  if (want < 1) want = 1;
+  return (int)(want < cap ? want : cap);
+}

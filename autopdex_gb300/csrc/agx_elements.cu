@@ -1,0 +1,449 @@
+// Element residual / tangent assembly for the built-in Q1 models.
+//
+// Replaces the per-element AD of AutoPDEx (jacrev / jacfwd(jacrev) under vmap / lax.map,
+// assembler.py:1064-1149, :1216-1306, :1310-1389) and the scatter-adds of _get_residual
+// (assembler.py:331-436) and of the BCOO tangent (assembler.py:1142-1148, summed later by
+// scipy_assembling, solver.py:1180-1222).
+//
+// Mapping to the GPU: a group of NEN consecutive lanes handles one element, lane a owning
+// element node a.  Per Gauss point each lane evaluates its own shape function N_a and
+// physical gradient g_a = dN_a/dxi J^-1 (the rule of fem_iso_line_quad_brick with
+// overwrite_diff=True, spaces.py:12162-12190); element sums (Jacobian, field values and
+// gradients at the point) are butterfly reductions inside the group, and the values of
+// the other nodes needed for row a of the tangent are read from a per-warp shared-memory
+// slab.  Lane a accumulates residual entries R_a and tangent row K_ab in registers and adds
+// them into the residual vector and the node-block CSR values at positions precomputed by
+// agx_build_pattern.  Entries of prescribed rows/columns are skipped (Dirichlet row and
+// column deletion of scipy_assembling); prescribed diagonals are set to one beforehand.
+//
+// The element formulas are the closed forms of what the reference differentiates:
+//   potential 1/2 k |grad u|^2 - s u        R_a = k grad u . g_a - s N_a,  K_ab = k g_a . g_b
+//   neo-Hooke (Ciarlet, models.py:1122-1146), P = mu F + c F^-T, c = lam/2 (J^2-1) - mu
+//     R_a,i = P_iJ g_a,J
+//     K_ab,ik = mu (g_a.g_b) d_ik - c h_b,i h_a,k + lam J^2 h_a,i h_b,k,  h = F^-T g
+//   backward-Euler heat rho_c (T-T_n)/dt v + k(T) grad T . grad v, k = k0 + k2 T^2
+//     K_ab = rho_c/dt N_a N_b + k g_a.g_b + k'(T) N_b grad T . g_a   (non-symmetric)
+//   Neumann traction (models.py:744-780, :1818-1827)  R_a,i = -N_a t_i |dX/dxi|
+// all times the Gauss weight and det J; the oracle derives the same quantities by AD.
+#include "agx_common.cuh"
+
+namespace {
+
+template <int ET>
+struct ElemTraits;
+template <>
+struct ElemTraits<AGX_QUAD4> {
+  static constexpr int RDIM = 2, NEN = 4, NQ = 4;
+};
+template <>
+struct ElemTraits<AGX_HEX8> {
+  static constexpr int RDIM = 3, NEN = 8, NQ = 8;
+};
+template <>
+struct ElemTraits<AGX_LINE2> {
+  static constexpr int RDIM = 1, NEN = 2, NQ = 2;
+};
+
+// 2-point Gauss-Legendre on [-1, 1] from the [0, 1] rule of seeder.py:382-386 mapped as
+// seeder.py:1053-1058; weights 2 * 0.5 = 1.
+__device__ __forceinline__ double gauss_point(int i) {
+  return i ? (2.0 * 0.7886751345948129 - 1.0) : (2.0 * 0.21132486540518713 - 1.0);
+}
+
+// reference-node sign of node a in direction d (node orders of spaces.py:1913-1922,
+// :12057-12081, :356-358)
+template <int ET>
+__device__ __forceinline__ int node_sign(int a, int d) {
+  if (ET == AGX_LINE2) return a ? 1 : -1;
+  if (d == 0) return (a & 3) == 1 || (a & 3) == 2 ? 1 : -1;
+  if (d == 1) return (a & 3) >= 2 ? 1 : -1;
+  return a >= 4 ? 1 : -1;
+}
+
+template <int NEN, typename T>
+__device__ __forceinline__ T group_sum(T v) {
+#pragma unroll
+  for (int o = NEN / 2; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T det2(const T (&m)[2][2]) { return m[0][0] * m[1][1] - m[0][1] * m[1][0]; }
+template <typename T>
+__device__ __forceinline__ T det3(const T (&m)[3][3]) {
+  return m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) - m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+         m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+}
+// inverse by the adjugate (utility.py:706-770)
+template <typename T, int D>
+__device__ __forceinline__ T inverse(const T (&m)[D][D], T (&inv)[D][D]) {
+  if constexpr (D == 2) {
+    T d = det2(m), r = T(1) / d;
+    inv[0][0] = m[1][1] * r; inv[0][1] = -m[0][1] * r;
+    inv[1][0] = -m[1][0] * r; inv[1][1] = m[0][0] * r;
+    return d;
+  } else {
+    T d = det3(m), r = T(1) / d;
+    inv[0][0] = (m[1][1] * m[2][2] - m[1][2] * m[2][1]) * r;
+    inv[0][1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) * r;
+    inv[0][2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) * r;
+    inv[1][0] = (m[1][2] * m[2][0] - m[1][0] * m[2][2]) * r;
+    inv[1][1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) * r;
+    inv[1][2] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]) * r;
+    inv[2][0] = (m[1][0] * m[2][1] - m[1][1] * m[2][0]) * r;
+    inv[2][1] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]) * r;
+    inv[2][2] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) * r;
+    return d;
+  }
+}
+
+struct ModelParams {
+  double p[AGX_MAX_PARAMS];
+};
+
+template <int MODEL, int SDIM>
+struct ModelTraits {
+  static constexpr int NDOF = (MODEL == AGX_MODEL_NEO_HOOKE || MODEL == AGX_MODEL_NEUMANN) ? SDIM : 1;
+  static constexpr bool HAS_K = MODEL != AGX_MODEL_NEUMANN;
+  static constexpr int SLOTS = 1 + SDIM + (MODEL == AGX_MODEL_NEO_HOOKE ? SDIM : 0);  // N, g, h
+};
+
+// One kernel per (element type, model, arithmetic type, what to compute).
+template <int ET, int MODEL, typename T, bool DO_R, bool DO_K>
+__global__ void __launch_bounds__(AGX_BLOCK)
+element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* __restrict__ epos,
+               const double* __restrict__ coords, const double* __restrict__ dofs,
+               const double* __restrict__ elem_field, const double* __restrict__ node_field,
+               const uint8_t* __restrict__ dmask_node, ModelParams mp, double* __restrict__ R,
+               T* __restrict__ vals) {
+  using ET_ = ElemTraits<ET>;
+  constexpr int RDIM = ET_::RDIM, NEN = ET_::NEN, NQ = ET_::NQ;
+  constexpr int SDIM = (ET == AGX_HEX8) ? 3 : 2;
+  using MT = ModelTraits<MODEL, SDIM>;
+  constexpr int NDOF = MT::NDOF, SLOTS = MT::SLOTS;
+
+  __shared__ T slab[AGX_BLOCK / 32][32][SLOTS];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int a = lane % NEN, gbase = lane - a;
+  const int64_t total = ((n_elem * NEN + 31) / 32) * 32;
+
+  for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total;
+       L += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e_raw = L / NEN;
+    const bool valid = e_raw < n_elem;
+    const int64_t e = valid ? e_raw : (n_elem - 1);
+    const int node = conn[e * NEN + a];
+
+    T xa[SDIM];
+#pragma unroll
+    for (int d = 0; d < SDIM; ++d) xa[d] = (T)coords[(int64_t)node * SDIM + d];
+    T ua[NDOF];
+#pragma unroll
+    for (int c = 0; c < NDOF; ++c) ua[c] = (MODEL == AGX_MODEL_NEUMANN) ? T(0) : (T)dofs[(int64_t)node * NDOF + c];
+    T tna = 0;
+    if constexpr (MODEL == AGX_MODEL_HEAT_BE) tna = (T)node_field[node];
+    T ke = 1;
+    if constexpr (MODEL == AGX_MODEL_HEAT_POTENTIAL) ke = elem_field ? (T)elem_field[e] : T(1);
+
+    double Ra[NDOF];
+#pragma unroll
+    for (int c = 0; c < NDOF; ++c) Ra[c] = 0.0;
+    T K[DO_K ? NEN : 1][DO_K ? NDOF : 1][DO_K ? NDOF : 1];
+    if constexpr (DO_K) {
+#pragma unroll
+      for (int b = 0; b < NEN; ++b)
+#pragma unroll
+        for (int i = 0; i < NDOF; ++i)
+#pragma unroll
+          for (int j = 0; j < NDOF; ++j) K[b][i][j] = 0;
+    }
+
+#pragma unroll 1
+    for (int q = 0; q < NQ; ++q) {
+      // shape function and reference derivatives of node a
+      T fac[RDIM], xi[RDIM];
+#pragma unroll
+      for (int d = 0; d < RDIM; ++d) {
+        xi[d] = (T)gauss_point((q >> d) & 1);
+        fac[d] = (T(1) + T(node_sign<ET>(a, d)) * xi[d]) * T(0.5);
+      }
+      T Na = 1;
+#pragma unroll
+      for (int d = 0; d < RDIM; ++d) Na *= fac[d];
+      T dN[RDIM];
+#pragma unroll
+      for (int d = 0; d < RDIM; ++d) {
+        T v = T(node_sign<ET>(a, d)) * T(0.5);
+#pragma unroll
+        for (int d2 = 0; d2 < RDIM; ++d2)
+          if (d2 != d) v *= fac[d2];
+        dN[d] = v;
+      }
+      // isoparametric Jacobian dX/dxi
+      T J[SDIM][RDIM];
+#pragma unroll
+      for (int i = 0; i < SDIM; ++i)
+#pragma unroll
+        for (int j = 0; j < RDIM; ++j) J[i][j] = group_sum<NEN>(xa[i] * dN[j]);
+
+      if constexpr (MODEL == AGX_MODEL_NEUMANN) {
+        // line in 2-D: |G1 x E3| = |G1| (models.py:1818-1823); weight 1
+        T len = sqrt(J[0][0] * J[0][0] + J[1][0] * J[1][0]);
+        if constexpr (DO_R) {
+#pragma unroll
+          for (int c = 0; c < NDOF; ++c) Ra[c] += -(double)(Na * (T)mp.p[c] * len);
+        }
+        continue;
+      } else {
+        T Jm[SDIM][SDIM], Ji[SDIM][SDIM];
+#pragma unroll
+        for (int i = 0; i < SDIM; ++i)
+#pragma unroll
+          for (int j = 0; j < SDIM; ++j) Jm[i][j] = J[i][j];
+        const T wdet = inverse<T, SDIM>(Jm, Ji);  // Gauss weight is 1
+        T ga[SDIM];
+#pragma unroll
+        for (int d = 0; d < SDIM; ++d) {
+          T v = 0;
+#pragma unroll
+          for (int k = 0; k < SDIM; ++k) v += dN[k] * Ji[k][d];
+          ga[d] = v;
+        }
+
+        if constexpr (MODEL == AGX_MODEL_POISSON_SINCOS || MODEL == AGX_MODEL_HEAT_POTENTIAL ||
+                      MODEL == AGX_MODEL_HEAT_BE) {
+          T gu[SDIM];
+#pragma unroll
+          for (int d = 0; d < SDIM; ++d) gu[d] = group_sum<NEN>(ua[0] * ga[d]);
+          T gug = 0;
+#pragma unroll
+          for (int d = 0; d < SDIM; ++d) gug += gu[d] * ga[d];
+          T kq = ke, dkq = 0, mass = 0, src = 0;
+          if constexpr (MODEL == AGX_MODEL_POISSON_SINCOS) {
+            if constexpr (DO_R) {
+              T xq[SDIM];
+#pragma unroll
+              for (int d = 0; d < SDIM; ++d) xq[d] = group_sum<NEN>(Na * xa[d]);
+              T r1 = 0, r2 = 0;
+#pragma unroll
+              for (int d = 0; d < SDIM; ++d) {
+                r1 += xq[d] * xq[d];
+                T y = xq[d] - (T)mp.p[2 + d];
+                r2 += y * y;
+              }
+              const T w = (T)mp.p[1];
+              src = (T)mp.p[0] * (sin(w * r1) - cos(w * r2));
+            }
+          } else if constexpr (MODEL == AGX_MODEL_HEAT_POTENTIAL) {
+            src = (T)mp.p[0];
+          } else {  // HEAT_BE: params k0, k2, rho_c, dt
+            const T Tq = group_sum<NEN>(Na * ua[0]);
+            const T Tn = group_sum<NEN>(Na * tna);
+            kq = (T)mp.p[0] + (T)mp.p[1] * Tq * Tq;
+            dkq = T(2) * (T)mp.p[1] * Tq;
+            mass = (T)mp.p[2] / (T)mp.p[3];
+            src = -mass * (Tq - Tn);  // enters as -src * N_a
+          }
+          if constexpr (DO_R) Ra[0] += (double)(wdet * (kq * gug - src * Na));
+          if constexpr (DO_K) {
+            __syncwarp();
+            slab[warp][lane][0] = Na;
+#pragma unroll
+            for (int d = 0; d < SDIM; ++d) slab[warp][lane][1 + d] = ga[d];
+            __syncwarp();
+#pragma unroll
+            for (int b = 0; b < NEN; ++b) {
+              const T Nb = slab[warp][gbase + b][0];
+              T gg = 0;
+#pragma unroll
+              for (int d = 0; d < SDIM; ++d) gg += ga[d] * slab[warp][gbase + b][1 + d];
+              T kab = kq * gg;
+              if constexpr (MODEL == AGX_MODEL_HEAT_BE) kab += mass * Na * Nb + dkq * Nb * gug;
+              K[b][0][0] += wdet * kab;
+            }
+          }
+        } else if constexpr (MODEL == AGX_MODEL_NEO_HOOKE) {
+          // displacement gradient and deformation gradient (plane strain: F33 = 1)
+          T F[SDIM][SDIM];
+#pragma unroll
+          for (int i = 0; i < SDIM; ++i)
+#pragma unroll
+            for (int j = 0; j < SDIM; ++j) F[i][j] = group_sum<NEN>(ua[i] * ga[j]) + (i == j ? T(1) : T(0));
+          T Fi[SDIM][SDIM];
+          const T Jdet = inverse<T, SDIM>(F, Fi);
+          const T E = (T)mp.p[0], nu = (T)mp.p[1];
+          const T lam = E * nu / ((T(1) + nu) * (T(1) - T(2) * nu));
+          const T mu = E / (T(2) * (T(1) + nu));
+          const T c = lam * T(0.5) * (Jdet * Jdet - T(1)) - mu;
+          T ha[SDIM];
+#pragma unroll
+          for (int i = 0; i < SDIM; ++i) {
+            T v = 0;
+#pragma unroll
+            for (int j = 0; j < SDIM; ++j) v += Fi[j][i] * ga[j];  // (F^-T g)_i
+            ha[i] = v;
+          }
+          if constexpr (DO_R) {
+#pragma unroll
+            for (int i = 0; i < SDIM; ++i) {
+              T fg = 0;
+#pragma unroll
+              for (int j = 0; j < SDIM; ++j) fg += F[i][j] * ga[j];
+              Ra[i] += (double)(wdet * (mu * fg + c * ha[i]));
+            }
+          }
+          if constexpr (DO_K) {
+            __syncwarp();
+#pragma unroll
+            for (int d = 0; d < SDIM; ++d) {
+              slab[warp][lane][1 + d] = ga[d];
+              slab[warp][lane][1 + SDIM + d] = ha[d];
+            }
+            __syncwarp();
+            const T lj2 = lam * Jdet * Jdet;
+#pragma unroll
+            for (int b = 0; b < NEN; ++b) {
+              T gb[SDIM], hb[SDIM];
+#pragma unroll
+              for (int d = 0; d < SDIM; ++d) {
+                gb[d] = slab[warp][gbase + b][1 + d];
+                hb[d] = slab[warp][gbase + b][1 + SDIM + d];
+              }
+              T gg = 0;
+#pragma unroll
+              for (int d = 0; d < SDIM; ++d) gg += ga[d] * gb[d];
+#pragma unroll
+              for (int i = 0; i < SDIM; ++i)
+#pragma unroll
+                for (int k = 0; k < SDIM; ++k)
+                  K[b][i][k] += wdet * ((i == k ? mu * gg : T(0)) - c * hb[i] * ha[k] + lj2 * ha[i] * hb[k]);
+            }
+          }
+        }
+      }
+    }
+
+    // scatter into the residual and the pattern
+    const unsigned dma = dmask_node[node];
+    if constexpr (DO_R) {
+      if (valid) {
+#pragma unroll
+        for (int c = 0; c < NDOF; ++c) atomicAdd(R + (int64_t)node * NDOF + c, Ra[c]);
+      }
+    }
+    if constexpr (DO_K && MT::HAS_K) {
+#pragma unroll
+      for (int b = 0; b < NEN; ++b) {
+        const unsigned dmb = __shfl_sync(0xffffffffu, dma, gbase + b);
+        if (valid) {
+          const int64_t pos = epos[(e * NEN + a) * NEN + b];
+          T* blk = vals + pos * (NDOF * NDOF);
+#pragma unroll
+          for (int i = 0; i < NDOF; ++i)
+#pragma unroll
+            for (int j = 0; j < NDOF; ++j)
+              if (!((dma >> i) & 1u) && !((dmb >> j) & 1u)) atomicAdd(blk + i * NDOF + j, K[b][i][j]);
+        }
+      }
+    }
+  }
+}
+
+// prescribed diagonal entries of the (zeroed) value array set to one
+template <typename T>
+__global__ void set_dirichlet_diag(int64_t n_dir, const int32_t* __restrict__ dir_dofs,
+                                   const int32_t* __restrict__ diagpos, int ndof, T* __restrict__ vals) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n_dir; k += (int64_t)gridDim.x * blockDim.x) {
+    const int d = dir_dofs[k];
+    const int p = d / ndof, c = d - p * ndof;
+    vals[(int64_t)diagpos[p] * ndof * ndof + c * ndof + c] = T(1);
+  }
+}
+
+// inverse diagonal for Jacobi
+template <typename T>
+__global__ void inverse_diagonal(int64_t n_dofs, int ndof, const int32_t* __restrict__ diagpos,
+                                 const T* __restrict__ vals, T* __restrict__ dinv) {
+  for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d < n_dofs; d += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = d / ndof;
+    const int c = (int)(d - p * ndof);
+    const T v = vals[(int64_t)diagpos[p] * ndof * ndof + c * ndof + c];
+    dinv[d] = v != T(0) ? T(1) / v : T(0);
+  }
+}
+
+template <int ET, int MODEL, typename T, bool DO_R, bool DO_K>
+void launch_element(agx_context* ctx, agx_element_set& s, const double* dofs, double* R, T* vals) {
+  ModelParams mp;
+  for (int i = 0; i < AGX_MAX_PARAMS; ++i) mp.p[i] = s.params[i];
+  const int64_t lanes = s.n_elem * ElemTraits<ET>::NEN;
+  const int grid = agx_grid(ctx, lanes, 8);
+  element_kernel<ET, MODEL, T, DO_R, DO_K><<<grid, AGX_BLOCK, 0, ctx->stream>>>(
+      s.n_elem, s.d_conn, s.d_epos, ctx->d_coords, dofs, s.d_elem_field, s.d_node_field, ctx->d_dmask_node, mp, R,
+      vals);
+}
+
+// dispatch on (element type, model) for one pass kind
+template <typename T, bool DO_R, bool DO_K>
+int dispatch(agx_context* ctx, agx_element_set& s, const double* dofs, double* R, T* vals) {
+#define AGX_CASE(ETV, MV)                                                  \
+  if (s.elem_type == ETV && s.model == MV) {                               \
+    launch_element<ETV, MV, T, DO_R, DO_K>(ctx, s, dofs, R, vals);         \
+    return AGX_OK;                                                         \
+  }
+  AGX_CASE(AGX_QUAD4, AGX_MODEL_POISSON_SINCOS)
+  AGX_CASE(AGX_QUAD4, AGX_MODEL_HEAT_POTENTIAL)
+  AGX_CASE(AGX_QUAD4, AGX_MODEL_NEO_HOOKE)
+  AGX_CASE(AGX_QUAD4, AGX_MODEL_HEAT_BE)
+  AGX_CASE(AGX_HEX8, AGX_MODEL_POISSON_SINCOS)
+  AGX_CASE(AGX_HEX8, AGX_MODEL_HEAT_POTENTIAL)
+  AGX_CASE(AGX_HEX8, AGX_MODEL_NEO_HOOKE)
+  AGX_CASE(AGX_HEX8, AGX_MODEL_HEAT_BE)
+  AGX_CASE(AGX_LINE2, AGX_MODEL_NEUMANN)
+#undef AGX_CASE
+  return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "element type %d with model %d is not supported", s.elem_type, s.model);
+}
+
+}  // namespace
+
+int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, int tangent_dtype) {
+  const int bs = ctx->ndof * ctx->ndof;
+  if (residual) AGX_CUDA(ctx, cudaMemsetAsync(residual, 0, sizeof(double) * ctx->n_dofs, ctx->stream));
+  if (tangent_dtype == AGX_F64) {
+    AGX_CUDA(ctx, cudaMemsetAsync(ctx->d_vals64, 0, sizeof(double) * ctx->nnzb * bs, ctx->stream));
+    if (ctx->n_dir > 0)
+      set_dirichlet_diag<double><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(
+          ctx->n_dir, ctx->d_dir_dofs, ctx->d_diagpos, ctx->ndof, ctx->d_vals64);
+  } else if (tangent_dtype == AGX_F32) {
+    AGX_CUDA(ctx, cudaMemsetAsync(ctx->d_vals32, 0, sizeof(float) * ctx->nnzb * bs, ctx->stream));
+    if (ctx->n_dir > 0)
+      set_dirichlet_diag<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(
+          ctx->n_dir, ctx->d_dir_dofs, ctx->d_diagpos, ctx->ndof, ctx->d_vals32);
+  }
+  for (auto& s : ctx->sets) {
+    int rc = AGX_OK;
+    if (tangent_dtype == AGX_F64) {
+      rc = residual ? dispatch<double, true, true>(ctx, s, dofs, residual, ctx->d_vals64)
+                    : dispatch<double, false, true>(ctx, s, dofs, nullptr, ctx->d_vals64);
+    } else if (tangent_dtype == AGX_F32) {
+      // float32 tangent pass; the float64 residual is a separate float64 pass
+      rc = dispatch<float, false, true>(ctx, s, dofs, nullptr, ctx->d_vals32);
+      if (rc == AGX_OK && residual) rc = dispatch<double, true, false>(ctx, s, dofs, residual, (double*)nullptr);
+    } else if (residual) {
+      rc = dispatch<double, true, false>(ctx, s, dofs, residual, (double*)nullptr);
+    }
+    if (rc != AGX_OK) return rc;
+    AGX_CHECK_LAUNCH(ctx);
+  }
+  if (tangent_dtype == AGX_F64) {
+    inverse_diagonal<double><<<agx_grid(ctx, ctx->n_dofs), AGX_BLOCK, 0, ctx->stream>>>(
+        ctx->n_dofs, ctx->ndof, ctx->d_diagpos, ctx->d_vals64, ctx->d_dinv64);
+    ctx->tangent_valid = AGX_F64;
+  } else if (tangent_dtype == AGX_F32) {
+    inverse_diagonal<float><<<agx_grid(ctx, ctx->n_dofs), AGX_BLOCK, 0, ctx->stream>>>(
+        ctx->n_dofs, ctx->ndof, ctx->d_diagpos, ctx->d_vals32, ctx->d_dinv32);
+    ctx->tangent_valid = AGX_F32;
+  }
+  AGX_CHECK_LAUNCH(ctx);
+  return AGX_OK;
+}

@@ -1,0 +1,700 @@
+// Sparse products and Krylov solvers on the node-block CSR tangent.
+//
+// Replaces the host solve behind jax.pure_callback (solver.py:642-659 -> scipy_assembling +
+// spsolve, solver.py:1180-1222, :1493-1539) and the matrix-free CG of the 'jax' backend
+// (jax.scipy.sparse.linalg.cg with a Jacobi preconditioner, solver.py:1084-1116).
+//
+// Every iteration is a handful of fused kernels: the sparse product carries the dot product
+// that the step length needs, the vector update carries the dots of the next step.  Each
+// reduction writes one partial per block; the last block to finish (atomic ticket, no
+// waiting) sums the partials in block order -- deterministic -- and updates the scalars
+// in device memory.  Once a solve has converged every kernel returns at entry, so the host
+// launches iterations in chunks and reads the scalars only between chunks.
+#include <algorithm>
+
+#include "agx_common.cuh"
+
+namespace {
+
+constexpr int NWARP = AGX_BLOCK / 32;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-reduces NV values, publishes the block's partials and lets the last block combine
+// them.  Returns true in the last block (all threads), with totals in `tot` (thread 0).
+template <int NV>
+__device__ bool reduce_last_block(double (&v)[NV], double* __restrict__ partials, unsigned* __restrict__ counter,
+                                  double (&tot)[NV]) {
+  __shared__ double sh[NV][NWARP];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double s = warp_sum(v[k]);
+    if (lane == 0) sh[k][warp] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double s = 0;
+      for (int w = 0; w < NWARP; ++w) s += sh[k][w];
+      partials[(size_t)k * gridDim.x + blockIdx.x] = s;
+    }
+    __threadfence();
+    const unsigned t = atomicAdd(counter, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double s = 0;
+    for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) s += __ldcg(partials + (size_t)k * gridDim.x + i);
+    s = warp_sum(s);
+    __syncthreads();
+    if (lane == 0) sh[k][warp] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int w = 0; w < NWARP; ++w) t += sh[k][w];
+      tot[k] = t;
+    }
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+  return true;
+}
+
+__device__ __forceinline__ bool bad(double x) { return !isfinite(x) || x == 0.0; }
+
+// ---- sparse product ------------------------------------------------------------------
+// y = A x for the node-block CSR; TPR lanes per block row.  Optionally returns partial
+// (p, A p) with p = x.
+template <typename T, int NDOF, int TPR>
+__device__ __forceinline__ void bsr_row(int64_t row, int sub, const int32_t* __restrict__ rowptr,
+                                        const int32_t* __restrict__ col, const T* __restrict__ vals,
+                                        const T* __restrict__ x, T (&y)[NDOF]) {
+#pragma unroll
+  for (int i = 0; i < NDOF; ++i) y[i] = 0;
+  const int beg = rowptr[row], end = rowptr[row + 1];
+  for (int k = beg + sub; k < end; k += TPR) {
+    const int c = col[k];
+    T xc[NDOF];
+#pragma unroll
+    for (int j = 0; j < NDOF; ++j) xc[j] = x[(int64_t)c * NDOF + j];
+    const T* v = vals + (int64_t)k * NDOF * NDOF;
+#pragma unroll
+    for (int i = 0; i < NDOF; ++i)
+#pragma unroll
+      for (int j = 0; j < NDOF; ++j) y[i] += v[i * NDOF + j] * xc[j];
+  }
+#pragma unroll
+  for (int o = TPR / 2; o >= 1; o >>= 1)
+#pragma unroll
+    for (int i = 0; i < NDOF; ++i) y[i] += __shfl_xor_sync(0xffffffffu, y[i], o);
+}
+
+template <typename T, int NDOF, int TPR>
+__global__ void __launch_bounds__(AGX_BLOCK) spmv_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr,
+                                                         const int32_t* __restrict__ col, const T* __restrict__ vals,
+                                                         const T* __restrict__ x, T* __restrict__ y) {
+  const int sub = threadIdx.x % TPR;
+  const int64_t total = ((n_rows * TPR + 31) / 32) * 32;
+  for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = L / TPR;
+    T yr[NDOF];
+    bsr_row<T, NDOF, TPR>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, x, yr);
+    if (row < n_rows && sub == 0) {
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i) y[row * NDOF + i] = yr[i];
+    }
+  }
+}
+
+// q = A p and alpha = rz / (p, q)
+template <typename T, int NDOF, int TPR>
+__global__ void __launch_bounds__(AGX_BLOCK)
+spmv_dot_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                const T* __restrict__ vals, const T* __restrict__ p, T* __restrict__ q, agx_krylov_scalars* sc,
+                double* partials, unsigned* counter, int mode) {
+  if (sc->converged) return;
+  const int sub = threadIdx.x % TPR;
+  const int64_t total = ((n_rows * TPR + 31) / 32) * 32;
+  double acc[1] = {0.0};
+  for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = L / TPR;
+    T yr[NDOF];
+    bsr_row<T, NDOF, TPR>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, p, yr);
+    if (row < n_rows && sub == 0) {
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i) {
+        q[row * NDOF + i] = yr[i];
+        acc[0] += (double)yr[i] * (double)p[row * NDOF + i];
+      }
+    }
+  }
+  double tot[1];
+  if (reduce_last_block<1>(acc, partials, counter, tot) && threadIdx.x == 0) {
+    sc->pq = tot[0];
+    if (bad(tot[0]) || tot[0] < 0.0) {
+      sc->converged = 2;
+    } else {
+      sc->alpha = sc->rz / tot[0];
+    }
+  }
+}
+
+// ---- PCG (Jacobi or external preconditioner) ------------------------------------------
+// norm of b and the scale used by the single-precision inner solve
+__global__ void __launch_bounds__(AGX_BLOCK) norm_init_kernel(int64_t n, const double* __restrict__ b,
+                                                              agx_krylov_scalars* sc, double* partials,
+                                                              unsigned* counter, double rtol, double atol) {
+  double acc[1] = {0.0};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc[0] += b[i] * b[i];
+  double tot[1];
+  if (reduce_last_block<1>(acc, partials, counter, tot) && threadIdx.x == 0) {
+    const double bb = tot[0];
+    sc->extra[0] = bb > 0.0 ? 1.0 / sqrt(bb) : 1.0;  // inner scale
+    sc->extra[1] = bb > 0.0 ? sqrt(bb) : 1.0;
+    sc->rr = bb;
+    sc->rr_stop = fmax(rtol * rtol * bb, atol * atol);
+    sc->iters = 0;
+    sc->converged = (bb <= sc->rr_stop || bb == 0.0) ? 1 : (isfinite(bb) ? 0 : 2);
+    sc->alpha = sc->beta = sc->pq = 0.0;
+    sc->omega = sc->rho = 1.0;
+  }
+}
+
+// x = 0; r = s b; z = Dinv r (when jacobi); rz, rr.  For the mixed method s = 1/||b||.
+template <typename T>
+__global__ void __launch_bounds__(AGX_BLOCK)
+pcg_init_kernel(int64_t n, const double* __restrict__ b, const T* __restrict__ dinv, T* __restrict__ x,
+                T* __restrict__ r, T* __restrict__ z, T* __restrict__ p, agx_krylov_scalars* sc, double* partials,
+                unsigned* counter, int scaled, int jacobi) {
+  const double s = scaled ? sc->extra[0] : 1.0;
+  double acc[2] = {0.0, 0.0};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T ri = (T)(b[i] * s);
+    x[i] = 0;
+    r[i] = ri;
+    if (jacobi) {
+      const T zi = dinv[i] * ri;
+      z[i] = zi;
+      p[i] = zi;
+      acc[0] += (double)ri * (double)zi;
+    }
+    acc[1] += (double)ri * (double)ri;
+  }
+  double tot[2];
+  if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+    if (jacobi) sc->rz = tot[0];
+    sc->rr = tot[1];
+    if (scaled) sc->rr_stop *= sc->extra[0] * sc->extra[0];
+  }
+}
+
+// x += a p; r -= a q; z = Dinv r; rz_new, rr; beta
+template <typename T>
+__global__ void __launch_bounds__(AGX_BLOCK)
+pcg_update_kernel(int64_t n, T* __restrict__ x, T* __restrict__ r, T* __restrict__ z, const T* __restrict__ p,
+                  const T* __restrict__ q, const T* __restrict__ dinv, agx_krylov_scalars* sc, double* partials,
+                  unsigned* counter) {
+  if (sc->converged) return;
+  const T a = (T)sc->alpha;
+  double acc[2] = {0.0, 0.0};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += a * p[i];
+    const T ri = r[i] - a * q[i];
+    r[i] = ri;
+    const T zi = dinv[i] * ri;
+    z[i] = zi;
+    acc[0] += (double)ri * (double)zi;
+    acc[1] += (double)ri * (double)ri;
+  }
+  double tot[2];
+  if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+    sc->iters += 1;
+    sc->rr = tot[1];
+    if (!isfinite(tot[0]) || !isfinite(tot[1])) {
+      sc->converged = 2;
+    } else if (tot[1] <= sc->rr_stop) {
+      sc->converged = 1;
+    } else if (sc->rz == 0.0) {
+      sc->converged = 2;
+    } else {
+      sc->beta = tot[0] / sc->rz;
+      sc->rz = tot[0];
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(AGX_BLOCK)
+pcg_direction_kernel(int64_t n, T* __restrict__ p, const T* __restrict__ z, const agx_krylov_scalars* sc) {
+  if (sc->converged) return;
+  const T bta = (T)sc->beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = z[i] + bta * p[i];
+}
+
+// ---- flexible CG (Notay FCG(1)): beta = -(z_new, q) / (p, q) ----------------------------
+template <typename T>
+__global__ void __launch_bounds__(AGX_BLOCK)
+fcg_update_kernel(int64_t n, T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p, const T* __restrict__ q,
+                  agx_krylov_scalars* sc, double* partials, unsigned* counter) {
+  if (sc->converged) return;
+  const T a = (T)sc->alpha;
+  double acc[1] = {0.0};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += a * p[i];
+    const T ri = r[i] - a * q[i];
+    r[i] = ri;
+    acc[0] += (double)ri * (double)ri;
+  }
+  double tot[1];
+  if (reduce_last_block<1>(acc, partials, counter, tot) && threadIdx.x == 0) {
+    sc->iters += 1;
+    sc->rr = tot[0];
+    if (!isfinite(tot[0])) sc->converged = 2;
+    else if (tot[0] <= sc->rr_stop) sc->converged = 1;
+  }
+}
+
+// after z = M r: rz = (r, z), beta = -(z, q)/(p, q)   (first=1: only rz, p = z)
+template <typename T>
+__global__ void __launch_bounds__(AGX_BLOCK)
+fcg_direction_dots(int64_t n, const T* __restrict__ r, const T* __restrict__ z, const T* __restrict__ q,
+                   agx_krylov_scalars* sc, double* partials, unsigned* counter) {
+  if (sc->converged) return;
+  double acc[2] = {0.0, 0.0};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    acc[0] += (double)r[i] * (double)z[i];
+    acc[1] += (double)z[i] * (double)q[i];
+  }
+  double tot[2];
+  if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+    sc->rz = tot[0];
+    sc->beta = sc->iters == 0 ? 0.0 : -tot[1] / sc->pq;
+    if (!isfinite(tot[0]) || tot[0] <= 0.0) sc->converged = 2;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(AGX_BLOCK)
+jacobi_apply(int64_t n, const T* __restrict__ dinv, const T* __restrict__ r, T* __restrict__ z,
+             const agx_krylov_scalars* sc) {
+  if (sc->converged) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    z[i] = dinv[i] * r[i];
+}
+
+// ---- BiCGStab (right Jacobi preconditioning), float64 --------------------------------
+// p = r + beta (p - omega v); y = Dinv p
+__global__ void __launch_bounds__(AGX_BLOCK)
+bicg_p_kernel(int64_t n, double* __restrict__ p, const double* __restrict__ r, const double* __restrict__ v,
+              double* __restrict__ y, const double* __restrict__ dinv, const agx_krylov_scalars* sc) {
+  if (sc->converged) return;
+  const double bta = sc->beta, om = sc->omega;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double pi = r[i] + bta * (p[i] - om * v[i]);
+    p[i] = pi;
+    y[i] = dinv[i] * pi;
+  }
+}
+
+// v = A y; alpha = rho / (rhat, v)
+template <int NDOF, int TPR>
+__global__ void __launch_bounds__(AGX_BLOCK)
+bicg_spmv_rhat(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+               const double* __restrict__ vals, const double* __restrict__ y, double* __restrict__ v,
+               const double* __restrict__ rhat, agx_krylov_scalars* sc, double* partials, unsigned* counter) {
+  if (sc->converged) return;
+  const int sub = threadIdx.x % TPR;
+  const int64_t total = ((n_rows * TPR + 31) / 32) * 32;
+  double acc[1] = {0.0};
+  for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = L / TPR;
+    double yr[NDOF];
+    bsr_row<double, NDOF, TPR>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, y, yr);
+    if (row < n_rows && sub == 0) {
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i) {
+        v[row * NDOF + i] = yr[i];
+        acc[0] += rhat[row * NDOF + i] * yr[i];
+      }
+    }
+  }
+  double tot[1];
+  if (reduce_last_block<1>(acc, partials, counter, tot) && threadIdx.x == 0) {
+    if (bad(tot[0])) sc->converged = 2;
+    else sc->alpha = sc->rho / tot[0];
+  }
+}
+
+// s = r - alpha v; z = Dinv s
+__global__ void __launch_bounds__(AGX_BLOCK)
+bicg_s_kernel(int64_t n, const double* __restrict__ r, const double* __restrict__ v, double* __restrict__ s,
+              double* __restrict__ z, const double* __restrict__ dinv, const agx_krylov_scalars* sc) {
+  if (sc->converged) return;
+  const double a = sc->alpha;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double si = r[i] - a * v[i];
+    s[i] = si;
+    z[i] = dinv[i] * si;
+  }
+}
+
+// t = A z; omega = (t, s)/(t, t)
+template <int NDOF, int TPR>
+__global__ void __launch_bounds__(AGX_BLOCK)
+bicg_spmv_ts(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+             const double* __restrict__ vals, const double* __restrict__ z, double* __restrict__ t,
+             const double* __restrict__ s, agx_krylov_scalars* sc, double* partials, unsigned* counter) {
+  if (sc->converged) return;
+  const int sub = threadIdx.x % TPR;
+  const int64_t total = ((n_rows * TPR + 31) / 32) * 32;
+  double acc[2] = {0.0, 0.0};
+  for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = L / TPR;
+    double yr[NDOF];
+    bsr_row<double, NDOF, TPR>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, z, yr);
+    if (row < n_rows && sub == 0) {
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i) {
+        t[row * NDOF + i] = yr[i];
+        acc[0] += yr[i] * s[row * NDOF + i];
+        acc[1] += yr[i] * yr[i];
+      }
+    }
+  }
+  double tot[2];
+  if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+    if (!isfinite(tot[0]) || bad(tot[1])) sc->converged = 2;
+    else sc->omega = tot[0] / tot[1];
+  }
+}
+
+// x += alpha y + omega z; r = s - omega t; rho_new = (rhat, r); rr
+__global__ void __launch_bounds__(AGX_BLOCK)
+bicg_update(int64_t n, double* __restrict__ x, double* __restrict__ r, const double* __restrict__ y,
+            const double* __restrict__ z, const double* __restrict__ s, const double* __restrict__ t,
+            const double* __restrict__ rhat, agx_krylov_scalars* sc, double* partials, unsigned* counter) {
+  if (sc->converged) return;
+  const double a = sc->alpha, om = sc->omega;
+  double acc[2] = {0.0, 0.0};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += a * y[i] + om * z[i];
+    const double ri = s[i] - om * t[i];
+    r[i] = ri;
+    acc[0] += rhat[i] * ri;
+    acc[1] += ri * ri;
+  }
+  double tot[2];
+  if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+    sc->iters += 1;
+    sc->rr = tot[1];
+    if (!isfinite(tot[1])) sc->converged = 2;
+    else if (tot[1] <= sc->rr_stop) sc->converged = 1;
+    else if (bad(tot[0]) || sc->omega == 0.0) sc->converged = 2;
+    else {
+      sc->beta = (tot[0] / sc->rho) * (a / om);
+      sc->rho = tot[0];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(AGX_BLOCK)
+bicg_init(int64_t n, const double* __restrict__ b, double* __restrict__ x, double* __restrict__ r,
+          double* __restrict__ rhat, double* __restrict__ p, double* __restrict__ v, agx_krylov_scalars* sc) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] = 0.0;
+    r[i] = b[i];
+    rhat[i] = b[i];
+    p[i] = 0.0;
+    v[i] = 0.0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    sc->rho = sc->rr;  // (rhat, r0) = (b, b)
+    sc->beta = 0.0;
+    sc->omega = 1.0;
+    sc->alpha = 1.0;
+  }
+}
+
+// ---- conversions and helpers ---------------------------------------------------------
+template <typename T>
+__global__ void to_double_scaled(int64_t n, const T* __restrict__ x, double* __restrict__ out,
+                                 const agx_krylov_scalars* sc, int scaled) {
+  const double s = scaled ? sc->extra[1] : 1.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (double)x[i] * s;
+}
+
+__global__ void __launch_bounds__(AGX_BLOCK) masked_norm_kernel(int64_t n, const double* __restrict__ v,
+                                                                const uint8_t* __restrict__ dmask, double* out,
+                                                                double* partials, unsigned* counter) {
+  double acc[2] = {0.0, 0.0};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = dmask[i] ? 0.0 : v[i];
+    acc[0] += x * x;
+    if (!isfinite(x)) acc[1] += 1.0;
+  }
+  double tot[2];
+  if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+    out[0] = tot[0];
+    out[1] = tot[1];
+  }
+}
+
+__global__ void set_dirichlet_kernel(int64_t n_dir, const int32_t* __restrict__ dir, double* __restrict__ dofs,
+                                     const double* __restrict__ values) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n_dir; k += (int64_t)gridDim.x * blockDim.x)
+    dofs[dir[k]] = values[dir[k]];
+}
+
+// dofs[free] += damping dx; dofs[prescribed] = values (solver.py:879-892)
+__global__ void newton_update_kernel(int64_t n, double* __restrict__ dofs, const double* __restrict__ dx,
+                                     const double* __restrict__ values, const uint8_t* __restrict__ dmask,
+                                     double damping) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dofs[i] = dmask[i] ? values[i] : dofs[i] + damping * dx[i];
+}
+
+// dst = s * src on free DOFs, 0 on prescribed DOFs; s = -1 gives rhs = -R
+// (solver.py:610-611 with the row deletion of solver.py:1514-1517)
+__global__ void masked_scale_kernel(int64_t n, const double* __restrict__ src, double* __restrict__ dst,
+                                    const uint8_t* __restrict__ dmask, double s) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = dmask[i] ? 0.0 : s * src[i];
+}
+
+template <typename T>
+__global__ void zero_prescribed(int64_t n_dir, const int32_t* __restrict__ dir, T* __restrict__ v) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n_dir; k += (int64_t)gridDim.x * blockDim.x)
+    v[dir[k]] = T(0);
+}
+
+template <int NDOF>
+constexpr int tpr_for(int dim) {
+  return NDOF == 1 ? (dim == 3 ? 8 : 4) : (NDOF == 2 ? 4 : 8);
+}
+
+// launch helpers dispatching on the block size
+template <typename T>
+void launch_spmv_dot(agx_context* ctx, const T* vals, const T* p, T* q) {
+  const int64_t nr = ctx->n_nodes;
+  const int g = ctx->red_blocks;
+  auto* sc = ctx->d_scal;
+  if (ctx->ndof == 1) {
+    if (ctx->dim == 3)
+      spmv_dot_kernel<T, 1, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, vals, p, q, sc,
+                                                                ctx->d_partials, ctx->d_counter, 0);
+    else
+      spmv_dot_kernel<T, 1, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, vals, p, q, sc,
+                                                                ctx->d_partials, ctx->d_counter, 0);
+  } else if (ctx->ndof == 2) {
+    spmv_dot_kernel<T, 2, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, vals, p, q, sc,
+                                                              ctx->d_partials, ctx->d_counter, 0);
+  } else {
+    spmv_dot_kernel<T, 3, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, vals, p, q, sc,
+                                                              ctx->d_partials, ctx->d_counter, 0);
+  }
+}
+
+template <int NDOF, int TPR>
+void launch_bicg_spmvs(agx_context* ctx, int which, double* a, double* b, double* c) {
+  const int g = ctx->red_blocks;
+  if (which == 0)
+    bicg_spmv_rhat<NDOF, TPR><<<g, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_nodes, ctx->d_rowptr, ctx->d_col,
+                                                                ctx->d_vals64, a, b, c, ctx->d_scal, ctx->d_partials,
+                                                                ctx->d_counter);
+  else
+    bicg_spmv_ts<NDOF, TPR><<<g, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_nodes, ctx->d_rowptr, ctx->d_col, ctx->d_vals64,
+                                                              a, b, c, ctx->d_scal, ctx->d_partials, ctx->d_counter);
+}
+
+void launch_bicg_spmv(agx_context* ctx, int which, double* a, double* b, double* c) {
+  if (ctx->ndof == 1) {
+    if (ctx->dim == 3) launch_bicg_spmvs<1, 8>(ctx, which, a, b, c);
+    else launch_bicg_spmvs<1, 4>(ctx, which, a, b, c);
+  } else if (ctx->ndof == 2) {
+    launch_bicg_spmvs<2, 4>(ctx, which, a, b, c);
+  } else {
+    launch_bicg_spmvs<3, 8>(ctx, which, a, b, c);
+  }
+}
+
+int read_scalars(agx_context* ctx) {
+  AGX_CUDA(ctx, cudaMemcpyAsync(ctx->h_scal, ctx->d_scal, sizeof(agx_krylov_scalars), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  AGX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return AGX_OK;
+}
+
+}  // namespace
+
+int agx_spmv_impl(agx_context* ctx, int dtype, const void* x, void* y) {
+  const int64_t nr = ctx->n_nodes;
+  const int g = agx_grid(ctx, nr * 8, 8);
+  auto go = [&](auto tag) {
+    using T = decltype(tag);
+    const T* v = dtype == AGX_F64 ? (const T*)ctx->d_vals64 : (const T*)ctx->d_vals32;
+    if (ctx->ndof == 1) {
+      if (ctx->dim == 3)
+        spmv_kernel<T, 1, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, (const T*)x, (T*)y);
+      else
+        spmv_kernel<T, 1, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, (const T*)x, (T*)y);
+    } else if (ctx->ndof == 2) {
+      spmv_kernel<T, 2, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, (const T*)x, (T*)y);
+    } else {
+      spmv_kernel<T, 3, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, (const T*)x, (T*)y);
+    }
+  };
+  if (dtype == AGX_F64) go(double{});
+  else go(float{});
+  AGX_CHECK_LAUNCH(ctx);
+  return AGX_OK;
+}
+
+void agx_launch_set_dirichlet(agx_context* ctx, double* dofs, const double* values) {
+  if (ctx->n_dir > 0)
+    set_dirichlet_kernel<<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir, ctx->d_dir_dofs, dofs,
+                                                                                  values);
+}
+
+void agx_launch_newton_update(agx_context* ctx, double* dofs, const double* dx, const double* values, double damping) {
+  newton_update_kernel<<<agx_grid(ctx, ctx->n_dofs), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dofs, dofs, dx, values,
+                                                                                  ctx->d_dmask_dof, damping);
+}
+
+void agx_launch_negate_free(agx_context* ctx, const double* R, double* b) {
+  agx_launch_masked_scale(ctx, R, b, -1.0);
+}
+
+void agx_launch_masked_scale(agx_context* ctx, const double* src, double* dst, double s) {
+  masked_scale_kernel<<<agx_grid(ctx, ctx->n_dofs), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dofs, src, dst,
+                                                                                ctx->d_dmask_dof, s);
+}
+
+int agx_residual_norm(agx_context* ctx, const double* R, double* norm2, double* nonfinite) {
+  masked_norm_kernel<<<ctx->red_blocks, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dofs, R, ctx->d_dmask_dof, ctx->d_norm,
+                                                                   ctx->d_partials, ctx->d_counter);
+  AGX_CHECK_LAUNCH(ctx);
+  AGX_CUDA(ctx, cudaMemcpyAsync(ctx->h_norm, ctx->d_norm, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  AGX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *norm2 = ctx->h_norm[0];
+  *nonfinite = ctx->h_norm[1];
+  return AGX_OK;
+}
+
+int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_solve_opts* opts, agx_solve_info* info) {
+  const int64_t n = ctx->n_dofs;
+  const int g = ctx->red_blocks;
+  const int gv = agx_grid(ctx, n);
+  const int method = opts->method;
+  const int every = opts->check_every > 0 ? opts->check_every : 16;
+  const int maxiter = opts->maxiter > 0 ? opts->maxiter : 10000;
+  auto* sc = ctx->d_scal;
+  if ((method == AGX_PCG || method == AGX_BICGSTAB) && ctx->tangent_valid != AGX_F64)
+    return agx_fail(ctx, AGX_ERR_STATE, "float64 Krylov method needs a float64 tangent (assemble first)");
+  if ((method == AGX_PCG_MIXED || method == AGX_FCG_MIXED) && ctx->tangent_valid != AGX_F32)
+    return agx_fail(ctx, AGX_ERR_STATE, "mixed Krylov method needs a float32 tangent (assemble first)");
+
+  norm_init_kernel<<<g, AGX_BLOCK, 0, ctx->stream>>>(n, rhs, sc, ctx->d_partials, ctx->d_counter, opts->rtol,
+                                                    opts->atol);
+  AGX_CHECK_LAUNCH(ctx);
+  int it_done = 0;
+  if (method == AGX_PCG) {
+    pcg_init_kernel<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, rhs, ctx->d_dinv64, x, ctx->d_r, ctx->d_z, ctx->d_p,
+                                                             sc, ctx->d_partials, ctx->d_counter, 0, 1);
+    while (true) {
+      for (int k = 0, kn = std::min(every, maxiter - it_done); k < kn; ++k) {
+        launch_spmv_dot<double>(ctx, ctx->d_vals64, ctx->d_p, ctx->d_q);
+        pcg_update_kernel<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, x, ctx->d_r, ctx->d_z, ctx->d_p, ctx->d_q,
+                                                                   ctx->d_dinv64, sc, ctx->d_partials, ctx->d_counter);
+        pcg_direction_kernel<double><<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_p, ctx->d_z, sc);
+      }
+      AGX_CHECK_LAUNCH(ctx);
+      int rc = read_scalars(ctx);
+      if (rc) return rc;
+      it_done = ctx->h_scal->iters;
+      if (ctx->h_scal->converged || it_done >= maxiter) break;
+    }
+  } else if (method == AGX_PCG_MIXED || method == AGX_FCG_MIXED) {
+    const bool flexible = method == AGX_FCG_MIXED && ctx->precond != nullptr;
+    pcg_init_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, rhs, ctx->d_dinv32, ctx->f_x, ctx->f_r, ctx->f_z,
+                                                            ctx->f_p, sc, ctx->d_partials, ctx->d_counter, 1,
+                                                            flexible ? 0 : 1);
+    if (flexible) {
+      if (ctx->precond(ctx->precond_user, ctx->f_r, ctx->f_z, n, ctx->stream) != 0)
+        return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");
+      zero_prescribed<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir, ctx->d_dir_dofs,
+                                                                                     ctx->f_z);
+      fcg_direction_dots<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_r, ctx->f_z, ctx->f_q, sc, ctx->d_partials,
+                                                                 ctx->d_counter);
+      AGX_CUDA(ctx, cudaMemcpyAsync(ctx->f_p, ctx->f_z, sizeof(float) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    while (true) {
+      for (int k = 0, kn = std::min(every, maxiter - it_done); k < kn; ++k) {
+        launch_spmv_dot<float>(ctx, ctx->d_vals32, ctx->f_p, ctx->f_q);
+        if (!flexible) {
+          pcg_update_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, ctx->f_r, ctx->f_z, ctx->f_p,
+                                                                    ctx->f_q, ctx->d_dinv32, sc, ctx->d_partials,
+                                                                    ctx->d_counter);
+        } else {
+          fcg_update_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, ctx->f_r, ctx->f_p, ctx->f_q, sc,
+                                                                    ctx->d_partials, ctx->d_counter);
+          if (ctx->precond(ctx->precond_user, ctx->f_r, ctx->f_z, n, ctx->stream) != 0)
+            return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");
+          zero_prescribed<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir,
+                                                                                         ctx->d_dir_dofs, ctx->f_z);
+          fcg_direction_dots<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_r, ctx->f_z, ctx->f_q, sc,
+                                                                     ctx->d_partials, ctx->d_counter);
+        }
+        pcg_direction_kernel<float><<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_p, ctx->f_z, sc);
+      }
+      AGX_CHECK_LAUNCH(ctx);
+      int rc = read_scalars(ctx);
+      if (rc) return rc;
+      it_done = ctx->h_scal->iters;
+      if (ctx->h_scal->converged || it_done >= maxiter) break;
+    }
+    to_double_scaled<float><<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, x, sc, 1);
+  } else if (method == AGX_BICGSTAB) {
+    bicg_init<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, rhs, x, ctx->d_r, ctx->d_rhat, ctx->d_p, ctx->d_v, sc);
+    while (true) {
+      for (int k = 0, kn = std::min(every, maxiter - it_done); k < kn; ++k) {
+        bicg_p_kernel<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_p, ctx->d_r, ctx->d_v, ctx->d_q, ctx->d_dinv64, sc);
+        launch_bicg_spmv(ctx, 0, ctx->d_q, ctx->d_v, ctx->d_rhat);  // v = A y, y in d_q
+        bicg_s_kernel<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_r, ctx->d_v, ctx->d_s, ctx->d_z, ctx->d_dinv64, sc);
+        launch_bicg_spmv(ctx, 1, ctx->d_z, ctx->d_t, ctx->d_s);  // t = A z
+        bicg_update<<<g, AGX_BLOCK, 0, ctx->stream>>>(n, x, ctx->d_r, ctx->d_q, ctx->d_z, ctx->d_s, ctx->d_t,
+                                                     ctx->d_rhat, sc, ctx->d_partials, ctx->d_counter);
+      }
+      AGX_CHECK_LAUNCH(ctx);
+      int rc = read_scalars(ctx);
+      if (rc) return rc;
+      it_done = ctx->h_scal->iters;
+      if (ctx->h_scal->converged || it_done >= maxiter) break;
+    }
+  } else {
+    return agx_fail(ctx, AGX_ERR_ARG, "unknown Krylov method %d", method);
+  }
+  AGX_CHECK_LAUNCH(ctx);
+  int rc = read_scalars(ctx);
+  if (rc) return rc;
+  const agx_krylov_scalars& s = *ctx->h_scal;
+  const double bb_scale = (method == AGX_PCG_MIXED || method == AGX_FCG_MIXED) ? 1.0 : s.extra[0] * s.extra[0];
+  if (info) {
+    info->iterations = s.iters;
+    info->rel_residual = sqrt(s.rr * bb_scale);
+    info->status = s.converged == 1 ? AGX_OK : (s.converged == 2 ? AGX_DIVERGED : AGX_NOT_CONVERGED);
+  }
+  return AGX_OK;
+}

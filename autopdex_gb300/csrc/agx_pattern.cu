@@ -1,0 +1,131 @@
+// Node-block CSR (BSR) pattern of the tangent and the element -> pattern scatter map.
+//
+// AutoPDEx keeps the tangent as a BCOO with one entry per element-matrix entry
+// (assembler.py:1142-1148, indices from _get_indices, assembler.py:47-141) and sums the
+// duplicates on the host in every Newton step (scipy_assembling, solver.py:1180-1222).
+// Here the pattern is built once per mesh: row p holds every node that shares an element
+// with node p (sorted), each row/column entry is an ndof x ndof block, and for every
+// element and local node pair (a, b) the position of block (conn[a], conn[b]) is stored,
+// so that assembly adds element blocks straight into their final slots.
+#include <algorithm>
+#include <thread>
+
+#include "agx_common.cuh"
+
+namespace {
+
+template <class F>
+void parallel_for(int64_t n, F&& f) {
+  unsigned hw = std::thread::hardware_concurrency();
+  int nt = (int)std::min<int64_t>(std::max(1u, hw), std::max<int64_t>(1, n / 4096));
+  if (nt <= 1) {
+    f(0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  int64_t chunk = (n + nt - 1) / nt;
+  for (int t = 0; t < nt; ++t) {
+    int64_t b = t * chunk, e = std::min<int64_t>(n, b + chunk);
+    if (b >= e) break;
+    th.emplace_back([&f, b, e] { f(b, e); });
+  }
+  for (auto& t : th) t.join();
+}
+
+}  // namespace
+
+int agx_build_pattern(agx_context* ctx) {
+  const int64_t nn = ctx->n_nodes;
+  // node -> (set, element) incidence, counting sort
+  std::vector<int64_t> inc_ptr(nn + 1, 0);
+  for (auto& s : ctx->sets)
+    for (int64_t i = 0; i < s.n_elem * s.nen; ++i) inc_ptr[s.h_conn[i] + 1]++;
+  for (int64_t p = 0; p < nn; ++p) inc_ptr[p + 1] += inc_ptr[p];
+  std::vector<int64_t> inc(inc_ptr[nn]);   // encoded (set << 40) | element
+  {
+    std::vector<int64_t> fill(inc_ptr.begin(), inc_ptr.end() - 1);
+    for (size_t si = 0; si < ctx->sets.size(); ++si) {
+      auto& s = ctx->sets[si];
+      for (int64_t e = 0; e < s.n_elem; ++e)
+        for (int a = 0; a < s.nen; ++a) {
+          int32_t p = s.h_conn[e * s.nen + a];
+          inc[fill[p]++] = ((int64_t)si << 40) | e;
+        }
+    }
+  }
+  // neighbours of every node: sorted unique union of the nodes of its elements
+  std::vector<int32_t> row_len(nn);
+  auto neighbours = [&](int64_t p, std::vector<int32_t>& buf) {
+    buf.clear();
+    for (int64_t k = inc_ptr[p]; k < inc_ptr[p + 1]; ++k) {
+      auto& s = ctx->sets[inc[k] >> 40];
+      int64_t e = inc[k] & ((1LL << 40) - 1);
+      for (int b = 0; b < s.nen; ++b) buf.push_back(s.h_conn[e * s.nen + b]);
+    }
+    buf.push_back((int32_t)p);  // keep the diagonal even for nodes outside every element
+    std::sort(buf.begin(), buf.end());
+    buf.erase(std::unique(buf.begin(), buf.end()), buf.end());
+  };
+  parallel_for(nn, [&](int64_t b, int64_t e) {
+    std::vector<int32_t> buf;
+    for (int64_t p = b; p < e; ++p) {
+      neighbours(p, buf);
+      row_len[p] = (int32_t)buf.size();
+    }
+  });
+  std::vector<int32_t> rowptr(nn + 1, 0);
+  int64_t acc = 0;
+  for (int64_t p = 0; p < nn; ++p) {
+    rowptr[p] = (int32_t)acc;
+    acc += row_len[p];
+    if (acc > INT32_MAX) return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "pattern exceeds 2^31 blocks");
+  }
+  rowptr[nn] = (int32_t)acc;
+  ctx->nnzb = acc;
+  std::vector<int32_t> col(acc), diagpos(nn);
+  parallel_for(nn, [&](int64_t b, int64_t e) {
+    std::vector<int32_t> buf;
+    for (int64_t p = b; p < e; ++p) {
+      neighbours(p, buf);
+      std::copy(buf.begin(), buf.end(), col.begin() + rowptr[p]);
+      diagpos[p] = rowptr[p] + (int32_t)(std::lower_bound(buf.begin(), buf.end(), (int32_t)p) - buf.begin());
+    }
+  });
+  // element scatter maps
+  std::vector<std::vector<int32_t>> epos(ctx->sets.size());
+  for (size_t si = 0; si < ctx->sets.size(); ++si) {
+    auto& s = ctx->sets[si];
+    auto& ep = epos[si];
+    ep.resize((size_t)s.n_elem * s.nen * s.nen);
+    parallel_for(s.n_elem, [&](int64_t b, int64_t e) {
+      for (int64_t el = b; el < e; ++el)
+        for (int a = 0; a < s.nen; ++a) {
+          int32_t p = s.h_conn[el * s.nen + a];
+          const int32_t* rb = col.data() + rowptr[p];
+          const int32_t* re = col.data() + rowptr[p + 1];
+          for (int c = 0; c < s.nen; ++c) {
+            int32_t q = s.h_conn[el * s.nen + c];
+            ep[(el * s.nen + a) * s.nen + c] = rowptr[p] + (int32_t)(std::lower_bound(rb, re, q) - rb);
+          }
+        }
+    });
+  }
+  // upload
+  const int bs = ctx->ndof * ctx->ndof;
+  AGX_CUDA(ctx, cudaMalloc(&ctx->d_rowptr, sizeof(int32_t) * (nn + 1)));
+  AGX_CUDA(ctx, cudaMalloc(&ctx->d_col, sizeof(int32_t) * std::max<int64_t>(1, acc)));
+  AGX_CUDA(ctx, cudaMalloc(&ctx->d_diagpos, sizeof(int32_t) * nn));
+  AGX_CUDA(ctx, cudaMalloc(&ctx->d_vals64, sizeof(double) * std::max<int64_t>(1, acc * bs)));
+  AGX_CUDA(ctx, cudaMalloc(&ctx->d_vals32, sizeof(float) * std::max<int64_t>(1, acc * bs)));
+  AGX_CUDA(ctx, cudaMemcpy(ctx->d_rowptr, rowptr.data(), sizeof(int32_t) * (nn + 1), cudaMemcpyHostToDevice));
+  AGX_CUDA(ctx, cudaMemcpy(ctx->d_col, col.data(), sizeof(int32_t) * acc, cudaMemcpyHostToDevice));
+  AGX_CUDA(ctx, cudaMemcpy(ctx->d_diagpos, diagpos.data(), sizeof(int32_t) * nn, cudaMemcpyHostToDevice));
+  for (size_t si = 0; si < ctx->sets.size(); ++si) {
+    auto& s = ctx->sets[si];
+    size_t n = epos[si].size();
+    AGX_CUDA(ctx, cudaMalloc(&s.d_epos, sizeof(int32_t) * std::max<size_t>(1, n)));
+    AGX_CUDA(ctx, cudaMemcpy(s.d_epos, epos[si].data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+  }
+  ctx->pattern_ready = true;
+  return AGX_OK;
+}

@@ -1,0 +1,220 @@
+"""``solver.solver`` of AutoPDEx, run by the GB300 backend.
+
+Drop-in for ``autopdex.solver.solver(dofs, settings, static_settings, **kwargs)``
+(solver.py:41-137) when ``static_settings['solver backend'] == 'gb300'``: same dicts, same
+DOF pytree in and out, same ``infos = (n_iter, res_norm, diverged)`` of the Newton solvers
+(solver.py:740-948).  Assembly, the sparse pattern, the Dirichlet elimination, the Krylov
+solve and the Newton loop run on the GPU through libautopdex_gb300.
+
+Keys read from ``static_settings`` (besides AutoPDEx's own):
+
+* ``'solver'``: ``'pcg'`` / ``'cg'`` (Jacobi-PCG, default), ``'bicgstab'`` (non-symmetric
+  tangents), ``'fcg'`` (flexible CG for the learned preconditioner); the direct-solver names
+  ``'lapack'`` / ``'umfpack'`` / ``'direct'`` run Jacobi-PCG to a relative residual of 1e-13.
+* ``'precision'``: ``'float64'`` (default) or ``'mixed'`` (float32 tangent and Krylov
+  iterations inside the float64 Newton / refinement loop).
+* ``'type of preconditioner'``: ``'jacobi'`` (default) or ``'learned'`` (the network set with
+  :func:`set_learned_preconditioner`; Jacobi when none is set).
+
+Extra keyword arguments: ``newton_tol``, ``maxiter`` (Newton), ``newton_rtol`` (stop also at
+``||R|| <= newton_rtol ||R_0||``), ``krylov_tol``, ``krylov_maxiter``, ``reuse_tangent``.
+"""
+import numpy as np
+import torch
+
+from . import _native as N
+from ._problem import get_problem, flatten, _np
+
+last_info = None
+
+
+def _method(static_settings, kwargs):
+    name = static_settings.get("solver", "pcg")
+    precision = static_settings.get("precision", "float64")
+    precond = static_settings.get("type of preconditioner", "jacobi")
+    direct = name in ("lapack", "umfpack", "direct", "lu", "cholesky")
+    if name in ("pcg", "cg") or direct:
+        method = N.AGX_PCG_MIXED if precision == "mixed" else N.AGX_PCG
+    elif name == "bicgstab":
+        if precision == "mixed":
+            raise NotImplementedError("BiCGStab runs in float64 only")
+        method = N.AGX_BICGSTAB
+    elif name == "fcg":
+        method = N.AGX_FCG_MIXED
+    else:
+        raise NotImplementedError(f"solver {name!r} is not available in the gb300 backend")
+    if precond == "learned":
+        method = N.AGX_FCG_MIXED
+    elif precond != "jacobi":
+        raise NotImplementedError(f"preconditioner {precond!r} is not available in the gb300 backend")
+    mixed = method in (N.AGX_PCG_MIXED, N.AGX_FCG_MIXED)
+    default_tol = 1e-13 if direct else (1e-5 if mixed else 1e-11)
+    opts = N.SolveOpts()
+    opts.method = method
+    opts.rtol = float(kwargs.get("krylov_tol", default_tol))
+    opts.atol = float(kwargs.get("krylov_atol", 0.0))
+    opts.maxiter = int(kwargs.get("krylov_maxiter", 100000))
+    opts.check_every = int(kwargs.get("krylov_check_every", 32))
+    return opts, (N.AGX_F32 if mixed else N.AGX_F64)
+
+
+def _reuse_default(static_settings):
+    """Tangents of the quadratic potentials do not depend on the DOFs."""
+    from . import _native as NN
+    return all(getattr(m, "kernel", None) in (NN.AGX_MODEL_POISSON_SINCOS, NN.AGX_MODEL_HEAT_POTENTIAL,
+                                               NN.AGX_MODEL_NEUMANN) for m in static_settings["model"])
+
+
+def _backend_check(static_settings):
+    if static_settings.get("solver backend") != "gb300":
+        raise ValueError("autopdex_gb300.solver needs static_settings['solver backend'] == 'gb300'")
+    sol = static_settings.get("solution structure", ())
+    if any(s != "nodal imposition" for s in sol):
+        raise NotImplementedError("the gb300 backend implements 'nodal imposition' of Dirichlet DOFs")
+
+
+def _out_like(flat_dev, dofs, key):
+    """Result with the structure and array type of ``dofs``."""
+    ref = dofs[key] if isinstance(dofs, dict) else dofs
+    if isinstance(ref, torch.Tensor):
+        out = flat_dev.reshape(ref.shape).to(ref.device)
+    else:
+        out = flat_dev.cpu().numpy().reshape(np.shape(ref))
+    return {key: out} if isinstance(dofs, dict) else out
+
+
+def solver(dofs, settings, static_settings, **kwargs):
+    """General solver (solver.py:41-137): dispatch on static_settings['solver type']."""
+    _backend_check(static_settings)
+    solver_type = static_settings["solver type"]
+    if solver_type == "newton":
+        return solve_newton(dofs, settings, static_settings, **kwargs)
+    if solver_type == "damped newton":
+        return solve_damped_newton(dofs, settings, static_settings, **kwargs)
+    if solver_type == "linear":
+        return solve_linear(dofs, settings, static_settings, **kwargs), None
+    assert False, "Solver type not implemented!"
+
+
+def solve_newton(dofs, settings, static_settings, newton_tol=1e-8, maxiter=30, **kwargs):
+    """Newton-Raphson: damped Newton with damping 1 (solver.py:740-768)."""
+    return solve_damped_newton(dofs, settings, static_settings, newton_tol, 1.0, maxiter, **kwargs)
+
+
+def solve_damped_newton(dofs, settings, static_settings, newton_tol=1e-8, damping_coefficient=0.8, maxiter=30,
+                        **kwargs):
+    """Damped Newton (solver.py:770-948) with the loop, the assembly and the linear solves
+    on the GPU.  Returns (dofs, (n_iter, res_norm, diverged))."""
+    global last_info
+    _backend_check(static_settings)
+    prob = get_problem(dofs, settings, static_settings)
+    prob.update_models(settings)
+    opts = N.NewtonOpts()
+    kopts, tdt = _method(static_settings, kwargs)
+    if kopts.method == N.AGX_FCG_MIXED:
+        _attach_learned(prob, static_settings)
+    opts.newton_tol = float(newton_tol)
+    opts.newton_rtol = float(kwargs.get("newton_rtol", 0.0))
+    opts.maxiter = int(maxiter)
+    opts.damping = float(damping_coefficient)
+    opts.tangent_dtype = tdt
+    opts.krylov = kopts
+    opts.reuse_tangent = int(kwargs.get("reuse_tangent", _reuse_default(static_settings)))
+    opts.verbose = int(static_settings.get("verbose", 0))
+    x = prob.to_device(dofs)
+    x = x.clone() if isinstance(dofs, torch.Tensor) or (isinstance(dofs, dict) and isinstance(
+        dofs[prob.key], torch.Tensor)) else x
+    cond = settings.get("dirichlet conditions")
+    g = prob.to_device(cond) if cond is not None else torch.zeros(prob.n_dofs, dtype=torch.float64,
+                                                                   device=prob.device)
+    info = N.NewtonInfo()
+    prob._call("agx_newton", N.C.c_void_p(x.data_ptr()), N.C.c_void_p(g.data_ptr()), N.C.byref(opts),
+               N.C.byref(info))
+    last_info = info
+    sol = _out_like(x, dofs, prob.key)
+    return sol, (int(info.iterations), float(info.res_norm), bool(info.diverged))
+
+
+def solve_linear(dofs, settings, static_settings, **kwargs):
+    """One linear solve with nodal imposition (solver.py:544-659): the returned DOFs hold
+    the increment on free DOFs and the prescribed values on Dirichlet DOFs."""
+    _backend_check(static_settings)
+    prob = get_problem(dofs, settings, static_settings)
+    prob.update_models(settings)
+    kopts, tdt = _method(static_settings, kwargs)
+    if kopts.method == N.AGX_FCG_MIXED:
+        _attach_learned(prob, static_settings)
+    x = prob.to_device(dofs).clone()
+    cond = settings.get("dirichlet conditions")
+    g = prob.to_device(cond) if cond is not None else torch.zeros_like(x)
+    m = torch.as_tensor(prob.mask.astype(bool), device=prob.device)
+    x = torch.where(m, g, x)
+    R = torch.empty_like(x)
+    prob._call("agx_assemble", N.C.c_void_p(x.data_ptr()), N.C.c_void_p(R.data_ptr()), tdt)
+    dx = torch.empty_like(x)
+    info = N.SolveInfo()
+    # agx_solve solves K dx = rhs on the free DOFs; rhs = -R
+    rhs = -R
+    prob._call("agx_solve", N.C.c_void_p(rhs.data_ptr()), N.C.c_void_p(dx.data_ptr()), N.C.byref(kopts),
+               N.C.byref(info))
+    out = torch.where(m, g, dx)
+    return _out_like(out, dofs, prob.key)
+
+
+def adaptive_load_stepping(dofs, settings, static_settings,
+                           multiplier_settings=lambda settings, multiplier: (
+                               settings.update({"load multiplier": multiplier}), settings)[1],
+                           path_dependent=True, implicit_diff_mode=None, max_multiplier=1.0, min_increment=0.01,
+                           max_increment=1.0, init_increment=0.2, max_load_steps=1000, target_num_newton_iter=7,
+                           newton_tol=1e-10, **kwargs):
+    """Adaptive load stepping (solver.py:139-457): multiplier loop around :func:`solver` with
+    the same increment control, roll-back on divergence and returned carry
+    (dofs, multiplier, increment, load_step, settings, res_norm)."""
+    if implicit_diff_mode is not None:
+        raise NotImplementedError("implicit differentiation through the gb300 backend is not implemented")
+    verbose = static_settings.get("verbose", 0)
+    multiplier, increment, load_step, res = 0.0, float(init_increment), 0.0, 0.0
+    while multiplier < max_multiplier and increment > min_increment:
+        multiplier += increment
+        if verbose > -1:
+            if verbose > 0:
+                print("")
+            print(f"Multiplier: {multiplier}")
+        settings = multiplier_settings(settings, multiplier)
+        new, (steps, res, div) = solver(dofs, settings, static_settings, newton_tol=newton_tol, **kwargs)
+        if div:
+            multiplier -= increment
+            increment *= 0.5
+        else:
+            increment *= 1 + 0.5 * (target_num_newton_iter - steps) / target_num_newton_iter
+            dofs = new
+        increment = min(increment, max_increment)
+        if multiplier + increment > max_multiplier:
+            increment = max_multiplier - multiplier
+        load_step = 1.0 * load_step
+        if multiplier < max_multiplier - min_increment and increment < min_increment:
+            print("Adaptive load stepping could not converge; increment size below min_increment!")
+    return dofs, multiplier, increment, load_step, settings, res
+
+
+# ---- learned preconditioner hook ------------------------------------------------------
+_learned = {}
+
+
+def set_learned_preconditioner(static_settings_or_key, preconditioner):
+    """Register a learned preconditioner (``autopdex_gb300.learned.GridPreconditioner``)
+    for problems solved with ``'type of preconditioner': 'learned'``."""
+    _learned["default"] = preconditioner
+
+
+def _attach_learned(prob, static_settings):
+    pc = _learned.get("default")
+    if static_settings.get("type of preconditioner") != "learned" or pc is None:
+        prob._call("agx_set_preconditioner", N.PRECOND_FN(0), None)
+        prob.learned = None
+        return
+    if prob.learned is not pc:
+        cb = pc.callback(prob)
+        prob._precond_cb = cb
+        prob._call("agx_set_preconditioner", cb, None)
+        prob.learned = pc

@@ -1,0 +1,30 @@
+"""Ansatz spaces known to the GB300 kernels.
+
+``fem_iso_line_quad_brick`` marks the isoparametric Lagrange space of AutoPDEx
+(spaces.py:302-12190); the kernels implement its Q1 members: 2-node lines, 4-node quads
+and 8-node bricks, with the physical-gradient rule of its custom JVP
+(spaces.py:12162-12190).  Calling it evaluates the Q1 interpolation on the host.
+"""
+import numpy as np
+
+_SIGNS = {
+    1: np.array([[-1.0], [1.0]]),
+    2: np.array([[-1.0, -1.0], [1.0, -1.0], [1.0, 1.0], [-1.0, 1.0]]),
+    3: np.array([[-1.0, -1.0, -1.0], [1.0, -1.0, -1.0], [1.0, 1.0, -1.0], [-1.0, 1.0, -1.0],
+                 [-1.0, -1.0, 1.0], [1.0, -1.0, 1.0], [1.0, 1.0, 1.0], [-1.0, 1.0, 1.0]]),
+}
+
+
+def q1_shape_functions(xi, n_dim):
+    """N_a(xi) of the Q1 element of dimension ``n_dim`` in AutoPDEx's node order."""
+    s = _SIGNS[n_dim]
+    xi = np.atleast_1d(np.asarray(xi, dtype=np.float64))
+    return np.prod((1 + s * xi[None, :]) / 2, axis=1)
+
+
+def fem_iso_line_quad_brick(x, xI, fI, settings, overwrite_diff, n_dim):
+    """Q1 interpolation sum_a N_a(x) fI[a] at the reference point ``x`` (host only)."""
+    xI = np.asarray(xI)
+    if xI.shape[0] != 2 ** n_dim:
+        raise NotImplementedError("the gb300 backend implements the Q1 members of this space")
+    return np.tensordot(q1_shape_functions(x, n_dim), np.asarray(fI, dtype=np.float64), axes=(0, 0))

@@ -1,0 +1,178 @@
+/*
+ * autopdex_gb300 -- C ABI of the GB300 solve backend for AutoPDEx.
+ *
+ * The library replaces, for the built-in Q1 models, the device work and the host hop of
+ * AutoPDEx's Newton solve path:
+ *   element residual/tangent assembly   autopdex/assembler.py:587-777, :1064-1389
+ *   COO -> CSR summation + Dirichlet row/column deletion
+ *                                       autopdex/solver.py:1180-1222 (scipy_assembling)
+ *   the linear solve of each Newton step
+ *                                       autopdex/solver.py:544-659 (solve_linear),
+ *                                       :1493-1539 (linear_solve_scipy), :951-1178 (linear_solve_jax)
+ *   the damped Newton loop              autopdex/solver.py:740-948
+ * The Python layer (autopdex_gb300.solver) mirrors solver.solver(dofs, settings,
+ * static_settings) and calls these functions through ctypes.
+ *
+ * Conventions
+ *   - Every function returns an int status: AGX_OK (0); > 0 numerical outcome
+ *     (AGX_NOT_CONVERGED, AGX_DIVERGED); < 0 usage or CUDA error.  No C++ exception
+ *     crosses the ABI.  agx_last_error() gives the message of the last failure.
+ *   - Set-up functions (agx_set_nodes, agx_add_element_set, agx_set_dirichlet,
+ *     agx_set_model, agx_set_element_field) take HOST pointers and copy.  Compute
+ *     functions take DEVICE pointers owned by the caller; the library owns the pattern,
+ *     the matrix values and all scratch vectors.
+ *   - DOFs are one flat float64 vector, node-major: dof = node * ndof + component, the
+ *     numbering AutoPDEx uses for a single-field dict or an (n_nodes, ndof) array
+ *     (assembler.py:47-141, :331-436).
+ *   - One context per CUDA stream; a context is not thread-safe.
+ */
+#ifndef AUTOPDEX_GB300_H
+#define AUTOPDEX_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define AGX_OK 0
+#define AGX_NOT_CONVERGED 1   /* iteration limit reached (solver.py:926-930) */
+#define AGX_DIVERGED 2        /* NaN/Inf or growth > 10x (solver.py:914-925), Krylov breakdown */
+#define AGX_ERR_ARG (-1)
+#define AGX_ERR_CUDA (-2)
+#define AGX_ERR_UNSUPPORTED (-3)
+#define AGX_ERR_STATE (-5)
+
+/* element types: Q1 quad (spaces.py:1913-1922), Q1 hex (spaces.py:12057-12081),
+   2-node line for surface tractions (spaces.py:356-358) */
+#define AGX_QUAD4 0
+#define AGX_HEX8 1
+#define AGX_LINE2 2
+
+/* built-in models (descriptors of the closures AutoPDEx builds in models.py) */
+#define AGX_MODEL_POISSON_SINCOS 0 /* 'user potential' 1/2|grad u|^2 - b(x) u,
+                                      b = a (sin(w x.x) - cos(w |x-c|^2)); params a, w, c[dim]
+                                      (tests/test_dicts_as_dofs_user_potential.py:25-35) */
+#define AGX_MODEL_HEAT_POTENTIAL 1 /* 'user potential' 1/2 k_e |grad u|^2 - f u; params f;
+                                      element field k_e (models.py:1188-1269) */
+#define AGX_MODEL_NEO_HOOKE 2      /* 'user element' hyperelastic Galerkin, Ciarlet neo-Hooke,
+                                      plane strain (quad) or 3d (hex); params E, nu
+                                      (models.py:917-1000, :1122-1146, :1616-1718) */
+#define AGX_MODEL_NEUMANN 3        /* 'user element' surface traction, zero tangent; params t[dim]
+                                      (models.py:744-780, :1723-1851) */
+#define AGX_MODEL_HEAT_BE 4        /* 'user residual' backward Euler, k(T) = k0 + k2 T^2;
+                                      params k0, k2, rho_c, dt; node field T_n
+                                      (models.py:1272-1357) */
+
+/* matrix value types */
+#define AGX_F64 0
+#define AGX_F32 1
+
+/* Krylov methods for agx_solve / the linear step of agx_newton */
+#define AGX_PCG 0        /* Jacobi-PCG, float64 matrix and vectors */
+#define AGX_PCG_MIXED 1  /* Jacobi-PCG in float32 (matrix, vectors), float64 dots */
+#define AGX_BICGSTAB 2   /* Jacobi-BiCGStab in float64, for non-symmetric tangents */
+#define AGX_FCG_MIXED 3  /* flexible CG in float32 with the registered preconditioner
+                            (agx_set_preconditioner), Jacobi when none is registered */
+
+typedef struct agx_context agx_context;
+
+/* Preconditioner callback for AGX_FCG_MIXED: z = M(r) on the free DOFs, float32 device
+   vectors of length n_dofs, launched on `stream`.  Returns 0 on success. */
+typedef int (*agx_precond_fn)(void* user, const float* r, float* z, int64_t n, void* stream);
+
+typedef struct {
+  int method;          /* AGX_PCG, AGX_PCG_MIXED, AGX_BICGSTAB, AGX_FCG_MIXED */
+  double rtol;         /* stop when ||r|| <= rtol ||b|| (jax.scipy cg semantics, solver.py:1116) */
+  double atol;         /* ... or ||r|| <= atol */
+  int maxiter;
+  int check_every;     /* iterations between host convergence checks (>= 1) */
+} agx_solve_opts;
+
+typedef struct {
+  int iterations;
+  double rel_residual; /* ||r|| / ||b|| of the recurrence residual */
+  int status;          /* AGX_OK, AGX_NOT_CONVERGED, AGX_DIVERGED */
+} agx_solve_info;
+
+typedef struct {
+  double newton_tol;   /* absolute tolerance on ||R_free||_2 (solver.py:899-903) */
+  double newton_rtol;  /* stop also when ||R_free|| <= newton_rtol * ||R_free(first iterate)||;
+                          0 disables (the reference has the absolute test only) */
+  int maxiter;         /* solver.py:740-768 default 30 */
+  double damping;      /* 1.0 for 'newton' (solver.py:767) */
+  int tangent_dtype;   /* AGX_F64 or AGX_F32 */
+  agx_solve_opts krylov;
+  int reuse_tangent;   /* 1: assemble the tangent once (models whose tangent does not
+                          depend on the DOFs: iterative refinement) */
+  int verbose;
+} agx_newton_opts;
+
+typedef struct {
+  int iterations;                 /* Newton iterations performed */
+  double res_norm;                /* ||R_free||_2 after the last iteration */
+  double res0;                    /* ||R_free||_2 at the first iterate (prescribed values set) */
+  int diverged;                   /* solver.py:914-930 semantics */
+  int krylov_iterations;          /* total inner iterations */
+  int n_history;
+  double res_history[64];
+  int krylov_history[64];
+} agx_newton_info;
+
+/* ---- context ---------------------------------------------------------------------- */
+/* Replaces the jit set-up of solver.solver (solver.py:41, utility.py:32-80). */
+int agx_create(agx_context** ctx, void* cuda_stream);
+int agx_destroy(agx_context* ctx);
+const char* agx_last_error(const agx_context* ctx);
+
+/* ---- problem definition (host pointers) -------------------------------------------- */
+/* settings['node coordinates'] and the DOF layout (assembler.py:143-183). */
+int agx_set_nodes(agx_context* ctx, int64_t n_nodes, int dim, const double* coords, int ndof);
+/* One entry of settings['connectivity'] / static_settings['assembling mode']
+   (assembler.py:587-777); returns the set index in *set_id. */
+int agx_add_element_set(agx_context* ctx, int elem_type, int64_t n_elem, int nen,
+                        const int64_t* conn, int* set_id);
+/* settings['dirichlet dofs'] flattened (solver.py:586-604); 1 = prescribed. */
+int agx_set_dirichlet(agx_context* ctx, const uint8_t* mask);
+/* Builds the node-block CSR pattern and the element -> pattern scatter map, the work
+   that scipy_assembling redoes on the host every Newton step (solver.py:1180-1222). */
+int agx_finalize(agx_context* ctx);
+/* static_settings['model'][set] (models.py builders); params as listed per model. */
+int agx_set_model(agx_context* ctx, int set_id, int model, const double* params, int n_params);
+/* per-element coefficient (host pointer, n_elem values), e.g. conductivity k_e */
+int agx_set_element_field(agx_context* ctx, int set_id, const double* field);
+/* per-DOF auxiliary field (DEVICE pointer, kept by reference), e.g. settings['dofs n'] */
+int agx_set_node_field(agx_context* ctx, int set_id, const double* field_dev);
+
+/* ---- compute (device pointers) ----------------------------------------------------- */
+/* assemble_residual (assembler.py:587-637) into `residual` (n_dofs, may be NULL) and,
+   when tangent_dtype >= 0, assemble_tangent (assembler.py:682-777) into the library's
+   BSR values with Dirichlet rows/columns eliminated (identity rows). */
+int agx_assemble(agx_context* ctx, const double* dofs, double* residual, int tangent_dtype);
+/* Pattern and values of the last assembled tangent (device pointers owned by the
+   library): rowptr (n_nodes+1), col (nnzb), vals (nnzb*ndof*ndof of the dtype). */
+int agx_get_matrix(agx_context* ctx, int dtype, const int32_t** rowptr, const int32_t** col,
+                   const void** vals, int64_t* nnzb);
+/* Copies the pattern and the values of the last assembled tangent of `dtype` into
+   caller-owned DEVICE buffers (rowptr n_nodes+1, col nnzb, vals nnzb*ndof*ndof). */
+int agx_copy_matrix(agx_context* ctx, int dtype, int32_t* rowptr, int32_t* col, void* vals);
+/* y = K x with the last assembled tangent of `dtype` (x, y of that dtype). */
+int agx_spmv(agx_context* ctx, int dtype, const void* x, void* y);
+/* Linear solve K x = rhs on the free DOFs, zeros on prescribed DOFs: the callback
+   contract of linear_solve_scipy (solver.py:1493-1539) with an iterative method. */
+int agx_solve(agx_context* ctx, const double* rhs, double* x, const agx_solve_opts* opts,
+              agx_solve_info* info);
+/* The Newton loop of solve_damped_newton/damped_newton (solver.py:770-948): `dofs` is
+   updated in place; `dirichlet_values` (n_dofs) holds settings['dirichlet conditions']. */
+int agx_newton(agx_context* ctx, double* dofs, const double* dirichlet_values,
+               const agx_newton_opts* opts, agx_newton_info* info);
+/* Registers the preconditioner used by AGX_FCG_MIXED (NULL restores Jacobi). */
+int agx_set_preconditioner(agx_context* ctx, agx_precond_fn fn, void* user);
+/* Sizes for the host layer: n_dofs, nnzb, ndof. */
+int agx_get_sizes(const agx_context* ctx, int64_t* n_dofs, int64_t* nnzb, int* ndof);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AUTOPDEX_GB300_H */

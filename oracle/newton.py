@@ -1,0 +1,196 @@
+"""Oracle: global assembly, SciPy linear solve and the damped Newton loop (float64).
+
+Test infrastructure only (see ``oracle/__init__.py``).
+
+A problem is a list of element *sets* sharing one flat DOF vector laid out node-major
+(``dof = node * ndof + component``), which is how AutoPDEx numbers the DOFs of a
+single-field dict or an ``(n_nodes, ndof)`` array (assembler.py:47-141, :331-436).
+"""
+import numpy as np
+import scipy.sparse
+import scipy.sparse.linalg
+import torch
+
+from . import elements as el
+
+DT = torch.float64
+
+
+class ElementSet:
+    """One domain of the problem ('assembling mode' entry).
+
+    kind: 'potential' | 'element' | 'residual' | 'neumann'
+    fun:  the element routine from ``oracle.elements``
+    params(settings) -> per-element parameters, shape (n_e, p)
+    """
+
+    def __init__(self, kind, conn, fun, params, ndof, traction=None):
+        self.kind = kind
+        self.conn = np.asarray(conn, dtype=np.int64)
+        self.fun = fun
+        self.params = params
+        self.ndof = ndof
+        self.traction = traction
+
+    def element_dofs(self):
+        """Global DOF indices per element, node-major: (n_e, nen*ndof)."""
+        c = self.conn[:, :, None] * self.ndof + np.arange(self.ndof)[None, None, :]
+        return c.reshape(self.conn.shape[0], -1)
+
+
+def element_contributions(s, dofs, coords, settings):
+    """R_e (n_e, m) and K_e (n_e, m, m) for every element of set ``s``."""
+    conn = s.conn
+    xI = torch.as_tensor(coords[conn], dtype=DT)
+    if s.kind == "neumann":
+        t = s.traction(settings)
+        R = np.stack([s.fun(coords[c], t) for c in conn])
+        m = R.shape[1]
+        return R, np.zeros((conn.shape[0], m, m))
+    p = torch.as_tensor(s.params(settings), dtype=DT)
+    if s.ndof == 1:
+        fI = torch.as_tensor(dofs[conn], dtype=DT)
+    else:
+        fI = torch.as_tensor(dofs.reshape(-1, s.ndof)[conn], dtype=DT)
+    if s.kind == "residual":
+        TnI = torch.as_tensor(np.asarray(settings["dofs n"]).reshape(-1)[conn], dtype=DT)
+        R, K = el.batched(s.fun, fI, TnI, xI, p)
+    else:
+        R, K = el.batched(s.fun, fI, xI, p)
+    n_e = conn.shape[0]
+    return R.reshape(n_e, -1).numpy(), K.reshape(n_e, R.reshape(n_e, -1).shape[1], -1).numpy()
+
+
+def assemble(sets, dofs, coords, settings, n_dofs, tangent=True):
+    """Residual (n_dofs,) and the COO tangent with duplicates (rows, cols, data).
+
+    Residual: scatter-add of element vectors (assembler.py:331-436).  Tangent entries in
+    the order of ``_get_indices`` -- per element, rows repeated, columns tiled
+    (assembler.py:123-141) -- with the duplicates kept, as the BCOO of
+    assembler.py:1142-1148 keeps them.
+    """
+    R = np.zeros(n_dofs)
+    rows, cols, data = [], [], []
+    for s in sets:
+        Re, Ke = element_contributions(s, dofs, coords, settings)
+        ed = s.element_dofs()
+        np.add.at(R, ed.ravel(), Re.ravel())
+        if tangent:
+            m = ed.shape[1]
+            rows.append(np.repeat(ed, m, axis=1).ravel())
+            cols.append(np.tile(ed, (1, m)).ravel())
+            data.append(Ke.reshape(-1))
+    if not tangent:
+        return R, None
+    return R, (np.concatenate(rows), np.concatenate(cols), np.concatenate(data))
+
+
+def scipy_assembling(coo, n_dofs, free):
+    """COO -> CSR with duplicates summed, then Dirichlet columns and rows deleted
+    (solver.py:1180-1222)."""
+    rows, cols, data = coo
+    A = scipy.sparse.csr_matrix(scipy.sparse.coo_matrix((data, (rows, cols)), shape=(n_dofs, n_dofs)))
+    if free is not None:
+        A = A[:, free]
+        A = A[free]
+    return A
+
+
+def linear_solve_scipy(coo, rhs, n_dofs, free):
+    """spsolve on the reduced system; zeros on Dirichlet entries (solver.py:1493-1539)."""
+    A = scipy_assembling(coo, n_dofs, free)
+    b = rhs[free] if free is not None else rhs
+    x = scipy.sparse.linalg.spsolve(A.tocsc(), b)
+    sol = np.zeros_like(rhs)
+    if free is not None:
+        sol[free] = x
+    else:
+        sol[:] = x
+    return sol
+
+
+def linear_solve_cg_jacobi(coo, rhs, n_dofs, free, rtol=1e-10, maxiter=100000):
+    """Jacobi-preconditioned CG on the reduced assembled system (the algorithm of the
+    reference's 'jax' backend with 'cg' + 'jacobi', solver.py:1093-1116, on an assembled
+    matrix instead of a matrix-free product)."""
+    A = scipy_assembling(coo, n_dofs, free)
+    b = rhs[free]
+    d = A.diagonal()
+    M = scipy.sparse.linalg.LinearOperator(A.shape, matvec=lambda v: v / d)
+    x, info = scipy.sparse.linalg.cg(A, b, rtol=rtol, atol=0.0, M=M, maxiter=maxiter)
+    sol = np.zeros_like(rhs)
+    sol[free] = x
+    return sol
+
+
+class Problem:
+    """settings/static_settings equivalent for the oracle."""
+
+    def __init__(self, sets, coords, n_dofs, dirichlet_mask, dirichlet_values, linear_solver="lapack"):
+        self.sets = sets
+        self.coords = np.asarray(coords, dtype=np.float64)
+        self.n_dofs = n_dofs
+        self.dirichlet = np.asarray(dirichlet_mask, dtype=bool).reshape(-1)
+        self.values = np.asarray(dirichlet_values, dtype=np.float64).reshape(-1)
+        self.linear_solver = linear_solver
+
+    def residual(self, dofs, settings):
+        return assemble(self.sets, dofs, self.coords, settings, self.n_dofs, tangent=False)[0]
+
+    def solve_linear(self, dofs, settings):
+        """solver.solve_linear with nodal imposition (solver.py:544-659): set the Dirichlet
+        values, rhs = -R, solve on the free DOFs, return dofs with free entries replaced by
+        the increment and Dirichlet entries holding the prescribed values."""
+        dofs = np.where(self.dirichlet, self.values, dofs)
+        R, coo = assemble(self.sets, dofs, self.coords, settings, self.n_dofs)
+        free = ~self.dirichlet
+        if self.linear_solver == "lapack":
+            sol = linear_solve_scipy(coo, -R, self.n_dofs, free)
+        else:
+            sol = linear_solve_cg_jacobi(coo, -R, self.n_dofs, free)
+        return np.where(free, sol, dofs)
+
+
+def damped_newton(problem, dofs0, settings, newton_tol=1e-8, maxiter=30, damping=1.0, verbose=-1):
+    """solver.damped_newton (solver.py:837-948), one loop iteration per step:
+    solve, damped update of the free DOFs, Dirichlet DOFs set, residual norm over the free
+    DOFs, stop at ||R_free|| <= tol, divergence if the norm grows tenfold after the second
+    iteration or is NaN/Inf, and a final forced stop after ``maxiter``."""
+    free = ~problem.dirichlet
+    dofs = np.asarray(dofs0, dtype=np.float64).reshape(-1).copy()
+    itt, not_stop, res_old, div = 0, True, 0.0, False
+    history = []
+    while not_stop:
+        delta = problem.solve_linear(dofs, settings)
+        delta = np.where(free, damping * delta, delta)
+        dofs = np.where(free, dofs + delta, delta)
+        R = problem.residual(dofs, settings)
+        rf = np.where(free, R, 0.0)
+        res = float(np.linalg.norm(rf))
+        history.append(res)
+        keep = res > newton_tol
+        if itt < maxiter:
+            with np.errstate(divide="ignore", invalid="ignore"):
+                div = bool((res / res_old > 10 if res_old != 0 else res > 0) and itt > 1)
+            if not np.all(np.isfinite(rf)):
+                div = True
+            nxt = not div
+        else:
+            nxt, div = False, True
+        itt += 1
+        res_old = res
+        not_stop = keep and nxt
+    return dofs, (itt, res, div), history
+
+
+def load_stepping(problem, dofs0, settings, multipliers, set_multiplier, newton_tol=1e-10, maxiter=30):
+    """Fixed load steps, each a Newton solve started from the previous solution (the loop of
+    solver.adaptive_load_stepping, solver.py:308-378, with prescribed increments)."""
+    dofs = np.asarray(dofs0, dtype=np.float64).reshape(-1).copy()
+    infos = []
+    for m in multipliers:
+        settings = set_multiplier(settings, m)
+        problem.values = settings.get("__dirichlet_values__", problem.values)
+        dofs, info, _ = damped_newton(problem, dofs, settings, newton_tol, maxiter)
+        infos.append(info)
+    return dofs, infos

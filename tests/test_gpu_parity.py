@@ -1,0 +1,187 @@
+"""GPU kernels against the CPU oracle on the same seeded inputs (parity proper).
+
+Tolerances, written where they are used:
+* float64 residuals:   ||R_gpu - R_oracle|| <= 1e-12 ||R_oracle||  (random, non-converged DOFs)
+* float64 tangents:    max |K_gpu - K_oracle| <= 1e-12 max |K_oracle|
+* float32 tangents:    max |K32 - K_oracle| <= 2e-6 max |K_oracle|
+* Newton solutions:    ||u_gpu - u_oracle||_inf <= 1e-8 max(1, ||u_oracle||_inf), both converged
+                       to the Newton tolerance (solver.py:899-903 semantics)
+"""
+import numpy as np
+import pytest
+import scipy.sparse
+
+from autopdex_gb300 import configs
+from oracle import newton
+from oracle_setup import oracle_problem, oracle_settings
+
+pytestmark = pytest.mark.gpu
+
+
+def _flat(d):
+    a = next(iter(d.values())) if isinstance(d, dict) else d
+    return np.asarray(a, dtype=np.float64).reshape(-1)
+
+
+def _like(w, flat):
+    d = w.dofs
+    if isinstance(d, dict):
+        k = next(iter(d))
+        return {k: flat.reshape(np.shape(d[k]))}
+    return flat.reshape(np.shape(d))
+
+
+def _random_dofs(w, scale, seed=0):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(-scale, scale, w.n_dofs)
+
+
+CASES = {
+    "poisson": (lambda: configs.poisson(n=12), 1.0),
+    "heat": (lambda: configs.heat_grf(n=10, seed=4), 1.0),
+    "neo_hooke_3d": (lambda: configs.neo_hooke_cube(n=3, n_steps=2), 0.02),
+    "cook": (lambda: configs.cook_membrane(n=6, n_steps=2), 0.05),
+    "heat_be": (lambda: configs.heat_transient(n=3, n_steps=1), 1.0),
+}
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_residual_parity(case):
+    from autopdex_gb300 import assembler
+    make, scale = CASES[case]
+    w = make()
+    if case == "cook":
+        w.settings["load multiplier"] = 0.03
+    u = _random_dofs(w, scale)
+    R_gpu = _flat(assembler.assemble_residual(_like(w, u), w.settings, w.static_settings))
+    prob = oracle_problem(w)
+    R_or = newton.assemble(prob.sets, u, prob.coords, oracle_settings(w), prob.n_dofs, tangent=False)[0]
+    assert np.linalg.norm(R_gpu - R_or) <= 1e-12 * np.linalg.norm(R_or)
+
+
+@pytest.mark.parametrize("case", list(CASES))
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_tangent_parity(case, dtype):
+    from autopdex_gb300 import assembler
+    make, scale = CASES[case]
+    w = make()
+    u = _random_dofs(w, scale, seed=1)
+    K = assembler.assemble_tangent(_like(w, u), w.settings, w.static_settings, dtype=dtype).to_scipy()
+    prob = oracle_problem(w)
+    _, coo = newton.assemble(prob.sets, u, prob.coords, oracle_settings(w), prob.n_dofs)
+    K_or = newton.scipy_assembling(coo, prob.n_dofs, None)
+    diff = abs(K - K_or).max()
+    tol = 1e-12 if dtype == "float64" else 2e-6
+    assert diff <= tol * abs(K_or).max()
+
+
+def test_dirichlet_elimination_matches_row_column_deletion():
+    """Free-free block equals scipy_assembling's reduced matrix (solver.py:1214-1217);
+    prescribed rows/columns are identity."""
+    from autopdex_gb300 import assembler
+    w = configs.cook_membrane(n=5, n_steps=2)
+    u = _random_dofs(w, 0.05, seed=2)
+    K = assembler.assemble_tangent(_like(w, u), w.settings, w.static_settings, eliminate_dirichlet=True).to_scipy()
+    prob = oracle_problem(w)
+    _, coo = newton.assemble(prob.sets, u, prob.coords, oracle_settings(w), prob.n_dofs)
+    free = ~prob.dirichlet
+    K_red = newton.scipy_assembling(coo, prob.n_dofs, free)
+    assert abs(K[free][:, free] - K_red).max() <= 1e-12 * abs(K_red).max()
+    d = prob.dirichlet
+    Kd = K[d]
+    assert np.array_equal(Kd.toarray(), scipy.sparse.eye(prob.n_dofs, format="csr")[d].toarray())
+
+
+def test_golden_poisson_5x5_through_backend():
+    """The reference's golden test (test_dicts_as_dofs_user_potential.py:63) with
+    'solver backend': 'gb300'."""
+    from autopdex_gb300 import solver
+    w = configs.poisson(n=5, solver="lapack")
+    sol, (it, res, div) = solver.solver(w.dofs, w.settings, w.static_settings)
+    assert not div
+    assert abs(sol["phi"].sum() - 1.9066412530282952) <= 1e-10 * 1.9066412530282952
+
+
+@pytest.mark.parametrize("case", ["poisson", "heat"])
+@pytest.mark.parametrize("precision", ["float64", "mixed"])
+def test_linear_solve_matches_oracle(case, precision):
+    from autopdex_gb300 import solver
+    w = configs.poisson(n=40, precision=precision) if case == "poisson" else configs.heat_grf(n=32, seed=7,
+                                                                                             precision=precision)
+    sol, (it, res, div) = solver.solver(w.dofs, w.settings, w.static_settings, newton_tol=1e-10,
+                                        newton_rtol=1e-12)
+    assert not div
+    prob = oracle_problem(w)
+    ref, info, _ = newton.damped_newton(prob, np.zeros(w.n_dofs), oracle_settings(w), 1e-10)
+    u = _flat(sol)
+    assert np.abs(u - ref).max() <= 1e-8 * max(1.0, np.abs(ref).max())
+    if precision == "mixed":
+        assert it >= 2  # float32 inner solves refined by float64 Newton residuals
+
+
+@pytest.mark.parametrize("precision", ["float64", "mixed"])
+def test_neo_hooke_cube_load_steps_match_oracle(precision):
+    from autopdex_gb300 import solver
+    w = configs.neo_hooke_cube(n=3, n_steps=2, precision=precision)
+    prob = oracle_problem(w)
+    u_gpu = w.dofs
+    u_or = np.zeros(w.n_dofs)
+    for step in w.steps:
+        w.settings = step(w.settings)
+        prob.values = np.asarray(w.settings["dirichlet conditions"]).reshape(-1)
+        u_gpu, (it, res, div) = solver.solver(u_gpu, w.settings, w.static_settings, newton_tol=1e-9)
+        assert not div and res <= 1e-9
+        u_or, info, _ = newton.damped_newton(prob, u_or, oracle_settings(w), 1e-9)
+    assert np.abs(_flat(u_gpu) - u_or).max() <= 1e-8 * max(1.0, np.abs(u_or).max())
+
+
+def test_cook_load_steps_match_oracle():
+    from autopdex_gb300 import solver
+    w = configs.cook_membrane(n=6, n_steps=2)
+    prob = oracle_problem(w)
+    u_gpu = w.dofs
+    u_or = np.zeros(w.n_dofs)
+    for step in w.steps:
+        w.settings = step(w.settings)
+        u_gpu, (it, res, div) = solver.solver(u_gpu, w.settings, w.static_settings, newton_tol=1e-9)
+        assert not div
+        u_or, info, _ = newton.damped_newton(prob, u_or, oracle_settings(w), 1e-9)
+    assert np.abs(_flat(u_gpu) - u_or).max() <= 1e-8 * max(1.0, np.abs(u_or).max())
+
+
+def test_heat_backward_euler_step_matches_oracle():
+    from autopdex_gb300 import solver
+    w = configs.heat_transient(n=4, n_steps=1)
+    prob = oracle_problem(w)
+    sol, (it, res, div) = solver.solver(w.dofs, w.settings, w.static_settings, newton_tol=1e-10)
+    assert not div
+    ref, info, _ = newton.damped_newton(prob, w.raw["T0"].copy(), oracle_settings(w), 1e-10)
+    assert np.abs(_flat(sol) - ref).max() <= 1e-8
+
+
+def test_newton_reports_divergence_on_nan_input():
+    """NaN DOFs (injected on the host) give the reference's diverged flag, no exception."""
+    from autopdex_gb300 import solver
+    w = configs.neo_hooke_cube(n=2, n_steps=1)
+    w.settings = w.steps[0](w.settings)
+    u = np.zeros((w.n_dofs // 3, 3))
+    u[5, 1] = np.nan
+    sol, (it, res, div) = solver.solver(u, w.settings, w.static_settings, maxiter=3)
+    assert div
+
+
+def test_newton_maxiter_stop():
+    from autopdex_gb300 import solver
+    w = configs.neo_hooke_cube(n=2, n_steps=1)
+    w.settings = w.steps[0](w.settings)
+    sol, (it, res, div) = solver.solver(w.dofs, w.settings, w.static_settings, newton_tol=1e-300, maxiter=1)
+    assert it == 2 and div  # maxiter + 1 passes, then the forced stop (solver.py:926-930)
+
+
+def test_all_dofs_prescribed():
+    from autopdex_gb300 import solver
+    w = configs.poisson(n=3)
+    w.settings["dirichlet dofs"] = {"phi": np.ones(16, dtype=bool)}
+    w.settings["dirichlet conditions"] = {"phi": np.arange(16.0)}
+    sol, (it, res, div) = solver.solver(w.dofs, w.settings, w.static_settings)
+    assert np.array_equal(sol["phi"], np.arange(16.0)) and res == 0.0 and not div
