@@ -22,6 +22,9 @@ AGX_MODEL_HEAT_BE = 4
 AGX_F64, AGX_F32 = 0, 1
 AGX_PCG, AGX_PCG_MIXED, AGX_BICGSTAB, AGX_FCG_MIXED = 0, 1, 2, 3
 
+AGX_PROF_TANGENT, AGX_PROF_RESIDUAL, AGX_PROF_SPMV, AGX_PROF_VECTOR, AGX_PROF_PRECOND = 0, 1, 2, 3, 4
+AGX_PROF_CATEGORIES = 8
+
 PRECOND_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p)
 
 
@@ -65,6 +68,9 @@ _SIGNATURES = {
     "agx_solve": (C.c_int, [_P, _P, _P, C.POINTER(SolveOpts), C.POINTER(SolveInfo)]),
     "agx_newton": (C.c_int, [_P, _P, _P, C.POINTER(NewtonOpts), C.POINTER(NewtonInfo)]),
     "agx_set_preconditioner": (C.c_int, [_P, PRECOND_FN, _P]),
+    "agx_profile": (C.c_int, [_P, C.c_int]),
+    "agx_profile_read": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    "agx_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "agx_get_sizes": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
 }
 

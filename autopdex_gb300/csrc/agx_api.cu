@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -59,6 +60,10 @@ void free_device(agx_context* ctx) {
   release(ctx->d_counter);
   release(ctx->d_scal);
   release(ctx->d_norm);
+  for (int c = 0; c < AGX_PROF_CATEGORIES; ++c) {
+    for (auto e : ctx->prof_ev[c]) cudaEventDestroy(e);
+    ctx->prof_ev[c].clear();
+  }
   if (ctx->h_scal) cudaFreeHost(ctx->h_scal);
   if (ctx->h_norm) cudaFreeHost(ctx->h_norm);
   ctx->h_scal = nullptr;
@@ -104,6 +109,8 @@ int agx_create(agx_context** out, void* stream) {
   agx_context* ctx = new (std::nothrow) agx_context();
   if (!ctx) return AGX_ERR_ARG;
   ctx->stream = (cudaStream_t)stream;
+  const char* dbg = getenv("AGX_DEBUG");
+  ctx->debug = (dbg && dbg[0] == '1') ? 1 : 0;
   cudaError_t e = cudaGetDevice(&ctx->device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
   if (e != cudaSuccess) {
@@ -301,6 +308,36 @@ int agx_copy_matrix(agx_context* ctx, int dtype, int32_t* rowptr, int32_t* col, 
     AGX_CUDA(ctx, cudaMemcpyAsync(vals, src, es * bs * ctx->nnzb, cudaMemcpyDeviceToDevice, ctx->stream));
   }
   AGX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return AGX_OK;
+}
+
+int agx_profile(agx_context* ctx, int enable) {
+  if (!ctx) return AGX_ERR_ARG;
+  ctx->prof_on = enable != 0;
+  for (int c = 0; c < AGX_PROF_CATEGORIES; ++c) ctx->prof_used[c] = 0;
+  return AGX_OK;
+}
+
+int agx_profile_read(agx_context* ctx, double* ms, int64_t* launches) {
+  if (!ctx) return AGX_ERR_ARG;
+  AGX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int c = 0; c < AGX_PROF_CATEGORIES; ++c) {
+    double tot = 0;
+    for (size_t i = 0; i < ctx->prof_used[c]; ++i) {
+      float t = 0;
+      AGX_CUDA(ctx, cudaEventElapsedTime(&t, ctx->prof_ev[c][2 * i], ctx->prof_ev[c][2 * i + 1]));
+      tot += t;
+    }
+    if (ms) ms[c] = tot;
+    if (launches) launches[c] = (int64_t)ctx->prof_used[c];
+    ctx->prof_used[c] = 0;
+  }
+  return AGX_OK;
+}
+
+int agx_launch_count(const agx_context* ctx, int64_t* launches) {
+  if (!ctx || !launches) return AGX_ERR_ARG;
+  *launches = ctx->n_launches;
   return AGX_OK;
 }
 

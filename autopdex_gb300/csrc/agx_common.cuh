@@ -52,6 +52,7 @@ struct agx_context {
   std::string err;
   int device = 0;
   int sm_count = 152;
+  int debug = 0;  // AGX_DEBUG=1 in the environment: print Krylov scalars at every host check
 
   // nodes and DOFs
   int64_t n_nodes = 0;
@@ -96,6 +97,14 @@ struct agx_context {
   double* d_norm = nullptr;              // 4 doubles
   double* h_norm = nullptr;              // pinned
 
+  // kernels launched by this context (for the benchmark's launch count)
+  int64_t n_launches = 0;
+
+  // kernel timing (agx_profile): event pairs per category, reused across reads
+  bool prof_on = false;
+  std::vector<cudaEvent_t> prof_ev[AGX_PROF_CATEGORIES];
+  size_t prof_used[AGX_PROF_CATEGORIES] = {0};
+
   // learned preconditioner hook (set by the host layer; null = Jacobi)
   agx_precond_fn precond = nullptr;
   void* precond_user = nullptr;
@@ -128,6 +137,29 @@ void agx_launch_newton_update(agx_context* ctx, double* dofs, const double* dx, 
                               double damping);
 void agx_launch_negate_free(agx_context* ctx, const double* R, double* b);
 int agx_spmv_impl(agx_context* ctx, int dtype, const void* x, void* y);
+
+// Brackets the launches issued during its lifetime with events of category `cat`.
+struct agx_prof_scope {
+  agx_context* ctx;
+  int cat;
+  cudaEvent_t stop = nullptr;
+  agx_prof_scope(agx_context* c, int k) : ctx(c), cat(k) {
+    if (!ctx->prof_on) return;
+    auto& ev = ctx->prof_ev[cat];
+    size_t u = ctx->prof_used[cat];
+    while (ev.size() < 2 * (u + 1)) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return;
+      ev.push_back(e);
+    }
+    cudaEventRecord(ev[2 * u], ctx->stream);
+    stop = ev[2 * u + 1];
+    ctx->prof_used[cat] = u + 1;
+  }
+  ~agx_prof_scope() {
+    if (stop) cudaEventRecord(stop, ctx->stream);
+  }
+};
 
 static inline int agx_grid(const agx_context* ctx, int64_t n, int per_sm = 8) {
   int64_t want = (n + AGX_BLOCK - 1) / AGX_BLOCK;

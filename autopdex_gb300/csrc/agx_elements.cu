@@ -144,6 +144,14 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
     if constexpr (MODEL == AGX_MODEL_HEAT_BE) tna = (T)node_field[node];
     T ke = 1;
     if constexpr (MODEL == AGX_MODEL_HEAT_POTENTIAL) ke = elem_field ? (T)elem_field[e] : T(1);
+    // Lame parameters (models.py:955-956) formed in float64 and then rounded: in float32,
+    // 1 - 2 nu loses four digits at nu = 0.4999
+    T lam = 0, mu = 0;
+    if constexpr (MODEL == AGX_MODEL_NEO_HOOKE) {
+      const double E = mp.p[0], nu = mp.p[1];
+      lam = (T)(E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)));
+      mu = (T)(E / (2.0 * (1.0 + nu)));
+    }
 
     double Ra[NDOF];
 #pragma unroll
@@ -271,9 +279,6 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
             for (int j = 0; j < SDIM; ++j) F[i][j] = group_sum<NEN>(ua[i] * ga[j]) + (i == j ? T(1) : T(0));
           T Fi[SDIM][SDIM];
           const T Jdet = inverse<T, SDIM>(F, Fi);
-          const T E = (T)mp.p[0], nu = (T)mp.p[1];
-          const T lam = E * nu / ((T(1) + nu) * (T(1) - T(2) * nu));
-          const T mu = E / (T(2) * (T(1) + nu));
           const T c = lam * T(0.5) * (Jdet * Jdet - T(1)) - mu;
           T ha[SDIM];
 #pragma unroll
@@ -381,6 +386,7 @@ void launch_element(agx_context* ctx, agx_element_set& s, const double* dofs, do
   element_kernel<ET, MODEL, T, DO_R, DO_K><<<grid, AGX_BLOCK, 0, ctx->stream>>>(
       s.n_elem, s.d_conn, s.d_epos, ctx->d_coords, dofs, s.d_elem_field, s.d_node_field, ctx->d_dmask_node, mp, R,
       vals);
+  ctx->n_launches += 1;
 }
 
 // dispatch on (element type, model) for one pass kind
@@ -423,18 +429,27 @@ int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, in
   for (auto& s : ctx->sets) {
     int rc = AGX_OK;
     if (tangent_dtype == AGX_F64) {
+      agx_prof_scope ps(ctx, AGX_PROF_TANGENT);
       rc = residual ? dispatch<double, true, true>(ctx, s, dofs, residual, ctx->d_vals64)
                     : dispatch<double, false, true>(ctx, s, dofs, nullptr, ctx->d_vals64);
     } else if (tangent_dtype == AGX_F32) {
       // float32 tangent pass; the float64 residual is a separate float64 pass
-      rc = dispatch<float, false, true>(ctx, s, dofs, nullptr, ctx->d_vals32);
-      if (rc == AGX_OK && residual) rc = dispatch<double, true, false>(ctx, s, dofs, residual, (double*)nullptr);
+      {
+        agx_prof_scope ps(ctx, AGX_PROF_TANGENT);
+        rc = dispatch<float, false, true>(ctx, s, dofs, nullptr, ctx->d_vals32);
+      }
+      if (rc == AGX_OK && residual) {
+        agx_prof_scope ps(ctx, AGX_PROF_RESIDUAL);
+        rc = dispatch<double, true, false>(ctx, s, dofs, residual, (double*)nullptr);
+      }
     } else if (residual) {
+      agx_prof_scope ps(ctx, AGX_PROF_RESIDUAL);
       rc = dispatch<double, true, false>(ctx, s, dofs, residual, (double*)nullptr);
     }
     if (rc != AGX_OK) return rc;
     AGX_CHECK_LAUNCH(ctx);
   }
+  if (tangent_dtype >= 0) ctx->n_launches += (ctx->n_dir > 0 ? 2 : 1);  // Dirichlet diagonal + inverse diagonal
   if (tangent_dtype == AGX_F64) {
     inverse_diagonal<double><<<agx_grid(ctx, ctx->n_dofs), AGX_BLOCK, 0, ctx->stream>>>(
         ctx->n_dofs, ctx->ndof, ctx->d_diagpos, ctx->d_vals64, ctx->d_dinv64);

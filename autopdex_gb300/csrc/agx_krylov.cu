@@ -141,7 +141,10 @@ spmv_dot_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_
   double tot[1];
   if (reduce_last_block<1>(acc, partials, counter, tot) && threadIdx.x == 0) {
     sc->pq = tot[0];
-    if (bad(tot[0]) || tot[0] < 0.0) {
+    // Only a zero or non-finite (p, Ap) is a breakdown: the tangents of clockwise-numbered
+    // quads (mesher.py:88-94 numbers quads clockwise, so det J < 0) are negative definite,
+    // and CG with a Jacobi preconditioner of the same sign runs as on (-K, -D).
+    if (bad(tot[0])) {
       sc->converged = 2;
     } else {
       sc->alpha = sc->rz / tot[0];
@@ -281,7 +284,7 @@ fcg_direction_dots(int64_t n, const T* __restrict__ r, const T* __restrict__ z, 
   if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
     sc->rz = tot[0];
     sc->beta = sc->iters == 0 ? 0.0 : -tot[1] / sc->pq;
-    if (!isfinite(tot[0]) || tot[0] <= 0.0) sc->converged = 2;
+    if (bad(tot[0])) sc->converged = 2;
   }
 }
 
@@ -488,6 +491,7 @@ constexpr int tpr_for(int dim) {
 // launch helpers dispatching on the block size
 template <typename T>
 void launch_spmv_dot(agx_context* ctx, const T* vals, const T* p, T* q) {
+  agx_prof_scope ps(ctx, AGX_PROF_SPMV);
   const int64_t nr = ctx->n_nodes;
   const int g = ctx->red_blocks;
   auto* sc = ctx->d_scal;
@@ -520,6 +524,7 @@ void launch_bicg_spmvs(agx_context* ctx, int which, double* a, double* b, double
 }
 
 void launch_bicg_spmv(agx_context* ctx, int which, double* a, double* b, double* c) {
+  agx_prof_scope ps(ctx, AGX_PROF_SPMV);
   if (ctx->ndof == 1) {
     if (ctx->dim == 3) launch_bicg_spmvs<1, 8>(ctx, which, a, b, c);
     else launch_bicg_spmvs<1, 4>(ctx, which, a, b, c);
@@ -534,6 +539,11 @@ int read_scalars(agx_context* ctx) {
   AGX_CUDA(ctx, cudaMemcpyAsync(ctx->h_scal, ctx->d_scal, sizeof(agx_krylov_scalars), cudaMemcpyDeviceToHost,
                                 ctx->stream));
   AGX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (ctx->debug) {
+    const agx_krylov_scalars& s = *ctx->h_scal;
+    fprintf(stderr, "[agx] it=%d conv=%d rz=%.6e rr=%.6e pq=%.6e alpha=%.6e beta=%.6e rr_stop=%.6e\n", s.iters,
+            s.converged, s.rz, s.rr, s.pq, s.alpha, s.beta, s.rr_stop);
+  }
   return AGX_OK;
 }
 
@@ -563,12 +573,14 @@ int agx_spmv_impl(agx_context* ctx, int dtype, const void* x, void* y) {
 }
 
 void agx_launch_set_dirichlet(agx_context* ctx, double* dofs, const double* values) {
+  ctx->n_launches += ctx->n_dir > 0 ? 1 : 0;
   if (ctx->n_dir > 0)
     set_dirichlet_kernel<<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir, ctx->d_dir_dofs, dofs,
                                                                                   values);
 }
 
 void agx_launch_newton_update(agx_context* ctx, double* dofs, const double* dx, const double* values, double damping) {
+  ctx->n_launches += 1;
   newton_update_kernel<<<agx_grid(ctx, ctx->n_dofs), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dofs, dofs, dx, values,
                                                                                   ctx->d_dmask_dof, damping);
 }
@@ -578,11 +590,13 @@ void agx_launch_negate_free(agx_context* ctx, const double* R, double* b) {
 }
 
 void agx_launch_masked_scale(agx_context* ctx, const double* src, double* dst, double s) {
+  ctx->n_launches += 1;
   masked_scale_kernel<<<agx_grid(ctx, ctx->n_dofs), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dofs, src, dst,
                                                                                 ctx->d_dmask_dof, s);
 }
 
 int agx_residual_norm(agx_context* ctx, const double* R, double* norm2, double* nonfinite) {
+  ctx->n_launches += 1;
   masked_norm_kernel<<<ctx->red_blocks, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dofs, R, ctx->d_dmask_dof, ctx->d_norm,
                                                                    ctx->d_partials, ctx->d_counter);
   AGX_CHECK_LAUNCH(ctx);
@@ -609,13 +623,17 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
   norm_init_kernel<<<g, AGX_BLOCK, 0, ctx->stream>>>(n, rhs, sc, ctx->d_partials, ctx->d_counter, opts->rtol,
                                                     opts->atol);
   AGX_CHECK_LAUNCH(ctx);
+  ctx->n_launches += 2;  // norm + method initialisation
   int it_done = 0;
   if (method == AGX_PCG) {
     pcg_init_kernel<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, rhs, ctx->d_dinv64, x, ctx->d_r, ctx->d_z, ctx->d_p,
                                                              sc, ctx->d_partials, ctx->d_counter, 0, 1);
     while (true) {
-      for (int k = 0, kn = std::min(every, maxiter - it_done); k < kn; ++k) {
+      const int kn = std::min(every, maxiter - it_done);
+      ctx->n_launches += 3 * kn;
+      for (int k = 0; k < kn; ++k) {
         launch_spmv_dot<double>(ctx, ctx->d_vals64, ctx->d_p, ctx->d_q);
+        agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
         pcg_update_kernel<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, x, ctx->d_r, ctx->d_z, ctx->d_p, ctx->d_q,
                                                                    ctx->d_dinv64, sc, ctx->d_partials, ctx->d_counter);
         pcg_direction_kernel<double><<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_p, ctx->d_z, sc);
@@ -641,15 +659,22 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
       AGX_CUDA(ctx, cudaMemcpyAsync(ctx->f_p, ctx->f_z, sizeof(float) * n, cudaMemcpyDeviceToDevice, ctx->stream));
     }
     while (true) {
-      for (int k = 0, kn = std::min(every, maxiter - it_done); k < kn; ++k) {
+      const int kn = std::min(every, maxiter - it_done);
+      ctx->n_launches += (flexible ? 5 : 3) * kn;
+      for (int k = 0; k < kn; ++k) {
         launch_spmv_dot<float>(ctx, ctx->d_vals32, ctx->f_p, ctx->f_q);
         if (!flexible) {
+          agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
           pcg_update_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, ctx->f_r, ctx->f_z, ctx->f_p,
                                                                     ctx->f_q, ctx->d_dinv32, sc, ctx->d_partials,
                                                                     ctx->d_counter);
         } else {
-          fcg_update_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, ctx->f_r, ctx->f_p, ctx->f_q, sc,
-                                                                    ctx->d_partials, ctx->d_counter);
+          {
+            agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
+            fcg_update_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, ctx->f_r, ctx->f_p, ctx->f_q, sc,
+                                                                      ctx->d_partials, ctx->d_counter);
+          }
+          agx_prof_scope pp(ctx, AGX_PROF_PRECOND);
           if (ctx->precond(ctx->precond_user, ctx->f_r, ctx->f_z, n, ctx->stream) != 0)
             return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");
           zero_prescribed<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir,
@@ -657,6 +682,7 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
           fcg_direction_dots<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_r, ctx->f_z, ctx->f_q, sc,
                                                                      ctx->d_partials, ctx->d_counter);
         }
+        agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
         pcg_direction_kernel<float><<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_p, ctx->f_z, sc);
       }
       AGX_CHECK_LAUNCH(ctx);
@@ -666,10 +692,14 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
       if (ctx->h_scal->converged || it_done >= maxiter) break;
     }
     to_double_scaled<float><<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, x, sc, 1);
+    ctx->n_launches += 1;
   } else if (method == AGX_BICGSTAB) {
     bicg_init<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, rhs, x, ctx->d_r, ctx->d_rhat, ctx->d_p, ctx->d_v, sc);
     while (true) {
-      for (int k = 0, kn = std::min(every, maxiter - it_done); k < kn; ++k) {
+      const int kn = std::min(every, maxiter - it_done);
+      ctx->n_launches += 5 * kn;
+      for (int k = 0; k < kn; ++k) {
+        agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
         bicg_p_kernel<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_p, ctx->d_r, ctx->d_v, ctx->d_q, ctx->d_dinv64, sc);
         launch_bicg_spmv(ctx, 0, ctx->d_q, ctx->d_v, ctx->d_rhat);  // v = A y, y in d_q
         bicg_s_kernel<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_r, ctx->d_v, ctx->d_s, ctx->d_z, ctx->d_dinv64, sc);

@@ -1,0 +1,360 @@
+"""Benchmark of the GB300 solve backend on the 3-D neo-Hooke cube (config 2).
+
+Workload: 64^3 Q1 bricks (274,625 nodes, 823,875 DOFs), E = 1, nu = 0.3, x = 0 clamped,
+u_x prescribed on x = 1.  One step = one load-step solve (load step 1 of 10, u_x = 0.03)
+from the undeformed state to a float64 Newton residual of 1e-10 times the first one,
+i.e. one ``solver.solver`` call.  Metric: time to the 1e-10 relative residual (s, lower is
+better) of the mixed-precision path (float32 tangent and Jacobi-PCG inside the float64
+Newton/refinement loop); the plain float64 Jacobi-PCG path is timed beside it.  The
+64^3 problem (~0.3 GB of float32 matrix, 0.6 GB float64) exceeds the 129 MB L2, so no
+flush is needed between steps.
+
+--impl reference times the CPU oracle (float64 NumPy/SciPy/torch.func restatement of the
+reference path) on a bounded sample of the same workload and scales it to one load step.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def _peaks():
+    try:
+        with open(PEAKS) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", "0"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        try:
+            rows = [l.split(",") for l in open(self.path).read().strip().splitlines() if l.strip()]
+            sm = [float(r[1]) for r in rows]
+            mx = max(float(r[2]) for r in rows)
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if "Active" in v and "Not" not in v})
+            return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows)}
+        except Exception as e:  # noqa: BLE001
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "error": str(e)}
+
+
+def _solve_once(w, static, newton_rtol, x0=None, profile_ctx=None):
+    from autopdex_gb300 import solver
+    st = dict(w.settings)
+    st = w.steps[0](st)
+    sol, info = solver.solver(w.dofs if x0 is None else x0, st, static, newton_tol=0.0, newton_rtol=newton_rtol,
+                              maxiter=30)
+    return sol, info
+
+
+def gpu_arm(args):
+    import torch
+    import ctypes as C
+    from autopdex_gb300 import configs, solver, _native as N
+    from autopdex_gb300._problem import get_problem
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    n = args.size
+    w = configs.neo_hooke_cube(n=n, n_steps=10)
+    mixed = dict(w.static_settings, precision="mixed", solver="pcg")
+    plain = dict(w.static_settings, precision="float64", solver="pcg")
+    rtol = 1e-10
+    kw = dict(krylov_tol=args.krylov_tol)
+
+    # device-resident inputs: dofs and prescribed values already on the GPU
+    st = w.steps[0](dict(w.settings))
+    prob = get_problem(w.dofs, st, mixed)
+    dev = prob.device
+    x0_host = np.zeros(w.n_dofs)
+    g_dev = torch.as_tensor(np.asarray(st["dirichlet conditions"], dtype=np.float64).reshape(-1), device=dev)
+    st_dev = dict(st)
+    st_dev["dirichlet conditions"] = g_dev.reshape(-1, 3)
+    x0_dev = torch.zeros((w.n_dofs // 3, 3), dtype=torch.float64, device=dev)
+
+    def run_dev(static):
+        return solver.solver(x0_dev, st_dev, static, newton_tol=0.0, newton_rtol=rtol, maxiter=30, **kw)
+
+    for _ in range(args.warmup):
+        run_dev(mixed)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    lib = N.load()
+    l0 = C.c_int64()
+    prob._call("agx_launch_count", C.byref(l0))
+    prob._call("agx_profile", 1)
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    infos = []
+    with Clocks() as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            sol, info = run_dev(mixed)
+            infos.append((info, solver.last_info.krylov_iterations))
+        e1.record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t_ms = e0.elapsed_time(e1)
+    ms = (C.c_double * N.AGX_PROF_CATEGORIES)()
+    cnt = (C.c_int64 * N.AGX_PROF_CATEGORIES)()
+    prob._call("agx_profile_read", ms, cnt)
+    prob._call("agx_profile", 0)
+    l1 = C.c_int64()
+    prob._call("agx_launch_count", C.byref(l1))
+    if dist:
+        t = torch.tensor([t_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_ms = float(t.item())
+    per_step_s = t_ms / 1e3 / args.steps
+
+    # verify the solution of the last timed step: float64 residual ratio
+    res0 = solver.last_info.res0
+    res_end = solver.last_info.res_norm
+
+    # plain float64 Jacobi-PCG on the same step (reported beside the headline)
+    run_dev(plain)
+    torch.cuda.synchronize()
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    prob_plain = get_problem(x0_dev, st_dev, plain)
+    e2.record(stream)
+    sol_p, info_p = run_dev(plain)
+    e3.record(stream)
+    torch.cuda.synchronize()
+    plain_s = e2.elapsed_time(e3) / 1e3
+    plain_kry = solver.last_info.krylov_iterations
+
+    # end to end through the public API with host buffers (H2D of the inputs, D2H of the result)
+    def run_host():
+        s = dict(st)
+        return solver.solver(x0_host.reshape(-1, 3), s, mixed, newton_tol=0.0, newton_rtol=rtol, maxiter=30, **kw)
+    run_host()
+    torch.cuda.synchronize()
+    k_e2e = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(k_e2e):
+        out_host, _ = run_host()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / k_e2e
+
+    # roofline of the dominant kernel (largest category)
+    cats = {"tangent_assembly": N.AGX_PROF_TANGENT, "residual_assembly": N.AGX_PROF_RESIDUAL,
+            "spmv": N.AGX_PROF_SPMV, "krylov_vector": N.AGX_PROF_VECTOR}
+    shares = {k: ms[v] for k, v in cats.items()}
+    launches = {k: int(cnt[v]) for k, v in cats.items()}
+    b = 3
+    nnzb = prob.nnzb
+    n_nodes = w.n_dofs // 3
+    spmv_bytes = nnzb * (b * b * 4 + 4) + (n_nodes + 1) * 4 + 2 * w.n_dofs * 4
+    spmv_avg_ms = ms[N.AGX_PROF_SPMV] / max(1, cnt[N.AGX_PROF_SPMV])
+    peak, peak_kind = _peaks()
+    achieved = spmv_bytes / (spmv_avg_ms * 1e-3) / 1e9
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tr_path):
+        try:
+            traffic = json.load(open(tr_path)).get("spmv_f32_bsr3_64cube_bytes_per_launch")
+        except Exception:
+            traffic = None
+    # element tangent pass: algorithmic bytes (coords, dofs, conn, scatter map, float32 values)
+    n_e = n ** 3
+    asm_bytes = n_nodes * 3 * 8 + w.n_dofs * 8 + n_e * 8 * 4 + n_e * 64 * 4 + nnzb * 9 * 4
+    asm_avg_ms = ms[N.AGX_PROF_TANGENT] / max(1, cnt[N.AGX_PROF_TANGENT])
+
+    line = {
+        "metric": "time_to_1e-10_relative_fp64_residual (config 2: 64^3 neo-Hooke, load step 1 of 10)",
+        "value": per_step_s,
+        "unit": "s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": per_step_s * 1e3,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 tangent/SpMV + f64 residual",
+        "data": "synthetic (structured mesh of the config; no dataset)",
+        "config": {"workload": f"neo_hooke_cube_{n}^3_hex8_load_step_1", "n_dofs": w.n_dofs, "nnz": nnzb * 9,
+                   "newton_rtol": rtol, "krylov": "jacobi-pcg f32 (rtol %.0e)" % args.krylov_tol,
+                   "l2": "working set > 129 MB L2 (no flush needed)", "parallelism": "replicas" if world > 1 else "1 gpu"},
+        "plain_fp64_pcg_s": plain_s,
+        "speedup_mixed_vs_plain_fp64": plain_s / per_step_s,
+        "newton_iterations": int(infos[-1][0][0]),
+        "krylov_iterations_mixed": int(infos[-1][1]),
+        "krylov_iterations_plain_fp64": int(plain_kry),
+        "final_residual_ratio": res_end / res0 if res0 else None,
+        "kernel_ms_per_step": {k: v / args.steps for k, v in shares.items()},
+        "kernel_launches_per_step": {k: v / args.steps for k, v in launches.items()},
+        "roofline": {"bound": "hbm", "kernel": "spmv_dot_kernel<float,3,8> (BSR 3x3 SpMV + dot)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": traffic, "algorithmic_bytes": spmv_bytes,
+                     "avg_launch_ms": spmv_avg_ms},
+        "assembly": {"kernel": "element_kernel<HEX8,NEO_HOOKE,float> (tangent pass)",
+                     "algorithmic_bytes": asm_bytes, "avg_launch_ms": asm_avg_ms,
+                     "achieved_gbs": asm_bytes / (asm_avg_ms * 1e-3) / 1e9 if asm_avg_ms else None},
+        "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 2 * w.n_dofs * 8,
+                "d2h_bytes_per_step": w.n_dofs * 8},
+        "gpu_launches": int(l1.value - l0.value),
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(n, infos[-1][0][0], int(plain_kry), budget_s=args.cpu_budget)
+    if dist:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def cpu_baseline(n, newton_iters, cg_iters, budget_s=20.0):
+    """CPU oracle on a bounded sample of the workload, scaled to one load step.
+
+    Sample: (a) float64 AD element residual+tangent (oracle.elements, torch.func) on 512
+    elements of the mesh -> cost per element; (b) SciPy Jacobi-CG iterations on the
+    assembled 16^3 cube matrix -> cost per CG iteration per stored entry.  Scaled with the
+    Newton and CG iteration counts of the float64 GPU path on the full 64^3 problem:
+    t = newton_iters * (2 n_e t_elem) + cg_iters * t_iter(nnz_64 / nnz_16)."""
+    import torch
+    import scipy.sparse.linalg as sla
+    from autopdex_gb300 import configs
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle import elements as el, newton
+
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    w = configs.neo_hooke_cube(n=8, n_steps=10)
+    fun = el.hyperelastic_element(3, 8, 2, "3d")
+    conn = w.raw["conns"][0][:512]
+    xI = torch.as_tensor(w.raw["coords"][conn])
+    uI = torch.zeros((conn.shape[0], 8, 3), dtype=torch.float64) + 1e-3
+    p = torch.tensor([[1.0, 0.3]] * conn.shape[0], dtype=torch.float64)
+    el.batched(fun, uI[:8], xI[:8], p[:8])
+    t0 = time.perf_counter()
+    el.batched(fun, uI, xI, p)
+    t_elem = (time.perf_counter() - t0) / conn.shape[0]
+
+    from oracle_setup import oracle_problem
+    w16 = configs.neo_hooke_cube(n=16, n_steps=10)
+    prob = oracle_problem(w16)
+    st = w16.steps[0](dict(w16.settings))
+    prob.values = np.asarray(st["dirichlet conditions"]).reshape(-1)
+    _, coo = newton.assemble(prob.sets, np.zeros(prob.n_dofs), prob.coords, st, prob.n_dofs)
+    free = ~prob.dirichlet
+    A = newton.scipy_assembling(coo, prob.n_dofs, free)
+    b = np.random.default_rng(0).standard_normal(A.shape[0])
+    d = A.diagonal()
+    M = sla.LinearOperator(A.shape, matvec=lambda v: v / d)
+    iters = 200
+    t0 = time.perf_counter()
+    sla.cg(A, b, rtol=1e-30, maxiter=iters, M=M)
+    t_iter16 = (time.perf_counter() - t0) / iters
+    nnz64 = 81 * 9 * (n + 1) ** 3  # upper bound of stored entries of the 64^3 matrix (27 blocks of 9 per row)
+    t_iter = t_iter16 * nnz64 / max(1, A.nnz)
+    n_e = n ** 3
+    est = newton_iters * 2 * n_e * t_elem + cg_iters * t_iter
+    return {"value": est, "unit": "s", "cores": threads, "kind": "port",
+            "sample": (f"float64 AD element routine on 512 elements ({t_elem * 1e6:.1f} us/element) and "
+                       f"{iters} SciPy Jacobi-CG iterations on the 16^3 cube ({t_iter16 * 1e3:.2f} ms/iteration, "
+                       f"scaled by stored entries to 64^3); combined with the float64 GPU path's "
+                       f"{newton_iters} Newton and {cg_iters} CG iterations")}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    n = args.size
+    # iteration counts of the float64 path on the 64^3 load step, measured on the GPU arm
+    newton_iters, cg_iters = args.ref_newton_iters, args.ref_cg_iters
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(n, newton_iters, cg_iters)
+    t0 = time.perf_counter()
+    last = None
+    for _ in range(args.steps):
+        last = cpu_baseline(n, newton_iters, cg_iters)
+        vals.append(last["value"])
+    wall = time.perf_counter() - t0
+    v = float(np.median(vals))
+    line = {"impl": "reference",
+            "metric": "time_to_1e-10_relative_fp64_residual (config 2: 64^3 neo-Hooke, load step 1 of 10)",
+            "value": v, "unit": "s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"neo_hooke_cube_{n}^3_hex8_load_step_1"},
+            "cpu_baseline": {"value": v, "unit": "s", "cores": last["cores"], "kind": last["kind"],
+                             "sample": last["sample"]},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=64)
+    ap.add_argument("--krylov-tol", type=float, default=1e-4)
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-newton-iters", type=int, default=4)
+    ap.add_argument("--ref-cg-iters", type=int, default=3000)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -169,6 +169,20 @@ int agx_newton(agx_context* ctx, double* dofs, const double* dirichlet_values,
                const agx_newton_opts* opts, agx_newton_info* info);
 /* Registers the preconditioner used by AGX_FCG_MIXED (NULL restores Jacobi). */
 int agx_set_preconditioner(agx_context* ctx, agx_precond_fn fn, void* user);
+/* Kernel timing.  While enabled, the library brackets its kernel launches with CUDA events
+   on its stream and accumulates the elapsed time per category; agx_profile_read
+   synchronizes the stream, returns totals (ms) and launch counts, and resets them. */
+#define AGX_PROF_TANGENT 0   /* element passes that assemble a tangent (with the residual
+                                when fused) */
+#define AGX_PROF_RESIDUAL 1  /* float64 residual-only element passes */
+#define AGX_PROF_SPMV 2      /* sparse products of the Krylov iterations */
+#define AGX_PROF_VECTOR 3    /* Krylov vector updates with their reductions */
+#define AGX_PROF_PRECOND 4   /* preconditioner applications */
+#define AGX_PROF_CATEGORIES 8
+int agx_profile(agx_context* ctx, int enable);
+int agx_profile_read(agx_context* ctx, double* ms, int64_t* launches);
+/* Number of kernels this context has launched since it was created. */
+int agx_launch_count(const agx_context* ctx, int64_t* launches);
 /* Sizes for the host layer: n_dofs, nnzb, ndof. */
 int agx_get_sizes(const agx_context* ctx, int64_t* n_dofs, int64_t* nnzb, int* ndof);
 

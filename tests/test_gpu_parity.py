@@ -135,17 +135,20 @@ def test_neo_hooke_cube_load_steps_match_oracle(precision):
     assert np.abs(_flat(u_gpu) - u_or).max() <= 1e-8 * max(1.0, np.abs(u_or).max())
 
 
-def test_cook_load_steps_match_oracle():
+@pytest.mark.parametrize("precision", ["float64", "mixed"])
+def test_cook_load_steps_match_oracle(precision):
+    """Nearly incompressible (nu = 0.4999): the float64 residual floor is ~2e-9 here (the
+    oracle stalls there too), so the reference's default tolerance 1e-8 is used."""
     from autopdex_gb300 import solver
-    w = configs.cook_membrane(n=6, n_steps=2)
+    w = configs.cook_membrane(n=6, n_steps=2, precision=precision)
     prob = oracle_problem(w)
     u_gpu = w.dofs
     u_or = np.zeros(w.n_dofs)
     for step in w.steps:
         w.settings = step(w.settings)
-        u_gpu, (it, res, div) = solver.solver(u_gpu, w.settings, w.static_settings, newton_tol=1e-9)
-        assert not div
-        u_or, info, _ = newton.damped_newton(prob, u_or, oracle_settings(w), 1e-9)
+        u_gpu, (it, res, div) = solver.solver(u_gpu, w.settings, w.static_settings, newton_tol=1e-8)
+        assert not div and res <= 1e-8
+        u_or, info, _ = newton.damped_newton(prob, u_or, oracle_settings(w), 1e-8)
     assert np.abs(_flat(u_gpu) - u_or).max() <= 1e-8 * max(1.0, np.abs(u_or).max())
 
 
