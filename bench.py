@@ -2,8 +2,10 @@
 
 Workload: 64^3 Q1 bricks (274,625 nodes, 823,875 DOFs), E = 1, nu = 0.3, x = 0 clamped,
 u_x prescribed on x = 1.  One step = one load-step solve (load step 1 of 10, u_x = 0.03)
-from the undeformed state to a float64 Newton residual of 1e-10 times the first one,
-i.e. one ``solver.solver`` call.  Metric: time to the 1e-10 relative residual (s, lower is
+to a float64 Newton residual of 1e-10 times the first one, i.e. one ``solver.solver``
+call, started from the linear lifting u_x = 0.03 x of the prescribed values (from u = 0 the
+first element layer is stretched threefold at h = 1/64 and undamped Newton, the
+reference's algorithm, diverges).  Metric: time to the 1e-10 relative residual (s, lower is
 better) of the mixed-precision path (float32 tangent and Jacobi-PCG inside the float64
 Newton/refinement loop); the plain float64 Jacobi-PCG path is timed beside it.  The
 64^3 problem (~0.3 GB of float32 matrix, 0.6 GB float64) exceeds the 129 MB L2, so no
@@ -111,14 +113,17 @@ def gpu_arm(args):
     st = w.steps[0](dict(w.settings))
     prob = get_problem(w.dofs, st, mixed)
     dev = prob.device
-    x0_host = np.zeros(w.n_dofs)
+    x0_host = np.zeros((w.n_dofs // 3, 3))
+    x0_host[:, 0] = w.raw["stretch"] / w.raw["n_steps"] * w.raw["coords"][:, 0]
+    x0_host = x0_host.reshape(-1)
     g_dev = torch.as_tensor(np.asarray(st["dirichlet conditions"], dtype=np.float64).reshape(-1), device=dev)
     st_dev = dict(st)
     st_dev["dirichlet conditions"] = g_dev.reshape(-1, 3)
-    x0_dev = torch.zeros((w.n_dofs // 3, 3), dtype=torch.float64, device=dev)
+    x0_dev = torch.as_tensor(x0_host.reshape(-1, 3), device=dev)
 
-    def run_dev(static):
-        return solver.solver(x0_dev, st_dev, static, newton_tol=0.0, newton_rtol=rtol, maxiter=30, **kw)
+    def run_dev(static, **over):
+        k = dict(kw, **over)
+        return solver.solver(x0_dev, st_dev, static, newton_tol=0.0, newton_rtol=rtol, maxiter=30, **k)
 
     for _ in range(args.warmup):
         run_dev(mixed)
@@ -160,31 +165,38 @@ def gpu_arm(args):
     res0 = solver.last_info.res0
     res_end = solver.last_info.res_norm
 
-    # plain float64 Jacobi-PCG on the same step (reported beside the headline)
-    run_dev(plain)
-    torch.cuda.synchronize()
-    e2 = torch.cuda.Event(enable_timing=True)
-    e3 = torch.cuda.Event(enable_timing=True)
-    prob_plain = get_problem(x0_dev, st_dev, plain)
-    e2.record(stream)
-    sol_p, info_p = run_dev(plain)
-    e3.record(stream)
-    torch.cuda.synchronize()
-    plain_s = e2.elapsed_time(e3) / 1e3
-    plain_kry = solver.last_info.krylov_iterations
+    # plain float64 Jacobi-PCG on the same step, beside the headline: (a) with the same inner
+    # tolerance schedule as the mixed path, (b) with inner solves to 1e-11 (direct-solve accuracy)
+    def timed(static, **over):
+        run_dev(static, **over)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        _, inf = run_dev(static, **over)
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3, inf, solver.last_info.krylov_iterations
+    if args.only_mixed:
+        plain_s, info_p, plain_kry = float("nan"), (0, 0.0, False), 0
+        tight_s, info_t, tight_kry = float("nan"), (0, 0.0, False), 0
+    else:
+        plain_s, info_p, plain_kry = timed(plain)
+        tight_s, info_t, tight_kry = timed(plain, krylov_tol=1e-11)
 
     # end to end through the public API with host buffers (H2D of the inputs, D2H of the result)
     def run_host():
         s = dict(st)
         return solver.solver(x0_host.reshape(-1, 3), s, mixed, newton_tol=0.0, newton_rtol=rtol, maxiter=30, **kw)
-    run_host()
+    if not args.only_mixed:
+        run_host()
     torch.cuda.synchronize()
-    k_e2e = max(1, min(args.steps, 3))
+    k_e2e = 0 if args.only_mixed else max(1, min(args.steps, 3))
     t0 = time.perf_counter()
     for _ in range(k_e2e):
         out_host, _ = run_host()
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / k_e2e
+    e2e_s = (time.perf_counter() - t0) / max(1, k_e2e)
 
     # roofline of the dominant kernel (largest category)
     cats = {"tangent_assembly": N.AGX_PROF_TANGENT, "residual_assembly": N.AGX_PROF_RESIDUAL,
@@ -228,9 +240,14 @@ def gpu_arm(args):
                    "l2": "working set > 129 MB L2 (no flush needed)", "parallelism": "replicas" if world > 1 else "1 gpu"},
         "plain_fp64_pcg_s": plain_s,
         "speedup_mixed_vs_plain_fp64": plain_s / per_step_s,
+        "plain_fp64_pcg_tight_s": tight_s,
         "newton_iterations": int(infos[-1][0][0]),
+        "newton_iterations_plain_fp64": int(info_p[0]),
+        "newton_iterations_plain_fp64_tight": int(info_t[0]),
         "krylov_iterations_mixed": int(infos[-1][1]),
         "krylov_iterations_plain_fp64": int(plain_kry),
+        "krylov_iterations_plain_fp64_tight": int(tight_kry),
+        "converged": bool(not infos[-1][0][2]) and (res_end <= rtol * res0 * 1.0000001),
         "final_residual_ratio": res_end / res0 if res0 else None,
         "kernel_ms_per_step": {k: v / args.steps for k, v in shares.items()},
         "kernel_launches_per_step": {k: v / args.steps for k, v in launches.items()},
@@ -246,8 +263,8 @@ def gpu_arm(args):
         "gpu_launches": int(l1.value - l0.value),
         "clocks": clk.summary(),
     }
-    if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(n, infos[-1][0][0], int(plain_kry), budget_s=args.cpu_budget)
+    if rank == 0 and not args.no_cpu_baseline and not args.only_mixed:
+        line["cpu_baseline"] = cpu_baseline(n, int(info_t[0]), int(tight_kry), budget_s=args.cpu_budget)
     if dist:
         dist.destroy_process_group()
     if rank == 0:
@@ -259,9 +276,9 @@ def cpu_baseline(n, newton_iters, cg_iters, budget_s=20.0):
 
     Sample: (a) float64 AD element residual+tangent (oracle.elements, torch.func) on 512
     elements of the mesh -> cost per element; (b) SciPy Jacobi-CG iterations on the
-    assembled 16^3 cube matrix -> cost per CG iteration per stored entry.  Scaled with the
+    assembled 12^3 cube matrix -> cost per CG iteration per stored entry.  Scaled with the
     Newton and CG iteration counts of the float64 GPU path on the full 64^3 problem:
-    t = newton_iters * (2 n_e t_elem) + cg_iters * t_iter(nnz_64 / nnz_16)."""
+    t = newton_iters * (2 n_e t_elem) + cg_iters * t_iter(nnz_64 / nnz_12)."""
     import torch
     import scipy.sparse.linalg as sla
     from autopdex_gb300 import configs
@@ -282,7 +299,7 @@ def cpu_baseline(n, newton_iters, cg_iters, budget_s=20.0):
     t_elem = (time.perf_counter() - t0) / conn.shape[0]
 
     from oracle_setup import oracle_problem
-    w16 = configs.neo_hooke_cube(n=16, n_steps=10)
+    w16 = configs.neo_hooke_cube(n=12, n_steps=10)
     prob = oracle_problem(w16)
     st = w16.steps[0](dict(w16.settings))
     prob.values = np.asarray(st["dirichlet conditions"]).reshape(-1)
@@ -302,7 +319,7 @@ def cpu_baseline(n, newton_iters, cg_iters, budget_s=20.0):
     est = newton_iters * 2 * n_e * t_elem + cg_iters * t_iter
     return {"value": est, "unit": "s", "cores": threads, "kind": "port",
             "sample": (f"float64 AD element routine on 512 elements ({t_elem * 1e6:.1f} us/element) and "
-                       f"{iters} SciPy Jacobi-CG iterations on the 16^3 cube ({t_iter16 * 1e3:.2f} ms/iteration, "
+                       f"{iters} SciPy Jacobi-CG iterations on the 12^3 cube ({t_iter16 * 1e3:.2f} ms/iteration, "
                        f"scaled by stored entries to 64^3); combined with the float64 GPU path's "
                        f"{newton_iters} Newton and {cg_iters} CG iterations")}
 
@@ -346,6 +363,7 @@ def main():
     ap.add_argument("--krylov-tol", type=float, default=1e-4)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only-mixed", action="store_true", help="time the mixed path only (profiling runs)")
     ap.add_argument("--ref-newton-iters", type=int, default=4)
     ap.add_argument("--ref-cg-iters", type=int, default=3000)
     args = ap.parse_args()
