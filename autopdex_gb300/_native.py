@@ -24,6 +24,7 @@ AGX_PCG, AGX_PCG_MIXED, AGX_BICGSTAB, AGX_FCG_MIXED = 0, 1, 2, 3
 
 AGX_PROF_TANGENT, AGX_PROF_RESIDUAL, AGX_PROF_SPMV, AGX_PROF_VECTOR, AGX_PROF_PRECOND = 0, 1, 2, 3, 4
 AGX_PROF_CATEGORIES = 8
+AGX_NOALLOC_MAX_DOFS = 262144
 
 PRECOND_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p)
 
@@ -71,6 +72,8 @@ _SIGNATURES = {
     "agx_profile": (C.c_int, [_P, C.c_int]),
     "agx_profile_read": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     "agx_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+"agx_pcg_noalloc": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int, _P, _P, C.c_double, C.c_int, _P,
+                                C.POINTER(SolveInfo), C.c_char_p, C.c_int]),
     "agx_get_sizes": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
 }
 

@@ -181,6 +181,21 @@ int agx_set_preconditioner(agx_context* ctx, agx_precond_fn fn, void* user);
 #define AGX_PROF_CATEGORIES 8
 int agx_profile(agx_context* ctx, int enable);
 int agx_profile_read(agx_context* ctx, double* ms, int64_t* launches);
+/* ---- allocation-free solve ----------------------------------------------------------
+   No counterpart in the reference.  Jacobi-PCG on a caller-provided float64 node-block
+   CSR matrix (rowptr n_nodes+1, col nnzb, vals nnzb*ndof*ndof; device pointers, e.g. from
+   agx_copy_matrix) for callers that cannot allocate device memory during a solve: solves
+   K x = rhs from x = 0 until ||r|| <= rtol ||rhs||, without any context.  Its work vectors
+   live in a fixed file-scope device array of AGX_NOALLOC_MAX_DOFS DOFs (10 MiB, reserved on
+   every device that loads the library until the process exits); larger systems are
+   rejected with AGX_ERR_ARG and a message in errbuf (nullable).  The first call on a device
+   looks the array's address up (call it once before any stream capture).  All calls share
+   the array: calls that overlap on the GPU race.  Returns AGX_OK, AGX_NOT_CONVERGED,
+   AGX_DIVERGED or a negative error. */
+#define AGX_NOALLOC_MAX_DOFS 262144
+int agx_pcg_noalloc(const int32_t* rowptr, const int32_t* col, const double* vals, int64_t n_nodes, int ndof,
+                    const double* rhs, double* x, double rtol, int maxiter, void* cuda_stream,
+                    agx_solve_info* info, char* errbuf, int errbuf_len);
 /* Number of kernels this context has launched since it was created. */
 int agx_launch_count(const agx_context* ctx, int64_t* launches);
 /* Sizes for the host layer: n_dofs, nnzb, ndof. */
