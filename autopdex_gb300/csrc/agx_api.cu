@@ -41,6 +41,7 @@ void free_device(agx_context* ctx) {
     release(s.d_conn);
     release(s.d_epos);
     release(s.d_elem_field);
+    release(s.d_geo);
   }
   release(ctx->d_dmask_node);
   release(ctx->d_dmask_dof);
@@ -212,8 +213,8 @@ int agx_finalize(agx_context* ctx) {
     if (int rc = alloc(ctx, p, n)) return rc;
   for (float** p : {&ctx->f_x, &ctx->f_r, &ctx->f_z, &ctx->f_p, &ctx->f_q, &ctx->f_rold, &ctx->d_dinv32})
     if (int rc = alloc(ctx, p, n)) return rc;
-  ctx->red_blocks = ctx->sm_count * 4;
-  if (int rc = alloc(ctx, &ctx->d_partials, (int64_t)ctx->red_blocks * 4)) return rc;
+  ctx->red_blocks = ctx->sm_count * 8;  // one resident wave of 256-thread blocks
+  if (int rc = alloc(ctx, &ctx->d_partials, (int64_t)ctx->red_blocks * 4)) return rc;  // up to 4 values per block
   if (int rc = alloc(ctx, &ctx->d_counter, 1)) return rc;
   if (int rc = alloc(ctx, &ctx->d_scal, 1)) return rc;
   if (int rc = alloc(ctx, &ctx->d_norm, 4)) return rc;
@@ -296,16 +297,18 @@ int agx_get_matrix(agx_context* ctx, int dtype, const int32_t** rowptr, const in
 int agx_copy_matrix(agx_context* ctx, int dtype, int32_t* rowptr, int32_t* col, void* vals) {
   if (!ctx || !ctx->pattern_ready) return agx_fail(ctx, AGX_ERR_STATE, "agx_finalize first");
   if (dtype != AGX_F64 && dtype != AGX_F32) return agx_fail(ctx, AGX_ERR_ARG, "dtype must be AGX_F64 or AGX_F32");
-  const size_t bs = (size_t)ctx->ndof * ctx->ndof;
   if (rowptr)
     AGX_CUDA(ctx, cudaMemcpyAsync(rowptr, ctx->d_rowptr, sizeof(int32_t) * (ctx->n_nodes + 1),
                                   cudaMemcpyDeviceToDevice, ctx->stream));
   if (col)
     AGX_CUDA(ctx, cudaMemcpyAsync(col, ctx->d_col, sizeof(int32_t) * ctx->nnzb, cudaMemcpyDeviceToDevice, ctx->stream));
   if (vals) {
-    const void* src = dtype == AGX_F64 ? (const void*)ctx->d_vals64 : (const void*)ctx->d_vals32;
-    const size_t es = dtype == AGX_F64 ? sizeof(double) : sizeof(float);
-    AGX_CUDA(ctx, cudaMemcpyAsync(vals, src, es * bs * ctx->nnzb, cudaMemcpyDeviceToDevice, ctx->stream));
+    // library layout: entry-major planes; caller layout: row-major ndof x ndof blocks
+    if (dtype == AGX_F64)
+      agx_launch_planes_to_blocks(ctx, ctx->d_vals64, (double*)vals);
+    else
+      agx_launch_planes_to_blocks(ctx, ctx->d_vals32, (float*)vals);
+    AGX_CHECK_LAUNCH(ctx);
   }
   AGX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return AGX_OK;

@@ -29,6 +29,7 @@ struct agx_element_set {
   double params[AGX_MAX_PARAMS] = {0};
   double* d_elem_field = nullptr;        // one value per element (owned)
   const double* d_node_field = nullptr;  // one value per DOF (caller-owned device pointer)
+  double* d_geo = nullptr;  // float64 geometry cache: per element, Gauss point and node, (g_a, w det J)
 };
 
 // Scalars of one Krylov solve, kept in device memory so that iterations need no host
@@ -53,6 +54,7 @@ struct agx_context {
   int device = 0;
   int sm_count = 152;
   int debug = 0;  // AGX_DEBUG=1 in the environment: print Krylov scalars at every host check
+  size_t geo_cache_limit = (size_t)16 << 30;  // largest float64 geometry cache per set (bytes)
 
   // nodes and DOFs
   int64_t n_nodes = 0;
@@ -137,6 +139,8 @@ void agx_launch_newton_update(agx_context* ctx, double* dofs, const double* dx, 
                               double damping);
 void agx_launch_negate_free(agx_context* ctx, const double* R, double* b);
 int agx_spmv_impl(agx_context* ctx, int dtype, const void* x, void* y);
+void agx_launch_planes_to_blocks(agx_context* ctx, const double* planes, double* blocks);
+void agx_launch_planes_to_blocks(agx_context* ctx, const float* planes, float* blocks);
 
 // Brackets the launches issued during its lifetime with events of category `cat`.
 struct agx_prof_scope {

@@ -25,6 +25,8 @@
 //     K_ab = rho_c/dt N_a N_b + k g_a.g_b + k'(T) N_b grad T . g_a   (non-symmetric)
 //   Neumann traction (models.py:744-780, :1818-1827)  R_a,i = -N_a t_i |dX/dxi|
 // all times the Gauss weight and det J; the oracle derives the same quantities by AD.
+#include <type_traits>
+
 #include "agx_common.cuh"
 
 namespace {
@@ -115,7 +117,7 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
                const double* __restrict__ coords, const double* __restrict__ dofs,
                const double* __restrict__ elem_field, const double* __restrict__ node_field,
                const uint8_t* __restrict__ dmask_node, ModelParams mp, double* __restrict__ R,
-               T* __restrict__ vals) {
+               T* __restrict__ vals, int64_t nnzb, const double* __restrict__ geo, double* __restrict__ geo_out) {
   using ET_ = ElemTraits<ET>;
   constexpr int RDIM = ET_::RDIM, NEN = ET_::NEN, NQ = ET_::NQ;
   constexpr int SDIM = (ET == AGX_HEX8) ? 3 : 2;
@@ -139,7 +141,8 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
     for (int d = 0; d < SDIM; ++d) xa[d] = (T)coords[(int64_t)node * SDIM + d];
     T ua[NDOF];
 #pragma unroll
-    for (int c = 0; c < NDOF; ++c) ua[c] = (MODEL == AGX_MODEL_NEUMANN) ? T(0) : (T)dofs[(int64_t)node * NDOF + c];
+    for (int c = 0; c < NDOF; ++c)
+      ua[c] = (MODEL == AGX_MODEL_NEUMANN || dofs == nullptr) ? T(0) : (T)dofs[(int64_t)node * NDOF + c];
     T tna = 0;
     if constexpr (MODEL == AGX_MODEL_HEAT_BE) tna = (T)node_field[node];
     T ke = 1;
@@ -187,35 +190,46 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
           if (d2 != d) v *= fac[d2];
         dN[d] = v;
       }
-      // isoparametric Jacobian dX/dxi
-      T J[SDIM][RDIM];
-#pragma unroll
-      for (int i = 0; i < SDIM; ++i)
-#pragma unroll
-        for (int j = 0; j < RDIM; ++j) J[i][j] = group_sum<NEN>(xa[i] * dN[j]);
-
       if constexpr (MODEL == AGX_MODEL_NEUMANN) {
         // line in 2-D: |G1 x E3| = |G1| (models.py:1818-1823); weight 1
-        T len = sqrt(J[0][0] * J[0][0] + J[1][0] * J[1][0]);
+        T G[SDIM];
+#pragma unroll
+        for (int i = 0; i < SDIM; ++i) G[i] = group_sum<NEN>(xa[i] * dN[0]);
+        T len = sqrt(G[0] * G[0] + G[1] * G[1]);
         if constexpr (DO_R) {
 #pragma unroll
           for (int c = 0; c < NDOF; ++c) Ra[c] += -(double)(Na * (T)mp.p[c] * len);
         }
         continue;
       } else {
-        T Jm[SDIM][SDIM], Ji[SDIM][SDIM];
-#pragma unroll
-        for (int i = 0; i < SDIM; ++i)
-#pragma unroll
-          for (int j = 0; j < SDIM; ++j) Jm[i][j] = J[i][j];
-        const T wdet = inverse<T, SDIM>(Jm, Ji);  // Gauss weight is 1
+        // physical gradient g_a = dN_a/dxi J^-1 and w det J: from the float64 geometry cache
+        // when one is given (uniform branch), else from the isoparametric Jacobian dX/dxi
         T ga[SDIM];
+        T wdet;
+        const int64_t grec = ((e * NQ + q) * NEN + a) * (SDIM + 1);
+        if (geo != nullptr) {
 #pragma unroll
-        for (int d = 0; d < SDIM; ++d) {
-          T v = 0;
+          for (int d = 0; d < SDIM; ++d) ga[d] = (T)geo[grec + d];
+          wdet = (T)geo[grec + SDIM];
+        } else {
+          T Jm[SDIM][SDIM], Ji[SDIM][SDIM];
 #pragma unroll
-          for (int k = 0; k < SDIM; ++k) v += dN[k] * Ji[k][d];
-          ga[d] = v;
+          for (int i = 0; i < SDIM; ++i)
+#pragma unroll
+            for (int j = 0; j < SDIM; ++j) Jm[i][j] = group_sum<NEN>(xa[i] * dN[j]);
+          wdet = inverse<T, SDIM>(Jm, Ji);  // Gauss weight is 1
+#pragma unroll
+          for (int d = 0; d < SDIM; ++d) {
+            T v = 0;
+#pragma unroll
+            for (int k = 0; k < SDIM; ++k) v += dN[k] * Ji[k][d];
+            ga[d] = v;
+          }
+          if (geo_out != nullptr && valid) {
+#pragma unroll
+            for (int d = 0; d < SDIM; ++d) geo_out[grec + d] = (double)ga[d];
+            geo_out[grec + SDIM] = (double)wdet;
+          }
         }
 
         if constexpr (MODEL == AGX_MODEL_POISSON_SINCOS || MODEL == AGX_MODEL_HEAT_POTENTIAL ||
@@ -341,13 +355,14 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
       for (int b = 0; b < NEN; ++b) {
         const unsigned dmb = __shfl_sync(0xffffffffu, dma, gbase + b);
         if (valid) {
-          const int64_t pos = epos[(e * NEN + a) * NEN + b];
-          T* blk = vals + pos * (NDOF * NDOF);
+          // entry-major value planes: entry (i, j) of block pos at vals[(i ndof + j) nnzb + pos]
+          T* blk = vals + epos[(e * NEN + a) * NEN + b];
 #pragma unroll
           for (int i = 0; i < NDOF; ++i)
 #pragma unroll
             for (int j = 0; j < NDOF; ++j)
-              if (!((dma >> i) & 1u) && !((dmb >> j) & 1u)) atomicAdd(blk + i * NDOF + j, K[b][i][j]);
+              if (!((dma >> i) & 1u) && !((dmb >> j) & 1u))
+                atomicAdd(blk + (int64_t)(i * NDOF + j) * nnzb, K[b][i][j]);
         }
       }
     }
@@ -357,35 +372,39 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
 // prescribed diagonal entries of the (zeroed) value array set to one
 template <typename T>
 __global__ void set_dirichlet_diag(int64_t n_dir, const int32_t* __restrict__ dir_dofs,
-                                   const int32_t* __restrict__ diagpos, int ndof, T* __restrict__ vals) {
+                                   const int32_t* __restrict__ diagpos, int ndof, int64_t nnzb,
+                                   T* __restrict__ vals) {
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n_dir; k += (int64_t)gridDim.x * blockDim.x) {
     const int d = dir_dofs[k];
     const int p = d / ndof, c = d - p * ndof;
-    vals[(int64_t)diagpos[p] * ndof * ndof + c * ndof + c] = T(1);
+    vals[(int64_t)(c * ndof + c) * nnzb + diagpos[p]] = T(1);
   }
 }
 
 // inverse diagonal for Jacobi
 template <typename T>
-__global__ void inverse_diagonal(int64_t n_dofs, int ndof, const int32_t* __restrict__ diagpos,
+__global__ void inverse_diagonal(int64_t n_dofs, int ndof, int64_t nnzb, const int32_t* __restrict__ diagpos,
                                  const T* __restrict__ vals, T* __restrict__ dinv) {
   for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d < n_dofs; d += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = d / ndof;
     const int c = (int)(d - p * ndof);
-    const T v = vals[(int64_t)diagpos[p] * ndof * ndof + c * ndof + c];
+    const T v = vals[(int64_t)(c * ndof + c) * nnzb + diagpos[p]];
     dinv[d] = v != T(0) ? T(1) / v : T(0);
   }
 }
 
 template <int ET, int MODEL, typename T, bool DO_R, bool DO_K>
-void launch_element(agx_context* ctx, agx_element_set& s, const double* dofs, double* R, T* vals) {
+void launch_element(agx_context* ctx, agx_element_set& s, const double* dofs, double* R, T* vals,
+                    double* geo_out = nullptr) {
+  // the float64 passes read the geometry cache once it exists
+  const double* geo = (std::is_same<T, double>::value && geo_out == nullptr) ? s.d_geo : nullptr;
   ModelParams mp;
   for (int i = 0; i < AGX_MAX_PARAMS; ++i) mp.p[i] = s.params[i];
   const int64_t lanes = s.n_elem * ElemTraits<ET>::NEN;
   const int grid = agx_grid(ctx, lanes, 8);
   element_kernel<ET, MODEL, T, DO_R, DO_K><<<grid, AGX_BLOCK, 0, ctx->stream>>>(
       s.n_elem, s.d_conn, s.d_epos, ctx->d_coords, dofs, s.d_elem_field, s.d_node_field, ctx->d_dmask_node, mp, R,
-      vals);
+      vals, ctx->nnzb, geo, geo_out);
   ctx->n_launches += 1;
 }
 
@@ -410,21 +429,43 @@ int dispatch(agx_context* ctx, agx_element_set& s, const double* dofs, double* R
   return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "element type %d with model %d is not supported", s.elem_type, s.model);
 }
 
+// one-time float64 geometry pass of a domain set: fills s.d_geo
+int build_geometry(agx_context* ctx, agx_element_set& s) {
+  if (s.elem_type == AGX_LINE2 || s.d_geo) return AGX_OK;
+  const int nq = s.elem_type == AGX_HEX8 ? 8 : 4;
+  const int sd = s.elem_type == AGX_HEX8 ? 3 : 2;
+  const size_t bytes = sizeof(double) * (size_t)s.n_elem * nq * s.nen * (sd + 1);
+  if (bytes > ctx->geo_cache_limit) return AGX_OK;  // too large: the passes recompute the geometry
+  AGX_CUDA(ctx, cudaMalloc((void**)&s.d_geo, bytes));
+  // the geometry does not depend on the model: one scalar-model pass serves every model
+  if (s.elem_type == AGX_HEX8)
+    launch_element<AGX_HEX8, AGX_MODEL_HEAT_POTENTIAL, double, false, false>(ctx, s, nullptr, nullptr, nullptr,
+                                                                             s.d_geo);
+  else
+    launch_element<AGX_QUAD4, AGX_MODEL_HEAT_POTENTIAL, double, false, false>(ctx, s, nullptr, nullptr, nullptr,
+                                                                              s.d_geo);
+  AGX_CHECK_LAUNCH(ctx);
+  return AGX_OK;
+}
+
 }  // namespace
 
 int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, int tangent_dtype) {
   const int bs = ctx->ndof * ctx->ndof;
+  if (residual || tangent_dtype == AGX_F64)
+    for (auto& s : ctx->sets)
+      if (int rc = build_geometry(ctx, s)) return rc;
   if (residual) AGX_CUDA(ctx, cudaMemsetAsync(residual, 0, sizeof(double) * ctx->n_dofs, ctx->stream));
   if (tangent_dtype == AGX_F64) {
     AGX_CUDA(ctx, cudaMemsetAsync(ctx->d_vals64, 0, sizeof(double) * ctx->nnzb * bs, ctx->stream));
     if (ctx->n_dir > 0)
       set_dirichlet_diag<double><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(
-          ctx->n_dir, ctx->d_dir_dofs, ctx->d_diagpos, ctx->ndof, ctx->d_vals64);
+          ctx->n_dir, ctx->d_dir_dofs, ctx->d_diagpos, ctx->ndof, ctx->nnzb, ctx->d_vals64);
   } else if (tangent_dtype == AGX_F32) {
     AGX_CUDA(ctx, cudaMemsetAsync(ctx->d_vals32, 0, sizeof(float) * ctx->nnzb * bs, ctx->stream));
     if (ctx->n_dir > 0)
       set_dirichlet_diag<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(
-          ctx->n_dir, ctx->d_dir_dofs, ctx->d_diagpos, ctx->ndof, ctx->d_vals32);
+          ctx->n_dir, ctx->d_dir_dofs, ctx->d_diagpos, ctx->ndof, ctx->nnzb, ctx->d_vals32);
   }
   for (auto& s : ctx->sets) {
     int rc = AGX_OK;
@@ -452,11 +493,11 @@ int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, in
   if (tangent_dtype >= 0) ctx->n_launches += (ctx->n_dir > 0 ? 2 : 1);  // Dirichlet diagonal + inverse diagonal
   if (tangent_dtype == AGX_F64) {
     inverse_diagonal<double><<<agx_grid(ctx, ctx->n_dofs), AGX_BLOCK, 0, ctx->stream>>>(
-        ctx->n_dofs, ctx->ndof, ctx->d_diagpos, ctx->d_vals64, ctx->d_dinv64);
+        ctx->n_dofs, ctx->ndof, ctx->nnzb, ctx->d_diagpos, ctx->d_vals64, ctx->d_dinv64);
     ctx->tangent_valid = AGX_F64;
   } else if (tangent_dtype == AGX_F32) {
     inverse_diagonal<float><<<agx_grid(ctx, ctx->n_dofs), AGX_BLOCK, 0, ctx->stream>>>(
-        ctx->n_dofs, ctx->ndof, ctx->d_diagpos, ctx->d_vals32, ctx->d_dinv32);
+        ctx->n_dofs, ctx->ndof, ctx->nnzb, ctx->d_diagpos, ctx->d_vals32, ctx->d_dinv32);
     ctx->tangent_valid = AGX_F32;
   }
   AGX_CHECK_LAUNCH(ctx);

@@ -73,25 +73,29 @@ __device__ bool reduce_last_block(double (&v)[NV], double* __restrict__ partials
 __device__ __forceinline__ bool bad(double x) { return !isfinite(x) || x == 0.0; }
 
 // ---- sparse product ------------------------------------------------------------------
-// y = A x for the node-block CSR; TPR lanes per block row.  Optionally returns partial
-// (p, A p) with p = x.
-template <typename T, int NDOF, int TPR>
+// Values are stored entry-major: entry (i, j) of block k at vals[(i ndof + j) nnzb + k], so
+// the TPR lanes of a row (consecutive k) read each entry plane with contiguous loads.
+// y = A x for the node-block CSR with TPR lanes per block row; with `dir` the operand is
+// formed on the fly as x = z + beta p_old (the CG direction update folded into the product).
+template <typename T, int NDOF, int TPR, bool DIR>
 __device__ __forceinline__ void bsr_row(int64_t row, int sub, const int32_t* __restrict__ rowptr,
-                                        const int32_t* __restrict__ col, const T* __restrict__ vals,
-                                        const T* __restrict__ x, T (&y)[NDOF]) {
+                                        const int32_t* __restrict__ col, const T* __restrict__ vals, int64_t nnzb,
+                                        const T* __restrict__ x, const T* __restrict__ pold, T beta, T (&y)[NDOF]) {
 #pragma unroll
   for (int i = 0; i < NDOF; ++i) y[i] = 0;
   const int beg = rowptr[row], end = rowptr[row + 1];
   for (int k = beg + sub; k < end; k += TPR) {
-    const int c = col[k];
+    const int64_t c = col[k];
     T xc[NDOF];
 #pragma unroll
-    for (int j = 0; j < NDOF; ++j) xc[j] = x[(int64_t)c * NDOF + j];
-    const T* v = vals + (int64_t)k * NDOF * NDOF;
+    for (int j = 0; j < NDOF; ++j) {
+      xc[j] = x[c * NDOF + j];
+      if constexpr (DIR) xc[j] += beta * pold[c * NDOF + j];
+    }
 #pragma unroll
     for (int i = 0; i < NDOF; ++i)
 #pragma unroll
-      for (int j = 0; j < NDOF; ++j) y[i] += v[i * NDOF + j] * xc[j];
+      for (int j = 0; j < NDOF; ++j) y[i] += vals[(int64_t)(i * NDOF + j) * nnzb + k] * xc[j];
   }
 #pragma unroll
   for (int o = TPR / 2; o >= 1; o >>= 1)
@@ -102,13 +106,14 @@ __device__ __forceinline__ void bsr_row(int64_t row, int sub, const int32_t* __r
 template <typename T, int NDOF, int TPR>
 __global__ void __launch_bounds__(AGX_BLOCK) spmv_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr,
                                                          const int32_t* __restrict__ col, const T* __restrict__ vals,
-                                                         const T* __restrict__ x, T* __restrict__ y) {
+                                                         int64_t nnzb, const T* __restrict__ x, T* __restrict__ y) {
   const int sub = threadIdx.x % TPR;
   const int64_t total = ((n_rows * TPR + 31) / 32) * 32;
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = L / TPR;
     T yr[NDOF];
-    bsr_row<T, NDOF, TPR>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, x, yr);
+    bsr_row<T, NDOF, TPR, false>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, x, nullptr, T(0),
+                                 yr);
     if (row < n_rows && sub == 0) {
 #pragma unroll
       for (int i = 0; i < NDOF; ++i) y[row * NDOF + i] = yr[i];
@@ -116,25 +121,30 @@ __global__ void __launch_bounds__(AGX_BLOCK) spmv_kernel(int64_t n_rows, const i
   }
 }
 
-// q = A p and alpha = rz / (p, q)
+// p_new = z + beta p_old (own rows), q = A p_new, alpha = rz / (p_new, q).  beta = 0 on the
+// first iteration (p_old = 0), which makes p_new = z.
 template <typename T, int NDOF, int TPR>
 __global__ void __launch_bounds__(AGX_BLOCK)
 spmv_dot_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-                const T* __restrict__ vals, const T* __restrict__ p, T* __restrict__ q, agx_krylov_scalars* sc,
-                double* partials, unsigned* counter, int mode) {
+                const T* __restrict__ vals, int64_t nnzb, const T* __restrict__ z, const T* __restrict__ pold,
+                T* __restrict__ pnew, T* __restrict__ q, agx_krylov_scalars* sc, double* partials, unsigned* counter) {
   if (sc->converged) return;
+  const T beta = (T)sc->beta;
   const int sub = threadIdx.x % TPR;
   const int64_t total = ((n_rows * TPR + 31) / 32) * 32;
   double acc[1] = {0.0};
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = L / TPR;
     T yr[NDOF];
-    bsr_row<T, NDOF, TPR>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, p, yr);
+    bsr_row<T, NDOF, TPR, true>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, z, pold, beta, yr);
     if (row < n_rows && sub == 0) {
 #pragma unroll
       for (int i = 0; i < NDOF; ++i) {
-        q[row * NDOF + i] = yr[i];
-        acc[0] += (double)yr[i] * (double)p[row * NDOF + i];
+        const int64_t d = row * NDOF + i;
+        const T pn = z[d] + beta * pold[d];
+        pnew[d] = pn;
+        q[d] = yr[i];
+        acc[0] += (double)yr[i] * (double)pn;
       }
     }
   }
@@ -186,10 +196,10 @@ pcg_init_kernel(int64_t n, const double* __restrict__ b, const T* __restrict__ d
     const T ri = (T)(b[i] * s);
     x[i] = 0;
     r[i] = ri;
+    p[i] = 0;  // p_old of the first fused product (beta = 0)
     if (jacobi) {
       const T zi = dinv[i] * ri;
       z[i] = zi;
-      p[i] = zi;
       acc[0] += (double)ri * (double)zi;
     }
     acc[1] += (double)ri * (double)ri;
@@ -235,15 +245,6 @@ pcg_update_kernel(int64_t n, T* __restrict__ x, T* __restrict__ r, T* __restrict
       sc->rz = tot[0];
     }
   }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(AGX_BLOCK)
-pcg_direction_kernel(int64_t n, T* __restrict__ p, const T* __restrict__ z, const agx_krylov_scalars* sc) {
-  if (sc->converged) return;
-  const T bta = (T)sc->beta;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = z[i] + bta * p[i];
 }
 
 // ---- flexible CG (Notay FCG(1)): beta = -(z_new, q) / (p, q) ----------------------------
@@ -315,7 +316,7 @@ bicg_p_kernel(int64_t n, double* __restrict__ p, const double* __restrict__ r, c
 template <int NDOF, int TPR>
 __global__ void __launch_bounds__(AGX_BLOCK)
 bicg_spmv_rhat(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-               const double* __restrict__ vals, const double* __restrict__ y, double* __restrict__ v,
+               const double* __restrict__ vals, int64_t nnzb, const double* __restrict__ y, double* __restrict__ v,
                const double* __restrict__ rhat, agx_krylov_scalars* sc, double* partials, unsigned* counter) {
   if (sc->converged) return;
   const int sub = threadIdx.x % TPR;
@@ -324,7 +325,8 @@ bicg_spmv_rhat(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = L / TPR;
     double yr[NDOF];
-    bsr_row<double, NDOF, TPR>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, y, yr);
+    bsr_row<double, NDOF, TPR, false>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, y, nullptr, 0.0,
+                                      yr);
     if (row < n_rows && sub == 0) {
 #pragma unroll
       for (int i = 0; i < NDOF; ++i) {
@@ -357,7 +359,7 @@ bicg_s_kernel(int64_t n, const double* __restrict__ r, const double* __restrict_
 template <int NDOF, int TPR>
 __global__ void __launch_bounds__(AGX_BLOCK)
 bicg_spmv_ts(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-             const double* __restrict__ vals, const double* __restrict__ z, double* __restrict__ t,
+             const double* __restrict__ vals, int64_t nnzb, const double* __restrict__ z, double* __restrict__ t,
              const double* __restrict__ s, agx_krylov_scalars* sc, double* partials, unsigned* counter) {
   if (sc->converged) return;
   const int sub = threadIdx.x % TPR;
@@ -366,7 +368,8 @@ bicg_spmv_ts(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* 
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = L / TPR;
     double yr[NDOF];
-    bsr_row<double, NDOF, TPR>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, z, yr);
+    bsr_row<double, NDOF, TPR, false>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, z, nullptr, 0.0,
+                                      yr);
     if (row < n_rows && sub == 0) {
 #pragma unroll
       for (int i = 0; i < NDOF; ++i) {
@@ -489,26 +492,40 @@ constexpr int tpr_for(int dim) {
 }
 
 // launch helpers dispatching on the block size
+// One resident wave: blocks per SM from the occupancy calculator (cached per kernel), capped by
+// the partials buffer (red_blocks).
+template <class K>
+int resident_grid(agx_context* ctx, K kernel) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, AGX_BLOCK, 0) != cudaSuccess || nb < 1) nb = 4;
+  const int g = nb * ctx->sm_count;
+  return g < ctx->red_blocks ? g : ctx->red_blocks;
+}
+
 template <typename T>
-void launch_spmv_dot(agx_context* ctx, const T* vals, const T* p, T* q) {
+void launch_spmv_dot(agx_context* ctx, const T* vals, const T* z, const T* pold, T* pnew, T* q) {
   agx_prof_scope ps(ctx, AGX_PROF_SPMV);
   const int64_t nr = ctx->n_nodes;
-  const int g = ctx->red_blocks;
   auto* sc = ctx->d_scal;
+#define AGX_SPMV_DOT(ND, TP)                                                                                   \
+  do {                                                                                                         \
+    static int g_cache = 0;                                                                                    \
+    if (!g_cache) g_cache = resident_grid(ctx, spmv_dot_kernel<T, ND, TP>);                                    \
+    spmv_dot_kernel<T, ND, TP><<<g_cache, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, vals,    \
+                                                                       ctx->nnzb, z, pold, pnew, q, sc,        \
+                                                                       ctx->d_partials, ctx->d_counter);       \
+  } while (0)
   if (ctx->ndof == 1) {
     if (ctx->dim == 3)
-      spmv_dot_kernel<T, 1, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, vals, p, q, sc,
-                                                                ctx->d_partials, ctx->d_counter, 0);
+      AGX_SPMV_DOT(1, 8);
     else
-      spmv_dot_kernel<T, 1, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, vals, p, q, sc,
-                                                                ctx->d_partials, ctx->d_counter, 0);
+      AGX_SPMV_DOT(1, 4);
   } else if (ctx->ndof == 2) {
-    spmv_dot_kernel<T, 2, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, vals, p, q, sc,
-                                                              ctx->d_partials, ctx->d_counter, 0);
+    AGX_SPMV_DOT(2, 4);
   } else {
-    spmv_dot_kernel<T, 3, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, vals, p, q, sc,
-                                                              ctx->d_partials, ctx->d_counter, 0);
+    AGX_SPMV_DOT(3, 8);
   }
+#undef AGX_SPMV_DOT
 }
 
 template <int NDOF, int TPR>
@@ -516,11 +533,12 @@ void launch_bicg_spmvs(agx_context* ctx, int which, double* a, double* b, double
   const int g = ctx->red_blocks;
   if (which == 0)
     bicg_spmv_rhat<NDOF, TPR><<<g, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_nodes, ctx->d_rowptr, ctx->d_col,
-                                                                ctx->d_vals64, a, b, c, ctx->d_scal, ctx->d_partials,
-                                                                ctx->d_counter);
+                                                                ctx->d_vals64, ctx->nnzb, a, b, c, ctx->d_scal,
+                                                                ctx->d_partials, ctx->d_counter);
   else
     bicg_spmv_ts<NDOF, TPR><<<g, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_nodes, ctx->d_rowptr, ctx->d_col, ctx->d_vals64,
-                                                              a, b, c, ctx->d_scal, ctx->d_partials, ctx->d_counter);
+                                                              ctx->nnzb, a, b, c, ctx->d_scal, ctx->d_partials,
+                                                              ctx->d_counter);
 }
 
 void launch_bicg_spmv(agx_context* ctx, int which, double* a, double* b, double* c) {
@@ -549,6 +567,30 @@ int read_scalars(agx_context* ctx) {
 
 }  // namespace
 
+template <typename T>
+__global__ void planes_to_blocks_kernel(int64_t nnzb, int bs, const T* __restrict__ planes, T* __restrict__ blocks) {
+  const int64_t total = nnzb * bs;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = t / bs;
+    const int e = (int)(t - k * bs);
+    blocks[t] = planes[(int64_t)e * nnzb + k];
+  }
+}
+
+void agx_launch_planes_to_blocks(agx_context* ctx, const double* planes, double* blocks) {
+  const int bs = ctx->ndof * ctx->ndof;
+  planes_to_blocks_kernel<double><<<agx_grid(ctx, ctx->nnzb * bs), AGX_BLOCK, 0, ctx->stream>>>(ctx->nnzb, bs, planes,
+                                                                                               blocks);
+  ctx->n_launches += 1;
+}
+
+void agx_launch_planes_to_blocks(agx_context* ctx, const float* planes, float* blocks) {
+  const int bs = ctx->ndof * ctx->ndof;
+  planes_to_blocks_kernel<float><<<agx_grid(ctx, ctx->nnzb * bs), AGX_BLOCK, 0, ctx->stream>>>(ctx->nnzb, bs, planes,
+                                                                                             blocks);
+  ctx->n_launches += 1;
+}
+
 int agx_spmv_impl(agx_context* ctx, int dtype, const void* x, void* y) {
   const int64_t nr = ctx->n_nodes;
   const int g = agx_grid(ctx, nr * 8, 8);
@@ -557,13 +599,17 @@ int agx_spmv_impl(agx_context* ctx, int dtype, const void* x, void* y) {
     const T* v = dtype == AGX_F64 ? (const T*)ctx->d_vals64 : (const T*)ctx->d_vals32;
     if (ctx->ndof == 1) {
       if (ctx->dim == 3)
-        spmv_kernel<T, 1, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, (const T*)x, (T*)y);
+        spmv_kernel<T, 1, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb,
+                                                              (const T*)x, (T*)y);
       else
-        spmv_kernel<T, 1, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, (const T*)x, (T*)y);
+        spmv_kernel<T, 1, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb,
+                                                              (const T*)x, (T*)y);
     } else if (ctx->ndof == 2) {
-      spmv_kernel<T, 2, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, (const T*)x, (T*)y);
+      spmv_kernel<T, 2, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, (const T*)x,
+                                                            (T*)y);
     } else {
-      spmv_kernel<T, 3, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, (const T*)x, (T*)y);
+      spmv_kernel<T, 3, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, (const T*)x,
+                                                            (T*)y);
     }
   };
   if (dtype == AGX_F64) go(double{});
@@ -626,17 +672,22 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
   ctx->n_launches += 2;  // norm + method initialisation
   int it_done = 0;
   if (method == AGX_PCG) {
-    pcg_init_kernel<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, rhs, ctx->d_dinv64, x, ctx->d_r, ctx->d_z, ctx->d_p,
+    // two direction buffers used alternately: the product of iteration k forms p_k from
+    // z_k and p_(k-1) (d_p and d_s; BiCGStab's s is free here)
+    double* pbuf[2] = {ctx->d_p, ctx->d_s};
+    int cur = 0;
+    pcg_init_kernel<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, rhs, ctx->d_dinv64, x, ctx->d_r, ctx->d_z, pbuf[0],
                                                              sc, ctx->d_partials, ctx->d_counter, 0, 1);
     while (true) {
       const int kn = std::min(every, maxiter - it_done);
-      ctx->n_launches += 3 * kn;
+      ctx->n_launches += 2 * kn;
       for (int k = 0; k < kn; ++k) {
-        launch_spmv_dot<double>(ctx, ctx->d_vals64, ctx->d_p, ctx->d_q);
+        double* pnew = pbuf[cur ^ 1];
+        launch_spmv_dot<double>(ctx, ctx->d_vals64, ctx->d_z, pbuf[cur], pnew, ctx->d_q);
         agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
-        pcg_update_kernel<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, x, ctx->d_r, ctx->d_z, ctx->d_p, ctx->d_q,
+        pcg_update_kernel<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, x, ctx->d_r, ctx->d_z, pnew, ctx->d_q,
                                                                    ctx->d_dinv64, sc, ctx->d_partials, ctx->d_counter);
-        pcg_direction_kernel<double><<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_p, ctx->d_z, sc);
+        cur ^= 1;
       }
       AGX_CHECK_LAUNCH(ctx);
       int rc = read_scalars(ctx);
@@ -646,8 +697,10 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
     }
   } else if (method == AGX_PCG_MIXED || method == AGX_FCG_MIXED) {
     const bool flexible = method == AGX_FCG_MIXED && ctx->precond != nullptr;
+    float* pbuf[2] = {ctx->f_p, ctx->f_rold};
+    int cur = 0;
     pcg_init_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, rhs, ctx->d_dinv32, ctx->f_x, ctx->f_r, ctx->f_z,
-                                                            ctx->f_p, sc, ctx->d_partials, ctx->d_counter, 1,
+                                                            pbuf[0], sc, ctx->d_partials, ctx->d_counter, 1,
                                                             flexible ? 0 : 1);
     if (flexible) {
       if (ctx->precond(ctx->precond_user, ctx->f_r, ctx->f_z, n, ctx->stream) != 0)
@@ -656,22 +709,23 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
                                                                                      ctx->f_z);
       fcg_direction_dots<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_r, ctx->f_z, ctx->f_q, sc, ctx->d_partials,
                                                                  ctx->d_counter);
-      AGX_CUDA(ctx, cudaMemcpyAsync(ctx->f_p, ctx->f_z, sizeof(float) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+      ctx->n_launches += 2;
     }
     while (true) {
       const int kn = std::min(every, maxiter - it_done);
-      ctx->n_launches += (flexible ? 5 : 3) * kn;
+      ctx->n_launches += (flexible ? 4 : 2) * kn;
       for (int k = 0; k < kn; ++k) {
-        launch_spmv_dot<float>(ctx, ctx->d_vals32, ctx->f_p, ctx->f_q);
+        float* pnew = pbuf[cur ^ 1];
+        launch_spmv_dot<float>(ctx, ctx->d_vals32, ctx->f_z, pbuf[cur], pnew, ctx->f_q);
         if (!flexible) {
           agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
-          pcg_update_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, ctx->f_r, ctx->f_z, ctx->f_p,
+          pcg_update_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, ctx->f_r, ctx->f_z, pnew,
                                                                     ctx->f_q, ctx->d_dinv32, sc, ctx->d_partials,
                                                                     ctx->d_counter);
         } else {
           {
             agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
-            fcg_update_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, ctx->f_r, ctx->f_p, ctx->f_q, sc,
+            fcg_update_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, ctx->f_r, pnew, ctx->f_q, sc,
                                                                       ctx->d_partials, ctx->d_counter);
           }
           agx_prof_scope pp(ctx, AGX_PROF_PRECOND);
@@ -682,8 +736,7 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
           fcg_direction_dots<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_r, ctx->f_z, ctx->f_q, sc,
                                                                      ctx->d_partials, ctx->d_counter);
         }
-        agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
-        pcg_direction_kernel<float><<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_p, ctx->f_z, sc);
+        cur ^= 1;
       }
       AGX_CHECK_LAUNCH(ctx);
       int rc = read_scalars(ctx);

@@ -206,7 +206,8 @@ def gpu_arm(args):
     b = 3
     nnzb = prob.nnzb
     n_nodes = w.n_dofs // 3
-    spmv_bytes = nnzb * (b * b * 4 + 4) + (n_nodes + 1) * 4 + 2 * w.n_dofs * 4
+    # fused product: matrix planes + columns + rowptr; reads z and p_old, writes p_new and q
+    spmv_bytes = nnzb * (b * b * 4 + 4) + (n_nodes + 1) * 4 + 4 * w.n_dofs * 4
     spmv_avg_ms = ms[N.AGX_PROF_SPMV] / max(1, cnt[N.AGX_PROF_SPMV])
     peak, peak_kind = _peaks()
     achieved = spmv_bytes / (spmv_avg_ms * 1e-3) / 1e9
@@ -251,7 +252,7 @@ def gpu_arm(args):
         "final_residual_ratio": res_end / res0 if res0 else None,
         "kernel_ms_per_step": {k: v / args.steps for k, v in shares.items()},
         "kernel_launches_per_step": {k: v / args.steps for k, v in launches.items()},
-        "roofline": {"bound": "hbm", "kernel": "spmv_dot_kernel<float,3,8> (BSR 3x3 SpMV + dot)",
+        "roofline": {"bound": "hbm", "kernel": "spmv_dot_kernel<float,3,8> (BSR 3x3 SpMV, direction update, dot)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic, "algorithmic_bytes": spmv_bytes,
                      "avg_launch_ms": spmv_avg_ms},

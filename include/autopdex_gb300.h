@@ -151,11 +151,13 @@ int agx_set_node_field(agx_context* ctx, int set_id, const double* field_dev);
    BSR values with Dirichlet rows/columns eliminated (identity rows). */
 int agx_assemble(agx_context* ctx, const double* dofs, double* residual, int tangent_dtype);
 /* Pattern and values of the last assembled tangent (device pointers owned by the
-   library): rowptr (n_nodes+1), col (nnzb), vals (nnzb*ndof*ndof of the dtype). */
+   library): rowptr (n_nodes+1), col (nnzb), vals (nnzb*ndof*ndof of the dtype) stored
+   entry-major: entry (i, j) of block k at vals[(i*ndof + j)*nnzb + k]. */
 int agx_get_matrix(agx_context* ctx, int dtype, const int32_t** rowptr, const int32_t** col,
                    const void** vals, int64_t* nnzb);
 /* Copies the pattern and the values of the last assembled tangent of `dtype` into
-   caller-owned DEVICE buffers (rowptr n_nodes+1, col nnzb, vals nnzb*ndof*ndof). */
+   caller-owned DEVICE buffers (rowptr n_nodes+1, col nnzb, vals nnzb*ndof*ndof as
+   row-major ndof x ndof blocks, block k at vals + k*ndof*ndof). */
 int agx_copy_matrix(agx_context* ctx, int dtype, int32_t* rowptr, int32_t* col, void* vals);
 /* y = K x with the last assembled tangent of `dtype` (x, y of that dtype). */
 int agx_spmv(agx_context* ctx, int dtype, const void* x, void* y);
