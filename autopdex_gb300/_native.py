@@ -75,17 +75,33 @@ _SIGNATURES = {
 "agx_pcg_noalloc": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int, _P, _P, C.c_double, C.c_int, _P,
                                 C.POINTER(SolveInfo), C.c_char_p, C.c_int]),
     "agx_get_sizes": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
+    # learned preconditioner (include/autopdex_gb300_nn.h)
+    "agx_nn_conv3x3": (C.c_int, [_P, _P, C.c_int, C.c_int, _P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int,
+                                 C.c_int, C.c_int, _P, _P]),
+    "agx_nn_wgrad3x3": (C.c_int, [_P, _P, C.c_int, C.c_int, _P, C.c_int, _P, C.c_int, C.c_int, C.c_int, _P, _P]),
+    "agx_nn_pack_weights": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P]),
+    "agx_nn_unpack_wgrad": (C.c_int, [_P, C.c_int, C.c_int, _P, _P]),
+    "agx_nn_pool2": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
+    "agx_nn_upsample2": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
+    "agx_nn_relu_backward": (C.c_int, [_P, _P, C.c_int64, _P]),
+    "agx_nn_add": (C.c_int, [_P, _P, C.c_int64, _P]),
+    "agx_nn_bias_grad": (C.c_int, [_P, C.c_int64, C.c_int, _P, _P]),
+    "agx_nn_grid_from_vector": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, _P]),
+    "agx_nn_vector_from_grid": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P]),
 }
 
 _lib = None
 
 
 def header_symbols():
-    """Function names declared in include/autopdex_gb300.h."""
-    path = os.path.join(_build.INCLUDE, "autopdex_gb300.h")
-    with open(path) as fh:
-        txt = fh.read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(agx_\w+)\s*\(", txt, re.M)))
+    """Function names declared in the headers under include/."""
+    names = set()
+    for f in sorted(os.listdir(_build.INCLUDE)):
+        if f.endswith(".h"):
+            with open(os.path.join(_build.INCLUDE, f)) as fh:
+                txt = fh.read()
+            names |= set(re.findall(r"^\s*(?:int|const char\*)\s+(agx_\w+)\s*\(", txt, re.M))
+    return sorted(names)
 
 
 def lib_path():

@@ -214,6 +214,7 @@ int agx_finalize(agx_context* ctx) {
   for (float** p : {&ctx->f_x, &ctx->f_r, &ctx->f_z, &ctx->f_p, &ctx->f_q, &ctx->f_rold, &ctx->d_dinv32})
     if (int rc = alloc(ctx, p, n)) return rc;
   ctx->red_blocks = ctx->sm_count * 8;  // one resident wave of 256-thread blocks
+  ctx->vec_blocks = ctx->sm_count * 2;
   if (int rc = alloc(ctx, &ctx->d_partials, (int64_t)ctx->red_blocks * 4)) return rc;  // up to 4 values per block
   if (int rc = alloc(ctx, &ctx->d_counter, 1)) return rc;
   if (int rc = alloc(ctx, &ctx->d_scal, 1)) return rc;

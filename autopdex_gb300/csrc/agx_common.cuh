@@ -91,7 +91,8 @@ struct agx_context {
   float *f_x = nullptr, *f_r = nullptr, *f_z = nullptr, *f_p = nullptr, *f_q = nullptr, *f_rold = nullptr;
 
   // reductions
-  int red_blocks = 0;
+  int red_blocks = 0;   // largest grid of a reducing kernel (8 per SM)
+  int vec_blocks = 0;   // grid of the reducing vector kernels (2 per SM: short reduction tails)
   double* d_partials = nullptr;          // red_blocks * 4
   unsigned int* d_counter = nullptr;
   agx_krylov_scalars* d_scal = nullptr;

@@ -54,8 +54,14 @@ __device__ bool reduce_last_block(double (&v)[NV], double* __restrict__ partials
   __threadfence();
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
-    double s = 0;
-    for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) s += __ldcg(partials + (size_t)k * gridDim.x + i);
+    // all partial loads of a thread issued before any add (grids are at most 8 x 256 blocks)
+    double part[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const unsigned i = threadIdx.x + u * blockDim.x;
+      part[u] = i < gridDim.x ? __ldcg(partials + (size_t)k * gridDim.x + i) : 0.0;
+    }
+    double s = ((part[0] + part[1]) + (part[2] + part[3])) + ((part[4] + part[5]) + (part[6] + part[7]));
     s = warp_sum(s);
     __syncthreads();
     if (lane == 0) sh[k][warp] = s;
@@ -132,7 +138,7 @@ spmv_dot_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_
   const T beta = (T)sc->beta;
   const int sub = threadIdx.x % TPR;
   const int64_t total = ((n_rows * TPR + 31) / 32) * 32;
-  double acc[1] = {0.0};
+  T acc_t = 0;  // per-thread partial in T (a few rows), block and grid sums in float64
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = L / TPR;
     T yr[NDOF];
@@ -144,10 +150,11 @@ spmv_dot_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_
         const T pn = z[d] + beta * pold[d];
         pnew[d] = pn;
         q[d] = yr[i];
-        acc[0] += (double)yr[i] * (double)pn;
+        acc_t += yr[i] * pn;
       }
     }
   }
+  double acc[1] = {(double)acc_t};
   double tot[1];
   if (reduce_last_block<1>(acc, partials, counter, tot) && threadIdx.x == 0) {
     sc->pq = tot[0];
@@ -220,16 +227,17 @@ pcg_update_kernel(int64_t n, T* __restrict__ x, T* __restrict__ r, T* __restrict
                   unsigned* counter) {
   if (sc->converged) return;
   const T a = (T)sc->alpha;
-  double acc[2] = {0.0, 0.0};
+  T rz_t = 0, rr_t = 0;  // per-thread partials in T, block and grid sums in float64
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     x[i] += a * p[i];
     const T ri = r[i] - a * q[i];
     r[i] = ri;
     const T zi = dinv[i] * ri;
     z[i] = zi;
-    acc[0] += (double)ri * (double)zi;
-    acc[1] += (double)ri * (double)ri;
+    rz_t += ri * zi;
+    rr_t += ri * ri;
   }
+  double acc[2] = {(double)rz_t, (double)rr_t};
   double tot[2];
   if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
     sc->iters += 1;
@@ -643,7 +651,7 @@ void agx_launch_masked_scale(agx_context* ctx, const double* src, double* dst, d
 
 int agx_residual_norm(agx_context* ctx, const double* R, double* norm2, double* nonfinite) {
   ctx->n_launches += 1;
-  masked_norm_kernel<<<ctx->red_blocks, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dofs, R, ctx->d_dmask_dof, ctx->d_norm,
+  masked_norm_kernel<<<ctx->vec_blocks, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dofs, R, ctx->d_dmask_dof, ctx->d_norm,
                                                                    ctx->d_partials, ctx->d_counter);
   AGX_CHECK_LAUNCH(ctx);
   AGX_CUDA(ctx, cudaMemcpyAsync(ctx->h_norm, ctx->d_norm, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -655,7 +663,7 @@ int agx_residual_norm(agx_context* ctx, const double* R, double* norm2, double* 
 
 int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_solve_opts* opts, agx_solve_info* info) {
   const int64_t n = ctx->n_dofs;
-  const int g = ctx->red_blocks;
+  const int g = ctx->vec_blocks;  // reducing vector kernels
   const int gv = agx_grid(ctx, n);
   const int method = opts->method;
   const int every = opts->check_every > 0 ? opts->check_every : 16;

@@ -1,0 +1,635 @@
+// BF16 tensor-core kernels of the learned preconditioner (a small convolutional U-Net on
+// the structured node grid, applied inside flexible CG).  Nothing in AutoPDEx corresponds to
+// this part; it is the learned-preconditioner addition of this backend.
+//
+// Tensors are NHWC bf16 with 16, 32 or 64 channels.  A 3x3 convolution (stride 1, zero
+// padding 1) is an implicit GEMM D[pixel, cout] = sum_k A[pixel, k] B[cout, k] with
+// k = tap * CIN + cin: each CTA gathers the A rows of 128 output pixels (all nine taps) and
+// the packed weight image into shared memory in the no-swizzle K-major core-matrix layout
+// (8 rows x 16 bytes per core matrix), one thread issues tcgen05.mma (kind::f16, bf16 in,
+// f32 accumulate, M = 128, N = COUT, K = 16 per instruction) into a TMEM accumulator, the
+// MMA completion is committed to an mbarrier, and the four warps read their 32 TMEM lanes
+// back with tcgen05.ld for the epilogue (bias, ReLU, bf16 store).  The input gradient is the
+// same kernel with the weights flipped and transposed at packing time.  The weight gradient
+// is a second tcgen05 GEMM with the reduction running over pixels.
+//
+// Every wait is bounded: a CTA whose MMA does not complete in time records an error flag
+// and still releases its TMEM.
+#include <cuda_bf16.h>
+
+#include "agx_common.cuh"
+
+namespace {
+
+constexpr int kTile = 128;        // output pixels per CTA (MMA M)
+constexpr int kWaitLimit = 1 << 22;
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  // tcgen05 shared-memory matrix descriptor, no swizzle: start >> 4 (bits 0-13), leading
+  // byte offset >> 4 (16-29: distance of core matrices along K), stride byte offset >> 4
+  // (32-45: distance of 8-row groups along M/N), descriptor version 1 (bits 46-47)
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+__device__ __forceinline__ uint32_t idesc_bf16(int M, int N) {
+  // kind::f16 instruction descriptor: f32 accumulator (bits 4-5 = 1), A and B bf16 (bits 7-9,
+  // 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+      "l"(da), "l"(db), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ int mbar_wait(uint32_t addr, uint32_t phase) {
+  for (int it = 0; it < kWaitLimit; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\tselp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(ok)
+        : "r"(addr), "r"(phase)
+        : "memory");
+    if (ok) return 1;
+  }
+  return 0;
+}
+
+// 32 lanes x 16 consecutive f32 columns of TMEM per call (thread = lane = row)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+template <int NCOLS>
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(slot);
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s), "n"(NCOLS) : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+template <int NCOLS>
+__device__ __forceinline__ void tmem_free(uint32_t tmem) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(NCOLS) : "memory");
+}
+
+__host__ __device__ constexpr int tmem_cols(int n) { return n <= 32 ? 32 : (n <= 64 ? 64 : 128); }
+
+// byte offset of element (row, k) in a K-major no-swizzle operand with `rgroups` 8-row groups
+__device__ __forceinline__ uint32_t core_off(int row, int k, int rgroups) {
+  return (uint32_t)((((k >> 3) * rgroups + (row >> 3)) * 8 + (row & 7)) * 16 + (k & 7) * 2);
+}
+
+struct ConvArgs {
+  const __nv_bfloat16* in1;  // NHWC, C1 channels
+  const __nv_bfloat16* in2;  // NHWC, C2 channels (concatenated after in1), or null when C2 == 0
+  const __nv_bfloat16* wpk;  // packed B image (COUT rows x 9 CIN), core-matrix order
+  const float* bias;         // COUT values or null
+  __nv_bfloat16* out1;       // channels [0, S) (NHWC with S channels)
+  __nv_bfloat16* out2;       // channels [S, COUT) or null when S == COUT
+  int split;                 // S
+  int B, H, W;
+  int* err;
+};
+
+// out = epi(conv3x3(concat(in1, in2)) + bias); EPI 0: identity, 1: ReLU
+template <int C1, int C2, int COUT, int EPI>
+__global__ void __launch_bounds__(kTile) conv3x3_tc(ConvArgs a) {
+  constexpr int CIN = C1 + C2, K = 9 * CIN, NG = COUT / 8;
+  constexpr int A_BYTES = K * kTile * 2;
+  constexpr int NCOLS = tmem_cols(COUT);
+  static_assert(CIN % 16 == 0 && COUT % 16 == 0, "channel counts must be multiples of 16");
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* sA = smem;
+  unsigned char* sB = smem + A_BYTES;
+  __shared__ uint32_t tmem_slot;
+  __shared__ __align__(8) uint64_t mbar;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int64_t HW = (int64_t)a.H * a.W, P = HW * a.B;
+  const int64_t p = (int64_t)blockIdx.x * kTile + tid;
+  const bool pv = p < P;
+  int b = 0, y = 0, x = 0;
+  if (pv) {
+    b = (int)(p / HW);
+    const int64_t rem = p - (int64_t)b * HW;
+    y = (int)(rem / a.W);
+    x = (int)(rem - (int64_t)y * a.W);
+  }
+  // gather the A rows of this thread's pixel: nine taps, CIN channels, 16-byte chunks
+#pragma unroll
+  for (int t = 0; t < 9; ++t) {
+    const int yy = y + t / 3 - 1, xx = x + t % 3 - 1;
+    const bool ok = pv && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+    const int64_t q = ((int64_t)b * a.H + yy) * a.W + xx;
+#pragma unroll
+    for (int j = 0; j < C1 / 8; ++j) {
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (ok) v = reinterpret_cast<const uint4*>(a.in1 + q * C1)[j];
+      *reinterpret_cast<uint4*>(sA + core_off(tid, t * CIN + 8 * j, kTile / 8)) = v;
+    }
+    if constexpr (C2 > 0) {
+#pragma unroll
+      for (int j = 0; j < C2 / 8; ++j) {
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (ok) v = reinterpret_cast<const uint4*>(a.in2 + q * C2)[j];
+        *reinterpret_cast<uint4*>(sA + core_off(tid, t * CIN + C1 + 8 * j, kTile / 8)) = v;
+      }
+    }
+  }
+  // packed weights: already in core-matrix order
+  for (int i = tid; i < K * COUT * 2 / 16; i += kTile)
+    reinterpret_cast<uint4*>(sB)[i] = reinterpret_cast<const uint4*>(a.wpk)[i];
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  const uint32_t mbar_addr = (uint32_t)__cvta_generic_to_shared(&mbar);
+  if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_addr) : "memory");
+  if (warp == 0) tmem_alloc<NCOLS>(&tmem_slot);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  if (tid == 0) {
+    const uint32_t a0 = (uint32_t)__cvta_generic_to_shared(sA), b0 = (uint32_t)__cvta_generic_to_shared(sB);
+    const uint32_t id = idesc_bf16(kTile, COUT);
+#pragma unroll 1
+    for (int s = 0; s < K / 16; ++s) {
+      const uint64_t da = smem_desc(a0 + (uint32_t)(2 * s * (kTile / 8)) * 128u, (kTile / 8) * 128, 128);
+      const uint64_t db = smem_desc(b0 + (uint32_t)(2 * s * NG) * 128u, NG * 128, 128);
+      mma_bf16(tmem, da, db, id, s > 0 ? 1u : 0u);
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_addr)
+                 : "memory");
+  }
+  const int done = mbar_wait(mbar_addr, 0);
+  if (!done && tid == 0) atomicExch(a.err, 1);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (done) {
+    float acc[COUT];
+#pragma unroll
+    for (int c = 0; c < COUT; c += 16) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, acc + c);
+    if (pv) {
+#pragma unroll
+      for (int c = 0; c < COUT; ++c) {
+        float v = acc[c] + (a.bias ? a.bias[c] : 0.0f);
+        if (EPI == 1) v = fmaxf(v, 0.0f);
+        acc[c] = v;
+      }
+      const int S = a.split;
+      for (int c0 = 0; c0 < COUT; c0 += 8) {
+        __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) h[u] = __float2bfloat16(acc[c0 + u]);
+        if (c0 < S)
+          *reinterpret_cast<uint4*>(a.out1 + p * S + c0) = *reinterpret_cast<uint4*>(h);
+        else
+          *reinterpret_cast<uint4*>(a.out2 + p * (COUT - S) + (c0 - S)) = *reinterpret_cast<uint4*>(h);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) tmem_free<NCOLS>(tmem);
+}
+
+struct WgradArgs {
+  const __nv_bfloat16* in1;  // forward inputs, NHWC, C1 (+ C2) channels
+  const __nv_bfloat16* in2;
+  const __nv_bfloat16* dout; // gradient of the pre-activation output, NHWC, COUT channels
+  float* dw;                 // (9 CIN) x COUT, f32, accumulated with atomics
+  int B, H, W;
+  int64_t pix_per_cta;       // pixels reduced by one CTA (multiple of 16)
+  int* err;
+};
+
+// dW[k, co] += sum_p A[k, p] dOut[p, co], A[t CIN + ci, p] = in[p + tap_t, ci]; one CTA per
+// (128-row slice of k, pixel chunk); the pixel chunk is consumed in sub-chunks of PCH pixels.
+template <int C1, int C2, int COUT, int PCH>
+__global__ void __launch_bounds__(kTile) wgrad_tc(WgradArgs a) {
+  constexpr int CIN = C1 + C2, KW = 9 * CIN;
+  constexpr int A_BYTES = kTile * PCH * 2;   // 128 rows x PCH pixels
+  constexpr int NCOLS = tmem_cols(COUT);
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* sA = smem;
+  unsigned char* sB = smem + A_BYTES;        // COUT rows x PCH pixels
+  __shared__ uint32_t tmem_slot;
+  __shared__ __align__(8) uint64_t mbar;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int row0 = blockIdx.y * kTile;       // first k row of this CTA
+  const int64_t HW = (int64_t)a.H * a.W, P = HW * a.B;
+  const int64_t pbeg = (int64_t)blockIdx.x * a.pix_per_cta;
+  const int64_t pend = pbeg + a.pix_per_cta < P ? pbeg + a.pix_per_cta : P;
+  const uint32_t mbar_addr = (uint32_t)__cvta_generic_to_shared(&mbar);
+  if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_addr) : "memory");
+  if (warp == 0) tmem_alloc<NCOLS>(&tmem_slot);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  const uint32_t a0 = (uint32_t)__cvta_generic_to_shared(sA), b0 = (uint32_t)__cvta_generic_to_shared(sB);
+  uint32_t phase = 0;
+  int ok_all = 1;
+  int first = 1;
+  for (int64_t c0 = pbeg; c0 < pend; c0 += PCH) {
+    // A tile: thread handles (8 consecutive k rows = 8 channels of one tap, 8 pixels) blocks
+    for (int blk = tid; blk < (kTile / 8) * (PCH / 8); blk += kTile) {
+      const int rg = blk / (PCH / 8), pg = blk % (PCH / 8);
+      const int krow = row0 + rg * 8;  // first of 8 k rows (same tap: CIN % 8 == 0)
+      __align__(16) __nv_bfloat16 tile[8][8];  // [pixel][channel]
+      const int t = krow / CIN, ci = krow % CIN;
+      const bool rowok = krow < KW;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int64_t pp = c0 + pg * 8 + u;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (rowok && pp < pend) {
+          const int bb = (int)(pp / HW);
+          const int64_t rem = pp - (int64_t)bb * HW;
+          const int y = (int)(rem / a.W), x = (int)(rem - (int64_t)y * a.W);
+          const int yy = y + t / 3 - 1, xx = x + t % 3 - 1;
+          if (yy >= 0 && yy < a.H && xx >= 0 && xx < a.W) {
+            const int64_t q = ((int64_t)bb * a.H + yy) * a.W + xx;
+            if (ci < C1)
+              v = *reinterpret_cast<const uint4*>(a.in1 + q * C1 + ci);
+            else
+              v = *reinterpret_cast<const uint4*>(a.in2 + q * C2 + (ci - C1));
+          }
+        }
+        *reinterpret_cast<uint4*>(tile[u]) = v;
+      }
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        __align__(16) __nv_bfloat16 col[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) col[u] = tile[u][r];
+        *reinterpret_cast<uint4*>(sA + core_off(rg * 8 + r, pg * 8, kTile / 8)) = *reinterpret_cast<uint4*>(col);
+      }
+    }
+    // B tile: dOut^T, rows co, k = pixel
+    for (int blk = tid; blk < (COUT / 8) * (PCH / 8); blk += kTile) {
+      const int ng = blk / (PCH / 8), pg = blk % (PCH / 8);
+      __align__(16) __nv_bfloat16 tile[8][8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int64_t pp = c0 + pg * 8 + u;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (pp < pend) v = *reinterpret_cast<const uint4*>(a.dout + pp * COUT + ng * 8);
+        *reinterpret_cast<uint4*>(tile[u]) = v;
+      }
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        __align__(16) __nv_bfloat16 col[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) col[u] = tile[u][r];
+        *reinterpret_cast<uint4*>(sB + core_off(ng * 8 + r, pg * 8, COUT / 8)) = *reinterpret_cast<uint4*>(col);
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t id = idesc_bf16(kTile, COUT);
+#pragma unroll 1
+      for (int s = 0; s < PCH / 16; ++s) {
+        const uint64_t da = smem_desc(a0 + (uint32_t)(2 * s * (kTile / 8)) * 128u, (kTile / 8) * 128, 128);
+        const uint64_t db = smem_desc(b0 + (uint32_t)(2 * s * (COUT / 8)) * 128u, (COUT / 8) * 128, 128);
+        mma_bf16(tmem, da, db, id, first ? 0u : 1u);
+        first = 0;
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_addr)
+                   : "memory");
+    }
+    first = 0;
+    // the shared tiles are reused by the next sub-chunk only after the MMAs have read them
+    const int done = mbar_wait(mbar_addr, phase);
+    phase ^= 1u;
+    if (!done) {
+      ok_all = 0;
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    __syncthreads();
+  }
+  if (!ok_all && tid == 0) atomicExch(a.err, 1);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok_all && pbeg < pend) {
+    float acc[COUT];
+#pragma unroll
+    for (int c = 0; c < COUT; c += 16) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, acc + c);
+    const int k = row0 + tid;
+    if (k < KW) {
+#pragma unroll
+      for (int c = 0; c < COUT; ++c) atomicAdd(a.dw + (int64_t)k * COUT + c, acc[c]);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) tmem_free<NCOLS>(tmem);
+}
+
+// ---- small kernels ----------------------------------------------------------------------
+// Packs f32 weights W[co][ci][3][3] into the B image of the forward conv (rows co,
+// k = tap CIN + ci) or of the input-gradient conv (rows ci, k = tap' COUT + co with the taps
+// flipped, tap' = 8 - tap).
+__global__ void pack_weights_kernel(const float* __restrict__ w, int cout, int cin, int mode,
+                                    __nv_bfloat16* __restrict__ img) {
+  const int total = cout * cin * 9;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int co = i / (cin * 9), rem = i % (cin * 9), ci = rem / 9, t = rem % 9;
+    int row, k, rows;
+    if (mode == 0) {
+      row = co;
+      k = t * cin + ci;
+      rows = cout;
+    } else {
+      row = ci;
+      k = (8 - t) * cout + co;
+      rows = cin;
+    }
+    const int off = (((k >> 3) * (rows / 8) + (row >> 3)) * 8 + (row & 7)) * 8 + (k & 7);
+    img[off] = __float2bfloat16(w[i]);
+  }
+}
+
+// dW rows (tap CIN + ci) x cout -> torch layout [co][ci][3][3]
+__global__ void unpack_wgrad_kernel(const float* __restrict__ dwk, int cout, int cin, float* __restrict__ dw) {
+  const int total = cout * cin * 9;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int co = i / (cin * 9), rem = i % (cin * 9), ci = rem / 9, t = rem % 9;
+    dw[i] = dwk[(t * cin + ci) * cout + co];
+  }
+}
+
+// 2x2 average pooling (H, W even) and its adjoint
+__global__ void avgpool2_kernel(const __nv_bfloat16* __restrict__ in, __nv_bfloat16* __restrict__ out, int B, int H,
+                                int W, int C, int backward) {
+  const int Ho = H / 2, Wo = W / 2;
+  const int64_t total = (int64_t)B * Ho * Wo * C;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    const int64_t pix = i / C;
+    const int xo = (int)(pix % Wo), yo = (int)((pix / Wo) % Ho), b = (int)(pix / ((int64_t)Wo * Ho));
+    const int64_t base = (((int64_t)b * H + 2 * yo) * W + 2 * xo) * C + c;
+    if (!backward) {
+      const float s = __bfloat162float(in[base]) + __bfloat162float(in[base + C]) +
+                      __bfloat162float(in[base + (int64_t)W * C]) + __bfloat162float(in[base + (int64_t)W * C + C]);
+      out[i] = __float2bfloat16(0.25f * s);
+    } else {  // in: gradient at the pooled size; out: gradient at full size
+      const __nv_bfloat16 g = __float2bfloat16(0.25f * __bfloat162float(in[i]));
+      out[base] = g;
+      out[base + C] = g;
+      out[base + (int64_t)W * C] = g;
+      out[base + (int64_t)W * C + C] = g;
+    }
+  }
+}
+
+// nearest 2x upsampling and its adjoint (sum over the 2x2 block)
+__global__ void upsample2_kernel(const __nv_bfloat16* __restrict__ in, __nv_bfloat16* __restrict__ out, int B, int H,
+                                 int W, int C, int backward) {
+  // H, W: the coarse size
+  const int64_t total = (int64_t)B * H * W * C;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    const int64_t pix = i / C;
+    const int x = (int)(pix % W), y = (int)((pix / W) % H), b = (int)(pix / ((int64_t)W * H));
+    const int64_t base = (((int64_t)b * 2 * H + 2 * y) * 2 * W + 2 * x) * C + c;
+    const int64_t W2C = (int64_t)2 * W * C;
+    if (!backward) {
+      const __nv_bfloat16 v = in[i];
+      out[base] = v;
+      out[base + C] = v;
+      out[base + W2C] = v;
+      out[base + W2C + C] = v;
+    } else {
+      const float s = __bfloat162float(in[base]) + __bfloat162float(in[base + C]) + __bfloat162float(in[base + W2C]) +
+                      __bfloat162float(in[base + W2C + C]);
+      out[i] = __float2bfloat16(s);
+    }
+  }
+}
+
+// g *= (y > 0): gradient through a ReLU whose output is y
+__global__ void relu_backward_kernel(__nv_bfloat16* __restrict__ g, const __nv_bfloat16* __restrict__ y, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (!(__bfloat162float(y[i]) > 0.0f)) g[i] = __float2bfloat16(0.0f);
+}
+
+// a += b (bf16, for gradients that meet at a skip connection)
+__global__ void add_inplace_kernel(__nv_bfloat16* __restrict__ a, const __nv_bfloat16* __restrict__ b, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    a[i] = __float2bfloat16(__bfloat162float(a[i]) + __bfloat162float(b[i]));
+}
+
+// dbias[c] += sum over pixels of g[p, c]
+__global__ void bias_grad_kernel(const __nv_bfloat16* __restrict__ g, int64_t P, int C, float* __restrict__ db) {
+  extern __shared__ float sh[];
+  for (int c = threadIdx.x; c < C; c += blockDim.x) sh[c] = 0.0f;
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P * C; i += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&sh[i % C], __bfloat162float(g[i]));
+  __syncthreads();
+  for (int c = threadIdx.x; c < C; c += blockDim.x) atomicAdd(&db[c], sh[c]);
+}
+
+// node vector (float, n_nodes = Hn x Wn, node i*Wn + j) -> NHWC C = 16 image (Hp x Wp) with
+// channel 0 = s * r, channel 1 = aux (per-node feature), other channels 0; s = 1/rms(r) read
+// from scale[0] (null: 1).  One image per call (B = 1).
+__global__ void grid_from_vector_kernel(const float* __restrict__ r, const float* __restrict__ aux,
+                                        const float* __restrict__ scale, int Hn, int Wn, int Hp, int Wp,
+                                        __nv_bfloat16* __restrict__ img) {
+  const int64_t total = (int64_t)Hp * Wp;
+  const float s = scale ? scale[0] : 1.0f;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < total; p += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(p / Wp), j = (int)(p % Wp);
+    __align__(16) __nv_bfloat16 h[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) h[c] = __float2bfloat16(0.0f);
+    if (i < Hn && j < Wn) {
+      const int64_t node = (int64_t)i * Wn + j;
+      h[0] = __float2bfloat16(s * r[node]);
+      if (aux) h[1] = __float2bfloat16(aux[node]);
+    }
+    uint4* dst = reinterpret_cast<uint4*>(img + p * 16);
+    dst[0] = reinterpret_cast<uint4*>(h)[0];
+    dst[1] = reinterpret_cast<uint4*>(h)[1];
+  }
+}
+
+// channel 0 of an NHWC image with C channels -> node vector
+__global__ void vector_from_grid_kernel(const __nv_bfloat16* __restrict__ img, int C, int Hn, int Wn, int Wp,
+                                        float* __restrict__ z) {
+  const int64_t total = (int64_t)Hn * Wn;
+  for (int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; node < total;
+       node += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(node / Wn), j = (int)(node % Wn);
+    z[node] = __bfloat162float(img[((int64_t)i * Wp + j) * C]);
+  }
+}
+
+// 1 / rms of a float vector (single block)
+__global__ void inv_rms_kernel(const float* __restrict__ r, int64_t n, float* __restrict__ out) {
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += (double)r[i] * (double)r[i];
+  for (int o = 16; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+    out[0] = t > 0.0 ? (float)(1.0 / sqrt(t / (double)n)) : 1.0f;
+  }
+}
+
+template <int C1, int C2, int COUT, int EPI>
+int launch_conv(const ConvArgs& a, cudaStream_t s) {
+  constexpr int CIN = C1 + C2;
+  const int smem = 9 * CIN * kTile * 2 + 9 * CIN * COUT * 2;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(conv3x3_tc<C1, C2, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+        cudaSuccess)
+      return AGX_ERR_CUDA;
+    attr = true;
+  }
+  const int64_t P = (int64_t)a.B * a.H * a.W;
+  const int grid = (int)((P + kTile - 1) / kTile);
+  conv3x3_tc<C1, C2, COUT, EPI><<<grid, kTile, smem, s>>>(a);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+template <int C1, int C2, int COUT>
+int launch_wgrad(const WgradArgs& a0, cudaStream_t s) {
+  constexpr int CIN = C1 + C2, PCH = 256;
+  const int smem = kTile * PCH * 2 + COUT * PCH * 2;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(wgrad_tc<C1, C2, COUT, PCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+        cudaSuccess)
+      return AGX_ERR_CUDA;
+    attr = true;
+  }
+  WgradArgs a = a0;
+  const int64_t P = (int64_t)a.B * a.H * a.W;
+  a.pix_per_cta = 2048;
+  const dim3 grid((unsigned)((P + a.pix_per_cta - 1) / a.pix_per_cta), (unsigned)((9 * CIN + kTile - 1) / kTile));
+  wgrad_tc<C1, C2, COUT, PCH><<<grid, kTile, smem, s>>>(a);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+int grid1(int64_t n) {
+  int64_t g = (n + 255) / 256;
+  return (int)(g < 152 * 8 ? (g < 1 ? 1 : g) : 152 * 8);
+}
+
+}  // namespace
+
+extern "C" {
+
+int agx_nn_conv3x3(const void* in1, const void* in2, int c1, int c2, const void* wpk, const float* bias, void* out1,
+                   void* out2, int split, int cout, int relu, int B, int H, int W, int* err, void* stream) {
+  ConvArgs a{(const __nv_bfloat16*)in1, (const __nv_bfloat16*)in2, (const __nv_bfloat16*)wpk, bias,
+             (__nv_bfloat16*)out1, (__nv_bfloat16*)out2, split, B, H, W, err};
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!in1 || !wpk || !out1 || !err || B <= 0 || H <= 0 || W <= 0) return AGX_ERR_ARG;
+  if (split <= 0 || split > cout || split % 8 || (split < cout && !out2)) return AGX_ERR_ARG;
+#define AGX_CONV(C1_, C2_, CO_, R_)                                                         \
+  if (c1 == C1_ && c2 == C2_ && cout == CO_ && relu == R_) return launch_conv<C1_, C2_, CO_, R_>(a, s);
+  AGX_CONV(16, 0, 32, 1)
+  AGX_CONV(32, 0, 32, 1)
+  AGX_CONV(32, 32, 32, 1)
+  AGX_CONV(32, 0, 16, 0)
+  // input-gradient convolutions (no epilogue): dOut channels in, layer-input channels out
+  AGX_CONV(32, 0, 16, 0)
+  AGX_CONV(32, 0, 32, 0)
+  AGX_CONV(32, 0, 64, 0)
+  AGX_CONV(16, 0, 32, 0)
+#undef AGX_CONV
+  return AGX_ERR_UNSUPPORTED;
+}
+
+int agx_nn_wgrad3x3(const void* in1, const void* in2, int c1, int c2, const void* dout, int cout, float* dw_rows,
+                    int B, int H, int W, int* err, void* stream) {
+  if (!in1 || !dout || !dw_rows || !err || B <= 0 || H <= 0 || W <= 0) return AGX_ERR_ARG;
+  WgradArgs a{(const __nv_bfloat16*)in1, (const __nv_bfloat16*)in2, (const __nv_bfloat16*)dout, dw_rows, B, H, W, 0,
+              err};
+  cudaStream_t s = (cudaStream_t)stream;
+#define AGX_WG(C1_, C2_, CO_) \
+  if (c1 == C1_ && c2 == C2_ && cout == CO_) return launch_wgrad<C1_, C2_, CO_>(a, s);
+  AGX_WG(16, 0, 32)
+  AGX_WG(32, 0, 32)
+  AGX_WG(32, 32, 32)
+  AGX_WG(32, 0, 16)
+#undef AGX_WG
+  return AGX_ERR_UNSUPPORTED;
+}
+
+int agx_nn_pack_weights(const float* w, int cout, int cin, int mode, void* img, void* stream) {
+  if (!w || !img || cout % 8 || cin % 8) return AGX_ERR_ARG;
+  pack_weights_kernel<<<grid1((int64_t)cout * cin * 9), 256, 0, (cudaStream_t)stream>>>(w, cout, cin, mode,
+                                                                                       (__nv_bfloat16*)img);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+int agx_nn_unpack_wgrad(const float* dw_rows, int cout, int cin, float* dw, void* stream) {
+  unpack_wgrad_kernel<<<grid1((int64_t)cout * cin * 9), 256, 0, (cudaStream_t)stream>>>(dw_rows, cout, cin, dw);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+int agx_nn_pool2(const void* in, void* out, int B, int H, int W, int C, int backward, void* stream) {
+  if (H % 2 || W % 2) return AGX_ERR_ARG;
+  avgpool2_kernel<<<grid1((int64_t)B * H * W * C / 4), 256, 0, (cudaStream_t)stream>>>(
+      (const __nv_bfloat16*)in, (__nv_bfloat16*)out, B, H, W, C, backward);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+int agx_nn_upsample2(const void* in, void* out, int B, int H, int W, int C, int backward, void* stream) {
+  upsample2_kernel<<<grid1((int64_t)B * H * W * C), 256, 0, (cudaStream_t)stream>>>(
+      (const __nv_bfloat16*)in, (__nv_bfloat16*)out, B, H, W, C, backward);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+int agx_nn_relu_backward(void* g, const void* y, int64_t n, void* stream) {
+  relu_backward_kernel<<<grid1(n), 256, 0, (cudaStream_t)stream>>>((__nv_bfloat16*)g, (const __nv_bfloat16*)y, n);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+int agx_nn_add(void* a, const void* b, int64_t n, void* stream) {
+  add_inplace_kernel<<<grid1(n), 256, 0, (cudaStream_t)stream>>>((__nv_bfloat16*)a, (const __nv_bfloat16*)b, n);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+int agx_nn_bias_grad(const void* g, int64_t P, int C, float* db, void* stream) {
+  bias_grad_kernel<<<grid1(P * C), 256, C * sizeof(float), (cudaStream_t)stream>>>((const __nv_bfloat16*)g, P, C, db);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+int agx_nn_grid_from_vector(const float* r, const float* aux, int Hn, int Wn, int Hp, int Wp, int normalize,
+                            float* scale, void* img, void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (normalize) inv_rms_kernel<<<1, 1024, 0, s>>>(r, (int64_t)Hn * Wn, scale);
+  grid_from_vector_kernel<<<grid1((int64_t)Hp * Wp), 256, 0, s>>>(r, aux, normalize ? scale : nullptr, Hn, Wn, Hp, Wp,
+                                                                  (__nv_bfloat16*)img);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+int agx_nn_vector_from_grid(const void* img, int C, int Hn, int Wn, int Wp, float* z, void* stream) {
+  vector_from_grid_kernel<<<grid1((int64_t)Hn * Wn), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)img, C,
+                                                                                    Hn, Wn, Wp, z);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,53 @@
+/*
+ * autopdex_gb300 -- BF16 tensor-core kernels of the learned preconditioner.
+ *
+ * No counterpart in AutoPDEx: these kernels implement the convolutional network that
+ * this backend applies inside flexible CG ('type of preconditioner': 'learned').  Tensors
+ * are NHWC bf16 device arrays; every function launches on `stream` and returns 0 or a
+ * negative status (AGX_ERR_ARG, AGX_ERR_UNSUPPORTED, AGX_ERR_CUDA).  `err` (device int)
+ * is set to 1 by a CTA whose tensor-core work did not complete within its wait limit.
+ */
+#ifndef AUTOPDEX_GB300_NN_H
+#define AUTOPDEX_GB300_NN_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* out = act(conv3x3(concat(in1[c1], in2[c2])) + bias), cout output channels written as
+   out1 (channels [0, split)) and out2 (channels [split, cout)); relu: 0 or 1.  Packed
+   weights from agx_nn_pack_weights (mode 0), or the input-gradient image (mode 1) with
+   in1 = output gradient, no bias and relu = 0. */
+int agx_nn_conv3x3(const void* in1, const void* in2, int c1, int c2, const void* wpk, const float* bias,
+                   void* out1, void* out2, int split, int cout, int relu, int B, int H, int W, int* err,
+                   void* stream);
+/* dw_rows[(tap * (c1 + c2) + ci) * cout + co] += sum over pixels of in(p + tap)[ci] * dout(p)[co] */
+int agx_nn_wgrad3x3(const void* in1, const void* in2, int c1, int c2, const void* dout, int cout, float* dw_rows,
+                    int B, int H, int W, int* err, void* stream);
+/* f32 weights [cout][cin][3][3] -> bf16 operand image; mode 0 forward, 1 input gradient */
+int agx_nn_pack_weights(const float* w, int cout, int cin, int mode, void* img, void* stream);
+/* wgrad rows -> f32 [cout][cin][3][3] */
+int agx_nn_unpack_wgrad(const float* dw_rows, int cout, int cin, float* dw, void* stream);
+/* 2x2 average pooling (backward = 0) or its adjoint (backward = 1); H, W: full size */
+int agx_nn_pool2(const void* in, void* out, int B, int H, int W, int C, int backward, void* stream);
+/* nearest 2x upsampling (backward = 0) or its adjoint; H, W: coarse size */
+int agx_nn_upsample2(const void* in, void* out, int B, int H, int W, int C, int backward, void* stream);
+/* g *= (y > 0) */
+int agx_nn_relu_backward(void* g, const void* y, int64_t n, void* stream);
+/* a += b */
+int agx_nn_add(void* a, const void* b, int64_t n, void* stream);
+/* db[c] += sum over P pixels of g[p][c] */
+int agx_nn_bias_grad(const void* g, int64_t P, int C, float* db, void* stream);
+/* node vector (Hn x Wn, node i*Wn + j) -> NHWC 16-channel image Hp x Wp: channel 0 the
+   vector (scaled to unit rms when normalize; 1/rms written to scale[0]), channel 1 aux */
+int agx_nn_grid_from_vector(const float* r, const float* aux, int Hn, int Wn, int Hp, int Wp, int normalize,
+                            float* scale, void* img, void* stream);
+/* channel 0 of an NHWC image with C channels -> node vector */
+int agx_nn_vector_from_grid(const void* img, int C, int Hn, int Wn, int Wp, float* z, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AUTOPDEX_GB300_NN_H */

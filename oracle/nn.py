@@ -1,0 +1,43 @@
+"""Oracle: the learned preconditioner's U-Net in float64 on the CPU (torch) -- TEST ONLY.
+
+Same layers, parameter names and NHWC tensors as ``autopdex_gb300.learned``: 3x3
+convolutions with zero padding, 2x2 average pooling, nearest 2x upsampling, channel
+concatenation (decoder input first, encoder skip second), ReLU everywhere except the output
+layer.  Gradients come from torch autograd in float64, the reference for the GPU's own
+forward and backward kernels.
+"""
+import torch
+import torch.nn.functional as F
+
+LAYERS = [("e0a", 16, 0, 32, 1), ("e0b", 32, 0, 32, 1), ("e1a", 32, 0, 32, 1), ("e1b", 32, 0, 32, 1),
+          ("e2a", 32, 0, 32, 1), ("e2b", 32, 0, 32, 1), ("b3a", 32, 0, 32, 1), ("b3b", 32, 0, 32, 1),
+          ("d2a", 32, 32, 32, 1), ("d2b", 32, 0, 32, 1), ("d1a", 32, 32, 32, 1), ("d1b", 32, 0, 32, 1),
+          ("d0a", 32, 32, 32, 1), ("d0b", 32, 0, 32, 1), ("out", 32, 0, 16, 0)]
+RELU = {name: relu for name, _, _, _, relu in LAYERS}
+
+
+def conv(x, w, b, relu):
+    """x: (B, H, W, C) -> (B, H, W, Cout); w: (Cout, C, 3, 3)."""
+    y = F.conv2d(x.permute(0, 3, 1, 2), w, b, padding=1).permute(0, 2, 3, 1)
+    return F.relu(y) if relu else y
+
+
+def pool(x):
+    return F.avg_pool2d(x.permute(0, 3, 1, 2), 2).permute(0, 2, 3, 1)
+
+
+def up(x):
+    return F.interpolate(x.permute(0, 3, 1, 2), scale_factor=2, mode="nearest").permute(0, 2, 3, 1)
+
+
+def unet(x, P):
+    """P: dict name -> (w, b) float64 tensors."""
+    c = lambda n, t: conv(t, P[n][0], P[n][1], RELU[n])
+    s0 = c("e0b", c("e0a", x))
+    s1 = c("e1b", c("e1a", pool(s0)))
+    s2 = c("e2b", c("e2a", pool(s1)))
+    b3 = c("b3b", c("b3a", pool(s2)))
+    d2 = c("d2b", c("d2a", torch.cat([up(b3), s2], dim=-1)))
+    d1 = c("d1b", c("d1a", torch.cat([up(d2), s1], dim=-1)))
+    d0 = c("d0b", c("d0a", torch.cat([up(d1), s0], dim=-1)))
+    return c("out", d0)
