@@ -65,12 +65,18 @@ _SIGNATURES = {
     "agx_assemble": (C.c_int, [_P, _P, _P, C.c_int]),
     "agx_get_matrix": (C.c_int, [_P, C.c_int, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(C.c_int64)]),
     "agx_copy_matrix": (C.c_int, [_P, C.c_int, _P, _P, _P]),
+    "agx_copy_values": (C.c_int, [_P, C.c_int, _P]),
+    "agx_spmv_values": (C.c_int, [_P, C.c_int, _P, _P, _P]),
+    "agx_jacobi": (C.c_int, [_P, C.c_int, _P, _P]),
     "agx_spmv": (C.c_int, [_P, C.c_int, _P, _P]),
     "agx_solve": (C.c_int, [_P, _P, _P, C.POINTER(SolveOpts), C.POINTER(SolveInfo)]),
     "agx_newton": (C.c_int, [_P, _P, _P, C.POINTER(NewtonOpts), C.POINTER(NewtonInfo)]),
     "agx_set_preconditioner": (C.c_int, [_P, PRECOND_FN, _P]),
+    "agx_set_preconditioner_mode": (C.c_int, [_P, C.c_int]),
     "agx_profile": (C.c_int, [_P, C.c_int]),
     "agx_profile_read": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    "agx_autotune": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
+    "agx_set_tuning": (C.c_int, [_P, C.c_int]),
     "agx_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
 "agx_pcg_noalloc": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int, _P, _P, C.c_double, C.c_int, _P,
                                 C.POINTER(SolveInfo), C.c_char_p, C.c_int]),

@@ -6,6 +6,7 @@ AutoPDEx reuses a jit compilation per static_settings (utility.py:32-80).  Conne
 coordinate arrays must not be changed in place between calls (JAX arrays cannot be).
 """
 import ctypes as C
+import os
 from collections import OrderedDict
 
 import numpy as np
@@ -171,6 +172,38 @@ class Problem:
             return values.reshape(-1).to(torch.float64).contiguous()
         host = torch.from_numpy(np.ascontiguousarray(flatten(values, self.key)))
         return host.pin_memory().to(self.device, non_blocking=True) if self.n_dofs > 4096 else host.to(self.device)
+
+    def ensure_tuned(self, dofs_dev):
+        """Lanes per block row of the Krylov product from the autotuner, cached per GPU model
+        and problem class in autopdex_gb300/_lib/autotune.json."""
+        if getattr(self, "_tuned", False):
+            return
+        import json
+        from . import build as _b
+        path = os.path.join(_b.LIBDIR, "autotune.json")
+        key = f"{torch.cuda.get_device_name(self.device)}|ndof={self.ndof}|dim={self.dim}|" \
+              f"nnzb=2^{int(np.log2(max(1, self.nnzb)))}"
+        cache = {}
+        try:
+            with open(path) as fh:
+                cache = json.load(fh)
+        except (OSError, ValueError):
+            cache = {}
+        if key in cache:
+            self._call("agx_set_tuning", int(cache[key]["spmv_tpr"]))
+        else:
+            self._call("agx_assemble", C.c_void_p(dofs_dev.data_ptr()), None, N.AGX_F32)
+            tpr = C.c_int()
+            ms = C.c_float()
+            self._call("agx_autotune", C.byref(tpr), C.byref(ms))
+            cache[key] = {"spmv_tpr": int(tpr.value), "spmv_ms": float(ms.value)}
+            try:
+                os.makedirs(os.path.dirname(path), exist_ok=True)
+                with open(path, "w") as fh:
+                    json.dump(cache, fh, indent=1)
+            except OSError:
+                pass
+        self._tuned = True
 
     def matrix(self, dtype):
         rp, col, vals = C.c_void_p(), C.c_void_p(), C.c_void_p()

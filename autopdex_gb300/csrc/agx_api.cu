@@ -56,7 +56,9 @@ void free_device(agx_context* ctx) {
   for (double** p : {&ctx->d_R, &ctx->d_b, &ctx->d_dx, &ctx->d_r, &ctx->d_z, &ctx->d_p, &ctx->d_q, &ctx->d_s,
                      &ctx->d_t, &ctx->d_rhat, &ctx->d_v})
     release(*p);
-  for (float** p : {&ctx->f_x, &ctx->f_r, &ctx->f_z, &ctx->f_p, &ctx->f_q, &ctx->f_rold}) release(*p);
+  for (float** p : {&ctx->f_x, &ctx->f_r, &ctx->f_z, &ctx->f_p, &ctx->f_q, &ctx->f_rold, &ctx->f_w1, &ctx->f_w2,
+                    &ctx->f_w3})
+    release(*p);
   release(ctx->d_partials);
   release(ctx->d_counter);
   release(ctx->d_scal);
@@ -64,6 +66,18 @@ void free_device(agx_context* ctx) {
   for (int c = 0; c < AGX_PROF_CATEGORIES; ++c) {
     for (auto e : ctx->prof_ev[c]) cudaEventDestroy(e);
     ctx->prof_ev[c].clear();
+  }
+  if (ctx->graph_stream) cudaStreamDestroy(ctx->graph_stream);
+  for (auto& e : ctx->graph_ev)
+    if (e) cudaEventDestroy(e);
+  ctx->graph_stream = nullptr;
+  for (auto& gr : ctx->graphs) {
+    if (gr.exec) cudaGraphExecDestroy(gr.exec);
+    gr.exec = nullptr;
+    for (auto& v : gr.ev) {
+      for (auto e : v) cudaEventDestroy(e);
+      v.clear();
+    }
   }
   if (ctx->h_scal) cudaFreeHost(ctx->h_scal);
   if (ctx->h_norm) cudaFreeHost(ctx->h_norm);
@@ -211,7 +225,8 @@ int agx_finalize(agx_context* ctx) {
   for (double** p : {&ctx->d_R, &ctx->d_b, &ctx->d_dx, &ctx->d_r, &ctx->d_z, &ctx->d_p, &ctx->d_q, &ctx->d_s,
                      &ctx->d_t, &ctx->d_rhat, &ctx->d_v, &ctx->d_dinv64})
     if (int rc = alloc(ctx, p, n)) return rc;
-  for (float** p : {&ctx->f_x, &ctx->f_r, &ctx->f_z, &ctx->f_p, &ctx->f_q, &ctx->f_rold, &ctx->d_dinv32})
+  for (float** p : {&ctx->f_x, &ctx->f_r, &ctx->f_z, &ctx->f_p, &ctx->f_q, &ctx->f_rold, &ctx->d_dinv32, &ctx->f_w1,
+                    &ctx->f_w2, &ctx->f_w3})
     if (int rc = alloc(ctx, p, n)) return rc;
   ctx->red_blocks = ctx->sm_count * 8;  // one resident wave of 256-thread blocks
   ctx->vec_blocks = ctx->sm_count * 2;
@@ -318,7 +333,11 @@ int agx_copy_matrix(agx_context* ctx, int dtype, int32_t* rowptr, int32_t* col, 
 int agx_profile(agx_context* ctx, int enable) {
   if (!ctx) return AGX_ERR_ARG;
   ctx->prof_on = enable != 0;
-  for (int c = 0; c < AGX_PROF_CATEGORIES; ++c) ctx->prof_used[c] = 0;
+  for (int c = 0; c < AGX_PROF_CATEGORIES; ++c) {
+    ctx->prof_used[c] = 0;
+    ctx->prof_extra_ms[c] = 0;
+    ctx->prof_extra_n[c] = 0;
+  }
   return AGX_OK;
 }
 
@@ -332,9 +351,11 @@ int agx_profile_read(agx_context* ctx, double* ms, int64_t* launches) {
       AGX_CUDA(ctx, cudaEventElapsedTime(&t, ctx->prof_ev[c][2 * i], ctx->prof_ev[c][2 * i + 1]));
       tot += t;
     }
-    if (ms) ms[c] = tot;
-    if (launches) launches[c] = (int64_t)ctx->prof_used[c];
+    if (ms) ms[c] = tot + ctx->prof_extra_ms[c];
+    if (launches) launches[c] = (int64_t)ctx->prof_used[c] + ctx->prof_extra_n[c];
     ctx->prof_used[c] = 0;
+    ctx->prof_extra_ms[c] = 0;
+    ctx->prof_extra_n[c] = 0;
   }
   return AGX_OK;
 }
@@ -360,10 +381,55 @@ int agx_spmv(agx_context* ctx, int dtype, const void* x, void* y) {
   return agx_spmv_impl(ctx, dtype, x, y);
 }
 
+int agx_spmv_values(agx_context* ctx, int dtype, const void* values, const void* x, void* y) {
+  if (!ctx || !ctx->pattern_ready) return agx_fail(ctx, AGX_ERR_STATE, "agx_finalize first");
+  if (!values || !x || !y) return agx_fail(ctx, AGX_ERR_ARG, "null pointer");
+  if (dtype != AGX_F64 && dtype != AGX_F32) return agx_fail(ctx, AGX_ERR_ARG, "dtype must be AGX_F64 or AGX_F32");
+  return agx_spmv_values_impl(ctx, dtype, values, x, y);
+}
+
+int agx_jacobi(agx_context* ctx, int dtype, const void* r, void* z) {
+  if (!ctx || !ctx->pattern_ready) return agx_fail(ctx, AGX_ERR_STATE, "agx_finalize first");
+  if (ctx->tangent_valid != dtype) return agx_fail(ctx, AGX_ERR_STATE, "no assembled tangent of dtype %d", dtype);
+  if (!r || !z) return agx_fail(ctx, AGX_ERR_ARG, "null pointer");
+  agx_launch_jacobi(ctx, dtype, r, z);
+  AGX_CHECK_LAUNCH(ctx);
+  return AGX_OK;
+}
+
+int agx_copy_values(agx_context* ctx, int dtype, void* values) {
+  if (!ctx || !ctx->pattern_ready || !values) return agx_fail(ctx, AGX_ERR_ARG, "bad arguments");
+  const size_t bs = (size_t)ctx->ndof * ctx->ndof * ctx->nnzb;
+  if (dtype == AGX_F64)
+    AGX_CUDA(ctx, cudaMemcpyAsync(values, ctx->d_vals64, sizeof(double) * bs, cudaMemcpyDeviceToDevice, ctx->stream));
+  else
+    AGX_CUDA(ctx, cudaMemcpyAsync(values, ctx->d_vals32, sizeof(float) * bs, cudaMemcpyDeviceToDevice, ctx->stream));
+  return AGX_OK;
+}
+
 int agx_set_preconditioner(agx_context* ctx, agx_precond_fn fn, void* user) {
   if (!ctx) return AGX_ERR_ARG;
   ctx->precond = fn;
   ctx->precond_user = user;
+  return AGX_OK;
+}
+
+int agx_autotune(agx_context* ctx, int* spmv_tpr, float* spmv_ms) {
+  if (int rc = check_ready(ctx)) return rc;
+  return agx_autotune_spmv(ctx, spmv_tpr, spmv_ms);
+}
+
+int agx_set_tuning(agx_context* ctx, int spmv_tpr) {
+  if (!ctx) return AGX_ERR_ARG;
+  if (spmv_tpr != 0 && spmv_tpr != 2 && spmv_tpr != 4 && spmv_tpr != 8 && spmv_tpr != 16)
+    return agx_fail(ctx, AGX_ERR_ARG, "lanes per row must be 0, 2, 4, 8 or 16");
+  ctx->spmv_tpr = spmv_tpr;
+  return AGX_OK;
+}
+
+int agx_set_preconditioner_mode(agx_context* ctx, int mode) {
+  if (!ctx || mode < 0 || mode > 1) return agx_fail(ctx, AGX_ERR_ARG, "preconditioner mode must be 0 or 1");
+  ctx->precond_mode = mode;
   return AGX_OK;
 }
 

@@ -89,6 +89,7 @@ struct agx_context {
   double *d_s = nullptr, *d_t = nullptr, *d_rhat = nullptr, *d_v = nullptr;
   // single-precision Krylov vectors (mixed precision inner solve)
   float *f_x = nullptr, *f_r = nullptr, *f_z = nullptr, *f_p = nullptr, *f_q = nullptr, *f_rold = nullptr;
+  float *f_w1 = nullptr, *f_w2 = nullptr, *f_w3 = nullptr;  // two-level preconditioner work
 
   // reductions
   int red_blocks = 0;   // largest grid of a reducing kernel (8 per SM)
@@ -107,10 +108,31 @@ struct agx_context {
   bool prof_on = false;
   std::vector<cudaEvent_t> prof_ev[AGX_PROF_CATEGORIES];
   size_t prof_used[AGX_PROF_CATEGORIES] = {0};
+  double prof_extra_ms[AGX_PROF_CATEGORIES] = {0};   // from replayed CUDA graphs
+  int64_t prof_extra_n[AGX_PROF_CATEGORIES] = {0};
+
+  // CUDA graphs of Krylov iteration chunks (one per method slot)
+  struct graph_rec {
+    cudaGraphExec_t exec = nullptr;
+    const void* key_x = nullptr;  // output vector captured in the graph
+    int every = 0;
+    bool prof = false;             // captured with timing events
+    int tpr = 0;                   // lanes per row of the captured products
+    std::vector<cudaEvent_t> ev[AGX_PROF_CATEGORIES];  // event pairs recorded by each replay
+  };
+  graph_rec graphs[2];
+  graph_rec* capturing = nullptr;  // set while a chunk is being captured
+  bool use_graphs = true;
+  // the legacy default stream cannot be captured: graphs then run on this private stream,
+  // ordered against the context stream by events
+  cudaStream_t graph_stream = nullptr;
+  cudaEvent_t graph_ev[2] = {nullptr, nullptr};
 
   // learned preconditioner hook (set by the host layer; null = Jacobi)
   agx_precond_fn precond = nullptr;
   void* precond_user = nullptr;
+  int precond_mode = 1;
+  int spmv_tpr = 0;      // lanes per block row of the Krylov product (0: default; set by the autotuner)  // 0: z = M(r); 1: z = D^-1 r + c M(r - A D^-1 r), c energy-optimal
 };
 
 // ------------------------------------------------------------------------------------
@@ -140,6 +162,9 @@ void agx_launch_newton_update(agx_context* ctx, double* dofs, const double* dx, 
                               double damping);
 void agx_launch_negate_free(agx_context* ctx, const double* R, double* b);
 int agx_spmv_impl(agx_context* ctx, int dtype, const void* x, void* y);
+int agx_spmv_values_impl(agx_context* ctx, int dtype, const void* values, const void* x, void* y);
+void agx_launch_jacobi(agx_context* ctx, int dtype, const void* r, void* z);
+int agx_autotune_spmv(agx_context* ctx, int* chosen, float* best_ms);
 void agx_launch_planes_to_blocks(agx_context* ctx, const double* planes, double* blocks);
 void agx_launch_planes_to_blocks(agx_context* ctx, const float* planes, float* blocks);
 
@@ -150,6 +175,17 @@ struct agx_prof_scope {
   cudaEvent_t stop = nullptr;
   agx_prof_scope(agx_context* c, int k) : ctx(c), cat(k) {
     if (!ctx->prof_on) return;
+    if (ctx->capturing) {  // the graph owns the events; each replay records them again
+      auto& gev = ctx->capturing->ev[cat];
+      cudaEvent_t a, b;
+      if (cudaEventCreate(&a) != cudaSuccess) return;
+      if (cudaEventCreate(&b) != cudaSuccess) return;
+      gev.push_back(a);
+      gev.push_back(b);
+      cudaEventRecord(a, ctx->stream);
+      stop = b;
+      return;
+    }
     auto& ev = ctx->prof_ev[cat];
     size_t u = ctx->prof_used[cat];
     while (ev.size() < 2 * (u + 1)) {

@@ -133,12 +133,13 @@ template <typename T, int NDOF, int TPR>
 __global__ void __launch_bounds__(AGX_BLOCK)
 spmv_dot_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                 const T* __restrict__ vals, int64_t nnzb, const T* __restrict__ z, const T* __restrict__ pold,
-                T* __restrict__ pnew, T* __restrict__ q, agx_krylov_scalars* sc, double* partials, unsigned* counter) {
+                T* __restrict__ pnew, T* __restrict__ q, agx_krylov_scalars* sc, double* partials, unsigned* counter,
+                const T* __restrict__ rflex) {
   if (sc->converged) return;
   const T beta = (T)sc->beta;
   const int sub = threadIdx.x % TPR;
   const int64_t total = ((n_rows * TPR + 31) / 32) * 32;
-  T acc_t = 0;  // per-thread partial in T (a few rows), block and grid sums in float64
+  T acc_t = 0, accr_t = 0;  // per-thread partials in T (a few rows), block and grid sums in float64
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = L / TPR;
     T yr[NDOF];
@@ -151,13 +152,17 @@ spmv_dot_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_
         pnew[d] = pn;
         q[d] = yr[i];
         acc_t += yr[i] * pn;
+        if (rflex) accr_t += rflex[d] * pn;
       }
     }
   }
-  double acc[1] = {(double)acc_t};
-  double tot[1];
-  if (reduce_last_block<1>(acc, partials, counter, tot) && threadIdx.x == 0) {
+  double acc[2] = {(double)acc_t, (double)accr_t};
+  double tot[2];
+  if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
     sc->pq = tot[0];
+    // flexible CG: the step is the exact line minimiser (p, r) / (p, A p), which differs from
+    // (r, z) / (p, A p) once the preconditioner varies from one iteration to the next
+    if (rflex) sc->rz = tot[1];
     // Only a zero or non-finite (p, Ap) is a breakdown: the tangents of clockwise-numbered
     // quads (mesher.py:88-94 numbers quads clockwise, so det J < 0) are negative definite,
     // and CG with a Jacobi preconditioner of the same sign runs as on (-K, -D).
@@ -298,12 +303,53 @@ fcg_direction_dots(int64_t n, const T* __restrict__ r, const T* __restrict__ z, 
 }
 
 template <typename T>
+__global__ void jacobi_dinv(int64_t n, const T* __restrict__ dinv, const T* __restrict__ r, T* __restrict__ z) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    z[i] = dinv[i] * r[i];
+}
+
+template <typename T>
 __global__ void __launch_bounds__(AGX_BLOCK)
 jacobi_apply(int64_t n, const T* __restrict__ dinv, const T* __restrict__ r, T* __restrict__ z,
              const agx_krylov_scalars* sc) {
   if (sc->converged) return;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     z[i] = dinv[i] * r[i];
+}
+
+// ---- two-level application of a registered preconditioner -----------------------------
+// z0 = D^-1 r and r1 = r - t with t = K z0 (t computed before by a product)
+__global__ void __launch_bounds__(AGX_BLOCK)
+tl_residual(int64_t n, const float* __restrict__ r, const float* __restrict__ t, float* __restrict__ r1,
+            const agx_krylov_scalars* sc) {
+  if (sc->converged) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    r1[i] = r[i] - t[i];
+}
+
+// c = (r1, y) / (y, K y) with t = K y; c = 0 when the denominator vanishes
+__global__ void __launch_bounds__(AGX_BLOCK)
+tl_step(int64_t n, const float* __restrict__ r1, const float* __restrict__ y, const float* __restrict__ t,
+        agx_krylov_scalars* sc, double* partials, unsigned* counter) {
+  if (sc->converged) return;
+  float a_t = 0, b_t = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    a_t += r1[i] * y[i];
+    b_t += y[i] * t[i];
+  }
+  double acc[2] = {(double)a_t, (double)b_t};
+  double tot[2];
+  if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0)
+    sc->extra[2] = (isfinite(tot[0]) && isfinite(tot[1]) && tot[1] != 0.0) ? tot[0] / tot[1] : 0.0;
+}
+
+// z = z0 + c y
+__global__ void __launch_bounds__(AGX_BLOCK)
+tl_combine(int64_t n, float* __restrict__ z, const float* __restrict__ y, const agx_krylov_scalars* sc) {
+  if (sc->converged) return;
+  const float c = (float)sc->extra[2];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    z[i] += c * y[i];
 }
 
 // ---- BiCGStab (right Jacobi preconditioning), float64 --------------------------------
@@ -510,30 +556,38 @@ int resident_grid(agx_context* ctx, K kernel) {
   return g < ctx->red_blocks ? g : ctx->red_blocks;
 }
 
-template <typename T>
-void launch_spmv_dot(agx_context* ctx, const T* vals, const T* z, const T* pold, T* pnew, T* q) {
-  agx_prof_scope ps(ctx, AGX_PROF_SPMV);
-  const int64_t nr = ctx->n_nodes;
-  auto* sc = ctx->d_scal;
-#define AGX_SPMV_DOT(ND, TP)                                                                                   \
-  do {                                                                                                         \
-    static int g_cache = 0;                                                                                    \
-    if (!g_cache) g_cache = resident_grid(ctx, spmv_dot_kernel<T, ND, TP>);                                    \
-    spmv_dot_kernel<T, ND, TP><<<g_cache, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, vals,    \
-                                                                       ctx->nnzb, z, pold, pnew, q, sc,        \
-                                                                       ctx->d_partials, ctx->d_counter);       \
-  } while (0)
-  if (ctx->ndof == 1) {
-    if (ctx->dim == 3)
-      AGX_SPMV_DOT(1, 8);
-    else
-      AGX_SPMV_DOT(1, 4);
-  } else if (ctx->ndof == 2) {
-    AGX_SPMV_DOT(2, 4);
-  } else {
-    AGX_SPMV_DOT(3, 8);
+template <typename T, int ND, int TP>
+void spmv_dot_variant(agx_context* ctx, const T* vals, const T* z, const T* pold, T* pnew, T* q, const T* rflex) {
+  static int g_cache = 0;
+  if (!g_cache) g_cache = resident_grid(ctx, spmv_dot_kernel<T, ND, TP>);
+  spmv_dot_kernel<T, ND, TP><<<g_cache, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_nodes, ctx->d_rowptr, ctx->d_col, vals,
+                                                                     ctx->nnzb, z, pold, pnew, q, ctx->d_scal,
+                                                                     ctx->d_partials, ctx->d_counter, rflex);
+}
+
+// default lanes per block row when the autotuner has not chosen one
+int default_tpr(const agx_context* ctx) { return ctx->ndof == 1 ? (ctx->dim == 3 ? 8 : 4) : (ctx->ndof == 2 ? 4 : 8); }
+
+template <typename T, int ND>
+void spmv_dot_nd(agx_context* ctx, int tpr, const T* vals, const T* z, const T* pold, T* pnew, T* q,
+                 const T* rflex) {
+  switch (tpr) {
+    case 2: spmv_dot_variant<T, ND, 2>(ctx, vals, z, pold, pnew, q, rflex); break;
+    case 4: spmv_dot_variant<T, ND, 4>(ctx, vals, z, pold, pnew, q, rflex); break;
+    case 16: spmv_dot_variant<T, ND, 16>(ctx, vals, z, pold, pnew, q, rflex); break;
+    default: spmv_dot_variant<T, ND, 8>(ctx, vals, z, pold, pnew, q, rflex); break;
   }
-#undef AGX_SPMV_DOT
+}
+
+// rflex (flexible CG only): the residual whose dot with the new direction gives the step
+template <typename T>
+void launch_spmv_dot(agx_context* ctx, const T* vals, const T* z, const T* pold, T* pnew, T* q,
+                     const T* rflex = nullptr) {
+  agx_prof_scope ps(ctx, AGX_PROF_SPMV);
+  const int tpr = ctx->spmv_tpr > 0 ? ctx->spmv_tpr : default_tpr(ctx);
+  if (ctx->ndof == 1) spmv_dot_nd<T, 1>(ctx, tpr, vals, z, pold, pnew, q, rflex);
+  else if (ctx->ndof == 2) spmv_dot_nd<T, 2>(ctx, tpr, vals, z, pold, pnew, q, rflex);
+  else spmv_dot_nd<T, 3>(ctx, tpr, vals, z, pold, pnew, q, rflex);
 }
 
 template <int NDOF, int TPR>
@@ -559,6 +613,73 @@ void launch_bicg_spmv(agx_context* ctx, int which, double* a, double* b, double*
   } else {
     launch_bicg_spmvs<3, 8>(ctx, which, a, b, c);
   }
+}
+
+// Issues kn iterations through `chunk`: full chunks of an even length replay a CUDA graph
+// captured at the first use (keyed by the output vector; re-captured when it changes), the
+// remainder is launched directly.
+template <class F>
+int run_chunk(agx_context* ctx, int slot, const void* x, int every, int kn, F&& chunk) {
+  auto& gr = ctx->graphs[slot];
+  // events recorded by graph nodes cannot be timed: profiling runs launch directly
+  if (!ctx->use_graphs || ctx->prof_on || kn != every || every % 2 != 0) {
+    chunk(kn);
+    AGX_CHECK_LAUNCH(ctx);
+    return AGX_OK;
+  }
+  const cudaStream_t work = ctx->stream;
+  const bool legacy = work == nullptr || work == cudaStreamLegacy;
+  if (legacy && !ctx->graph_stream) {
+    AGX_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->graph_stream, cudaStreamNonBlocking));
+    AGX_CUDA(ctx, cudaEventCreateWithFlags(&ctx->graph_ev[0], cudaEventDisableTiming));
+    AGX_CUDA(ctx, cudaEventCreateWithFlags(&ctx->graph_ev[1], cudaEventDisableTiming));
+  }
+  const cudaStream_t gs = legacy ? ctx->graph_stream : work;
+  if (!gr.exec || gr.key_x != x || gr.every != every || gr.prof != ctx->prof_on || gr.tpr != ctx->spmv_tpr) {
+    if (gr.exec) cudaGraphExecDestroy(gr.exec);
+    gr.exec = nullptr;
+    for (auto& v : gr.ev) {
+      for (auto e : v) cudaEventDestroy(e);
+      v.clear();
+    }
+    cudaGraph_t graph = nullptr;
+    AGX_CUDA(ctx, cudaStreamBeginCapture(gs, cudaStreamCaptureModeThreadLocal));
+    ctx->capturing = &gr;
+    ctx->stream = gs;  // the chunk's launches go to the capturing stream
+    chunk(every);
+    ctx->stream = work;
+    ctx->capturing = nullptr;
+    cudaError_t e = cudaStreamEndCapture(gs, &graph);
+    if (e != cudaSuccess) return agx_fail(ctx, AGX_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&gr.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return agx_fail(ctx, AGX_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+    gr.key_x = x;
+    gr.every = every;
+    gr.prof = ctx->prof_on;
+    gr.tpr = ctx->spmv_tpr;
+  }
+  if (legacy) {
+    AGX_CUDA(ctx, cudaEventRecord(ctx->graph_ev[0], work));
+    AGX_CUDA(ctx, cudaStreamWaitEvent(gs, ctx->graph_ev[0], 0));
+    AGX_CUDA(ctx, cudaGraphLaunch(gr.exec, gs));
+    AGX_CUDA(ctx, cudaEventRecord(ctx->graph_ev[1], gs));
+    AGX_CUDA(ctx, cudaStreamWaitEvent(work, ctx->graph_ev[1], 0));
+  } else {
+    AGX_CUDA(ctx, cudaGraphLaunch(gr.exec, work));
+  }
+  if (gr.prof) {
+    // the replay re-recorded the graph's events: add their times once the chunk is done
+    AGX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int c = 0; c < AGX_PROF_CATEGORIES; ++c)
+      for (size_t i = 0; i + 1 < gr.ev[c].size(); i += 2) {
+        float t = 0;
+        AGX_CUDA(ctx, cudaEventElapsedTime(&t, gr.ev[c][i], gr.ev[c][i + 1]));
+        ctx->prof_extra_ms[c] += t;
+        ctx->prof_extra_n[c] += 1;
+      }
+  }
+  return AGX_OK;
 }
 
 int read_scalars(agx_context* ctx) {
@@ -599,12 +720,71 @@ void agx_launch_planes_to_blocks(agx_context* ctx, const float* planes, float* b
   ctx->n_launches += 1;
 }
 
+// Times the fused float32 product for every lanes-per-row candidate on the assembled matrix
+// and keeps the fastest (the Krylov scalars are reset afterwards by the next solve).
+int agx_autotune_spmv(agx_context* ctx, int* chosen, float* best_ms) {
+  if (ctx->tangent_valid != AGX_F32) return agx_fail(ctx, AGX_ERR_STATE, "autotune needs a float32 tangent");
+  const int cands[4] = {2, 4, 8, 16};
+  cudaEvent_t e0, e1;
+  AGX_CUDA(ctx, cudaEventCreate(&e0));
+  AGX_CUDA(ctx, cudaEventCreate(&e1));
+  AGX_CUDA(ctx, cudaMemsetAsync(ctx->d_scal, 0, sizeof(agx_krylov_scalars), ctx->stream));
+  AGX_CUDA(ctx, cudaMemsetAsync(ctx->f_z, 0, sizeof(float) * ctx->n_dofs, ctx->stream));
+  AGX_CUDA(ctx, cudaMemsetAsync(ctx->f_p, 0, sizeof(float) * ctx->n_dofs, ctx->stream));
+  float best = 1e30f;
+  int pick = default_tpr(ctx);
+  for (int c : cands) {
+    if (ctx->ndof == 3 && c == 2) continue;
+    auto run = [&]() {
+      if (ctx->ndof == 1)
+        spmv_dot_nd<float, 1>(ctx, c, ctx->d_vals32, ctx->f_z, ctx->f_p, ctx->f_rold, ctx->f_q, nullptr);
+      else if (ctx->ndof == 2)
+        spmv_dot_nd<float, 2>(ctx, c, ctx->d_vals32, ctx->f_z, ctx->f_p, ctx->f_rold, ctx->f_q, nullptr);
+      else
+        spmv_dot_nd<float, 3>(ctx, c, ctx->d_vals32, ctx->f_z, ctx->f_p, ctx->f_rold, ctx->f_q, nullptr);
+    };
+    for (int w = 0; w < 3; ++w) run();
+    AGX_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+    for (int r = 0; r < 10; ++r) run();
+    AGX_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+    AGX_CUDA(ctx, cudaEventSynchronize(e1));
+    float ms = 0;
+    AGX_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
+    ms /= 10.0f;
+    if (ms < best) {
+      best = ms;
+      pick = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  AGX_CHECK_LAUNCH(ctx);
+  ctx->spmv_tpr = pick;
+  if (chosen) *chosen = pick;
+  if (best_ms) *best_ms = best;
+  return AGX_OK;
+}
+
 int agx_spmv_impl(agx_context* ctx, int dtype, const void* x, void* y) {
+  return agx_spmv_values_impl(ctx, dtype, dtype == AGX_F64 ? (const void*)ctx->d_vals64 : (const void*)ctx->d_vals32,
+                              x, y);
+}
+
+void agx_launch_jacobi(agx_context* ctx, int dtype, const void* r, void* z) {
+  const int gv = agx_grid(ctx, ctx->n_dofs);
+  if (dtype == AGX_F64)
+    jacobi_dinv<double><<<gv, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dofs, ctx->d_dinv64, (const double*)r, (double*)z);
+  else
+    jacobi_dinv<float><<<gv, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dofs, ctx->d_dinv32, (const float*)r, (float*)z);
+  ctx->n_launches += 1;
+}
+
+int agx_spmv_values_impl(agx_context* ctx, int dtype, const void* values, const void* x, void* y) {
   const int64_t nr = ctx->n_nodes;
   const int g = agx_grid(ctx, nr * 8, 8);
   auto go = [&](auto tag) {
     using T = decltype(tag);
-    const T* v = dtype == AGX_F64 ? (const T*)ctx->d_vals64 : (const T*)ctx->d_vals32;
+    const T* v = (const T*)values;
     if (ctx->ndof == 1) {
       if (ctx->dim == 3)
         spmv_kernel<T, 1, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb,
@@ -661,6 +841,32 @@ int agx_residual_norm(agx_context* ctx, const double* R, double* norm2, double* 
   return AGX_OK;
 }
 
+// z = M(r) on the float32 Krylov vectors (f_r -> f_z) for the flexible method
+int apply_registered_preconditioner(agx_context* ctx) {
+  const int64_t n = ctx->n_dofs;
+  const int gv = agx_grid(ctx, n);
+  auto* sc = ctx->d_scal;
+  if (ctx->precond_mode == 0) {
+    if (ctx->precond(ctx->precond_user, ctx->f_r, ctx->f_z, n, ctx->stream) != 0) return -1;
+    zero_prescribed<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir, ctx->d_dir_dofs,
+                                                                                   ctx->f_z);
+    ctx->n_launches += 1;
+    return 0;
+  }
+  jacobi_apply<float><<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv32, ctx->f_r, ctx->f_z, sc);
+  agx_spmv_impl(ctx, AGX_F32, ctx->f_z, ctx->f_w1);
+  tl_residual<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_r, ctx->f_w1, ctx->f_w2, sc);
+  if (ctx->precond(ctx->precond_user, ctx->f_w2, ctx->f_w3, n, ctx->stream) != 0) return -1;
+  zero_prescribed<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir, ctx->d_dir_dofs,
+                                                                                 ctx->f_w3);
+  agx_spmv_impl(ctx, AGX_F32, ctx->f_w3, ctx->f_w1);
+  tl_step<<<ctx->vec_blocks, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_w2, ctx->f_w3, ctx->f_w1, sc, ctx->d_partials,
+                                                        ctx->d_counter);
+  tl_combine<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_z, ctx->f_w3, sc);
+  ctx->n_launches += 7;
+  return 0;
+}
+
 int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_solve_opts* opts, agx_solve_info* info) {
   const int64_t n = ctx->n_dofs;
   const int g = ctx->vec_blocks;  // reducing vector kernels
@@ -686,9 +892,7 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
     int cur = 0;
     pcg_init_kernel<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, rhs, ctx->d_dinv64, x, ctx->d_r, ctx->d_z, pbuf[0],
                                                              sc, ctx->d_partials, ctx->d_counter, 0, 1);
-    while (true) {
-      const int kn = std::min(every, maxiter - it_done);
-      ctx->n_launches += 2 * kn;
+    auto chunk = [&](int kn) {
       for (int k = 0; k < kn; ++k) {
         double* pnew = pbuf[cur ^ 1];
         launch_spmv_dot<double>(ctx, ctx->d_vals64, ctx->d_z, pbuf[cur], pnew, ctx->d_q);
@@ -697,7 +901,11 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
                                                                    ctx->d_dinv64, sc, ctx->d_partials, ctx->d_counter);
         cur ^= 1;
       }
-      AGX_CHECK_LAUNCH(ctx);
+    };
+    while (true) {
+      const int kn = std::min(every, maxiter - it_done);
+      ctx->n_launches += 2 * kn;
+      if (int rc = run_chunk(ctx, 0, x, every, kn, chunk)) return rc;
       int rc = read_scalars(ctx);
       if (rc) return rc;
       it_done = ctx->h_scal->iters;
@@ -705,26 +913,24 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
     }
   } else if (method == AGX_PCG_MIXED || method == AGX_FCG_MIXED) {
     const bool flexible = method == AGX_FCG_MIXED && ctx->precond != nullptr;
+    bool precond_failed = false;
     float* pbuf[2] = {ctx->f_p, ctx->f_rold};
     int cur = 0;
     pcg_init_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, rhs, ctx->d_dinv32, ctx->f_x, ctx->f_r, ctx->f_z,
                                                             pbuf[0], sc, ctx->d_partials, ctx->d_counter, 1,
                                                             flexible ? 0 : 1);
     if (flexible) {
-      if (ctx->precond(ctx->precond_user, ctx->f_r, ctx->f_z, n, ctx->stream) != 0)
+      if (apply_registered_preconditioner(ctx) != 0)
         return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");
-      zero_prescribed<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir, ctx->d_dir_dofs,
-                                                                                     ctx->f_z);
       fcg_direction_dots<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_r, ctx->f_z, ctx->f_q, sc, ctx->d_partials,
                                                                  ctx->d_counter);
       ctx->n_launches += 2;
     }
-    while (true) {
-      const int kn = std::min(every, maxiter - it_done);
-      ctx->n_launches += (flexible ? 4 : 2) * kn;
+    auto chunk = [&](int kn) {
       for (int k = 0; k < kn; ++k) {
         float* pnew = pbuf[cur ^ 1];
-        launch_spmv_dot<float>(ctx, ctx->d_vals32, ctx->f_z, pbuf[cur], pnew, ctx->f_q);
+        launch_spmv_dot<float>(ctx, ctx->d_vals32, ctx->f_z, pbuf[cur], pnew, ctx->f_q,
+                               flexible ? (const float*)ctx->f_r : nullptr);
         if (!flexible) {
           agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
           pcg_update_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, ctx->f_r, ctx->f_z, pnew,
@@ -736,17 +942,26 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
             fcg_update_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, ctx->f_r, pnew, ctx->f_q, sc,
                                                                       ctx->d_partials, ctx->d_counter);
           }
-          agx_prof_scope pp(ctx, AGX_PROF_PRECOND);
-          if (ctx->precond(ctx->precond_user, ctx->f_r, ctx->f_z, n, ctx->stream) != 0)
-            return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");
-          zero_prescribed<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir,
-                                                                                         ctx->d_dir_dofs, ctx->f_z);
+          {
+            agx_prof_scope pp(ctx, AGX_PROF_PRECOND);
+            if (apply_registered_preconditioner(ctx) != 0) precond_failed = true;
+          }
           fcg_direction_dots<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_r, ctx->f_z, ctx->f_q, sc,
                                                                      ctx->d_partials, ctx->d_counter);
         }
         cur ^= 1;
       }
-      AGX_CHECK_LAUNCH(ctx);
+    };
+    while (true) {
+      const int kn = std::min(every, maxiter - it_done);
+      ctx->n_launches += (flexible ? 4 : 2) * kn;
+      if (flexible) {
+        chunk(kn);  // the preconditioner is host code: no graph
+        AGX_CHECK_LAUNCH(ctx);
+        if (precond_failed) return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");
+      } else if (int rc = run_chunk(ctx, 1, ctx->f_x, every, kn, chunk)) {
+        return rc;
+      }
       int rc = read_scalars(ctx);
       if (rc) return rc;
       it_done = ctx->h_scal->iters;

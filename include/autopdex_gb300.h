@@ -161,6 +161,14 @@ int agx_get_matrix(agx_context* ctx, int dtype, const int32_t** rowptr, const in
 int agx_copy_matrix(agx_context* ctx, int dtype, int32_t* rowptr, int32_t* col, void* vals);
 /* y = K x with the last assembled tangent of `dtype` (x, y of that dtype). */
 int agx_spmv(agx_context* ctx, int dtype, const void* x, void* y);
+/* y = K x with the library's pattern and caller-provided values in the library's layout
+   (entry-major planes, as agx_copy_values writes them): products with stored tangents. */
+int agx_spmv_values(agx_context* ctx, int dtype, const void* values, const void* x, void* y);
+/* Raw copy of the last assembled tangent values in the library's layout (nnzb*ndof*ndof). */
+int agx_copy_values(agx_context* ctx, int dtype, void* values);
+/* z = D^-1 r with the diagonal of the last assembled tangent of `dtype` (Jacobi,
+   solver.py:1093-1099). */
+int agx_jacobi(agx_context* ctx, int dtype, const void* r, void* z);
 /* Linear solve K x = rhs on the free DOFs, zeros on prescribed DOFs: the callback
    contract of linear_solve_scipy (solver.py:1493-1539) with an iterative method. */
 int agx_solve(agx_context* ctx, const double* rhs, double* x, const agx_solve_opts* opts,
@@ -171,6 +179,10 @@ int agx_newton(agx_context* ctx, double* dofs, const double* dirichlet_values,
                const agx_newton_opts* opts, agx_newton_info* info);
 /* Registers the preconditioner used by AGX_FCG_MIXED (NULL restores Jacobi). */
 int agx_set_preconditioner(agx_context* ctx, agx_precond_fn fn, void* user);
+/* How AGX_FCG_MIXED applies the registered preconditioner M: 0, z = M(r); 1 (default),
+   two-level: z0 = D^-1 r, r1 = r - K z0, y = M(r1), z = z0 + c y with the energy-optimal
+   c = (r1, y) / (y, K y) -- never a worse step than Jacobi alone. */
+int agx_set_preconditioner_mode(agx_context* ctx, int mode);
 /* Kernel timing.  While enabled, the library brackets its kernel launches with CUDA events
    on its stream and accumulates the elapsed time per category; agx_profile_read
    synchronizes the stream, returns totals (ms) and launch counts, and resets them. */
@@ -198,6 +210,11 @@ int agx_profile_read(agx_context* ctx, double* ms, int64_t* launches);
 int agx_pcg_noalloc(const int32_t* rowptr, const int32_t* col, const double* vals, int64_t n_nodes, int ndof,
                     const double* rhs, double* x, double rtol, int maxiter, void* cuda_stream,
                     agx_solve_info* info, char* errbuf, int errbuf_len);
+/* Autotuner: times every lanes-per-block-row variant of the Krylov product on the last
+   assembled float32 tangent (CUDA events), keeps the fastest and reports it. */
+int agx_autotune(agx_context* ctx, int* spmv_tpr, float* spmv_ms);
+/* Applies a tuning decision (e.g. from the autotuner's cache); 0 restores the default. */
+int agx_set_tuning(agx_context* ctx, int spmv_tpr);
 /* Number of kernels this context has launched since it was created. */
 int agx_launch_count(const agx_context* ctx, int64_t* launches);
 /* Sizes for the host layer: n_dofs, nnzb, ndof. */

@@ -30,9 +30,13 @@ def up(x):
     return F.interpolate(x.permute(0, 3, 1, 2), scale_factor=2, mode="nearest").permute(0, 2, 3, 1)
 
 
-def unet(x, P):
-    """P: dict name -> (w, b) float64 tensors."""
-    c = lambda n, t: conv(t, P[n][0], P[n][1], RELU[n])
+def unet(x, P, masks=None):
+    """P: dict name -> (w, b) float64 tensors.  With ``masks`` (name -> 0/1 tensor), ReLU
+    layers multiply their pre-activation by the given mask instead of thresholding it."""
+    def c(n, t):
+        if masks is not None and RELU[n]:
+            return conv(t, P[n][0], P[n][1], 0) * masks[n]
+        return conv(t, P[n][0], P[n][1], RELU[n])
     s0 = c("e0b", c("e0a", x))
     s1 = c("e1b", c("e1a", pool(s0)))
     s2 = c("e2b", c("e2a", pool(s1)))

@@ -74,8 +74,11 @@ def test_conv_forward_and_gradients(c1, c2, co, relu):
 
 
 def test_unet_forward_and_backward_match_oracle():
+    """Forward against the float64 oracle; parameter gradients against the oracle's autograd
+    with the ReLU masks taken from the GPU's own activations (a pre-activation within bf16
+    rounding of zero may switch sides between precisions, which alone changes gradients by
+    O(1) at that point)."""
     from autopdex_gb300 import learned
-    torch.manual_seed(0)
     net = learned.UNet(seed=3)
     B, H, W = 2, 32, 48
     g = torch.Generator().manual_seed(5)
@@ -84,11 +87,12 @@ def test_unet_forward_and_backward_match_oracle():
     out, acts = net.forward(x.to(torch.bfloat16).cuda(), keep=True)
     P = {n: (_bf(net.w[n].double().cpu()).requires_grad_(True), net.b[n].double().cpu().requires_grad_(True))
          for n, *_ in learned.LAYERS}
-    ref = onn.unet(x, P)
-    got = out.double().cpu()
-    assert (got - ref.detach()).abs().max() <= 5e-2 * ref.abs().max()
+    ref = onn.unet(x, {n: (w.detach(), b.detach()) for n, (w, b) in P.items()})
+    assert (out.double().cpu() - ref).abs().max() <= 5e-2 * ref.abs().max()
+    masks = {n: (acts[n].double().cpu() > 0).double() for n, c1, c2, co, relu in learned.LAYERS if relu}
+    ref_m = onn.unet(x, P, masks=masks)
     gy = _bf(torch.randn(B, H, W, 16, generator=g, dtype=torch.float64))
-    (ref * gy).sum().backward()
+    (ref_m * gy).sum().backward()
     gw, gb = net.backward(gy.to(torch.bfloat16).cuda(), acts)
     torch.cuda.synchronize()
     net.check()
@@ -97,7 +101,7 @@ def test_unet_forward_and_backward_match_oracle():
         rw, rb = P[n][0].grad, P[n][1].grad
         rel[n] = (float((gw[n].double().cpu() - rw).norm() / rw.norm()),
                   float((gb[n].double().cpu() - rb).norm() / rb.norm().clamp_min(1e-12)))
-    assert all(a <= 1e-1 and b <= 1e-1 for a, b in rel.values()), rel
+    assert all(a <= 3e-2 and b <= 3e-2 for a, b in rel.values()), rel
 
 
 def test_trained_network_reduces_fcg_iterations():
