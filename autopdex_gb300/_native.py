@@ -11,6 +11,7 @@ from . import build as _build
 
 AGX_OK = 0
 AGX_NOT_CONVERGED = 1
+AGX_PRECOND_CAPTURABLE = 1
 AGX_DIVERGED = 2
 
 AGX_QUAD4, AGX_HEX8, AGX_LINE2 = 0, 1, 2
@@ -72,7 +73,7 @@ _SIGNATURES = {
     "agx_solve": (C.c_int, [_P, _P, _P, C.POINTER(SolveOpts), C.POINTER(SolveInfo)]),
     "agx_newton": (C.c_int, [_P, _P, _P, C.POINTER(NewtonOpts), C.POINTER(NewtonInfo)]),
     "agx_set_preconditioner": (C.c_int, [_P, PRECOND_FN, _P]),
-    "agx_set_preconditioner_mode": (C.c_int, [_P, C.c_int]),
+    "agx_set_preconditioner_mode": (C.c_int, [_P, C.c_int, C.c_double, C.c_int, C.c_int]),
     "agx_profile": (C.c_int, [_P, C.c_int]),
     "agx_profile_read": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     "agx_autotune": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
@@ -93,6 +94,8 @@ _SIGNATURES = {
     "agx_nn_add": (C.c_int, [_P, _P, C.c_int64, _P]),
     "agx_nn_bias_grad": (C.c_int, [_P, C.c_int64, C.c_int, _P, _P]),
     "agx_nn_grid_from_vector": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, _P]),
+    "agx_nn_restrict": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, _P, _P]),
+    "agx_nn_prolong": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P]),
     "agx_nn_vector_from_grid": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P]),
 }
 

@@ -57,7 +57,7 @@ void free_device(agx_context* ctx) {
                      &ctx->d_t, &ctx->d_rhat, &ctx->d_v})
     release(*p);
   for (float** p : {&ctx->f_x, &ctx->f_r, &ctx->f_z, &ctx->f_p, &ctx->f_q, &ctx->f_rold, &ctx->f_w1, &ctx->f_w2,
-                    &ctx->f_w3})
+                    &ctx->f_w3, &ctx->f_w4})
     release(*p);
   release(ctx->d_partials);
   release(ctx->d_counter);
@@ -226,7 +226,7 @@ int agx_finalize(agx_context* ctx) {
                      &ctx->d_t, &ctx->d_rhat, &ctx->d_v, &ctx->d_dinv64})
     if (int rc = alloc(ctx, p, n)) return rc;
   for (float** p : {&ctx->f_x, &ctx->f_r, &ctx->f_z, &ctx->f_p, &ctx->f_q, &ctx->f_rold, &ctx->d_dinv32, &ctx->f_w1,
-                    &ctx->f_w2, &ctx->f_w3})
+                    &ctx->f_w2, &ctx->f_w3, &ctx->f_w4})
     if (int rc = alloc(ctx, p, n)) return rc;
   ctx->red_blocks = ctx->sm_count * 8;  // one resident wave of 256-thread blocks
   ctx->vec_blocks = ctx->sm_count * 2;
@@ -411,6 +411,7 @@ int agx_set_preconditioner(agx_context* ctx, agx_precond_fn fn, void* user) {
   if (!ctx) return AGX_ERR_ARG;
   ctx->precond = fn;
   ctx->precond_user = user;
+  ctx->precond_gen += 1;
   return AGX_OK;
 }
 
@@ -427,9 +428,16 @@ int agx_set_tuning(agx_context* ctx, int spmv_tpr) {
   return AGX_OK;
 }
 
-int agx_set_preconditioner_mode(agx_context* ctx, int mode) {
-  if (!ctx || mode < 0 || mode > 1) return agx_fail(ctx, AGX_ERR_ARG, "preconditioner mode must be 0 or 1");
+int agx_set_preconditioner_mode(agx_context* ctx, int mode, double omega, int sweeps, int flags) {
+  if (!ctx || mode < 0 || mode > 2) return agx_fail(ctx, AGX_ERR_ARG, "preconditioner mode must be 0, 1 or 2");
+  if (!(omega > 0.0 && omega <= 1.0)) return agx_fail(ctx, AGX_ERR_ARG, "Jacobi damping must lie in (0, 1]");
+  if (sweeps < 1 || sweeps > 16) return agx_fail(ctx, AGX_ERR_ARG, "smoothing sweeps must lie in 1 .. 16");
+  if (flags & ~AGX_PRECOND_CAPTURABLE) return agx_fail(ctx, AGX_ERR_ARG, "unknown preconditioner flags");
   ctx->precond_mode = mode;
+  ctx->precond_omega = omega;
+  ctx->precond_sweeps = sweeps;
+  ctx->precond_capturable = (flags & AGX_PRECOND_CAPTURABLE) != 0;
+  ctx->precond_gen += 1;
   return AGX_OK;
 }
 

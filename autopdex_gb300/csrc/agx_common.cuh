@@ -89,7 +89,7 @@ struct agx_context {
   double *d_s = nullptr, *d_t = nullptr, *d_rhat = nullptr, *d_v = nullptr;
   // single-precision Krylov vectors (mixed precision inner solve)
   float *f_x = nullptr, *f_r = nullptr, *f_z = nullptr, *f_p = nullptr, *f_q = nullptr, *f_rold = nullptr;
-  float *f_w1 = nullptr, *f_w2 = nullptr, *f_w3 = nullptr;  // two-level preconditioner work
+  float *f_w1 = nullptr, *f_w2 = nullptr, *f_w3 = nullptr, *f_w4 = nullptr;  // two-level preconditioner work
 
   // reductions
   int red_blocks = 0;   // largest grid of a reducing kernel (8 per SM)
@@ -115,6 +115,7 @@ struct agx_context {
   struct graph_rec {
     cudaGraphExec_t exec = nullptr;
     const void* key_x = nullptr;  // output vector captured in the graph
+    int64_t pc_key = -1;          // preconditioner generation captured (flexible CG), else -1
     int every = 0;
     bool prof = false;             // captured with timing events
     int tpr = 0;                   // lanes per row of the captured products
@@ -131,7 +132,11 @@ struct agx_context {
   // learned preconditioner hook (set by the host layer; null = Jacobi)
   agx_precond_fn precond = nullptr;
   void* precond_user = nullptr;
-  int precond_mode = 1;
+  int precond_mode = 2;
+  double precond_omega = 2.0 / 3.0;
+  int precond_sweeps = 1;
+  int precond_capturable = 0;  // the callback only enqueues work on the stream it is given
+  int64_t precond_gen = 0;     // bumped whenever the callback or its mode changes
   int spmv_tpr = 0;      // lanes per block row of the Krylov product (0: default; set by the autotuner)  // 0: z = M(r); 1: z = D^-1 r + c M(r - A D^-1 r), c energy-optimal
 };
 

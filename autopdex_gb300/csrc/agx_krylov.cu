@@ -318,16 +318,30 @@ jacobi_apply(int64_t n, const T* __restrict__ dinv, const T* __restrict__ r, T* 
 }
 
 // ---- two-level application of a registered preconditioner -----------------------------
-// z0 = D^-1 r and r1 = r - t with t = K z0 (t computed before by a product)
+// One damped Jacobi sweep on the running residual: rc = rin - t (t = K dz of the previous
+// sweep, or none), dz = w D^-1 rc, z = dz (first sweep) or z + dz.
 __global__ void __launch_bounds__(AGX_BLOCK)
-tl_residual(int64_t n, const float* __restrict__ r, const float* __restrict__ t, float* __restrict__ r1,
-            const agx_krylov_scalars* sc) {
+tl_sweep(int64_t n, const float* __restrict__ dinv, float w, const float* rin, float* rc, const float* __restrict__ t,
+         float* __restrict__ z, float* __restrict__ dz, int first, const agx_krylov_scalars* sc) {
   if (sc->converged) return;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    r1[i] = r[i] - t[i];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float v = t ? rin[i] - t[i] : rin[i];
+    rc[i] = v;
+    const float d = w * dinv[i] * v;
+    dz[i] = d;
+    z[i] = first ? d : z[i] + d;
+  }
 }
 
-// c = (r1, y) / (y, K y) with t = K y; c = 0 when the denominator vanishes
+// rc -= t
+__global__ void __launch_bounds__(AGX_BLOCK)
+tl_residual(int64_t n, float* __restrict__ rc, const float* __restrict__ t, const agx_krylov_scalars* sc) {
+  if (sc->converged) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    rc[i] -= t[i];
+}
+
+// c = (rc, y) / (y, K y) with t = K y; c = 0 when the denominator vanishes
 __global__ void __launch_bounds__(AGX_BLOCK)
 tl_step(int64_t n, const float* __restrict__ r1, const float* __restrict__ y, const float* __restrict__ t,
         agx_krylov_scalars* sc, double* partials, unsigned* counter) {
@@ -343,13 +357,16 @@ tl_step(int64_t n, const float* __restrict__ r1, const float* __restrict__ y, co
     sc->extra[2] = (isfinite(tot[0]) && isfinite(tot[1]) && tot[1] != 0.0) ? tot[0] / tot[1] : 0.0;
 }
 
-// z = z0 + c y
+// z += c y; rc -= c t (t = K y): rc stays r - K z
 __global__ void __launch_bounds__(AGX_BLOCK)
-tl_combine(int64_t n, float* __restrict__ z, const float* __restrict__ y, const agx_krylov_scalars* sc) {
+tl_combine(int64_t n, float* __restrict__ z, const float* __restrict__ y, float* __restrict__ rc,
+           const float* __restrict__ t, const agx_krylov_scalars* sc) {
   if (sc->converged) return;
   const float c = (float)sc->extra[2];
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     z[i] += c * y[i];
+    rc[i] -= c * t[i];
+  }
 }
 
 // ---- BiCGStab (right Jacobi preconditioning), float64 --------------------------------
@@ -619,7 +636,7 @@ void launch_bicg_spmv(agx_context* ctx, int which, double* a, double* b, double*
 // captured at the first use (keyed by the output vector; re-captured when it changes), the
 // remainder is launched directly.
 template <class F>
-int run_chunk(agx_context* ctx, int slot, const void* x, int every, int kn, F&& chunk) {
+int run_chunk(agx_context* ctx, int slot, const void* x, int every, int kn, F&& chunk, int64_t pc_key = -1) {
   auto& gr = ctx->graphs[slot];
   // events recorded by graph nodes cannot be timed: profiling runs launch directly
   if (!ctx->use_graphs || ctx->prof_on || kn != every || every % 2 != 0) {
@@ -635,7 +652,8 @@ int run_chunk(agx_context* ctx, int slot, const void* x, int every, int kn, F&& 
     AGX_CUDA(ctx, cudaEventCreateWithFlags(&ctx->graph_ev[1], cudaEventDisableTiming));
   }
   const cudaStream_t gs = legacy ? ctx->graph_stream : work;
-  if (!gr.exec || gr.key_x != x || gr.every != every || gr.prof != ctx->prof_on || gr.tpr != ctx->spmv_tpr) {
+  if (!gr.exec || gr.key_x != x || gr.every != every || gr.prof != ctx->prof_on || gr.tpr != ctx->spmv_tpr ||
+      gr.pc_key != pc_key) {
     if (gr.exec) cudaGraphExecDestroy(gr.exec);
     gr.exec = nullptr;
     for (auto& v : gr.ev) {
@@ -658,6 +676,7 @@ int run_chunk(agx_context* ctx, int slot, const void* x, int every, int kn, F&& 
     gr.every = every;
     gr.prof = ctx->prof_on;
     gr.tpr = ctx->spmv_tpr;
+    gr.pc_key = pc_key;
   }
   if (legacy) {
     AGX_CUDA(ctx, cudaEventRecord(ctx->graph_ev[0], work));
@@ -853,17 +872,32 @@ int apply_registered_preconditioner(agx_context* ctx) {
     ctx->n_launches += 1;
     return 0;
   }
-  jacobi_apply<float><<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv32, ctx->f_r, ctx->f_z, sc);
-  agx_spmv_impl(ctx, AGX_F32, ctx->f_z, ctx->f_w1);
-  tl_residual<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_r, ctx->f_w1, ctx->f_w2, sc);
-  if (ctx->precond(ctx->precond_user, ctx->f_w2, ctx->f_w3, n, ctx->stream) != 0) return -1;
-  zero_prescribed<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir, ctx->d_dir_dofs,
-                                                                                 ctx->f_w3);
-  agx_spmv_impl(ctx, AGX_F32, ctx->f_w3, ctx->f_w1);
-  tl_step<<<ctx->vec_blocks, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_w2, ctx->f_w3, ctx->f_w1, sc, ctx->d_partials,
-                                                        ctx->d_counter);
-  tl_combine<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_z, ctx->f_w3, sc);
-  ctx->n_launches += 7;
+  // nu damped Jacobi sweeps from z = 0 (the running residual rc = r - K z in f_w2, the
+  // last increment in f_w4, products in f_w1), then y = M(rc) in f_w3 with the
+  // energy-optimal step c = (rc, y) / (y, K y), z += c y, and in mode 2 nu post-sweeps
+  const float w = (float)ctx->precond_omega;
+  const int nu = ctx->precond_sweeps;
+  float *rc = ctx->f_w2, *t = ctx->f_w1, *y = ctx->f_w3, *dz = ctx->f_w4;
+  for (int s = 0; s < nu; ++s) {
+    tl_sweep<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv32, w, s == 0 ? ctx->f_r : rc, rc, s == 0 ? nullptr : t,
+                                                ctx->f_z, dz, s == 0, sc);
+    agx_spmv_impl(ctx, AGX_F32, dz, t);
+  }
+  tl_residual<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, rc, t, sc);
+  if (ctx->precond(ctx->precond_user, rc, y, n, ctx->stream) != 0) return -1;
+  zero_prescribed<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir, ctx->d_dir_dofs, y);
+  agx_spmv_impl(ctx, AGX_F32, y, t);
+  tl_step<<<ctx->vec_blocks, AGX_BLOCK, 0, ctx->stream>>>(n, rc, y, t, sc, ctx->d_partials, ctx->d_counter);
+  tl_combine<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_z, y, rc, t, sc);
+  ctx->n_launches += 2 * nu + 5;
+  if (ctx->precond_mode == 2) {
+    for (int s = 0; s < nu; ++s) {
+      tl_sweep<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv32, w, rc, rc, s == 0 ? nullptr : t, ctx->f_z, dz, 0,
+                                                  sc);
+      if (s + 1 < nu) agx_spmv_impl(ctx, AGX_F32, dz, t);
+    }
+    ctx->n_launches += 2 * nu - 1;
+  }
   return 0;
 }
 
@@ -955,13 +989,13 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
     while (true) {
       const int kn = std::min(every, maxiter - it_done);
       ctx->n_launches += (flexible ? 4 : 2) * kn;
-      if (flexible) {
-        chunk(kn);  // the preconditioner is host code: no graph
+      if (flexible && !ctx->precond_capturable) {
+        chunk(kn);  // a preconditioner that may synchronise or allocate: no graph
         AGX_CHECK_LAUNCH(ctx);
-        if (precond_failed) return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");
-      } else if (int rc = run_chunk(ctx, 1, ctx->f_x, every, kn, chunk)) {
+      } else if (int rc = run_chunk(ctx, 1, ctx->f_x, every, kn, chunk, flexible ? ctx->precond_gen : -1)) {
         return rc;
       }
+      if (precond_failed) return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");
       int rc = read_scalars(ctx);
       if (rc) return rc;
       it_done = ctx->h_scal->iters;

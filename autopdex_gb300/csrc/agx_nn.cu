@@ -4,9 +4,9 @@
 //
 // Tensors are NHWC bf16 with 16, 32 or 64 channels.  A 3x3 convolution (stride 1, zero
 // padding 1) is an implicit GEMM D[pixel, cout] = sum_k A[pixel, k] B[cout, k] with
-// k = tap * CIN + cin: each CTA gathers the A rows of 128 output pixels (all nine taps) and
-// the packed weight image into shared memory in the no-swizzle K-major core-matrix layout
-// (8 rows x 16 bytes per core matrix), one thread issues tcgen05.mma (kind::f16, bf16 in,
+// k = tap * CIN + cin: each persistent CTA holds the packed weight image and double-buffered
+// input halos of 128-pixel row tiles in shared memory in the no-swizzle K-major core-matrix
+// layout (8 rows x 16 bytes per core matrix), one thread issues tcgen05.mma (kind::f16, bf16 in,
 // f32 accumulate, M = 128, N = COUT, K = 16 per instruction) into a TMEM accumulator, the
 // MMA completion is committed to an mbarrier, and the four warps read their 32 TMEM lanes
 // back with tcgen05.ld for the epilogue (bias, ReLU, bf16 store).  The input gradient is the
@@ -15,7 +15,9 @@
 //
 // Every wait is bounded: a CTA whose MMA does not complete in time records an error flag
 // and still releases its TMEM.
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 
 #include "agx_common.cuh"
 
@@ -106,99 +108,195 @@ struct ConvArgs {
   int* err;
 };
 
-// out = epi(conv3x3(concat(in1, in2)) + bias); EPI 0: identity, 1: ReLU
+// out = epi(conv3x3(concat(in1, in2)) + bias); EPI 0: identity, 1: ReLU.
+//
+// Persistent over row tiles of 128 output pixels (b, y, x0 .. x0 + 127).  A tile's input is a
+// halo of 3 rows x 130 pixels, stored as CIN / 8 channel planes of 16-byte pixel chunks
+// (plane c holds channels 8c .. 8c + 7 of every halo pixel, 16 bytes apart): each plane is one
+// TMA box {8 channels, 130 pixels, 3 rows} of the NHWC tensor, with the zero fill of the
+// tensor copy supplying the padding.  In that layout the A operand of tap (dy, dx) -- 128
+// pixels x 16 channels -- is a no-swizzle K-major view starting at halo pixel
+// ((dy + 1) * 130 + dx + 1) of plane 2 kc: 8-pixel core matrices 128 bytes apart (SBO) and
+// channel chunks one plane apart (LBO), so the nine taps are nine descriptors over one copy of
+// the input instead of a nine-fold gather.  The packed weights stay in shared memory for the
+// CTA's lifetime.  Halos cycle through kStages buffers filled kStages - 1 tiles ahead (one
+// mbarrier each, completed by the copies' transaction bytes), and the accumulator alternates
+// between two TMEM column ranges, so the MMAs of tile k run while the four warps drain tile
+// k - 1 through tcgen05.ld, and the copies of tiles k + 1 .. k + kStages - 1 are in flight.
+constexpr int kHaloW = kTile + 2;                 // halo pixels per row
+constexpr int kHaloPx = 3 * kHaloW;               // halo pixels per tile
+constexpr int kPlaneData = kHaloPx * 16;          // bytes one TMA box writes
+constexpr int kPlaneBytes = (kPlaneData + 127) / 128 * 128;  // plane stride (128-byte aligned)
+constexpr int kStages = 3;                        // halo buffers in the ring
+
+struct ConvMaps {
+  CUtensorMap in1;  // {C1, W, H, B} bf16, box {8, 130, 3, 1}
+  CUtensorMap in2;  // {C2, W, H, B}, unused when C2 == 0
+};
+
+__device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tma_load4(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                          uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+      : "memory");
+}
+
+// one thread: the CIN / 8 plane copies of a tile's halo, completing on `bar`
+template <int C1, int C2>
+__device__ __forceinline__ void issue_halo(const ConvMaps& m, const ConvArgs& a, int64_t tile, int tiles_x,
+                                           uint32_t halo, uint32_t bar) {
+  constexpr int NCH = (C1 + C2) / 8;
+  const int64_t row = tile / tiles_x;  // b * H + y
+  const int x0 = (int)(tile - row * tiles_x) * kTile;
+  const int b = (int)(row / a.H), y = (int)(row - (int64_t)b * a.H);
+  mbar_expect(bar, (uint32_t)(NCH * kPlaneData));
+#pragma unroll
+  for (int c = 0; c < C1 / 8; ++c) tma_load4(halo + (uint32_t)(c * kPlaneBytes), &m.in1, 8 * c, x0 - 1, y - 1, b, bar);
+  if constexpr (C2 > 0) {
+#pragma unroll
+    for (int c = 0; c < C2 / 8; ++c)
+      tma_load4(halo + (uint32_t)((C1 / 8 + c) * kPlaneBytes), &m.in2, 8 * c, x0 - 1, y - 1, b, bar);
+  }
+}
+
+template <int COUT, int EPI>
+__device__ __forceinline__ void conv_epilogue(const ConvArgs& a, uint32_t tacc, int64_t tile, int tiles_x, int tid,
+                                              int warp) {
+  float acc[COUT];
+#pragma unroll
+  for (int c = 0; c < COUT; c += 16) tmem_ld16(tacc + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, acc + c);
+  const int64_t row = tile / tiles_x;
+  const int x = (int)(tile - row * tiles_x) * kTile + tid;
+  if (x >= a.W) return;
+  const int64_t p = row * a.W + x;
+#pragma unroll
+  for (int c = 0; c < COUT; ++c) {
+    float v = acc[c] + (a.bias ? a.bias[c] : 0.0f);
+    if (EPI == 1) v = fmaxf(v, 0.0f);
+    acc[c] = v;
+  }
+  const int S = a.split;
+#pragma unroll
+  for (int c0 = 0; c0 < COUT; c0 += 8) {
+    __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) h[u] = __float2bfloat16(acc[c0 + u]);
+    if (c0 < S)
+      *reinterpret_cast<uint4*>(a.out1 + p * S + c0) = *reinterpret_cast<uint4*>(h);
+    else
+      *reinterpret_cast<uint4*>(a.out2 + p * (COUT - S) + (c0 - S)) = *reinterpret_cast<uint4*>(h);
+  }
+}
+
 template <int C1, int C2, int COUT, int EPI>
-__global__ void __launch_bounds__(kTile) conv3x3_tc(ConvArgs a) {
-  constexpr int CIN = C1 + C2, K = 9 * CIN, NG = COUT / 8;
-  constexpr int A_BYTES = K * kTile * 2;
-  constexpr int NCOLS = tmem_cols(COUT);
+__global__ void __launch_bounds__(kTile) conv3x3_tc(const __grid_constant__ ConvMaps maps, ConvArgs a) {
+  constexpr int CIN = C1 + C2, K = 9 * CIN, NG = COUT / 8, NCH = CIN / 8;
+  constexpr int B_BYTES = K * COUT * 2;
+  constexpr int HALO_BYTES = NCH * kPlaneBytes;
+  constexpr int NCOLS = tmem_cols(2 * COUT);  // two accumulators
   static_assert(CIN % 16 == 0 && COUT % 16 == 0, "channel counts must be multiples of 16");
+  static_assert(B_BYTES % 1024 == 0 && HALO_BYTES % 128 == 0, "shared-memory carve-up");
   extern __shared__ __align__(1024) unsigned char smem[];
-  unsigned char* sA = smem;
-  unsigned char* sB = smem + A_BYTES;
+  unsigned char* sB = smem;
   __shared__ uint32_t tmem_slot;
-  __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t full_bar[kStages];
+  __shared__ __align__(8) uint64_t mma_bar[2];
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int64_t HW = (int64_t)a.H * a.W, P = HW * a.B;
-  const int64_t p = (int64_t)blockIdx.x * kTile + tid;
-  const bool pv = p < P;
-  int b = 0, y = 0, x = 0;
-  if (pv) {
-    b = (int)(p / HW);
-    const int64_t rem = p - (int64_t)b * HW;
-    y = (int)(rem / a.W);
-    x = (int)(rem - (int64_t)y * a.W);
+  const int tiles_x = (a.W + kTile - 1) / kTile;
+  const int64_t ntiles = (int64_t)a.B * a.H * tiles_x;
+  const int64_t first = blockIdx.x, stride = gridDim.x;
+  const int64_t my_tiles = first < ntiles ? (ntiles - first + stride - 1) / stride : 0;
+  const uint32_t b0 = (uint32_t)__cvta_generic_to_shared(sB);
+  const uint32_t halo_base = b0 + B_BYTES;
+  const uint32_t fbar0 = (uint32_t)__cvta_generic_to_shared(&full_bar[0]);
+  const uint32_t mbar0 = (uint32_t)__cvta_generic_to_shared(&mma_bar[0]);
+  if (tid == 0) {
+#pragma unroll
+    for (int s = 0; s < kStages; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(fbar0 + 8u * s));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar0));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar0 + 8u));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    // prologue: the first kStages halos of this CTA, one per buffer
+    for (int j = 0; j < kStages && j < my_tiles; ++j)
+      issue_halo<C1, C2>(maps, a, first + j * stride, tiles_x, halo_base + (uint32_t)(j * HALO_BYTES), fbar0 + 8u * j);
   }
-  // gather the A rows of this thread's pixel: nine taps, CIN channels, 16-byte chunks
-#pragma unroll
-  for (int t = 0; t < 9; ++t) {
-    const int yy = y + t / 3 - 1, xx = x + t % 3 - 1;
-    const bool ok = pv && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
-    const int64_t q = ((int64_t)b * a.H + yy) * a.W + xx;
-#pragma unroll
-    for (int j = 0; j < C1 / 8; ++j) {
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (ok) v = reinterpret_cast<const uint4*>(a.in1 + q * C1)[j];
-      *reinterpret_cast<uint4*>(sA + core_off(tid, t * CIN + 8 * j, kTile / 8)) = v;
-    }
-    if constexpr (C2 > 0) {
-#pragma unroll
-      for (int j = 0; j < C2 / 8; ++j) {
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (ok) v = reinterpret_cast<const uint4*>(a.in2 + q * C2)[j];
-        *reinterpret_cast<uint4*>(sA + core_off(tid, t * CIN + C1 + 8 * j, kTile / 8)) = v;
-      }
-    }
-  }
-  // packed weights: already in core-matrix order
-  for (int i = tid; i < K * COUT * 2 / 16; i += kTile)
+  // packed weights: already in core-matrix order (generic-proxy stores, fenced for the MMAs)
+  for (int i = tid; i < B_BYTES / 16; i += kTile)
     reinterpret_cast<uint4*>(sB)[i] = reinterpret_cast<const uint4*>(a.wpk)[i];
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  const uint32_t mbar_addr = (uint32_t)__cvta_generic_to_shared(&mbar);
-  if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_addr) : "memory");
   if (warp == 0) tmem_alloc<NCOLS>(&tmem_slot);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_slot;
-  if (tid == 0) {
-    const uint32_t a0 = (uint32_t)__cvta_generic_to_shared(sA), b0 = (uint32_t)__cvta_generic_to_shared(sB);
-    const uint32_t id = idesc_bf16(kTile, COUT);
-#pragma unroll 1
-    for (int s = 0; s < K / 16; ++s) {
-      const uint64_t da = smem_desc(a0 + (uint32_t)(2 * s * (kTile / 8)) * 128u, (kTile / 8) * 128, 128);
-      const uint64_t db = smem_desc(b0 + (uint32_t)(2 * s * NG) * 128u, NG * 128, 128);
-      mma_bf16(tmem, da, db, id, s > 0 ? 1u : 0u);
-    }
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_addr)
-                 : "memory");
-  }
-  const int done = mbar_wait(mbar_addr, 0);
-  if (!done && tid == 0) atomicExch(a.err, 1);
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (done) {
-    float acc[COUT];
+  const uint32_t id = idesc_bf16(kTile, COUT);
+  int ok = 1;
+  int64_t issued = kStages < my_tiles ? kStages : my_tiles;  // halos issued so far (thread 0's count)
+  int64_t consumed = 0;                                       // halos waited for by thread 0
+  for (int64_t k = 0; k <= my_tiles && ok; ++k) {
+    // (1) MMAs of tile k into accumulator k % 2 (its previous use, tile k - 2, was drained
+    //     before the barrier that closed the last iteration)
+    if (k < my_tiles && tid == 0) {
+      const int st = (int)(k % kStages);
+      if (!mbar_wait(fbar0 + 8u * st, (uint32_t)((k / kStages) & 1))) {
+        atomicExch(a.err, 1);
+        ok = 0;
+      } else {
+        consumed = k + 1;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t halo = halo_base + (uint32_t)(st * HALO_BYTES);
+        const uint32_t tacc = tmem + (uint32_t)((k & 1) * COUT);
+        // descriptors of tap 0 / k-step 0; every other step adds a compile-time offset (>> 4)
+        const uint64_t da0 = smem_desc(halo, kPlaneBytes, 128);
+        const uint64_t db0 = smem_desc(b0, NG * 128, 128);
 #pragma unroll
-    for (int c = 0; c < COUT; c += 16) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, acc + c);
-    if (pv) {
+        for (int t = 0; t < 9; ++t) {
 #pragma unroll
-      for (int c = 0; c < COUT; ++c) {
-        float v = acc[c] + (a.bias ? a.bias[c] : 0.0f);
-        if (EPI == 1) v = fmaxf(v, 0.0f);
-        acc[c] = v;
-      }
-      const int S = a.split;
-      for (int c0 = 0; c0 < COUT; c0 += 8) {
-        __align__(16) __nv_bfloat16 h[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) h[u] = __float2bfloat16(acc[c0 + u]);
-        if (c0 < S)
-          *reinterpret_cast<uint4*>(a.out1 + p * S + c0) = *reinterpret_cast<uint4*>(h);
-        else
-          *reinterpret_cast<uint4*>(a.out2 + p * (COUT - S) + (c0 - S)) = *reinterpret_cast<uint4*>(h);
+          for (int kc = 0; kc < CIN / 16; ++kc) {
+            const int s = t * (CIN / 16) + kc;
+            const uint32_t aoff = (uint32_t)(2 * kc * kPlaneBytes + ((t / 3) * kHaloW + t % 3) * 16) >> 4;
+            const uint32_t boff = (uint32_t)(2 * s * NG * 128) >> 4;
+            mma_bf16(tacc, da0 + aoff, db0 + boff, id, s > 0 ? 1u : 0u);
+          }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         mbar0 + 8u * (uint32_t)(k & 1))
+                     : "memory");
       }
     }
+    // (2) drain tile k - 1: its MMAs done also frees its halo buffer, refilled with tile k + 2
+    //     (= issued: the prologue filled every buffer)
+    if (k >= 1) {
+      const int64_t j = k - 1;
+      const int done = mbar_wait(mbar0 + 8u * (uint32_t)(j & 1), (uint32_t)((j >> 1) & 1));
+      if (!done) {
+        if (tid == 0) atomicExch(a.err, 1);
+        ok = 0;
+      } else {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (tid == 0 && issued < my_tiles) {
+          const int st = (int)(issued % kStages);
+          issue_halo<C1, C2>(maps, a, first + issued * stride, tiles_x, halo_base + (uint32_t)(st * HALO_BYTES),
+                             fbar0 + 8u * st);
+          ++issued;
+        }
+        conv_epilogue<COUT, EPI>(a, tmem + (uint32_t)((j & 1) * COUT), first + j * stride, tiles_x, tid, warp);
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    ok = __syncthreads_and(ok);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   }
+  // copies issued but never waited for (only after an error): wait for them (bounded) before
+  // leaving; each is the latest use of its buffer, so its phase parity identifies it
+  if (tid == 0)
+    for (int64_t j = consumed; j < issued; ++j) mbar_wait(fbar0 + 8u * (uint32_t)(j % kStages), (uint32_t)((j / kStages) & 1));
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) tmem_free<NCOLS>(tmem);
@@ -494,20 +592,121 @@ __global__ void inv_rms_kernel(const float* __restrict__ r, int64_t n, float* __
   }
 }
 
+// Bilinear transfer between a structured coarse node grid Hc x Wc and the fine grid
+// Hf x Wf = ((Hc - 1) f + 1) x ((Wc - 1) f + 1) whose node (f I, f J) is coarse node (I, J).
+// Prolongation: fine(i, j) = sum over the (up to 4) surrounding coarse nodes of
+// w(i - f I) w(j - f J) coarse(I, J), w(d) = 1 - |d| / f.  Restriction is its transpose,
+// evaluated as a gather over the (2f - 1)^2 fine nodes around each coarse node.
+__global__ void prolong_kernel(const float* __restrict__ c, int Hc, int Wc, int f, float* __restrict__ out) {
+  const int Wf = (Wc - 1) * f + 1;
+  const int64_t total = (int64_t)((Hc - 1) * f + 1) * Wf;
+  const float inv = 1.0f / (float)f;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < total; p += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(p / Wf), j = (int)(p - (int64_t)(p / Wf) * Wf);
+    const int I = i / f, J = j / f;
+    const float ti = (float)(i - I * f) * inv, tj = (float)(j - J * f) * inv;
+    const int I1 = I + 1 < Hc ? I + 1 : I, J1 = J + 1 < Wc ? J + 1 : J;
+    const float v00 = c[(int64_t)I * Wc + J], v01 = c[(int64_t)I * Wc + J1];
+    const float v10 = c[(int64_t)I1 * Wc + J], v11 = c[(int64_t)I1 * Wc + J1];
+    out[p] = (1.0f - ti) * ((1.0f - tj) * v00 + tj * v01) + ti * ((1.0f - tj) * v10 + tj * v11);
+  }
+}
+
+__global__ void restrict_kernel(const float* __restrict__ fine, const unsigned char* __restrict__ fixed, int Hc, int Wc,
+                                int f, float* __restrict__ out) {
+  const int Hf = (Hc - 1) * f + 1, Wf = (Wc - 1) * f + 1;
+  const int64_t total = (int64_t)Hc * Wc;
+  const float inv = 1.0f / (float)f;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int I = (int)(q / Wc), J = (int)(q - (int64_t)(q / Wc) * Wc);
+    const int ci = I * f, cj = J * f;
+    float acc = 0.0f;
+    if (!(fixed && fixed[(int64_t)ci * Wf + cj])) {
+      for (int di = -(f - 1); di <= f - 1; ++di) {
+        const int i = ci + di;
+        if (i < 0 || i >= Hf) continue;
+        const float wi = 1.0f - (float)abs(di) * inv;
+        float row = 0.0f;
+        for (int dj = -(f - 1); dj <= f - 1; ++dj) {
+          const int j = cj + dj;
+          if (j < 0 || j >= Wf) continue;
+          row += (1.0f - (float)abs(dj) * inv) * fine[(int64_t)i * Wf + j];
+        }
+        acc += wi * row;
+      }
+    }
+    out[q] = acc;
+  }
+}
+
+int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// NHWC bf16 tensor {C, W, H, B} with the halo box {8, 130, 3, 1}
+int make_halo_map(CUtensorMap* m, const void* base, int C, int B, int H, int W) {
+  auto fn = encode_fn();
+  if (!fn) return AGX_ERR_CUDA;
+  const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+  const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+  const cuuint32_t box[4] = {8, (cuuint32_t)kHaloW, 3, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? AGX_OK : AGX_ERR_ARG;
+}
+
 template <int C1, int C2, int COUT, int EPI>
 int launch_conv(const ConvArgs& a, cudaStream_t s) {
   constexpr int CIN = C1 + C2;
-  const int smem = 9 * CIN * kTile * 2 + 9 * CIN * COUT * 2;
-  static bool attr = false;
-  if (!attr) {
+  constexpr int smem = 9 * CIN * COUT * 2 + kStages * (CIN / 8) * kPlaneBytes;
+  static int per_sm = 0;
+  if (!per_sm) {
     if (cudaFuncSetAttribute(conv3x3_tc<C1, C2, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
-        cudaSuccess)
+            cudaSuccess ||
+        cudaFuncSetAttribute(conv3x3_tc<C1, C2, COUT, EPI>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared) != cudaSuccess)
       return AGX_ERR_CUDA;
-    attr = true;
+    // resident CTAs per SM from the shared-memory budget (at most 8: TMEM holds 512 columns)
+    int dev = 0, per_sm_smem = 0, reserved = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&per_sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    per_sm = per_sm_smem / (smem + reserved + 256);
+    const int tmem_cap = 512 / tmem_cols(2 * COUT);
+    per_sm = per_sm < 1 ? 1 : (per_sm > tmem_cap ? tmem_cap : per_sm);
   }
-  const int64_t P = (int64_t)a.B * a.H * a.W;
-  const int grid = (int)((P + kTile - 1) / kTile);
-  conv3x3_tc<C1, C2, COUT, EPI><<<grid, kTile, smem, s>>>(a);
+  ConvMaps maps;
+  if (int rc = make_halo_map(&maps.in1, a.in1, C1, a.B, a.H, a.W)) return rc;
+  if (C2 > 0) {
+    if (int rc = make_halo_map(&maps.in2, a.in2, C2, a.B, a.H, a.W)) return rc;
+  } else {
+    maps.in2 = maps.in1;
+  }
+  const int64_t tiles = (int64_t)a.B * a.H * ((a.W + kTile - 1) / kTile);
+  const int64_t cap = (int64_t)per_sm * sm_count();
+  const int grid = (int)(tiles < cap ? tiles : cap);
+  conv3x3_tc<C1, C2, COUT, EPI><<<grid, kTile, smem, s>>>(maps, a);
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
 }
 
@@ -623,6 +822,20 @@ int agx_nn_grid_from_vector(const float* r, const float* aux, int Hn, int Wn, in
   if (normalize) inv_rms_kernel<<<1, 1024, 0, s>>>(r, (int64_t)Hn * Wn, scale);
   grid_from_vector_kernel<<<grid1((int64_t)Hp * Wp), 256, 0, s>>>(r, aux, normalize ? scale : nullptr, Hn, Wn, Hp, Wp,
                                                                   (__nv_bfloat16*)img);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+int agx_nn_restrict(const float* fine, const unsigned char* fixed, int Hc, int Wc, int f, float* coarse,
+                    void* stream) {
+  if (!fine || !coarse || Hc < 2 || Wc < 2 || f < 1 || f > 64) return AGX_ERR_ARG;
+  restrict_kernel<<<grid1((int64_t)Hc * Wc), 256, 0, (cudaStream_t)stream>>>(fine, fixed, Hc, Wc, f, coarse);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+int agx_nn_prolong(const float* coarse, int Hc, int Wc, int f, float* fine, void* stream) {
+  if (!fine || !coarse || Hc < 2 || Wc < 2 || f < 1 || f > 64) return AGX_ERR_ARG;
+  prolong_kernel<<<grid1((int64_t)((Hc - 1) * f + 1) * ((Wc - 1) * f + 1)), 256, 0, (cudaStream_t)stream>>>(
+      coarse, Hc, Wc, f, fine);
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
 }
 

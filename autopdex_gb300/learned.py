@@ -1,12 +1,15 @@
 """Learned preconditioner: a 4-level, 32-channel convolutional U-Net on the node grid.
 
 The network maps a residual r (and the log-conductivity of the problem, averaged to the
-nodes) to an approximation of K^-1 r; flexible CG (``'type of preconditioner': 'learned'``)
-applies it at every iteration, and the true float64 Newton residual judges every solve.
+nodes) to a correction y whose energy-optimal multiple approximates K^-1 r after damped
+Jacobi smoothing; flexible CG (``'type of preconditioner': 'learned'``) applies it at every
+iteration in a symmetric two-level form, and the true float64 Newton residual judges every
+solve.
 Every convolution, pooling, upsampling and gradient runs in this package's own BF16
 tensor-core kernels (include/autopdex_gb300_nn.h); PyTorch holds the float32 master
-weights and runs the Adam update.  Training pairs (r, K^-1 r) come from the plain float64
-Jacobi-PCG solver of this backend on seeded random-conductivity problems.
+weights and runs the Adam update.  Training pairs (residual, error) come from the iterates of
+the plain float64 Jacobi-PCG solver of this backend on seeded random-conductivity problems,
+and the loss is the fraction of the error energy the correction leaves.
 
 This part has no counterpart in AutoPDEx.
 """
@@ -22,8 +25,10 @@ from . import _native as N
 C_HID = 32
 C_IN = 16
 C_OUT = 16
-# (name, c1, c2, cout, relu): encoder (two convs per level, 2x2 average pooling between levels),
-# bottleneck, decoder (nearest upsampling, concatenation with the encoder output of the level)
+POOL = 4  # 4 x 4 average pooling between levels: the coarsest level of a 320 x 320 grid is 5 x 5
+# (name, c1, c2, cout, relu): encoder (two convs per level, POOL x POOL average pooling between
+# levels), bottleneck, decoder (nearest POOL x upsampling, concatenation with the encoder output
+# of the level)
 LAYERS = [("e0a", 16, 0, 32, 1), ("e0b", 32, 0, 32, 1), ("e1a", 32, 0, 32, 1), ("e1b", 32, 0, 32, 1),
           ("e2a", 32, 0, 32, 1), ("e2b", 32, 0, 32, 1), ("b3a", 32, 0, 32, 1), ("b3b", 32, 0, 32, 1),
           ("d2a", 32, 32, 32, 1), ("d2b", 32, 0, 32, 1), ("d1a", 32, 32, 32, 1), ("d1b", 32, 0, 32, 1),
@@ -36,8 +41,9 @@ def _p(t):
 
 
 def padded(n):
-    """Grid extent padded to a multiple of 8 (three 2x poolings)."""
-    return (n + 7) // 8 * 8
+    """Grid extent padded to a multiple of POOL^3 (three poolings)."""
+    m = POOL ** 3
+    return (n + m - 1) // m * m
 
 
 class UNet:
@@ -57,6 +63,7 @@ class UNet:
         if params is not None:
             self.load_state(params)
         self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self._s, self._arena = None, None
         self.pack()
 
     # ---- parameters -------------------------------------------------------------------
@@ -94,6 +101,8 @@ class UNet:
 
     # ---- helpers ------------------------------------------------------------------------
     def _stream(self):
+        if self._s is not None:
+            return self._s
         return C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
 
     @staticmethod
@@ -101,50 +110,77 @@ class UNet:
         if rc != 0:
             raise RuntimeError(f"{fn} failed with status {rc}")
 
-    def _act(self, B, H, W, c):
+    def _act(self, B, H, W, c, key=None):
+        """Activation buffer: from the arena when one is active (allocated on first use)."""
+        if self._arena is not None and key is not None:
+            t = self._arena.get(key)
+            if t is None or t.shape != (B, H, W, c):
+                t = torch.empty((B, H, W, c), dtype=torch.bfloat16, device=self.device)
+                self._arena[key] = t
+            return t
         return torch.empty((B, H, W, c), dtype=torch.bfloat16, device=self.device)
 
     def _conv(self, name, x1, x2, B, H, W):
         _, c1, c2, co, relu = next(l for l in LAYERS if l[0] == name)
-        out = self._act(B, H, W, co)
+        out = self._act(B, H, W, co, name)
         rc = self.lib.agx_nn_conv3x3(_p(x1), _p(x2), c1, c2, _p(self.img_f[name]), _p(self.b[name]), _p(out), None,
                                      co, co, relu, B, H, W, _p(self.err), self._stream())
         self._ok("agx_nn_conv3x3", rc)
         return out
 
-    def _pool(self, x, B, H, W, c):
-        out = self._act(B, H // 2, W // 2, c)
-        self._ok("agx_nn_pool2", self.lib.agx_nn_pool2(_p(x), _p(out), B, H, W, c, 0, self._stream()))
-        return out
+    def _pool(self, x, B, H, W, c, key):
+        """POOL x POOL average pooling as repeated 2 x 2 pooling."""
+        f = 1
+        while f < POOL:
+            out = self._act(B, H // (2 * f), W // (2 * f), c, f"{key}.{f}")
+            self._ok("agx_nn_pool2", self.lib.agx_nn_pool2(_p(x), _p(out), B, H // f, W // f, c, 0, self._stream()))
+            x, f = out, 2 * f
+        return x
 
-    def _up(self, x, B, H, W, c):
-        out = self._act(B, 2 * H, 2 * W, c)
-        self._ok("agx_nn_upsample2", self.lib.agx_nn_upsample2(_p(x), _p(out), B, H, W, c, 0, self._stream()))
-        return out
+    def _up(self, x, B, H, W, c, key):
+        """Nearest POOL x upsampling of an H x W image as repeated 2 x upsampling."""
+        f = 1
+        while f < POOL:
+            out = self._act(B, 2 * f * H, 2 * f * W, c, f"{key}.{f}")
+            self._ok("agx_nn_upsample2", self.lib.agx_nn_upsample2(_p(x), _p(out), B, f * H, f * W, c, 0,
+                                                                   self._stream()))
+            x, f = out, 2 * f
+        return x
 
     # ---- forward / backward -------------------------------------------------------------
-    def forward(self, x, keep=False):
-        """x: (B, H, W, 16) bf16 with H, W multiples of 8 -> (B, H, W, 16) bf16."""
+    def forward(self, x, keep=False, stream=None, arena=None):
+        """x: (B, H, W, 16) bf16 with H, W multiples of POOL^3 -> (B, H, W, 16) bf16.
+
+        ``stream``: launch on this CUDA stream (a c_void_p) instead of torch's current one;
+        ``arena``: a dict of activation buffers reused across calls (no allocation once warm)."""
+        self._s, self._arena = stream, arena
+        try:
+            return self._forward(x, keep)
+        finally:
+            self._s, self._arena = None, None
+
+    def _forward(self, x, keep):
         B, H, W, _ = x.shape
+        q1, q2, q3 = POOL, POOL ** 2, POOL ** 3
         a = {"x": x}
         a["e0a"] = self._conv("e0a", x, None, B, H, W)
         a["e0b"] = self._conv("e0b", a["e0a"], None, B, H, W)
-        a["p0"] = self._pool(a["e0b"], B, H, W, C_HID)
-        a["e1a"] = self._conv("e1a", a["p0"], None, B, H // 2, W // 2)
-        a["e1b"] = self._conv("e1b", a["e1a"], None, B, H // 2, W // 2)
-        a["p1"] = self._pool(a["e1b"], B, H // 2, W // 2, C_HID)
-        a["e2a"] = self._conv("e2a", a["p1"], None, B, H // 4, W // 4)
-        a["e2b"] = self._conv("e2b", a["e2a"], None, B, H // 4, W // 4)
-        a["p2"] = self._pool(a["e2b"], B, H // 4, W // 4, C_HID)
-        a["b3a"] = self._conv("b3a", a["p2"], None, B, H // 8, W // 8)
-        a["b3b"] = self._conv("b3b", a["b3a"], None, B, H // 8, W // 8)
-        a["u2"] = self._up(a["b3b"], B, H // 8, W // 8, C_HID)
-        a["d2a"] = self._conv("d2a", a["u2"], a["e2b"], B, H // 4, W // 4)
-        a["d2b"] = self._conv("d2b", a["d2a"], None, B, H // 4, W // 4)
-        a["u1"] = self._up(a["d2b"], B, H // 4, W // 4, C_HID)
-        a["d1a"] = self._conv("d1a", a["u1"], a["e1b"], B, H // 2, W // 2)
-        a["d1b"] = self._conv("d1b", a["d1a"], None, B, H // 2, W // 2)
-        a["u0"] = self._up(a["d1b"], B, H // 2, W // 2, C_HID)
+        a["p0"] = self._pool(a["e0b"], B, H, W, C_HID, "p0")
+        a["e1a"] = self._conv("e1a", a["p0"], None, B, H // q1, W // q1)
+        a["e1b"] = self._conv("e1b", a["e1a"], None, B, H // q1, W // q1)
+        a["p1"] = self._pool(a["e1b"], B, H // q1, W // q1, C_HID, "p1")
+        a["e2a"] = self._conv("e2a", a["p1"], None, B, H // q2, W // q2)
+        a["e2b"] = self._conv("e2b", a["e2a"], None, B, H // q2, W // q2)
+        a["p2"] = self._pool(a["e2b"], B, H // q2, W // q2, C_HID, "p2")
+        a["b3a"] = self._conv("b3a", a["p2"], None, B, H // q3, W // q3)
+        a["b3b"] = self._conv("b3b", a["b3a"], None, B, H // q3, W // q3)
+        a["u2"] = self._up(a["b3b"], B, H // q3, W // q3, C_HID, "u2")
+        a["d2a"] = self._conv("d2a", a["u2"], a["e2b"], B, H // q2, W // q2)
+        a["d2b"] = self._conv("d2b", a["d2a"], None, B, H // q2, W // q2)
+        a["u1"] = self._up(a["d2b"], B, H // q2, W // q2, C_HID, "u1")
+        a["d1a"] = self._conv("d1a", a["u1"], a["e1b"], B, H // q1, W // q1)
+        a["d1b"] = self._conv("d1b", a["d1a"], None, B, H // q1, W // q1)
+        a["u0"] = self._up(a["d1b"], B, H // q1, W // q1, C_HID, "u0")
         a["d0a"] = self._conv("d0a", a["u0"], a["e0b"], B, H, W)
         a["d0b"] = self._conv("d0b", a["d0a"], None, B, H, W)
         out = self._conv("out", a["d0b"], None, B, H, W)
@@ -180,39 +216,47 @@ class UNet:
         self.gw = {k: torch.zeros_like(v) for k, v in self.w.items()}
         self.gb = {k: torch.zeros_like(v) for k, v in self.b.items()}
 
-        def upb(g, h, w):  # adjoint of upsampling to (h, w) -> coarse
-            out = self._act(B, h // 2, w // 2, C_HID)
-            self._ok("agx_nn_upsample2", self.lib.agx_nn_upsample2(_p(g), _p(out), B, h // 2, w // 2, C_HID, 1, s))
-            return out
+        def upb(g, h, w):  # adjoint of upsampling to (h, w) -> coarse (h / POOL, w / POOL)
+            f = 2
+            while f <= POOL:
+                out = self._act(B, h // f, w // f, C_HID)
+                self._ok("agx_nn_upsample2", self.lib.agx_nn_upsample2(_p(g), _p(out), B, h // f, w // f, C_HID, 1,
+                                                                       s))
+                g, f = out, 2 * f
+            return g
 
-        def poolb(g, h, w):  # adjoint of pooling from (h, w)
-            out = self._act(B, h, w, C_HID)
-            self._ok("agx_nn_pool2", self.lib.agx_nn_pool2(_p(g), _p(out), B, h, w, C_HID, 1, s))
-            return out
+        def poolb(g, h, w):  # adjoint of pooling from (h, w): coarse (h / POOL, w / POOL) -> (h, w)
+            f = POOL // 2
+            while f >= 1:
+                out = self._act(B, h // f, w // f, C_HID)
+                self._ok("agx_nn_pool2", self.lib.agx_nn_pool2(_p(g), _p(out), B, h // f, w // f, C_HID, 1, s))
+                g, f = out, f // 2
+            return g
 
         def add(x, y):
             self._ok("agx_nn_add", self.lib.agx_nn_add(_p(x), _p(y), x.numel(), s))
             return x
 
+        q1, q2, q3 = POOL, POOL ** 2, POOL ** 3
         g = gout.clone()
         g, _ = self._layer_backward("out", g, a["d0b"], None, None, B, H, W)
         g, _ = self._layer_backward("d0b", g, a["d0a"], None, a["d0b"], B, H, W)
         g_u0, g_s0 = self._layer_backward("d0a", g, a["u0"], a["e0b"], a["d0a"], B, H, W)
         g = upb(g_u0, H, W)
-        g, _ = self._layer_backward("d1b", g, a["d1a"], None, a["d1b"], B, H // 2, W // 2)
-        g_u1, g_s1 = self._layer_backward("d1a", g, a["u1"], a["e1b"], a["d1a"], B, H // 2, W // 2)
-        g = upb(g_u1, H // 2, W // 2)
-        g, _ = self._layer_backward("d2b", g, a["d2a"], None, a["d2b"], B, H // 4, W // 4)
-        g_u2, g_s2 = self._layer_backward("d2a", g, a["u2"], a["e2b"], a["d2a"], B, H // 4, W // 4)
-        g = upb(g_u2, H // 4, W // 4)
-        g, _ = self._layer_backward("b3b", g, a["b3a"], None, a["b3b"], B, H // 8, W // 8)
-        g, _ = self._layer_backward("b3a", g, a["p2"], None, a["b3a"], B, H // 8, W // 8)
-        g = add(poolb(g, H // 4, W // 4), g_s2)
-        g, _ = self._layer_backward("e2b", g, a["e2a"], None, a["e2b"], B, H // 4, W // 4)
-        g, _ = self._layer_backward("e2a", g, a["p1"], None, a["e2a"], B, H // 4, W // 4)
-        g = add(poolb(g, H // 2, W // 2), g_s1)
-        g, _ = self._layer_backward("e1b", g, a["e1a"], None, a["e1b"], B, H // 2, W // 2)
-        g, _ = self._layer_backward("e1a", g, a["p0"], None, a["e1a"], B, H // 2, W // 2)
+        g, _ = self._layer_backward("d1b", g, a["d1a"], None, a["d1b"], B, H // q1, W // q1)
+        g_u1, g_s1 = self._layer_backward("d1a", g, a["u1"], a["e1b"], a["d1a"], B, H // q1, W // q1)
+        g = upb(g_u1, H // q1, W // q1)
+        g, _ = self._layer_backward("d2b", g, a["d2a"], None, a["d2b"], B, H // q2, W // q2)
+        g_u2, g_s2 = self._layer_backward("d2a", g, a["u2"], a["e2b"], a["d2a"], B, H // q2, W // q2)
+        g = upb(g_u2, H // q2, W // q2)
+        g, _ = self._layer_backward("b3b", g, a["b3a"], None, a["b3b"], B, H // q3, W // q3)
+        g, _ = self._layer_backward("b3a", g, a["p2"], None, a["b3a"], B, H // q3, W // q3)
+        g = add(poolb(g, H // q2, W // q2), g_s2)
+        g, _ = self._layer_backward("e2b", g, a["e2a"], None, a["e2b"], B, H // q2, W // q2)
+        g, _ = self._layer_backward("e2a", g, a["p1"], None, a["e2a"], B, H // q2, W // q2)
+        g = add(poolb(g, H // q1, W // q1), g_s1)
+        g, _ = self._layer_backward("e1b", g, a["e1a"], None, a["e1b"], B, H // q1, W // q1)
+        g, _ = self._layer_backward("e1a", g, a["p0"], None, a["e1a"], B, H // q1, W // q1)
         g = add(poolb(g, H, W), g_s0)
         g, _ = self._layer_backward("e0b", g, a["e0a"], None, a["e0b"], B, H, W)
         self._layer_backward("e0a", g, a["x"], None, a["e0a"], B, H, W, need_input_grad=False)
@@ -249,38 +293,99 @@ def to_image(lib, r, aux, Hn, Wn, normalize=True, out=None, scale=None, stream=N
     return img, sc
 
 
-def make_training_set(n_problems, n=256, rhs_per_problem=2, seed0=0, krylov_tol=1e-6, verbose=False):
-    """(r, aux, e) triples from the plain float64 Jacobi-PCG solver of this backend on
-    heat-conduction problems with seeded random conductivity (config-4 family at n x n)."""
+OMEGA = 2.0 / 3.0  # damped Jacobi smoothing around the network (preconditioner mode 2)
+ITERATES = (0, 2, 5, 10, 20, 40, 80, 160)  # Jacobi-PCG iterations whose residuals are sampled
+
+
+class TrainingSet:
+    """Residual-to-error pairs of the plain solver, reduced to what the loss needs.
+
+    For a Jacobi-PCG iterate x_k of K x = b (solution x*), r = b - K x_k and e = x* - x_k;
+    after the damped Jacobi pre-smoothing of the two-level preconditioner the network sees
+    r1 = r - w K D^-1 r with error e1 = e - w D^-1 r.  Stored per sample: r1 / rms(r1)
+    (float32, on the GPU), its error energy s = (r1, e1) / rms(r1)^2, and the index of its
+    problem, whose float32 tangent values (the library's layout) are kept for K y."""
+
+    def __init__(self, n, prob, r1, s, pid, aux, values, free):
+        self.n, self.prob = n, prob
+        self.r1, self.s, self.pid, self.aux, self.values, self.free = r1, s, pid, aux, values, free
+
+    def __len__(self):
+        return self.r1.shape[0]
+
+
+def _solve(prob, rhs, x, rtol, maxiter):
+    opts = N.SolveOpts()
+    opts.method, opts.rtol, opts.atol, opts.maxiter, opts.check_every = N.AGX_PCG, rtol, 0.0, maxiter, 64
+    info = N.SolveInfo()
+    rc = prob.lib.agx_solve(prob.ctx, C.c_void_p(rhs.data_ptr()), C.c_void_p(x.data_ptr()), C.byref(opts),
+                            C.byref(info))
+    if rc not in (N.AGX_OK, N.AGX_NOT_CONVERGED):
+        N.check(prob.ctx, "agx_solve", rc)
+    return info
+
+
+def make_training_set(n_problems, n=256, rhs_per_problem=2, seed0=0, iterates=ITERATES, krylov_tol=1e-10,
+                      omega=OMEGA, verbose=False):
+    """Samples from the plain float64 Jacobi-PCG solver of this backend on heat-conduction
+    problems with seeded random conductivity (the config-4 family at n x n): for every
+    problem and right-hand side (constant, then smooth-plus-rough random fields) one solve
+    to ``krylov_tol`` gives x*, and the iterates x_k, k in ``iterates``, give the pairs."""
     from . import configs
     from ._problem import get_problem
     w = configs.heat_grf(n=n, seed=seed0)
     prob = get_problem(w.dofs, w.settings, w.static_settings)
-    mask = torch.as_tensor(prob.mask.astype(bool), device=prob.device)
+    dev = prob.device
+    mask = torch.as_tensor(prob.mask.astype(bool), device=dev)
+    free = (~mask).float()
     rng = np.random.default_rng(seed0 + 12345)
-    R, A, E = [], [], []
-    opts = N.SolveOpts()
-    opts.method, opts.rtol, opts.atol, opts.maxiter, opts.check_every = N.AGX_PCG, krylov_tol, 0.0, 200000, 64
-    x0 = torch.zeros(prob.n_dofs, dtype=torch.float64, device=prob.device)
+    nv = prob.nnzb * prob.ndof * prob.ndof
+    values = torch.empty((n_problems, nv), dtype=torch.float32, device=dev)
+    auxs = torch.empty((n_problems, prob.n_dofs), dtype=torch.float32, device=dev)
+    S = n_problems * rhs_per_problem * len(iterates)
+    r1s = torch.empty((S, prob.n_dofs), dtype=torch.float32, device=dev)
+    ss = torch.empty(S, dtype=torch.float32, device=dev)
+    pid = torch.empty(S, dtype=torch.int64)
+    x0 = torch.zeros(prob.n_dofs, dtype=torch.float64, device=dev)
+    t = torch.empty_like(x0)
+    xs = torch.empty_like(x0)
+    xk = torch.empty_like(x0)
+    z = torch.empty_like(x0)
+    j_out = 0
     for i in range(n_problems):
         k = np.exp(configs.gaussian_random_field(n, seed=seed0 + i)).reshape(-1)
         w.settings["conductivity"] = k
         prob.update_models(w.settings)
         prob._call("agx_assemble", C.c_void_p(x0.data_ptr()), None, N.AGX_F64)
-        aux = torch.as_tensor(node_log_conductivity(k, n, n), device=prob.device)
+        auxs[i] = torch.as_tensor(node_log_conductivity(k, n, n), device=dev)
         for j in range(rhs_per_problem):
-            r = _random_rhs(rng, n + 1, prob.device) if j else torch.ones(prob.n_dofs, dtype=torch.float64,
-                                                                         device=prob.device)
-            r = torch.where(mask, torch.zeros_like(r), r)
-            e = torch.zeros_like(r)
-            info = N.SolveInfo()
-            prob._call("agx_solve", C.c_void_p(r.data_ptr()), C.c_void_p(e.data_ptr()), C.byref(opts), C.byref(info))
-            R.append(r.float())
-            A.append(aux)
-            E.append(e.float())
+            b = _random_rhs(rng, n + 1, dev) if j else torch.ones(prob.n_dofs, dtype=torch.float64, device=dev)
+            b = torch.where(mask, torch.zeros_like(b), b)
+            info = _solve(prob, b, xs, krylov_tol, 200000)
+            for it in iterates:
+                if it == 0:
+                    xk.zero_()
+                else:
+                    _solve(prob, b, xk, 0.0, it)
+                prob._call("agx_spmv", N.AGX_F64, C.c_void_p(xk.data_ptr()), C.c_void_p(t.data_ptr()))
+                r = b - t
+                prob._call("agx_jacobi", N.AGX_F64, C.c_void_p(r.data_ptr()), C.c_void_p(z.data_ptr()))
+                z.mul_(omega)
+                prob._call("agx_spmv", N.AGX_F64, C.c_void_p(z.data_ptr()), C.c_void_p(t.data_ptr()))
+                r1 = r - t
+                e1 = (xs - xk) - z
+                r1[mask] = 0.0
+                e1[mask] = 0.0
+                rms = r1.pow(2).mean().sqrt().clamp_min(1e-300)
+                r1s[j_out] = (r1 / rms).float()
+                ss[j_out] = float((r1 @ e1) / (rms * rms))
+                pid[j_out] = i
+                j_out += 1
+        prob._call("agx_assemble", C.c_void_p(x0.data_ptr()), None, N.AGX_F32)
+        prob._call("agx_copy_values", N.AGX_F32, C.c_void_p(values[i].data_ptr()))
         if verbose and i % 100 == 0:
-            print(f"training problem {i}: {info.iterations} CG iterations")
-    return torch.stack(R), torch.stack(A), torch.stack(E)
+            print(f"training problem {i}: {info.iterations} CG iterations to {krylov_tol:g}", flush=True)
+    return TrainingSet(n, prob, r1s, ss, pid, auxs, values, free)
 
 
 def _random_rhs(rng, m, device):
@@ -293,76 +398,166 @@ def _random_rhs(rng, m, device):
     return torch.as_tensor(f.reshape(-1), dtype=torch.float64, device=device)
 
 
-def train(net, R, A, E, n, steps=2000, batch=16, lr=2e-3, seed=0, verbose=False):
-    """Adam on the scale-invariant loss ||z - e~||^2 / ||e~||^2 with e~ = e / rms(e),
-    z = channel 0 of the network output on the node grid."""
+SCALE_PENALTY = 1e-3  # weight of (log rms(y))^2, which keeps the output scale near 1
+
+
+def energy_loss(r1, y, Ky, s):
+    """Per-sample loss 1 - (r1, y)^2 / ((y, K y) (r1, e1)) and its gradient with respect to y.
+
+    With the energy-optimal step c = (r1, y) / (y, K y) the error left after z = c y is
+    ||e1 - c y||_K^2 = ||e1||_K^2 - (r1, y)^2 / (y, K y), so the loss is the fraction of the
+    error energy the correction leaves (0 for y parallel to e1), independent of the scales of
+    y and r1.  It is evaluated in float64 on y / rms(y) (for a function homogeneous of degree
+    0, grad L(y) = grad L(y / sigma) / sigma); K is symmetric:
+    d/dy = -2 a / (b s) (r1 - (a / b) K y), a = (r1, y), b = (y, K y).  A weak penalty
+    SCALE_PENALTY (log sigma)^2 keeps sigma = rms(y) near 1: the loss alone is blind to the
+    scale, which otherwise drifts.  Samples whose values are not finite get zero gradient."""
+    r1, y, Ky, s = r1.double(), y.double(), Ky.double(), s.double()
+    n = y.shape[1]
+    sig = y.pow(2).mean(1).sqrt().clamp_min(1e-30)
+    yn, Kyn = y / sig[:, None], Ky / sig[:, None]
+    a = (r1 * yn).sum(1)
+    bq = (yn * Kyn).sum(1)
+    bq = torch.where(bq.abs() > 1e-30, bq, torch.full_like(bq, 1e-30))
+    loss = 1.0 - a * a / (bq * s)
+    grad = -(2.0 * a / (bq * s))[:, None] * (r1 - (a / bq)[:, None] * Kyn) / sig[:, None]
+    grad = grad + (2.0 * SCALE_PENALTY * torch.log(sig) / (n * sig * sig))[:, None] * y
+    ok = torch.isfinite(loss) & torch.isfinite(grad).all(1)
+    loss = torch.where(ok, loss, torch.zeros_like(loss))
+    grad = torch.where(ok[:, None], grad, torch.zeros_like(grad))
+    return loss, grad.float()
+
+
+def train(net, ts, steps=3000, batch=16, lr=2e-3, seed=0, verbose=False):
+    """Adam with a cosine learning-rate schedule on :func:`energy_loss`; every product K y
+    runs through agx_spmv_values with the stored tangent of the sample's problem."""
     lib = net.lib
-    Hn = Wn = n + 1
+    prob = ts.prob
+    Hn = Wn = ts.n + 1
     Hp, Wp = padded(Hn), padded(Wn)
     params = net.parameters()
     opt = torch.optim.Adam(params, lr=lr)
+    sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, steps)
     gen = torch.Generator().manual_seed(seed)
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     losses = []
     x = torch.empty((batch, Hp, Wp, C_IN), dtype=torch.bfloat16, device=net.device)
     sc = torch.empty(batch, dtype=torch.float32, device=net.device)
+    Ky = torch.empty((batch, prob.n_dofs), dtype=torch.float32, device=net.device)
+    g = torch.zeros((batch, Hp, Wp, C_OUT), dtype=torch.float32, device=net.device)
     for step in range(steps):
-        idx = torch.randint(0, R.shape[0], (batch,), generator=gen)
-        for b, i in enumerate(idx.tolist()):
-            to_image(lib, R[i], A[i], Hn, Wn, True, out=x[b:b + 1], scale=sc[b:b + 1], stream=stream)
+        idx = torch.randint(0, len(ts), (batch,), generator=gen)
+        pids = ts.pid[idx].tolist()
+        for b, (i, pi) in enumerate(zip(idx.tolist(), pids)):
+            to_image(lib, ts.r1[i], ts.aux[pi], Hn, Wn, True, out=x[b:b + 1], scale=sc[b:b + 1], stream=stream)
         out, acts = net.forward(x, keep=True)
-        z = out[..., 0].float()[:, :Hn, :Wn].reshape(batch, -1)
-        e = E[idx]
-        et = e / e.pow(2).mean(dim=1, keepdim=True).sqrt().clamp_min(1e-30)
-        diff = z - et
-        loss = (diff.pow(2).sum(dim=1) / et.pow(2).sum(dim=1)).mean()
-        g = torch.zeros_like(out, dtype=torch.float32)
-        g[:, :Hn, :Wn, 0] = (2.0 * diff / et.pow(2).sum(dim=1, keepdim=True) / batch).reshape(batch, Hn, Wn)
-        gw, gb = net.backward(g.to(torch.bfloat16), acts)
+        y = (out[..., 0].float()[:, :Hn, :Wn].reshape(batch, -1) * ts.free).contiguous()
+        for b, pi in enumerate(pids):
+            prob._call("agx_spmv_values", N.AGX_F32, C.c_void_p(ts.values[pi].data_ptr()),
+                       C.c_void_p(y[b].data_ptr()), C.c_void_p(Ky[b].data_ptr()))
+        r1 = ts.r1[idx.to(net.device)]
+        loss, grad = energy_loss(r1, y, Ky, ts.s[idx.to(net.device)])
+        g[:, :Hn, :Wn, 0] = (grad * ts.free / batch).reshape(batch, Hn, Wn)
+        # the backward pass is linear in g: run it on g / max|g| (bf16-friendly) and rescale
+        gmax = float(g.abs().max().clamp_min(1e-30))
+        gw, gb = net.backward((g / gmax).to(torch.bfloat16), acts)
         for name, *_ in LAYERS:
-            net.w[name].grad = gw[name]
-            net.b[name].grad = gb[name]
-        opt.step()
+            net.w[name].grad = gw[name] * gmax
+            net.b[name].grad = gb[name] * gmax
+        if bool(torch.stack([torch.isfinite(t.grad).all() for t in params]).all()):
+            opt.step()
+        sched.step()
         opt.zero_grad(set_to_none=True)
         with torch.no_grad():
             net.w["e0a"][:, 2:] = 0.0
         net.pack()
-        losses.append(float(loss))
+        losses.append(float(loss.mean()))
         if verbose and step % 100 == 0:
-            print(f"step {step}: loss {losses[-1]:.4f}")
+            print(f"step {step}: loss {np.mean(losses[-50:]):.4f}", flush=True)
     net.check()
     return losses
 
 
 # ---- preconditioner for flexible CG ----------------------------------------------------------
-class GridPreconditioner:
-    """z = net(r) on the node grid of an nx x ny structured quad mesh (scalar field)."""
+def coarse_log_conductivity(k_elem, nx, ny, f):
+    """Node log-conductivity of the grid coarsened by f: k averaged over f x f element blocks,
+    then :func:`node_log_conductivity` on the (nx / f) x (ny / f) coarse elements."""
+    k = np.asarray(k_elem, dtype=np.float64).reshape(nx, ny)
+    kc = k.reshape(nx // f, f, ny // f, f).mean(axis=(1, 3))
+    return node_log_conductivity(kc.reshape(-1), nx // f, ny // f)
 
-    def __init__(self, net, nx, ny, k_elem):
+
+class GridPreconditioner:
+    """The network as the coarse solver of a two-level preconditioner on the node grid of an
+    nx x ny structured quad mesh (scalar field).
+
+    FCG applies it in the symmetric two-level form it was trained for (mode 2): damped Jacobi
+    smoothing, y = P net(P^T r) with the energy-optimal step, damped Jacobi smoothing.  P is
+    bilinear interpolation from the grid coarsened by ``factor`` (1: the network runs on the
+    node grid itself), so a network trained on n x n problems serves (factor n) x (factor n)
+    problems on its own resolution.  All buffers are allocated here and the callback only
+    enqueues kernels on the stream it is given, so FCG captures it into CUDA graphs."""
+
+    def __init__(self, net, nx, ny, k_elem, factor=1, mode=2, omega=OMEGA, sweeps=None, fixed=None):
+        if nx % factor or ny % factor:
+            raise ValueError("the grid must be divisible by the coarsening factor")
         self.net = net
+        self.mode, self.omega = mode, omega
+        self.sweeps = sweeps if sweeps is not None else (1 if factor == 1 else 2)
+        self.factor = factor
         self.nx, self.ny = nx, ny
-        self.Hn, self.Wn = nx + 1, ny + 1
+        self.Hn, self.Wn = nx // factor + 1, ny // factor + 1
         self.Hp, self.Wp = padded(self.Hn), padded(self.Wn)
-        self.aux = torch.as_tensor(node_log_conductivity(k_elem, nx, ny), device=net.device)
-        self.img = torch.empty((1, self.Hp, self.Wp, C_IN), dtype=torch.bfloat16, device=net.device)
-        self.scale = torch.empty(1, dtype=torch.float32, device=net.device)
+        dev = net.device
+        self.aux = torch.as_tensor(coarse_log_conductivity(k_elem, nx, ny, factor), device=dev)
+        self.img = torch.zeros((1, self.Hp, self.Wp, C_IN), dtype=torch.bfloat16, device=dev)
+        self.scale = torch.empty(1, dtype=torch.float32, device=dev)
+        self.rc = torch.zeros(self.Hn * self.Wn, dtype=torch.float32, device=dev)
+        self.yc = torch.zeros(self.Hn * self.Wn, dtype=torch.float32, device=dev)
+        self.fixed = None if fixed is None else torch.as_tensor(np.asarray(fixed, dtype=np.uint8), device=dev)
+        self.arena = {}
         self.applications = 0
+        net.forward(self.img, arena=self.arena)  # allocate the activations once
+        torch.cuda.synchronize(dev)
 
     def apply_ptr(self, r_ptr, z_ptr, n, stream):
         lib = self.net.lib
-        rc = lib.agx_nn_grid_from_vector(C.c_void_p(r_ptr), _p(self.aux), self.Hn, self.Wn, self.Hp, self.Wp, 1,
-                                         _p(self.scale), _p(self.img), C.c_void_p(stream))
+        st = C.c_void_p(stream)
+        f = self.factor
+        if f > 1:
+            fixed = _p(self.fixed)
+            rc = lib.agx_nn_restrict(C.c_void_p(r_ptr), fixed, self.Hn, self.Wn, f, _p(self.rc), st)
+            if rc != 0:
+                return rc
+            src = self.rc.data_ptr()
+        else:
+            src = r_ptr
+        rc = lib.agx_nn_grid_from_vector(C.c_void_p(src), _p(self.aux), self.Hn, self.Wn, self.Hp, self.Wp, 1,
+                                         _p(self.scale), _p(self.img), st)
         if rc != 0:
             return rc
-        out = self.net.forward(self.img)
-        rc = lib.agx_nn_vector_from_grid(_p(out), C_OUT, self.Hn, self.Wn, self.Wp, C.c_void_p(z_ptr),
-                                         C.c_void_p(stream))
+        out = self.net.forward(self.img, stream=st, arena=self.arena)
+        dst = self.yc.data_ptr() if f > 1 else z_ptr
+        rc = lib.agx_nn_vector_from_grid(_p(out), C_OUT, self.Hn, self.Wn, self.Wp, C.c_void_p(dst), st)
+        if rc == 0 and f > 1:
+            rc = lib.agx_nn_prolong(_p(self.yc), self.Hn, self.Wn, f, C.c_void_p(z_ptr), st)
         self.applications += 1
         return rc
 
+    def attach(self, prob):
+        """Register with a problem's native context (FCG then calls it and captures it)."""
+        cb = self.callback(prob)
+        prob._precond_cb = cb
+        prob._call("agx_set_preconditioner", cb, None)
+        prob._call("agx_set_preconditioner_mode", int(self.mode), float(self.omega), int(self.sweeps),
+                   N.AGX_PRECOND_CAPTURABLE)
+        prob.learned = self
+
     def callback(self, prob):
-        if prob.n_dofs != self.Hn * self.Wn:
+        if prob.n_dofs != (self.nx + 1) * (self.ny + 1):
             raise ValueError("the learned preconditioner was built for another grid")
+        if self.factor > 1 and self.fixed is None:
+            self.fixed = torch.as_tensor(prob.mask.astype(np.uint8), device=self.net.device)
 
         def fn(user, r, z, n, stream):
             try:

@@ -216,7 +216,4 @@ def _attach_learned(prob, static_settings):
         prob.learned = None
         return
     if prob.learned is not pc:
-        cb = pc.callback(prob)
-        prob._precond_cb = cb
-        prob._call("agx_set_preconditioner", cb, None)
-        prob.learned = pc
+        pc.attach(prob)

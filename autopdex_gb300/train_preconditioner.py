@@ -1,13 +1,15 @@
 """Trains the learned preconditioner on the GPU and saves its weights.
 
-    python -m autopdex_gb300.train_preconditioner --n 256 --problems 2000 --steps 3000 \
+    python -m autopdex_gb300.train_preconditioner --n 256 --problems 2000 --steps 6000 \
         --out autopdex_gb300/weights/heat_unet_n256.npz
 
-Training pairs (r, K^-1 r) come from the plain float64 Jacobi-PCG solver on heat-conduction
-problems -div(k grad T) = r with k = exp(Gaussian random field) seeded 0 .. problems-1
-(length 0.05, std 1, the config-4 family), one constant and one random right-hand side each.
+Training pairs (residual, error) come from the iterates of the plain float64 Jacobi-PCG solver
+on heat-conduction problems -div(k grad T) = b with k = exp(Gaussian random field) seeded
+0 .. problems-1 (length 0.05, std 1, the 1024 x 1024 heat workload's family at n x n), one
+constant and one random right-hand side each.
 """
 import argparse
+import json
 import os
 import time
 
@@ -20,22 +22,31 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--problems", type=int, default=2000)
-    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--steps", type=int, default=6000)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", default=os.path.join(learned.WEIGHTS_DIR, "heat_unet_n256.npz"))
     args = ap.parse_args()
     t0 = time.time()
-    R, A, E = learned.make_training_set(args.problems, n=args.n, seed0=args.seed, verbose=True)
+    ts = learned.make_training_set(args.problems, n=args.n, seed0=args.seed, verbose=True)
     t1 = time.time()
     net = learned.UNet(seed=args.seed)
-    losses = learned.train(net, R, A, E, args.n, steps=args.steps, batch=args.batch, lr=args.lr, verbose=True)
+    losses = learned.train(net, ts, steps=args.steps, batch=args.batch, lr=args.lr, verbose=True)
     torch.cuda.synchronize()
     t2 = time.time()
     os.makedirs(os.path.dirname(args.out), exist_ok=True)
     net.save(args.out)
-    print(f"data {t1 - t0:.1f} s ({R.shape[0]} pairs), training {t2 - t1:.1f} s, "
+    meta = {"train_n": args.n, "problems": args.problems, "steps": args.steps, "batch": args.batch,
+            "samples": len(ts), "data_seconds": round(t1 - t0, 1), "train_seconds": round(t2 - t1, 1),
+            "loss_first50": round(sum(losses[:50]) / 50, 4), "loss_last50": round(sum(losses[-50:]) / 50, 4),
+            "loss_per_100_steps": [round(sum(losses[i:i + 100]) / len(losses[i:i + 100]), 4)
+                                   for i in range(0, len(losses), 100)],
+            "command": f"python -m autopdex_gb300.train_preconditioner --n {args.n} --problems {args.problems} "
+                       f"--steps {args.steps}"}
+    with open(os.path.splitext(args.out)[0] + ".json", "w") as fh:
+        json.dump(meta, fh, indent=1)
+    print(f"data {t1 - t0:.1f} s ({len(ts)} pairs), training {t2 - t1:.1f} s, "
           f"loss {sum(losses[:50]) / 50:.4f} -> {sum(losses[-50:]) / 50:.4f}; saved {args.out}")
 
 

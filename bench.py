@@ -277,6 +277,9 @@ def gpu_arm(args):
         print(json.dumps(line))
 
 
+TRAIN_N = 256  # resolution the shipped network was trained on (heat_unet_n256.npz)
+
+
 def config4(n=1024, seed=10000, rtol=1e-10):
     """Config 4 (heat, k = exp(GRF), n x n Q1): time to a 1e-10 relative float64 residual for
     plain float64 Jacobi-PCG, mixed Jacobi-PCG and the learned preconditioner in mixed FCG."""
@@ -286,16 +289,19 @@ def config4(n=1024, seed=10000, rtol=1e-10):
     if not os.path.exists(path):
         return {"skipped": "no trained weights"}
     net = learned.UNet.load(path)
-    out = {"workload": f"heat_grf_{n}x{n}_q1 (seed {seed})", "weights": os.path.basename(path)}
+    out = {"workload": f"heat_grf_{n}x{n}_q1 (seed {seed})", "weights": os.path.basename(path),
+           "network_grid": f"{n // max(1, n // TRAIN_N) + 1}^2 nodes (coarsening {max(1, n // TRAIN_N)})"}
     variants = [("plain_fp64_pcg", dict(precision="float64", solver="pcg"), dict(krylov_tol=1e-11)),
-                ("mixed_pcg", dict(precision="mixed", solver="pcg"), dict(krylov_tol=1e-4)),
+                ("mixed_pcg", dict(precision="mixed", solver="pcg"), dict(krylov_tol=1e-5)),
                 ("learned_mixed_fcg", dict(precision="mixed", solver="fcg", **{"type of preconditioner": "learned"}),
-                 dict(krylov_tol=1e-4))]
+                 dict(krylov_tol=1e-5))]
+    factor = max(1, n // TRAIN_N)
     for name, st, kw in variants:
         w = configs.heat_grf(n=n, seed=seed)
         static = dict(w.static_settings, **st)
         if name.startswith("learned"):
-            solver.set_learned_preconditioner(None, learned.GridPreconditioner(net, n, n, w.settings["conductivity"]))
+            solver.set_learned_preconditioner(None, learned.GridPreconditioner(net, n, n, w.settings["conductivity"],
+                                                                                  factor=factor))
         solver.solver(w.dofs, w.settings, static, newton_tol=0.0, newton_rtol=rtol, maxiter=30,
                       krylov_maxiter=400000, **kw)  # warm-up (context, graphs)
         torch.cuda.synchronize()

@@ -179,10 +179,19 @@ int agx_newton(agx_context* ctx, double* dofs, const double* dirichlet_values,
                const agx_newton_opts* opts, agx_newton_info* info);
 /* Registers the preconditioner used by AGX_FCG_MIXED (NULL restores Jacobi). */
 int agx_set_preconditioner(agx_context* ctx, agx_precond_fn fn, void* user);
-/* How AGX_FCG_MIXED applies the registered preconditioner M: 0, z = M(r); 1 (default),
-   two-level: z0 = D^-1 r, r1 = r - K z0, y = M(r1), z = z0 + c y with the energy-optimal
-   c = (r1, y) / (y, K y) -- never a worse step than Jacobi alone. */
-int agx_set_preconditioner_mode(agx_context* ctx, int mode);
+/* How FCG applies the registered preconditioner M (no counterpart in the reference).
+   mode 0: z = M(r).
+   mode 1, two-level: `sweeps` damped Jacobi sweeps z += w D^-1 (r - K z) from z = 0, then
+   y = M(r - K z) and z += c y with the energy-optimal c = (r - K z, y) / (y, K y) -- never a
+   worse step than the sweeps alone.
+   mode 2 (default), symmetric two-level: mode 1 followed by `sweeps` post-smoothing sweeps.
+   w (default 2/3) is the Jacobi damping, in (0, 1]; sweeps (default 1) in 1 .. 16.
+   flags: AGX_PRECOND_CAPTURABLE declares that the callback only enqueues device work on the
+   stream it is given (no synchronisation, allocation or host reads), so that FCG captures
+   its iterations, callback included, into CUDA graphs and replays them; the callback's
+   buffers must then stay valid until the preconditioner is replaced. */
+#define AGX_PRECOND_CAPTURABLE 1
+int agx_set_preconditioner_mode(agx_context* ctx, int mode, double omega, int sweeps, int flags);
 /* Kernel timing.  While enabled, the library brackets its kernel launches with CUDA events
    on its stream and accumulates the elapsed time per category; agx_profile_read
    synchronizes the stream, returns totals (ms) and launch counts, and resets them. */

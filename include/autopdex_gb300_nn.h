@@ -44,6 +44,14 @@ int agx_nn_bias_grad(const void* g, int64_t P, int C, float* db, void* stream);
    vector (scaled to unit rms when normalize; 1/rms written to scale[0]), channel 1 aux */
 int agx_nn_grid_from_vector(const float* r, const float* aux, int Hn, int Wn, int Hp, int Wp, int normalize,
                             float* scale, void* img, void* stream);
+/* Bilinear grid transfer for a network applied on a coarser node grid.  The fine grid has
+   ((Hc - 1) f + 1) x ((Wc - 1) f + 1) nodes (node i*Wf + j) and its node (f I, f J) is coarse
+   node (I, J).  agx_nn_prolong: fine = P coarse, P the bilinear interpolation;
+   agx_nn_restrict: coarse = P^T fine, with coarse nodes whose fine node is flagged in
+   `fixed` (optional, one byte per fine node: the Dirichlet nodes) set to zero. */
+int agx_nn_restrict(const float* fine, const unsigned char* fixed, int Hc, int Wc, int f, float* coarse,
+                    void* stream);
+int agx_nn_prolong(const float* coarse, int Hc, int Wc, int f, float* fine, void* stream);
 /* channel 0 of an NHWC image with C channels -> node vector */
 int agx_nn_vector_from_grid(const void* img, int C, int Hn, int Wn, int Wp, float* z, void* stream);
 

@@ -1,7 +1,7 @@
 """Oracle: the learned preconditioner's U-Net in float64 on the CPU (torch) -- TEST ONLY.
 
 Same layers, parameter names and NHWC tensors as ``autopdex_gb300.learned``: 3x3
-convolutions with zero padding, 2x2 average pooling, nearest 2x upsampling, channel
+convolutions with zero padding, 4x4 average pooling, nearest 4x upsampling, channel
 concatenation (decoder input first, encoder skip second), ReLU everywhere except the output
 layer.  Gradients come from torch autograd in float64, the reference for the GPU's own
 forward and backward kernels.
@@ -22,12 +22,34 @@ def conv(x, w, b, relu):
     return F.relu(y) if relu else y
 
 
+POOL = 4
+
+
 def pool(x):
-    return F.avg_pool2d(x.permute(0, 3, 1, 2), 2).permute(0, 2, 3, 1)
+    return F.avg_pool2d(x.permute(0, 3, 1, 2), POOL).permute(0, 2, 3, 1)
 
 
 def up(x):
-    return F.interpolate(x.permute(0, 3, 1, 2), scale_factor=2, mode="nearest").permute(0, 2, 3, 1)
+    return F.interpolate(x.permute(0, 3, 1, 2), scale_factor=POOL, mode="nearest").permute(0, 2, 3, 1)
+
+
+def prolong(c, f):
+    """Bilinear interpolation of a coarse node field (Hc, Wc) to the fine node grid
+    ((Hc - 1) f + 1, (Wc - 1) f + 1) whose node (f I, f J) is coarse node (I, J)."""
+    import numpy as np
+    c = np.asarray(c, dtype=np.float64)
+
+    def p1(m):
+        P = np.zeros(((m - 1) * f + 1, m))
+        for i in range(P.shape[0]):
+            I, t = divmod(i, f)
+            if I >= m - 1:
+                P[i, m - 1] = 1.0
+            else:
+                P[i, I] += 1.0 - t / f
+                P[i, I + 1] += t / f
+        return P
+    return p1(c.shape[0]) @ c @ p1(c.shape[1]).T
 
 
 def unet(x, P, masks=None):
