@@ -229,7 +229,7 @@ int agx_finalize(agx_context* ctx) {
                     &ctx->f_w2, &ctx->f_w3, &ctx->f_w4})
     if (int rc = alloc(ctx, p, n)) return rc;
   ctx->red_blocks = ctx->sm_count * 8;  // one resident wave of 256-thread blocks
-  ctx->vec_blocks = ctx->sm_count * 2;
+  ctx->vec_blocks = ctx->sm_count * 4;  // reducing vector kernels (16-byte accesses)
   if (int rc = alloc(ctx, &ctx->d_partials, (int64_t)ctx->red_blocks * 4)) return rc;  // up to 4 values per block
   if (int rc = alloc(ctx, &ctx->d_counter, 1)) return rc;
   if (int rc = alloc(ctx, &ctx->d_scal, 1)) return rc;

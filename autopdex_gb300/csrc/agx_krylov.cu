@@ -224,16 +224,49 @@ pcg_init_kernel(int64_t n, const double* __restrict__ b, const T* __restrict__ d
   }
 }
 
-// x += a p; r -= a q; z = Dinv r; rz_new, rr; beta
+// x += a p; r -= a q; z = Dinv r; rz_new, rr; beta.  16-byte vector loads and stores (4 floats
+// or 2 doubles per access) when every vector is 16-byte aligned (the library's own are; a
+// caller's x may not be), a scalar loop for the rest.
+template <typename T>
+struct alignas(16) vec16 {
+  T v[16 / sizeof(T)];
+};
+
 template <typename T>
 __global__ void __launch_bounds__(AGX_BLOCK)
 pcg_update_kernel(int64_t n, T* __restrict__ x, T* __restrict__ r, T* __restrict__ z, const T* __restrict__ p,
                   const T* __restrict__ q, const T* __restrict__ dinv, agx_krylov_scalars* sc, double* partials,
                   unsigned* counter) {
   if (sc->converged) return;
+  constexpr int V = 16 / sizeof(T);
+  using W = vec16<T>;
   const T a = (T)sc->alpha;
   T rz_t = 0, rr_t = 0;  // per-thread partials in T, block and grid sums in float64
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  const bool aligned = ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(r) |
+                         reinterpret_cast<uintptr_t>(z) | reinterpret_cast<uintptr_t>(p) |
+                         reinterpret_cast<uintptr_t>(q) | reinterpret_cast<uintptr_t>(dinv)) & 15u) == 0;
+  const int64_t nv = aligned ? n / V : 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nv; k += stride) {
+    W xv = reinterpret_cast<const W*>(x)[k], rv = reinterpret_cast<const W*>(r)[k];
+    const W pv = reinterpret_cast<const W*>(p)[k], qv = reinterpret_cast<const W*>(q)[k];
+    const W dv = reinterpret_cast<const W*>(dinv)[k];
+    W zv;
+#pragma unroll
+    for (int u = 0; u < V; ++u) {
+      xv.v[u] += a * pv.v[u];
+      const T ri = rv.v[u] - a * qv.v[u];
+      rv.v[u] = ri;
+      const T zi = dv.v[u] * ri;
+      zv.v[u] = zi;
+      rz_t += ri * zi;
+      rr_t += ri * ri;
+    }
+    reinterpret_cast<W*>(x)[k] = xv;
+    reinterpret_cast<W*>(r)[k] = rv;
+    reinterpret_cast<W*>(z)[k] = zv;
+  }
+  for (int64_t i = nv * V + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     x[i] += a * p[i];
     const T ri = r[i] - a * q[i];
     r[i] = ri;

@@ -269,6 +269,11 @@ def gpu_arm(args):
             line["config4"] = config4(n=args.config4_n)
         except Exception as e:  # noqa: BLE001 -- reported, the headline stands
             line["config4"] = {"error": str(e)[:200]}
+    if rank == 0 and args.configs:
+        try:
+            line["other_configs"] = other_configs()
+        except Exception as e:  # noqa: BLE001 -- reported, the headline stands
+            line["other_configs"] = {"error": str(e)[:300]}
     if rank == 0 and not args.no_cpu_baseline and not args.only_mixed:
         line["cpu_baseline"] = cpu_baseline(n, int(info_t[0]), int(tight_kry), budget_s=args.cpu_budget)
     if dist:
@@ -313,6 +318,63 @@ def config4(n=1024, seed=10000, rtol=1e-10):
         out[name] = {"s": time.perf_counter() - t0, "newton": int(info[0]), "krylov": int(li.krylov_iterations),
                      "residual_ratio": li.res_norm / li.res0 if li.res0 else None, "diverged": bool(info[2])}
     out["speedup_learned_vs_plain_fp64"] = out["plain_fp64_pcg"]["s"] / out["learned_mixed_fcg"]["s"]
+    return out
+
+
+def _timed_solve(w, static, step=None, x0=None, rtol=1e-10, **kw):
+    """One solver.solver call (warm context: a first call builds it), CUDA-synchronised wall
+    time, with the Newton and Krylov counts and the final float64 residual ratio."""
+    import torch
+    from autopdex_gb300 import solver
+    st = dict(w.settings)
+    if step is not None:
+        st = step(st)
+    dofs = w.dofs if x0 is None else x0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sol, info = solver.solver(dofs, st, static, newton_tol=0.0, newton_rtol=rtol, maxiter=30, **kw)
+    torch.cuda.synchronize()
+    li = solver.last_info
+    return sol, {"s": time.perf_counter() - t0, "newton": int(info[0]), "krylov": int(li.krylov_iterations),
+                 "residual_ratio": li.res_norm / li.res0 if li.res0 else None, "diverged": bool(info[2])}
+
+
+def other_configs(cook_n=128, cook_rtol=1e-6, heat3d_n=128, heat3d_steps=2):
+    """Configs 1, 3 and 5 beside the headline: plain float64 against mixed precision where the
+    method allows it (BiCGStab, for the non-symmetric backward-Euler tangent, runs in float64).
+
+    Config 3 (Cook, nu = 0.4999) is run at cook_n^2 to a relative Newton residual of cook_rtol:
+    with Jacobi-PCG the float64 Newton residual of this nearly incompressible problem stalls
+    near 4.5e-7 of the first one already at 128^2 (measured: 31 Newton iterations and 1.8 M CG
+    iterations without getting below it), so 1e-10 is out of reach for the plain method."""
+    from autopdex_gb300 import configs
+    out = {}
+    # config 1: 200^2 Poisson, one Newton step with the direct-solver name ('lapack')
+    w = configs.poisson(n=200, solver="lapack")
+    _timed_solve(w, w.static_settings)
+    _, out["config1_poisson_200_fp64_direct"] = _timed_solve(w, w.static_settings)
+    # config 3: Cook membrane, load step 1 of 20, Newton to 1e-10 of the first residual
+    res = {}
+    for name, prec, ktol in (("plain_fp64_pcg", "float64", 1e-8), ("mixed_pcg", "mixed", 1e-5)):
+        w = configs.cook_membrane(n=cook_n, precision=prec)
+        _timed_solve(w, w.static_settings, step=w.steps[0], rtol=cook_rtol, krylov_tol=ktol, krylov_maxiter=400000)
+        _, res[name] = _timed_solve(w, w.static_settings, step=w.steps[0], rtol=cook_rtol, krylov_tol=ktol,
+                                    krylov_maxiter=400000)
+    res["speedup_mixed_vs_plain_fp64"] = res["plain_fp64_pcg"]["s"] / res["mixed_pcg"]["s"]
+    out[f"config3_cook_{cook_n}_load_step_1_rtol_{cook_rtol:g}"] = res
+    # config 5: 3-D nonlinear backward-Euler heat, the first time steps (Newton + BiCGStab f64)
+    import numpy as np
+    w = configs.heat_transient(n=heat3d_n)
+    T = np.asarray(w.raw["T0"], dtype=np.float64)
+    steps = []
+    for k in range(heat3d_steps + 1):
+        w.settings["dofs n"] = {"T": T.copy()}
+        sol, r = _timed_solve(w, w.static_settings, x0={"T": T.copy()}, krylov_tol=1e-11)
+        T = np.asarray(sol["T"])
+        if k:
+            steps.append(r)  # the first call builds the context and is not counted
+    out[f"config5_heat_be_{heat3d_n}^3_fp64"] = {"steps_timed": heat3d_steps, "s_per_step": sum(r["s"] for r in steps) /
+                                                 len(steps), "per_step": steps}
     return out
 
 
@@ -411,6 +473,7 @@ def main():
     ap.add_argument("--only-mixed", action="store_true", help="time the mixed path only (profiling runs)")
     ap.add_argument("--no-config4", action="store_true")
     ap.add_argument("--config4-n", type=int, default=1024)
+    ap.add_argument("--configs", action="store_true", help="also time configs 1, 3 and 5 (plain vs mixed)")
     ap.add_argument("--ref-newton-iters", type=int, default=4)
     ap.add_argument("--ref-cg-iters", type=int, default=3000)
     args = ap.parse_args()
