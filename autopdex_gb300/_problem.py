@@ -190,13 +190,15 @@ class Problem:
         except (OSError, ValueError):
             cache = {}
         if key in cache:
-            self._call("agx_set_tuning", int(cache[key]["spmv_tpr"]))
+            self.spmv_tpr = int(cache[key]["spmv_tpr"])
+            self._call("agx_set_tuning", self.spmv_tpr)
         else:
             self._call("agx_assemble", C.c_void_p(dofs_dev.data_ptr()), None, N.AGX_F32)
             tpr = C.c_int()
             ms = C.c_float()
             self._call("agx_autotune", C.byref(tpr), C.byref(ms))
             cache[key] = {"spmv_tpr": int(tpr.value), "spmv_ms": float(ms.value)}
+            self.spmv_tpr = int(tpr.value)
             try:
                 os.makedirs(os.path.dirname(path), exist_ok=True)
                 with open(path, "w") as fh:

@@ -90,18 +90,34 @@ __device__ __forceinline__ void bsr_row(int64_t row, int sub, const int32_t* __r
 #pragma unroll
   for (int i = 0; i < NDOF; ++i) y[i] = 0;
   const int beg = rowptr[row], end = rowptr[row + 1];
-  for (int k = beg + sub; k < end; k += TPR) {
-    const int64_t c = col[k];
-    T xc[NDOF];
+  // two blocks per lane and trip: both blocks' columns and value planes are requested before
+  // any gather or FMA, so each lane keeps twice the loads in flight; matrix data is streamed
+  // (evict-first) so that the gathered vectors stay in L2
+  for (int k = beg + sub; k < end; k += 2 * TPR) {
+    const int k2 = k + TPR;
+    const bool two = k2 < end;
+    const int64_t c1 = __ldcs(col + k);
+    const int64_t c2 = two ? __ldcs(col + k2) : c1;
+    T v1[NDOF * NDOF], v2[NDOF * NDOF];
+#pragma unroll
+    for (int e = 0; e < NDOF * NDOF; ++e) {
+      v1[e] = __ldcs(vals + (int64_t)e * nnzb + k);
+      v2[e] = two ? __ldcs(vals + (int64_t)e * nnzb + k2) : T(0);
+    }
+    T x1[NDOF], x2[NDOF];
 #pragma unroll
     for (int j = 0; j < NDOF; ++j) {
-      xc[j] = x[c * NDOF + j];
-      if constexpr (DIR) xc[j] += beta * pold[c * NDOF + j];
+      x1[j] = x[c1 * NDOF + j];
+      x2[j] = two ? x[c2 * NDOF + j] : T(0);
+      if constexpr (DIR) {
+        x1[j] += beta * pold[c1 * NDOF + j];
+        if (two) x2[j] += beta * pold[c2 * NDOF + j];
+      }
     }
 #pragma unroll
     for (int i = 0; i < NDOF; ++i)
 #pragma unroll
-      for (int j = 0; j < NDOF; ++j) y[i] += vals[(int64_t)(i * NDOF + j) * nnzb + k] * xc[j];
+      for (int j = 0; j < NDOF; ++j) y[i] += v1[i * NDOF + j] * x1[j] + v2[i * NDOF + j] * x2[j];
   }
 #pragma unroll
   for (int o = TPR / 2; o >= 1; o >>= 1)

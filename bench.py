@@ -252,7 +252,8 @@ def gpu_arm(args):
         "final_residual_ratio": res_end / res0 if res0 else None,
         "kernel_ms_per_step": {k: v / args.steps for k, v in shares.items()},
         "kernel_launches_per_step": {k: v / args.steps for k, v in launches.items()},
-        "roofline": {"bound": "hbm", "kernel": "spmv_dot_kernel<float,3,8> (BSR 3x3 SpMV, direction update, dot)",
+        "roofline": {"bound": "hbm", "kernel": f"spmv_dot_kernel<float,3,{getattr(prob, 'spmv_tpr', 8)}> "
+                                                "(BSR 3x3 SpMV, direction update, dot)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic, "algorithmic_bytes": spmv_bytes,
                      "avg_launch_ms": spmv_avg_ms},
