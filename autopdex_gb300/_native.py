@@ -77,7 +77,7 @@ _SIGNATURES = {
     "agx_profile": (C.c_int, [_P, C.c_int]),
     "agx_profile_read": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     "agx_autotune": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
-    "agx_set_tuning": (C.c_int, [_P, C.c_int]),
+    "agx_set_tuning": (C.c_int, [_P, C.c_int, C.c_int]),
     "agx_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
 "agx_pcg_noalloc": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int, _P, _P, C.c_double, C.c_int, _P,
                                 C.POINTER(SolveInfo), C.c_char_p, C.c_int]),

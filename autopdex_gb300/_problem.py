@@ -173,16 +173,17 @@ class Problem:
         host = torch.from_numpy(np.ascontiguousarray(flatten(values, self.key)))
         return host.pin_memory().to(self.device, non_blocking=True) if self.n_dofs > 4096 else host.to(self.device)
 
-    def ensure_tuned(self, dofs_dev):
-        """Lanes per block row of the Krylov product from the autotuner, cached per GPU model
-        and problem class in autopdex_gb300/_lib/autotune.json."""
-        if getattr(self, "_tuned", False):
+    def ensure_tuned(self, dofs_dev, dtype=N.AGX_F32):
+        """Lanes per block row of the Krylov product (float32 or float64) from the autotuner,
+        cached per GPU model, precision and problem class in autopdex_gb300/_lib/autotune.json."""
+        tuned = getattr(self, "_tuned", set())
+        if dtype in tuned:
             return
         import json
         from . import build as _b
         path = os.path.join(_b.LIBDIR, "autotune.json")
-        key = f"{torch.cuda.get_device_name(self.device)}|ndof={self.ndof}|dim={self.dim}|" \
-              f"nnzb=2^{int(np.log2(max(1, self.nnzb)))}"
+        key = f"{torch.cuda.get_device_name(self.device)}|{'f32' if dtype == N.AGX_F32 else 'f64'}|" \
+              f"ndof={self.ndof}|dim={self.dim}|nnzb=2^{int(np.log2(max(1, self.nnzb)))}"
         cache = {}
         try:
             with open(path) as fh:
@@ -190,22 +191,26 @@ class Problem:
         except (OSError, ValueError):
             cache = {}
         if key in cache:
-            self.spmv_tpr = int(cache[key]["spmv_tpr"])
-            self._call("agx_set_tuning", self.spmv_tpr)
+            tpr_v = int(cache[key]["spmv_tpr"])
+            self._call("agx_set_tuning", dtype, tpr_v)
         else:
-            self._call("agx_assemble", C.c_void_p(dofs_dev.data_ptr()), None, N.AGX_F32)
+            self._call("agx_assemble", C.c_void_p(dofs_dev.data_ptr()), None, dtype)
             tpr = C.c_int()
             ms = C.c_float()
             self._call("agx_autotune", C.byref(tpr), C.byref(ms))
             cache[key] = {"spmv_tpr": int(tpr.value), "spmv_ms": float(ms.value)}
-            self.spmv_tpr = int(tpr.value)
+            tpr_v = int(tpr.value)
             try:
                 os.makedirs(os.path.dirname(path), exist_ok=True)
                 with open(path, "w") as fh:
                     json.dump(cache, fh, indent=1)
             except OSError:
                 pass
-        self._tuned = True
+        if dtype == N.AGX_F32:
+            self.spmv_tpr = tpr_v
+        else:
+            self.spmv_tpr64 = tpr_v
+        self._tuned = tuned | {dtype}
 
     def matrix(self, dtype):
         rp, col, vals = C.c_void_p(), C.c_void_p(), C.c_void_p()

@@ -30,6 +30,10 @@ struct agx_element_set {
   double* d_elem_field = nullptr;        // one value per element (owned)
   const double* d_node_field = nullptr;  // one value per DOF (caller-owned device pointer)
   double* d_geo = nullptr;  // float64 geometry cache: per element, Gauss point and node, (g_a, w det J)
+  // structured quad grid of the mesher's numbering (element i ny + j has nodes (i, j), (i, j+1),
+  // (i+1, j+1), (i+1, j), node (i, j) = i (ny + 1) + j) whose pattern rows are exactly the
+  // in-range 3 x 3 node stencils; 0 when the set is not such a grid
+  int grid_nx = 0, grid_ny = 0;
 };
 
 // Scalars of one Krylov solve, kept in device memory so that iterations need no host
@@ -137,7 +141,7 @@ struct agx_context {
   int precond_sweeps = 1;
   int precond_capturable = 0;  // the callback only enqueues work on the stream it is given
   int64_t precond_gen = 0;     // bumped whenever the callback or its mode changes
-  int spmv_tpr = 0;      // lanes per block row of the Krylov product (0: default; set by the autotuner)  // 0: z = M(r); 1: z = D^-1 r + c M(r - A D^-1 r), c energy-optimal
+  int spmv_tpr[2] = {0, 0};  // lanes per block row of the Krylov product, float64 / float32 (0: default)
 };
 
 // ------------------------------------------------------------------------------------

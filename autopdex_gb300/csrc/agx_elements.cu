@@ -369,6 +369,147 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
   }
 }
 
+// ---- atomic-free tangent of a structured quad grid ---------------------------------------
+// For a set that detect_structured_grid recognised and a scalar potential model (K_ab =
+// k int g_a . g_b, symmetric), the tangent is written row by row: a block owns a tile of
+// GT_Y x GT_X nodes, computes the 4 x 4 matrices of the (GT_Y + 1) x (GT_X + 1) elements that
+// touch them (its own and one halo row and column) into shared memory, and every thread sums
+// the row of its node from its four incident elements and writes it once.  No atomics, no
+// memset, no scatter map: DRAM traffic is coordinates, element coefficients, row pointers and
+// the values, each once.  Dirichlet rows become identity rows and Dirichlet columns zeros, as
+// in the element scatter.
+constexpr int GT_X = 32, GT_Y = 8;
+constexpr int GT_THREADS = 320;  // >= the (GT_Y + 1) x (GT_X + 1) = 297 element matrices: one round
+
+__device__ __forceinline__ int sym4(int a, int b) {
+  const int lo = a < b ? a : b, hi = a < b ? b : a;
+  return lo * 4 - lo * (lo - 1) / 2 + (hi - lo);  // row-major upper triangle of a 4 x 4
+}
+
+template <int MODEL, typename T>
+__global__ void __launch_bounds__(GT_THREADS)
+grid_tangent_kernel(int nx, int ny, const double* __restrict__ coords, const double* __restrict__ elem_field,
+                    const uint8_t* __restrict__ dmask_node, const int32_t* __restrict__ rowptr, T* __restrict__ vals) {
+  constexpr int EX = GT_X + 1, EY = GT_Y + 1;
+  constexpr int MX = GT_X + 2, MY = GT_Y + 2;  // node window of the tile with a one-node ring
+  __shared__ T ke[EY * EX][10];
+  __shared__ T stage[GT_Y][GT_X * 9];
+  __shared__ uint8_t fixed[MY][MX];
+  const int tid = threadIdx.x;
+  const int i0 = blockIdx.y * GT_Y, j0 = blockIdx.x * GT_X;
+  const int64_t W = (int64_t)ny + 1;  // nodes per grid row
+  // local node a of element (i, j) sits at node (i + oi[a], j + oj[a]) (mesher order)
+  constexpr int oi[4] = {0, 0, 1, 1}, oj[4] = {0, 1, 1, 0};
+  // row pointers of the owned rows and the Dirichlet flags of the node window, requested
+  // before the element integrals so that their latency overlaps the arithmetic
+  const int ty = tid / GT_X, tx = tid % GT_X;  // warps 0 .. GT_Y - 1: one node row each
+  const int i = i0 + ty, j = j0 + tx;
+  const bool row_warp = ty < GT_Y && i <= nx;
+  const int64_t p = (int64_t)i * W + j;
+  int32_t base = 0, span = 0, rp = 0;
+  if (row_warp) {
+    const int jl = (j0 + GT_X - 1 < ny ? j0 + GT_X - 1 : ny);  // last owned node of this grid row
+    base = rowptr[(int64_t)i * W + j0];
+    span = rowptr[(int64_t)i * W + jl + 1] - base;
+    if (j <= ny) rp = rowptr[p];
+  }
+  for (int t = tid; t < MY * MX; t += GT_THREADS) {
+    const int ni = i0 - 1 + t / MX, nj = j0 - 1 + t % MX;
+    fixed[t / MX][t % MX] =
+        (ni >= 0 && ni <= nx && nj >= 0 && nj <= ny) ? (uint8_t)(dmask_node[(int64_t)ni * W + nj] & 1u) : (uint8_t)0;
+  }
+  for (int t = tid; t < EY * EX; t += GT_THREADS) {
+    const int ei = i0 - 1 + t / EX, ej = j0 - 1 + t % EX;
+    T K[10];
+#pragma unroll
+    for (int u = 0; u < 10; ++u) K[u] = 0;
+    if (ei >= 0 && ei < nx && ej >= 0 && ej < ny) {
+      const int64_t n00 = (int64_t)ei * W + ej;
+      T x[4][2];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        const double2 c = reinterpret_cast<const double2*>(coords)[n00 + oi[a] * W + oj[a]];  // (x, y) of a node
+        x[a][0] = (T)c.x;
+        x[a][1] = (T)c.y;
+      }
+      T k = 1;
+      if constexpr (MODEL == AGX_MODEL_HEAT_POTENTIAL) k = elem_field ? (T)elem_field[(int64_t)ei * ny + ej] : T(1);
+      // w det J g_a . g_b = dN_a^T M dN_b with M = adj(J) adj(J)^T / det J (Gauss weight 1):
+      // per point J, det J and the three entries of M, then three FMAs per pair with the
+      // reference derivatives as compile-time constants
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        T dN[4][2];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          const T f0 = (T(1) + T(node_sign<AGX_QUAD4>(a, 0)) * (T)gauss_point(q & 1)) * T(0.5);
+          const T f1 = (T(1) + T(node_sign<AGX_QUAD4>(a, 1)) * (T)gauss_point((q >> 1) & 1)) * T(0.5);
+          dN[a][0] = T(node_sign<AGX_QUAD4>(a, 0)) * T(0.5) * f1;
+          dN[a][1] = T(node_sign<AGX_QUAD4>(a, 1)) * T(0.5) * f0;
+        }
+        T J00 = 0, J01 = 0, J10 = 0, J11 = 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          J00 += x[a][0] * dN[a][0];
+          J01 += x[a][0] * dN[a][1];
+          J10 += x[a][1] * dN[a][0];
+          J11 += x[a][1] * dN[a][1];
+        }
+        const T rdet = T(1) / (J00 * J11 - J01 * J10);
+        const T M00 = (J11 * J11 + J01 * J01) * rdet;
+        const T M01 = -(J11 * J10 + J01 * J00) * rdet;
+        const T M11 = (J10 * J10 + J00 * J00) * rdet;
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = a; b < 4; ++b)
+            K[sym4(a, b)] += M00 * (dN[a][0] * dN[b][0]) + M01 * (dN[a][0] * dN[b][1] + dN[a][1] * dN[b][0]) +
+                             M11 * (dN[a][1] * dN[b][1]);
+      }
+#pragma unroll
+      for (int u = 0; u < 10; ++u) K[u] *= k;
+    }
+#pragma unroll
+    for (int u = 0; u < 10; ++u) ke[t][u] = K[u];
+  }
+  __syncthreads();
+  if (!row_warp) return;  // whole warps: the extra element warps and rows past the grid
+  const bool own = j <= ny;
+  if (own) {
+    T v[9];
+#pragma unroll
+    for (int u = 0; u < 9; ++u) v[u] = 0;
+    if (fixed[ty + 1][tx + 1]) {
+      v[4] = T(1);
+    } else {
+      // out-of-range elements hold zero matrices in shared memory: no tests needed
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        const int t = (ty + 1 - oi[a]) * EX + (tx + 1 - oj[a]);
+#pragma unroll
+        for (int b = 0; b < 4; ++b) v[(oi[b] - oi[a] + 1) * 3 + (oj[b] - oj[a] + 1)] += ke[t][sym4(a, b)];
+      }
+      // Dirichlet columns are deleted
+#pragma unroll
+      for (int di = 0; di < 3; ++di)
+#pragma unroll
+        for (int dj = 0; dj < 3; ++dj)
+          if (fixed[ty + di][tx + dj]) v[di * 3 + dj] = T(0);
+    }
+    // the row's entries are the in-range stencil neighbours in column order; stage the warp's
+    // rows (consecutive nodes: one contiguous range of values) for a coalesced store
+    const int32_t off = rp - base;
+    int idx = 0;
+#pragma unroll
+    for (int di = -1; di <= 1; ++di)
+#pragma unroll
+      for (int dj = -1; dj <= 1; ++dj)
+        if (i + di >= 0 && i + di <= nx && j + dj >= 0 && j + dj <= ny) stage[ty][off + idx++] = v[(di + 1) * 3 + (dj + 1)];
+  }
+  __syncwarp();
+  for (int u = tx; u < span; u += GT_X) vals[base + u] = stage[ty][u];
+}
+
 // prescribed diagonal entries of the (zeroed) value array set to one
 template <typename T>
 __global__ void set_dirichlet_diag(int64_t n_dir, const int32_t* __restrict__ dir_dofs,
@@ -450,13 +591,42 @@ int build_geometry(agx_context* ctx, agx_element_set& s) {
 
 }  // namespace
 
+// the set whose tangent the structured row kernel writes on its own, or null
+static agx_element_set* grid_tangent_set(agx_context* ctx) {
+  agx_element_set* hit = nullptr;
+  int with_k = 0;
+  for (auto& s : ctx->sets) {
+    if (s.model == AGX_MODEL_NEUMANN) continue;  // no tangent contribution
+    ++with_k;
+    if (s.grid_nx > 0 && ctx->ndof == 1 &&
+        (s.model == AGX_MODEL_HEAT_POTENTIAL || s.model == AGX_MODEL_POISSON_SINCOS))
+      hit = &s;
+  }
+  return with_k == 1 ? hit : nullptr;
+}
+
+template <typename T>
+static void launch_grid_tangent(agx_context* ctx, agx_element_set& s, T* vals) {
+  const dim3 grid((unsigned)((s.grid_ny + 1 + GT_X - 1) / GT_X), (unsigned)((s.grid_nx + 1 + GT_Y - 1) / GT_Y));
+  if (s.model == AGX_MODEL_HEAT_POTENTIAL)
+    grid_tangent_kernel<AGX_MODEL_HEAT_POTENTIAL, T><<<grid, GT_THREADS, 0, ctx->stream>>>(
+        s.grid_nx, s.grid_ny, ctx->d_coords, s.d_elem_field, ctx->d_dmask_node, ctx->d_rowptr, vals);
+  else
+    grid_tangent_kernel<AGX_MODEL_POISSON_SINCOS, T><<<grid, GT_THREADS, 0, ctx->stream>>>(
+        s.grid_nx, s.grid_ny, ctx->d_coords, s.d_elem_field, ctx->d_dmask_node, ctx->d_rowptr, vals);
+  ctx->n_launches += 1;
+}
+
 int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, int tangent_dtype) {
   const int bs = ctx->ndof * ctx->ndof;
+  agx_element_set* gset = tangent_dtype >= 0 ? grid_tangent_set(ctx) : nullptr;
   if (residual || tangent_dtype == AGX_F64)
     for (auto& s : ctx->sets)
       if (int rc = build_geometry(ctx, s)) return rc;
   if (residual) AGX_CUDA(ctx, cudaMemsetAsync(residual, 0, sizeof(double) * ctx->n_dofs, ctx->stream));
-  if (tangent_dtype == AGX_F64) {
+  if (gset) {
+    // every entry of every row is written by the row kernel: no zeroing, no diagonal pass
+  } else if (tangent_dtype == AGX_F64) {
     AGX_CUDA(ctx, cudaMemsetAsync(ctx->d_vals64, 0, sizeof(double) * ctx->nnzb * bs, ctx->stream));
     if (ctx->n_dir > 0)
       set_dirichlet_diag<double><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(
@@ -469,7 +639,21 @@ int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, in
   }
   for (auto& s : ctx->sets) {
     int rc = AGX_OK;
-    if (tangent_dtype == AGX_F64) {
+    if (gset == &s) {
+      {
+        agx_prof_scope ps(ctx, AGX_PROF_TANGENT);
+        if (tangent_dtype == AGX_F64)
+          launch_grid_tangent<double>(ctx, s, ctx->d_vals64);
+        else
+          launch_grid_tangent<float>(ctx, s, ctx->d_vals32);
+      }
+      if (residual) {
+        agx_prof_scope ps(ctx, AGX_PROF_RESIDUAL);
+        rc = dispatch<double, true, false>(ctx, s, dofs, residual, (double*)nullptr);
+      }
+    } else if (gset && s.model != AGX_MODEL_NEUMANN) {
+      rc = AGX_ERR_STATE;  // unreachable: the row kernel serves the only set with a tangent
+    } else if (tangent_dtype == AGX_F64) {
       agx_prof_scope ps(ctx, AGX_PROF_TANGENT);
       rc = residual ? dispatch<double, true, true>(ctx, s, dofs, residual, ctx->d_vals64)
                     : dispatch<double, false, true>(ctx, s, dofs, nullptr, ctx->d_vals64);
@@ -490,7 +674,7 @@ int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, in
     if (rc != AGX_OK) return rc;
     AGX_CHECK_LAUNCH(ctx);
   }
-  if (tangent_dtype >= 0) ctx->n_launches += (ctx->n_dir > 0 ? 2 : 1);  // Dirichlet diagonal + inverse diagonal
+  if (tangent_dtype >= 0) ctx->n_launches += (ctx->n_dir > 0 && !gset ? 2 : 1);  // Dirichlet diagonal + inverse diagonal
   if (tangent_dtype == AGX_F64) {
     inverse_diagonal<double><<<agx_grid(ctx, ctx->n_dofs), AGX_BLOCK, 0, ctx->stream>>>(
         ctx->n_dofs, ctx->ndof, ctx->nnzb, ctx->d_diagpos, ctx->d_vals64, ctx->d_dinv64);

@@ -12,6 +12,8 @@
 // launches iterations in chunks and reads the scalars only between chunks.
 #include <algorithm>
 
+#include <type_traits>
+
 #include "agx_common.cuh"
 
 namespace {
@@ -638,6 +640,7 @@ template <typename T, int ND>
 void spmv_dot_nd(agx_context* ctx, int tpr, const T* vals, const T* z, const T* pold, T* pnew, T* q,
                  const T* rflex) {
   switch (tpr) {
+    case 1: spmv_dot_variant<T, ND, 1>(ctx, vals, z, pold, pnew, q, rflex); break;
     case 2: spmv_dot_variant<T, ND, 2>(ctx, vals, z, pold, pnew, q, rflex); break;
     case 4: spmv_dot_variant<T, ND, 4>(ctx, vals, z, pold, pnew, q, rflex); break;
     case 16: spmv_dot_variant<T, ND, 16>(ctx, vals, z, pold, pnew, q, rflex); break;
@@ -650,7 +653,8 @@ template <typename T>
 void launch_spmv_dot(agx_context* ctx, const T* vals, const T* z, const T* pold, T* pnew, T* q,
                      const T* rflex = nullptr) {
   agx_prof_scope ps(ctx, AGX_PROF_SPMV);
-  const int tpr = ctx->spmv_tpr > 0 ? ctx->spmv_tpr : default_tpr(ctx);
+  const int tuned = ctx->spmv_tpr[std::is_same<T, float>::value ? 1 : 0];
+  const int tpr = tuned > 0 ? tuned : default_tpr(ctx);
   if (ctx->ndof == 1) spmv_dot_nd<T, 1>(ctx, tpr, vals, z, pold, pnew, q, rflex);
   else if (ctx->ndof == 2) spmv_dot_nd<T, 2>(ctx, tpr, vals, z, pold, pnew, q, rflex);
   else spmv_dot_nd<T, 3>(ctx, tpr, vals, z, pold, pnew, q, rflex);
@@ -701,7 +705,7 @@ int run_chunk(agx_context* ctx, int slot, const void* x, int every, int kn, F&& 
     AGX_CUDA(ctx, cudaEventCreateWithFlags(&ctx->graph_ev[1], cudaEventDisableTiming));
   }
   const cudaStream_t gs = legacy ? ctx->graph_stream : work;
-  if (!gr.exec || gr.key_x != x || gr.every != every || gr.prof != ctx->prof_on || gr.tpr != ctx->spmv_tpr ||
+  if (!gr.exec || gr.key_x != x || gr.every != every || gr.prof != ctx->prof_on || gr.tpr != ctx->spmv_tpr[0] * 64 + ctx->spmv_tpr[1] ||
       gr.pc_key != pc_key) {
     if (gr.exec) cudaGraphExecDestroy(gr.exec);
     gr.exec = nullptr;
@@ -724,7 +728,7 @@ int run_chunk(agx_context* ctx, int slot, const void* x, int every, int kn, F&& 
     gr.key_x = x;
     gr.every = every;
     gr.prof = ctx->prof_on;
-    gr.tpr = ctx->spmv_tpr;
+    gr.tpr = ctx->spmv_tpr[0] * 64 + ctx->spmv_tpr[1];
     gr.pc_key = pc_key;
   }
   if (legacy) {
@@ -788,28 +792,52 @@ void agx_launch_planes_to_blocks(agx_context* ctx, const float* planes, float* b
   ctx->n_launches += 1;
 }
 
-// Times the fused float32 product for every lanes-per-row candidate on the assembled matrix
-// and keeps the fastest (the Krylov scalars are reset afterwards by the next solve).
+template <typename T>
+__global__ void fill_kernel(int64_t n, T* __restrict__ v, T value) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v[i] = value;
+}
+
+// Times the fused product for every lanes-per-row candidate on the last assembled tangent (its
+// precision) and keeps the fastest (the Krylov scalars are reset afterwards by the next solve).
+// The operand is all ones and the solve scalars are cleared before every timed launch: a
+// product whose (p, A p) came out zero would flag a breakdown and turn the following launches
+// into no-ops.
 int agx_autotune_spmv(agx_context* ctx, int* chosen, float* best_ms) {
-  if (ctx->tangent_valid != AGX_F32) return agx_fail(ctx, AGX_ERR_STATE, "autotune needs a float32 tangent");
-  const int cands[4] = {2, 4, 8, 16};
+  if (ctx->tangent_valid != AGX_F32 && ctx->tangent_valid != AGX_F64)
+    return agx_fail(ctx, AGX_ERR_STATE, "autotune needs an assembled tangent");
+  const bool f32 = ctx->tangent_valid == AGX_F32;
+  const int cands[5] = {1, 2, 4, 8, 16};
   cudaEvent_t e0, e1;
   AGX_CUDA(ctx, cudaEventCreate(&e0));
   AGX_CUDA(ctx, cudaEventCreate(&e1));
   AGX_CUDA(ctx, cudaMemsetAsync(ctx->d_scal, 0, sizeof(agx_krylov_scalars), ctx->stream));
-  AGX_CUDA(ctx, cudaMemsetAsync(ctx->f_z, 0, sizeof(float) * ctx->n_dofs, ctx->stream));
+  const int gv = agx_grid(ctx, ctx->n_dofs);
+  fill_kernel<float><<<gv, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dofs, ctx->f_z, 1.0f);
+  fill_kernel<double><<<gv, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dofs, ctx->d_z, 1.0);
   AGX_CUDA(ctx, cudaMemsetAsync(ctx->f_p, 0, sizeof(float) * ctx->n_dofs, ctx->stream));
+  AGX_CUDA(ctx, cudaMemsetAsync(ctx->d_p, 0, sizeof(double) * ctx->n_dofs, ctx->stream));
   float best = 1e30f;
   int pick = default_tpr(ctx);
   for (int c : cands) {
-    if (ctx->ndof == 3 && c == 2) continue;
+    if (ctx->ndof == 3 && c < 4) continue;
     auto run = [&]() {
-      if (ctx->ndof == 1)
-        spmv_dot_nd<float, 1>(ctx, c, ctx->d_vals32, ctx->f_z, ctx->f_p, ctx->f_rold, ctx->f_q, nullptr);
-      else if (ctx->ndof == 2)
-        spmv_dot_nd<float, 2>(ctx, c, ctx->d_vals32, ctx->f_z, ctx->f_p, ctx->f_rold, ctx->f_q, nullptr);
-      else
-        spmv_dot_nd<float, 3>(ctx, c, ctx->d_vals32, ctx->f_z, ctx->f_p, ctx->f_rold, ctx->f_q, nullptr);
+      cudaMemsetAsync(ctx->d_scal, 0, sizeof(agx_krylov_scalars), ctx->stream);
+      if (f32) {
+        if (ctx->ndof == 1)
+          spmv_dot_nd<float, 1>(ctx, c, ctx->d_vals32, ctx->f_z, ctx->f_p, ctx->f_rold, ctx->f_q, nullptr);
+        else if (ctx->ndof == 2)
+          spmv_dot_nd<float, 2>(ctx, c, ctx->d_vals32, ctx->f_z, ctx->f_p, ctx->f_rold, ctx->f_q, nullptr);
+        else
+          spmv_dot_nd<float, 3>(ctx, c, ctx->d_vals32, ctx->f_z, ctx->f_p, ctx->f_rold, ctx->f_q, nullptr);
+      } else {
+        if (ctx->ndof == 1)
+          spmv_dot_nd<double, 1>(ctx, c, ctx->d_vals64, ctx->d_z, ctx->d_p, ctx->d_s, ctx->d_q, nullptr);
+        else if (ctx->ndof == 2)
+          spmv_dot_nd<double, 2>(ctx, c, ctx->d_vals64, ctx->d_z, ctx->d_p, ctx->d_s, ctx->d_q, nullptr);
+        else
+          spmv_dot_nd<double, 3>(ctx, c, ctx->d_vals64, ctx->d_z, ctx->d_p, ctx->d_s, ctx->d_q, nullptr);
+      }
     };
     for (int w = 0; w < 3; ++w) run();
     AGX_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
@@ -827,7 +855,7 @@ int agx_autotune_spmv(agx_context* ctx, int* chosen, float* best_ms) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   AGX_CHECK_LAUNCH(ctx);
-  ctx->spmv_tpr = pick;
+  ctx->spmv_tpr[f32 ? 1 : 0] = pick;
   if (chosen) *chosen = pick;
   if (best_ms) *best_ms = best;
   return AGX_OK;

@@ -32,6 +32,33 @@ void parallel_for(int64_t n, F&& f) {
   for (auto& t : th) t.join();
 }
 
+// A QUAD4 set that is the mesher's structured nx x ny grid over all nodes, with every pattern
+// row the in-range 3 x 3 stencil of its node: then a node row's entries, in column order, are
+// its stencil neighbours in (di, dj) order, and the tangent can be assembled row by row.
+void detect_structured_grid(agx_context* ctx, agx_element_set& s, const std::vector<int32_t>& rowptr) {
+  s.grid_nx = s.grid_ny = 0;
+  if (s.elem_type != AGX_QUAD4 || ctx->dim != 2 || s.n_elem < 1) return;
+  const int32_t* c = s.h_conn.data();
+  const int64_t ny = (int64_t)c[3] - 1;
+  if (ny < 1 || s.n_elem % ny) return;
+  const int64_t nx = s.n_elem / ny;
+  if ((nx + 1) * (ny + 1) != ctx->n_nodes) return;
+  for (int64_t i = 0; i < nx; ++i)
+    for (int64_t j = 0; j < ny; ++j) {
+      const int32_t* e = c + (i * ny + j) * 4;
+      const int64_t n00 = i * (ny + 1) + j;
+      if (e[0] != n00 || e[1] != n00 + 1 || e[2] != n00 + ny + 2 || e[3] != n00 + ny + 1) return;
+    }
+  for (int64_t i = 0; i <= nx; ++i)
+    for (int64_t j = 0; j <= ny; ++j) {
+      const int64_t ri = (i > 0) + 1 + (i < nx), rj = (j > 0) + 1 + (j < ny);
+      const int64_t p = i * (ny + 1) + j;
+      if (rowptr[p + 1] - rowptr[p] != ri * rj) return;
+    }
+  s.grid_nx = (int)nx;
+  s.grid_ny = (int)ny;
+}
+
 }  // namespace
 
 int agx_build_pattern(agx_context* ctx) {
@@ -110,6 +137,7 @@ int agx_build_pattern(agx_context* ctx) {
         }
     });
   }
+  for (auto& s : ctx->sets) detect_structured_grid(ctx, s, rowptr);
   // upload
   const int bs = ctx->ndof * ctx->ndof;
   AGX_CUDA(ctx, cudaMalloc(&ctx->d_rowptr, sizeof(int32_t) * (nn + 1)));

@@ -6,6 +6,8 @@
         # launched `reps` times (a small, self-contained case for ncu captures of conv3x3_tc)
     python -m autopdex_gb300.diag assembly --workload heat --size 1024 --reps 20
         # tangent / residual assembly passes of one workload, timed with CUDA events
+    python -m autopdex_gb300.diag solve --workload heat --size 1024 --precision float64 --krylov-tol 1e-11
+        # one solver.solver call (after a warm-up call) with per-category kernel times
 """
 import argparse
 import os
@@ -89,12 +91,43 @@ def assembly(workload, size, reps):
     print(json.dumps(out))
 
 
+def solve(workload, size, precision, krylov_tol):
+    import ctypes as C
+    import json
+    import time
+    import torch
+    from autopdex_gb300 import configs, solver, _native as N
+    from autopdex_gb300._problem import get_problem
+    w = configs.heat_grf(n=size, seed=10000, precision=precision) if workload == "heat" else \
+        configs.poisson(n=size, precision=precision)
+    kw = dict(newton_tol=0.0, newton_rtol=1e-10, maxiter=30, krylov_tol=krylov_tol, krylov_maxiter=400000)
+    solver.solver(w.dofs, w.settings, w.static_settings, **kw)
+    prob = get_problem(w.dofs, w.settings, w.static_settings)
+    prob._call("agx_profile", 1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, info = solver.solver(w.dofs, w.settings, w.static_settings, **kw)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    ms = (C.c_double * N.AGX_PROF_CATEGORIES)()
+    cnt = (C.c_int64 * N.AGX_PROF_CATEGORIES)()
+    prob._call("agx_profile_read", ms, cnt)
+    prob._call("agx_profile", 0)
+    names = ["tangent", "residual", "spmv", "vector", "precond"]
+    print(json.dumps({"workload": w.name, "precision": precision, "s (profiled, no graphs)": dt,
+                      "newton": int(info[0]), "krylov": int(solver.last_info.krylov_iterations),
+                      "ms": {n: ms[i] for i, n in enumerate(names)},
+                      "launches": {n: int(cnt[i]) for i, n in enumerate(names)}}))
+
+
 def main():
     if len(sys.argv) < 2 or sys.argv[1] == "probe":
         probe()
         return
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["conv", "assembly"])
+    ap.add_argument("what", choices=["conv", "assembly", "solve"])
+    ap.add_argument("--precision", default="float64")
+    ap.add_argument("--krylov-tol", type=float, default=1e-11)
     ap.add_argument("--size", type=int, default=1088)
     ap.add_argument("--layer", default="e0b")
     ap.add_argument("--workload", default="heat", choices=["heat", "poisson", "neo_hooke"])
@@ -102,8 +135,10 @@ def main():
     a = ap.parse_args()
     if a.what == "conv":
         conv(a.size, a.layer, a.reps)
-    else:
+    elif a.what == "assembly":
         assembly(a.workload, a.size, a.reps)
+    else:
+        solve(a.workload, a.size, a.precision, a.krylov_tol)
 
 
 if __name__ == "__main__":

@@ -127,8 +127,8 @@ def solve_damped_newton(dofs, settings, static_settings, newton_tol=1e-8, dampin
     cond = settings.get("dirichlet conditions")
     g = prob.to_device(cond) if cond is not None else torch.zeros(prob.n_dofs, dtype=torch.float64,
                                                                    device=prob.device)
-    if tdt == N.AGX_F32 and kwargs.get("autotune", True):
-        prob.ensure_tuned(x)
+    if kwargs.get("autotune", True):
+        prob.ensure_tuned(x, tdt)
     info = N.NewtonInfo()
     prob._call("agx_newton", N.C.c_void_p(x.data_ptr()), N.C.c_void_p(g.data_ptr()), N.C.byref(opts),
                N.C.byref(info))

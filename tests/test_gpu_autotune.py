@@ -1,0 +1,76 @@
+"""The autotuner's SpMV variants (1, 2, 4, 8 or 16 lanes per block row) solve identically, the
+autotuner picks one of them per precision, and invalid tuning values are rejected."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from autopdex_gb300 import _native as N
+from autopdex_gb300 import configs
+from autopdex_gb300._problem import get_problem
+
+pytestmark = pytest.mark.gpu
+
+
+def _solve(prob, rhs, method):
+    o = N.SolveOpts()
+    o.method, o.rtol, o.atol, o.maxiter, o.check_every = method, 1e-10 if method == N.AGX_PCG else 1e-5, 0.0, 20000, 32
+    info = N.SolveInfo()
+    x = torch.zeros_like(rhs)
+    prob._call("agx_solve", C.c_void_p(rhs.data_ptr()), C.c_void_p(x.data_ptr()), C.byref(o), C.byref(info))
+    assert info.status == N.AGX_OK
+    return x.cpu().numpy(), info.iterations
+
+
+@pytest.mark.parametrize("dtype", [N.AGX_F64, N.AGX_F32])
+def test_variants_agree_and_autotuner_picks_one(dtype):
+    w = configs.heat_grf(n=48, seed=2)
+    prob = get_problem(w.dofs, w.settings, w.static_settings)
+    prob.update_models(w.settings)
+    x0 = torch.zeros(prob.n_dofs, dtype=torch.float64, device=prob.device)
+    prob._call("agx_assemble", C.c_void_p(x0.data_ptr()), None, dtype)
+    mask = torch.as_tensor(prob.mask.astype(bool), device=prob.device)
+    rhs = torch.where(mask, torch.zeros_like(x0), torch.ones_like(x0))
+    method = N.AGX_PCG if dtype == N.AGX_F64 else N.AGX_PCG_MIXED
+    sols = {}
+    for tpr in (1, 2, 4, 8, 16):
+        prob._call("agx_set_tuning", dtype, tpr)
+        sols[tpr] = _solve(prob, rhs, method)
+    ref, its = sols[4]
+    tol = 1e-8 if dtype == N.AGX_F64 else 1e-3
+    for tpr, (x, n) in sols.items():
+        assert np.abs(x - ref).max() <= tol * np.abs(ref).max(), tpr
+        assert abs(n - its) <= 2 + its // 50, (tpr, n, its)
+    tpr = C.c_int()
+    ms = C.c_float()
+    prob._call("agx_autotune", C.byref(tpr), C.byref(ms))
+    assert tpr.value in (1, 2, 4, 8, 16) and ms.value > 0.0
+    prob._call("agx_set_tuning", dtype, 0)
+
+
+def test_invalid_tuning_is_rejected():
+    w = configs.neo_hooke_cube(n=2, n_steps=1)
+    prob = get_problem(w.dofs, w.settings, w.static_settings)
+    lib = prob.lib
+    assert lib.agx_set_tuning(prob.ctx, N.AGX_F32, 3) != N.AGX_OK
+    assert lib.agx_set_tuning(prob.ctx, N.AGX_F32, 2) != N.AGX_OK  # 3 DOFs per node need >= 4 lanes
+    assert lib.agx_set_tuning(prob.ctx, 7, 4) != N.AGX_OK
+    assert lib.agx_set_tuning(prob.ctx, N.AGX_F64, 8) == N.AGX_OK
+
+
+def test_autotuner_times_real_products():
+    """Every timed launch does the full product: the reported time is not below what the
+    matrix bytes need at 8 TB/s (a launch that found the solve flagged as finished would
+    return at once and report a few microseconds)."""
+    w = configs.heat_grf(n=1024, seed=1)
+    prob = get_problem(w.dofs, w.settings, w.static_settings)
+    prob.update_models(w.settings)
+    x0 = torch.zeros(prob.n_dofs, dtype=torch.float64, device=prob.device)
+    for dtype, s in ((N.AGX_F32, 4), (N.AGX_F64, 8)):
+        prob._call("agx_assemble", C.c_void_p(x0.data_ptr()), None, dtype)
+        tpr = C.c_int()
+        ms = C.c_float()
+        prob._call("agx_autotune", C.byref(tpr), C.byref(ms))
+        matrix_bytes = prob.nnzb * (s + 4)
+        assert ms.value * 1e-3 >= matrix_bytes / 8e12, (dtype, tpr.value, ms.value)
