@@ -328,7 +328,7 @@ def _solve(prob, rhs, x, rtol, maxiter):
 def make_training_set(n_problems, n=256, rhs_per_problem=2, seed0=0, iterates=ITERATES, krylov_tol=1e-10,
                       omega=OMEGA, verbose=False):
     """Samples from the plain float64 Jacobi-PCG solver of this backend on heat-conduction
-    problems with seeded random conductivity (the config-4 family at n x n): for every
+    problems with seeded random conductivity (the 1024^2 heat workload's family at n x n): for every
     problem and right-hand side (constant, then smooth-plus-rough random fields) one solve
     to ``krylov_tol`` gives x*, and the iterates x_k, k in ``iterates``, give the pairs."""
     from . import configs

@@ -1,4 +1,4 @@
-"""Benchmark of the GB300 solve backend on the 3-D neo-Hooke cube (config 2).
+"""Benchmark of the GB300 solve backend on the 3-D neo-Hooke cube (64^3 Q1 bricks).
 
 Workload: 64^3 Q1 bricks (274,625 nodes, 823,875 DOFs), E = 1, nu = 0.3, x = 0 clamped,
 u_x prescribed on x = 1.  One step = one load-step solve (load step 1 of 10, u_x = 0.03)
@@ -19,6 +19,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -43,7 +44,7 @@ class Clocks:
 
     def __init__(self):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"agx_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
@@ -223,7 +224,7 @@ def gpu_arm(args):
     asm_avg_ms = ms[N.AGX_PROF_TANGENT] / max(1, cnt[N.AGX_PROF_TANGENT])
 
     line = {
-        "metric": "time_to_1e-10_relative_fp64_residual (config 2: 64^3 neo-Hooke, load step 1 of 10)",
+        "metric": "time_to_1e-10_relative_fp64_residual (64^3 neo-Hooke cube, load step 1 of 10)",
         "value": per_step_s,
         "unit": "s",
         "n_gpus": world,
@@ -234,7 +235,7 @@ def gpu_arm(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32 tangent/SpMV + f64 residual",
-        "data": "synthetic (structured mesh of the config; no dataset)",
+        "data": "synthetic (structured meshes of the workloads; no dataset)",
         "config": {"workload": f"neo_hooke_cube_{n}^3_hex8_load_step_1", "n_dofs": w.n_dofs, "nnz": nnzb * 9,
                    "newton_rtol": rtol, "krylov": "jacobi-pcg f32 (rtol %.0e)" % args.krylov_tol,
                    "l2": "working set > 129 MB L2 (no flush needed)", "parallelism": "replicas" if world > 1 else "1 gpu",
@@ -270,16 +271,16 @@ def gpu_arm(args):
             line["assembly_hbm"] = assembly_roofline()
         except Exception as e:  # noqa: BLE001 -- reported, the headline stands
             line["assembly_hbm"] = {"error": str(e)[:200]}
-    if rank == 0 and not args.only_mixed and not args.no_config4:
+    if rank == 0 and not args.only_mixed and not args.no_learned:
         try:
-            line["config4"] = config4(n=args.config4_n)
+            line["heat_learned"] = heat_learned(n=args.learned_n)
         except Exception as e:  # noqa: BLE001 -- reported, the headline stands
-            line["config4"] = {"error": str(e)[:200]}
-    if rank == 0 and args.configs:
+            line["heat_learned"] = {"error": str(e)[:200]}
+    if rank == 0 and args.more_workloads:
         try:
-            line["other_configs"] = other_configs()
+            line["other_workloads"] = other_workloads()
         except Exception as e:  # noqa: BLE001 -- reported, the headline stands
-            line["other_configs"] = {"error": str(e)[:300]}
+            line["other_workloads"] = {"error": str(e)[:300]}
     if rank == 0 and not args.no_cpu_baseline and not args.only_mixed:
         line["cpu_baseline"] = cpu_baseline(n, int(info_t[0]), int(tight_kry), budget_s=args.cpu_budget)
     if dist:
@@ -291,8 +292,8 @@ def gpu_arm(args):
 TRAIN_N = 256  # resolution the shipped network was trained on (heat_unet_n256.npz)
 
 
-def config4(n=1024, seed=10000, rtol=1e-10):
-    """Config 4 (heat, k = exp(GRF), n x n Q1): time to a 1e-10 relative float64 residual for
+def heat_learned(n=1024, seed=10000, rtol=1e-10):
+    """Heat conduction with k = exp(GRF) on n x n Q1 quads: time to a 1e-10 relative float64 residual for
     plain float64 Jacobi-PCG, mixed Jacobi-PCG and the learned preconditioner in mixed FCG."""
     import torch
     from autopdex_gb300 import configs, learned, solver
@@ -328,10 +329,10 @@ def config4(n=1024, seed=10000, rtol=1e-10):
 
 
 def assembly_roofline(n=1024, reps=20):
-    """Float32 tangent assembly of the 1024^2 heat workload (config 4's mesh and conductivity,
-    the HBM-bound assembly of the survey), timed with CUDA events per agx_assemble call.
+    """Float32 tangent assembly of the 1024^2 random-conductivity heat mesh (an HBM-bound
+    assembly: a scalar potential on Q1 quads), timed with CUDA events per agx_assemble call.
 
-    Algorithmic bytes: the survey's tangent formula, coordinates + DOFs + connectivity +
+    Algorithmic bytes: coordinates + DOFs + connectivity +
     values written once (n_nodes dim 8 + n_dofs 8 + n_e nen 4 + nnz 4); the row kernel of
     structured grids moves coordinates, conductivities, row pointers and values."""
     import ctypes as C
@@ -385,21 +386,22 @@ def _timed_solve(w, static, step=None, x0=None, rtol=1e-10, **kw):
                  "residual_ratio": li.res_norm / li.res0 if li.res0 else None, "diverged": bool(info[2])}
 
 
-def other_configs(cook_n=128, cook_rtol=1e-6, heat3d_n=128, heat3d_steps=2):
-    """Configs 1, 3 and 5 beside the headline: plain float64 against mixed precision where the
+def other_workloads(cook_n=128, cook_rtol=1e-6, heat3d_n=128, heat3d_steps=2):
+    """The 200^2 Poisson, Cook membrane and 3-D backward-Euler heat workloads beside the headline:
+    plain float64 against mixed precision where the
     method allows it (BiCGStab, for the non-symmetric backward-Euler tangent, runs in float64).
 
-    Config 3 (Cook, nu = 0.4999) is run at cook_n^2 to a relative Newton residual of cook_rtol:
+    Cook's membrane (nu = 0.4999) is run at cook_n^2 to a relative Newton residual of cook_rtol:
     with Jacobi-PCG the float64 Newton residual of this nearly incompressible problem stalls
     near 4.5e-7 of the first one already at 128^2 (measured: 31 Newton iterations and 1.8 M CG
     iterations without getting below it), so 1e-10 is out of reach for the plain method."""
     from autopdex_gb300 import configs
     out = {}
-    # config 1: 200^2 Poisson, one Newton step with the direct-solver name ('lapack')
+    # 200^2 Poisson, one Newton step with the direct-solver name ('lapack')
     w = configs.poisson(n=200, solver="lapack")
     _timed_solve(w, w.static_settings)
-    _, out["config1_poisson_200_fp64_direct"] = _timed_solve(w, w.static_settings)
-    # config 3: Cook membrane, load step 1 of 20, Newton to 1e-10 of the first residual
+    _, out["poisson_200_fp64_direct"] = _timed_solve(w, w.static_settings)
+    # Cook membrane, load step 1 of 20
     res = {}
     for name, prec, ktol in (("plain_fp64_pcg", "float64", 1e-8), ("mixed_pcg", "mixed", 1e-5)):
         w = configs.cook_membrane(n=cook_n, precision=prec)
@@ -407,8 +409,8 @@ def other_configs(cook_n=128, cook_rtol=1e-6, heat3d_n=128, heat3d_steps=2):
         _, res[name] = _timed_solve(w, w.static_settings, step=w.steps[0], rtol=cook_rtol, krylov_tol=ktol,
                                     krylov_maxiter=400000)
     res["speedup_mixed_vs_plain_fp64"] = res["plain_fp64_pcg"]["s"] / res["mixed_pcg"]["s"]
-    out[f"config3_cook_{cook_n}_load_step_1_rtol_{cook_rtol:g}"] = res
-    # config 5: 3-D nonlinear backward-Euler heat, the first time steps (Newton + BiCGStab f64)
+    out[f"cook_{cook_n}_load_step_1_rtol_{cook_rtol:g}"] = res
+    # 3-D nonlinear backward-Euler heat, the first time steps (Newton + BiCGStab f64)
     import numpy as np
     w = configs.heat_transient(n=heat3d_n)
     T = np.asarray(w.raw["T0"], dtype=np.float64)
@@ -419,7 +421,7 @@ def other_configs(cook_n=128, cook_rtol=1e-6, heat3d_n=128, heat3d_steps=2):
         T = np.asarray(sol["T"])
         if k:
             steps.append(r)  # the first call builds the context and is not counted
-    out[f"config5_heat_be_{heat3d_n}^3_fp64"] = {"steps_timed": heat3d_steps, "s_per_step": sum(r["s"] for r in steps) /
+    out[f"heat_be_{heat3d_n}^3_fp64"] = {"steps_timed": heat3d_steps, "s_per_step": sum(r["s"] for r in steps) /
                                                  len(steps), "per_step": steps}
     return out
 
@@ -495,7 +497,7 @@ def reference_arm(args):
     wall = time.perf_counter() - t0
     v = float(np.median(vals))
     line = {"impl": "reference",
-            "metric": "time_to_1e-10_relative_fp64_residual (config 2: 64^3 neo-Hooke, load step 1 of 10)",
+            "metric": "time_to_1e-10_relative_fp64_residual (64^3 neo-Hooke cube, load step 1 of 10)",
             "value": v, "unit": "s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -517,9 +519,9 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--only-mixed", action="store_true", help="time the mixed path only (profiling runs)")
-    ap.add_argument("--no-config4", action="store_true")
-    ap.add_argument("--config4-n", type=int, default=1024)
-    ap.add_argument("--configs", action="store_true", help="also time configs 1, 3 and 5 (plain vs mixed)")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner heat section")
+    ap.add_argument("--learned-n", type=int, default=1024)
+    ap.add_argument("--more-workloads", action="store_true", help="also time the Poisson, Cook and 3-D transient heat workloads")
     ap.add_argument("--ref-newton-iters", type=int, default=4)
     ap.add_argument("--ref-cg-iters", type=int, default=3000)
     args = ap.parse_args()
