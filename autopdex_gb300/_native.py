@@ -14,7 +14,7 @@ AGX_NOT_CONVERGED = 1
 AGX_PRECOND_CAPTURABLE = 1
 AGX_DIVERGED = 2
 
-AGX_QUAD4, AGX_HEX8, AGX_LINE2 = 0, 1, 2
+AGX_QUAD4, AGX_HEX8, AGX_LINE2, AGX_QUAD9, AGX_LINE3 = 0, 1, 2, 3, 4
 AGX_MODEL_POISSON_SINCOS = 0
 AGX_MODEL_HEAT_POTENTIAL = 1
 AGX_MODEL_NEO_HOOKE = 2
@@ -67,6 +67,7 @@ _SIGNATURES = {
     "agx_get_matrix": (C.c_int, [_P, C.c_int, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(C.c_int64)]),
     "agx_copy_matrix": (C.c_int, [_P, C.c_int, _P, _P, _P]),
     "agx_copy_values": (C.c_int, [_P, C.c_int, _P]),
+    "agx_set_quadrature": (C.c_int, [_P, C.c_int, C.c_int]),
     "agx_spmv_values": (C.c_int, [_P, C.c_int, _P, _P, _P]),
     "agx_jacobi": (C.c_int, [_P, C.c_int, _P, _P]),
     "agx_spmv": (C.c_int, [_P, C.c_int, _P, _P]),

@@ -65,8 +65,12 @@ def _elem_type(nen, dim):
         return N.AGX_HEX8
     if dim == 2 and nen == 2:
         return N.AGX_LINE2
+    if dim == 2 and nen == 9:
+        return N.AGX_QUAD9
+    if dim == 2 and nen == 3:
+        return N.AGX_LINE3
     raise NotImplementedError(f"elements with {nen} nodes in {dim}-D are not supported by the gb300 backend "
-                              "(Q1 quads, Q1 bricks, 2-node boundary lines)")
+                              "(Q1/Q2 quads, Q1 bricks, 2- and 3-node boundary lines)")
 
 
 def flatten(values, key):
@@ -108,6 +112,8 @@ class Problem:
             sid = C.c_int()
             self._call("agx_add_element_set", et, conn.shape[0], conn.shape[1], conn.ctypes.data, C.byref(sid))
             self.conns.append(conn)
+        for sid, desc in enumerate(self.models[:len(self.conns)]):
+            self._call("agx_set_quadrature", sid, int(getattr(desc, "ngauss", 2)))
         if len(self.conns) != len(self.models):
             raise ValueError("settings['connectivity'] must have one entry per set")
         self.mask = None

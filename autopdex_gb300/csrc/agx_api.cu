@@ -91,19 +91,24 @@ bool model_ok(int elem_type, int model, int dim, int ndof, int n_params, std::st
     case AGX_MODEL_POISSON_SINCOS:
       if (ndof != 1) return why = "POISSON_SINCOS needs 1 DOF per node", false;
       if (n_params < 2 + sdim) return why = "POISSON_SINCOS needs params a, w, c[dim]", false;
-      return elem_type == AGX_QUAD4 || elem_type == AGX_HEX8 ? true : (why = "domain element required", false);
+      return elem_type == AGX_QUAD4 || elem_type == AGX_HEX8 || elem_type == AGX_QUAD9
+                 ? true
+                 : (why = "domain element required", false);
     case AGX_MODEL_HEAT_POTENTIAL:
       if (ndof != 1) return why = "HEAT_POTENTIAL needs 1 DOF per node", false;
       if (n_params < 1) return why = "HEAT_POTENTIAL needs param f", false;
-      return elem_type == AGX_QUAD4 || elem_type == AGX_HEX8 ? true : (why = "domain element required", false);
+      return elem_type == AGX_QUAD4 || elem_type == AGX_HEX8 || elem_type == AGX_QUAD9
+                 ? true
+                 : (why = "domain element required", false);
     case AGX_MODEL_NEO_HOOKE:
       if (ndof != sdim) return why = "NEO_HOOKE needs dim DOFs per node", false;
       if (n_params < 2) return why = "NEO_HOOKE needs params E, nu", false;
-      if (elem_type == AGX_QUAD4 && dim == 2) return true;
+      if ((elem_type == AGX_QUAD4 || elem_type == AGX_QUAD9) && dim == 2) return true;
       if (elem_type == AGX_HEX8 && dim == 3) return true;
-      return why = "NEO_HOOKE needs quad4 in 2-D or hex8 in 3-D", false;
+      return why = "NEO_HOOKE needs quad4/quad9 in 2-D or hex8 in 3-D", false;
     case AGX_MODEL_NEUMANN:
-      if (elem_type != AGX_LINE2 || dim != 2) return why = "NEUMANN supports 2-node lines in 2-D", false;
+      if ((elem_type != AGX_LINE2 && elem_type != AGX_LINE3) || dim != 2)
+        return why = "NEUMANN supports 2- and 3-node lines in 2-D", false;
       if (ndof != 2 || n_params < 2) return why = "NEUMANN needs 2 DOFs per node and params t0, t1", false;
       return true;
     case AGX_MODEL_HEAT_BE:
@@ -165,10 +170,15 @@ int agx_add_element_set(agx_context* ctx, int elem_type, int64_t n_elem, int nen
   if (!ctx || !conn || n_elem <= 0) return agx_fail(ctx, AGX_ERR_ARG, "bad element set arguments");
   if (ctx->n_nodes == 0) return agx_fail(ctx, AGX_ERR_STATE, "agx_set_nodes first");
   if (ctx->pattern_ready) return agx_fail(ctx, AGX_ERR_STATE, "pattern already finalized");
-  const int want = elem_type == AGX_QUAD4 ? 4 : elem_type == AGX_HEX8 ? 8 : elem_type == AGX_LINE2 ? 2 : -1;
+  const int want = elem_type == AGX_QUAD4   ? 4
+                   : elem_type == AGX_HEX8  ? 8
+                   : elem_type == AGX_LINE2 ? 2
+                   : elem_type == AGX_QUAD9 ? 9
+                   : elem_type == AGX_LINE3 ? 3
+                                            : -1;
   if (want < 0 || nen != want) return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "element type %d with %d nodes", elem_type, nen);
   if ((elem_type == AGX_HEX8) != (ctx->dim == 3))
-    return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "hex8 needs 3-D nodes, quad4/line2 2-D nodes");
+    return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "hex8 needs 3-D nodes, quads and lines 2-D nodes");
   agx_element_set s;
   s.elem_type = elem_type;
   s.nen = nen;
@@ -256,6 +266,22 @@ int agx_set_model(agx_context* ctx, int set_id, int model, const double* params,
   s.n_params = n_params;
   for (int i = 0; i < AGX_MAX_PARAMS; ++i) s.params[i] = i < n_params ? params[i] : 0.0;
   ctx->tangent_valid = -1;
+  return AGX_OK;
+}
+
+int agx_set_quadrature(agx_context* ctx, int set_id, int points_per_direction) {
+  if (!ctx || set_id < 0 || set_id >= (int)ctx->sets.size()) return agx_fail(ctx, AGX_ERR_ARG, "bad set id");
+  if (points_per_direction != 2 && points_per_direction != 3)
+    return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "2 or 3 Gauss points per direction are implemented");
+  auto& s = ctx->sets[set_id];
+  if (s.ngauss != points_per_direction) {
+    s.ngauss = points_per_direction;
+    if (s.d_geo) {  // the float64 geometry cache holds the old points
+      cudaFree(s.d_geo);
+      s.d_geo = nullptr;
+    }
+    ctx->tangent_valid = -1;
+  }
   return AGX_OK;
 }
 

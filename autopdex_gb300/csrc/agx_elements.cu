@@ -33,17 +33,26 @@ namespace {
 
 template <int ET>
 struct ElemTraits;
+// GROUP: lanes per element (a power of two >= NEN; lanes a >= NEN carry zero shape functions)
 template <>
 struct ElemTraits<AGX_QUAD4> {
-  static constexpr int RDIM = 2, NEN = 4, NQ = 4;
+  static constexpr int RDIM = 2, NEN = 4, GROUP = 4;
 };
 template <>
 struct ElemTraits<AGX_HEX8> {
-  static constexpr int RDIM = 3, NEN = 8, NQ = 8;
+  static constexpr int RDIM = 3, NEN = 8, GROUP = 8;
 };
 template <>
 struct ElemTraits<AGX_LINE2> {
-  static constexpr int RDIM = 1, NEN = 2, NQ = 2;
+  static constexpr int RDIM = 1, NEN = 2, GROUP = 2;
+};
+template <>
+struct ElemTraits<AGX_QUAD9> {
+  static constexpr int RDIM = 2, NEN = 9, GROUP = 16;
+};
+template <>
+struct ElemTraits<AGX_LINE3> {
+  static constexpr int RDIM = 1, NEN = 3, GROUP = 4;
 };
 
 // 2-point Gauss-Legendre on [-1, 1] from the [0, 1] rule of seeder.py:382-386 mapped as
@@ -52,15 +61,85 @@ __device__ __forceinline__ double gauss_point(int i) {
   return i ? (2.0 * 0.7886751345948129 - 1.0) : (2.0 * 0.21132486540518713 - 1.0);
 }
 
+// n-point rule (n = 2 or 3) on [-1, 1]: the [0, 1] points and weights of seeder.py:324-386
+// mapped as seeder.py:1053-1058 (x -> 2 x - 1, w -> 2 w)
+__device__ __forceinline__ void gauss_rule(int n, int i, double& x, double& w) {
+  if (n == 3) {
+    const double p = i == 0 ? 0.1127016653792583 : (i == 1 ? 0.5 : 0.8872983346207417);
+    const double v = i == 1 ? 0.44444444444444453 : 0.2777777777777777;
+    x = 2.0 * p - 1.0;
+    w = 2.0 * v;
+  } else {
+    x = gauss_point(i);
+    w = 1.0;
+  }
+}
+
+// 1-D quadratic Lagrange basis on nodes -1, 0, +1 (index 0, 1, 2) and its derivative
+template <typename T>
+__device__ __forceinline__ void lagrange2(int k, T x, T& l, T& dl) {
+  if (k == 0) {
+    l = T(0.5) * x * (x - T(1));
+    dl = x - T(0.5);
+  } else if (k == 1) {
+    l = T(1) - x * x;
+    dl = T(-2) * x;
+  } else {
+    l = T(0.5) * x * (x + T(1));
+    dl = x + T(0.5);
+  }
+}
+
 // reference-node sign of node a in direction d (node orders of spaces.py:1913-1922,
 // :12057-12081, :356-358)
 template <int ET>
 __device__ __forceinline__ int node_sign(int a, int d) {
-  if (ET == AGX_LINE2) return a ? 1 : -1;
+  if (ET == AGX_LINE2 || ET == AGX_LINE3) return a ? 1 : -1;
   if (d == 0) return (a & 3) == 1 || (a & 3) == 2 ? 1 : -1;
   if (d == 1) return (a & 3) >= 2 ? 1 : -1;
   return a >= 4 ? 1 : -1;
 }
+
+// N_a(xi) and dN_a/dxi of the element's node a (node orders of spaces.py:1913-1922,
+// :12057-12081, :356-358 and the quadratic orders of fem_iso_line_quad_brick)
+template <int ET, typename T>
+__device__ __forceinline__ void shape(int a, const T* xi, T& Na, T* dN) {
+  if constexpr (ET == AGX_QUAD9) {
+    // corners (-1,-1) (1,-1) (1,1) (-1,1), mid-sides (0,-1) (1,0) (0,1) (-1,0), centre:
+    // x indices 0 2 2 0 1 2 1 0 1 and y indices 0 0 2 2 0 1 2 1 1, two bits per node
+    constexpr unsigned IX = 0u | 2u << 2 | 2u << 4 | 0u << 6 | 1u << 8 | 2u << 10 | 1u << 12 | 0u << 14 | 1u << 16;
+    constexpr unsigned IY = 0u | 0u << 2 | 2u << 4 | 2u << 6 | 0u << 8 | 1u << 10 | 2u << 12 | 1u << 14 | 1u << 16;
+    T lx, dlx, ly, dly;
+    lagrange2<T>((int)((IX >> (2 * a)) & 3u), xi[0], lx, dlx);
+    lagrange2<T>((int)((IY >> (2 * a)) & 3u), xi[1], ly, dly);
+    Na = lx * ly;
+    dN[0] = dlx * ly;
+    dN[1] = lx * dly;
+  } else if constexpr (ET == AGX_LINE3) {
+    // end nodes -1, +1, then the middle node: indices 0 2 1
+    T l, dl;
+    lagrange2<T>(a == 0 ? 0 : (a == 1 ? 2 : 1), xi[0], l, dl);
+    Na = l;
+    dN[0] = dl;
+  } else {
+    constexpr int RD = ElemTraits<ET>::RDIM;
+    T fac[RD];
+#pragma unroll
+    for (int d = 0; d < RD; ++d) fac[d] = (T(1) + T(node_sign<ET>(a, d)) * xi[d]) * T(0.5);
+    Na = 1;
+#pragma unroll
+    for (int d = 0; d < RD; ++d) Na *= fac[d];
+#pragma unroll
+    for (int d = 0; d < RD; ++d) {
+      T v = T(node_sign<ET>(a, d)) * T(0.5);
+#pragma unroll
+      for (int d2 = 0; d2 < RD; ++d2)
+        if (d2 != d) v *= fac[d2];
+      dN[d] = v;
+    }
+  }
+}
+
 
 template <int NEN, typename T>
 __device__ __forceinline__ T group_sum(T v) {
@@ -117,24 +196,28 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
                const double* __restrict__ coords, const double* __restrict__ dofs,
                const double* __restrict__ elem_field, const double* __restrict__ node_field,
                const uint8_t* __restrict__ dmask_node, ModelParams mp, double* __restrict__ R,
-               T* __restrict__ vals, int64_t nnzb, const double* __restrict__ geo, double* __restrict__ geo_out) {
+               T* __restrict__ vals, int64_t nnzb, const double* __restrict__ geo, double* __restrict__ geo_out,
+               int ng) {
   using ET_ = ElemTraits<ET>;
-  constexpr int RDIM = ET_::RDIM, NEN = ET_::NEN, NQ = ET_::NQ;
+  constexpr int RDIM = ET_::RDIM, NEN = ET_::NEN, GROUP = ET_::GROUP;
+  const int NQ = RDIM == 1 ? ng : (RDIM == 2 ? ng * ng : ng * ng * ng);  // Gauss points per element
   constexpr int SDIM = (ET == AGX_HEX8) ? 3 : 2;
   using MT = ModelTraits<MODEL, SDIM>;
   constexpr int NDOF = MT::NDOF, SLOTS = MT::SLOTS;
 
   __shared__ T slab[AGX_BLOCK / 32][32][SLOTS];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int a = lane % NEN, gbase = lane - a;
-  const int64_t total = ((n_elem * NEN + 31) / 32) * 32;
+  const int a = lane % GROUP, gbase = lane - a;
+  const bool act = a < NEN;   // lanes past the element's nodes carry zero shape functions
+  const int ac = act ? a : 0;
+  const int64_t total = ((n_elem * GROUP + 31) / 32) * 32;
 
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total;
        L += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t e_raw = L / NEN;
+    const int64_t e_raw = L / GROUP;
     const bool valid = e_raw < n_elem;
     const int64_t e = valid ? e_raw : (n_elem - 1);
-    const int node = conn[e * NEN + a];
+    const int node = conn[e * NEN + ac];
 
     T xa[SDIM];
 #pragma unroll
@@ -171,34 +254,37 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
 
 #pragma unroll 1
     for (int q = 0; q < NQ; ++q) {
-      // shape function and reference derivatives of node a
-      T fac[RDIM], xi[RDIM];
+      // Gauss point q (first reference coordinate fastest, seeder.py:1046-1062), its weight,
+      // and the shape function and reference derivatives of node a
+      T xi[RDIM];
+      double wq = 1.0;
+      {
+        int r = q;
 #pragma unroll
-      for (int d = 0; d < RDIM; ++d) {
-        xi[d] = (T)gauss_point((q >> d) & 1);
-        fac[d] = (T(1) + T(node_sign<ET>(a, d)) * xi[d]) * T(0.5);
+        for (int d = 0; d < RDIM; ++d) {
+          double x, w;
+          gauss_rule(ng, r % ng, x, w);
+          r /= ng;
+          xi[d] = (T)x;
+          wq *= w;
+        }
       }
-      T Na = 1;
+      T Na, dN[RDIM];
+      shape<ET, T>(ac, xi, Na, dN);
+      if (!act) {
+        Na = 0;
 #pragma unroll
-      for (int d = 0; d < RDIM; ++d) Na *= fac[d];
-      T dN[RDIM];
-#pragma unroll
-      for (int d = 0; d < RDIM; ++d) {
-        T v = T(node_sign<ET>(a, d)) * T(0.5);
-#pragma unroll
-        for (int d2 = 0; d2 < RDIM; ++d2)
-          if (d2 != d) v *= fac[d2];
-        dN[d] = v;
+        for (int d = 0; d < RDIM; ++d) dN[d] = 0;
       }
       if constexpr (MODEL == AGX_MODEL_NEUMANN) {
-        // line in 2-D: |G1 x E3| = |G1| (models.py:1818-1823); weight 1
+        // line in 2-D: |G1 x E3| = |G1| (models.py:1818-1823)
         T G[SDIM];
 #pragma unroll
-        for (int i = 0; i < SDIM; ++i) G[i] = group_sum<NEN>(xa[i] * dN[0]);
+        for (int i = 0; i < SDIM; ++i) G[i] = group_sum<GROUP>(xa[i] * dN[0]);
         T len = sqrt(G[0] * G[0] + G[1] * G[1]);
         if constexpr (DO_R) {
 #pragma unroll
-          for (int c = 0; c < NDOF; ++c) Ra[c] += -(double)(Na * (T)mp.p[c] * len);
+          for (int c = 0; c < NDOF; ++c) Ra[c] += -(double)(Na * (T)mp.p[c] * len) * wq;
         }
         continue;
       } else {
@@ -206,18 +292,18 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
         // when one is given (uniform branch), else from the isoparametric Jacobian dX/dxi
         T ga[SDIM];
         T wdet;
-        const int64_t grec = ((e * NQ + q) * NEN + a) * (SDIM + 1);
+        const int64_t grec = ((e * NQ + q) * NEN + ac) * (SDIM + 1);
         if (geo != nullptr) {
 #pragma unroll
-          for (int d = 0; d < SDIM; ++d) ga[d] = (T)geo[grec + d];
+          for (int d = 0; d < SDIM; ++d) ga[d] = act ? (T)geo[grec + d] : T(0);
           wdet = (T)geo[grec + SDIM];
         } else {
           T Jm[SDIM][SDIM], Ji[SDIM][SDIM];
 #pragma unroll
           for (int i = 0; i < SDIM; ++i)
 #pragma unroll
-            for (int j = 0; j < SDIM; ++j) Jm[i][j] = group_sum<NEN>(xa[i] * dN[j]);
-          wdet = inverse<T, SDIM>(Jm, Ji);  // Gauss weight is 1
+            for (int j = 0; j < SDIM; ++j) Jm[i][j] = group_sum<GROUP>(xa[i] * dN[j]);
+          wdet = inverse<T, SDIM>(Jm, Ji) * (T)wq;
 #pragma unroll
           for (int d = 0; d < SDIM; ++d) {
             T v = 0;
@@ -225,7 +311,7 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
             for (int k = 0; k < SDIM; ++k) v += dN[k] * Ji[k][d];
             ga[d] = v;
           }
-          if (geo_out != nullptr && valid) {
+          if (geo_out != nullptr && valid && act) {
 #pragma unroll
             for (int d = 0; d < SDIM; ++d) geo_out[grec + d] = (double)ga[d];
             geo_out[grec + SDIM] = (double)wdet;
@@ -236,7 +322,7 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
                       MODEL == AGX_MODEL_HEAT_BE) {
           T gu[SDIM];
 #pragma unroll
-          for (int d = 0; d < SDIM; ++d) gu[d] = group_sum<NEN>(ua[0] * ga[d]);
+          for (int d = 0; d < SDIM; ++d) gu[d] = group_sum<GROUP>(ua[0] * ga[d]);
           T gug = 0;
 #pragma unroll
           for (int d = 0; d < SDIM; ++d) gug += gu[d] * ga[d];
@@ -245,7 +331,7 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
             if constexpr (DO_R) {
               T xq[SDIM];
 #pragma unroll
-              for (int d = 0; d < SDIM; ++d) xq[d] = group_sum<NEN>(Na * xa[d]);
+              for (int d = 0; d < SDIM; ++d) xq[d] = group_sum<GROUP>(Na * xa[d]);
               T r1 = 0, r2 = 0;
 #pragma unroll
               for (int d = 0; d < SDIM; ++d) {
@@ -259,8 +345,8 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
           } else if constexpr (MODEL == AGX_MODEL_HEAT_POTENTIAL) {
             src = (T)mp.p[0];
           } else {  // HEAT_BE: params k0, k2, rho_c, dt
-            const T Tq = group_sum<NEN>(Na * ua[0]);
-            const T Tn = group_sum<NEN>(Na * tna);
+            const T Tq = group_sum<GROUP>(Na * ua[0]);
+            const T Tn = group_sum<GROUP>(Na * tna);
             kq = (T)mp.p[0] + (T)mp.p[1] * Tq * Tq;
             dkq = T(2) * (T)mp.p[1] * Tq;
             mass = (T)mp.p[2] / (T)mp.p[3];
@@ -290,7 +376,7 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
 #pragma unroll
           for (int i = 0; i < SDIM; ++i)
 #pragma unroll
-            for (int j = 0; j < SDIM; ++j) F[i][j] = group_sum<NEN>(ua[i] * ga[j]) + (i == j ? T(1) : T(0));
+            for (int j = 0; j < SDIM; ++j) F[i][j] = group_sum<GROUP>(ua[i] * ga[j]) + (i == j ? T(1) : T(0));
           T Fi[SDIM][SDIM];
           const T Jdet = inverse<T, SDIM>(F, Fi);
           const T c = lam * T(0.5) * (Jdet * Jdet - T(1)) - mu;
@@ -345,7 +431,7 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
     // scatter into the residual and the pattern
     const unsigned dma = dmask_node[node];
     if constexpr (DO_R) {
-      if (valid) {
+      if (valid && act) {
 #pragma unroll
         for (int c = 0; c < NDOF; ++c) atomicAdd(R + (int64_t)node * NDOF + c, Ra[c]);
       }
@@ -354,7 +440,7 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
 #pragma unroll
       for (int b = 0; b < NEN; ++b) {
         const unsigned dmb = __shfl_sync(0xffffffffu, dma, gbase + b);
-        if (valid) {
+        if (valid && act) {
           // entry-major value planes: entry (i, j) of block pos at vals[(i ndof + j) nnzb + pos]
           T* blk = vals + epos[(e * NEN + a) * NEN + b];
 #pragma unroll
@@ -541,11 +627,11 @@ void launch_element(agx_context* ctx, agx_element_set& s, const double* dofs, do
   const double* geo = (std::is_same<T, double>::value && geo_out == nullptr) ? s.d_geo : nullptr;
   ModelParams mp;
   for (int i = 0; i < AGX_MAX_PARAMS; ++i) mp.p[i] = s.params[i];
-  const int64_t lanes = s.n_elem * ElemTraits<ET>::NEN;
+  const int64_t lanes = s.n_elem * ElemTraits<ET>::GROUP;
   const int grid = agx_grid(ctx, lanes, 8);
   element_kernel<ET, MODEL, T, DO_R, DO_K><<<grid, AGX_BLOCK, 0, ctx->stream>>>(
       s.n_elem, s.d_conn, s.d_epos, ctx->d_coords, dofs, s.d_elem_field, s.d_node_field, ctx->d_dmask_node, mp, R,
-      vals, ctx->nnzb, geo, geo_out);
+      vals, ctx->nnzb, geo, geo_out, s.ngauss);
   ctx->n_launches += 1;
 }
 
@@ -566,15 +652,19 @@ int dispatch(agx_context* ctx, agx_element_set& s, const double* dofs, double* R
   AGX_CASE(AGX_HEX8, AGX_MODEL_NEO_HOOKE)
   AGX_CASE(AGX_HEX8, AGX_MODEL_HEAT_BE)
   AGX_CASE(AGX_LINE2, AGX_MODEL_NEUMANN)
+  AGX_CASE(AGX_QUAD9, AGX_MODEL_POISSON_SINCOS)
+  AGX_CASE(AGX_QUAD9, AGX_MODEL_HEAT_POTENTIAL)
+  AGX_CASE(AGX_QUAD9, AGX_MODEL_NEO_HOOKE)
+  AGX_CASE(AGX_LINE3, AGX_MODEL_NEUMANN)
 #undef AGX_CASE
   return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "element type %d with model %d is not supported", s.elem_type, s.model);
 }
 
 // one-time float64 geometry pass of a domain set: fills s.d_geo
 int build_geometry(agx_context* ctx, agx_element_set& s) {
-  if (s.elem_type == AGX_LINE2 || s.d_geo) return AGX_OK;
-  const int nq = s.elem_type == AGX_HEX8 ? 8 : 4;
+  if (s.elem_type == AGX_LINE2 || s.elem_type == AGX_LINE3 || s.d_geo) return AGX_OK;
   const int sd = s.elem_type == AGX_HEX8 ? 3 : 2;
+  const int nq = sd == 3 ? s.ngauss * s.ngauss * s.ngauss : s.ngauss * s.ngauss;
   const size_t bytes = sizeof(double) * (size_t)s.n_elem * nq * s.nen * (sd + 1);
   if (bytes > ctx->geo_cache_limit) return AGX_OK;  // too large: the passes recompute the geometry
   AGX_CUDA(ctx, cudaMalloc((void**)&s.d_geo, bytes));
@@ -582,6 +672,9 @@ int build_geometry(agx_context* ctx, agx_element_set& s) {
   if (s.elem_type == AGX_HEX8)
     launch_element<AGX_HEX8, AGX_MODEL_HEAT_POTENTIAL, double, false, false>(ctx, s, nullptr, nullptr, nullptr,
                                                                              s.d_geo);
+  else if (s.elem_type == AGX_QUAD9)
+    launch_element<AGX_QUAD9, AGX_MODEL_HEAT_POTENTIAL, double, false, false>(ctx, s, nullptr, nullptr, nullptr,
+                                                                              s.d_geo);
   else
     launch_element<AGX_QUAD4, AGX_MODEL_HEAT_POTENTIAL, double, false, false>(ctx, s, nullptr, nullptr, nullptr,
                                                                               s.d_geo);
@@ -598,7 +691,7 @@ static agx_element_set* grid_tangent_set(agx_context* ctx) {
   for (auto& s : ctx->sets) {
     if (s.model == AGX_MODEL_NEUMANN) continue;  // no tangent contribution
     ++with_k;
-    if (s.grid_nx > 0 && ctx->ndof == 1 &&
+    if (s.grid_nx > 0 && s.ngauss == 2 && ctx->ndof == 1 &&
         (s.model == AGX_MODEL_HEAT_POTENTIAL || s.model == AGX_MODEL_POISSON_SINCOS))
       hit = &s;
   }

@@ -106,13 +106,14 @@ def neumann_weak(neumann_fun):
 class ModelDescriptor:
     """What ``static_settings['model'][set]`` holds for the gb300 backend."""
 
-    def __init__(self, mode, kernel, integrand=None, weak=None, field_key=None, dim=None):
+    def __init__(self, mode, kernel, integrand=None, weak=None, field_key=None, dim=None, ngauss=2):
         self.mode = mode            # 'user potential' | 'user element' | 'user residual'
         self.kernel = kernel        # AGX_MODEL_*
         self.integrand = integrand
         self.weak = weak
         self.field_key = field_key
         self.dim = dim
+        self.ngauss = ngauss        # Gauss-Legendre points per reference direction
 
     def resolve(self, settings, coords, conn):
         """(model id, params, per-element field or None, per-node field or None)."""
@@ -168,12 +169,17 @@ def _scalar(v, settings, coords):
 
 
 def _check_rule(ref_int_coor, ref_int_weights, dim):
-    x, w = seeder.gauss_legendre_nd(dim, 2)
-    ok = (np.asarray(ref_int_coor).shape == x.shape and np.allclose(ref_int_coor, x, rtol=0, atol=1e-15)
-          and np.allclose(ref_int_weights, w, rtol=0, atol=1e-15))
-    if not ok:
-        raise NotImplementedError("the gb300 kernels integrate Q1 elements with the 2-point Gauss-Legendre rule "
-                                  "(seeder.gauss_legendre_nd(dim, 2) or order 3)")
+    """Points per direction of a tensor Gauss-Legendre rule the kernels implement: the rules of
+    seeder.gauss_legendre_nd(dim, order) for order 2-3 (2 points) and 4-5 (3 points)."""
+    coor = np.asarray(ref_int_coor, dtype=np.float64)
+    for order, npts in ((2, 2), (4, 3)):
+        x, w = seeder.gauss_legendre_nd(dim, order)
+        if (coor.reshape(x.shape) if coor.size == x.size else None) is not None and \
+                np.allclose(coor.reshape(x.shape), x, rtol=0, atol=1e-15) and \
+                np.allclose(ref_int_weights, w, rtol=0, atol=1e-15):
+            return npts
+    raise NotImplementedError("the gb300 kernels integrate with the 2- or 3-point Gauss-Legendre rule "
+                              "(seeder.gauss_legendre_nd(dim, order), order 2-5)")
 
 
 def _check_space(fun):
@@ -190,9 +196,10 @@ def mixed_reference_domain_potential(integrand_fun, ansatz_fun, ref_int_coor, re
         raise NotImplementedError("one field, mapped by its own space, is supported")
     _check_space(next(iter(ansatz_fun.values())))
     dim = np.asarray(ref_int_coor).shape[1]
-    _check_rule(ref_int_coor, ref_int_weights, dim)
+    ng = _check_rule(ref_int_coor, ref_int_weights, dim)
     kernel = N.AGX_MODEL_POISSON_SINCOS if integrand_fun.kind == "poisson_sincos" else N.AGX_MODEL_HEAT_POTENTIAL
-    return ModelDescriptor("user potential", kernel, integrand=integrand_fun, field_key=mapping_key, dim=dim)
+    return ModelDescriptor("user potential", kernel, integrand=integrand_fun, field_key=mapping_key, dim=dim,
+                           ngauss=ng)
 
 
 def mixed_reference_domain_residual(integrand_fun, ansatz_fun, ref_int_coor, ref_int_weights, mapping_key):
@@ -203,9 +210,9 @@ def mixed_reference_domain_residual(integrand_fun, ansatz_fun, ref_int_coor, ref
         raise NotImplementedError("one field, mapped by its own space, is supported")
     _check_space(next(iter(ansatz_fun.values())))
     dim = np.asarray(ref_int_coor).shape[1]
-    _check_rule(ref_int_coor, ref_int_weights, dim)
+    ng = _check_rule(ref_int_coor, ref_int_weights, dim)
     return ModelDescriptor("user residual", N.AGX_MODEL_HEAT_BE, integrand=integrand_fun, field_key=mapping_key,
-                           dim=dim)
+                           dim=dim, ngauss=ng)
 
 
 def isoparametric_domain_element_galerkin(weak_form_fun, ansatz_fun, ref_int_coor, ref_int_weights,
@@ -217,10 +224,10 @@ def isoparametric_domain_element_galerkin(weak_form_fun, ansatz_fun, ref_int_coo
         raise NotImplementedError("only the initial configuration mapping is implemented")
     _check_space(ansatz_fun)
     dim = np.asarray(ref_int_coor).shape[1]
-    _check_rule(ref_int_coor, ref_int_weights, dim)
+    ng = _check_rule(ref_int_coor, ref_int_weights, dim)
     if (weak_form_fun.params["mode"] == "plain strain") != (dim == 2):
         raise NotImplementedError("'plain strain' needs quads, '3d' needs bricks")
-    return ModelDescriptor("user element", N.AGX_MODEL_NEO_HOOKE, weak=weak_form_fun, dim=dim)
+    return ModelDescriptor("user element", N.AGX_MODEL_NEO_HOOKE, weak=weak_form_fun, dim=dim, ngauss=ng)
 
 
 def isoparametric_surface_element_galerkin(weak_form_fun, ansatz_fun, ref_int_coor, ref_int_weights,
@@ -233,7 +240,5 @@ def isoparametric_surface_element_galerkin(weak_form_fun, ansatz_fun, ref_int_co
     if not initial_config:
         raise NotImplementedError("only the initial configuration mapping is implemented")
     _check_space(ansatz_fun)
-    x, w = seeder.gauss_legendre_nd(1, 2)
-    if not (np.allclose(np.asarray(ref_int_coor).reshape(-1), x) and np.allclose(ref_int_weights, w)):
-        raise NotImplementedError("2-point Gauss-Legendre on lines is implemented")
-    return ModelDescriptor("user element", N.AGX_MODEL_NEUMANN, weak=weak_form_fun, dim=1)
+    ng = _check_rule(np.asarray(ref_int_coor).reshape(-1), ref_int_weights, 1)
+    return ModelDescriptor("user element", N.AGX_MODEL_NEUMANN, weak=weak_form_fun, dim=1, ngauss=ng)

@@ -18,6 +18,10 @@ Keys read from ``static_settings`` (besides AutoPDEx's own):
 
 Extra keyword arguments: ``newton_tol``, ``maxiter`` (Newton), ``newton_rtol`` (stop also at
 ``||R|| <= newton_rtol ||R_0||``), ``krylov_tol``, ``krylov_maxiter``, ``reuse_tangent``.
+
+:func:`sensitivities` gives the forward implicit derivatives of a converged solution with
+respect to scalar settings (what adaptive_load_stepping's implicit_diff_mode='forward'
+differentiates).
 """
 import numpy as np
 import torch
@@ -173,7 +177,8 @@ def adaptive_load_stepping(dofs, settings, static_settings,
     the same increment control, roll-back on divergence and returned carry
     (dofs, multiplier, increment, load_step, settings, res_norm)."""
     if implicit_diff_mode is not None:
-        raise NotImplementedError("implicit differentiation through the gb300 backend is not implemented")
+        raise NotImplementedError("JAX-traced implicit differentiation needs JAX; use "
+                                  "autopdex_gb300.solver.sensitivities on the converged DOFs instead")
     verbose = static_settings.get("verbose", 0)
     multiplier, increment, load_step, res = 0.0, float(init_increment), 0.0, 0.0
     while multiplier < max_multiplier and increment > min_increment:
@@ -197,6 +202,49 @@ def adaptive_load_stepping(dofs, settings, static_settings,
         if multiplier < max_multiplier - min_increment and increment < min_increment:
             print("Adaptive load stepping could not converge; increment size below min_increment!")
     return dofs, multiplier, increment, load_step, settings, res
+
+
+def sensitivities(dofs, settings, static_settings, params, rel_step=1e-6, krylov_tol=1e-12, **kwargs):
+    """Forward-mode implicit derivatives du/dp of a converged solution with respect to scalar
+    settings entries (the 'forward' implicit differentiation of adaptive_load_stepping,
+    solver.py:200-300 with implicit_diff.custom_root, implicit_diff.py:487-542, at the final
+    state of a path-independent problem): K du/dp = -dR/dp on the free DOFs, du/dp = 0 on
+    the prescribed ones.
+
+    K is the float64 tangent at ``dofs`` with Dirichlet elimination; dR/dp is the central
+    difference of the float64 residual with step rel_step |p| (exact up to rounding for
+    parameters the residual is linear in, such as a Young's modulus; O(step^2) otherwise);
+    the linear solves are float64 Jacobi-PCG to ``krylov_tol``.  Returns {key: du/dp} with the
+    structure of ``dofs``."""
+    _backend_check(static_settings)
+    prob = get_problem(dofs, settings, static_settings)
+    x = prob.to_device(dofs)
+    m = torch.as_tensor(prob.mask.astype(bool), device=prob.device)
+    opts = N.SolveOpts()
+    opts.method, opts.rtol, opts.atol = N.AGX_PCG, float(krylov_tol), 0.0
+    opts.maxiter, opts.check_every = int(kwargs.get("krylov_maxiter", 1000000)), 32
+    out = {}
+    for key in params:
+        p0 = float(np.asarray(settings[key]))
+        h = rel_step * (abs(p0) if p0 != 0.0 else 1.0)
+        res = []
+        for v in (p0 + h, p0 - h):
+            st = dict(settings)
+            st[key] = v
+            prob.update_models(st)
+            R = torch.empty_like(x)
+            prob._call("agx_assemble", N.C.c_void_p(x.data_ptr()), N.C.c_void_p(R.data_ptr()), -1)
+            res.append(R)
+        dR = (res[0] - res[1]) / (2.0 * h)
+        prob.update_models(settings)
+        prob._call("agx_assemble", N.C.c_void_p(x.data_ptr()), None, N.AGX_F64)
+        rhs = torch.where(m, torch.zeros_like(dR), -dR)
+        du = torch.empty_like(x)
+        info = N.SolveInfo()
+        prob._call("agx_solve", N.C.c_void_p(rhs.data_ptr()), N.C.c_void_p(du.data_ptr()), N.C.byref(opts),
+                   N.C.byref(info))
+        out[key] = _out_like(du, dofs, prob.key)
+    return out
 
 
 # ---- learned preconditioner hook ------------------------------------------------------

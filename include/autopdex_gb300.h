@@ -49,6 +49,8 @@ extern "C" {
 #define AGX_QUAD4 0
 #define AGX_HEX8 1
 #define AGX_LINE2 2
+#define AGX_QUAD9 3 /* 9-node quadratic quad: corners, mid-sides (bottom, right, top, left), centre */
+#define AGX_LINE3 4 /* 3-node quadratic line: end nodes, then the middle node */
 
 /* built-in models (descriptors of the closures AutoPDEx builds in models.py) */
 #define AGX_MODEL_POISSON_SINCOS 0 /* 'user potential' 1/2|grad u|^2 - b(x) u,
@@ -141,6 +143,10 @@ int agx_finalize(agx_context* ctx);
 /* static_settings['model'][set] (models.py builders); params as listed per model. */
 int agx_set_model(agx_context* ctx, int set_id, int model, const double* params, int n_params);
 /* per-element coefficient (host pointer, n_elem values), e.g. conductivity k_e */
+/* Gauss-Legendre points per reference direction of a set (2, the default, or 3): the rule
+   seeder.gauss_legendre_nd(dim, order) gives for order 2-3 and 4-5 (seeder.py:303-386,
+   :1046-1062), which the model closures integrate with (models.py:1188-1269, :1616-1718). */
+int agx_set_quadrature(agx_context* ctx, int set_id, int points_per_direction);
 int agx_set_element_field(agx_context* ctx, int set_id, const double* field);
 /* per-DOF auxiliary field (DEVICE pointer, kept by reference), e.g. settings['dofs n'] */
 int agx_set_node_field(agx_context* ctx, int set_id, const double* field_dev);

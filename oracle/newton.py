@@ -194,3 +194,20 @@ def load_stepping(problem, dofs0, settings, multipliers, set_multiplier, newton_
         dofs, info, _ = damped_newton(problem, dofs, settings, newton_tol, maxiter)
         infos.append(info)
     return dofs, infos
+
+
+def implicit_sensitivity(problem, dofs, settings, key, rel_step=1e-6):
+    """du/dp of a converged solution for a scalar settings entry p (forward implicit
+    differentiation at the final state, as adaptive_load_stepping's implicit_diff_mode
+    'forward' with implicit_diff.custom_root, solver.py:200-300, implicit_diff.py:487-542):
+    K du = -dR/dp on the free DOFs, dR/dp by a central difference of the residual."""
+    p0 = float(settings[key])
+    h = rel_step * (abs(p0) if p0 != 0.0 else 1.0)
+    res = []
+    for v in (p0 + h, p0 - h):
+        st = dict(settings)
+        st[key] = v
+        res.append(problem.residual(dofs, st))
+    dR = (res[0] - res[1]) / (2.0 * h)
+    _, coo = assemble(problem.sets, dofs, problem.coords, settings, problem.n_dofs)
+    return linear_solve_scipy(coo, -dR, problem.n_dofs, ~problem.dirichlet)

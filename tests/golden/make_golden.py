@@ -6,7 +6,8 @@ Run in a container that has the reference checkout (it is not needed to run the 
 * cook_q2_mesh.npz: the inline Q2 Cook-membrane mesh of
   tests/test_user_elem_impl_diff_and_adaptive_load_step.py:31-55 (x_nodes, elements,
   surface_elements), parsed from the file as data.
-* golden.json: the golden scalars asserted by the reference's tests on this path.
+* golden.json: the golden scalars asserted by the reference's tests on this path (the Q2 Cook
+  solution's u.u and its derivatives with respect to Young's modulus and Poisson's ratio).
 """
 import json
 import os
@@ -33,12 +34,17 @@ def main(ref):
     s = grab("surface_elements").astype(np.int64)
     np.savez(os.path.join(HERE, "cook_q2_mesh.npz"), x_nodes=x, elements=e, surface_elements=s)
     g1 = re.search(r"isclose\(test, ([0-9.]+)\)", open(os.path.join(ref, "tests", "test_dicts_as_dofs_user_potential.py")).read())
-    g2 = re.search(r"jnp\.array\(([0-9.]+), dtype=jnp\.float64\)", src)
+    # test1 .. test3 of the reference test: u.u and its first derivatives in E and nu
+    g2 = re.findall(r"jnp\.array\((-?[0-9.]+), dtype=jnp\.float64\)", src)
     golden = {
         "poisson_5x5_sum_phi": {"value": float(g1.group(1)),
                                 "source": "tests/test_dicts_as_dofs_user_potential.py:63"},
-        "cook_q2_dofs_dot_dofs": {"value": float(g2.group(1)),
+        "cook_q2_dofs_dot_dofs": {"value": float(g2[0]),
                                   "source": "tests/test_user_elem_impl_diff_and_adaptive_load_step.py:153"},
+        "cook_q2_d_dofs_dot_dofs_d_youngs_modulus": {
+            "value": float(g2[1]), "source": "tests/test_user_elem_impl_diff_and_adaptive_load_step.py:154"},
+        "cook_q2_d_dofs_dot_dofs_d_poisson_ratio": {
+            "value": float(g2[2]), "source": "tests/test_user_elem_impl_diff_and_adaptive_load_step.py:155"},
     }
     with open(os.path.join(HERE, "golden.json"), "w") as fh:
         json.dump(golden, fh, indent=1)

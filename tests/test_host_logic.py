@@ -64,9 +64,13 @@ def test_descriptors_reject_unknown_models():
     x, w = seeder.gauss_legendre_nd(2, 2)
     with pytest.raises(NotImplementedError):
         models.mixed_reference_domain_potential(lambda *a: 0.0, {"phi": spaces.fem_iso_line_quad_brick}, x, w, "phi")
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(NotImplementedError):  # a rule that is not a 2- or 3-point Gauss-Legendre rule
         models.mixed_reference_domain_potential(models.poisson_sincos_integrand(), {"phi": spaces.fem_iso_line_quad_brick},
+                                                0.5 * x, w, "phi")
+    # the 3-point rule (order 4) is accepted and recorded
+    d = models.mixed_reference_domain_potential(models.poisson_sincos_integrand(), {"phi": spaces.fem_iso_line_quad_brick},
                                                 *seeder.gauss_legendre_nd(2, 4), "phi")
+    assert d.ngauss == 3
     with pytest.raises(NotImplementedError):
         models.hyperelastic_steady_state_weak(lambda F, p: 0.0, 1.0, 0.3, "3d")
 

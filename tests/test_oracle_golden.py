@@ -48,8 +48,9 @@ def _q2_test_arrays():
 
 
 def test_golden_q2_cook_neo_hooke():
-    """tests/test_user_elem_impl_diff_and_adaptive_load_step.py:153 -> dofs.dofs = 19390.35027108
-    (Q2 user element, neo-Hooke plane strain, Neumann traction 20, load stepping to 1)."""
+    """tests/test_user_elem_impl_diff_and_adaptive_load_step.py:153-155 -> dofs.dofs =
+    19390.35027108 and its derivatives -216.0310416 (E) and -1859.43760286 (nu) (Q2 user
+    element, neo-Hooke plane strain, Neumann traction 20, load stepping to 1)."""
     x, E, S = _q2_test_arrays()
     pts = [[0., 0.], [48., 44.], [48., 60.], [0., 44.]]
     dn = mesh.in_planes(x, pts[0], [1., 0.])
@@ -69,6 +70,13 @@ def test_golden_q2_cook_neo_hooke():
         assert not info[2]
     g = GOLDEN["cook_q2_dofs_dot_dofs"]["value"]
     assert abs(dofs @ dofs - g) <= 1e-9 * g
+    # first derivatives of u.u in E and nu by implicit differentiation at the final state
+    # (the golden values carry 10 and 12 significant digits)
+    for key, name in (("E", "cook_q2_d_dofs_dot_dofs_d_youngs_modulus"),
+                      ("nu", "cook_q2_d_dofs_dot_dofs_d_poisson_ratio")):
+        du = newton.implicit_sensitivity(prob, dofs, st, key)
+        ref = GOLDEN[name]["value"]
+        assert abs(2.0 * dofs @ du - ref) <= 1e-7 * abs(ref), (key, 2.0 * dofs @ du, ref)
 
 
 def _fd_check(fun, args, idx=0, h=1e-6):
