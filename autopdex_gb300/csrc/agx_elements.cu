@@ -475,10 +475,11 @@ __device__ __forceinline__ int sym4(int a, int b) {
 template <int MODEL, typename T>
 __global__ void __launch_bounds__(GT_THREADS)
 grid_tangent_kernel(int nx, int ny, const double* __restrict__ coords, const double* __restrict__ elem_field,
-                    const uint8_t* __restrict__ dmask_node, const int32_t* __restrict__ rowptr, T* __restrict__ vals) {
+                    const uint8_t* __restrict__ dmask_node, const int32_t* __restrict__ rowptr, T* __restrict__ vals,
+                    T* __restrict__ dinv) {
   constexpr int EX = GT_X + 1, EY = GT_Y + 1;
   constexpr int MX = GT_X + 2, MY = GT_Y + 2;  // node window of the tile with a one-node ring
-  __shared__ T ke[EY * EX][10];
+  __shared__ T ke[EY * EX][11];  // 10 entries, padded to 11 words per element: no bank conflicts
   __shared__ T stage[GT_Y][GT_X * 9];
   __shared__ uint8_t fixed[MY][MX];
   const int tid = threadIdx.x;
@@ -522,7 +523,43 @@ grid_tangent_kernel(int nx, int ny, const double* __restrict__ coords, const dou
       if constexpr (MODEL == AGX_MODEL_HEAT_POTENTIAL) k = elem_field ? (T)elem_field[(int64_t)ei * ny + ej] : T(1);
       // w det J g_a . g_b = dN_a^T M dN_b with M = adj(J) adj(J)^T / det J (Gauss weight 1):
       // per point J, det J and the three entries of M, then three FMAs per pair with the
-      // reference derivatives as compile-time constants
+      // reference derivatives as compile-time constants.  A parallelogram (x0 + x2 = x1 + x3)
+      // has one J for all points: then K = M00 C00 + M01 C01 + M11 C11 with the point sums
+      // C.. of the derivative products, three FMAs per pair in all.
+      const T ex = x[0][0] + x[2][0] - x[1][0] - x[3][0], ey = x[0][1] + x[2][1] - x[1][1] - x[3][1];
+      const T scale = fabs(x[2][0] - x[0][0]) + fabs(x[2][1] - x[0][1]) + fabs(x[1][0] - x[3][0]) +
+                      fabs(x[1][1] - x[3][1]);
+      const bool affine = fabs(ex) + fabs(ey) <= scale * (sizeof(T) == 4 ? T(1e-6) : T(1e-13));
+      if (affine) {
+        // J = (1/2) [x1 - x0 | x3 - x0] in the mesher's node order (dN constant in the other
+        // variable's direction cancels for a parallelogram)
+        const T J00 = T(0.5) * (x[1][0] - x[0][0]), J01 = T(0.5) * (x[3][0] - x[0][0]);
+        const T J10 = T(0.5) * (x[1][1] - x[0][1]), J11 = T(0.5) * (x[3][1] - x[0][1]);
+        const T rdet = T(1) / (J00 * J11 - J01 * J10);
+        const T M00 = (J11 * J11 + J01 * J01) * rdet;
+        const T M01 = -(J11 * J10 + J01 * J00) * rdet;
+        const T M11 = (J10 * J10 + J00 * J00) * rdet;
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = a; b < 4; ++b) {
+            T c00 = 0, c01 = 0, c11 = 0;  // compile-time sums over the four points
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const T xq = (T)gauss_point(q & 1), yq = (T)gauss_point((q >> 1) & 1);
+              const T fa0 = (T(1) + T(node_sign<AGX_QUAD4>(a, 0)) * xq) * T(0.5);
+              const T fa1 = (T(1) + T(node_sign<AGX_QUAD4>(a, 1)) * yq) * T(0.5);
+              const T fb0 = (T(1) + T(node_sign<AGX_QUAD4>(b, 0)) * xq) * T(0.5);
+              const T fb1 = (T(1) + T(node_sign<AGX_QUAD4>(b, 1)) * yq) * T(0.5);
+              const T da0 = T(node_sign<AGX_QUAD4>(a, 0)) * T(0.5) * fa1, da1 = T(node_sign<AGX_QUAD4>(a, 1)) * T(0.5) * fa0;
+              const T db0 = T(node_sign<AGX_QUAD4>(b, 0)) * T(0.5) * fb1, db1 = T(node_sign<AGX_QUAD4>(b, 1)) * T(0.5) * fb0;
+              c00 += da0 * db0;
+              c01 += da0 * db1 + da1 * db0;
+              c11 += da1 * db1;
+            }
+            K[sym4(a, b)] = M00 * c00 + M01 * c01 + M11 * c11;
+          }
+      } else {
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         T dN[4][2];
@@ -551,6 +588,7 @@ grid_tangent_kernel(int nx, int ny, const double* __restrict__ coords, const dou
           for (int b = a; b < 4; ++b)
             K[sym4(a, b)] += M00 * (dN[a][0] * dN[b][0]) + M01 * (dN[a][0] * dN[b][1] + dN[a][1] * dN[b][0]) +
                              M11 * (dN[a][1] * dN[b][1]);
+      }
       }
 #pragma unroll
       for (int u = 0; u < 10; ++u) K[u] *= k;
@@ -582,6 +620,8 @@ grid_tangent_kernel(int nx, int ny, const double* __restrict__ coords, const dou
         for (int dj = 0; dj < 3; ++dj)
           if (fixed[ty + di][tx + dj]) v[di * 3 + dj] = T(0);
     }
+    // the Jacobi inverse diagonal of the row (the inverse_diagonal pass, fused)
+    dinv[p] = v[4] != T(0) ? T(1) / v[4] : T(0);
     // the row's entries are the in-range stencil neighbours in column order; stage the warp's
     // rows (consecutive nodes: one contiguous range of values) for a coalesced store
     const int32_t off = rp - base;
@@ -699,14 +739,14 @@ static agx_element_set* grid_tangent_set(agx_context* ctx) {
 }
 
 template <typename T>
-static void launch_grid_tangent(agx_context* ctx, agx_element_set& s, T* vals) {
+static void launch_grid_tangent(agx_context* ctx, agx_element_set& s, T* vals, T* dinv) {
   const dim3 grid((unsigned)((s.grid_ny + 1 + GT_X - 1) / GT_X), (unsigned)((s.grid_nx + 1 + GT_Y - 1) / GT_Y));
   if (s.model == AGX_MODEL_HEAT_POTENTIAL)
     grid_tangent_kernel<AGX_MODEL_HEAT_POTENTIAL, T><<<grid, GT_THREADS, 0, ctx->stream>>>(
-        s.grid_nx, s.grid_ny, ctx->d_coords, s.d_elem_field, ctx->d_dmask_node, ctx->d_rowptr, vals);
+        s.grid_nx, s.grid_ny, ctx->d_coords, s.d_elem_field, ctx->d_dmask_node, ctx->d_rowptr, vals, dinv);
   else
     grid_tangent_kernel<AGX_MODEL_POISSON_SINCOS, T><<<grid, GT_THREADS, 0, ctx->stream>>>(
-        s.grid_nx, s.grid_ny, ctx->d_coords, s.d_elem_field, ctx->d_dmask_node, ctx->d_rowptr, vals);
+        s.grid_nx, s.grid_ny, ctx->d_coords, s.d_elem_field, ctx->d_dmask_node, ctx->d_rowptr, vals, dinv);
   ctx->n_launches += 1;
 }
 
@@ -736,9 +776,9 @@ int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, in
       {
         agx_prof_scope ps(ctx, AGX_PROF_TANGENT);
         if (tangent_dtype == AGX_F64)
-          launch_grid_tangent<double>(ctx, s, ctx->d_vals64);
+          launch_grid_tangent<double>(ctx, s, ctx->d_vals64, ctx->d_dinv64);
         else
-          launch_grid_tangent<float>(ctx, s, ctx->d_vals32);
+          launch_grid_tangent<float>(ctx, s, ctx->d_vals32, ctx->d_dinv32);
       }
       if (residual) {
         agx_prof_scope ps(ctx, AGX_PROF_RESIDUAL);
@@ -767,8 +807,10 @@ int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, in
     if (rc != AGX_OK) return rc;
     AGX_CHECK_LAUNCH(ctx);
   }
-  if (tangent_dtype >= 0) ctx->n_launches += (ctx->n_dir > 0 && !gset ? 2 : 1);  // Dirichlet diagonal + inverse diagonal
-  if (tangent_dtype == AGX_F64) {
+  if (tangent_dtype >= 0 && !gset) ctx->n_launches += (ctx->n_dir > 0 ? 2 : 1);  // Dirichlet diagonal + inverse diagonal
+  if (gset) {
+    ctx->tangent_valid = tangent_dtype;  // the row kernel wrote the inverse diagonal
+  } else if (tangent_dtype == AGX_F64) {
     inverse_diagonal<double><<<agx_grid(ctx, ctx->n_dofs), AGX_BLOCK, 0, ctx->stream>>>(
         ctx->n_dofs, ctx->ndof, ctx->nnzb, ctx->d_diagpos, ctx->d_vals64, ctx->d_dinv64);
     ctx->tangent_valid = AGX_F64;

@@ -875,26 +875,30 @@ void agx_launch_jacobi(agx_context* ctx, int dtype, const void* r, void* z) {
   ctx->n_launches += 1;
 }
 
+template <typename T, int ND>
+void spmv_nd(agx_context* ctx, int tpr, int g, const T* v, const T* x, T* y) {
+  const int64_t nr = ctx->n_nodes;
+  switch (tpr) {
+    case 1: spmv_kernel<T, ND, 1><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
+    case 2: spmv_kernel<T, ND, 2><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
+    case 4: spmv_kernel<T, ND, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
+    case 16: spmv_kernel<T, ND, 16><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
+    default: spmv_kernel<T, ND, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
+  }
+}
+
+// y = K x with the lanes per row the autotuner chose for the precision (the fused product's)
 int agx_spmv_values_impl(agx_context* ctx, int dtype, const void* values, const void* x, void* y) {
   const int64_t nr = ctx->n_nodes;
-  const int g = agx_grid(ctx, nr * 8, 8);
+  const int tuned = ctx->spmv_tpr[dtype == AGX_F32 ? 1 : 0];
+  const int tpr = tuned > 0 ? tuned : default_tpr(ctx);
+  const int g = agx_grid(ctx, nr * tpr, 8);
   auto go = [&](auto tag) {
     using T = decltype(tag);
     const T* v = (const T*)values;
-    if (ctx->ndof == 1) {
-      if (ctx->dim == 3)
-        spmv_kernel<T, 1, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb,
-                                                              (const T*)x, (T*)y);
-      else
-        spmv_kernel<T, 1, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb,
-                                                              (const T*)x, (T*)y);
-    } else if (ctx->ndof == 2) {
-      spmv_kernel<T, 2, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, (const T*)x,
-                                                            (T*)y);
-    } else {
-      spmv_kernel<T, 3, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, (const T*)x,
-                                                            (T*)y);
-    }
+    if (ctx->ndof == 1) spmv_nd<T, 1>(ctx, tpr, g, v, (const T*)x, (T*)y);
+    else if (ctx->ndof == 2) spmv_nd<T, 2>(ctx, tpr, g, v, (const T*)x, (T*)y);
+    else spmv_nd<T, 3>(ctx, tpr, g, v, (const T*)x, (T*)y);
   };
   if (dtype == AGX_F64) go(double{});
   else go(float{});

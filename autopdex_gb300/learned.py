@@ -504,9 +504,9 @@ class GridPreconditioner:
         self.net = net
         self.mode, self.omega = mode, omega
         # damped Jacobi sweeps on either side of the network: measured optimum for the 1024^2
-        # heat workload with the network on the 257^2 grid (factor 4): 4 sweeps (0.110 s to a
-        # 1e-10 residual; 2: 0.158 s, 6: 0.123 s)
-        self.sweeps = sweeps if sweeps is not None else (2 if factor == 1 else 4)
+        # heat workload with the network on the 257^2 grid (factor 4): 5 sweeps (0.093 s to a
+        # 1e-10 residual; 3: 0.120 s, 4: 0.107 s, 6: 0.099 s, 8: 0.093 s, 10: 0.103 s)
+        self.sweeps = sweeps if sweeps is not None else (2 if factor == 1 else 5)
         self.factor = factor
         self.nx, self.ny = nx, ny
         self.Hn, self.Wn = nx // factor + 1, ny // factor + 1

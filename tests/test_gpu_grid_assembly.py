@@ -6,7 +6,8 @@ the element kernel with its atomic scatter.  Both must give the same matrix: flo
 1e-13 of the largest entry (summation order differs), float32 to 5e-6 (both are float32
 element integrals with different rounding sequences, each within 2e-6 of float64); with and without
 Dirichlet elimination, for the Poisson and heat (random conductivity) potentials, on grids
-whose extents are not multiples of the 32 x 8 node tile.
+whose extents are not multiples of the 32 x 8 node tile; the unit-square grids take the
+parallelogram branch of the row kernel, the grid on Cook's quadrilateral the general one.
 """
 import numpy as np
 import pytest
@@ -29,11 +30,24 @@ def _shuffled(w, seed=3):
     return settings, w.static_settings  # a new connectivity array: a new native context
 
 
-@pytest.mark.parametrize("case", ["poisson", "heat"])
+def _heat_on_trapezoid(n=33):
+    """Heat with random conductivity on Cook's quadrilateral: a structured grid whose
+    elements are not parallelograms (the row kernel's general, non-affine integral)."""
+    from autopdex_gb300 import mesher
+    w = configs.heat_grf(n=n, seed=5)
+    coords, _ = mesher.structured_mesh((n, n), [[0., 0.], [48., 44.], [48., 60.], [0., 44.]], "quad")
+    settings = dict(w.settings)
+    settings["node coordinates"] = {"T": coords}
+    w.settings = settings
+    return w
+
+
+@pytest.mark.parametrize("case", ["poisson", "heat", "heat_trapezoid"])
 @pytest.mark.parametrize("dtype", ["float64", "float32"])
 @pytest.mark.parametrize("eliminate", [False, True])
 def test_grid_rows_match_element_scatter(case, dtype, eliminate):
-    w = configs.poisson(n=45) if case == "poisson" else configs.heat_grf(n=37, seed=11)
+    w = {"poisson": lambda: configs.poisson(n=45), "heat": lambda: configs.heat_grf(n=37, seed=11),
+         "heat_trapezoid": _heat_on_trapezoid}[case]()
     ref = assembler.assemble_tangent(w.dofs, w.settings, w.static_settings, dtype=dtype,
                                      eliminate_dirichlet=eliminate).to_scipy()
     settings, static = _shuffled(w)
