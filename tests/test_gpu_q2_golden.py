@@ -61,3 +61,20 @@ def test_q2_cook_golden_and_sensitivities():
         du = np.asarray(sens[key]).reshape(-1)
         ref = golden[name]["value"]
         assert abs(2.0 * u @ du - ref) <= 1e-7 * abs(ref), (key, 2.0 * u @ du, ref)
+
+
+def test_sensitivity_of_a_linear_problem_is_exact():
+    """Heat with a source given by a settings entry s: R = K u - s f, so du/ds = u / s; the
+    residual is linear in s and the central difference is exact up to rounding."""
+    from autopdex_gb300 import configs
+    w = configs.heat_grf(n=48, seed=3)
+    integrand = models.heat_conduction_integrand("conductivity", "source")
+    model = models.mixed_reference_domain_potential(integrand, {"T": spaces.fem_iso_line_quad_brick},
+                                                    *seeder.gauss_legendre_nd(2, 2), "T")
+    static = dict(w.static_settings, model=(model,), solver="pcg", precision="float64")
+    settings = dict(w.settings, source=2.5)
+    sol, info = solver.solver(w.dofs, settings, static, newton_tol=0.0, newton_rtol=1e-12, krylov_tol=1e-13)
+    assert not info[2]
+    du = solver.sensitivities(sol, settings, static, ["source"])["source"]
+    u = np.asarray(sol["T"])
+    assert np.abs(np.asarray(du["T"]) - u / 2.5).max() <= 1e-9 * np.abs(u / 2.5).max()
