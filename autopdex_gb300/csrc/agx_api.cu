@@ -458,8 +458,10 @@ int agx_set_tuning(agx_context* ctx, int dtype, int spmv_tpr) {
 }
 
 int agx_set_preconditioner_mode(agx_context* ctx, int mode, double omega, int sweeps, int flags) {
-  if (!ctx || mode < 0 || mode > 2) return agx_fail(ctx, AGX_ERR_ARG, "preconditioner mode must be 0, 1 or 2");
-  if (!(omega > 0.0 && omega <= 1.0)) return agx_fail(ctx, AGX_ERR_ARG, "Jacobi damping must lie in (0, 1]");
+  if (!ctx || mode < 0 || mode > 3) return agx_fail(ctx, AGX_ERR_ARG, "preconditioner mode must be 0 .. 3");
+  if (!(omega > 0.0 && omega < (mode == 3 ? 1.0 : 1.0000001)))
+    return agx_fail(ctx, AGX_ERR_ARG, mode == 3 ? "the Chebyshev interval fraction must lie in (0, 1)"
+                                               : "Jacobi damping must lie in (0, 1]");
   if (sweeps < 1 || sweeps > 16) return agx_fail(ctx, AGX_ERR_ARG, "smoothing sweeps must lie in 1 .. 16");
   if (flags & ~AGX_PRECOND_CAPTURABLE) return agx_fail(ctx, AGX_ERR_ARG, "unknown preconditioner flags");
   ctx->precond_mode = mode;

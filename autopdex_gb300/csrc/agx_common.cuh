@@ -140,6 +140,9 @@ struct agx_context {
   int precond_mode = 2;
   double precond_omega = 2.0 / 3.0;
   int precond_sweeps = 1;
+  double cheb_lmax = 2.0;      // Gershgorin bound of D^-1 K for the Chebyshev smoother
+  int64_t cheb_gen = -1;       // tangent generation the bound belongs to
+  int64_t tangent_gen = 0;     // bumped by every tangent assembly
   int precond_capturable = 0;  // the callback only enqueues work on the stream it is given
   int64_t precond_gen = 0;     // bumped whenever the callback or its mode changes
   int spmv_tpr[2] = {0, 0};  // lanes per block row of the Krylov product, float64 / float32 (0: default)

@@ -819,6 +819,7 @@ int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, in
         ctx->n_dofs, ctx->ndof, ctx->nnzb, ctx->d_diagpos, ctx->d_vals32, ctx->d_dinv32);
     ctx->tangent_valid = AGX_F32;
   }
+  if (tangent_dtype >= 0) ctx->tangent_gen += 1;
   AGX_CHECK_LAUNCH(ctx);
   return AGX_OK;
 }

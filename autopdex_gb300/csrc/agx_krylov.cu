@@ -369,18 +369,49 @@ jacobi_apply(int64_t n, const T* __restrict__ dinv, const T* __restrict__ r, T* 
 }
 
 // ---- two-level application of a registered preconditioner -----------------------------
-// One damped Jacobi sweep on the running residual: rc = rin - t (t = K dz of the previous
-// sweep, or none), dz = w D^-1 rc, z = dz (first sweep) or z + dz.
+// One smoothing step on the running residual: rc = rin - t (t = K d of the previous step, or
+// none), d = a d + b D^-1 rc, z = d (first step) or z + d.  Damped Jacobi: a = 0, b = w;
+// Chebyshev: the coefficients of the three-term recurrence.
 __global__ void __launch_bounds__(AGX_BLOCK)
-tl_sweep(int64_t n, const float* __restrict__ dinv, float w, const float* rin, float* rc, const float* __restrict__ t,
-         float* __restrict__ z, float* __restrict__ dz, int first, const agx_krylov_scalars* sc) {
+tl_sweep(int64_t n, const float* __restrict__ dinv, float b, float a, const float* rin, float* rc,
+         const float* __restrict__ t, float* __restrict__ z, float* __restrict__ dz, int first,
+         const agx_krylov_scalars* sc) {
   if (sc->converged) return;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float v = t ? rin[i] - t[i] : rin[i];
     rc[i] = v;
-    const float d = w * dinv[i] * v;
+    const float d = (a != 0.0f ? a * dz[i] : 0.0f) + b * dinv[i] * v;
     dz[i] = d;
     z[i] = first ? d : z[i] + d;
+  }
+}
+
+// Gershgorin bound of the spectrum of D^-1 K: max over rows of sum_j |K_ij| / |K_ii|
+// (float32 tangent; one value per block, the host takes the maximum)
+template <int NDOF>
+__global__ void __launch_bounds__(AGX_BLOCK)
+gershgorin_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ diagpos,
+                  const float* __restrict__ vals, int64_t nnzb, float* __restrict__ block_max) {
+  float m = 0.0f;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n_rows * NDOF;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t node = r / NDOF;
+    const int i = (int)(r - node * NDOF);
+    float s = 0.0f;
+    for (int k = rowptr[node]; k < rowptr[node + 1]; ++k)
+#pragma unroll
+      for (int j = 0; j < NDOF; ++j) s += fabsf(vals[(int64_t)(i * NDOF + j) * nnzb + k]);
+    const float d = fabsf(vals[(int64_t)(i * NDOF + i) * nnzb + diagpos[node]]);
+    if (d > 0.0f) m = fmaxf(m, s / d);
+  }
+  for (int o = 16; o >= 1; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ float sh[AGX_BLOCK / 32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.0f;
+    for (int w = 0; w < AGX_BLOCK / 32; ++w) t = fmaxf(t, sh[w]);
+    block_max[blockIdx.x] = t;
   }
 }
 
@@ -953,15 +984,35 @@ int apply_registered_preconditioner(agx_context* ctx) {
     ctx->n_launches += 1;
     return 0;
   }
-  // nu damped Jacobi sweeps from z = 0 (the running residual rc = r - K z in f_w2, the
-  // last increment in f_w4, products in f_w1), then y = M(rc) in f_w3 with the
-  // energy-optimal step c = (rc, y) / (y, K y), z += c y, and in mode 2 nu post-sweeps
-  const float w = (float)ctx->precond_omega;
+  // nu smoothing steps from z = 0 (the running residual rc = r - K z in f_w2, the last
+  // increment in f_w4, products in f_w1), then y = M(rc) in f_w3 with the energy-optimal step
+  // c = (rc, y) / (y, K y), z += c y, and in modes 2 and 3 nu post-smoothing steps.  Modes 1
+  // and 2 smooth with damped Jacobi (weight w); mode 3 with the Chebyshev polynomial of
+  // degree nu for D^-1 K on [w lmax, lmax], lmax the Gershgorin bound of the tangent.
   const int nu = ctx->precond_sweeps;
+  float ca[16], cb[16];
+  if (ctx->precond_mode == 3) {
+    const double lmax = ctx->cheb_lmax, lmin = ctx->precond_omega * lmax;
+    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
+    double rho = 1.0 / sigma;
+    ca[0] = 0.0f;
+    cb[0] = (float)(1.0 / theta);
+    for (int k = 1; k < nu; ++k) {
+      const double rn = 1.0 / (2.0 * sigma - rho);
+      ca[k] = (float)(rn * rho);
+      cb[k] = (float)(2.0 * rn / delta);
+      rho = rn;
+    }
+  } else {
+    for (int k = 0; k < nu; ++k) {
+      ca[k] = 0.0f;
+      cb[k] = (float)ctx->precond_omega;
+    }
+  }
   float *rc = ctx->f_w2, *t = ctx->f_w1, *y = ctx->f_w3, *dz = ctx->f_w4;
   for (int s = 0; s < nu; ++s) {
-    tl_sweep<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv32, w, s == 0 ? ctx->f_r : rc, rc, s == 0 ? nullptr : t,
-                                                ctx->f_z, dz, s == 0, sc);
+    tl_sweep<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv32, cb[s], ca[s], s == 0 ? ctx->f_r : rc, rc,
+                                                s == 0 ? nullptr : t, ctx->f_z, dz, s == 0, sc);
     agx_spmv_impl(ctx, AGX_F32, dz, t);
   }
   tl_residual<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, rc, t, sc);
@@ -971,15 +1022,42 @@ int apply_registered_preconditioner(agx_context* ctx) {
   tl_step<<<ctx->vec_blocks, AGX_BLOCK, 0, ctx->stream>>>(n, rc, y, t, sc, ctx->d_partials, ctx->d_counter);
   tl_combine<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_z, y, rc, t, sc);
   ctx->n_launches += 2 * nu + 5;
-  if (ctx->precond_mode == 2) {
+  if (ctx->precond_mode >= 2) {
     for (int s = 0; s < nu; ++s) {
-      tl_sweep<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv32, w, rc, rc, s == 0 ? nullptr : t, ctx->f_z, dz, 0,
-                                                  sc);
+      tl_sweep<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv32, cb[s], ca[s], rc, rc, s == 0 ? nullptr : t,
+                                                  ctx->f_z, dz, 0, sc);
       if (s + 1 < nu) agx_spmv_impl(ctx, AGX_F32, dz, t);
     }
     ctx->n_launches += 2 * nu - 1;
   }
   return 0;
+}
+
+// Gershgorin bound for the Chebyshev smoother, recomputed once per float32 tangent (host
+// synchronisation; called before any capture)
+int update_chebyshev_bound(agx_context* ctx) {
+  if (ctx->precond_mode != 3 || ctx->cheb_gen == ctx->tangent_gen) return AGX_OK;
+  const int g = ctx->red_blocks;
+  float* bm = reinterpret_cast<float*>(ctx->d_partials);  // red_blocks * 4 doubles: room to spare
+  if (ctx->ndof == 1)
+    gershgorin_kernel<1><<<g, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_nodes, ctx->d_rowptr, ctx->d_diagpos,
+                                                           ctx->d_vals32, ctx->nnzb, bm);
+  else if (ctx->ndof == 2)
+    gershgorin_kernel<2><<<g, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_nodes, ctx->d_rowptr, ctx->d_diagpos,
+                                                           ctx->d_vals32, ctx->nnzb, bm);
+  else
+    gershgorin_kernel<3><<<g, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_nodes, ctx->d_rowptr, ctx->d_diagpos,
+                                                           ctx->d_vals32, ctx->nnzb, bm);
+  std::vector<float> h(g);
+  AGX_CUDA(ctx, cudaMemcpyAsync(h.data(), bm, sizeof(float) * g, cudaMemcpyDeviceToHost, ctx->stream));
+  AGX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  float m = 0.0f;
+  for (float v : h) m = v > m ? v : m;
+  ctx->cheb_lmax = m > 0.0f ? m : 2.0;
+  ctx->cheb_gen = ctx->tangent_gen;
+  ctx->precond_gen += 1;  // the coefficients are baked into captured graphs
+  ctx->n_launches += 1;
+  return AGX_OK;
 }
 
 int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_solve_opts* opts, agx_solve_info* info) {
@@ -1035,6 +1113,7 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
                                                             pbuf[0], sc, ctx->d_partials, ctx->d_counter, 1,
                                                             flexible ? 0 : 1);
     if (flexible) {
+      if (int rc = update_chebyshev_bound(ctx)) return rc;
       if (apply_registered_preconditioner(ctx) != 0)
         return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");
       fcg_direction_dots<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_r, ctx->f_z, ctx->f_q, sc, ctx->d_partials,

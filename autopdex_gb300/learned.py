@@ -491,22 +491,27 @@ class GridPreconditioner:
     """The network as the coarse solver of a two-level preconditioner on the node grid of an
     nx x ny structured quad mesh (scalar field).
 
-    FCG applies it in the symmetric two-level form it was trained for (mode 2): damped Jacobi
-    smoothing, y = P net(P^T r) with the energy-optimal step, damped Jacobi smoothing.  P is
-    bilinear interpolation from the grid coarsened by ``factor`` (1: the network runs on the
-    node grid itself), so a network trained on n x n problems serves (factor n) x (factor n)
-    problems on its own resolution.  All buffers are allocated here and the callback only
+    FCG applies it in a symmetric two-level form: smoothing (damped Jacobi, mode 2, as in
+    training, or Chebyshev, mode 3), y = P net(P^T r) with the energy-optimal step, and
+    smoothing again.  P is bilinear interpolation from the grid coarsened by ``factor`` (1: the
+    network runs on the node grid itself), so a network trained on n x n problems serves
+    (factor n) x (factor n) problems on its own resolution.  All buffers are allocated here and the callback only
     enqueues kernels on the stream it is given, so FCG captures it into CUDA graphs."""
 
-    def __init__(self, net, nx, ny, k_elem, factor=1, mode=2, omega=OMEGA, sweeps=None, fixed=None):
+    def __init__(self, net, nx, ny, k_elem, factor=1, mode=None, omega=None, sweeps=None, fixed=None):
         if nx % factor or ny % factor:
             raise ValueError("the grid must be divisible by the coarsening factor")
         self.net = net
-        self.mode, self.omega = mode, omega
-        # damped Jacobi sweeps on either side of the network: measured optimum for the 1024^2
-        # heat workload with the network on the 257^2 grid (factor 4): 5 sweeps (0.093 s to a
-        # 1e-10 residual; 3: 0.120 s, 4: 0.107 s, 6: 0.099 s, 8: 0.093 s, 10: 0.103 s)
-        self.sweeps = sweeps if sweeps is not None else (2 if factor == 1 else 5)
+        # smoothing around the network, measured on the 1024^2 heat workload to a 1e-10
+        # residual: on a coarsened grid (factor 4) the degree-3 Chebyshev smoother on
+        # [lmax/30, lmax] (mode 3: 0.070 s; damped Jacobi, mode 2, best at 5 sweeps: 0.093 s);
+        # on the network's own grid (256^2, launch-bound) 2 damped Jacobi sweeps (0.026 s;
+        # Chebyshev degree 2: 0.031 s)
+        if mode is None:
+            mode = 2 if factor == 1 else 3
+        self.mode = mode
+        self.omega = omega if omega is not None else (OMEGA if mode != 3 else 1.0 / 30.0)
+        self.sweeps = sweeps if sweeps is not None else (2 if mode != 3 else 3)
         self.factor = factor
         self.nx, self.ny = nx, ny
         self.Hn, self.Wn = nx // factor + 1, ny // factor + 1

@@ -191,7 +191,12 @@ int agx_set_preconditioner(agx_context* ctx, agx_precond_fn fn, void* user);
    y = M(r - K z) and z += c y with the energy-optimal c = (r - K z, y) / (y, K y) -- never a
    worse step than the sweeps alone.
    mode 2 (default), symmetric two-level: mode 1 followed by `sweeps` post-smoothing sweeps.
-   w (default 2/3) is the Jacobi damping, in (0, 1]; sweeps (default 1) in 1 .. 16.
+   mode 3, symmetric two-level with Chebyshev smoothing: the sweeps of mode 2 replaced by the
+   Chebyshev polynomial of degree `sweeps` for D^-1 K on [w lmax, lmax] (same cost per
+   degree: one product), lmax the Gershgorin bound of the float32 tangent, computed once
+   per assembled tangent.
+   w: the Jacobi damping in (0, 1] (modes 1, 2; default 2/3) or the interval fraction in
+   (0, 1) (mode 3); sweeps (default 1) in 1 .. 16.
    flags: AGX_PRECOND_CAPTURABLE declares that the callback only enqueues device work on the
    stream it is given (no synchronisation, allocation or host reads), so that FCG captures
    its iterations, callback included, into CUDA graphs and replays them; the callback's

@@ -146,10 +146,10 @@ def test_trained_network_reduces_fcg_iterations():
     """A network trained for a few hundred steps on 64 x 64 problems, used by flexible CG as
     the coarse solver of the symmetric two-level preconditioner on unseen conductivity fields,
     needs far fewer iterations than Jacobi-PCG and than the same two-level method without the
-    network (damped Jacobi sweeps only, the network output replaced by zeros) to the same
+    network (the smoothing only, the network output replaced by zeros) to the same
     relative residual (float32 iterations with float64 dots): on a 64 x 64 problem with the
-    network on the node grid itself, and on a 128 x 128 problem with the network on the grid
-    coarsened by 2 (bilinear transfer)."""
+    network on the node grid itself (damped Jacobi smoothing), and on a 128 x 128 problem with
+    the network on the grid coarsened by 2 (bilinear transfer, Chebyshev smoothing)."""
     from autopdex_gb300 import _native as N
     from autopdex_gb300 import configs, learned
     from autopdex_gb300._problem import get_problem
@@ -176,7 +176,7 @@ def test_trained_network_reduces_fcg_iterations():
 
         def solve(method, cb):
             prob._call("agx_set_preconditioner", cb, None)
-            prob._call("agx_set_preconditioner_mode", 2, learned.OMEGA, pc.sweeps, N.AGX_PRECOND_CAPTURABLE)
+            prob._call("agx_set_preconditioner_mode", pc.mode, pc.omega, pc.sweeps, N.AGX_PRECOND_CAPTURABLE)
             o = N.SolveOpts()
             o.method, o.rtol, o.atol, o.maxiter, o.check_every = method, 1e-6, 0.0, 20000, 8
             info = N.SolveInfo()
