@@ -78,3 +78,69 @@ def test_sensitivity_of_a_linear_problem_is_exact():
     du = solver.sensitivities(sol, settings, static, ["source"])["source"]
     u = np.asarray(sol["T"])
     assert np.abs(np.asarray(du["T"]) - u / 2.5).max() <= 1e-9 * np.abs(u / 2.5).max()
+
+
+def _q2_problem(kind):
+    """The golden Q2 Cook mesh with (a) the neo-Hooke element and traction lines or (b) the
+    Poisson user potential; GPU settings and the oracle problem for the same inputs."""
+    from oracle import elements as el, newton
+    d = np.load(os.path.join(HERE, "golden", "cook_q2_mesh.npz"))
+    x, E9, S = d["x_nodes"], d["elements"], d["surface_elements"]
+    pts = [[0., 0.], [48., 44.], [48., 60.], [0., 44.]]
+    dn = geometry.in_planes(x, pts[0], [1., 0.])
+    NE = S[geometry.select_elements_in_plane(x, S, pts[1], [1., 0.])]
+    if kind == "neo_hooke":
+        weak = models.hyperelastic_steady_state_weak(models.neo_hooke, 100., 0.3, "plain strain")
+        dom = models.isoparametric_domain_element_galerkin(weak, spaces.fem_iso_line_quad_brick,
+                                                           *seeder.gauss_legendre_nd(2, 4))
+        trac = models.isoparametric_surface_element_galerkin(
+            models.neumann_weak(lambda x_, s: np.asarray([0., s["load multiplier"]])), spaces.fem_iso_line_quad_brick,
+            *seeder.gauss_legendre_nd(1, 4), tangent_contributions=False)
+        dd = utility.dof_select(dn, np.asarray([True, True]))
+        static = {"assembling mode": ("user element", "user element"),
+                  "solution structure": ("nodal imposition", "nodal imposition"), "model": (dom, trac),
+                  "solver type": "newton", "solver backend": "gb300", "verbose": -1}
+        settings = {"dirichlet dofs": dd, "connectivity": (E9, NE), "node coordinates": x, "load multiplier": 7.0,
+                    "dirichlet conditions": np.zeros_like(dd, dtype=np.float64)}
+        s1 = newton.ElementSet("element", E9, el.hyperelastic_element(2, 9, 4, "plain strain"),
+                               lambda st: np.tile([100., 0.3], (E9.shape[0], 1)), 2)
+        s2 = newton.ElementSet("neumann", NE, el.neumann_line_element(3, 4), None, 2,
+                               traction=lambda st: np.array([0., st["load multiplier"]]))
+        prob = newton.Problem([s1, s2], x, x.shape[0] * 2, dd, np.zeros(x.shape[0] * 2))
+        shape = (x.shape[0], 2)
+    else:
+        pot = models.mixed_reference_domain_potential(models.poisson_sincos_integrand(), {"phi": spaces.fem_iso_line_quad_brick},
+                                                      *seeder.gauss_legendre_nd(2, 4), "phi")
+        xs = x / 48.0  # the source oscillates on the unit scale
+        static = {"assembling mode": ("user potential",), "solution structure": ("nodal imposition",),
+                  "model": (pot,), "solver type": "newton", "solver backend": "gb300", "verbose": -1}
+        settings = {"dirichlet dofs": {"phi": dn}, "connectivity": ({"phi": E9},), "node coordinates": {"phi": xs},
+                    "dirichlet conditions": {"phi": np.zeros(x.shape[0])}}
+        fun = el.user_potential_element(el.poisson_sincos_integrand(), 2, 9, order=4)
+        s1 = newton.ElementSet("potential", E9, fun, lambda st: np.zeros((E9.shape[0], 1)), 1)
+        prob = newton.Problem([s1], xs, x.shape[0], dn, np.zeros(x.shape[0]))
+        shape = None
+    return static, settings, prob, shape
+
+
+@pytest.mark.parametrize("kind", ["neo_hooke", "poisson"])
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_q2_element_parity(kind, dtype):
+    """Nine-node quads and three-node lines with 3-point Gauss rules: float64 residuals to
+    1e-12, float64 tangents to 1e-12 and float32 tangents to 2e-6 of the oracle's, at random
+    (non-converged) DOFs."""
+    from autopdex_gb300 import assembler
+    from oracle import newton
+    static, settings, prob, shape = _q2_problem(kind)
+    u = np.random.default_rng(4).uniform(-0.5, 0.5, prob.n_dofs)
+    dofs = u.reshape(shape) if shape else {"phi": u}
+    st = {"load multiplier": 7.0}
+    R_or, coo = newton.assemble(prob.sets, u, prob.coords, st, prob.n_dofs)
+    K_or = newton.scipy_assembling(coo, prob.n_dofs, None)
+    if dtype == "float64":
+        R = assembler.assemble_residual(dofs, settings, static)
+        R = np.asarray(R if shape else R["phi"], dtype=np.float64).reshape(-1)
+        assert np.linalg.norm(R - R_or) <= 1e-12 * np.linalg.norm(R_or)
+    K = assembler.assemble_tangent(dofs, settings, static, dtype=dtype).to_scipy()
+    tol = 1e-12 if dtype == "float64" else 2e-6
+    assert abs(K - K_or).max() <= tol * abs(K_or).max()
