@@ -636,6 +636,85 @@ grid_tangent_kernel(int nx, int ny, const double* __restrict__ coords, const dou
   for (int u = tx; u < span; u += GT_X) vals[base + u] = stage[ty][u];
 }
 
+// ---- float64 neo-Hooke residual, one Gauss point per lane ---------------------------------
+// With NQ = NEN Gauss points (2 per direction on Q1 quads and bricks), lane l of an element's
+// lane group is node l for the DOFs and the scatter and Gauss point l for the constitutive
+// law: it forms F = I + sum_b u_b (x) g_b(q_l) from the float64 geometry cache and the other
+// lanes' DOFs (shuffles), evaluates P = mu F + c F^-T once (instead of once per node), and
+// after an exchange of w det J P through shared memory forms R_l,i = sum_q (w det J P_q)_iJ
+// g_l,J(q).  Same quantities as element_kernel<NEO_HOOKE, double, residual only>, the
+// constitutive work divided by NEN.
+template <int ET>
+__global__ void __launch_bounds__(AGX_BLOCK)
+neo_hooke_residual_qp(int64_t n_elem, const int32_t* __restrict__ conn, const double* __restrict__ dofs,
+                      const double* __restrict__ geo, ModelParams mp, double* __restrict__ R) {
+  constexpr int NEN = ElemTraits<ET>::NEN, NQ = NEN;
+  constexpr int SDIM = (ET == AGX_HEX8) ? 3 : 2;
+  __shared__ double Psh[AGX_BLOCK / 32][32][SDIM * SDIM];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int l = lane % NEN, gbase = lane - l;
+  const double E = mp.p[0], nu = mp.p[1];
+  const double lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), mu = E / (2.0 * (1.0 + nu));
+  const int64_t total = ((n_elem * NEN + 31) / 32) * 32;
+  for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e_raw = L / NEN;
+    const bool valid = e_raw < n_elem;
+    const int64_t e = valid ? e_raw : n_elem - 1;
+    const int node = conn[e * NEN + l];
+    double ul[SDIM];
+#pragma unroll
+    for (int c = 0; c < SDIM; ++c) ul[c] = dofs[(int64_t)node * SDIM + c];
+    // F at Gauss point l
+    double F[SDIM][SDIM];
+#pragma unroll
+    for (int i = 0; i < SDIM; ++i)
+#pragma unroll
+      for (int j = 0; j < SDIM; ++j) F[i][j] = i == j ? 1.0 : 0.0;
+    const double* gq = geo + ((e * NQ + l) * NEN) * (SDIM + 1);
+#pragma unroll
+    for (int b = 0; b < NEN; ++b) {
+      double ub[SDIM], g[SDIM];
+#pragma unroll
+      for (int c = 0; c < SDIM; ++c) ub[c] = __shfl_sync(0xffffffffu, ul[c], gbase + b);
+#pragma unroll
+      for (int d = 0; d < SDIM; ++d) g[d] = gq[b * (SDIM + 1) + d];
+#pragma unroll
+      for (int i = 0; i < SDIM; ++i)
+#pragma unroll
+        for (int j = 0; j < SDIM; ++j) F[i][j] += ub[i] * g[j];
+    }
+    const double wdet = gq[SDIM];  // w det J at this point (stored with every node)
+    double Fi[SDIM][SDIM];
+    const double J = inverse<double, SDIM>(F, Fi);
+    const double c = lam * 0.5 * (J * J - 1.0) - mu;
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < SDIM; ++i)
+#pragma unroll
+      for (int j = 0; j < SDIM; ++j) Psh[warp][lane][i * SDIM + j] = wdet * (mu * F[i][j] + c * Fi[j][i]);
+    __syncwarp();
+    // R_l = sum over points q of (w det J P_q) g_l(q)
+    double Rl[SDIM];
+#pragma unroll
+    for (int i = 0; i < SDIM; ++i) Rl[i] = 0.0;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      const double* gl = geo + ((e * NQ + q) * NEN + l) * (SDIM + 1);
+      double g[SDIM];
+#pragma unroll
+      for (int d = 0; d < SDIM; ++d) g[d] = gl[d];
+#pragma unroll
+      for (int i = 0; i < SDIM; ++i)
+#pragma unroll
+        for (int j = 0; j < SDIM; ++j) Rl[i] += Psh[warp][gbase + q][i * SDIM + j] * g[j];
+    }
+    if (valid) {
+#pragma unroll
+      for (int i = 0; i < SDIM; ++i) atomicAdd(R + (int64_t)node * SDIM + i, Rl[i]);
+    }
+  }
+}
+
 // prescribed diagonal entries of the (zeroed) value array set to one
 template <typename T>
 __global__ void set_dirichlet_diag(int64_t n_dir, const int32_t* __restrict__ dir_dofs,
@@ -678,6 +757,21 @@ void launch_element(agx_context* ctx, agx_element_set& s, const double* dofs, do
 // dispatch on (element type, model) for one pass kind
 template <typename T, bool DO_R, bool DO_K>
 int dispatch(agx_context* ctx, agx_element_set& s, const double* dofs, double* R, T* vals) {
+  if constexpr (std::is_same<T, double>::value && DO_R && !DO_K) {
+    if (s.model == AGX_MODEL_NEO_HOOKE && s.d_geo && s.ngauss == 2 &&
+        (s.elem_type == AGX_HEX8 || s.elem_type == AGX_QUAD4)) {
+      ModelParams mp;
+      for (int i = 0; i < AGX_MAX_PARAMS; ++i) mp.p[i] = s.params[i];
+      const int64_t lanes = s.n_elem * s.nen;
+      const int grid = agx_grid(ctx, lanes, 8);
+      if (s.elem_type == AGX_HEX8)
+        neo_hooke_residual_qp<AGX_HEX8><<<grid, AGX_BLOCK, 0, ctx->stream>>>(s.n_elem, s.d_conn, dofs, s.d_geo, mp, R);
+      else
+        neo_hooke_residual_qp<AGX_QUAD4><<<grid, AGX_BLOCK, 0, ctx->stream>>>(s.n_elem, s.d_conn, dofs, s.d_geo, mp, R);
+      ctx->n_launches += 1;
+      return AGX_OK;
+    }
+  }
 #define AGX_CASE(ETV, MV)                                                  \
   if (s.elem_type == ETV && s.model == MV) {                               \
     launch_element<ETV, MV, T, DO_R, DO_K>(ctx, s, dofs, R, vals);         \
