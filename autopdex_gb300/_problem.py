@@ -18,7 +18,18 @@ _CACHE = OrderedDict()
 _CACHE_MAX = 4
 
 
+def is_foreign(a):
+    """An array from another framework (JAX, CuPy, ...) that exports DLPack."""
+    return hasattr(a, "__dlpack__") and not isinstance(a, (np.ndarray, torch.Tensor))
+
+
+def as_torch(a):
+    """torch view of a DLPack array (zero-copy on the same device), torch tensors unchanged."""
+    return torch.from_dlpack(a) if is_foreign(a) else a
+
+
 def _np(a, dtype=None):
+    a = as_torch(a)
     if isinstance(a, torch.Tensor):
         a = a.detach().cpu().numpy()
     a = np.asarray(a)
@@ -174,8 +185,12 @@ class Problem:
                 self._call("agx_set_node_field", sid, C.c_void_p(t.data_ptr()))
 
     def to_device(self, values):
-        if isinstance(values, torch.Tensor) and values.is_cuda:
-            return values.reshape(-1).to(torch.float64).contiguous()
+        """Flat float64 device vector of a DOF-shaped structure: torch CUDA tensors and DLPack
+        arrays on this device are used in place (no copy when already float64 and
+        contiguous), host arrays are copied over (pinned for large ones)."""
+        v = as_torch(_field(values, self.key))
+        if isinstance(v, torch.Tensor) and v.is_cuda:
+            return v.reshape(-1).to(device=self.device, dtype=torch.float64).contiguous()
         host = torch.from_numpy(np.ascontiguousarray(flatten(values, self.key)))
         return host.pin_memory().to(self.device, non_blocking=True) if self.n_dofs > 4096 else host.to(self.device)
 

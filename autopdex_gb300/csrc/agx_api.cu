@@ -23,6 +23,12 @@ int agx_fail(agx_context* ctx, int code, const char* fmt, ...) {
 
 namespace {
 
+// float32 copy of a set-up array, rounded to nearest as every float32 pass would round it
+__global__ void round_to_float(int64_t n, const double* __restrict__ in, float* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
 template <typename T>
 int alloc(agx_context* ctx, T** p, int64_t n) {
   AGX_CUDA(ctx, cudaMalloc((void**)p, sizeof(T) * (size_t)(n > 0 ? n : 1)));
@@ -37,10 +43,12 @@ void release(T*& p) {
 
 void free_device(agx_context* ctx) {
   release(ctx->d_coords);
+  release(ctx->d_coords32);
   for (auto& s : ctx->sets) {
     release(s.d_conn);
     release(s.d_epos);
     release(s.d_elem_field);
+    release(s.d_elem_field32);
     release(s.d_geo);
   }
   release(ctx->d_dmask_node);
@@ -162,6 +170,10 @@ int agx_set_nodes(agx_context* ctx, int64_t n_nodes, int dim, const double* coor
   ctx->n_dofs = n_nodes * ndof;
   if (int rc = alloc(ctx, &ctx->d_coords, n_nodes * dim)) return rc;
   AGX_CUDA(ctx, cudaMemcpy(ctx->d_coords, coords, sizeof(double) * n_nodes * dim, cudaMemcpyHostToDevice));
+  if (int rc = alloc(ctx, &ctx->d_coords32, n_nodes * dim)) return rc;
+  round_to_float<<<agx_grid(ctx, n_nodes * dim), AGX_BLOCK, 0, ctx->stream>>>(n_nodes * dim, ctx->d_coords,
+                                                                               ctx->d_coords32);
+  AGX_CHECK_LAUNCH(ctx);
   ctx->h_dmask.assign(ctx->n_dofs, 0);
   return AGX_OK;
 }
@@ -290,11 +302,16 @@ int agx_set_element_field(agx_context* ctx, int set_id, const double* field) {
   auto& s = ctx->sets[set_id];
   if (!field) {
     release(s.d_elem_field);
+    release(s.d_elem_field32);
     return AGX_OK;
   }
   if (!s.d_elem_field)
     if (int rc = alloc(ctx, &s.d_elem_field, s.n_elem)) return rc;
+  if (!s.d_elem_field32)
+    if (int rc = alloc(ctx, &s.d_elem_field32, s.n_elem)) return rc;
   AGX_CUDA(ctx, cudaMemcpy(s.d_elem_field, field, sizeof(double) * s.n_elem, cudaMemcpyHostToDevice));
+  round_to_float<<<agx_grid(ctx, s.n_elem), AGX_BLOCK, 0, ctx->stream>>>(s.n_elem, s.d_elem_field, s.d_elem_field32);
+  AGX_CHECK_LAUNCH(ctx);
   ctx->tangent_valid = -1;
   return AGX_OK;
 }

@@ -29,6 +29,7 @@ struct agx_element_set {
   int n_params = 0;
   double params[AGX_MAX_PARAMS] = {0};
   double* d_elem_field = nullptr;        // one value per element (owned)
+  float* d_elem_field32 = nullptr;       // the same rounded to float32 once (float32 tangent passes)
   const double* d_node_field = nullptr;  // one value per DOF (caller-owned device pointer)
   double* d_geo = nullptr;  // float64 geometry cache: per element, Gauss point and node, (g_a, w det J)
   // structured quad grid of the mesher's numbering (element i ny + j has nodes (i, j), (i, j+1),
@@ -67,6 +68,8 @@ struct agx_context {
   int ndof = 0;            // DOFs per node (BSR block size)
   int64_t n_dofs = 0;
   double* d_coords = nullptr;   // n_nodes * dim
+  float* d_coords32 = nullptr;  // the same rounded to float32 once: float32 tangent passes read
+                                // half the bytes and convert nothing on the 1/59-rate FP64 pipe
   std::vector<agx_element_set> sets;
 
   // Dirichlet DOFs

@@ -62,16 +62,16 @@ __device__ __forceinline__ double gauss_point(int i) {
 }
 
 // n-point rule (n = 2 or 3) on [-1, 1]: the [0, 1] points and weights of seeder.py:324-386
-// mapped as seeder.py:1053-1058 (x -> 2 x - 1, w -> 2 w)
-__device__ __forceinline__ void gauss_rule(int n, int i, double& x, double& w) {
+// mapped as seeder.py:1053-1058 (x -> 2 x - 1, w -> 2 w), formed in float64 at compile time
+// and rounded to T once, so that a float32 pass selects constants instead of converting
+template <typename T>
+__device__ __forceinline__ void gauss_rule(int n, int i, T& x, T& w) {
   if (n == 3) {
-    const double p = i == 0 ? 0.1127016653792583 : (i == 1 ? 0.5 : 0.8872983346207417);
-    const double v = i == 1 ? 0.44444444444444453 : 0.2777777777777777;
-    x = 2.0 * p - 1.0;
-    w = 2.0 * v;
+    x = i == 0 ? T(2.0 * 0.1127016653792583 - 1.0) : (i == 1 ? T(2.0 * 0.5 - 1.0) : T(2.0 * 0.8872983346207417 - 1.0));
+    w = i == 1 ? T(2.0 * 0.44444444444444453) : T(2.0 * 0.2777777777777777);
   } else {
-    x = gauss_point(i);
-    w = 1.0;
+    x = i ? T(2.0 * 0.7886751345948129 - 1.0) : T(2.0 * 0.21132486540518713 - 1.0);
+    w = T(1);
   }
 }
 
@@ -193,8 +193,8 @@ struct ModelTraits {
 template <int ET, int MODEL, typename T, bool DO_R, bool DO_K>
 __global__ void __launch_bounds__(AGX_BLOCK)
 element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* __restrict__ epos,
-               const double* __restrict__ coords, const double* __restrict__ dofs,
-               const double* __restrict__ elem_field, const double* __restrict__ node_field,
+               const T* __restrict__ coords, const double* __restrict__ dofs,
+               const T* __restrict__ elem_field, const double* __restrict__ node_field,
                const uint8_t* __restrict__ dmask_node, ModelParams mp, double* __restrict__ R,
                T* __restrict__ vals, int64_t nnzb, const double* __restrict__ geo, double* __restrict__ geo_out,
                int ng) {
@@ -221,7 +221,7 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
 
     T xa[SDIM];
 #pragma unroll
-    for (int d = 0; d < SDIM; ++d) xa[d] = (T)coords[(int64_t)node * SDIM + d];
+    for (int d = 0; d < SDIM; ++d) xa[d] = coords[(int64_t)node * SDIM + d];
     T ua[NDOF];
 #pragma unroll
     for (int c = 0; c < NDOF; ++c)
@@ -229,7 +229,7 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
     T tna = 0;
     if constexpr (MODEL == AGX_MODEL_HEAT_BE) tna = (T)node_field[node];
     T ke = 1;
-    if constexpr (MODEL == AGX_MODEL_HEAT_POTENTIAL) ke = elem_field ? (T)elem_field[e] : T(1);
+    if constexpr (MODEL == AGX_MODEL_HEAT_POTENTIAL) ke = elem_field ? elem_field[e] : T(1);
     // Lame parameters (models.py:955-956) formed in float64 and then rounded: in float32,
     // 1 - 2 nu loses four digits at nu = 0.4999
     T lam = 0, mu = 0;
@@ -257,15 +257,15 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
       // Gauss point q (first reference coordinate fastest, seeder.py:1046-1062), its weight,
       // and the shape function and reference derivatives of node a
       T xi[RDIM];
-      double wq = 1.0;
+      T wq = 1;
       {
         int r = q;
 #pragma unroll
         for (int d = 0; d < RDIM; ++d) {
-          double x, w;
+          T x, w;
           gauss_rule(ng, r % ng, x, w);
           r /= ng;
-          xi[d] = (T)x;
+          xi[d] = x;
           wq *= w;
         }
       }
@@ -303,7 +303,7 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
           for (int i = 0; i < SDIM; ++i)
 #pragma unroll
             for (int j = 0; j < SDIM; ++j) Jm[i][j] = group_sum<GROUP>(xa[i] * dN[j]);
-          wdet = inverse<T, SDIM>(Jm, Ji) * (T)wq;
+          wdet = inverse<T, SDIM>(Jm, Ji) * wq;
 #pragma unroll
           for (int d = 0; d < SDIM; ++d) {
             T v = 0;
@@ -474,7 +474,7 @@ __device__ __forceinline__ int sym4(int a, int b) {
 
 template <int MODEL, typename T>
 __global__ void __launch_bounds__(GT_THREADS)
-grid_tangent_kernel(int nx, int ny, const double* __restrict__ coords, const double* __restrict__ elem_field,
+grid_tangent_kernel(int nx, int ny, const T* __restrict__ coords, const T* __restrict__ elem_field,
                     const uint8_t* __restrict__ dmask_node, const int32_t* __restrict__ rowptr, T* __restrict__ vals,
                     T* __restrict__ dinv) {
   constexpr int EX = GT_X + 1, EY = GT_Y + 1;
@@ -515,12 +515,13 @@ grid_tangent_kernel(int nx, int ny, const double* __restrict__ coords, const dou
       T x[4][2];
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
-        const double2 c = reinterpret_cast<const double2*>(coords)[n00 + oi[a] * W + oj[a]];  // (x, y) of a node
-        x[a][0] = (T)c.x;
-        x[a][1] = (T)c.y;
+        using V2 = typename std::conditional<std::is_same<T, float>::value, float2, double2>::type;
+        const V2 c = reinterpret_cast<const V2*>(coords)[n00 + oi[a] * W + oj[a]];  // (x, y) of a node
+        x[a][0] = c.x;
+        x[a][1] = c.y;
       }
       T k = 1;
-      if constexpr (MODEL == AGX_MODEL_HEAT_POTENTIAL) k = elem_field ? (T)elem_field[(int64_t)ei * ny + ej] : T(1);
+      if constexpr (MODEL == AGX_MODEL_HEAT_POTENTIAL) k = elem_field ? elem_field[(int64_t)ei * ny + ej] : T(1);
       // w det J g_a . g_b = dN_a^T M dN_b with M = adj(J) adj(J)^T / det J (Gauss weight 1):
       // per point J, det J and the three entries of M, then three FMAs per pair with the
       // reference derivatives as compile-time constants.  A parallelogram (x0 + x2 = x1 + x3)
@@ -739,6 +740,18 @@ __global__ void inverse_diagonal(int64_t n_dofs, int ndof, int64_t nnzb, const i
   }
 }
 
+// the coordinates and element field in a pass's arithmetic type (float32 copies made at set-up)
+template <typename T>
+const T* coords_of(const agx_context* ctx) {
+  if constexpr (std::is_same<T, double>::value) return ctx->d_coords;
+  else return ctx->d_coords32;
+}
+template <typename T>
+const T* elem_field_of(const agx_element_set& s) {
+  if constexpr (std::is_same<T, double>::value) return s.d_elem_field;
+  else return s.d_elem_field32;
+}
+
 template <int ET, int MODEL, typename T, bool DO_R, bool DO_K>
 void launch_element(agx_context* ctx, agx_element_set& s, const double* dofs, double* R, T* vals,
                     double* geo_out = nullptr) {
@@ -749,8 +762,8 @@ void launch_element(agx_context* ctx, agx_element_set& s, const double* dofs, do
   const int64_t lanes = s.n_elem * ElemTraits<ET>::GROUP;
   const int grid = agx_grid(ctx, lanes, 8);
   element_kernel<ET, MODEL, T, DO_R, DO_K><<<grid, AGX_BLOCK, 0, ctx->stream>>>(
-      s.n_elem, s.d_conn, s.d_epos, ctx->d_coords, dofs, s.d_elem_field, s.d_node_field, ctx->d_dmask_node, mp, R,
-      vals, ctx->nnzb, geo, geo_out, s.ngauss);
+      s.n_elem, s.d_conn, s.d_epos, coords_of<T>(ctx), dofs, elem_field_of<T>(s), s.d_node_field, ctx->d_dmask_node,
+      mp, R, vals, ctx->nnzb, geo, geo_out, s.ngauss);
   ctx->n_launches += 1;
 }
 
@@ -837,10 +850,10 @@ static void launch_grid_tangent(agx_context* ctx, agx_element_set& s, T* vals, T
   const dim3 grid((unsigned)((s.grid_ny + 1 + GT_X - 1) / GT_X), (unsigned)((s.grid_nx + 1 + GT_Y - 1) / GT_Y));
   if (s.model == AGX_MODEL_HEAT_POTENTIAL)
     grid_tangent_kernel<AGX_MODEL_HEAT_POTENTIAL, T><<<grid, GT_THREADS, 0, ctx->stream>>>(
-        s.grid_nx, s.grid_ny, ctx->d_coords, s.d_elem_field, ctx->d_dmask_node, ctx->d_rowptr, vals, dinv);
+        s.grid_nx, s.grid_ny, coords_of<T>(ctx), elem_field_of<T>(s), ctx->d_dmask_node, ctx->d_rowptr, vals, dinv);
   else
     grid_tangent_kernel<AGX_MODEL_POISSON_SINCOS, T><<<grid, GT_THREADS, 0, ctx->stream>>>(
-        s.grid_nx, s.grid_ny, ctx->d_coords, s.d_elem_field, ctx->d_dmask_node, ctx->d_rowptr, vals, dinv);
+        s.grid_nx, s.grid_ny, coords_of<T>(ctx), elem_field_of<T>(s), ctx->d_dmask_node, ctx->d_rowptr, vals, dinv);
   ctx->n_launches += 1;
 }
 

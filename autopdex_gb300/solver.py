@@ -27,7 +27,7 @@ import numpy as np
 import torch
 
 from . import _native as N
-from ._problem import get_problem, flatten, _np
+from ._problem import get_problem, flatten, _np, is_foreign
 
 last_info = None
 
@@ -78,9 +78,13 @@ def _backend_check(static_settings):
 
 
 def _out_like(flat_dev, dofs, key):
-    """Result with the structure and array type of ``dofs``."""
+    """Result with the structure and array type of ``dofs``: NumPy in, NumPy out; torch in,
+    torch out; a DLPack array of another framework in, a torch tensor on the device out
+    (hand it to that framework's from_dlpack)."""
     ref = dofs[key] if isinstance(dofs, dict) else dofs
-    if isinstance(ref, torch.Tensor):
+    if is_foreign(ref):
+        out = flat_dev.reshape(tuple(ref.shape))
+    elif isinstance(ref, torch.Tensor):
         out = flat_dev.reshape(ref.shape).to(ref.device)
     else:
         out = flat_dev.cpu().numpy().reshape(np.shape(ref))
@@ -126,8 +130,9 @@ def solve_damped_newton(dofs, settings, static_settings, newton_tol=1e-8, dampin
     opts.reuse_tangent = int(kwargs.get("reuse_tangent", _reuse_default(static_settings)))
     opts.verbose = int(static_settings.get("verbose", 0))
     x = prob.to_device(dofs)
-    x = x.clone() if isinstance(dofs, torch.Tensor) or (isinstance(dofs, dict) and isinstance(
-        dofs[prob.key], torch.Tensor)) else x
+    ref = dofs[prob.key] if isinstance(dofs, dict) else dofs
+    if isinstance(ref, torch.Tensor) or is_foreign(ref):
+        x = x.clone()  # the caller's array is never modified
     cond = settings.get("dirichlet conditions")
     g = prob.to_device(cond) if cond is not None else torch.zeros(prob.n_dofs, dtype=torch.float64,
                                                                    device=prob.device)

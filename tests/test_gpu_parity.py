@@ -188,3 +188,37 @@ def test_all_dofs_prescribed():
     w.settings["dirichlet conditions"] = {"phi": np.arange(16.0)}
     sol, (it, res, div) = solver.solver(w.dofs, w.settings, w.static_settings)
     assert np.array_equal(sol["phi"], np.arange(16.0)) and res == 0.0 and not div
+
+
+class _Foreign:
+    """A minimal array of another framework: it exports DLPack and nothing torch knows."""
+
+    def __init__(self, t):
+        self._t = t
+        self.shape = tuple(t.shape)
+
+    def __dlpack__(self, stream=None, **kw):
+        return self._t.__dlpack__()
+
+    def __dlpack_device__(self):
+        return self._t.__dlpack_device__()
+
+
+def test_dlpack_inputs_match_numpy_path():
+    """DOFs and Dirichlet values handed over as foreign DLPack arrays on the device give the
+    same Newton solution as NumPy inputs; the result is a device tensor of the DOFs' shape
+    and the caller's array is left unchanged."""
+    import torch
+    from autopdex_gb300 import solver
+    w = configs.neo_hooke_cube(n=3, n_steps=2)
+    w.settings = w.steps[0](w.settings)
+    ref, (it0, res0, div0) = solver.solver(w.dofs, w.settings, w.static_settings, newton_tol=1e-10)
+    d0 = torch.as_tensor(np.asarray(w.dofs), device="cuda")
+    settings = dict(w.settings)
+    settings["dirichlet conditions"] = _Foreign(torch.as_tensor(np.asarray(w.settings["dirichlet conditions"]),
+                                                                device="cuda"))
+    sol, (it, res, div) = solver.solver(_Foreign(d0), settings, w.static_settings, newton_tol=1e-10)
+    assert not div and not div0 and it == it0
+    assert isinstance(sol, torch.Tensor) and sol.is_cuda and tuple(sol.shape) == np.shape(w.dofs)
+    assert np.abs(sol.cpu().numpy() - np.asarray(ref)).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+    assert torch.count_nonzero(d0) == 0

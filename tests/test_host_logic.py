@@ -121,3 +121,23 @@ def test_adaptive_load_stepping_controller(monkeypatch):
     assert np.isclose(calls[0], 0.2) and np.isclose(calls[1], 0.2 + 0.2 * (1 + 0.5 * 4 / 7))
     # the diverged step did not advance the DOFs
     assert dofs[0] == len(calls) - 1
+
+
+def test_dlpack_host_arrays_are_read():
+    """Arrays of other frameworks arrive through DLPack (host ones are read as NumPy)."""
+    import torch
+
+    class Foreign:
+        def __init__(self, t):
+            self._t, self.shape = t, tuple(t.shape)
+
+        def __dlpack__(self, stream=None, **kw):
+            return self._t.__dlpack__()
+
+        def __dlpack_device__(self):
+            return self._t.__dlpack_device__()
+
+    f = Foreign(torch.arange(6.0).reshape(3, 2))
+    assert _problem.is_foreign(f) and not _problem.is_foreign(np.zeros(2))
+    assert np.array_equal(_problem.flatten({"u": f}, "u"), np.arange(6.0))
+    assert _problem.dof_layout(f) == (None, 3, 2)
