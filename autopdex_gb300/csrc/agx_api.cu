@@ -170,6 +170,7 @@ int agx_set_nodes(agx_context* ctx, int64_t n_nodes, int dim, const double* coor
   ctx->n_dofs = n_nodes * ndof;
   if (int rc = alloc(ctx, &ctx->d_coords, n_nodes * dim)) return rc;
   AGX_CUDA(ctx, cudaMemcpy(ctx->d_coords, coords, sizeof(double) * n_nodes * dim, cudaMemcpyHostToDevice));
+  ctx->h_coords.assign(coords, coords + n_nodes * dim);
   if (int rc = alloc(ctx, &ctx->d_coords32, n_nodes * dim)) return rc;
   round_to_float<<<agx_grid(ctx, n_nodes * dim), AGX_BLOCK, 0, ctx->stream>>>(n_nodes * dim, ctx->d_coords,
                                                                                ctx->d_coords32);

@@ -36,6 +36,7 @@ struct agx_element_set {
   // (i+1, j+1), (i+1, j), node (i, j) = i (ny + 1) + j) whose pattern rows are exactly the
   // in-range 3 x 3 node stencils; 0 when the set is not such a grid
   int grid_nx = 0, grid_ny = 0;
+  bool grid_affine = false;  // every element of the grid is a parallelogram (float64 coordinates)
 };
 
 // Scalars of one Krylov solve, kept in device memory so that iterations need no host
@@ -68,6 +69,7 @@ struct agx_context {
   int ndof = 0;            // DOFs per node (BSR block size)
   int64_t n_dofs = 0;
   double* d_coords = nullptr;   // n_nodes * dim
+  std::vector<double> h_coords; // the same on the host (set-up checks)
   float* d_coords32 = nullptr;  // the same rounded to float32 once: float32 tangent passes read
                                 // half the bytes and convert nothing on the 1/59-rate FP64 pipe
   std::vector<agx_element_set> sets;

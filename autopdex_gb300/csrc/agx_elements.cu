@@ -455,186 +455,298 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
   }
 }
 
-// ---- atomic-free tangent of a structured quad grid ---------------------------------------
+// ---- atomic-free tangent of a structured quad grid (column sweep) -------------------------
 // For a set that detect_structured_grid recognised and a scalar potential model (K_ab =
-// k int g_a . g_b, symmetric), the tangent is written row by row: a block owns a tile of
-// GT_Y x GT_X nodes, computes the 4 x 4 matrices of the (GT_Y + 1) x (GT_X + 1) elements that
-// touch them (its own and one halo row and column) into shared memory, and every thread sums
-// the row of its node from its four incident elements and writes it once.  No atomics, no
-// memset, no scatter map: DRAM traffic is coordinates, element coefficients, row pointers and
-// the values, each once.  Dirichlet rows become identity rows and Dirichlet columns zeros, as
-// in the element scatter.
-constexpr int GT_X = 32, GT_Y = 8;
-constexpr int GT_THREADS = 320;  // >= the (GT_Y + 1) x (GT_X + 1) = 297 element matrices: one round
+// k int g_a . g_b, symmetric), the tangent is written row by row and without atomics.  A warp
+// owns a strip of GS_NODES = 31 node columns and a segment of node rows and walks down it:
+// lane l computes the element to the right of node column c0 + l - 1 (lane 0 the element left
+// of the strip), keeps the previous element row in registers, receives the left element's
+// share of its node's row by one shuffle per entry, and writes the node's nine entries and
+// its inverse diagonal once.  Coordinates, coefficients, Dirichlet flags and row pointers of
+// the next row are requested before the current row is computed.  DRAM traffic is each of
+// those once (plus one element row per segment) and the values; no memset, no scatter map.
+// Dirichlet rows become identity rows and Dirichlet columns zeros, as in the element scatter.
+constexpr int GS_WARPS = 4;   // independent warps per block
+constexpr int GS_NODES = 31;  // node columns per strip
+constexpr int GS_BLOCKS_PER_SM = 8;  // float32: 32 warps per SM, at most 64 registers a thread (float64: half)
+
+// round-to-nearest reciprocals: the correctly rounded 1 / x of either type
+__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
 
 __device__ __forceinline__ int sym4(int a, int b) {
   const int lo = a < b ? a : b, hi = a < b ? b : a;
   return lo * 4 - lo * (lo - 1) / 2 + (hi - lo);  // row-major upper triangle of a 4 x 4
 }
 
-template <int MODEL, typename T>
-__global__ void __launch_bounds__(GT_THREADS)
+// upper triangle of k int g_a . g_b over one bilinear quad (2 x 2 Gauss points), nodes in
+// the mesher's order
+template <typename T, bool AFFINE>
+__device__ __forceinline__ void quad_stiffness(const T (&x)[4][2], T k, T (&K)[10]) {
+#pragma unroll
+  for (int u = 0; u < 10; ++u) K[u] = 0;
+  // w det J g_a . g_b = dN_a^T M dN_b with M = adj(J) adj(J)^T / det J (Gauss weight 1):
+  // per point J, det J and the three entries of M, then three FMAs per pair with the
+  // reference derivatives as compile-time constants.  A parallelogram (x0 + x2 = x1 + x3)
+  // has one J for all points: then K = M00 C00 + M01 C01 + M11 C11 with the point sums
+  // C.. of the derivative products, three FMAs per pair in all.
+  const T ex = x[0][0] + x[2][0] - x[1][0] - x[3][0], ey = x[0][1] + x[2][1] - x[1][1] - x[3][1];
+  const T scale = fabs(x[2][0] - x[0][0]) + fabs(x[2][1] - x[0][1]) + fabs(x[1][0] - x[3][0]) +
+                  fabs(x[1][1] - x[3][1]);
+  // AFFINE: every element of the grid is a parallelogram (checked once on the float64
+  // coordinates when the grid was recognised)
+  const bool affine = AFFINE || fabs(ex) + fabs(ey) <= scale * (sizeof(T) == 4 ? T(1e-6) : T(1e-13));
+  if (affine) {
+    // J = (1/2) [x1 - x0 | x3 - x0] in the mesher's node order (dN constant in the other
+    // variable's direction cancels for a parallelogram)
+    const T J00 = T(0.5) * (x[1][0] - x[0][0]), J01 = T(0.5) * (x[3][0] - x[0][0]);
+    const T J10 = T(0.5) * (x[1][1] - x[0][1]), J11 = T(0.5) * (x[3][1] - x[0][1]);
+    const T rdet = rcp_rn(J00 * J11 - J01 * J10);
+    const T M00 = (J11 * J11 + J01 * J01) * rdet;
+    const T M01 = -(J11 * J10 + J01 * J00) * rdet;
+    const T M11 = (J10 * J10 + J00 * J00) * rdet;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = a; b < 4; ++b) {
+        T c00 = 0, c01 = 0, c11 = 0;  // compile-time sums over the four points
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const T xq = (T)gauss_point(q & 1), yq = (T)gauss_point((q >> 1) & 1);
+          const T fa0 = (T(1) + T(node_sign<AGX_QUAD4>(a, 0)) * xq) * T(0.5);
+          const T fa1 = (T(1) + T(node_sign<AGX_QUAD4>(a, 1)) * yq) * T(0.5);
+          const T fb0 = (T(1) + T(node_sign<AGX_QUAD4>(b, 0)) * xq) * T(0.5);
+          const T fb1 = (T(1) + T(node_sign<AGX_QUAD4>(b, 1)) * yq) * T(0.5);
+          const T da0 = T(node_sign<AGX_QUAD4>(a, 0)) * T(0.5) * fa1, da1 = T(node_sign<AGX_QUAD4>(a, 1)) * T(0.5) * fa0;
+          const T db0 = T(node_sign<AGX_QUAD4>(b, 0)) * T(0.5) * fb1, db1 = T(node_sign<AGX_QUAD4>(b, 1)) * T(0.5) * fb0;
+          c00 += da0 * db0;
+          c01 += da0 * db1 + da1 * db0;
+          c11 += da1 * db1;
+        }
+        K[sym4(a, b)] = M00 * c00 + M01 * c01 + M11 * c11;
+      }
+  } else {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      T dN[4][2];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        const T f0 = (T(1) + T(node_sign<AGX_QUAD4>(a, 0)) * (T)gauss_point(q & 1)) * T(0.5);
+        const T f1 = (T(1) + T(node_sign<AGX_QUAD4>(a, 1)) * (T)gauss_point((q >> 1) & 1)) * T(0.5);
+        dN[a][0] = T(node_sign<AGX_QUAD4>(a, 0)) * T(0.5) * f1;
+        dN[a][1] = T(node_sign<AGX_QUAD4>(a, 1)) * T(0.5) * f0;
+      }
+      T J00 = 0, J01 = 0, J10 = 0, J11 = 0;
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        J00 += x[a][0] * dN[a][0];
+        J01 += x[a][0] * dN[a][1];
+        J10 += x[a][1] * dN[a][0];
+        J11 += x[a][1] * dN[a][1];
+      }
+      const T rdet = rcp_rn(J00 * J11 - J01 * J10);
+      const T M00 = (J11 * J11 + J01 * J01) * rdet;
+      const T M01 = -(J11 * J10 + J01 * J00) * rdet;
+      const T M11 = (J10 * J10 + J00 * J00) * rdet;
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = a; b < 4; ++b)
+          K[sym4(a, b)] += M00 * (dN[a][0] * dN[b][0]) + M01 * (dN[a][0] * dN[b][1] + dN[a][1] * dN[b][0]) +
+                           M11 * (dN[a][1] * dN[b][1]);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < 10; ++u) K[u] *= k;
+}
+
+template <int MODEL, typename T, bool AFFINE>
+__global__ void __launch_bounds__(GS_WARPS * 32, sizeof(T) == 4 ? GS_BLOCKS_PER_SM : GS_BLOCKS_PER_SM / 2)
 grid_tangent_kernel(int nx, int ny, const T* __restrict__ coords, const T* __restrict__ elem_field,
                     const uint8_t* __restrict__ dmask_node, const int32_t* __restrict__ rowptr, T* __restrict__ vals,
                     T* __restrict__ dinv) {
-  constexpr int EX = GT_X + 1, EY = GT_Y + 1;
-  constexpr int MX = GT_X + 2, MY = GT_Y + 2;  // node window of the tile with a one-node ring
-  __shared__ T ke[EY * EX][11];  // 10 entries, padded to 11 words per element: no bank conflicts
-  __shared__ T stage[GT_Y][GT_X * 9];
-  __shared__ uint8_t fixed[MY][MX];
-  const int tid = threadIdx.x;
-  const int i0 = blockIdx.y * GT_Y, j0 = blockIdx.x * GT_X;
-  const int64_t W = (int64_t)ny + 1;  // nodes per grid row
-  // local node a of element (i, j) sits at node (i + oi[a], j + oj[a]) (mesher order)
-  constexpr int oi[4] = {0, 0, 1, 1}, oj[4] = {0, 1, 1, 0};
-  // row pointers of the owned rows and the Dirichlet flags of the node window, requested
-  // before the element integrals so that their latency overlaps the arithmetic
-  const int ty = tid / GT_X, tx = tid % GT_X;  // warps 0 .. GT_Y - 1: one node row each
-  const int i = i0 + ty, j = j0 + tx;
-  const bool row_warp = ty < GT_Y && i <= nx;
-  const int64_t p = (int64_t)i * W + j;
-  int32_t base = 0, span = 0, rp = 0;
-  if (row_warp) {
-    const int jl = (j0 + GT_X - 1 < ny ? j0 + GT_X - 1 : ny);  // last owned node of this grid row
-    base = rowptr[(int64_t)i * W + j0];
-    span = rowptr[(int64_t)i * W + jl + 1] - base;
-    if (j <= ny) rp = rowptr[p];
-  }
-  for (int t = tid; t < MY * MX; t += GT_THREADS) {
-    const int ni = i0 - 1 + t / MX, nj = j0 - 1 + t % MX;
-    fixed[t / MX][t % MX] =
-        (ni >= 0 && ni <= nx && nj >= 0 && nj <= ny) ? (uint8_t)(dmask_node[(int64_t)ni * W + nj] & 1u) : (uint8_t)0;
-  }
-  for (int t = tid; t < EY * EX; t += GT_THREADS) {
-    const int ei = i0 - 1 + t / EX, ej = j0 - 1 + t % EX;
-    T K[10];
+  using V2 = typename std::conditional<std::is_same<T, float>::value, float2, double2>::type;
+  using V = typename std::conditional<std::is_same<T, float>::value, float4, double2>::type;
+  constexpr int GVEC = 16 / (int)sizeof(T);  // values per 16-byte store
+  // a strip's values of one node row plus up to GVEC - 1 words of lead-in, in whole 16-byte chunks
+  constexpr int SROW = (GS_NODES * 9 + 2 * GVEC - 2) / GVEC * GVEC;
+  __shared__ __align__(16) T stage[GS_WARPS][SROW];
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  // node and element indices fit in 32 bits (agx_set_nodes rejects 2^31 nodes or more)
+  const int W = ny + 1, rows = nx + 1;
+  const int n_strips = (W + GS_NODES - 1) / GS_NODES;
+  // warp gw walks strip gw % n_strips over the node rows of segment gw / n_strips: the rows are
+  // split into as many segments as every strip can have (row counts within one of each
+  // other), and neighbouring warps take neighbouring strips of the same rows, so that the
+  // rows in flight are read and written across their whole width.  One wave of warps.
+  const int64_t nw = (int64_t)gridDim.x * GS_WARPS, gw = (int64_t)blockIdx.x * GS_WARPS + wib;
+  const int64_t nseg = nw / n_strips;
+  const int strip = (int)(gw % n_strips);
+  const int64_t seg = gw / n_strips;
+  const int64_t ns = max(nseg, (int64_t)1);
+  const int i_begin = (int)(rows * seg / ns), i_end = (int)(rows * (seg + 1) / ns);
+  if (seg >= nseg || i_begin >= i_end) return;  // whole warps; the kernel has no block-wide barrier
+  const int c0 = strip * GS_NODES;           // first node column of the strip (owned by lane 1)
+  const int col = c0 + lane - 1;             // this lane's node column and element column
+  const bool has_elem = col >= 0 && col < ny;
+  const bool owner = lane >= 1 && col <= ny;  // lane owns node (i, col) of every row i
+  const bool strip_interior = c0 >= 1 && c0 + GS_NODES - 1 < ny;  // every owned node has both column neighbours
+  // Every load is unconditional, at indices clamped into the grid.  A clamped row or column
+  // only feeds elements that do not exist (their matrices are zero) and flags of stencil
+  // entries outside the grid (never stored), so no load needs a branch.
+  const int colc = min(max(col, 0), ny);                 // node column
+  const int colx = min(c0 + GS_NODES, ny);               // lane 31: the column right of its node
+  const int cole = min(max(col, 0), ny - 1);             // element column
+  const int colr = min(max(col + 1, 0), W);              // row pointer of the next node (the row end last)
+  const V2* cp = reinterpret_cast<const V2*>(coords);
+  T* st = stage[wib];
+  auto rowc = [&](int n) { return min(max(n, 0), nx); };
+
+  // per node row n: (x, y) of this lane's node and of the node to its right, and the Dirichlet
+  // flags of the left, own and right node as bits 0, 1, 2
+  auto right_of = [&](V2 own, V2 ex) {
+    V2 r;
+    r.x = __shfl_down_sync(FULL, own.x, 1);
+    r.y = __shfl_down_sync(FULL, own.y, 1);
+    return lane == 31 ? ex : r;
+  };
+  auto pattern = [&](unsigned own, unsigned ex) {
+    const unsigned l = __shfl_up_sync(FULL, own, 1), r = __shfl_down_sync(FULL, own, 1);
+    return l | (own << 1) | ((lane == 31 ? ex : r) << 2);
+  };
+  auto element = [&](int r, V2 b0, V2 b1, V2 t0, V2 t1, T k, T (&K)[10]) {
 #pragma unroll
     for (int u = 0; u < 10; ++u) K[u] = 0;
-    if (ei >= 0 && ei < nx && ej >= 0 && ej < ny) {
-      const int64_t n00 = (int64_t)ei * W + ej;
-      T x[4][2];
+    if (r >= 0 && r < nx && has_elem) {
+      const T x[4][2] = {{b0.x, b0.y}, {b1.x, b1.y}, {t1.x, t1.y}, {t0.x, t0.y}};
+      quad_stiffness<T, AFFINE>(x, k, K);
+    }
+  };
+  auto coefficient = [&](int r) {
+    if constexpr (MODEL == AGX_MODEL_HEAT_POTENTIAL)
+      if (elem_field) return elem_field[min(max(r, 0), nx - 1) * ny + cole];
+    return T(1);
+  };
+
+  // the element row above the segment (i_begin - 1), the state entering row i_begin and,
+  // already in flight while that element is integrated, the loads one row ahead: node row
+  // i + 1 (the top of element row i), element row i's coefficients, node row i's row pointers
+  T Kp[10];
+  V2 bottom, bottom_r;
+  unsigned pat_up, pat_mid;
+  int rn = rowc(i_begin - 1) * W;
+  const V2 ao = cp[rn + colc], ax = cp[rn + colx];
+  const unsigned fa = dmask_node[rn + colc] & 1u, fax = dmask_node[rn + colx] & 1u;
+  rn = rowc(i_begin) * W;
+  const V2 bo = cp[rn + colc], bx = cp[rn + colx];
+  const unsigned fb = dmask_node[rn + colc] & 1u, fbx = dmask_node[rn + colx] & 1u;
+  const T ka = coefficient(i_begin - 1);
+  rn = rowc(i_begin + 1) * W;
+  V2 nto = cp[rn + colc], ntx = cp[rn + colx];
+  unsigned nfo = dmask_node[rn + colc], nfx = dmask_node[rn + colx];
+  T nk = coefficient(i_begin);
+  int32_t nrp = rowptr[i_begin * W + colr];
+  pat_up = pattern(fa, fax);
+  pat_mid = pattern(fb, fbx);
+  bottom = bo;
+  bottom_r = right_of(bo, bx);
+  element(i_begin - 1, ao, right_of(ao, ax), bo, bottom_r, ka, Kp);
+
+  for (int i = i_begin; i < i_end; ++i) {
+    const V2 top = nto, topx = ntx;
+    const unsigned tfo = nfo & 1u, tfx = nfx & 1u;
+    const T kc = nk;
+    const int32_t rpn = nrp;
+    rn = rowc(i + 2) * W;  // the next row's loads, in flight while this row is computed
+    nto = cp[rn + colc];
+    ntx = cp[rn + colx];
+    nfo = dmask_node[rn + colc];
+    nfx = dmask_node[rn + colx];
+    nk = coefficient(i + 1);
+    nrp = rowptr[min(i + 1, nx) * W + colr];
+
+    const V2 top_r = right_of(top, topx);
+    const unsigned pat_dn = pattern(tfo, tfx);
+    T Kc[10];
+    element(i, bottom, bottom_r, top, top_r, kc, Kc);
+    // this lane's elements' share of the row of its own node (i, col) and of the node to its
+    // right (i, col + 1): entries (row offset, column offset) of the 3 x 3 stencil
+    const T o_m0 = Kp[sym4(3, 0)], o_m1 = Kp[sym4(3, 1)];
+    const T o_01 = Kp[sym4(3, 2)] + Kc[sym4(0, 1)], o_00 = Kp[sym4(3, 3)] + Kc[sym4(0, 0)];
+    const T o_p1 = Kc[sym4(0, 2)], o_p0 = Kc[sym4(0, 3)];
+    const T r_mm = Kp[sym4(2, 0)], r_m0 = Kp[sym4(2, 1)];
+    const T r_00 = Kp[sym4(2, 2)] + Kc[sym4(1, 1)], r_0m = Kp[sym4(2, 3)] + Kc[sym4(1, 0)];
+    const T r_p0 = Kc[sym4(1, 2)], r_pm = Kc[sym4(1, 3)];
+    T v[9];  // (di + 1) * 3 + (dj + 1)
+    v[0] = __shfl_up_sync(FULL, r_mm, 1);
+    v[1] = __shfl_up_sync(FULL, r_m0, 1) + o_m0;
+    v[2] = o_m1;
+    v[3] = __shfl_up_sync(FULL, r_0m, 1);
+    v[4] = __shfl_up_sync(FULL, r_00, 1) + o_00;
+    v[5] = o_01;
+    v[6] = __shfl_up_sync(FULL, r_pm, 1);
+    v[7] = __shfl_up_sync(FULL, r_p0, 1) + o_p0;
+    v[8] = o_p1;
+    if (__any_sync(FULL, (pat_up | pat_mid | pat_dn) != 0u)) {
+      if (pat_mid & 2u) {  // a prescribed node: identity row
 #pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        using V2 = typename std::conditional<std::is_same<T, float>::value, float2, double2>::type;
-        const V2 c = reinterpret_cast<const V2*>(coords)[n00 + oi[a] * W + oj[a]];  // (x, y) of a node
-        x[a][0] = c.x;
-        x[a][1] = c.y;
+        for (int u = 0; u < 9; ++u) v[u] = T(0);
+        v[4] = T(1);
+      } else {  // prescribed columns are deleted
+#pragma unroll
+        for (int dj = 0; dj < 3; ++dj) {
+          if ((pat_up >> dj) & 1u) v[dj] = T(0);
+          if ((pat_mid >> dj) & 1u) v[3 + dj] = T(0);
+          if ((pat_dn >> dj) & 1u) v[6 + dj] = T(0);
+        }
       }
-      T k = 1;
-      if constexpr (MODEL == AGX_MODEL_HEAT_POTENTIAL) k = elem_field ? elem_field[(int64_t)ei * ny + ej] : T(1);
-      // w det J g_a . g_b = dN_a^T M dN_b with M = adj(J) adj(J)^T / det J (Gauss weight 1):
-      // per point J, det J and the three entries of M, then three FMAs per pair with the
-      // reference derivatives as compile-time constants.  A parallelogram (x0 + x2 = x1 + x3)
-      // has one J for all points: then K = M00 C00 + M01 C01 + M11 C11 with the point sums
-      // C.. of the derivative products, three FMAs per pair in all.
-      const T ex = x[0][0] + x[2][0] - x[1][0] - x[3][0], ey = x[0][1] + x[2][1] - x[1][1] - x[3][1];
-      const T scale = fabs(x[2][0] - x[0][0]) + fabs(x[2][1] - x[0][1]) + fabs(x[1][0] - x[3][0]) +
-                      fabs(x[1][1] - x[3][1]);
-      const bool affine = fabs(ex) + fabs(ey) <= scale * (sizeof(T) == 4 ? T(1e-6) : T(1e-13));
-      if (affine) {
-        // J = (1/2) [x1 - x0 | x3 - x0] in the mesher's node order (dN constant in the other
-        // variable's direction cancels for a parallelogram)
-        const T J00 = T(0.5) * (x[1][0] - x[0][0]), J01 = T(0.5) * (x[3][0] - x[0][0]);
-        const T J10 = T(0.5) * (x[1][1] - x[0][1]), J11 = T(0.5) * (x[3][1] - x[0][1]);
-        const T rdet = T(1) / (J00 * J11 - J01 * J10);
-        const T M00 = (J11 * J11 + J01 * J01) * rdet;
-        const T M01 = -(J11 * J10 + J01 * J00) * rdet;
-        const T M11 = (J10 * J10 + J00 * J00) * rdet;
+    }
+    // the Jacobi inverse diagonal of the row (the inverse_diagonal pass, fused); the
+    // round-to-nearest reciprocal is the correctly rounded 1 / x
+    if (owner) dinv[i * W + col] = v[4] != T(0) ? rcp_rn(v[4]) : T(0);
+    // the strip's rows are consecutive nodes: one contiguous range of values [base, end),
+    // staged so that global value base + u sits at stage word shift + u and 16-byte chunks
+    // line up.  Lane l's row starts where lane l - 1's next-node row pointer points.
+    const int32_t base = __shfl_sync(FULL, rpn, 0), end = __shfl_sync(FULL, rpn, 31);
+    const int32_t rp = __shfl_up_sync(FULL, rpn, 1);
+    const int shift = base & (GVEC - 1);
+    if (owner) {
+      T* sr = st + shift + (rp - base);
+      if (strip_interior && i >= 1 && i < nx) {
 #pragma unroll
-        for (int a = 0; a < 4; ++a)
-#pragma unroll
-          for (int b = a; b < 4; ++b) {
-            T c00 = 0, c01 = 0, c11 = 0;  // compile-time sums over the four points
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              const T xq = (T)gauss_point(q & 1), yq = (T)gauss_point((q >> 1) & 1);
-              const T fa0 = (T(1) + T(node_sign<AGX_QUAD4>(a, 0)) * xq) * T(0.5);
-              const T fa1 = (T(1) + T(node_sign<AGX_QUAD4>(a, 1)) * yq) * T(0.5);
-              const T fb0 = (T(1) + T(node_sign<AGX_QUAD4>(b, 0)) * xq) * T(0.5);
-              const T fb1 = (T(1) + T(node_sign<AGX_QUAD4>(b, 1)) * yq) * T(0.5);
-              const T da0 = T(node_sign<AGX_QUAD4>(a, 0)) * T(0.5) * fa1, da1 = T(node_sign<AGX_QUAD4>(a, 1)) * T(0.5) * fa0;
-              const T db0 = T(node_sign<AGX_QUAD4>(b, 0)) * T(0.5) * fb1, db1 = T(node_sign<AGX_QUAD4>(b, 1)) * T(0.5) * fb0;
-              c00 += da0 * db0;
-              c01 += da0 * db1 + da1 * db0;
-              c11 += da1 * db1;
-            }
-            K[sym4(a, b)] = M00 * c00 + M01 * c01 + M11 * c11;
-          }
+        for (int u = 0; u < 9; ++u) sr[u] = v[u];
       } else {
+        int idx = 0;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        T dN[4][2];
+        for (int di = -1; di <= 1; ++di)
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          const T f0 = (T(1) + T(node_sign<AGX_QUAD4>(a, 0)) * (T)gauss_point(q & 1)) * T(0.5);
-          const T f1 = (T(1) + T(node_sign<AGX_QUAD4>(a, 1)) * (T)gauss_point((q >> 1) & 1)) * T(0.5);
-          dN[a][0] = T(node_sign<AGX_QUAD4>(a, 0)) * T(0.5) * f1;
-          dN[a][1] = T(node_sign<AGX_QUAD4>(a, 1)) * T(0.5) * f0;
-        }
-        T J00 = 0, J01 = 0, J10 = 0, J11 = 0;
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          J00 += x[a][0] * dN[a][0];
-          J01 += x[a][0] * dN[a][1];
-          J10 += x[a][1] * dN[a][0];
-          J11 += x[a][1] * dN[a][1];
-        }
-        const T rdet = T(1) / (J00 * J11 - J01 * J10);
-        const T M00 = (J11 * J11 + J01 * J01) * rdet;
-        const T M01 = -(J11 * J10 + J01 * J00) * rdet;
-        const T M11 = (J10 * J10 + J00 * J00) * rdet;
-#pragma unroll
-        for (int a = 0; a < 4; ++a)
-#pragma unroll
-          for (int b = a; b < 4; ++b)
-            K[sym4(a, b)] += M00 * (dN[a][0] * dN[b][0]) + M01 * (dN[a][0] * dN[b][1] + dN[a][1] * dN[b][0]) +
-                             M11 * (dN[a][1] * dN[b][1]);
+          for (int dj = -1; dj <= 1; ++dj)
+            if (i + di >= 0 && i + di <= nx && col + dj >= 0 && col + dj <= ny)
+              sr[idx++] = v[(di + 1) * 3 + (dj + 1)];
       }
-      }
-#pragma unroll
-      for (int u = 0; u < 10; ++u) K[u] *= k;
     }
-#pragma unroll
-    for (int u = 0; u < 10; ++u) ke[t][u] = K[u];
-  }
-  __syncthreads();
-  if (!row_warp) return;  // whole warps: the extra element warps and rows past the grid
-  const bool own = j <= ny;
-  if (own) {
-    T v[9];
-#pragma unroll
-    for (int u = 0; u < 9; ++u) v[u] = 0;
-    if (fixed[ty + 1][tx + 1]) {
-      v[4] = T(1);
-    } else {
-      // out-of-range elements hold zero matrices in shared memory: no tests needed
-#pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        const int t = (ty + 1 - oi[a]) * EX + (tx + 1 - oj[a]);
-#pragma unroll
-        for (int b = 0; b < 4; ++b) v[(oi[b] - oi[a] + 1) * 3 + (oj[b] - oj[a] + 1)] += ke[t][sym4(a, b)];
-      }
-      // Dirichlet columns are deleted
-#pragma unroll
-      for (int di = 0; di < 3; ++di)
-#pragma unroll
-        for (int dj = 0; dj < 3; ++dj)
-          if (fixed[ty + di][tx + dj]) v[di * 3 + dj] = T(0);
+    __syncwarp();
+    {
+      const int end_w = shift + (end - base);
+      const int first_full = (shift + GVEC - 1) / GVEC, last_full = end_w / GVEC;
+      V* dst = reinterpret_cast<V*>(vals + (base - shift));
+      const V* src = reinterpret_cast<const V*>(st);
+      for (int c = first_full + lane; c < last_full; c += 32) dst[c] = src[c];
+      // the partial first and last chunks, word by word (at most GVEC - 1 words each)
+      const int hw = shift + lane, head_end = min(first_full * GVEC, end_w);
+      if (lane < GVEC - 1 && hw < head_end) vals[base - shift + hw] = st[hw];
+      const int tw = max(last_full, first_full) * GVEC + (lane - 16);
+      if (lane >= 16 && lane < 16 + GVEC - 1 && tw < end_w) vals[base - shift + tw] = st[tw];
     }
-    // the Jacobi inverse diagonal of the row (the inverse_diagonal pass, fused)
-    dinv[p] = v[4] != T(0) ? T(1) / v[4] : T(0);
-    // the row's entries are the in-range stencil neighbours in column order; stage the warp's
-    // rows (consecutive nodes: one contiguous range of values) for a coalesced store
-    const int32_t off = rp - base;
-    int idx = 0;
+    __syncwarp();  // the stage is rewritten by the next row
 #pragma unroll
-    for (int di = -1; di <= 1; ++di)
-#pragma unroll
-      for (int dj = -1; dj <= 1; ++dj)
-        if (i + di >= 0 && i + di <= nx && j + dj >= 0 && j + dj <= ny) stage[ty][off + idx++] = v[(di + 1) * 3 + (dj + 1)];
+    for (int u = 0; u < 10; ++u) Kp[u] = Kc[u];
+    bottom = top;
+    bottom_r = top_r;
+    pat_up = pat_mid;
+    pat_mid = pat_dn;
   }
-  __syncwarp();
-  for (int u = tx; u < span; u += GT_X) vals[base + u] = stage[ty][u];
 }
 
 // ---- float64 neo-Hooke residual, one Gauss point per lane ---------------------------------
@@ -845,16 +957,32 @@ static agx_element_set* grid_tangent_set(agx_context* ctx) {
   return with_k == 1 ? hit : nullptr;
 }
 
+template <int MODEL, typename T, bool AFFINE>
+static void launch_grid_tangent_as(agx_context* ctx, agx_element_set& s, T* vals, T* dinv) {
+  // one wave: the resident blocks of every SM (occupancy calculator), never more warps than
+  // (strip, node row) pairs and never fewer than strips (one segment of rows each)
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grid_tangent_kernel<MODEL, T, AFFINE>, GS_WARPS * 32, 0);
+    per_sm = std::max(per_sm, 1);
+  }
+  const int64_t strips = (s.grid_ny + 1 + GS_NODES - 1) / GS_NODES, rows = (int64_t)s.grid_nx + 1;
+  const int64_t warps = std::max<int64_t>(strips, std::min<int64_t>((int64_t)ctx->sm_count * per_sm * GS_WARPS, rows * strips));
+  const unsigned grid = (unsigned)((warps + GS_WARPS - 1) / GS_WARPS);
+  grid_tangent_kernel<MODEL, T, AFFINE><<<grid, GS_WARPS * 32, 0, ctx->stream>>>(
+      s.grid_nx, s.grid_ny, coords_of<T>(ctx), elem_field_of<T>(s), ctx->d_dmask_node, ctx->d_rowptr, vals, dinv);
+  ctx->n_launches += 1;
+}
+
 template <typename T>
 static void launch_grid_tangent(agx_context* ctx, agx_element_set& s, T* vals, T* dinv) {
-  const dim3 grid((unsigned)((s.grid_ny + 1 + GT_X - 1) / GT_X), (unsigned)((s.grid_nx + 1 + GT_Y - 1) / GT_Y));
-  if (s.model == AGX_MODEL_HEAT_POTENTIAL)
-    grid_tangent_kernel<AGX_MODEL_HEAT_POTENTIAL, T><<<grid, GT_THREADS, 0, ctx->stream>>>(
-        s.grid_nx, s.grid_ny, coords_of<T>(ctx), elem_field_of<T>(s), ctx->d_dmask_node, ctx->d_rowptr, vals, dinv);
-  else
-    grid_tangent_kernel<AGX_MODEL_POISSON_SINCOS, T><<<grid, GT_THREADS, 0, ctx->stream>>>(
-        s.grid_nx, s.grid_ny, coords_of<T>(ctx), elem_field_of<T>(s), ctx->d_dmask_node, ctx->d_rowptr, vals, dinv);
-  ctx->n_launches += 1;
+  if (s.model == AGX_MODEL_HEAT_POTENTIAL) {
+    if (s.grid_affine) launch_grid_tangent_as<AGX_MODEL_HEAT_POTENTIAL, T, true>(ctx, s, vals, dinv);
+    else launch_grid_tangent_as<AGX_MODEL_HEAT_POTENTIAL, T, false>(ctx, s, vals, dinv);
+  } else {
+    if (s.grid_affine) launch_grid_tangent_as<AGX_MODEL_POISSON_SINCOS, T, true>(ctx, s, vals, dinv);
+    else launch_grid_tangent_as<AGX_MODEL_POISSON_SINCOS, T, false>(ctx, s, vals, dinv);
+  }
 }
 
 int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, int tangent_dtype) {

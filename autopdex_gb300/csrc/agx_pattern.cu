@@ -57,6 +57,21 @@ void detect_structured_grid(agx_context* ctx, agx_element_set& s, const std::vec
     }
   s.grid_nx = (int)nx;
   s.grid_ny = (int)ny;
+  // parallelograms (x0 + x2 = x1 + x3 to float64 rounding, the row kernel's own test): the
+  // row kernel then takes the one-Jacobian integral for every element without testing
+  s.grid_affine = true;
+  const double* X = ctx->h_coords.data();
+  for (int64_t e = 0; e < s.n_elem && s.grid_affine; ++e) {
+    const int32_t* n = c + e * 4;
+    const double* x0 = X + 2 * (int64_t)n[0];
+    const double* x1 = X + 2 * (int64_t)n[1];
+    const double* x2 = X + 2 * (int64_t)n[2];
+    const double* x3 = X + 2 * (int64_t)n[3];
+    const double ex = x0[0] + x2[0] - x1[0] - x3[0], ey = x0[1] + x2[1] - x1[1] - x3[1];
+    const double scale =
+        std::fabs(x2[0] - x0[0]) + std::fabs(x2[1] - x0[1]) + std::fabs(x1[0] - x3[0]) + std::fabs(x1[1] - x3[1]);
+    s.grid_affine = std::fabs(ex) + std::fabs(ey) <= scale * 1e-13;
+  }
 }
 
 }  // namespace

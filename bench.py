@@ -269,6 +269,7 @@ def gpu_arm(args):
     if rank == 0 and not args.only_mixed:
         try:
             line["assembly_hbm"] = assembly_roofline()
+            line["assembly_hbm_2048"] = assembly_roofline(n=2048)  # values (151 MB) larger than L2
         except Exception as e:  # noqa: BLE001 -- reported, the headline stands
             line["assembly_hbm"] = {"error": str(e)[:200]}
     if rank == 0 and not args.only_mixed and not args.no_learned:
@@ -345,27 +346,37 @@ def assembly_roofline(n=1024, reps=20):
     x = torch.zeros(prob.n_dofs, dtype=torch.float64, device=prob.device)
     for _ in range(3):
         prob._call("agx_assemble", C.c_void_p(x.data_ptr()), None, N.AGX_F32)
-    prob._call("agx_profile", 1)
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record()
-    for _ in range(reps):
+    # The mesh's arrays and values (about 60 MB) fit in the 129 MB L2: every timed call
+    # follows a write of a 256 MB buffer, so that its inputs come from HBM.
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=prob.device)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for a, b in ev:  # per call, the library's own timing off
+        flush.fill_(1)
+        a.record()
         prob._call("agx_assemble", C.c_void_p(x.data_ptr()), None, N.AGX_F32)
-    b.record()
+        b.record()
+    torch.cuda.synchronize()
+    call_ms = sum(a.elapsed_time(b) for a, b in ev)
+    prob._call("agx_profile", 1)
+    for _ in range(reps):  # per kernel: the library's events around each row-kernel launch
+        flush.fill_(1)
+        prob._call("agx_assemble", C.c_void_p(x.data_ptr()), None, N.AGX_F32)
     torch.cuda.synchronize()
     ms = (C.c_double * N.AGX_PROF_CATEGORIES)()
     cnt = (C.c_int64 * N.AGX_PROF_CATEGORIES)()
     prob._call("agx_profile_read", ms, cnt)
     prob._call("agx_profile", 0)
+    del flush
     n_e = n * n
     nbytes = prob.n_nodes * 2 * 8 + prob.n_dofs * 8 + n_e * 4 * 4 + prob.nnzb * 4
-    call_s = a.elapsed_time(b) / 1e3 / reps
+    call_s = call_ms / 1e3 / reps
     kern_s = ms[N.AGX_PROF_TANGENT] / 1e3 / max(1, cnt[N.AGX_PROF_TANGENT])
     peak, kind = _peaks()
     return {"workload": f"heat_grf_{n}x{n}_q1 float32 tangent", "kernel": "grid_tangent_kernel<HEAT_POTENTIAL,float>",
             "algorithmic_bytes": nbytes, "call_us": call_s * 1e6, "kernel_us": kern_s * 1e6,
             "achieved_gbs_call": nbytes / call_s / 1e9, "achieved_gbs_kernel": nbytes / kern_s / 1e9,
             "peak_gbs": peak, "frac_call": nbytes / call_s / 1e9 / peak, "frac_kernel": nbytes / kern_s / 1e9 / peak,
-            "peak_source": kind}
+            "peak_source": kind, "l2": "256 MB buffer written before every timed call"}
 
 
 def _timed_solve(w, static, step=None, x0=None, rtol=1e-10, **kw):
