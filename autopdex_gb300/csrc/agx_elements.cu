@@ -501,7 +501,7 @@ __device__ __forceinline__ void quad_stiffness(const T (&x)[4][2], T k, T (&K)[1
     // variable's direction cancels for a parallelogram)
     const T J00 = T(0.5) * (x[1][0] - x[0][0]), J01 = T(0.5) * (x[3][0] - x[0][0]);
     const T J10 = T(0.5) * (x[1][1] - x[0][1]), J11 = T(0.5) * (x[3][1] - x[0][1]);
-    const T rdet = rcp_rn(J00 * J11 - J01 * J10);
+    const T rdet = k * rcp_rn(J00 * J11 - J01 * J10);  // the coefficient k folded in
     const T M00 = (J11 * J11 + J01 * J01) * rdet;
     const T M01 = -(J11 * J10 + J01 * J00) * rdet;
     const T M11 = (J10 * J10 + J00 * J00) * rdet;
@@ -555,9 +555,9 @@ __device__ __forceinline__ void quad_stiffness(const T (&x)[4][2], T k, T (&K)[1
           K[sym4(a, b)] += M00 * (dN[a][0] * dN[b][0]) + M01 * (dN[a][0] * dN[b][1] + dN[a][1] * dN[b][0]) +
                            M11 * (dN[a][1] * dN[b][1]);
     }
-  }
 #pragma unroll
-  for (int u = 0; u < 10; ++u) K[u] *= k;
+    for (int u = 0; u < 10; ++u) K[u] *= k;
+  }
 }
 
 template <int MODEL, typename T, bool AFFINE>
@@ -653,6 +653,8 @@ grid_tangent_kernel(int nx, int ny, const T* __restrict__ coords, const T* __res
   bottom_r = right_of(bo, bx);
   element(i_begin - 1, ao, right_of(ao, ax), bo, bottom_r, ka, Kp);
 
+  // two rows per trip: the element-row registers alternate without copies
+#pragma unroll 2
   for (int i = i_begin; i < i_end; ++i) {
     const V2 top = nto, topx = ntx;
     const unsigned tfo = nfo & 1u, tfx = nfx & 1u;
