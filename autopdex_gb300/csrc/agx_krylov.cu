@@ -78,6 +78,56 @@ __device__ bool reduce_last_block(double (&v)[NV], double* __restrict__ partials
   return true;
 }
 
+// Reductions of the Jacobi-PCG iteration: the product and the update kernels only write one
+// partial per block and value (no fence, no counter: the kernel boundary orders them), and a
+// one-block kernel after each sums them in block order and sets the step scalars.  The last-
+// block pattern above costs these two kernels 7-12 us per launch at 600-900 blocks on this
+// GPU (measured against the same kernels without a reduction); a separate one-block launch
+// costs a few microseconds.
+template <int NV>
+__device__ __forceinline__ void write_block_partials(const double (&v)[NV], double* __restrict__ partials) {
+  __shared__ double sh[NV][NWARP];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    const double s = warp_sum(v[k]);
+    if (lane == 0) sh[k][warp] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    double s = 0;
+    for (int w = 0; w < NWARP; ++w) s += sh[threadIdx.x][w];
+    partials[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = s;
+  }
+}
+
+// totals of NV partial arrays of `np` blocks each (np <= 8 * AGX_BLOCK), valid in thread 0
+template <int NV>
+__device__ __forceinline__ void sum_block_partials(const double* __restrict__ partials, int np, double (&tot)[NV]) {
+  __shared__ double sh[NV][NWARP];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double part[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int i = threadIdx.x + u * AGX_BLOCK;
+      part[u] = i < np ? __ldcg(partials + (size_t)k * np + i) : 0.0;
+    }
+    const double s = warp_sum(((part[0] + part[1]) + (part[2] + part[3])) + ((part[4] + part[5]) + (part[6] + part[7])));
+    if (lane == 0) sh[k][warp] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double t = 0;
+      for (int w = 0; w < NWARP; ++w) t += sh[k][w];
+      tot[k] = t;
+    }
+  }
+}
+
 __device__ __forceinline__ bool bad(double x) { return !isfinite(x) || x == 0.0; }
 
 // ---- sparse product ------------------------------------------------------------------
@@ -152,7 +202,7 @@ __global__ void __launch_bounds__(AGX_BLOCK)
 spmv_dot_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                 const T* __restrict__ vals, int64_t nnzb, const T* __restrict__ z, const T* __restrict__ pold,
                 T* __restrict__ pnew, T* __restrict__ q, agx_krylov_scalars* sc, double* partials, unsigned* counter,
-                const T* __restrict__ rflex) {
+                const T* __restrict__ rflex, int block_partials) {
   if (sc->converged) return;
   const T beta = (T)sc->beta;
   const int sub = threadIdx.x % TPR;
@@ -175,6 +225,11 @@ spmv_dot_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_
     }
   }
   double acc[2] = {(double)acc_t, (double)accr_t};
+  if (block_partials) {  // Jacobi-PCG: pcg_finish_pq sums them
+    const double acc1[1] = {acc[0]};
+    write_block_partials<1>(acc1, partials);
+    return;
+  }
   double tot[2];
   if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
     sc->pq = tot[0];
@@ -293,20 +348,44 @@ pcg_update_kernel(int64_t n, T* __restrict__ x, T* __restrict__ r, T* __restrict
     rz_t += ri * zi;
     rr_t += ri * ri;
   }
-  double acc[2] = {(double)rz_t, (double)rr_t};
-  double tot[2];
-  if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+  const double acc[2] = {(double)rz_t, (double)rr_t};
+  write_block_partials<2>(acc, partials);  // pcg_finish_rz sums them
+}
+
+// one block: alpha = (r, z) / (p, A p) from the product's block partials
+__global__ void __launch_bounds__(AGX_BLOCK)
+pcg_finish_pq(agx_krylov_scalars* sc, const double* __restrict__ parts, int np) {
+  if (sc->converged) return;
+  double t[1];
+  sum_block_partials<1>(parts, np, t);
+  if (threadIdx.x == 0) {
+    sc->pq = t[0];
+    // Only a zero or non-finite (p, Ap) is a breakdown: the tangents of clockwise-numbered
+    // quads (mesher.py:88-94 numbers quads clockwise, so det J < 0) are negative definite,
+    // and CG with a Jacobi preconditioner of the same sign runs as on (-K, -D).
+    if (bad(t[0])) sc->converged = 2;
+    else sc->alpha = sc->rz / t[0];
+  }
+}
+
+// one block: the update's (r, z) and (r, r): iteration count, convergence test, beta
+__global__ void __launch_bounds__(AGX_BLOCK)
+pcg_finish_rz(agx_krylov_scalars* sc, const double* __restrict__ parts, int np) {
+  if (sc->converged) return;
+  double t[2];
+  sum_block_partials<2>(parts, np, t);
+  if (threadIdx.x == 0) {
     sc->iters += 1;
-    sc->rr = tot[1];
-    if (!isfinite(tot[0]) || !isfinite(tot[1])) {
+    sc->rr = t[1];
+    if (!isfinite(t[0]) || !isfinite(t[1])) {
       sc->converged = 2;
-    } else if (tot[1] <= sc->rr_stop) {
+    } else if (t[1] <= sc->rr_stop) {
       sc->converged = 1;
     } else if (sc->rz == 0.0) {
       sc->converged = 2;
     } else {
-      sc->beta = tot[0] / sc->rz;
-      sc->rz = tot[0];
+      sc->beta = t[0] / sc->rz;
+      sc->rz = t[0];
     }
   }
 }
@@ -655,40 +734,44 @@ int resident_grid(agx_context* ctx, K kernel) {
   return g < ctx->red_blocks ? g : ctx->red_blocks;
 }
 
+// returns the grid (the number of block partials written when block_partials is set)
 template <typename T, int ND, int TP>
-void spmv_dot_variant(agx_context* ctx, const T* vals, const T* z, const T* pold, T* pnew, T* q, const T* rflex) {
+int spmv_dot_variant(agx_context* ctx, const T* vals, const T* z, const T* pold, T* pnew, T* q, const T* rflex,
+                     int block_partials) {
   static int g_cache = 0;
   if (!g_cache) g_cache = resident_grid(ctx, spmv_dot_kernel<T, ND, TP>);
   spmv_dot_kernel<T, ND, TP><<<g_cache, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_nodes, ctx->d_rowptr, ctx->d_col, vals,
                                                                      ctx->nnzb, z, pold, pnew, q, ctx->d_scal,
-                                                                     ctx->d_partials, ctx->d_counter, rflex);
+                                                                     ctx->d_partials, ctx->d_counter, rflex,
+                                                                     block_partials);
+  return g_cache;
 }
 
 // default lanes per block row when the autotuner has not chosen one
 int default_tpr(const agx_context* ctx) { return ctx->ndof == 1 ? (ctx->dim == 3 ? 8 : 4) : (ctx->ndof == 2 ? 4 : 8); }
 
 template <typename T, int ND>
-void spmv_dot_nd(agx_context* ctx, int tpr, const T* vals, const T* z, const T* pold, T* pnew, T* q,
-                 const T* rflex) {
+int spmv_dot_nd(agx_context* ctx, int tpr, const T* vals, const T* z, const T* pold, T* pnew, T* q,
+                const T* rflex, int block_partials = 0) {
   switch (tpr) {
-    case 1: spmv_dot_variant<T, ND, 1>(ctx, vals, z, pold, pnew, q, rflex); break;
-    case 2: spmv_dot_variant<T, ND, 2>(ctx, vals, z, pold, pnew, q, rflex); break;
-    case 4: spmv_dot_variant<T, ND, 4>(ctx, vals, z, pold, pnew, q, rflex); break;
-    case 16: spmv_dot_variant<T, ND, 16>(ctx, vals, z, pold, pnew, q, rflex); break;
-    default: spmv_dot_variant<T, ND, 8>(ctx, vals, z, pold, pnew, q, rflex); break;
+    case 1: return spmv_dot_variant<T, ND, 1>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
+    case 2: return spmv_dot_variant<T, ND, 2>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
+    case 4: return spmv_dot_variant<T, ND, 4>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
+    case 16: return spmv_dot_variant<T, ND, 16>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
+    default: return spmv_dot_variant<T, ND, 8>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
   }
 }
 
 // rflex (flexible CG only): the residual whose dot with the new direction gives the step
 template <typename T>
-void launch_spmv_dot(agx_context* ctx, const T* vals, const T* z, const T* pold, T* pnew, T* q,
-                     const T* rflex = nullptr) {
+int launch_spmv_dot(agx_context* ctx, const T* vals, const T* z, const T* pold, T* pnew, T* q,
+                    const T* rflex = nullptr, int block_partials = 0) {
   agx_prof_scope ps(ctx, AGX_PROF_SPMV);
   const int tuned = ctx->spmv_tpr[std::is_same<T, float>::value ? 1 : 0];
   const int tpr = tuned > 0 ? tuned : default_tpr(ctx);
-  if (ctx->ndof == 1) spmv_dot_nd<T, 1>(ctx, tpr, vals, z, pold, pnew, q, rflex);
-  else if (ctx->ndof == 2) spmv_dot_nd<T, 2>(ctx, tpr, vals, z, pold, pnew, q, rflex);
-  else spmv_dot_nd<T, 3>(ctx, tpr, vals, z, pold, pnew, q, rflex);
+  if (ctx->ndof == 1) return spmv_dot_nd<T, 1>(ctx, tpr, vals, z, pold, pnew, q, rflex, block_partials);
+  if (ctx->ndof == 2) return spmv_dot_nd<T, 2>(ctx, tpr, vals, z, pold, pnew, q, rflex, block_partials);
+  return spmv_dot_nd<T, 3>(ctx, tpr, vals, z, pold, pnew, q, rflex, block_partials);
 }
 
 template <int NDOF, int TPR>
@@ -1088,16 +1171,18 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
     auto chunk = [&](int kn) {
       for (int k = 0; k < kn; ++k) {
         double* pnew = pbuf[cur ^ 1];
-        launch_spmv_dot<double>(ctx, ctx->d_vals64, ctx->d_z, pbuf[cur], pnew, ctx->d_q);
+        const int ns = launch_spmv_dot<double>(ctx, ctx->d_vals64, ctx->d_z, pbuf[cur], pnew, ctx->d_q, nullptr, 1);
+        pcg_finish_pq<<<1, AGX_BLOCK, 0, ctx->stream>>>(sc, ctx->d_partials, ns);
         agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
         pcg_update_kernel<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, x, ctx->d_r, ctx->d_z, pnew, ctx->d_q,
                                                                    ctx->d_dinv64, sc, ctx->d_partials, ctx->d_counter);
+        pcg_finish_rz<<<1, AGX_BLOCK, 0, ctx->stream>>>(sc, ctx->d_partials, g);
         cur ^= 1;
       }
     };
     while (true) {
       const int kn = std::min(every, maxiter - it_done);
-      ctx->n_launches += 2 * kn;
+      ctx->n_launches += 4 * kn;
       if (int rc = run_chunk(ctx, 0, x, every, kn, chunk)) return rc;
       int rc = read_scalars(ctx);
       if (rc) return rc;
@@ -1123,13 +1208,15 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
     auto chunk = [&](int kn) {
       for (int k = 0; k < kn; ++k) {
         float* pnew = pbuf[cur ^ 1];
-        launch_spmv_dot<float>(ctx, ctx->d_vals32, ctx->f_z, pbuf[cur], pnew, ctx->f_q,
-                               flexible ? (const float*)ctx->f_r : nullptr);
+        const int ns = launch_spmv_dot<float>(ctx, ctx->d_vals32, ctx->f_z, pbuf[cur], pnew, ctx->f_q,
+                                              flexible ? (const float*)ctx->f_r : nullptr, flexible ? 0 : 1);
         if (!flexible) {
+          pcg_finish_pq<<<1, AGX_BLOCK, 0, ctx->stream>>>(sc, ctx->d_partials, ns);
           agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
           pcg_update_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, ctx->f_r, ctx->f_z, pnew,
                                                                     ctx->f_q, ctx->d_dinv32, sc, ctx->d_partials,
                                                                     ctx->d_counter);
+          pcg_finish_rz<<<1, AGX_BLOCK, 0, ctx->stream>>>(sc, ctx->d_partials, g);
         } else {
           {
             agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
@@ -1148,7 +1235,7 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
     };
     while (true) {
       const int kn = std::min(every, maxiter - it_done);
-      ctx->n_launches += (flexible ? 4 : 2) * kn;
+      ctx->n_launches += 4 * kn;
       if (flexible && !ctx->precond_capturable) {
         chunk(kn);  // a preconditioner that may synchronise or allocate: no graph
         AGX_CHECK_LAUNCH(ctx);
