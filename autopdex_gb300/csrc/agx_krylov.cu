@@ -297,9 +297,9 @@ pcg_init_kernel(int64_t n, const double* __restrict__ b, const T* __restrict__ d
   }
 }
 
-// x += a p; r -= a q; z = Dinv r; rz_new, rr; beta.  16-byte vector loads and stores (4 floats
-// or 2 doubles per access) when every vector is 16-byte aligned (the library's own are; a
-// caller's x may not be), a scalar loop for the rest.
+// x += a p; r -= a q; z = Dinv r; block partials of (r, z) and (r, r) for pcg_finish_rz.
+// 16-byte vector loads and stores (4 floats or 2 doubles per access) when every vector is
+// 16-byte aligned (the library's own are; a caller's x may not be), a scalar loop for the rest.
 template <typename T>
 struct alignas(16) vec16 {
   T v[16 / sizeof(T)];
@@ -308,8 +308,8 @@ struct alignas(16) vec16 {
 template <typename T>
 __global__ void __launch_bounds__(AGX_BLOCK)
 pcg_update_kernel(int64_t n, T* __restrict__ x, T* __restrict__ r, T* __restrict__ z, const T* __restrict__ p,
-                  const T* __restrict__ q, const T* __restrict__ dinv, agx_krylov_scalars* sc, double* partials,
-                  unsigned* counter) {
+                  const T* __restrict__ q, const T* __restrict__ dinv, agx_krylov_scalars* sc,
+                  double* __restrict__ partials) {
   if (sc->converged) return;
   constexpr int V = 16 / sizeof(T);
   using W = vec16<T>;
@@ -1175,7 +1175,7 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
         pcg_finish_pq<<<1, AGX_BLOCK, 0, ctx->stream>>>(sc, ctx->d_partials, ns);
         agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
         pcg_update_kernel<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, x, ctx->d_r, ctx->d_z, pnew, ctx->d_q,
-                                                                   ctx->d_dinv64, sc, ctx->d_partials, ctx->d_counter);
+                                                                   ctx->d_dinv64, sc, ctx->d_partials);
         pcg_finish_rz<<<1, AGX_BLOCK, 0, ctx->stream>>>(sc, ctx->d_partials, g);
         cur ^= 1;
       }
@@ -1214,8 +1214,7 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
           pcg_finish_pq<<<1, AGX_BLOCK, 0, ctx->stream>>>(sc, ctx->d_partials, ns);
           agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
           pcg_update_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, ctx->f_r, ctx->f_z, pnew,
-                                                                    ctx->f_q, ctx->d_dinv32, sc, ctx->d_partials,
-                                                                    ctx->d_counter);
+                                                                    ctx->f_q, ctx->d_dinv32, sc, ctx->d_partials);
           pcg_finish_rz<<<1, AGX_BLOCK, 0, ctx->stream>>>(sc, ctx->d_partials, g);
         } else {
           {
