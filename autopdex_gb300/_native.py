@@ -15,6 +15,7 @@ AGX_PRECOND_CAPTURABLE = 1
 AGX_DIVERGED = 2
 
 AGX_QUAD4, AGX_HEX8, AGX_LINE2, AGX_QUAD9, AGX_LINE3 = 0, 1, 2, 3, 4
+AGX_TRI3, AGX_TRI6, AGX_TET4 = 5, 6, 7
 AGX_MODEL_POISSON_SINCOS = 0
 AGX_MODEL_HEAT_POTENTIAL = 1
 AGX_MODEL_NEO_HOOKE = 2
@@ -68,6 +69,7 @@ _SIGNATURES = {
     "agx_copy_matrix": (C.c_int, [_P, C.c_int, _P, _P, _P]),
     "agx_copy_values": (C.c_int, [_P, C.c_int, _P]),
     "agx_set_quadrature": (C.c_int, [_P, C.c_int, C.c_int]),
+    "agx_set_quadrature_points": (C.c_int, [_P, C.c_int, C.c_int, _P, _P]),
     "agx_spmv_values": (C.c_int, [_P, C.c_int, _P, _P, _P]),
     "agx_jacobi": (C.c_int, [_P, C.c_int, _P, _P]),
     "agx_spmv": (C.c_int, [_P, C.c_int, _P, _P]),

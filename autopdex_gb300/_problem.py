@@ -69,19 +69,20 @@ def _field(obj, key):
     return obj
 
 
-def _elem_type(nen, dim):
-    if dim == 2 and nen == 4:
-        return N.AGX_QUAD4
-    if dim == 3 and nen == 8:
-        return N.AGX_HEX8
-    if dim == 2 and nen == 2:
-        return N.AGX_LINE2
-    if dim == 2 and nen == 9:
-        return N.AGX_QUAD9
-    if dim == 2 and nen == 3:
-        return N.AGX_LINE3
-    raise NotImplementedError(f"elements with {nen} nodes in {dim}-D are not supported by the gb300 backend "
-                              "(Q1/Q2 quads, Q1 bricks, 2- and 3-node boundary lines)")
+def _elem_type(nen, dim, surface=False):
+    """Element type of a set: boundary lines (a surface model) or domain elements by their
+    node count (3-node triangles and 3-node lines differ only in the model)."""
+    if surface:
+        if dim == 2 and nen in (2, 3):
+            return N.AGX_LINE2 if nen == 2 else N.AGX_LINE3
+    else:
+        table = {(2, 4): N.AGX_QUAD4, (2, 9): N.AGX_QUAD9, (2, 3): N.AGX_TRI3, (2, 6): N.AGX_TRI6,
+                 (3, 8): N.AGX_HEX8, (3, 4): N.AGX_TET4}
+        if (dim, nen) in table:
+            return table[(dim, nen)]
+    raise NotImplementedError(f"{'boundary' if surface else 'domain'} elements with {nen} nodes in {dim}-D are not "
+                              "supported by the gb300 backend (Q1/Q2 quads, P1/P2 triangles, Q1 bricks, P1 "
+                              "tetrahedra, 2- and 3-node boundary lines)")
 
 
 def flatten(values, key):
@@ -117,16 +118,25 @@ class Problem:
         self.ctx = ctx
         self._call("agx_set_nodes", self.n_nodes, self.dim, self.coords.ctypes.data, self.ndof)
         self.conns = []
-        for conn_obj in settings["connectivity"]:
+        if len(settings["connectivity"]) != len(self.models):
+            raise ValueError("settings['connectivity'] must have one entry per set")
+        for conn_obj, desc in zip(settings["connectivity"], self.models):
             conn = _np(_field(conn_obj, self.key), np.int64)
-            et = _elem_type(conn.shape[1], self.dim)
+            et = _elem_type(conn.shape[1], self.dim, surface=getattr(desc, "dim", None) == 1)
             sid = C.c_int()
             self._call("agx_add_element_set", et, conn.shape[0], conn.shape[1], conn.ctypes.data, C.byref(sid))
             self.conns.append(conn)
-        for sid, desc in enumerate(self.models[:len(self.conns)]):
-            self._call("agx_set_quadrature", sid, int(getattr(desc, "ngauss", 2)))
-        if len(self.conns) != len(self.models):
-            raise ValueError("settings['connectivity'] must have one entry per set")
+            qp = getattr(desc, "qpoints", None)
+            if et in (N.AGX_TRI3, N.AGX_TRI6, N.AGX_TET4):
+                if qp is None:
+                    raise NotImplementedError("simplex elements need a simplex rule (seeder.int_pts_ref_tri/tet)")
+                pts = np.ascontiguousarray(qp, dtype=np.float64)
+                w = np.ascontiguousarray(desc.qweights, dtype=np.float64)
+                self._call("agx_set_quadrature_points", sid, pts.shape[0], pts.ctypes.data, w.ctypes.data)
+            elif qp is not None:
+                raise NotImplementedError("a simplex rule was given for a quad/brick/line set")
+            else:
+                self._call("agx_set_quadrature", sid, int(getattr(desc, "ngauss", 2)))
         self.mask = None
         self.set_dirichlet(settings.get("dirichlet dofs"))
         self._call("agx_finalize")

@@ -95,25 +95,22 @@ void free_device(agx_context* ctx) {
 
 bool model_ok(int elem_type, int model, int dim, int ndof, int n_params, std::string& why) {
   const int sdim = dim;
+  const bool domain = elem_type == AGX_QUAD4 || elem_type == AGX_HEX8 || elem_type == AGX_QUAD9 ||
+                      elem_type == AGX_TRI3 || elem_type == AGX_TRI6 || elem_type == AGX_TET4;
   switch (model) {
     case AGX_MODEL_POISSON_SINCOS:
       if (ndof != 1) return why = "POISSON_SINCOS needs 1 DOF per node", false;
       if (n_params < 2 + sdim) return why = "POISSON_SINCOS needs params a, w, c[dim]", false;
-      return elem_type == AGX_QUAD4 || elem_type == AGX_HEX8 || elem_type == AGX_QUAD9
-                 ? true
-                 : (why = "domain element required", false);
+      return domain ? true : (why = "domain element required", false);
     case AGX_MODEL_HEAT_POTENTIAL:
       if (ndof != 1) return why = "HEAT_POTENTIAL needs 1 DOF per node", false;
       if (n_params < 1) return why = "HEAT_POTENTIAL needs param f", false;
-      return elem_type == AGX_QUAD4 || elem_type == AGX_HEX8 || elem_type == AGX_QUAD9
-                 ? true
-                 : (why = "domain element required", false);
+      return domain ? true : (why = "domain element required", false);
     case AGX_MODEL_NEO_HOOKE:
       if (ndof != sdim) return why = "NEO_HOOKE needs dim DOFs per node", false;
       if (n_params < 2) return why = "NEO_HOOKE needs params E, nu", false;
-      if ((elem_type == AGX_QUAD4 || elem_type == AGX_QUAD9) && dim == 2) return true;
-      if (elem_type == AGX_HEX8 && dim == 3) return true;
-      return why = "NEO_HOOKE needs quad4/quad9 in 2-D or hex8 in 3-D", false;
+      if (domain) return true;
+      return why = "NEO_HOOKE needs a domain element (quad4/quad9/tri3/tri6 in 2-D, hex8/tet4 in 3-D)", false;
     case AGX_MODEL_NEUMANN:
       if ((elem_type != AGX_LINE2 && elem_type != AGX_LINE3) || dim != 2)
         return why = "NEUMANN supports 2- and 3-node lines in 2-D", false;
@@ -188,10 +185,13 @@ int agx_add_element_set(agx_context* ctx, int elem_type, int64_t n_elem, int nen
                    : elem_type == AGX_LINE2 ? 2
                    : elem_type == AGX_QUAD9 ? 9
                    : elem_type == AGX_LINE3 ? 3
+                   : elem_type == AGX_TRI3  ? 3
+                   : elem_type == AGX_TRI6  ? 6
+                   : elem_type == AGX_TET4  ? 4
                                             : -1;
   if (want < 0 || nen != want) return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "element type %d with %d nodes", elem_type, nen);
-  if ((elem_type == AGX_HEX8) != (ctx->dim == 3))
-    return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "hex8 needs 3-D nodes, quads and lines 2-D nodes");
+  if ((elem_type == AGX_HEX8 || elem_type == AGX_TET4) != (ctx->dim == 3))
+    return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "hex8 and tet4 need 3-D nodes, quads, triangles and lines 2-D nodes");
   agx_element_set s;
   s.elem_type = elem_type;
   s.nen = nen;
@@ -295,6 +295,24 @@ int agx_set_quadrature(agx_context* ctx, int set_id, int points_per_direction) {
     }
     ctx->tangent_valid = -1;
   }
+  return AGX_OK;
+}
+
+int agx_set_quadrature_points(agx_context* ctx, int set_id, int n_points, const double* points,
+                              const double* weights) {
+  if (!ctx || set_id < 0 || set_id >= (int)ctx->sets.size()) return agx_fail(ctx, AGX_ERR_ARG, "bad set id");
+  auto& s = ctx->sets[set_id];
+  const int rdim = s.elem_type == AGX_TET4 ? 3 : 2;
+  if (s.elem_type != AGX_TRI3 && s.elem_type != AGX_TRI6 && s.elem_type != AGX_TET4)
+    return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "integration point tables are for simplex sets");
+  if (!points || !weights || n_points < 1 || n_points > AGX_MAX_QPOINTS)
+    return agx_fail(ctx, AGX_ERR_ARG, "1 to %d integration points", AGX_MAX_QPOINTS);
+  s.nqp = n_points;
+  for (int q = 0; q < AGX_MAX_QPOINTS; ++q) {
+    for (int d = 0; d < 3; ++d) s.qp[q][d] = (q < n_points && d < rdim) ? points[q * rdim + d] : 0.0;
+    s.qw[q] = q < n_points ? weights[q] : 0.0;
+  }
+  ctx->tangent_valid = -1;
   return AGX_OK;
 }
 

@@ -21,6 +21,9 @@ struct agx_element_set {
   int elem_type = -1;        // AGX_QUAD4 / AGX_HEX8 / AGX_LINE2 / AGX_QUAD9 / AGX_LINE3
   int nen = 0;               // nodes per element
   int ngauss = 2;            // Gauss-Legendre points per reference direction (2 or 3)
+  int nqp = 0;               // simplex sets: integration points and weights on the reference simplex
+  double qp[AGX_MAX_QPOINTS][3] = {};
+  double qw[AGX_MAX_QPOINTS] = {};
   int64_t n_elem = 0;
   int32_t* d_conn = nullptr; // n_elem * nen
   int32_t* d_epos = nullptr; // n_elem * nen * nen node-block positions in the BSR pattern

@@ -54,6 +54,29 @@ template <>
 struct ElemTraits<AGX_LINE3> {
   static constexpr int RDIM = 1, NEN = 3, GROUP = 4;
 };
+template <>
+struct ElemTraits<AGX_TRI3> {
+  static constexpr int RDIM = 2, NEN = 3, GROUP = 4;
+};
+template <>
+struct ElemTraits<AGX_TRI6> {
+  static constexpr int RDIM = 2, NEN = 6, GROUP = 8;
+};
+template <>
+struct ElemTraits<AGX_TET4> {
+  static constexpr int RDIM = 3, NEN = 4, GROUP = 4;
+};
+template <int ET>
+__host__ __device__ constexpr bool is_simplex() { return ET == AGX_TRI3 || ET == AGX_TRI6 || ET == AGX_TET4; }
+template <int ET>
+__host__ __device__ constexpr int space_dim() { return (ET == AGX_HEX8 || ET == AGX_TET4) ? 3 : 2; }
+
+// integration points of a simplex set (reference coordinates and weights), passed by value
+struct QuadTable {
+  int n;
+  double x[AGX_MAX_QPOINTS][3];
+  double w[AGX_MAX_QPOINTS];
+};
 
 // 2-point Gauss-Legendre on [-1, 1] from the [0, 1] rule of seeder.py:382-386 mapped as
 // seeder.py:1053-1058; weights 2 * 0.5 = 1.
@@ -115,6 +138,45 @@ __device__ __forceinline__ void shape(int a, const T* xi, T& Na, T* dN) {
     Na = lx * ly;
     dN[0] = dlx * ly;
     dN[1] = lx * dly;
+  } else if constexpr (ET == AGX_TRI3) {
+    // N = 1 - xi - eta, xi, eta (the 3-node case of fem_iso_line_tri_tet, n_dim 2)
+    Na = a == 0 ? T(1) - xi[0] - xi[1] : (a == 1 ? xi[0] : xi[1]);
+    dN[0] = a == 0 ? T(-1) : (a == 1 ? T(1) : T(0));
+    dN[1] = a == 0 ? T(-1) : (a == 2 ? T(1) : T(0));
+  } else if constexpr (ET == AGX_TET4) {
+    // N = 1 - xi - eta - zeta, xi, eta, zeta (the 4-node case, n_dim 3)
+    Na = a == 0 ? T(1) - xi[0] - xi[1] - xi[2] : (a == 1 ? xi[0] : (a == 2 ? xi[1] : xi[2]));
+#pragma unroll
+    for (int d = 0; d < 3; ++d) dN[d] = a == 0 ? T(-1) : (a == d + 1 ? T(1) : T(0));
+  } else if constexpr (ET == AGX_TRI6) {
+    // the 6-node case, in barycentric form with L0 = 1 - xi - eta, L1 = xi, L2 = eta:
+    // corners L_i (2 L_i - 1), mid-sides 4 L0 L1, 4 L1 L2, 4 L2 L0
+    const T L0 = T(1) - xi[0] - xi[1], L1 = xi[0], L2 = xi[1];
+    // dL/dxi = (-1, 1, 0), dL/deta = (-1, 0, 1)
+    if (a == 0) {
+      Na = L0 * (T(2) * L0 - T(1));
+      dN[0] = dN[1] = -(T(4) * L0 - T(1));
+    } else if (a == 1) {
+      Na = L1 * (T(2) * L1 - T(1));
+      dN[0] = T(4) * L1 - T(1);
+      dN[1] = T(0);
+    } else if (a == 2) {
+      Na = L2 * (T(2) * L2 - T(1));
+      dN[0] = T(0);
+      dN[1] = T(4) * L2 - T(1);
+    } else if (a == 3) {
+      Na = T(4) * L0 * L1;
+      dN[0] = T(4) * (L0 - L1);
+      dN[1] = -T(4) * L1;
+    } else if (a == 4) {
+      Na = T(4) * L1 * L2;
+      dN[0] = T(4) * L2;
+      dN[1] = T(4) * L1;
+    } else {
+      Na = T(4) * L2 * L0;
+      dN[0] = -T(4) * L2;
+      dN[1] = T(4) * (L0 - L2);
+    }
   } else if constexpr (ET == AGX_LINE3) {
     // end nodes -1, +1, then the middle node: indices 0 2 1
     T l, dl;
@@ -197,11 +259,12 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
                const T* __restrict__ elem_field, const double* __restrict__ node_field,
                const uint8_t* __restrict__ dmask_node, ModelParams mp, double* __restrict__ R,
                T* __restrict__ vals, int64_t nnzb, const double* __restrict__ geo, double* __restrict__ geo_out,
-               int ng) {
+               int ng, const QuadTable qt) {
   using ET_ = ElemTraits<ET>;
   constexpr int RDIM = ET_::RDIM, NEN = ET_::NEN, GROUP = ET_::GROUP;
-  const int NQ = RDIM == 1 ? ng : (RDIM == 2 ? ng * ng : ng * ng * ng);  // Gauss points per element
-  constexpr int SDIM = (ET == AGX_HEX8) ? 3 : 2;
+  // integration points per element: the simplex set's table, or the ng-point Gauss rule per direction
+  const int NQ = is_simplex<ET>() ? qt.n : (RDIM == 1 ? ng : (RDIM == 2 ? ng * ng : ng * ng * ng));
+  constexpr int SDIM = space_dim<ET>();
   using MT = ModelTraits<MODEL, SDIM>;
   constexpr int NDOF = MT::NDOF, SLOTS = MT::SLOTS;
 
@@ -258,7 +321,11 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
       // and the shape function and reference derivatives of node a
       T xi[RDIM];
       T wq = 1;
-      {
+      if constexpr (is_simplex<ET>()) {
+#pragma unroll
+        for (int d = 0; d < RDIM; ++d) xi[d] = (T)qt.x[q][d];
+        wq = (T)qt.w[q];
+      } else {
         int r = q;
 #pragma unroll
         for (int d = 0; d < RDIM; ++d) {
@@ -764,7 +831,7 @@ __global__ void __launch_bounds__(AGX_BLOCK)
 neo_hooke_residual_qp(int64_t n_elem, const int32_t* __restrict__ conn, const double* __restrict__ dofs,
                       const double* __restrict__ geo, ModelParams mp, double* __restrict__ R) {
   constexpr int NEN = ElemTraits<ET>::NEN, NQ = NEN;
-  constexpr int SDIM = (ET == AGX_HEX8) ? 3 : 2;
+  constexpr int SDIM = space_dim<ET>();
   __shared__ double Psh[AGX_BLOCK / 32][32][SDIM * SDIM];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int l = lane % NEN, gbase = lane - l;
@@ -875,9 +942,15 @@ void launch_element(agx_context* ctx, agx_element_set& s, const double* dofs, do
   for (int i = 0; i < AGX_MAX_PARAMS; ++i) mp.p[i] = s.params[i];
   const int64_t lanes = s.n_elem * ElemTraits<ET>::GROUP;
   const int grid = agx_grid(ctx, lanes, 8);
+  QuadTable qt;
+  qt.n = s.nqp;
+  for (int q = 0; q < AGX_MAX_QPOINTS; ++q) {
+    for (int d = 0; d < 3; ++d) qt.x[q][d] = s.qp[q][d];
+    qt.w[q] = s.qw[q];
+  }
   element_kernel<ET, MODEL, T, DO_R, DO_K><<<grid, AGX_BLOCK, 0, ctx->stream>>>(
       s.n_elem, s.d_conn, s.d_epos, coords_of<T>(ctx), dofs, elem_field_of<T>(s), s.d_node_field, ctx->d_dmask_node,
-      mp, R, vals, ctx->nnzb, geo, geo_out, s.ngauss);
+      mp, R, vals, ctx->nnzb, geo, geo_out, s.ngauss, qt);
   ctx->n_launches += 1;
 }
 
@@ -917,6 +990,15 @@ int dispatch(agx_context* ctx, agx_element_set& s, const double* dofs, double* R
   AGX_CASE(AGX_QUAD9, AGX_MODEL_HEAT_POTENTIAL)
   AGX_CASE(AGX_QUAD9, AGX_MODEL_NEO_HOOKE)
   AGX_CASE(AGX_LINE3, AGX_MODEL_NEUMANN)
+  AGX_CASE(AGX_TRI3, AGX_MODEL_POISSON_SINCOS)
+  AGX_CASE(AGX_TRI3, AGX_MODEL_HEAT_POTENTIAL)
+  AGX_CASE(AGX_TRI3, AGX_MODEL_NEO_HOOKE)
+  AGX_CASE(AGX_TRI6, AGX_MODEL_POISSON_SINCOS)
+  AGX_CASE(AGX_TRI6, AGX_MODEL_HEAT_POTENTIAL)
+  AGX_CASE(AGX_TRI6, AGX_MODEL_NEO_HOOKE)
+  AGX_CASE(AGX_TET4, AGX_MODEL_POISSON_SINCOS)
+  AGX_CASE(AGX_TET4, AGX_MODEL_HEAT_POTENTIAL)
+  AGX_CASE(AGX_TET4, AGX_MODEL_NEO_HOOKE)
 #undef AGX_CASE
   return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "element type %d with model %d is not supported", s.elem_type, s.model);
 }
@@ -924,6 +1006,8 @@ int dispatch(agx_context* ctx, agx_element_set& s, const double* dofs, double* R
 // one-time float64 geometry pass of a domain set: fills s.d_geo
 int build_geometry(agx_context* ctx, agx_element_set& s) {
   if (s.elem_type == AGX_LINE2 || s.elem_type == AGX_LINE3 || s.d_geo) return AGX_OK;
+  // simplices keep no cache: their Jacobian is one affine map per element, recomputed
+  if (s.elem_type == AGX_TRI3 || s.elem_type == AGX_TRI6 || s.elem_type == AGX_TET4) return AGX_OK;
   const int sd = s.elem_type == AGX_HEX8 ? 3 : 2;
   const int nq = sd == 3 ? s.ngauss * s.ngauss * s.ngauss : s.ngauss * s.ngauss;
   const size_t bytes = sizeof(double) * (size_t)s.n_elem * nq * s.nen * (sd + 1);
@@ -989,6 +1073,9 @@ static void launch_grid_tangent(agx_context* ctx, agx_element_set& s, T* vals, T
 
 int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, int tangent_dtype) {
   const int bs = ctx->ndof * ctx->ndof;
+  for (auto& s : ctx->sets)
+    if ((s.elem_type == AGX_TRI3 || s.elem_type == AGX_TRI6 || s.elem_type == AGX_TET4) && s.nqp < 1)
+      return agx_fail(ctx, AGX_ERR_STATE, "simplex set without integration points (agx_set_quadrature_points)");
   agx_element_set* gset = tangent_dtype >= 0 ? grid_tangent_set(ctx) : nullptr;
   if (residual || tangent_dtype == AGX_F64)
     for (auto& s : ctx->sets)

@@ -106,7 +106,7 @@ def neumann_weak(neumann_fun):
 class ModelDescriptor:
     """What ``static_settings['model'][set]`` holds for the gb300 backend."""
 
-    def __init__(self, mode, kernel, integrand=None, weak=None, field_key=None, dim=None, ngauss=2):
+    def __init__(self, mode, kernel, integrand=None, weak=None, field_key=None, dim=None, ngauss=2, rule=None):
         self.mode = mode            # 'user potential' | 'user element' | 'user residual'
         self.kernel = kernel        # AGX_MODEL_*
         self.integrand = integrand
@@ -114,6 +114,8 @@ class ModelDescriptor:
         self.field_key = field_key
         self.dim = dim
         self.ngauss = ngauss        # Gauss-Legendre points per reference direction
+        # simplex spaces: the integration points and weights as given to the builder
+        self.qpoints, self.qweights = rule if rule is not None else (None, None)
 
     def resolve(self, settings, coords, conn):
         """(model id, params, per-element field or None, per-node field or None)."""
@@ -183,8 +185,21 @@ def _check_rule(ref_int_coor, ref_int_weights, dim):
 
 
 def _check_space(fun):
-    if fun is not spaces.fem_iso_line_quad_brick:
-        raise NotImplementedError("the gb300 backend implements spaces.fem_iso_line_quad_brick (Q1) only")
+    if fun is not spaces.fem_iso_line_quad_brick and fun is not spaces.fem_iso_line_tri_tet:
+        raise NotImplementedError("the gb300 backend implements spaces.fem_iso_line_quad_brick (Q1 and Q2 quads, "
+                                  "Q1 bricks) and spaces.fem_iso_line_tri_tet (P1/P2 triangles, P1 tetrahedra)")
+
+
+def _quadrature(space, ref_int_coor, ref_int_weights, dim):
+    """(ngauss, rule): a tensor Gauss-Legendre rule for fem_iso_line_quad_brick, or any table
+    of at most 16 points (as seeder.int_pts_ref_tri / int_pts_ref_tet give) for the simplices."""
+    if space is spaces.fem_iso_line_tri_tet:
+        pts = np.asarray(ref_int_coor, dtype=np.float64).reshape(-1, dim)
+        w = np.asarray(ref_int_weights, dtype=np.float64).reshape(-1)
+        if pts.shape[0] != w.shape[0] or not 1 <= pts.shape[0] <= 16:
+            raise NotImplementedError("simplex rules of 1 to 16 points with one weight each are supported")
+        return 2, (pts, w)
+    return _check_rule(ref_int_coor, ref_int_weights, dim), None
 
 
 def mixed_reference_domain_potential(integrand_fun, ansatz_fun, ref_int_coor, ref_int_weights, mapping_key):
@@ -194,12 +209,13 @@ def mixed_reference_domain_potential(integrand_fun, ansatz_fun, ref_int_coor, re
                                   "(poisson_sincos_integrand, heat_conduction_integrand)")
     if len(ansatz_fun) != 1 or mapping_key not in ansatz_fun:
         raise NotImplementedError("one field, mapped by its own space, is supported")
-    _check_space(next(iter(ansatz_fun.values())))
+    space = next(iter(ansatz_fun.values()))
+    _check_space(space)
     dim = np.asarray(ref_int_coor).shape[1]
-    ng = _check_rule(ref_int_coor, ref_int_weights, dim)
+    ng, rule = _quadrature(space, ref_int_coor, ref_int_weights, dim)
     kernel = N.AGX_MODEL_POISSON_SINCOS if integrand_fun.kind == "poisson_sincos" else N.AGX_MODEL_HEAT_POTENTIAL
     return ModelDescriptor("user potential", kernel, integrand=integrand_fun, field_key=mapping_key, dim=dim,
-                           ngauss=ng)
+                           ngauss=ng, rule=rule)
 
 
 def mixed_reference_domain_residual(integrand_fun, ansatz_fun, ref_int_coor, ref_int_weights, mapping_key):
@@ -208,7 +224,8 @@ def mixed_reference_domain_residual(integrand_fun, ansatz_fun, ref_int_coor, ref
         raise NotImplementedError("the gb300 backend needs heat_backward_euler_integrand(...) here")
     if len(ansatz_fun) != 1 or mapping_key not in ansatz_fun:
         raise NotImplementedError("one field, mapped by its own space, is supported")
-    _check_space(next(iter(ansatz_fun.values())))
+    if next(iter(ansatz_fun.values())) is not spaces.fem_iso_line_quad_brick:
+        raise NotImplementedError("the backward-Euler heat residual is implemented on Q1 quads and bricks")
     dim = np.asarray(ref_int_coor).shape[1]
     ng = _check_rule(ref_int_coor, ref_int_weights, dim)
     return ModelDescriptor("user residual", N.AGX_MODEL_HEAT_BE, integrand=integrand_fun, field_key=mapping_key,
@@ -224,10 +241,11 @@ def isoparametric_domain_element_galerkin(weak_form_fun, ansatz_fun, ref_int_coo
         raise NotImplementedError("only the initial configuration mapping is implemented")
     _check_space(ansatz_fun)
     dim = np.asarray(ref_int_coor).shape[1]
-    ng = _check_rule(ref_int_coor, ref_int_weights, dim)
+    ng, rule = _quadrature(ansatz_fun, ref_int_coor, ref_int_weights, dim)
     if (weak_form_fun.params["mode"] == "plain strain") != (dim == 2):
-        raise NotImplementedError("'plain strain' needs quads, '3d' needs bricks")
-    return ModelDescriptor("user element", N.AGX_MODEL_NEO_HOOKE, weak=weak_form_fun, dim=dim, ngauss=ng)
+        raise NotImplementedError("'plain strain' needs 2-D elements, '3d' 3-D elements")
+    return ModelDescriptor("user element", N.AGX_MODEL_NEO_HOOKE, weak=weak_form_fun, dim=dim, ngauss=ng,
+                           rule=rule)
 
 
 def isoparametric_surface_element_galerkin(weak_form_fun, ansatz_fun, ref_int_coor, ref_int_weights,

@@ -28,3 +28,25 @@ def fem_iso_line_quad_brick(x, xI, fI, settings, overwrite_diff, n_dim):
     if xI.shape[0] != 2 ** n_dim:
         raise NotImplementedError("the gb300 backend implements the Q1 members of this space")
     return np.tensordot(q1_shape_functions(x, n_dim), np.asarray(fI, dtype=np.float64), axes=(0, 0))
+
+
+def simplex_shape_functions(xi, n_dim, n_nodes):
+    """N_a(xi) of the simplex members of fem_iso_line_tri_tet (spaces.py:12193): linear and
+    quadratic triangles (corners, then mid-sides 0-1, 1-2, 2-0) and linear tetrahedra."""
+    xi = np.asarray(xi, dtype=np.float64)
+    if n_dim == 2 and n_nodes == 3:
+        return np.array([1 - xi[0] - xi[1], xi[0], xi[1]])
+    if n_dim == 2 and n_nodes == 6:
+        L = np.array([1 - xi[0] - xi[1], xi[0], xi[1]])
+        return np.array([L[0] * (2 * L[0] - 1), L[1] * (2 * L[1] - 1), L[2] * (2 * L[2] - 1),
+                         4 * L[0] * L[1], 4 * L[1] * L[2], 4 * L[2] * L[0]])
+    if n_dim == 3 and n_nodes == 4:
+        return np.array([1 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2]])
+    raise NotImplementedError("the gb300 backend implements 3- and 6-node triangles and 4-node tetrahedra")
+
+
+def fem_iso_line_tri_tet(x, xI, fI, settings, overwrite_diff, n_dim):
+    """Simplex interpolation sum_a N_a(x) fI[a] at the reference point ``x`` (host only); the
+    kernels implement the 3- and 6-node triangles and the 4-node tetrahedron."""
+    N = simplex_shape_functions(x, n_dim, np.asarray(xI).shape[0])
+    return np.tensordot(N, np.asarray(fI, dtype=np.float64), axes=(0, 0))

@@ -51,6 +51,12 @@ extern "C" {
 #define AGX_LINE2 2
 #define AGX_QUAD9 3 /* 9-node quadratic quad: corners, mid-sides (bottom, right, top, left), centre */
 #define AGX_LINE3 4 /* 3-node quadratic line: end nodes, then the middle node */
+/* simplices of fem_iso_line_tri_tet (spaces.py:12193, node orders of its n_dim 2 / 3 cases):
+   reference triangle (0,0) (1,0) (0,1) and tetrahedron (0,0,0) (1,0,0) (0,1,0) (0,0,1) */
+#define AGX_TRI3 5  /* linear triangle: N = 1 - xi - eta, xi, eta */
+#define AGX_TRI6 6  /* quadratic triangle: corners, then mid-sides (0-1), (1-2), (2-0) */
+#define AGX_TET4 7  /* linear tetrahedron: N = 1 - xi - eta - zeta, xi, eta, zeta */
+#define AGX_MAX_QPOINTS 16
 
 /* built-in models (descriptors of the closures AutoPDEx builds in models.py) */
 #define AGX_MODEL_POISSON_SINCOS 0 /* 'user potential' 1/2|grad u|^2 - b(x) u,
@@ -147,6 +153,11 @@ int agx_set_model(agx_context* ctx, int set_id, int model, const double* params,
    seeder.gauss_legendre_nd(dim, order) gives for order 2-3 and 4-5 (seeder.py:303-386,
    :1046-1062), which the model closures integrate with (models.py:1188-1269, :1616-1718). */
 int agx_set_quadrature(agx_context* ctx, int set_id, int points_per_direction);
+/* The integration points of a simplex set (AGX_TRI3/TRI6/TET4): n_points <= AGX_MAX_QPOINTS
+   reference coordinates (n_points x 2 or x 3, row-major) and weights, as the model builders
+   receive them from seeder.int_pts_ref_tri / int_pts_ref_tet (seeder.py:1813-2290). */
+int agx_set_quadrature_points(agx_context* ctx, int set_id, int n_points, const double* points,
+                              const double* weights);
 int agx_set_element_field(agx_context* ctx, int set_id, const double* field);
 /* per-DOF auxiliary field (DEVICE pointer, kept by reference), e.g. settings['dofs n'] */
 int agx_set_node_field(agx_context* ctx, int set_id, const double* field_dev);

@@ -96,9 +96,10 @@ def heat_potential_integrand(source=1.0):
     return integrand
 
 
-def user_potential_element(integrand, dim, nen, order=2):
-    """Returns fun(fI, xI, elem_params) -> (R_e, K_e) for a scalar field potential."""
-    xq, wq = gauss_legendre_nd(dim, order)
+def user_potential_element(integrand, dim, nen, order=2, rule=None):
+    """Returns fun(fI, xI, elem_params) -> (R_e, K_e) for a scalar field potential; ``rule``
+    (points, weights) replaces the Gauss-Legendre rule (simplex elements)."""
+    xq, wq = rule if rule is not None else gauss_legendre_nd(dim, order)
     xq = _t(xq)
     wq = _t(wq)
 
@@ -131,14 +132,15 @@ def lame(E, nu):
     return E * nu / ((1 + nu) * (1 - 2 * nu)), E / (2 * (1 + nu))
 
 
-def hyperelastic_element(dim, nen, order, mode):
+def hyperelastic_element(dim, nen, order, mode, rule=None):
     """Returns fun(uI, xI, (E, nu)) -> (R_e (nen*dim,), K_e (nen*dim, nen*dim)).
 
     Per Gauss point: P = jacrev(psi)(F), weak form P:dF, R = jacrev(weak, test),
     K = jacfwd(R, trial) (models.py:1674-1711); plane strain embeds the 2x2
-    displacement gradient into a 3x3 F with F33 = 1 (models.py:963-976).
+    displacement gradient into a 3x3 F with F33 = 1 (models.py:963-976).  ``rule``
+    (points, weights) replaces the Gauss-Legendre rule (simplex elements).
     """
-    xq, wq = gauss_legendre_nd(dim, order)
+    xq, wq = rule if rule is not None else gauss_legendre_nd(dim, order)
     xq = _t(xq)
     wq = _t(wq)
 

@@ -103,7 +103,8 @@ def gauss_legendre_nd(dimension, order):
 # :12057-12081).  Written from the Lagrange tensor-product definitions; node order as there.
 # ----------------------------------------------------------------------------------
 def shape_functions(xi, n_dim, n_nodes, xp=np):
-    """N_a(xi) for line (2, 3 nodes), quad (4, 9 nodes) and brick (8 nodes) elements.
+    """N_a(xi) for line (2, 3 nodes), quad (4, 9 nodes), triangle (3, 6 nodes), brick (8 nodes)
+    and tetrahedron (4 nodes) elements.
 
     ``xi`` is a scalar (line) or a vector of length ``n_dim``; ``xp`` is ``numpy`` or
     ``torch`` so that the same definition serves the AD-based element routines.
@@ -123,6 +124,17 @@ def shape_functions(xi, n_dim, n_nodes, xp=np):
             ly = [0.5 * y * (y - 1), 1 - y * y, 0.5 * y * (y + 1)]
             order = [(0, 0), (2, 0), (2, 2), (0, 2), (1, 0), (2, 1), (1, 2), (0, 1), (1, 1)]
             return stack([lx[i] * ly[j] for i, j in order])
+    if n_dim == 2 and n_nodes == 3:  # fem_iso_line_tri_tet, n_dim 2, 3 nodes (spaces.py:13748-13752)
+        return stack([1 - xi[0] - xi[1], xi[0], xi[1]])
+    if n_dim == 2 and n_nodes == 6:  # the 6-node case (spaces.py:13753-13757), expanded as written there
+        x, y = xi[0], xi[1]
+        x0 = 4 * x
+        x1 = x0 * y
+        x2 = -x - y + 1
+        return stack([x1 + 2 * x ** 2 - 3 * x + 2 * y ** 2 - 3 * y + 1, x * (2 * x - 1), y * (2 * y - 1),
+                      x0 * x2, x1, 4 * x2 * y])
+    if n_dim == 3 and n_nodes == 4:  # n_dim 3, 4 nodes (spaces.py:14625-14630)
+        return stack([1 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2]])
     if n_dim == 3 and n_nodes == 8:
         x, y, z = xi[0], xi[1], xi[2]
         sgn = [(-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1),

@@ -1,0 +1,83 @@
+"""Simplex elements on the host: the oracle's triangle and tetrahedron routines against
+closed-form stiffness matrices, the simplex rules of seeder against exact monomial integrals,
+and the set-up's element-type mapping.  No GPU."""
+from math import factorial
+
+import numpy as np
+import pytest
+import torch
+
+from autopdex_gb300 import _problem, models, seeder, spaces
+from autopdex_gb300 import _native as N
+from oracle import elements as el
+
+
+def _stiffness(dim, nen, rule, xI):
+    fun = el.user_potential_element(el.heat_potential_integrand(0.0), dim, nen, rule=rule)
+    R, K = fun(torch.zeros(nen, dtype=torch.float64), torch.as_tensor(xI, dtype=torch.float64),
+               torch.tensor([1.0], dtype=torch.float64))
+    return K.numpy()
+
+
+def test_p1_triangle_and_tetrahedron_stiffness():
+    """grad N_a . grad N_b times the volume on the reference simplices (counter-clockwise,
+    det J = 1): 1/2 [[2,-1,-1],[-1,1,0],[-1,0,1]] and 1/6 [[3,-1,-1,-1],[-1,1,0,0],...]."""
+    K = _stiffness(2, 3, seeder.int_pts_ref_tri(1), [[0., 0.], [1., 0.], [0., 1.]])
+    assert np.allclose(K, 0.5 * np.array([[2, -1, -1], [-1, 1, 0], [-1, 0, 1]]), rtol=0, atol=1e-15)
+    K = _stiffness(3, 4, seeder.int_pts_ref_tet(1), [[0., 0., 0.], [1., 0., 0.], [0., 1., 0.], [0., 0., 1.]])
+    G = np.array([[-1., -1., -1.], [1., 0., 0.], [0., 1., 0.], [0., 0., 1.]])
+    assert np.allclose(K, G @ G.T / 6.0, rtol=0, atol=1e-15)
+
+
+def test_p2_triangle_stiffness_exact():
+    """The 6-node triangle with the degree-2 rule (exact for its quadratic integrand) against
+    the closed-form matrix, and against a scaled copy of the element (K is scale-free in 2-D)."""
+    sp = pytest.importorskip("sympy")
+    x, y = sp.symbols("x y")
+    L = [1 - x - y, x, y]
+    Nf = [L[0] * (2 * L[0] - 1), L[1] * (2 * L[1] - 1), L[2] * (2 * L[2] - 1), 4 * L[0] * L[1], 4 * L[1] * L[2],
+          4 * L[2] * L[0]]
+    G = [[sp.diff(n, x), sp.diff(n, y)] for n in Nf]
+    exact = np.array([[float(sp.integrate(sp.integrate(G[a][0] * G[b][0] + G[a][1] * G[b][1], (y, 0, 1 - x)),
+                                          (x, 0, 1))) for b in range(6)] for a in range(6)])
+    xI = [[0., 0.], [1., 0.], [0., 1.], [0.5, 0.], [0.5, 0.5], [0., 0.5]]
+    K = _stiffness(2, 6, seeder.int_pts_ref_tri(2), xI)
+    assert np.allclose(K, exact, rtol=0, atol=1e-14)
+    K3 = _stiffness(2, 6, seeder.int_pts_ref_tri(2), 3.0 * np.asarray(xI))
+    assert np.allclose(K3, exact, rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_triangle_rules_exact(order):
+    p, w = seeder.int_pts_ref_tri(order)
+    assert abs(w.sum() - 0.5) < 1e-15
+    for a in range(order + 1):
+        for b in range(order + 1 - a):
+            exact = factorial(a) * factorial(b) / factorial(a + b + 2)
+            assert abs(np.sum(w * p[:, 0] ** a * p[:, 1] ** b) - exact) < 1e-14, (a, b)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_tetrahedron_rules_exact(order):
+    p, w = seeder.int_pts_ref_tet(order)
+    for a in range(order + 1):
+        for b in range(order + 1 - a):
+            for c in range(order + 1 - a - b):
+                exact = factorial(a) * factorial(b) * factorial(c) / factorial(a + b + c + 3)
+                assert abs(np.sum(w * p[:, 0] ** a * p[:, 1] ** b * p[:, 2] ** c) - exact) < 1e-15
+
+
+def test_simplex_set_up():
+    assert _problem._elem_type(3, 2) == N.AGX_TRI3 and _problem._elem_type(3, 2, surface=True) == N.AGX_LINE3
+    assert _problem._elem_type(6, 2) == N.AGX_TRI6 and _problem._elem_type(4, 3) == N.AGX_TET4
+    assert _problem._elem_type(4, 2) == N.AGX_QUAD4
+    with pytest.raises(NotImplementedError):
+        _problem._elem_type(10, 3)
+    d = models.mixed_reference_domain_potential(models.poisson_sincos_integrand(), {"phi": spaces.fem_iso_line_tri_tet},
+                                                *seeder.int_pts_ref_tri(2), "phi")
+    assert d.qpoints.shape == (3, 2) and np.isclose(d.qweights.sum(), 0.5)
+    weak = models.hyperelastic_steady_state_weak(models.neo_hooke, 1.0, 0.3, "3d")
+    d = models.isoparametric_domain_element_galerkin(weak, spaces.fem_iso_line_tri_tet, *seeder.int_pts_ref_tet(2))
+    assert d.qpoints.shape == (4, 3)
+    assert np.allclose(spaces.fem_iso_line_tri_tet([0.2, 0.3], np.zeros((6, 2)), np.arange(6.0), {}, False, 2),
+                       spaces.simplex_shape_functions([0.2, 0.3], 2, 6) @ np.arange(6.0))
