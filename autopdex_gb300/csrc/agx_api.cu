@@ -96,7 +96,8 @@ void free_device(agx_context* ctx) {
 bool model_ok(int elem_type, int model, int dim, int ndof, int n_params, std::string& why) {
   const int sdim = dim;
   const bool domain = elem_type == AGX_QUAD4 || elem_type == AGX_HEX8 || elem_type == AGX_QUAD9 ||
-                      elem_type == AGX_TRI3 || elem_type == AGX_TRI6 || elem_type == AGX_TET4;
+                      elem_type == AGX_TRI3 || elem_type == AGX_TRI6 || elem_type == AGX_TET4 ||
+                      elem_type == AGX_TET10;
   switch (model) {
     case AGX_MODEL_POISSON_SINCOS:
       if (ndof != 1) return why = "POISSON_SINCOS needs 1 DOF per node", false;
@@ -110,7 +111,7 @@ bool model_ok(int elem_type, int model, int dim, int ndof, int n_params, std::st
       if (ndof != sdim) return why = "NEO_HOOKE needs dim DOFs per node", false;
       if (n_params < 2) return why = "NEO_HOOKE needs params E, nu", false;
       if (domain) return true;
-      return why = "NEO_HOOKE needs a domain element (quad4/quad9/tri3/tri6 in 2-D, hex8/tet4 in 3-D)", false;
+      return why = "NEO_HOOKE needs a domain element (quad4/quad9/tri3/tri6 in 2-D, hex8/tet4/tet10 in 3-D)", false;
     case AGX_MODEL_NEUMANN:
       if ((elem_type != AGX_LINE2 && elem_type != AGX_LINE3) || dim != 2)
         return why = "NEUMANN supports 2- and 3-node lines in 2-D", false;
@@ -188,10 +189,11 @@ int agx_add_element_set(agx_context* ctx, int elem_type, int64_t n_elem, int nen
                    : elem_type == AGX_TRI3  ? 3
                    : elem_type == AGX_TRI6  ? 6
                    : elem_type == AGX_TET4  ? 4
+                   : elem_type == AGX_TET10 ? 10
                                             : -1;
   if (want < 0 || nen != want) return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "element type %d with %d nodes", elem_type, nen);
-  if ((elem_type == AGX_HEX8 || elem_type == AGX_TET4) != (ctx->dim == 3))
-    return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "hex8 and tet4 need 3-D nodes, quads, triangles and lines 2-D nodes");
+  if ((elem_type == AGX_HEX8 || elem_type == AGX_TET4 || elem_type == AGX_TET10) != (ctx->dim == 3))
+    return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "bricks and tetrahedra need 3-D nodes, quads, triangles and lines 2-D nodes");
   agx_element_set s;
   s.elem_type = elem_type;
   s.nen = nen;
@@ -302,8 +304,8 @@ int agx_set_quadrature_points(agx_context* ctx, int set_id, int n_points, const 
                               const double* weights) {
   if (!ctx || set_id < 0 || set_id >= (int)ctx->sets.size()) return agx_fail(ctx, AGX_ERR_ARG, "bad set id");
   auto& s = ctx->sets[set_id];
-  const int rdim = s.elem_type == AGX_TET4 ? 3 : 2;
-  if (s.elem_type != AGX_TRI3 && s.elem_type != AGX_TRI6 && s.elem_type != AGX_TET4)
+  const int rdim = (s.elem_type == AGX_TET4 || s.elem_type == AGX_TET10) ? 3 : 2;
+  if (s.elem_type != AGX_TRI3 && s.elem_type != AGX_TRI6 && s.elem_type != AGX_TET4 && s.elem_type != AGX_TET10)
     return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "integration point tables are for simplex sets");
   if (!points || !weights || n_points < 1 || n_points > AGX_MAX_QPOINTS)
     return agx_fail(ctx, AGX_ERR_ARG, "1 to %d integration points", AGX_MAX_QPOINTS);

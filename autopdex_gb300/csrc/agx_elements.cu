@@ -66,10 +66,16 @@ template <>
 struct ElemTraits<AGX_TET4> {
   static constexpr int RDIM = 3, NEN = 4, GROUP = 4;
 };
+template <>
+struct ElemTraits<AGX_TET10> {
+  static constexpr int RDIM = 3, NEN = 10, GROUP = 16;
+};
 template <int ET>
-__host__ __device__ constexpr bool is_simplex() { return ET == AGX_TRI3 || ET == AGX_TRI6 || ET == AGX_TET4; }
+__host__ __device__ constexpr bool is_simplex() {
+  return ET == AGX_TRI3 || ET == AGX_TRI6 || ET == AGX_TET4 || ET == AGX_TET10;
+}
 template <int ET>
-__host__ __device__ constexpr int space_dim() { return (ET == AGX_HEX8 || ET == AGX_TET4) ? 3 : 2; }
+__host__ __device__ constexpr int space_dim() { return (ET == AGX_HEX8 || ET == AGX_TET4 || ET == AGX_TET10) ? 3 : 2; }
 
 // integration points of a simplex set (reference coordinates and weights), passed by value
 struct QuadTable {
@@ -148,6 +154,25 @@ __device__ __forceinline__ void shape(int a, const T* xi, T& Na, T* dN) {
     Na = a == 0 ? T(1) - xi[0] - xi[1] - xi[2] : (a == 1 ? xi[0] : (a == 2 ? xi[1] : xi[2]));
 #pragma unroll
     for (int d = 0; d < 3; ++d) dN[d] = a == 0 ? T(-1) : (a == d + 1 ? T(1) : T(0));
+  } else if constexpr (ET == AGX_TET10) {
+    // the 10-node case in barycentric form, L0 = 1 - xi - eta - zeta, L1..3 = xi, eta, zeta:
+    // corners L_k (2 L_k - 1), edges 4 L_i L_j for (i, j) = (0,1) (1,2) (0,2) (0,3) (1,3) (2,3)
+    auto L = [&](int k) { return k == 0 ? T(1) - xi[0] - xi[1] - xi[2] : (k == 1 ? xi[0] : (k == 2 ? xi[1] : xi[2])); };
+    auto dL = [](int k, int d) { return k == 0 ? T(-1) : (k == d + 1 ? T(1) : T(0)); };  // dL_k / dxi_d
+    if (a < 4) {
+      const T l = L(a);
+      Na = l * (T(2) * l - T(1));
+#pragma unroll
+      for (int d = 0; d < 3; ++d) dN[d] = (T(4) * l - T(1)) * dL(a, d);
+    } else {
+      constexpr unsigned EI = 0u | 1u << 4 | 0u << 8 | 0u << 12 | 1u << 16 | 2u << 20;
+      constexpr unsigned EJ = 1u | 2u << 4 | 2u << 8 | 3u << 12 | 3u << 16 | 3u << 20;
+      const int i = (int)((EI >> (4 * (a - 4))) & 15u), j = (int)((EJ >> (4 * (a - 4))) & 15u);
+      const T li = L(i), lj = L(j);
+      Na = T(4) * li * lj;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) dN[d] = T(4) * (li * dL(j, d) + lj * dL(i, d));
+    }
   } else if constexpr (ET == AGX_TRI6) {
     // the 6-node case, in barycentric form with L0 = 1 - xi - eta, L1 = xi, L2 = eta:
     // corners L_i (2 L_i - 1), mid-sides 4 L0 L1, 4 L1 L2, 4 L2 L0
@@ -999,6 +1024,9 @@ int dispatch(agx_context* ctx, agx_element_set& s, const double* dofs, double* R
   AGX_CASE(AGX_TET4, AGX_MODEL_POISSON_SINCOS)
   AGX_CASE(AGX_TET4, AGX_MODEL_HEAT_POTENTIAL)
   AGX_CASE(AGX_TET4, AGX_MODEL_NEO_HOOKE)
+  AGX_CASE(AGX_TET10, AGX_MODEL_POISSON_SINCOS)
+  AGX_CASE(AGX_TET10, AGX_MODEL_HEAT_POTENTIAL)
+  AGX_CASE(AGX_TET10, AGX_MODEL_NEO_HOOKE)
 #undef AGX_CASE
   return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "element type %d with model %d is not supported", s.elem_type, s.model);
 }
@@ -1007,7 +1035,8 @@ int dispatch(agx_context* ctx, agx_element_set& s, const double* dofs, double* R
 int build_geometry(agx_context* ctx, agx_element_set& s) {
   if (s.elem_type == AGX_LINE2 || s.elem_type == AGX_LINE3 || s.d_geo) return AGX_OK;
   // simplices keep no cache: their Jacobian is one affine map per element, recomputed
-  if (s.elem_type == AGX_TRI3 || s.elem_type == AGX_TRI6 || s.elem_type == AGX_TET4) return AGX_OK;
+  if (s.elem_type == AGX_TRI3 || s.elem_type == AGX_TRI6 || s.elem_type == AGX_TET4 || s.elem_type == AGX_TET10)
+    return AGX_OK;
   const int sd = s.elem_type == AGX_HEX8 ? 3 : 2;
   const int nq = sd == 3 ? s.ngauss * s.ngauss * s.ngauss : s.ngauss * s.ngauss;
   const size_t bytes = sizeof(double) * (size_t)s.n_elem * nq * s.nen * (sd + 1);
@@ -1074,7 +1103,8 @@ static void launch_grid_tangent(agx_context* ctx, agx_element_set& s, T* vals, T
 int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, int tangent_dtype) {
   const int bs = ctx->ndof * ctx->ndof;
   for (auto& s : ctx->sets)
-    if ((s.elem_type == AGX_TRI3 || s.elem_type == AGX_TRI6 || s.elem_type == AGX_TET4) && s.nqp < 1)
+    if ((s.elem_type == AGX_TRI3 || s.elem_type == AGX_TRI6 || s.elem_type == AGX_TET4 || s.elem_type == AGX_TET10) &&
+        s.nqp < 1)
       return agx_fail(ctx, AGX_ERR_STATE, "simplex set without integration points (agx_set_quadrature_points)");
   agx_element_set* gset = tangent_dtype >= 0 ? grid_tangent_set(ctx) : nullptr;
   if (residual || tangent_dtype == AGX_F64)

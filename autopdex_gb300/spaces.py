@@ -32,7 +32,8 @@ def fem_iso_line_quad_brick(x, xI, fI, settings, overwrite_diff, n_dim):
 
 def simplex_shape_functions(xi, n_dim, n_nodes):
     """N_a(xi) of the simplex members of fem_iso_line_tri_tet (spaces.py:12193): linear and
-    quadratic triangles (corners, then mid-sides 0-1, 1-2, 2-0) and linear tetrahedra."""
+    quadratic triangles (corners, then mid-sides 0-1, 1-2, 2-0) and tetrahedra (corners, then
+    edges 0-1, 1-2, 0-2, 0-3, 1-3, 2-3)."""
     xi = np.asarray(xi, dtype=np.float64)
     if n_dim == 2 and n_nodes == 3:
         return np.array([1 - xi[0] - xi[1], xi[0], xi[1]])
@@ -42,11 +43,15 @@ def simplex_shape_functions(xi, n_dim, n_nodes):
                          4 * L[0] * L[1], 4 * L[1] * L[2], 4 * L[2] * L[0]])
     if n_dim == 3 and n_nodes == 4:
         return np.array([1 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2]])
-    raise NotImplementedError("the gb300 backend implements 3- and 6-node triangles and 4-node tetrahedra")
+    if n_dim == 3 and n_nodes == 10:  # corners, then edges 0-1, 1-2, 0-2, 0-3, 1-3, 2-3
+        L = np.array([1 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2]])
+        edges = [(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)]
+        return np.concatenate([L * (2 * L - 1), [4 * L[i] * L[j] for i, j in edges]])
+    raise NotImplementedError("the gb300 backend implements 3- and 6-node triangles and 4- and 10-node tetrahedra")
 
 
 def fem_iso_line_tri_tet(x, xI, fI, settings, overwrite_diff, n_dim):
     """Simplex interpolation sum_a N_a(x) fI[a] at the reference point ``x`` (host only); the
-    kernels implement the 3- and 6-node triangles and the 4-node tetrahedron."""
+    kernels implement the 3- and 6-node triangles and the 4- and 10-node tetrahedra."""
     N = simplex_shape_functions(x, n_dim, np.asarray(xI).shape[0])
     return np.tensordot(N, np.asarray(fI, dtype=np.float64), axes=(0, 0))

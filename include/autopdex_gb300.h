@@ -56,6 +56,7 @@ extern "C" {
 #define AGX_TRI3 5  /* linear triangle: N = 1 - xi - eta, xi, eta */
 #define AGX_TRI6 6  /* quadratic triangle: corners, then mid-sides (0-1), (1-2), (2-0) */
 #define AGX_TET4 7  /* linear tetrahedron: N = 1 - xi - eta - zeta, xi, eta, zeta */
+#define AGX_TET10 8 /* quadratic tetrahedron: corners, then edges 0-1, 1-2, 0-2, 0-3, 1-3, 2-3 */
 #define AGX_MAX_QPOINTS 16
 
 /* built-in models (descriptors of the closures AutoPDEx builds in models.py) */

@@ -104,7 +104,7 @@ def gauss_legendre_nd(dimension, order):
 # ----------------------------------------------------------------------------------
 def shape_functions(xi, n_dim, n_nodes, xp=np):
     """N_a(xi) for line (2, 3 nodes), quad (4, 9 nodes), triangle (3, 6 nodes), brick (8 nodes)
-    and tetrahedron (4 nodes) elements.
+    and tetrahedron (4, 10 nodes) elements.
 
     ``xi`` is a scalar (line) or a vector of length ``n_dim``; ``xp`` is ``numpy`` or
     ``torch`` so that the same definition serves the AD-based element routines.
@@ -135,6 +135,16 @@ def shape_functions(xi, n_dim, n_nodes, xp=np):
                       x0 * x2, x1, 4 * x2 * y])
     if n_dim == 3 and n_nodes == 4:  # n_dim 3, 4 nodes (spaces.py:14625-14630)
         return stack([1 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2]])
+    if n_dim == 3 and n_nodes == 10:  # the 10-node case (spaces.py:14632-14640), expanded as written there
+        x, y, z = xi[0], xi[1], xi[2]
+        x0 = 4 * x
+        x1 = x0 * y
+        x2 = x0 * z
+        x3 = 4 * y
+        x4 = x3 * z
+        x5 = -x - y - z + 1
+        return stack([x1 + x2 + x4 + 2 * x ** 2 - 3 * x + 2 * y ** 2 - 3 * y + 2 * z ** 2 - 3 * z + 1,
+                      x * (2 * x - 1), y * (2 * y - 1), z * (2 * z - 1), x0 * x5, x1, x3 * x5, 4 * x5 * z, x2, x4])
     if n_dim == 3 and n_nodes == 8:
         x, y, z = xi[0], xi[1], xi[2]
         sgn = [(-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1),

@@ -1,9 +1,9 @@
 """Simplex elements on the GPU against the oracle (fem_iso_line_tri_tet, spaces.py:12193):
-linear and quadratic triangles and linear tetrahedra for the Poisson potential and neo-Hooke,
+linear and quadratic triangles and tetrahedra for the Poisson potential and neo-Hooke,
 float64 residuals and tangents to 1e-12 and float32 tangents to 5e-6 of the oracle's at
 random DOFs (float32 rounding: 2.5e-6 measured for neo-Hooke on 6-node triangles), and a
 Newton solve on linear triangles to the oracle's solution.  Meshes: the
-structured quads / bricks split into 2 triangles / 6 tetrahedra, quadratic triangles with a
+structured quads / bricks split into 2 triangles / 6 tetrahedra, quadratic elements with a
 node added on every edge."""
 import numpy as np
 import pytest
@@ -31,15 +31,29 @@ def _tri_mesh(n, quadratic=False):
     return np.array(pts), t6
 
 
-def _tet_mesh(n):
+def _tet_mesh(n, quadratic=False):
     coords, hexes = mesher.structured_mesh((n, n, n), [[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0],
                                                        [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], "brick")
     kuhn = [[0, 1, 2, 6], [0, 2, 3, 6], [0, 3, 7, 6], [0, 7, 4, 6], [0, 4, 5, 6], [0, 5, 1, 6]]
-    return coords, np.concatenate([hexes[:, k] for k in kuhn])
+    tets = np.concatenate([hexes[:, k] for k in kuhn])
+    if not quadratic:
+        return coords, tets
+    pts = [c for c in coords]
+    mid = {}
+
+    def node(a, b):
+        k = (min(a, b), max(a, b))
+        if k not in mid:
+            mid[k] = len(pts)
+            pts.append(0.5 * (coords[a] + coords[b]))
+        return mid[k]
+    edges = [(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)]  # the 10-node order
+    t10 = np.array([list(t) + [node(t[i], t[j]) for i, j in edges] for t in tets])
+    return np.array(pts), t10
 
 
 CASES = {  # name: (dim, nodes per element, rule order)
-    "tri3": (2, 3, 1), "tri6": (2, 6, 2), "tet4": (3, 4, 2),
+    "tri3": (2, 3, 1), "tri6": (2, 6, 2), "tet4": (3, 4, 2), "tet10": (3, 10, 2),
 }
 
 
@@ -50,7 +64,7 @@ def _problem(case, kind):
         coords, conn = _tri_mesh(6, quadratic=nen == 6)
         rule = seeder.int_pts_ref_tri(order)
     else:
-        coords, conn = _tet_mesh(3)
+        coords, conn = _tet_mesh(3 if nen == 4 else 2, quadratic=nen == 10)
         rule = seeder.int_pts_ref_tet(order)
     n = coords.shape[0]
     on_bnd = np.zeros(n, dtype=bool)

@@ -47,6 +47,23 @@ def test_p2_triangle_stiffness_exact():
     assert np.allclose(K3, exact, rtol=0, atol=1e-13)
 
 
+def test_p2_tetrahedron_stiffness_exact():
+    """The 10-node tetrahedron with the degree-2 rule against the closed-form matrix."""
+    sp = pytest.importorskip("sympy")
+    x, y, z = sp.symbols("x y z")
+    L = [1 - x - y - z, x, y, z]
+    Nf = [l * (2 * l - 1) for l in L] + [4 * L[i] * L[j] for i, j in [(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)]]
+    G = [[sp.diff(n, v) for v in (x, y, z)] for n in Nf]
+
+    def vol(f):
+        return float(sp.integrate(sp.integrate(sp.integrate(f, (z, 0, 1 - x - y)), (y, 0, 1 - x)), (x, 0, 1)))
+    exact = np.array([[vol(sum(G[a][d] * G[b][d] for d in range(3))) for b in range(10)] for a in range(10)])
+    c = np.array([[0., 0., 0.], [1., 0., 0.], [0., 1., 0.], [0., 0., 1.]])
+    mids = [0.5 * (c[i] + c[j]) for i, j in [(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)]]
+    K = _stiffness(3, 10, seeder.int_pts_ref_tet(2), np.vstack([c, mids]))
+    assert np.allclose(K, exact, rtol=0, atol=1e-14)
+
+
 @pytest.mark.parametrize("order", [1, 2, 3, 4])
 def test_triangle_rules_exact(order):
     p, w = seeder.int_pts_ref_tri(order)
@@ -70,9 +87,10 @@ def test_tetrahedron_rules_exact(order):
 def test_simplex_set_up():
     assert _problem._elem_type(3, 2) == N.AGX_TRI3 and _problem._elem_type(3, 2, surface=True) == N.AGX_LINE3
     assert _problem._elem_type(6, 2) == N.AGX_TRI6 and _problem._elem_type(4, 3) == N.AGX_TET4
+    assert _problem._elem_type(10, 3) == N.AGX_TET10
     assert _problem._elem_type(4, 2) == N.AGX_QUAD4
     with pytest.raises(NotImplementedError):
-        _problem._elem_type(10, 3)
+        _problem._elem_type(20, 3)
     d = models.mixed_reference_domain_potential(models.poisson_sincos_integrand(), {"phi": spaces.fem_iso_line_tri_tet},
                                                 *seeder.int_pts_ref_tri(2), "phi")
     assert d.qpoints.shape == (3, 2) and np.isclose(d.qweights.sum(), 0.5)
