@@ -43,7 +43,8 @@ struct agx_element_set {
 };
 
 // Scalars of one Krylov solve, kept in device memory so that iterations need no host
-// round trip.  Written only by the last block of a reduction kernel.
+// round trip.  Written only by one thread: of the last block of a reduction kernel, or of a
+// one-block kernel that sums block partials.
 struct agx_krylov_scalars {
   double rz;         // (r, z) of the current iterate
   double rr;         // (r, r)
