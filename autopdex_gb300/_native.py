@@ -15,7 +15,7 @@ AGX_PRECOND_CAPTURABLE = 1
 AGX_DIVERGED = 2
 
 AGX_QUAD4, AGX_HEX8, AGX_LINE2, AGX_QUAD9, AGX_LINE3 = 0, 1, 2, 3, 4
-AGX_TRI3, AGX_TRI6, AGX_TET4, AGX_TET10 = 5, 6, 7, 8
+AGX_TRI3, AGX_TRI6, AGX_TET4, AGX_TET10, AGX_HEX27 = 5, 6, 7, 8, 9
 AGX_MODEL_POISSON_SINCOS = 0
 AGX_MODEL_HEAT_POTENTIAL = 1
 AGX_MODEL_NEO_HOOKE = 2

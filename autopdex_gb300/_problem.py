@@ -77,11 +77,11 @@ def _elem_type(nen, dim, surface=False):
             return N.AGX_LINE2 if nen == 2 else N.AGX_LINE3
     else:
         table = {(2, 4): N.AGX_QUAD4, (2, 9): N.AGX_QUAD9, (2, 3): N.AGX_TRI3, (2, 6): N.AGX_TRI6,
-                 (3, 8): N.AGX_HEX8, (3, 4): N.AGX_TET4, (3, 10): N.AGX_TET10}
+                 (3, 8): N.AGX_HEX8, (3, 27): N.AGX_HEX27, (3, 4): N.AGX_TET4, (3, 10): N.AGX_TET10}
         if (dim, nen) in table:
             return table[(dim, nen)]
     raise NotImplementedError(f"{'boundary' if surface else 'domain'} elements with {nen} nodes in {dim}-D are not "
-                              "supported by the gb300 backend (Q1/Q2 quads, P1/P2 triangles, Q1 bricks, P1/P2 "
+                              "supported by the gb300 backend (Q1/Q2 quads, P1/P2 triangles, Q1/Q2 bricks, P1/P2 "
                               "tetrahedra, 2- and 3-node boundary lines)")
 
 

@@ -97,7 +97,7 @@ bool model_ok(int elem_type, int model, int dim, int ndof, int n_params, std::st
   const int sdim = dim;
   const bool domain = elem_type == AGX_QUAD4 || elem_type == AGX_HEX8 || elem_type == AGX_QUAD9 ||
                       elem_type == AGX_TRI3 || elem_type == AGX_TRI6 || elem_type == AGX_TET4 ||
-                      elem_type == AGX_TET10;
+                      elem_type == AGX_TET10 || elem_type == AGX_HEX27;
   switch (model) {
     case AGX_MODEL_POISSON_SINCOS:
       if (ndof != 1) return why = "POISSON_SINCOS needs 1 DOF per node", false;
@@ -110,6 +110,7 @@ bool model_ok(int elem_type, int model, int dim, int ndof, int n_params, std::st
     case AGX_MODEL_NEO_HOOKE:
       if (ndof != sdim) return why = "NEO_HOOKE needs dim DOFs per node", false;
       if (n_params < 2) return why = "NEO_HOOKE needs params E, nu", false;
+      if (elem_type == AGX_HEX27) return why = "NEO_HOOKE on 27-node bricks is not implemented", false;
       if (domain) return true;
       return why = "NEO_HOOKE needs a domain element (quad4/quad9/tri3/tri6 in 2-D, hex8/tet4/tet10 in 3-D)", false;
     case AGX_MODEL_NEUMANN:
@@ -190,9 +191,11 @@ int agx_add_element_set(agx_context* ctx, int elem_type, int64_t n_elem, int nen
                    : elem_type == AGX_TRI6  ? 6
                    : elem_type == AGX_TET4  ? 4
                    : elem_type == AGX_TET10 ? 10
+                   : elem_type == AGX_HEX27 ? 27
                                             : -1;
   if (want < 0 || nen != want) return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "element type %d with %d nodes", elem_type, nen);
-  if ((elem_type == AGX_HEX8 || elem_type == AGX_TET4 || elem_type == AGX_TET10) != (ctx->dim == 3))
+  if ((elem_type == AGX_HEX8 || elem_type == AGX_HEX27 || elem_type == AGX_TET4 || elem_type == AGX_TET10) !=
+      (ctx->dim == 3))
     return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "bricks and tetrahedra need 3-D nodes, quads, triangles and lines 2-D nodes");
   agx_element_set s;
   s.elem_type = elem_type;

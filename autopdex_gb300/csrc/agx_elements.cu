@@ -67,6 +67,10 @@ struct ElemTraits<AGX_TET4> {
   static constexpr int RDIM = 3, NEN = 4, GROUP = 4;
 };
 template <>
+struct ElemTraits<AGX_HEX27> {
+  static constexpr int RDIM = 3, NEN = 27, GROUP = 32;
+};
+template <>
 struct ElemTraits<AGX_TET10> {
   static constexpr int RDIM = 3, NEN = 10, GROUP = 16;
 };
@@ -75,7 +79,9 @@ __host__ __device__ constexpr bool is_simplex() {
   return ET == AGX_TRI3 || ET == AGX_TRI6 || ET == AGX_TET4 || ET == AGX_TET10;
 }
 template <int ET>
-__host__ __device__ constexpr int space_dim() { return (ET == AGX_HEX8 || ET == AGX_TET4 || ET == AGX_TET10) ? 3 : 2; }
+__host__ __device__ constexpr int space_dim() {
+  return (ET == AGX_HEX8 || ET == AGX_HEX27 || ET == AGX_TET4 || ET == AGX_TET10) ? 3 : 2;
+}
 
 // integration points of a simplex set (reference coordinates and weights), passed by value
 struct QuadTable {
@@ -154,6 +160,18 @@ __device__ __forceinline__ void shape(int a, const T* xi, T& Na, T* dN) {
     Na = a == 0 ? T(1) - xi[0] - xi[1] - xi[2] : (a == 1 ? xi[0] : (a == 2 ? xi[1] : xi[2]));
 #pragma unroll
     for (int d = 0; d < 3; ++d) dN[d] = a == 0 ? T(-1) : (a == d + 1 ? T(1) : T(0));
+  } else if constexpr (ET == AGX_HEX27) {
+    // tensor products of the 1-D quadratic basis (index 0: -1, 1: 0, 2: +1); two bits per
+    // node and direction in the node order of the 27-node case
+    constexpr unsigned long long IX = 0x15582819192828ull, IY = 0x1585a06464a0a0ull, IZ = 0x185555aa00aa00ull;
+    T lx, dlx, ly, dly, lz, dlz;
+    lagrange2<T>((int)((IX >> (2 * a)) & 3ull), xi[0], lx, dlx);
+    lagrange2<T>((int)((IY >> (2 * a)) & 3ull), xi[1], ly, dly);
+    lagrange2<T>((int)((IZ >> (2 * a)) & 3ull), xi[2], lz, dlz);
+    Na = lx * ly * lz;
+    dN[0] = dlx * ly * lz;
+    dN[1] = lx * dly * lz;
+    dN[2] = lx * ly * dlz;
   } else if constexpr (ET == AGX_TET10) {
     // the 10-node case in barycentric form, L0 = 1 - xi - eta - zeta, L1..3 = xi, eta, zeta:
     // corners L_k (2 L_k - 1), edges 4 L_i L_j for (i, j) = (0,1) (1,2) (0,2) (0,3) (1,3) (2,3)
@@ -1027,6 +1045,8 @@ int dispatch(agx_context* ctx, agx_element_set& s, const double* dofs, double* R
   AGX_CASE(AGX_TET10, AGX_MODEL_POISSON_SINCOS)
   AGX_CASE(AGX_TET10, AGX_MODEL_HEAT_POTENTIAL)
   AGX_CASE(AGX_TET10, AGX_MODEL_NEO_HOOKE)
+  AGX_CASE(AGX_HEX27, AGX_MODEL_POISSON_SINCOS)
+  AGX_CASE(AGX_HEX27, AGX_MODEL_HEAT_POTENTIAL)
 #undef AGX_CASE
   return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "element type %d with model %d is not supported", s.elem_type, s.model);
 }
@@ -1034,8 +1054,9 @@ int dispatch(agx_context* ctx, agx_element_set& s, const double* dofs, double* R
 // one-time float64 geometry pass of a domain set: fills s.d_geo
 int build_geometry(agx_context* ctx, agx_element_set& s) {
   if (s.elem_type == AGX_LINE2 || s.elem_type == AGX_LINE3 || s.d_geo) return AGX_OK;
-  // simplices keep no cache: their Jacobian is one affine map per element, recomputed
-  if (s.elem_type == AGX_TRI3 || s.elem_type == AGX_TRI6 || s.elem_type == AGX_TET4 || s.elem_type == AGX_TET10)
+  // simplices and 27-node bricks keep no cache: their geometry is recomputed per pass
+  if (s.elem_type == AGX_TRI3 || s.elem_type == AGX_TRI6 || s.elem_type == AGX_TET4 || s.elem_type == AGX_TET10 ||
+      s.elem_type == AGX_HEX27)
     return AGX_OK;
   const int sd = s.elem_type == AGX_HEX8 ? 3 : 2;
   const int nq = sd == 3 ? s.ngauss * s.ngauss * s.ngauss : s.ngauss * s.ngauss;

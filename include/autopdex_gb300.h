@@ -57,6 +57,10 @@ extern "C" {
 #define AGX_TRI6 6  /* quadratic triangle: corners, then mid-sides (0-1), (1-2), (2-0) */
 #define AGX_TET4 7  /* linear tetrahedron: N = 1 - xi - eta - zeta, xi, eta, zeta */
 #define AGX_TET10 8 /* quadratic tetrahedron: corners, then edges 0-1, 1-2, 0-2, 0-3, 1-3, 2-3 */
+/* 27-node quadratic brick of fem_iso_line_quad_brick (spaces.py:12083-12154): corners as the
+   8-node brick, mid-edges of the bottom face (x, y, x, y edges from node 0), of the top face,
+   the vertical edges, the face centres x-, x+, y-, y+, z-, z+, the centre; scalar models */
+#define AGX_HEX27 9
 #define AGX_MAX_QPOINTS 16
 
 /* built-in models (descriptors of the closures AutoPDEx builds in models.py) */

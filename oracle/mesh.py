@@ -102,9 +102,19 @@ def gauss_legendre_nd(dimension, order):
 # spaces.fem_iso_line_quad_brick shape functions (autopdex/spaces.py:356-366, :1913-1950,
 # :12057-12081).  Written from the Lagrange tensor-product definitions; node order as there.
 # ----------------------------------------------------------------------------------
+# 27-node brick: per node the 1-D basis index (0: -1, 1: 0, 2: +1) in x, y, z, in the node order
+# of spaces.py:12083-12154 -- corners as the 8-node brick, mid-edges of the bottom face
+# (0-1, 1-2, 2-3, 3-0), of the top face, the vertical edges (0-4, 1-5, 2-6, 3-7), the face
+# centres x-, x+, y-, y+, z-, z+, and the centre
+HEX27_NODES = [(0, 0, 0), (2, 0, 0), (2, 2, 0), (0, 2, 0), (0, 0, 2), (2, 0, 2), (2, 2, 2), (0, 2, 2),
+               (1, 0, 0), (2, 1, 0), (1, 2, 0), (0, 1, 0), (1, 0, 2), (2, 1, 2), (1, 2, 2), (0, 1, 2),
+               (0, 0, 1), (2, 0, 1), (2, 2, 1), (0, 2, 1), (0, 1, 1), (2, 1, 1), (1, 0, 1), (1, 2, 1),
+               (1, 1, 0), (1, 1, 2), (1, 1, 1)]
+
+
 def shape_functions(xi, n_dim, n_nodes, xp=np):
-    """N_a(xi) for line (2, 3 nodes), quad (4, 9 nodes), triangle (3, 6 nodes), brick (8 nodes)
-    and tetrahedron (4, 10 nodes) elements.
+    """N_a(xi) for line (2, 3 nodes), quad (4, 9 nodes), triangle (3, 6 nodes), brick (8, 27
+    nodes) and tetrahedron (4, 10 nodes) elements.
 
     ``xi`` is a scalar (line) or a vector of length ``n_dim``; ``xp`` is ``numpy`` or
     ``torch`` so that the same definition serves the AD-based element routines.
@@ -145,6 +155,12 @@ def shape_functions(xi, n_dim, n_nodes, xp=np):
         x5 = -x - y - z + 1
         return stack([x1 + x2 + x4 + 2 * x ** 2 - 3 * x + 2 * y ** 2 - 3 * y + 2 * z ** 2 - 3 * z + 1,
                       x * (2 * x - 1), y * (2 * y - 1), z * (2 * z - 1), x0 * x5, x1, x3 * x5, 4 * x5 * z, x2, x4])
+    if n_dim == 3 and n_nodes == 27:  # spaces.py:12083-12154: tensor products of the 1-D quadratic basis
+        x, y, z = xi[0], xi[1], xi[2]
+        lx = [0.5 * x * (x - 1), 1 - x * x, 0.5 * x * (x + 1)]
+        ly = [0.5 * y * (y - 1), 1 - y * y, 0.5 * y * (y + 1)]
+        lz = [0.5 * z * (z - 1), 1 - z * z, 0.5 * z * (z + 1)]
+        return stack([lx[i] * ly[j] * lz[k] for i, j, k in HEX27_NODES])
     if n_dim == 3 and n_nodes == 8:
         x, y, z = xi[0], xi[1], xi[2]
         sgn = [(-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1),

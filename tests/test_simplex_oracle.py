@@ -99,3 +99,28 @@ def test_simplex_set_up():
     assert d.qpoints.shape == (4, 3)
     assert np.allclose(spaces.fem_iso_line_tri_tet([0.2, 0.3], np.zeros((6, 2)), np.arange(6.0), {}, False, 2),
                        spaces.simplex_shape_functions([0.2, 0.3], 2, 6) @ np.arange(6.0))
+
+
+def test_q2_brick_oracle():
+    """The 27-node brick: N_a is 1 at its own node and 0 at the others, and the stiffness
+    with the 3-point rule equals the exact integral over the reference cube, assembled from
+    the exact 1-D mass and stiffness matrices of the quadratic basis (the integrand is a
+    sum of products of 1-D factors)."""
+    from numpy.polynomial import polynomial as P
+    from oracle.mesh import HEX27_NODES, shape_functions
+    pos = np.array(HEX27_NODES, dtype=float) - 1.0
+    V = np.array([shape_functions(p, 3, 27) for p in pos])
+    assert np.allclose(V, np.eye(27), rtol=0, atol=1e-15)
+    basis = [np.array([0.0, -0.5, 0.5]), np.array([1.0, 0.0, -1.0]), np.array([0.0, 0.5, 0.5])]  # t(t-1)/2, 1-t^2, t(t+1)/2
+
+    def integral(c):
+        ci = P.polyint(c)
+        return P.polyval(1.0, ci) - P.polyval(-1.0, ci)
+    M = np.array([[integral(P.polymul(bi, bj)) for bj in basis] for bi in basis])
+    S = np.array([[integral(P.polymul(P.polyder(bi), P.polyder(bj))) for bj in basis] for bi in basis])
+    idx = np.array(HEX27_NODES)
+    ix, iy, iz = (idx[:, d] for d in range(3))
+    exact = (S[np.ix_(ix, ix)] * M[np.ix_(iy, iy)] * M[np.ix_(iz, iz)] + M[np.ix_(ix, ix)] * S[np.ix_(iy, iy)] *
+             M[np.ix_(iz, iz)] + M[np.ix_(ix, ix)] * M[np.ix_(iy, iy)] * S[np.ix_(iz, iz)])
+    K = _stiffness(3, 27, seeder.gauss_legendre_nd(3, 4), pos)
+    assert np.allclose(K, exact, rtol=0, atol=1e-13)
