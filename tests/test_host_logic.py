@@ -141,3 +141,16 @@ def test_dlpack_host_arrays_are_read():
     assert _problem.is_foreign(f) and not _problem.is_foreign(np.zeros(2))
     assert np.array_equal(_problem.flatten({"u": f}, "u"), np.arange(6.0))
     assert _problem.dof_layout(f) == (None, 3, 2)
+
+
+def test_q2_host_shape_functions_match_oracle():
+    """The host Q2 interpolation of spaces.fem_iso_line_quad_brick against the oracle's."""
+    from autopdex_gb300 import spaces
+    from oracle import mesh as om
+    rng = np.random.default_rng(2)
+    for dim, nen in ((2, 9), (3, 27)):
+        xi = rng.uniform(-1, 1, dim)
+        assert np.allclose(spaces.q2_shape_functions(xi, dim), om.shape_functions(xi, dim, nen), rtol=0, atol=1e-15)
+        f = rng.standard_normal(nen)
+        v = spaces.fem_iso_line_quad_brick(xi, np.zeros((nen, dim)), f, {}, False, dim)
+        assert np.isclose(v, om.shape_functions(xi, dim, nen) @ f)
