@@ -447,8 +447,9 @@ def other_workloads(cook_n=128, cook_rtol=1e-6, heat3d_n=128, heat3d_steps=2):
 def cpu_baseline(n, newton_iters, cg_iters, budget_s=20.0):
     """CPU oracle on a bounded sample of the workload, scaled to one load step.
 
-    Sample: (a) float64 AD element residual+tangent (oracle.elements, torch.func) on 512
-    elements of the mesh -> cost per element; (b) SciPy Jacobi-CG iterations on the
+    Sample: (a) float64 AD element residual+tangent (oracle.elements, torch.func) on the 4096
+    elements of a 16^3 cube, one full vmap batch of the oracle (smaller batches cost up to 5x
+    more per element) -> cost per element; (b) SciPy Jacobi-CG iterations on the
     assembled 12^3 cube matrix -> cost per CG iteration per stored entry.  Scaled with the
     Newton and CG iteration counts of the float64 GPU path on the full 64^3 problem:
     t = newton_iters * (2 n_e t_elem) + cg_iters * t_iter(nnz_64 / nnz_12)."""
@@ -460,9 +461,9 @@ def cpu_baseline(n, newton_iters, cg_iters, budget_s=20.0):
 
     threads = os.cpu_count() or 1
     torch.set_num_threads(threads)
-    w = configs.neo_hooke_cube(n=8, n_steps=10)
+    w = configs.neo_hooke_cube(n=16, n_steps=10)
     fun = el.hyperelastic_element(3, 8, 2, "3d")
-    conn = w.raw["conns"][0][:512]
+    conn = w.raw["conns"][0][:4096]
     xI = torch.as_tensor(w.raw["coords"][conn])
     uI = torch.zeros((conn.shape[0], 8, 3), dtype=torch.float64) + 1e-3
     p = torch.tensor([[1.0, 0.3]] * conn.shape[0], dtype=torch.float64)
@@ -491,7 +492,7 @@ def cpu_baseline(n, newton_iters, cg_iters, budget_s=20.0):
     n_e = n ** 3
     est = newton_iters * 2 * n_e * t_elem + cg_iters * t_iter
     return {"value": est, "unit": "s", "cores": threads, "kind": "port",
-            "sample": (f"float64 AD element routine on 512 elements ({t_elem * 1e6:.1f} us/element) and "
+            "sample": (f"float64 AD element routine on {conn.shape[0]} elements ({t_elem * 1e6:.1f} us/element) and "
                        f"{iters} SciPy Jacobi-CG iterations on the 12^3 cube ({t_iter16 * 1e3:.2f} ms/iteration, "
                        f"scaled by stored entries to 64^3); combined with the float64 GPU path's "
                        f"{newton_iters} Newton and {cg_iters} CG iterations")}
