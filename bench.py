@@ -283,7 +283,10 @@ def gpu_arm(args):
         except Exception as e:  # noqa: BLE001 -- reported, the headline stands
             line["other_workloads"] = {"error": str(e)[:300]}
     if rank == 0 and not args.no_cpu_baseline and not args.only_mixed:
-        line["cpu_baseline"] = cpu_baseline(n, int(info_t[0]), int(tight_kry), budget_s=args.cpu_budget)
+        try:
+            line["cpu_baseline"] = cpu_baseline(n, int(info_t[0]), int(tight_kry), budget_s=args.cpu_budget)
+        except Exception as e:  # noqa: BLE001 -- reported, the headline stands
+            line["cpu_baseline"] = {"error": str(e)[:300]}
     if dist:
         dist.destroy_process_group()
     if rank == 0:
