@@ -121,21 +121,21 @@ def test_potential_tangents_are_symmetric(kind):
     if kind == "poisson_quad4":
         fun = el.user_potential_element(el.poisson_sincos_integrand(), 2, 4)
         args = (_t(rng.uniform(-1, 1, 4)), _t([[0., 0.], [1., 0.1], [1.2, 1.], [0., 0.8]]),
-                torch.zeros(1, dtype=torch.float64))
+                torch.zeros(1))
     elif kind == "heat_hex8":
         fun = el.user_potential_element(el.heat_potential_integrand(1.0), 3, 8)
         x = np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1], [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]],
                      dtype=float) * 0.5 + rng.uniform(-0.05, 0.05, (8, 3))
-        args = (_t(rng.uniform(-1, 1, 8)), _t(x), _t([2.5], dtype=torch.float64))
+        args = (_t(rng.uniform(-1, 1, 8)), _t(x), _t([2.5]))
     elif kind == "neo_hooke_quad4":
         fun = el.hyperelastic_element(2, 4, 2, "plain strain")
         args = (_t(rng.uniform(-0.05, 0.05, (4, 2))), _t([[0., 0.], [1., 0.1], [1.2, 1.], [0., 0.8]]),
-                _t([100.0, 0.3], dtype=torch.float64))
+                _t([100.0, 0.3]))
     else:
         fun = el.hyperelastic_element(3, 4, 0, "3d", rule=seeder.int_pts_ref_tet(2))
         args = (_t(rng.uniform(-0.05, 0.05, (4, 3))),
                 _t([[0., 0., 0.], [1., 0., 0.], [0., 1., 0.], [0., 0., 1.]]),
-                _t([100.0, 0.3], dtype=torch.float64))
+                _t([100.0, 0.3]))
     R, K = fun(*args)
     K = K.numpy().reshape(R.numel(), R.numel())
     assert np.abs(K - K.T).max() <= 1e-13 * np.abs(K).max()
