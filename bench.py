@@ -222,6 +222,12 @@ def gpu_arm(args):
     n_e = n ** 3
     asm_bytes = n_nodes * 3 * 8 + w.n_dofs * 8 + n_e * 8 * 4 + n_e * 64 * 4 + nnzb * 9 * 4
     asm_avg_ms = ms[N.AGX_PROF_TANGENT] / max(1, cnt[N.AGX_PROF_TANGENT])
+    # The 3-D neo-Hooke tangent is bound by arithmetic, not bytes: an analytic count of the
+    # float32 kernel's flops, per lane (8 per element) and Gauss point (8): Jacobian by group
+    # sums, its inverse and the gradients ~100, shape functions ~15, F, F^-1 and F^-T g ~110,
+    # the 8 rows of 3 x 3 tangent entries ~83 each -> ~890; against the measured FP32 rate.
+    asm_flops = n_e * 8 * 8 * (100 + 15 + 110 + 8 * 83)
+    fp32_peak_tflops = 69.8  # FMA-chain probe on this GPU (2 flops per FMA)
 
     line = {
         "metric": "time_to_1e-10_relative_fp64_residual (64^3 neo-Hooke cube, load step 1 of 10)",
@@ -260,7 +266,11 @@ def gpu_arm(args):
                      "avg_launch_ms": spmv_avg_ms},
         "assembly": {"kernel": "element_kernel<HEX8,NEO_HOOKE,float> (tangent pass)",
                      "algorithmic_bytes": asm_bytes, "avg_launch_ms": asm_avg_ms,
-                     "achieved_gbs": asm_bytes / (asm_avg_ms * 1e-3) / 1e9 if asm_avg_ms else None},
+                     "achieved_gbs": asm_bytes / (asm_avg_ms * 1e-3) / 1e9 if asm_avg_ms else None,
+                     "flops_estimate": asm_flops,
+                     "achieved_tflops": asm_flops / (asm_avg_ms * 1e-3) / 1e12 if asm_avg_ms else None,
+                     "fp32_peak_tflops": fp32_peak_tflops,
+                     "frac_fp32_peak": asm_flops / (asm_avg_ms * 1e-3) / 1e12 / fp32_peak_tflops if asm_avg_ms else None},
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 2 * w.n_dofs * 8,
                 "d2h_bytes_per_step": w.n_dofs * 8},
         "gpu_launches": int(l1.value - l0.value),
