@@ -154,3 +154,14 @@ def test_q2_host_shape_functions_match_oracle():
         f = rng.standard_normal(nen)
         v = spaces.fem_iso_line_quad_brick(xi, np.zeros((nen, dim)), f, {}, False, dim)
         assert np.isclose(v, om.shape_functions(xi, dim, nen) @ f)
+
+
+def test_no_cpu_fallback():
+    """Without a CUDA device the backend refuses to solve instead of falling back to the CPU."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    from autopdex_gb300 import solver
+    w = configs.poisson(n=4)
+    with pytest.raises(RuntimeError, match="CUDA"):
+        solver.solver(w.dofs, w.settings, w.static_settings)
