@@ -72,6 +72,8 @@ def _reuse_default(static_settings):
 def _backend_check(static_settings):
     if static_settings.get("solver backend") != "gb300":
         raise ValueError("autopdex_gb300.solver needs static_settings['solver backend'] == 'gb300'")
+    if not torch.cuda.is_available():
+        raise RuntimeError("the gb300 backend needs a CUDA device (there is no CPU fallback)")
     sol = static_settings.get("solution structure", ())
     if any(s != "nodal imposition" for s in sol):
         raise NotImplementedError("the gb300 backend implements 'nodal imposition' of Dirichlet DOFs")
