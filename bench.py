@@ -460,55 +460,54 @@ def other_workloads(cook_n=128, cook_rtol=1e-6, heat3d_n=128, heat3d_steps=2):
 def cpu_baseline(n, newton_iters, cg_iters, budget_s=20.0):
     """CPU oracle on a bounded sample of the workload, scaled to one load step.
 
-    Sample: (a) float64 AD element residual+tangent (oracle.elements, torch.func) on the 4096
-    elements of a 16^3 cube, one full vmap batch of the oracle (smaller batches cost up to 5x
-    more per element) -> cost per element; (b) SciPy Jacobi-CG iterations on the
-    assembled 12^3 cube matrix -> cost per CG iteration per stored entry.  Scaled with the
-    Newton and CG iteration counts of the float64 GPU path on the full 64^3 problem:
-    t = newton_iters * (2 n_e t_elem) + cg_iters * t_iter(nnz_64 / nnz_12)."""
-    import torch
-    import scipy.sparse.linalg as sla
+    The oracle's C restatement (oracle/c/orc.c: closed-form float64 neo-Hooke brick and
+    Jacobi-PCG on CSR, OpenMP over all host cores) on the 32^3 cube: (a) residual and tangent
+    cost per element; (b) COO -> CSR with Dirichlet rows and columns deleted, as
+    scipy_assembling does (solver.py:1180-1222, SciPy, single-threaded as there), per stored
+    entry; (c) Jacobi-PCG cost per iteration per stored entry -- the reference's 'cg' +
+    'jacobi' algorithm on the assembled matrix.  Scaled with the Newton and CG iteration
+    counts of the float64 GPU path on the full problem:
+    t = newton_iters (2 n_e t_res + n_e t_tan + nnz t_csr) + cg_iters nnz t_iter."""
+    import scipy.sparse as sps
     from autopdex_gb300 import configs
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from oracle import elements as el, newton
+    from oracle import corc
 
-    threads = os.cpu_count() or 1
-    torch.set_num_threads(threads)
-    w = configs.neo_hooke_cube(n=16, n_steps=10)
-    fun = el.hyperelastic_element(3, 8, 2, "3d")
-    conn = w.raw["conns"][0][:4096]
-    xI = torch.as_tensor(w.raw["coords"][conn])
-    uI = torch.zeros((conn.shape[0], 8, 3), dtype=torch.float64) + 1e-3
-    p = torch.tensor([[1.0, 0.3]] * conn.shape[0], dtype=torch.float64)
-    el.batched(fun, uI[:8], xI[:8], p[:8])
+    threads = corc.threads()
+    ns = 32
+    w = configs.neo_hooke_cube(n=ns, n_steps=10)
+    coords, conn = w.raw["coords"], w.raw["conns"][0]
+    n_e = conn.shape[0]
+    u = np.random.default_rng(0).uniform(-1e-3, 1e-3, coords.shape)
+    corc.neo_hooke_hex8(conn[:256], coords, u, w.raw["E"], w.raw["nu"])  # threads up, library loaded
     t0 = time.perf_counter()
-    el.batched(fun, uI, xI, p)
-    t_elem = (time.perf_counter() - t0) / conn.shape[0]
-
-    from oracle_setup import oracle_problem
-    w16 = configs.neo_hooke_cube(n=12, n_steps=10)
-    prob = oracle_problem(w16)
-    st = w16.steps[0](dict(w16.settings))
-    prob.values = np.asarray(st["dirichlet conditions"]).reshape(-1)
-    _, coo = newton.assemble(prob.sets, np.zeros(prob.n_dofs), prob.coords, st, prob.n_dofs)
-    free = ~prob.dirichlet
-    A = newton.scipy_assembling(coo, prob.n_dofs, free)
-    b = np.random.default_rng(0).standard_normal(A.shape[0])
-    d = A.diagonal()
-    M = sla.LinearOperator(A.shape, matvec=lambda v: v / d)
-    iters = 200
+    corc.neo_hooke_hex8(conn, coords, u, w.raw["E"], w.raw["nu"], tangent=False)
+    t_res = (time.perf_counter() - t0) / n_e
     t0 = time.perf_counter()
-    sla.cg(A, b, rtol=1e-30, maxiter=iters, M=M)
-    t_iter16 = (time.perf_counter() - t0) / iters
-    nnz64 = 81 * 9 * (n + 1) ** 3  # upper bound of stored entries of the 64^3 matrix (27 blocks of 9 per row)
-    t_iter = t_iter16 * nnz64 / max(1, A.nnz)
-    n_e = n ** 3
-    est = newton_iters * 2 * n_e * t_elem + cg_iters * t_iter
+    _, K_e = corc.neo_hooke_hex8(conn, coords, u, w.raw["E"], w.raw["nu"])
+    t_tan = (time.perf_counter() - t0) / n_e
+    edofs = (conn[:, :, None] * 3 + np.arange(3)).reshape(n_e, 24)
+    free = ~np.asarray(w.raw["dirichlet"], dtype=bool)
+    t0 = time.perf_counter()
+    A = sps.coo_matrix((K_e.ravel(), (np.repeat(edofs, 24, axis=1).ravel(), np.tile(edofs, (1, 24)).ravel())),
+                       shape=(free.size, free.size)).tocsr()
+    A = A[free][:, free].tocsr()
+    t_csr = (time.perf_counter() - t0) / A.nnz
+    del K_e
+    b = np.random.default_rng(1).standard_normal(A.shape[0])
+    corc.pcg_csr(A, b, 3)
+    iters = 100
+    t0 = time.perf_counter()
+    corc.pcg_csr(A, b, iters)
+    t_iter = (time.perf_counter() - t0) / iters / A.nnz
+    nnz = 243 * (n + 1) ** 3  # stored entries of the full problem: 27 node blocks of 3 x 3 per node (upper bound)
+    n_e_full = n ** 3
+    est = newton_iters * (2 * n_e_full * t_res + n_e_full * t_tan + nnz * t_csr) + cg_iters * nnz * t_iter
     return {"value": est, "unit": "s", "cores": threads, "kind": "port",
-            "sample": (f"float64 AD element routine on {conn.shape[0]} elements ({t_elem * 1e6:.1f} us/element) and "
-                       f"{iters} SciPy Jacobi-CG iterations on the 12^3 cube ({t_iter16 * 1e3:.2f} ms/iteration, "
-                       f"scaled by stored entries to 64^3); combined with the float64 GPU path's "
-                       f"{newton_iters} Newton and {cg_iters} CG iterations")}
+            "sample": (f"oracle C restatement on the {ns}^3 cube ({threads} threads): residual {t_res * 1e6:.2f} and "
+                       f"tangent {t_tan * 1e6:.2f} us per element, COO->CSR with Dirichlet deletion (SciPy) "
+                       f"{t_csr * 1e9:.1f} ns and Jacobi-PCG {t_iter * 1e9:.2f} ns per stored entry and iteration; "
+                       f"scaled to {n}^3 with the float64 GPU path's {newton_iters} Newton and {cg_iters} CG "
+                       f"iterations")}
 
 
 def reference_arm(args):

@@ -11,8 +11,12 @@ element derivatives), the algorithm AutoPDEx runs for its Newton solve path:
 * ``newton``    COO assembly with duplicates, the SciPy CSR conversion with
                 Dirichlet row/column deletion, ``spsolve``, and the damped Newton
                 loop with its stopping rules (solver.py, utility.py),
-* ``fast``      closed-form vectorised element kernels used as the timed CPU
-                baseline, checked against ``elements``.
+* ``nn``        the learned preconditioner's U-Net in float64 (forward and
+                gradients), the checker of the tensor-core kernels,
+* ``corc``      ctypes front end of ``c/orc.c``: the neo-Hooke brick element in
+                closed form and a Jacobi-PCG on CSR, in plain C with OpenMP
+                (built by ``build_oracle.py``), checked against ``elements`` and
+                used as the timed CPU baseline.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` leg of
 ``bench.py`` may import it, and only as the checker.  The GPU backend in
