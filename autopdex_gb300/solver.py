@@ -21,7 +21,8 @@ Extra keyword arguments: ``newton_tol``, ``maxiter`` (Newton), ``newton_rtol`` (
 
 :func:`sensitivities` gives the forward implicit derivatives of a converged solution with
 respect to scalar settings (what adaptive_load_stepping's implicit_diff_mode='forward'
-differentiates).
+differentiates), :func:`second_order_sensitivities` the second ones and
+:func:`adjoint_sensitivities` the reverse-mode gradient of a scalar function of the solution.
 """
 import numpy as np
 import torch
@@ -251,6 +252,89 @@ def sensitivities(dofs, settings, static_settings, params, rel_step=1e-6, krylov
         prob._call("agx_solve", N.C.c_void_p(rhs.data_ptr()), N.C.c_void_p(du.data_ptr()), N.C.byref(opts),
                    N.C.byref(info))
         out[key] = _out_like(du, dofs, prob.key)
+    return out
+
+
+class _DeviceOps:
+    """The float64 residual, tangent product and tangent solve of one problem on the GPU, in
+    the interface of ``implicit_diff`` (base point ``u`` with ``settings``)."""
+
+    def __init__(self, prob, u, settings, krylov_tol, krylov_maxiter):
+        self.prob, self.u, self.settings = prob, u, settings
+        self.free = torch.as_tensor(~prob.mask.astype(bool), device=prob.device).to(torch.float64)
+        self.opts = N.SolveOpts()
+        self.opts.method, self.opts.rtol, self.opts.atol = N.AGX_PCG, float(krylov_tol), 0.0
+        self.opts.maxiter, self.opts.check_every = int(krylov_maxiter), 32
+
+    def residual(self, w, settings):
+        w = w.contiguous()
+        self.prob.update_models(settings)
+        R = torch.empty_like(w)
+        self.prob._call("agx_assemble", N.C.c_void_p(w.data_ptr()), N.C.c_void_p(R.data_ptr()), -1)
+        return R
+
+    def tangent_apply(self, w, settings, v):
+        w, v = w.contiguous(), v.contiguous()
+        self.prob.update_models(settings)
+        self.prob._call("agx_assemble", N.C.c_void_p(w.data_ptr()), None, N.AGX_F64)
+        y = torch.empty_like(v)
+        self.prob._call("agx_spmv", N.AGX_F64, N.C.c_void_p(v.data_ptr()), N.C.c_void_p(y.data_ptr()))
+        return y
+
+    def solve(self, rhs):
+        rhs = rhs.contiguous()
+        self.prob.update_models(self.settings)
+        self.prob._call("agx_assemble", N.C.c_void_p(self.u.data_ptr()), None, N.AGX_F64)
+        x = torch.empty_like(rhs)
+        info = N.SolveInfo()
+        self.prob._call("agx_solve", N.C.c_void_p(rhs.data_ptr()), N.C.c_void_p(x.data_ptr()),
+                        N.C.byref(self.opts), N.C.byref(info))
+        return x
+
+
+def second_order_sensitivities(dofs, settings, static_settings, params, rel_step=1e-3, dir_step=1e-3,
+                               krylov_tol=1e-12, **kwargs):
+    """First and second forward implicit derivatives of a converged solution with respect to
+    scalar settings entries: what jacfwd of jacfwd of adaptive_load_stepping with
+    implicit_diff_mode='forward' gives at the final state of a path-independent problem
+    (tests/test_user_elem_impl_diff_and_adaptive_load_step.py:121-133).
+
+    K u_p = -dR/dp, then K u_pq = -D^2 R[(u_p, e_p), (u_q, e_q)] with the second directional
+    derivative of the float64 residual from four-point differences of tangent products
+    (``implicit_diff.second_directional_residual``); Jacobi-PCG to ``krylov_tol`` for every
+    solve.  Returns ``(first, second)``: {key: du/dp} and {(key_p, key_q): d2u/dp dq} (both
+    orders of every pair), each with the structure of ``dofs``."""
+    from . import implicit_diff
+    _backend_check(static_settings)
+    prob = get_problem(dofs, settings, static_settings)
+    u = prob.to_device(dofs)
+    ops = _DeviceOps(prob, u, settings, krylov_tol, kwargs.get("krylov_maxiter", 1000000))
+    first = implicit_diff.first_order(ops, u, settings, params, kwargs.get("first_rel_step", 1e-6))
+    second = implicit_diff.second_order(ops, u, settings, first, rel_step, dir_step)
+    prob.update_models(settings)
+    return ({k: _out_like(v, dofs, prob.key) for k, v in first.items()},
+            {k: _out_like(v, dofs, prob.key) for k, v in second.items()})
+
+
+def adjoint_sensitivities(dofs, settings, static_settings, params, dJ_du, rel_step=1e-6, krylov_tol=1e-12,
+                          **kwargs):
+    """Reverse implicit derivatives dJ/dp of a scalar J(u) of a converged solution (what jacrev
+    through adaptive_load_stepping with implicit_diff_mode='backward' gives at the final state
+    of a path-independent problem): one adjoint solve K^T lam = dJ/du, then dJ/dp =
+    -lam . dR/dp for every entry of ``params``.  ``dJ_du`` has the structure of ``dofs``.  The
+    tangent must be symmetric (potential-based models and hyperelastic elements; not the
+    backward-Euler 'user residual' model).  Returns {key: float}."""
+    from . import implicit_diff
+    _backend_check(static_settings)
+    if any(getattr(m, "kernel", None) == N.AGX_MODEL_HEAT_BE for m in static_settings["model"]):
+        raise NotImplementedError("the adjoint solve needs K^T; the backward-Euler residual model has a "
+                                  "non-symmetric tangent")
+    prob = get_problem(dofs, settings, static_settings)
+    u = prob.to_device(dofs)
+    g = prob.to_device(dJ_du)
+    ops = _DeviceOps(prob, u, settings, krylov_tol, kwargs.get("krylov_maxiter", 1000000))
+    out = implicit_diff.adjoint(ops, u, settings, params, g, rel_step)
+    prob.update_models(settings)
     return out
 
 

@@ -211,3 +211,96 @@ def implicit_sensitivity(problem, dofs, settings, key, rel_step=1e-6):
     dR = (res[0] - res[1]) / (2.0 * h)
     _, coo = assemble(problem.sets, dofs, problem.coords, settings, problem.n_dofs)
     return linear_solve_scipy(coo, -dR, problem.n_dofs, ~problem.dirichlet)
+
+
+def _param_direction(s, settings, key):
+    """d(element parameters)/d settings[key] for a set whose parameters are affine in that
+    entry (checked with two unit steps)."""
+    def at(v):
+        st = dict(settings)
+        st[key] = float(np.asarray(settings[key])) + v
+        return np.asarray(s.params(st), dtype=np.float64)
+    base = at(0.0)
+    d1, d2 = at(1.0) - base, (at(2.0) - base) / 2.0
+    if not np.allclose(d1, d2, rtol=1e-12, atol=1e-14 * (1.0 + np.abs(base).max())):
+        raise NotImplementedError("element parameters must be affine in the differentiated settings entry")
+    return d1
+
+
+def _traction_second(s, settings, key_i, key_j):
+    """Second mixed difference of a Neumann set's traction in two settings entries, exact for a
+    traction of degree <= 2 in them (unit steps)."""
+    def at(a, b):
+        st = dict(settings)
+        st[key_i] = float(np.asarray(st[key_i])) + a
+        st[key_j] = float(np.asarray(st[key_j])) + b
+        return np.asarray(s.traction(st), dtype=np.float64)
+    return at(1.0, 1.0) - at(1.0, 0.0) - at(0.0, 1.0) + at(0.0, 0.0)
+
+
+def second_directional_residual(problem, dofs, settings, du_i, key_i, du_j, key_j):
+    """D^2 R[d_i, d_j], the second derivative of the residual along the two directions
+    d = (du/dp, e_p) of (dofs, settings entry p), exact by nested forward-mode AD
+    (torch.func.jvp) of the element residuals; Neumann sets by the traction's second
+    difference (the traction enters the residual linearly)."""
+    from torch.func import jvp
+    D2 = np.zeros(problem.n_dofs)
+    for s in problem.sets:
+        ed = s.element_dofs()
+        if s.kind == "neumann":
+            t2 = _traction_second(s, settings, key_i, key_j)
+            Re = np.stack([s.fun(problem.coords[c], t2) for c in s.conn])
+            np.add.at(D2, ed.ravel(), Re.ravel())
+            continue
+        conn = s.conn
+        xI = torch.as_tensor(problem.coords[conn], dtype=DT)
+        p = torch.as_tensor(s.params(settings), dtype=DT)
+        dpi = torch.as_tensor(_param_direction(s, settings, key_i), dtype=DT)
+        dpj = torch.as_tensor(_param_direction(s, settings, key_j), dtype=DT)
+        shape = (-1,) if s.ndof == 1 else (-1, s.ndof)
+        fI = torch.as_tensor(np.asarray(dofs).reshape(shape)[conn], dtype=DT)
+        fIi = torch.as_tensor(np.asarray(du_i).reshape(shape)[conn], dtype=DT)
+        fIj = torch.as_tensor(np.asarray(du_j).reshape(shape)[conn], dtype=DT)
+        if s.kind == "residual":
+            TnI = torch.as_tensor(np.asarray(settings["dofs n"]).reshape(-1)[conn], dtype=DT)
+            res = lambda f, q, xe, tn: s.fun(f, tn, xe, q)[0].reshape(-1)
+            extra = (TnI,)
+        else:
+            res = lambda f, q, xe: s.fun(f, xe, q)[0].reshape(-1)
+            extra = ()
+
+        def one(f, q, xe, fi, qi, fj, qj, *ex):
+            first = lambda a, b: jvp(lambda u, v: res(u, v, xe, *ex), (a, b), (fi, qi))[1]
+            return jvp(first, (f, q), (fj, qj))[1]
+        Re = el.batched(one, fI, p, xI, fIi, dpi, fIj, dpj, *extra)
+        np.add.at(D2, ed.ravel(), Re.reshape(conn.shape[0], -1).numpy().ravel())
+    return D2
+
+
+def implicit_second_sensitivity(problem, dofs, settings, du_i, key_i, du_j, key_j):
+    """d^2u/(dp_i dp_j) of a converged solution (forward-over-forward implicit
+    differentiation, as jacfwd of jacfwd of adaptive_load_stepping with implicit_diff_mode
+    'forward', tests/test_user_elem_impl_diff_and_adaptive_load_step.py:121-133): from
+    R(u(p), p) = 0, K u_ij = -D^2 R[d_i, d_j] with d = (u_p, e_p), on the free DOFs."""
+    D2 = second_directional_residual(problem, dofs, settings, du_i, key_i, du_j, key_j)
+    _, coo = assemble(problem.sets, dofs, problem.coords, settings, problem.n_dofs)
+    return linear_solve_scipy(coo, -D2, problem.n_dofs, ~problem.dirichlet)
+
+
+def adjoint_sensitivity(problem, dofs, settings, dJ_du, key, rel_step=1e-6):
+    """dJ/dp of a scalar J(u) of a converged solution by reverse implicit differentiation
+    (implicit_diff_mode 'backward' with jacrev): K^T lam = dJ/du on the free DOFs,
+    dJ/dp = -lam . dR/dp."""
+    p0 = float(settings[key])
+    h = rel_step * (abs(p0) if p0 != 0.0 else 1.0)
+    res = []
+    for v in (p0 + h, p0 - h):
+        st = dict(settings)
+        st[key] = v
+        res.append(problem.residual(dofs, st))
+    dR = (res[0] - res[1]) / (2.0 * h)
+    _, coo = assemble(problem.sets, dofs, problem.coords, settings, problem.n_dofs)
+    rows, cols, data = coo
+    lam = linear_solve_scipy((cols, rows, data), np.asarray(dJ_du, dtype=np.float64), problem.n_dofs,
+                             ~problem.dirichlet)
+    return -float(lam[~problem.dirichlet] @ dR[~problem.dirichlet])

@@ -7,7 +7,8 @@ Run in a container that has the reference checkout (it is not needed to run the 
   tests/test_user_elem_impl_diff_and_adaptive_load_step.py:31-55 (x_nodes, elements,
   surface_elements), parsed from the file as data.
 * golden.json: the golden scalars asserted by the reference's tests on this path (the Q2 Cook
-  solution's u.u and its derivatives with respect to Young's modulus and Poisson's ratio).
+  solution's u.u, its first derivatives with respect to Young's modulus E and Poisson's ratio
+  nu, and its second derivatives d2/dE2, d2/dE dnu, d2/dnu dE, d2/dnu2).
 """
 import json
 import os
@@ -34,7 +35,7 @@ def main(ref):
     s = grab("surface_elements").astype(np.int64)
     np.savez(os.path.join(HERE, "cook_q2_mesh.npz"), x_nodes=x, elements=e, surface_elements=s)
     g1 = re.search(r"isclose\(test, ([0-9.]+)\)", open(os.path.join(ref, "tests", "test_dicts_as_dofs_user_potential.py")).read())
-    # test1 .. test3 of the reference test: u.u and its first derivatives in E and nu
+    # test1 .. test7 of the reference test: u.u, its first and its second derivatives in E and nu
     g2 = re.findall(r"jnp\.array\((-?[0-9.]+), dtype=jnp\.float64\)", src)
     golden = {
         "poisson_5x5_sum_phi": {"value": float(g1.group(1)),
@@ -46,6 +47,12 @@ def main(ref):
         "cook_q2_d_dofs_dot_dofs_d_poisson_ratio": {
             "value": float(g2[2]), "source": "tests/test_user_elem_impl_diff_and_adaptive_load_step.py:155"},
     }
+    # test4 .. test7: second derivatives (E E, E nu, nu E, nu nu), lines 156-159
+    for k, name in enumerate(("youngs_modulus_youngs_modulus", "youngs_modulus_poisson_ratio",
+                              "poisson_ratio_youngs_modulus", "poisson_ratio_poisson_ratio")):
+        golden["cook_q2_d2_dofs_dot_dofs_d_" + name] = {
+            "value": float(g2[3 + k]),
+            "source": "tests/test_user_elem_impl_diff_and_adaptive_load_step.py:%d" % (156 + k)}
     with open(os.path.join(HERE, "golden.json"), "w") as fh:
         json.dump(golden, fh, indent=1)
     print(golden)

@@ -20,8 +20,8 @@ pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def test_q2_cook_golden_and_sensitivities():
-    golden = json.load(open(os.path.join(HERE, "golden", "golden.json")))
+def _cook_golden_setup():
+    """Settings dicts of the reference's golden Q2 Cook case, for this backend."""
     d = np.load(os.path.join(HERE, "golden", "cook_q2_mesh.npz"))
     x_nodes, elements, surface = d["x_nodes"], d["elements"], d["surface_elements"]
     pts = [[0., 0.], [48., 44.], [48., 60.], [0., 44.]]
@@ -48,13 +48,23 @@ def test_q2_cook_golden_and_sensitivities():
                 "node coordinates": x_nodes, "dirichlet conditions": np.zeros_like(dirichlet_dofs, dtype=np.float64),
                 "youngs modulus": 100., "poisson ratio": 0.3}
     dofs0 = np.zeros((x_nodes.shape[0], 2))
+    return static, settings, multiplier_settings, dofs0
+
+
+def _cook_golden_solution():
+    static, settings, multiplier_settings, dofs0 = _cook_golden_setup()
     dofs, mult, *_ = solver.adaptive_load_stepping(dofs0, settings, static, multiplier_settings, False,
                                                    newton_tol=1e-8)
     assert abs(mult - 1.0) < 1e-12
+    return static, multiplier_settings(dict(settings), 1.0), dofs
+
+
+def test_q2_cook_golden_and_sensitivities():
+    golden = json.load(open(os.path.join(HERE, "golden", "golden.json")))
+    static, settings, dofs = _cook_golden_solution()
     u = np.asarray(dofs).reshape(-1)
     g = golden["cook_q2_dofs_dot_dofs"]["value"]
     assert abs(u @ u - g) <= 1e-9 * g, u @ u
-    settings = multiplier_settings(dict(settings), 1.0)
     sens = solver.sensitivities(dofs, settings, static, ["youngs modulus", "poisson ratio"])
     for key, name in (("youngs modulus", "cook_q2_d_dofs_dot_dofs_d_youngs_modulus"),
                       ("poisson ratio", "cook_q2_d_dofs_dot_dofs_d_poisson_ratio")):
@@ -144,3 +154,28 @@ def test_q2_element_parity(kind, dtype):
     K = assembler.assemble_tangent(dofs, settings, static, dtype=dtype).to_scipy()
     tol = 1e-12 if dtype == "float64" else 2e-6
     assert abs(K - K_or).max() <= tol * abs(K_or).max()
+
+
+def test_q2_cook_second_order_and_adjoint():
+    """The reference's second-order golden values (lines 156-159: d2(u.u)/dE2 = 4.17157824,
+    d2/dE dnu = d2/dnu dE = -51.42695148, d2/dnu2 = -45854.7002203) from
+    ``solver.second_order_sensitivities`` -- d2(u.u)/dp dq = 2 (u_p . u_q + u . u_pq) -- and
+    the first derivatives again by one adjoint solve (``solver.adjoint_sensitivities`` with
+    dJ/du = 2u), which the reference checks in 'backward' mode (lines 169-170).  Tolerance
+    1e-6 relative (the reference's own allclose uses 1e-5)."""
+    golden = json.load(open(os.path.join(HERE, "golden", "golden.json")))
+    static, settings, dofs = _cook_golden_solution()
+    keys = ["youngs modulus", "poisson ratio"]
+    first, second = solver.second_order_sensitivities(dofs, settings, static, keys)
+    u = np.asarray(dofs).reshape(-1)
+    du = {k: np.asarray(first[k]).reshape(-1) for k in keys}
+    name = {"youngs modulus": "youngs_modulus", "poisson ratio": "poisson_ratio"}
+    assert len(second) == 4
+    for (a, b), v in second.items():
+        val = 2.0 * (du[a] @ du[b] + u @ np.asarray(v).reshape(-1))
+        ref = golden["cook_q2_d2_dofs_dot_dofs_d_%s_%s" % (name[a], name[b])]["value"]
+        assert abs(val - ref) <= 1e-6 * abs(ref), (a, b, val, ref)
+    adj = solver.adjoint_sensitivities(dofs, settings, static, keys, 2.0 * np.asarray(dofs))
+    for k in keys:
+        ref = golden["cook_q2_d_dofs_dot_dofs_d_" + name[k]]["value"]
+        assert abs(adj[k] - ref) <= 1e-7 * abs(ref), (k, adj[k], ref)

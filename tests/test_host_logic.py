@@ -165,3 +165,19 @@ def test_no_cpu_fallback():
     w = configs.poisson(n=4)
     with pytest.raises(RuntimeError, match="CUDA"):
         solver.solver(w.dofs, w.settings, w.static_settings)
+    for fn in (lambda: solver.sensitivities(w.dofs, w.settings, w.static_settings, []),
+               lambda: solver.second_order_sensitivities(w.dofs, w.settings, w.static_settings, []),
+               lambda: solver.adjoint_sensitivities(w.dofs, w.settings, w.static_settings, [], w.dofs)):
+        with pytest.raises(RuntimeError, match="CUDA"):
+            fn()
+
+
+def test_implicit_diff_stencils():
+    """The central differences of the implicit-differentiation algebra: the two-point stencil
+    is exact for quadratics, the four-point one for quartics."""
+    from autopdex_gb300 import implicit_diff
+    f2 = lambda e: 3.0 + 2.0 * e + 5.0 * e * e
+    f4 = lambda e: 1.0 - e + 0.5 * e ** 2 + 7.0 * e ** 3 - 2.0 * e ** 4
+    assert abs(implicit_diff._central(f2, 0.1, 2) - 2.0) < 1e-13
+    assert abs(implicit_diff._central(f4, 0.1, 4) + 1.0) < 1e-12
+    assert abs(implicit_diff._central(f4, 0.1, 2) + 1.0) > 1e-3

@@ -47,10 +47,10 @@ def _q2_test_arrays():
     return d["x_nodes"], d["elements"], d["surface_elements"]
 
 
-def test_golden_q2_cook_neo_hooke():
-    """tests/test_user_elem_impl_diff_and_adaptive_load_step.py:153-155 -> dofs.dofs =
-    19390.35027108 and its derivatives -216.0310416 (E) and -1859.43760286 (nu) (Q2 user
-    element, neo-Hooke plane strain, Neumann traction 20, load stepping to 1)."""
+@pytest.fixture(scope="module")
+def cook_q2():
+    """The Q2 Cook membrane of tests/test_user_elem_impl_diff_and_adaptive_load_step.py (Q2
+    user element, neo-Hooke plane strain, Neumann traction 20) solved by load stepping to 1."""
     x, E, S = _q2_test_arrays()
     pts = [[0., 0.], [48., 44.], [48., 60.], [0., 44.]]
     dn = mesh.in_planes(x, pts[0], [1., 0.])
@@ -68,15 +68,103 @@ def test_golden_q2_cook_neo_hooke():
         st["load"] = m * 20.0
         dofs, info, _ = newton.damped_newton(prob, dofs, st, 1e-8)
         assert not info[2]
+    return prob, dofs, st
+
+
+_FIRST = (("E", "cook_q2_d_dofs_dot_dofs_d_youngs_modulus"), ("nu", "cook_q2_d_dofs_dot_dofs_d_poisson_ratio"))
+_NAME = {"E": "youngs_modulus", "nu": "poisson_ratio"}
+
+
+def test_golden_q2_cook_neo_hooke(cook_q2):
+    """tests/test_user_elem_impl_diff_and_adaptive_load_step.py:153-155 -> dofs.dofs =
+    19390.35027108 and its derivatives -216.0310416 (E) and -1859.43760286 (nu)."""
+    prob, dofs, st = cook_q2
     g = GOLDEN["cook_q2_dofs_dot_dofs"]["value"]
     assert abs(dofs @ dofs - g) <= 1e-9 * g
     # first derivatives of u.u in E and nu by implicit differentiation at the final state
     # (the golden values carry 10 and 12 significant digits)
-    for key, name in (("E", "cook_q2_d_dofs_dot_dofs_d_youngs_modulus"),
-                      ("nu", "cook_q2_d_dofs_dot_dofs_d_poisson_ratio")):
+    for key, name in _FIRST:
         du = newton.implicit_sensitivity(prob, dofs, st, key)
         ref = GOLDEN[name]["value"]
         assert abs(2.0 * dofs @ du - ref) <= 1e-7 * abs(ref), (key, 2.0 * dofs @ du, ref)
+
+
+def test_golden_q2_cook_second_order(cook_q2):
+    """tests/test_user_elem_impl_diff_and_adaptive_load_step.py:156-159 -> the second
+    derivatives of u.u: 4.17157824 (E E), -51.42695148 (E nu and nu E), -45854.7002203
+    (nu nu).  d2(u.u)/dp_i dp_j = 2 (u_i . u_j + u . u_ij), with u_ij from
+    K u_ij = -D^2 R[(u_i, e_i), (u_j, e_j)] (nested forward-mode AD of the elements)."""
+    prob, dofs, st = cook_q2
+    du = {k: newton.implicit_sensitivity(prob, dofs, st, k) for k in ("E", "nu")}
+    for a, b in (("E", "E"), ("E", "nu"), ("nu", "E"), ("nu", "nu")):
+        uab = newton.implicit_second_sensitivity(prob, dofs, st, du[a], a, du[b], b)
+        val = 2.0 * (du[a] @ du[b] + dofs @ uab)
+        ref = GOLDEN["cook_q2_d2_dofs_dot_dofs_d_%s_%s" % (_NAME[a], _NAME[b])]["value"]
+        assert abs(val - ref) <= 1e-8 * abs(ref), (a, b, val, ref)
+
+
+def test_golden_q2_cook_reverse_mode(cook_q2):
+    """Reverse implicit differentiation (implicit_diff_mode 'backward', checked by the
+    reference at tests/test_user_elem_impl_diff_and_adaptive_load_step.py:169-170 against
+    the forward values): one adjoint solve K^T lam = dJ/du = 2u gives dJ/dp = -lam . dR/dp
+    for every p, and the second derivative d2J/dnu2 = 2 u_nu . u_nu - lam . D^2 R[d_nu, d_nu]."""
+    prob, dofs, st = cook_q2
+    for key, name in _FIRST:
+        val = newton.adjoint_sensitivity(prob, dofs, st, 2.0 * dofs, key)
+        ref = GOLDEN[name]["value"]
+        assert abs(val - ref) <= 1e-7 * abs(ref), (key, val, ref)
+    du = newton.implicit_sensitivity(prob, dofs, st, "nu")
+    _, coo = newton.assemble(prob.sets, dofs, prob.coords, st, prob.n_dofs)
+    lam = newton.linear_solve_scipy((coo[1], coo[0], coo[2]), 2.0 * dofs, prob.n_dofs, ~prob.dirichlet)
+    D2 = newton.second_directional_residual(prob, dofs, st, du, "nu", du, "nu")
+    free = ~prob.dirichlet
+    val = 2.0 * du @ du - lam[free] @ D2[free]
+    ref = GOLDEN["cook_q2_d2_dofs_dot_dofs_d_poisson_ratio_poisson_ratio"]["value"]
+    assert abs(val - ref) <= 1e-8 * abs(ref), (val, ref)
+
+
+class _OracleOps:
+    """The oracle's residual, tangent product and spsolve in the interface the backend's
+    implicit-differentiation algebra (``autopdex_gb300.implicit_diff``) runs on."""
+
+    def __init__(self, prob, u, settings):
+        self.prob, self.u, self.settings = prob, u, settings
+        self.free = (~prob.dirichlet).astype(np.float64)
+
+    def residual(self, w, settings):
+        return self.prob.residual(w, settings)
+
+    def tangent_apply(self, w, settings, v):
+        import scipy.sparse
+        _, (r, c, d) = newton.assemble(self.prob.sets, w, self.prob.coords, settings, self.prob.n_dofs)
+        return scipy.sparse.coo_matrix((d, (r, c)), shape=(self.prob.n_dofs,) * 2).tocsr() @ v
+
+    def solve(self, rhs):
+        _, coo = newton.assemble(self.prob.sets, self.u, self.prob.coords, self.settings, self.prob.n_dofs)
+        return newton.linear_solve_scipy(coo, rhs, self.prob.n_dofs, ~self.prob.dirichlet)
+
+
+def test_implicit_diff_algebra_reproduces_golden(cook_q2):
+    """The backend's second-order and adjoint algebra (four-point differences of tangent
+    products and residuals, ``autopdex_gb300.implicit_diff``), run here on the oracle's
+    operations, reproduces the reference's seven golden values of the Q2 Cook case."""
+    from autopdex_gb300 import implicit_diff
+    prob, dofs, st = cook_q2
+    ops = _OracleOps(prob, dofs, st)
+    first = implicit_diff.first_order(ops, dofs, st, ["E", "nu"])
+    for key, name in _FIRST:
+        ref = GOLDEN[name]["value"]
+        assert abs(2.0 * dofs @ first[key] - ref) <= 1e-7 * abs(ref)
+    second = implicit_diff.second_order(ops, dofs, st, first)
+    assert len(second) == 4
+    for (a, b), uab in second.items():
+        val = 2.0 * (first[a] @ first[b] + dofs @ uab)
+        ref = GOLDEN["cook_q2_d2_dofs_dot_dofs_d_%s_%s" % (_NAME[a], _NAME[b])]["value"]
+        assert abs(val - ref) <= 1e-8 * abs(ref), (a, b, val, ref)
+    adj = implicit_diff.adjoint(ops, dofs, st, ["E", "nu"], 2.0 * dofs)
+    for key, name in _FIRST:
+        ref = GOLDEN[name]["value"]
+        assert abs(adj[key] - ref) <= 1e-7 * abs(ref), (key, adj[key], ref)
 
 
 def _fd_check(fun, args, idx=0, h=1e-6):
