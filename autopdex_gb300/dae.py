@@ -1,4 +1,4 @@
-"""Time stepping over the GB300 Newton solve: the backward-Euler subset of AutoPDEx's
+"""Time stepping over the GB300 Newton solve: the backward-Euler / BDF subset of AutoPDEx's
 ``dae.TimeSteppingManager`` (dae.py:1734-2283).
 
 The reference manager runs multi-stage integrators on 'user residual' forms written in
@@ -9,8 +9,14 @@ every step and calls ``solver.solver`` (the GPU Newton solve) as the root solver
 loop follows dae.py:2141-2250: t = min(t_n + dt, t_max), pre-step update, solve, step size
 controller (scaler, accept, interrupt), on acceptance the post-processing, post-step update
 and save policy, dt scaled either way; an interrupt ends the run with NaN states.
-Integrators other than ``BackwardEuler`` and controllers that need error estimates
-(``PIDController``) are not implemented.
+
+A k-step backward differentiation formula, q_t = (c_0 q + sum_k c_k q_(n+1-k)) / dt, is the
+backward-Euler form c_0 (q - q*) / dt with q* = -sum_k c_k q_(n+1-k) / c_0, so the same kernel
+integrates it: the manager passes q* as the previous state and dt / c_0 as the step.  Like
+the reference it uses the constant-step coefficients whatever the step history and starts
+from a history filled with the initial state (dae.py:1799-1806).
+Integrators other than ``BackwardEuler`` and ``BackwardDiffFormula`` and controllers that need
+error estimates (``PIDController``) are not implemented.
 """
 from dataclasses import dataclass, field
 from typing import Any
@@ -29,6 +35,32 @@ class BackwardEuler:
     order = 1
     stage_positions = np.array([1.0])
     stage_list = [0]
+    coeffs = (1.0, -1.0)
+
+
+class BackwardDiffFormula:
+    """BDF of 1 to 6 steps (dae.py:537-587): q_t = (c_0 q + sum_k c_k q_(n+1-k)) / dt with the
+    constant-step coefficients of order ``num_steps``; one implicit stage."""
+    _COEFFS = {
+        1: (1.0, -1.0),
+        2: (3.0 / 2.0, -2.0, 1.0 / 2.0),
+        3: (11.0 / 6.0, -3.0, 3.0 / 2.0, -1.0 / 3.0),
+        4: (25.0 / 12.0, -4.0, 3.0, -4.0 / 3.0, 1.0 / 4.0),
+        5: (137.0 / 60.0, -5.0, 5.0, -10.0 / 3.0, 5.0 / 4.0, -1.0 / 5.0),
+        6: (49.0 / 20.0, -6.0, 15.0 / 2.0, -20.0 / 3.0, 15.0 / 4.0, -6.0 / 5.0, 1.0 / 6.0),
+    }
+    num_stages = 1
+    num_derivs = 1
+    stage_positions = np.array([1.0])
+    stage_list = [0]
+
+    def __init__(self, num_steps):
+        if num_steps not in self._COEFFS:
+            raise ValueError("Order of BDF method not supported. Supported orders: 1 to 6. "
+                             "From 7 on the BDF method is not stable.")
+        self.num_steps = num_steps
+        self.order = num_steps
+        self.coeffs = self._COEFFS[num_steps]
 
 
 # ---- step size controllers (dae.py:1314-1573) -------------------------------------------
@@ -171,8 +203,13 @@ class TimeSteppingManager:
                  step_size_controller=None, postprocessing_fun=lambda q_fun, t, settings: {},
                  pre_step_updates=None, post_step_updates=None, **solver_kwargs):
         self.integrators = static_settings["time integrators"]
-        if not all(isinstance(i, BackwardEuler) for i in self.integrators.values()):
-            raise NotImplementedError("the gb300 time stepping implements BackwardEuler")
+        if not all(isinstance(i, (BackwardEuler, BackwardDiffFormula)) for i in self.integrators.values()):
+            raise NotImplementedError("the gb300 time stepping implements BackwardEuler and BackwardDiffFormula")
+        coeffs = {tuple(i.coeffs) for i in self.integrators.values()}
+        if len(coeffs) != 1:
+            raise NotImplementedError("all fields must use the same integrator (one previous-state entry)")
+        self.coeffs = coeffs.pop()
+        self.num_steps = len(self.coeffs) - 1
         if root_solver is not None:
             raise NotImplementedError("the root solver is the gb300 Newton solve (solver.solver)")
         keys = set()
@@ -199,6 +236,16 @@ class TimeSteppingManager:
         settings["current time"] = t
         return settings
 
+    def _backward_euler_form(self, history, dt):
+        """(q*, dt / c_0) of the step: the previous state and step the backward-Euler model
+        reads.  ``history[0]`` is the latest accepted state."""
+        if self.num_steps == 1:
+            return history[0], dt
+        c = self.coeffs
+        q_star = {k: sum(history[i][k] * c[i + 1] for i in range(self.num_steps)) * (-1.0 / c[0])
+                  for k in history[0]}
+        return q_star, dt / c[0]
+
     def run(self, dofs, dt0, t_max, num_time_steps, settings={"current time": 0.0}):
         """Steps from t = 0 until t_max or ``num_time_steps`` attempted steps (dae.py:2087-2283)."""
         if list(dofs.keys()) != sorted(dofs.keys()):
@@ -212,21 +259,23 @@ class TimeSteppingManager:
         hist = self.save_policy.save_step(hist, t_n, q_n, user) if self.save_policy else hist
         n_acc = n_rej = 0
         q = q_n
+        history = [q_n] * self.num_steps
         for _ in range(num_time_steps):
             if not t_n < t_max or ctrl.interrupt:
                 break
             t = min(t_n + dt, t_max)
             dt = t - t_n
             settings = self.pre_step_updates(t, settings)
-            settings[self.qn_key] = q_n
-            settings[self.dt_key] = dt
+            settings[self.qn_key], settings[self.dt_key] = self._backward_euler_form(history, dt)
             q, (n_it, res, diverged) = _solver.solver(q_n, settings, self.static_settings, **self.solver_kwargs)
             converged = not bool(diverged)
-            ctrl = self.step_size_controller.compute_scaler(None, q, q_n, ctrl, 1, converged, int(n_it), dt,
+            order = min(i.order for i in self.integrators.values())
+            ctrl = self.step_size_controller.compute_scaler(None, q, q_n, ctrl, order, converged, int(n_it), dt,
                                                             self.verbose)
             ctrl = self.step_size_controller.check_accept(ctrl, converged, self.verbose)
             if ctrl.accept and not ctrl.interrupt:
                 q_n = q
+                history = [q] + history[:-1]
                 user = self.postprocessing_fun(lambda tt: q, t, settings)
                 settings = self.post_step_updates(lambda tt: q, t, settings)
                 hist = self.save_policy.save_step(hist, t, q, user) if self.save_policy else hist

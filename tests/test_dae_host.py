@@ -75,8 +75,63 @@ def test_equidistant_saving(monkeypatch):
     assert np.allclose(st.history.t, [0.0, 0.5, 1.0])
 
 
-def test_only_backward_euler():
+def test_only_backward_euler_and_bdf():
     st = _static()
     st["time integrators"] = {"T": object()}
     with pytest.raises(NotImplementedError):
         dae.TimeSteppingManager(st)
+    with pytest.raises(ValueError):
+        dae.BackwardDiffFormula(7)
+
+
+def _fake_be_form(monkeypatch, log):
+    """Root solve of T' = -lam T in the backward-Euler form the model reads:
+    (T - T*) / dt_eff = -lam T."""
+    def solve(dofs, settings, static_settings, **kw):
+        q_star, dt_eff = settings["dofs n"], settings["time increment"]
+        log.append((np.asarray(q_star["T"]).copy(), dt_eff))
+        return {"T": np.asarray(q_star["T"]) / (1.0 + LAM * dt_eff)}, (3, 0.0, False)
+    monkeypatch.setattr(S, "solver", solve)
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5, 6])
+def test_bdf_steps_equal_the_multistep_recurrence(monkeypatch, k):
+    """BackwardDiffFormula(k) through the manager equals the k-step recurrence
+    (c_0 T_(n+1) + sum_i c_i T_(n+1-i)) / dt = -lam T_(n+1) with the reference's constant-step
+    coefficients and a history started from the initial state (dae.py:537-587, :1799-1806)."""
+    log = []
+    _fake_be_form(monkeypatch, log)
+    static = _static()
+    static["time integrators"] = {"T": dae.BackwardDiffFormula(k)}
+    dt, n = 0.05, 12
+    st = dae.TimeSteppingManager(static, save_policy=dae.SaveAllPolicy()).run({"T": np.ones(3)}, dt, n * dt, 20)
+    assert st.num_accepted == n
+    c = dae.BackwardDiffFormula(k).coeffs
+    hist = [1.0] * k
+    for _ in range(n):
+        T = -sum(ci * h for ci, h in zip(c[1:], hist)) / (c[0] + LAM * dt)
+        hist = [T] + hist[:-1]
+    assert abs(st.q["T"][0] - hist[0]) <= 1e-14 * abs(hist[0])
+    assert np.allclose(log[0][1], dt / c[0]) and np.allclose(log[0][0], 1.0)
+    assert np.allclose(st.history.q["T"][n, :], hist[0], rtol=1e-14, atol=0)
+
+
+def test_bdf_startup_history_and_order(monkeypatch):
+    """BDF2 keeps two states and the first step reads (T0, T0) as its history.  That start
+    (the reference's: a history filled with the initial state) is a first-order step, so on
+    T' = -lam T the error at t = 1 of BDF2 and BDF3 through the manager halves with dt."""
+    log = []
+    _fake_be_form(monkeypatch, log)
+    static = _static()
+    static["time integrators"] = {"T": dae.BackwardDiffFormula(2)}
+    dae.TimeSteppingManager(static).run({"T": np.ones(1)}, 0.1, 0.3, 3)
+    # step 1: q* = (2 T0 - T0 / 2) / (3/2) = T0; step 2: q* = (2 T1 - T0 / 2) / (3/2)
+    T1 = 1.0 / (1.0 + LAM * 0.1 / 1.5)
+    assert np.isclose(log[0][0][0], 1.0) and np.isclose(log[1][0][0], (2.0 * T1 - 0.5) / 1.5)
+    for k in (2, 3):
+        static["time integrators"] = {"T": dae.BackwardDiffFormula(k)}
+        errs = []
+        for dt in (0.02, 0.01, 0.005):
+            st = dae.TimeSteppingManager(static).run({"T": np.ones(1)}, dt, 1.0, 400)
+            errs.append(abs(st.q["T"][0] - np.exp(-LAM)))
+        assert 1.9 < errs[0] / errs[1] < 2.1 and 1.9 < errs[1] / errs[2] < 2.1, errs
