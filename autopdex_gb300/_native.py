@@ -72,6 +72,7 @@ _SIGNATURES = {
     "agx_set_quadrature_points": (C.c_int, [_P, C.c_int, C.c_int, _P, _P]),
     "agx_spmv_values": (C.c_int, [_P, C.c_int, _P, _P, _P]),
     "agx_jacobi": (C.c_int, [_P, C.c_int, _P, _P]),
+    "agx_get_diagonal": (C.c_int, [_P, C.c_int, _P]),
     "agx_spmv": (C.c_int, [_P, C.c_int, _P, _P]),
     "agx_solve": (C.c_int, [_P, _P, _P, C.POINTER(SolveOpts), C.POINTER(SolveInfo)]),
     "agx_newton": (C.c_int, [_P, _P, _P, C.POINTER(NewtonOpts), C.POINTER(NewtonInfo)]),

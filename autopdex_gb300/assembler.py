@@ -1,7 +1,8 @@
 """``assembler.assemble_residual`` / ``assemble_tangent`` of AutoPDEx on the GPU.
 
 ``assemble_residual(dofs, settings, static_settings)`` mirrors assembler.py:587-637 and
-returns the residual with the structure of ``dofs``.  ``assemble_tangent`` mirrors
+returns the residual with the structure of ``dofs``; ``assemble_tangent_diagonal`` mirrors
+assembler.py:639-680 (flat float64 diagonal, the sum over all element sets).  ``assemble_tangent`` mirrors
 assembler.py:682-777 but returns the summed node-block CSR matrix (the BCOO of AutoPDEx
 keeps the duplicates until scipy_assembling sums them, solver.py:1180-1222) as a
 :class:`BlockCSR` of device arrays; with ``eliminate_dirichlet=True`` the prescribed rows
@@ -74,3 +75,29 @@ def assemble_tangent(dofs, settings, static_settings, dtype="float64", eliminate
             prob._call("agx_set_dirichlet", mask.ctypes.data)
             prob.mask = mask
     return BlockCSR(out_rp, out_col, out_vals, prob.n_nodes, b)
+
+
+def assemble_tangent_diagonal(dofs, settings, static_settings, dtype="float64"):
+    """Diagonal of the tangent summed over all element sets (assembler.py:639-680, :1090-1113,
+    :1216-1306, :1310-1389): a flat float64 vector of length n_dofs, as ``dict_flatten``
+    orders the DOFs.  No Dirichlet elimination (the reference's diagonal has none)."""
+    _backend_check(static_settings)
+    prob = get_problem(dofs, settings, static_settings)
+    prob.update_models(settings)
+    x = prob.to_device(dofs)
+    dt = N.AGX_F64 if dtype == "float64" else N.AGX_F32
+    saved = prob.mask
+    prob.set_dirichlet(None)
+    try:
+        prob._call("agx_assemble", C.c_void_p(x.data_ptr()), None, dt)
+        diag = torch.empty(prob.n_dofs, dtype=torch.float64, device=prob.device)
+        prob._call("agx_get_diagonal", dt, C.c_void_p(diag.data_ptr()))
+    finally:
+        mask = saved.copy()
+        prob.mask = None
+        prob._call("agx_set_dirichlet", mask.ctypes.data)
+        prob.mask = mask
+    ref = dofs[prob.key] if isinstance(dofs, dict) else dofs
+    if isinstance(ref, np.ndarray) or not hasattr(ref, "shape"):
+        return diag.cpu().numpy()
+    return diag

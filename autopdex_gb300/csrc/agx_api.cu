@@ -464,6 +464,15 @@ int agx_jacobi(agx_context* ctx, int dtype, const void* r, void* z) {
   return AGX_OK;
 }
 
+int agx_get_diagonal(agx_context* ctx, int dtype, double* diag) {
+  if (!ctx || !ctx->pattern_ready) return agx_fail(ctx, AGX_ERR_STATE, "agx_finalize first");
+  if (ctx->tangent_valid != dtype) return agx_fail(ctx, AGX_ERR_STATE, "no assembled tangent of dtype %d", dtype);
+  if (!diag) return agx_fail(ctx, AGX_ERR_ARG, "null pointer");
+  agx_launch_diagonal(ctx, dtype, diag);
+  AGX_CHECK_LAUNCH(ctx);
+  return AGX_OK;
+}
+
 int agx_copy_values(agx_context* ctx, int dtype, void* values) {
   if (!ctx || !ctx->pattern_ready || !values) return agx_fail(ctx, AGX_ERR_ARG, "bad arguments");
   const size_t bs = (size_t)ctx->ndof * ctx->ndof * ctx->nnzb;

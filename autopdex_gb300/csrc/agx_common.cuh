@@ -186,6 +186,7 @@ void agx_launch_negate_free(agx_context* ctx, const double* R, double* b);
 int agx_spmv_impl(agx_context* ctx, int dtype, const void* x, void* y);
 int agx_spmv_values_impl(agx_context* ctx, int dtype, const void* values, const void* x, void* y);
 void agx_launch_jacobi(agx_context* ctx, int dtype, const void* r, void* z);
+void agx_launch_diagonal(agx_context* ctx, int dtype, double* diag);
 int agx_autotune_spmv(agx_context* ctx, int* chosen, float* best_ms);
 void agx_launch_planes_to_blocks(agx_context* ctx, const double* planes, double* blocks);
 void agx_launch_planes_to_blocks(agx_context* ctx, const float* planes, float* blocks);

@@ -283,6 +283,64 @@ __device__ __forceinline__ T inverse(const T (&m)[D][D], T (&inv)[D][D]) {
   }
 }
 
+// Ciarlet neo-Hooke quantities (models.py:1122-1146) from the displacement gradient H = F - I,
+// written without cancellation near F = I.  J - 1 = tr H + i2(H) + det H (i2 the sum of the
+// principal 2 x 2 minors; plane strain: tr H + det H), and I - F^-T = (H^T + (i2 + det H) I -
+// cof H) / J (plane strain: (H^T + det H I) / J), so that
+//   P = mu (F - F^-T) + lam/2 (J^2 - 1) F^-T = mu (H + I - F^-T) + lam/2 (J-1)(J+1) F^-T.
+// Forming J = det F and then J^2 - 1 loses |F| eps absolutely, which lam turns into a stress
+// error of lam eps: with nu = 0.4999 (lam / mu = 5000) that rounding, not the solver, bounded the
+// float64 Newton residual near 1e-6 of the load-step residual on Cook's membrane.  Returns J - 1
+// and fills P, F^-1 (for the tangent) and J.
+template <typename T, int D>
+__device__ __forceinline__ T neo_hooke_stress(const T (&H)[D][D], T lam, T mu, T (&P)[D][D], T (&Fi)[D][D], T& Jdet) {
+  T jm1, s;  // J - 1 and the scalar multiplying I in J (I - F^-T)
+  T C[D][D];  // cofactor matrix of F (F^-T = C / J)
+  if constexpr (D == 2) {
+    const T dH = det2(H);
+    jm1 = (H[0][0] + H[1][1]) + dH;
+    s = dH;
+    C[0][0] = T(1) + H[1][1]; C[0][1] = -H[1][0];
+    C[1][0] = -H[0][1];       C[1][1] = T(1) + H[0][0];
+  } else {
+    const T i2 = (H[0][0] * H[1][1] - H[0][1] * H[1][0]) + (H[0][0] * H[2][2] - H[0][2] * H[2][0]) +
+                 (H[1][1] * H[2][2] - H[1][2] * H[2][1]);
+    const T dH = det3(H);
+    jm1 = (H[0][0] + H[1][1] + H[2][2]) + (i2 + dH);
+    s = i2 + dH;
+    T F[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) F[i][j] = H[i][j] + (i == j ? T(1) : T(0));
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const int i1 = (i + 1) % 3, i2_ = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+        C[i][j] = F[i1][j1] * F[i2_][j2] - F[i1][j2] * F[i2_][j1];
+      }
+  }
+  Jdet = T(1) + jm1;
+  const T rJ = T(1) / Jdet;
+  const T pl = lam * T(0.5) * jm1 * (T(2) + jm1);  // lam/2 (J^2 - 1)
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      Fi[j][i] = C[i][j] * rJ;  // F^-1 = C^T / J
+      // cof H, the third term of J (I - F^-T) in 3-D: the cofactors of H
+      T cofH = T(0);
+      if constexpr (D == 3) {
+        const int i1 = (i + 1) % 3, i2_ = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+        cofH = H[i1][j1] * H[i2_][j2] - H[i1][j2] * H[i2_][j1];
+      }
+      const T m = (H[j][i] + (i == j ? s : T(0)) - cofH) * rJ;  // (I - F^-T)_ij
+      P[i][j] = mu * (H[i][j] + m) + pl * C[i][j] * rJ;
+    }
+  return jm1;
+}
+
 struct ModelParams {
   double p[AGX_MAX_PARAMS];
 };
@@ -482,14 +540,14 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
           }
         } else if constexpr (MODEL == AGX_MODEL_NEO_HOOKE) {
           // displacement gradient and deformation gradient (plane strain: F33 = 1)
-          T F[SDIM][SDIM];
+          T Hg[SDIM][SDIM];
 #pragma unroll
           for (int i = 0; i < SDIM; ++i)
 #pragma unroll
-            for (int j = 0; j < SDIM; ++j) F[i][j] = group_sum<GROUP>(ua[i] * ga[j]) + (i == j ? T(1) : T(0));
-          T Fi[SDIM][SDIM];
-          const T Jdet = inverse<T, SDIM>(F, Fi);
-          const T c = lam * T(0.5) * (Jdet * Jdet - T(1)) - mu;
+            for (int j = 0; j < SDIM; ++j) Hg[i][j] = group_sum<GROUP>(ua[i] * ga[j]);
+          T Fi[SDIM][SDIM], P[SDIM][SDIM], Jdet;
+          const T jm1 = neo_hooke_stress<T, SDIM>(Hg, lam, mu, P, Fi, Jdet);
+          const T c = lam * T(0.5) * jm1 * (T(2) + jm1) - mu;
           T ha[SDIM];
 #pragma unroll
           for (int i = 0; i < SDIM; ++i) {
@@ -501,10 +559,10 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
           if constexpr (DO_R) {
 #pragma unroll
             for (int i = 0; i < SDIM; ++i) {
-              T fg = 0;
+              T pg = 0;
 #pragma unroll
-              for (int j = 0; j < SDIM; ++j) fg += F[i][j] * ga[j];
-              Ra[i] += (double)(wdet * (mu * fg + c * ha[i]));
+              for (int j = 0; j < SDIM; ++j) pg += P[i][j] * ga[j];
+              Ra[i] += (double)(wdet * pg);
             }
           }
           if constexpr (DO_K) {
@@ -889,12 +947,12 @@ neo_hooke_residual_qp(int64_t n_elem, const int32_t* __restrict__ conn, const do
     double ul[SDIM];
 #pragma unroll
     for (int c = 0; c < SDIM; ++c) ul[c] = dofs[(int64_t)node * SDIM + c];
-    // F at Gauss point l
+    // displacement gradient H = F - I at Gauss point l
     double F[SDIM][SDIM];
 #pragma unroll
     for (int i = 0; i < SDIM; ++i)
 #pragma unroll
-      for (int j = 0; j < SDIM; ++j) F[i][j] = i == j ? 1.0 : 0.0;
+      for (int j = 0; j < SDIM; ++j) F[i][j] = 0.0;
     const double* gq = geo + ((e * NQ + l) * NEN) * (SDIM + 1);
 #pragma unroll
     for (int b = 0; b < NEN; ++b) {
@@ -909,14 +967,13 @@ neo_hooke_residual_qp(int64_t n_elem, const int32_t* __restrict__ conn, const do
         for (int j = 0; j < SDIM; ++j) F[i][j] += ub[i] * g[j];
     }
     const double wdet = gq[SDIM];  // w det J at this point (stored with every node)
-    double Fi[SDIM][SDIM];
-    const double J = inverse<double, SDIM>(F, Fi);
-    const double c = lam * 0.5 * (J * J - 1.0) - mu;
+    double Fi[SDIM][SDIM], P[SDIM][SDIM], J;
+    neo_hooke_stress<double, SDIM>(F, lam, mu, P, Fi, J);
     __syncwarp();
 #pragma unroll
     for (int i = 0; i < SDIM; ++i)
 #pragma unroll
-      for (int j = 0; j < SDIM; ++j) Psh[warp][lane][i * SDIM + j] = wdet * (mu * F[i][j] + c * Fi[j][i]);
+      for (int j = 0; j < SDIM; ++j) Psh[warp][lane][i * SDIM + j] = wdet * P[i][j];
     __syncwarp();
     // R_l = sum over points q of (w det J P_q) g_l(q)
     double Rl[SDIM];
@@ -961,6 +1018,17 @@ __global__ void inverse_diagonal(int64_t n_dofs, int ndof, int64_t nnzb, const i
     const int c = (int)(d - p * ndof);
     const T v = vals[(int64_t)(c * ndof + c) * nnzb + diagpos[p]];
     dinv[d] = v != T(0) ? T(1) / v : T(0);
+  }
+}
+
+// diagonal of the assembled tangent in float64 (assemble_tangent_diagonal)
+template <typename T>
+__global__ void tangent_diagonal(int64_t n_dofs, int ndof, int64_t nnzb, const int32_t* __restrict__ diagpos,
+                                 const T* __restrict__ vals, double* __restrict__ diag) {
+  for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d < n_dofs; d += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = d / ndof;
+    const int c = (int)(d - p * ndof);
+    diag[d] = (double)vals[(int64_t)(c * ndof + c) * nnzb + diagpos[p]];
   }
 }
 
@@ -1119,6 +1187,17 @@ static void launch_grid_tangent(agx_context* ctx, agx_element_set& s, T* vals, T
     if (s.grid_affine) launch_grid_tangent_as<AGX_MODEL_POISSON_SINCOS, T, true>(ctx, s, vals, dinv);
     else launch_grid_tangent_as<AGX_MODEL_POISSON_SINCOS, T, false>(ctx, s, vals, dinv);
   }
+}
+
+void agx_launch_diagonal(agx_context* ctx, int dtype, double* diag) {
+  const int g = agx_grid(ctx, ctx->n_dofs);
+  if (dtype == AGX_F64)
+    tangent_diagonal<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dofs, ctx->ndof, ctx->nnzb, ctx->d_diagpos,
+                                                               ctx->d_vals64, diag);
+  else
+    tangent_diagonal<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dofs, ctx->ndof, ctx->nnzb, ctx->d_diagpos,
+                                                              ctx->d_vals32, diag);
+  ctx->n_launches += 1;
 }
 
 int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, int tangent_dtype) {

@@ -18,7 +18,8 @@
 // Host code cannot hand the array's name to a kernel: on the host the name is a stand-in,
 // not a device address.  The first call on a device, with that device current, looks the
 // address up with cudaGetSymbolAddress and caches it; that first call should therefore come
-// before any stream capture.
+// before any stream capture.  The address is the current device's, so the stream passed in
+// must belong to the current device (checked; a stream of another device is rejected).
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -300,6 +301,12 @@ extern "C" int agx_pcg_noalloc(const int32_t* rowptr, const int32_t* col, const 
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return fail(errbuf, errbuf_len, AGX_ERR_CUDA, cudaGetErrorString(e));
   if (dev < 0 || dev >= 256) return fail(errbuf, errbuf_len, AGX_ERR_ARG, "agx_pcg_noalloc: device index too large");
+  // the work array is looked up for the current device, so the stream must belong to it
+  int sdev = dev;
+  e = cudaStreamGetDevice((cudaStream_t)stream, &sdev);
+  if (e != cudaSuccess) return fail(errbuf, errbuf_len, AGX_ERR_CUDA, cudaGetErrorString(e));
+  if (sdev != dev)
+    return fail(errbuf, errbuf_len, AGX_ERR_ARG, "agx_pcg_noalloc: the stream belongs to another device than the current one");
   void* base = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_mu);

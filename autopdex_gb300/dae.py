@@ -266,8 +266,12 @@ class TimeSteppingManager:
             t = min(t_n + dt, t_max)
             dt = t - t_n
             settings = self.pre_step_updates(t, settings)
-            settings[self.qn_key], settings[self.dt_key] = self._backward_euler_form(history, dt)
-            q, (n_it, res, diverged) = _solver.solver(q_n, settings, self.static_settings, **self.solver_kwargs)
+            # the root solve reads the backward-Euler form of the step (q*, dt / c_0); user
+            # callbacks keep the real step and the latest accepted state
+            solve_settings = dict(settings)
+            solve_settings[self.qn_key], solve_settings[self.dt_key] = self._backward_euler_form(history, dt)
+            settings[self.qn_key], settings[self.dt_key] = q_n, dt
+            q, (n_it, res, diverged) = _solver.solver(q_n, solve_settings, self.static_settings, **self.solver_kwargs)
             converged = not bool(diverged)
             order = min(i.order for i in self.integrators.values())
             ctrl = self.step_size_controller.compute_scaler(None, q, q_n, ctrl, order, converged, int(n_it), dt,
@@ -276,6 +280,7 @@ class TimeSteppingManager:
             if ctrl.accept and not ctrl.interrupt:
                 q_n = q
                 history = [q] + history[:-1]
+                settings[self.qn_key] = q
                 user = self.postprocessing_fun(lambda tt: q, t, settings)
                 settings = self.post_step_updates(lambda tt: q, t, settings)
                 hist = self.save_policy.save_step(hist, t, q, user) if self.save_policy else hist

@@ -212,6 +212,21 @@ def adaptive_load_stepping(dofs, settings, static_settings,
     return dofs, multiplier, increment, load_step, settings, res
 
 
+def _checked_solve(prob, rhs, x, opts, what):
+    """agx_solve that raises when the Krylov solve stops without meeting its tolerance
+    (iteration limit, breakdown on an indefinite tangent, non-finite values): a derivative from
+    an unconverged solve would be returned as if it were exact."""
+    info = N.SolveInfo()
+    rc = prob._call("agx_solve", N.C.c_void_p(rhs.data_ptr()), N.C.c_void_p(x.data_ptr()), N.C.byref(opts),
+                    N.C.byref(info))
+    if rc != N.AGX_OK or info.status != N.AGX_OK:
+        kind = "diverged (breakdown or non-finite values)" if N.AGX_DIVERGED in (rc, info.status) else \
+            "did not converge"
+        raise RuntimeError(f"the linear solve of the {what} {kind}: {info.iterations} iterations, relative "
+                           f"residual {info.rel_residual:.3e} against a tolerance of {opts.rtol:.1e}")
+    return info
+
+
 def sensitivities(dofs, settings, static_settings, params, rel_step=1e-6, krylov_tol=1e-12, **kwargs):
     """Forward-mode implicit derivatives du/dp of a converged solution with respect to scalar
     settings entries (the 'forward' implicit differentiation of adaptive_load_stepping,
@@ -248,9 +263,7 @@ def sensitivities(dofs, settings, static_settings, params, rel_step=1e-6, krylov
         prob._call("agx_assemble", N.C.c_void_p(x.data_ptr()), None, N.AGX_F64)
         rhs = torch.where(m, torch.zeros_like(dR), -dR)
         du = torch.empty_like(x)
-        info = N.SolveInfo()
-        prob._call("agx_solve", N.C.c_void_p(rhs.data_ptr()), N.C.c_void_p(du.data_ptr()), N.C.byref(opts),
-                   N.C.byref(info))
+        _checked_solve(prob, rhs, du, opts, f"du/d{key}")
         out[key] = _out_like(du, dofs, prob.key)
     return out
 
@@ -286,9 +299,7 @@ class _DeviceOps:
         self.prob.update_models(self.settings)
         self.prob._call("agx_assemble", N.C.c_void_p(self.u.data_ptr()), None, N.AGX_F64)
         x = torch.empty_like(rhs)
-        info = N.SolveInfo()
-        self.prob._call("agx_solve", N.C.c_void_p(rhs.data_ptr()), N.C.c_void_p(x.data_ptr()),
-                        N.C.byref(self.opts), N.C.byref(info))
+        _checked_solve(self.prob, rhs, x, self.opts, "implicit differentiation")
         return x
 
 

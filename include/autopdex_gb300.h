@@ -186,6 +186,10 @@ int agx_spmv(agx_context* ctx, int dtype, const void* x, void* y);
 /* y = K x with the library's pattern and caller-provided values in the library's layout
    (entry-major planes, as agx_copy_values writes them): products with stored tangents. */
 int agx_spmv_values(agx_context* ctx, int dtype, const void* values, const void* x, void* y);
+/* Diagonal of the last assembled tangent of `dtype` as float64 (n_dofs, DEVICE pointer):
+   assemble_tangent_diagonal (assembler.py:639-680, :1090-1113); identity entries on
+   eliminated Dirichlet DOFs. */
+int agx_get_diagonal(agx_context* ctx, int dtype, double* diag);
 /* Raw copy of the last assembled tangent values in the library's layout (nnzb*ndof*ndof). */
 int agx_copy_values(agx_context* ctx, int dtype, void* values);
 /* z = D^-1 r with the diagonal of the last assembled tangent of `dtype` (Jacobi,
@@ -239,9 +243,10 @@ int agx_profile_read(agx_context* ctx, double* ms, int64_t* launches);
    live in a fixed file-scope device array of AGX_NOALLOC_MAX_DOFS DOFs (10 MiB, reserved on
    every device that loads the library until the process exits); larger systems are
    rejected with AGX_ERR_ARG and a message in errbuf (nullable).  The first call on a device
-   looks the array's address up (call it once before any stream capture).  All calls share
-   the array: calls that overlap on the GPU race.  Returns AGX_OK, AGX_NOT_CONVERGED,
-   AGX_DIVERGED or a negative error. */
+   looks the array's address up (call it once before any stream capture).  The stream must
+   belong to the current device (another device's stream is rejected with AGX_ERR_ARG).  All
+   calls share the array: calls that overlap on the GPU race.  Returns AGX_OK,
+   AGX_NOT_CONVERGED, AGX_DIVERGED or a negative error. */
 #define AGX_NOALLOC_MAX_DOFS 262144
 int agx_pcg_noalloc(const int32_t* rowptr, const int32_t* col, const double* vals, int64_t n_nodes, int ndof,
                     const double* rhs, double* x, double rtol, int maxiter, void* cuda_stream,

@@ -135,3 +135,23 @@ def test_bdf_startup_history_and_order(monkeypatch):
             st = dae.TimeSteppingManager(static).run({"T": np.ones(1)}, dt, 1.0, 400)
             errs.append(abs(st.q["T"][0] - np.exp(-LAM)))
         assert 1.9 < errs[0] / errs[1] < 2.1 and 1.9 < errs[1] / errs[2] < 2.1, errs
+
+
+def test_callbacks_see_the_real_step_and_state(monkeypatch):
+    """For a k-step BDF the root solve reads (q*, dt / c_0); postprocessing and post-step
+    callbacks see the real step and the accepted state instead."""
+    log, seen = [], []
+    _fake_be_form(monkeypatch, log)
+    static = _static()
+    static["time integrators"] = {"T": dae.BackwardDiffFormula(2)}
+
+    def post(q_fun, t, settings):
+        seen.append((t, settings["time increment"], np.asarray(settings["dofs n"]["T"]).copy(),
+                     np.asarray(q_fun(t)["T"]).copy()))
+        return settings
+    dae.TimeSteppingManager(static, post_step_updates=post).run({"T": np.ones(1)}, 0.1, 0.3, 3)
+    assert len(seen) == 3
+    c0 = dae.BackwardDiffFormula(2).coeffs[0]
+    for (t, dt, qn, q), (q_star, dt_eff) in zip(seen, log):
+        assert np.isclose(dt, 0.1) and np.isclose(dt_eff, 0.1 / c0)
+        assert np.array_equal(qn, q)  # the accepted state, not the synthetic q*
