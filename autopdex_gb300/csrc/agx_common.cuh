@@ -155,6 +155,16 @@ struct agx_context {
   int precond_capturable = 0;  // the callback only enqueues work on the stream it is given
   int64_t precond_gen = 0;     // bumped whenever the callback or its mode changes
   int spmv_tpr[2] = {0, 0};  // lanes per block row of the Krylov product, float64 / float32 (0: default)
+
+  // banded Cholesky factor of the float64 tangent (AGX_CHOL_BAND): lower band stored by
+  // columns, entry (j + k, j) at d_band[j (band_w + 1) + k], k = 0 .. band_w
+  int64_t band_w = -1;          // half bandwidth in DOFs of the pattern (-1: not computed yet)
+  double* d_band = nullptr;     // n_dofs * (band_w + 1)
+  int* d_band_err = nullptr;    // first column whose pivot was not positive (+1), 0 if none
+  double* d_band_l11 = nullptr; // factored diagonal block of the current panel (scratch)
+  int64_t band_gen = -1;        // tangent generation the factor belongs to
+  double band_sign = 1.0;       // the factor is of band_sign * K (-1 for negative definite tangents)
+  size_t band_max_bytes = (size_t)24 << 30;  // largest factor this context allocates
 };
 
 // ------------------------------------------------------------------------------------
@@ -188,6 +198,8 @@ int agx_spmv_values_impl(agx_context* ctx, int dtype, const void* values, const 
 void agx_launch_jacobi(agx_context* ctx, int dtype, const void* r, void* z);
 void agx_launch_diagonal(agx_context* ctx, int dtype, double* diag);
 int agx_autotune_spmv(agx_context* ctx, int* chosen, float* best_ms);
+int agx_band_solve_impl(agx_context* ctx, const double* b, double* x, const agx_solve_opts* opts,
+                        agx_solve_info* info);
 void agx_launch_planes_to_blocks(agx_context* ctx, const double* planes, double* blocks);
 void agx_launch_planes_to_blocks(agx_context* ctx, const float* planes, float* blocks);
 

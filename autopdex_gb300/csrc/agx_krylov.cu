@@ -1144,6 +1144,7 @@ int update_chebyshev_bound(agx_context* ctx) {
 }
 
 int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_solve_opts* opts, agx_solve_info* info) {
+  if (opts->method == AGX_CHOL_BAND) return agx_band_solve_impl(ctx, rhs, x, opts, info);
   const int64_t n = ctx->n_dofs;
   const int g = ctx->vec_blocks;  // reducing vector kernels
   const int gv = agx_grid(ctx, n);

@@ -10,7 +10,11 @@ Keys read from ``static_settings`` (besides AutoPDEx's own):
 
 * ``'solver'``: ``'pcg'`` / ``'cg'`` (Jacobi-PCG, default), ``'bicgstab'`` (non-symmetric
   tangents), ``'fcg'`` (flexible CG for the learned preconditioner); the direct-solver names
-  ``'lapack'`` / ``'umfpack'`` / ``'direct'`` run Jacobi-PCG to a relative residual of 1e-13.
+  ``'lapack'`` / ``'umfpack'`` / ``'direct'`` / ``'cholesky'`` factor the float64 tangent
+  (banded Cholesky on the GPU, refined to a relative residual of 1e-13) -- the role of
+  spsolve in linear_solve_scipy (solver.py:1493-1539) -- for symmetric tangents (potentials,
+  hyperelastic elements) on meshes with a narrow band; the non-symmetric backward-Euler
+  residual model runs float64 BiCGStab to 1e-13 instead.
 * ``'precision'``: ``'float64'`` (default) or ``'mixed'`` (float32 tangent and Krylov
   iterations inside the float64 Newton / refinement loop).
 * ``'type of preconditioner'``: ``'jacobi'`` (default) or ``'learned'`` (the network set with
@@ -38,7 +42,10 @@ def _method(static_settings, kwargs):
     precision = static_settings.get("precision", "float64")
     precond = static_settings.get("type of preconditioner", "jacobi")
     direct = name in ("lapack", "umfpack", "direct", "lu", "cholesky")
-    if name in ("pcg", "cg") or direct:
+    symmetric = all(getattr(m, "kernel", None) != N.AGX_MODEL_HEAT_BE for m in static_settings.get("model", ()))
+    if direct:
+        method = N.AGX_CHOL_BAND if symmetric else N.AGX_BICGSTAB
+    elif name in ("pcg", "cg"):
         method = N.AGX_PCG_MIXED if precision == "mixed" else N.AGX_PCG
     elif name == "bicgstab":
         if precision == "mixed":

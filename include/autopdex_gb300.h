@@ -88,6 +88,12 @@ extern "C" {
 #define AGX_BICGSTAB 2   /* Jacobi-BiCGStab in float64, for non-symmetric tangents */
 #define AGX_FCG_MIXED 3  /* flexible CG in float32 with the registered preconditioner
                             (agx_set_preconditioner), Jacobi when none is registered */
+#define AGX_CHOL_BAND 4  /* direct: banded Cholesky of the float64 tangent with float64
+                            refinement to rtol (the 'lapack' / 'umfpack' spsolve of
+                            linear_solve_scipy, solver.py:1493-1539) for symmetric definite
+                            tangents whose band fits in memory (structured 2-D meshes);
+                            AGX_ERR_UNSUPPORTED otherwise, AGX_DIVERGED when a pivot is not
+                            positive */
 
 typedef struct agx_context agx_context;
 
@@ -96,7 +102,7 @@ typedef struct agx_context agx_context;
 typedef int (*agx_precond_fn)(void* user, const float* r, float* z, int64_t n, void* stream);
 
 typedef struct {
-  int method;          /* AGX_PCG, AGX_PCG_MIXED, AGX_BICGSTAB, AGX_FCG_MIXED */
+  int method;          /* AGX_PCG, AGX_PCG_MIXED, AGX_BICGSTAB, AGX_FCG_MIXED, AGX_CHOL_BAND */
   double rtol;         /* stop when ||r|| <= rtol ||b|| (jax.scipy cg semantics, solver.py:1116) */
   double atol;         /* ... or ||r|| <= atol */
   int maxiter;
@@ -232,6 +238,7 @@ int agx_set_preconditioner_mode(agx_context* ctx, int mode, double omega, int sw
 #define AGX_PROF_SPMV 2      /* sparse products of the Krylov iterations */
 #define AGX_PROF_VECTOR 3    /* Krylov vector updates with their reductions */
 #define AGX_PROF_PRECOND 4   /* preconditioner applications */
+#define AGX_PROF_FACTOR 5    /* direct factorizations */
 #define AGX_PROF_CATEGORIES 8
 int agx_profile(agx_context* ctx, int enable);
 int agx_profile_read(agx_context* ctx, double* ms, int64_t* launches);
