@@ -25,7 +25,7 @@ AGX_F64, AGX_F32 = 0, 1
 AGX_PCG, AGX_PCG_MIXED, AGX_BICGSTAB, AGX_FCG_MIXED, AGX_CHOL_BAND = 0, 1, 2, 3, 4
 
 AGX_PROF_TANGENT, AGX_PROF_RESIDUAL, AGX_PROF_SPMV, AGX_PROF_VECTOR, AGX_PROF_PRECOND = 0, 1, 2, 3, 4
-AGX_PROF_FACTOR = 5
+AGX_PROF_FACTOR, AGX_PROF_SMOOTH = 5, 6
 AGX_PROF_CATEGORIES = 8
 AGX_NOALLOC_MAX_DOFS = 262144
 

@@ -21,7 +21,7 @@
 // Solves: one CTA walks blocks of NB rows -- forward substitution with column updates of the
 // rows below, backward substitution with per-column dot products of the rows below -- and the
 // result is refined with the float64 product until ||b - K x|| <= rtol ||b|| (at most three
-// steps).
+// steps, fewer once a step no longer halves the residual).
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -413,8 +413,11 @@ int agx_band_solve_impl(agx_context* ctx, const double* b, double* x, const agx_
     ctx->n_launches += 2;
     double rr = 0.0;
     if (int rc = agx_residual_norm(ctx, ctx->d_v, &rr, &nf)) return rc;
+    const double prev = rel;
     rel = bb > 0.0 ? std::sqrt(rr / bb) : 0.0;
-    if (!(rel > rtol) || it == 3 || nf > 0) break;
+    // done, or refinement no longer gains (the float64 residual of an ill-conditioned system
+    // stagnates near eps ||K|| ||x|| / ||b||)
+    if (!(rel > rtol) || it == 3 || nf > 0 || (it > 0 && rel > 0.5 * prev)) break;
     scale_copy<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_v, ctx->d_v, sg);
     forward_backward(ctx, ctx->d_v);
     add_scaled<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, x, ctx->d_v, 1.0);

@@ -1061,6 +1061,7 @@ int apply_registered_preconditioner(agx_context* ctx) {
   const int gv = agx_grid(ctx, n);
   auto* sc = ctx->d_scal;
   if (ctx->precond_mode == 0) {
+    agx_prof_scope pn(ctx, AGX_PROF_PRECOND);
     if (ctx->precond(ctx->precond_user, ctx->f_r, ctx->f_z, n, ctx->stream) != 0) return -1;
     zero_prescribed<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir, ctx->d_dir_dofs,
                                                                                    ctx->f_z);
@@ -1093,23 +1094,44 @@ int apply_registered_preconditioner(agx_context* ctx) {
     }
   }
   float *rc = ctx->f_w2, *t = ctx->f_w1, *y = ctx->f_w3, *dz = ctx->f_w4;
+  // profiling categories: the products under AGX_PROF_SMOOTH, the element-wise kernels under
+  // AGX_PROF_VECTOR, the registered callback (the network) under AGX_PROF_PRECOND
+  auto smooth_product = [&](const float* in, float* out) {
+    agx_prof_scope pp(ctx, AGX_PROF_SMOOTH);
+    agx_spmv_impl(ctx, AGX_F32, in, out);
+  };
   for (int s = 0; s < nu; ++s) {
-    tl_sweep<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv32, cb[s], ca[s], s == 0 ? ctx->f_r : rc, rc,
-                                                s == 0 ? nullptr : t, ctx->f_z, dz, s == 0, sc);
-    agx_spmv_impl(ctx, AGX_F32, dz, t);
+    {
+      agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
+      tl_sweep<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv32, cb[s], ca[s], s == 0 ? ctx->f_r : rc, rc,
+                                                  s == 0 ? nullptr : t, ctx->f_z, dz, s == 0, sc);
+    }
+    smooth_product(dz, t);
   }
-  tl_residual<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, rc, t, sc);
-  if (ctx->precond(ctx->precond_user, rc, y, n, ctx->stream) != 0) return -1;
-  zero_prescribed<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir, ctx->d_dir_dofs, y);
-  agx_spmv_impl(ctx, AGX_F32, y, t);
-  tl_step<<<ctx->vec_blocks, AGX_BLOCK, 0, ctx->stream>>>(n, rc, y, t, sc, ctx->d_partials, ctx->d_counter);
-  tl_combine<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_z, y, rc, t, sc);
+  {
+    agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
+    tl_residual<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, rc, t, sc);
+  }
+  {
+    agx_prof_scope pn(ctx, AGX_PROF_PRECOND);
+    if (ctx->precond(ctx->precond_user, rc, y, n, ctx->stream) != 0) return -1;
+    zero_prescribed<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir, ctx->d_dir_dofs, y);
+  }
+  smooth_product(y, t);
+  {
+    agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
+    tl_step<<<ctx->vec_blocks, AGX_BLOCK, 0, ctx->stream>>>(n, rc, y, t, sc, ctx->d_partials, ctx->d_counter);
+    tl_combine<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_z, y, rc, t, sc);
+  }
   ctx->n_launches += 2 * nu + 5;
   if (ctx->precond_mode >= 2) {
     for (int s = 0; s < nu; ++s) {
-      tl_sweep<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv32, cb[s], ca[s], rc, rc, s == 0 ? nullptr : t,
-                                                  ctx->f_z, dz, 0, sc);
-      if (s + 1 < nu) agx_spmv_impl(ctx, AGX_F32, dz, t);
+      {
+        agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
+        tl_sweep<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv32, cb[s], ca[s], rc, rc, s == 0 ? nullptr : t,
+                                                    ctx->f_z, dz, 0, sc);
+      }
+      if (s + 1 < nu) smooth_product(dz, t);
     }
     ctx->n_launches += 2 * nu - 1;
   }
@@ -1223,10 +1245,7 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
             fcg_update_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, ctx->f_r, pnew, ctx->f_q, sc,
                                                                       ctx->d_partials, ctx->d_counter);
           }
-          {
-            agx_prof_scope pp(ctx, AGX_PROF_PRECOND);
-            if (apply_registered_preconditioner(ctx) != 0) precond_failed = true;
-          }
+          if (apply_registered_preconditioner(ctx) != 0) precond_failed = true;
           fcg_direction_dots<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_r, ctx->f_z, ctx->f_q, sc,
                                                                      ctx->d_partials, ctx->d_counter);
         }

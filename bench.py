@@ -1,18 +1,35 @@
-"""Benchmark of the GB300 solve backend on the 3-D neo-Hooke cube (64^3 Q1 bricks).
+"""Benchmark of the GB300 solve backend on the workloads of AutoPDEx's Newton solve path.
 
-Workload: 64^3 Q1 bricks (274,625 nodes, 823,875 DOFs), E = 1, nu = 0.3, x = 0 clamped,
-u_x prescribed on x = 1.  One step = one load-step solve (load step 1 of 10, u_x = 0.03)
-to a float64 Newton residual of 1e-10 times the first one, i.e. one ``solver.solver``
-call, started from the linear lifting u_x = 0.03 x of the prescribed values (from u = 0 the
-first element layer is stretched threefold at h = 1/64 and undamped Newton, the
-reference's algorithm, diverges).  Metric: time to the 1e-10 relative residual (s, lower is
-better) of the mixed-precision path (float32 tangent and Jacobi-PCG inside the float64
-Newton/refinement loop); the plain float64 Jacobi-PCG path is timed beside it.  The
-64^3 problem (~0.3 GB of float32 matrix, 0.6 GB float64) exceeds the 129 MB L2, so no
-flush is needed between steps.
+Headline (``value``): time to a 1e-10 relative float64 residual of the learned + mixed-precision
+solve of the 1024^2 random-conductivity heat problem -- flexible CG in float32 with the U-Net
+two-level preconditioner inside the float64 Newton / refinement loop -- through
+``solver.solver`` with device-resident inputs; the plain float64 Jacobi-PCG solve of the same
+problem is timed beside it (the metric compares the two).  One step = one solve from zero.
+The problem's matrix and vectors exceed the 129 MB L2 only in part (88 MB of float32 values),
+so a 256 MB buffer is written before every timed step.
 
---impl reference times the CPU oracle (float64 NumPy/SciPy/torch.func restatement of the
-reference path) on a bounded sample of the same workload and scales it to one load step.
+``e2e``: the same solve through solver.solver with host NumPy inputs and outputs (the host to
+device copies of the DOFs and prescribed values and the device to host copy of the solution
+inside the timed region).
+
+Sub-records (``configs``), each with its error against the float64 oracle:
+  poisson_200       200^2 Q1 Poisson, one Newton step with the direct (banded Cholesky) solve
+  neo_hooke_64cube  64^3 neo-Hooke cube, all 10 load steps, mixed precision and plain float64
+  cook_512          512^2 Cook membrane (nu = 0.4999), load steps of the 20, float64 direct and
+                    plain float64 Jacobi-PCG
+  heat_1024         the headline problem: plain float64, mixed and learned + mixed
+  heat_be_128cube   128^3 backward-Euler heat, time steps with mixed Jacobi-PCG and float64
+                    BiCGStab
+``roofline``: the dominant kernel of the headline solve (per-category CUDA-event times from a
+separate profiled pass; the timed region runs with CUDA graphs and no instrumentation).
+``assembly_hbm``: the float32 tangent assembly of the 1024^2 and 2048^2 heat meshes.
+``cpu_baseline``: the oracle's C restatement (C elements, SciPy COO -> CSR with Dirichlet
+deletion as scipy_assembling does, OpenMP Jacobi-PCG to the same 1e-10) on the full 1024^2
+problem, timed on the host's cores.
+
+``--impl reference`` times that CPU path (the reference itself is JAX code and no JAX exists
+offline) on the headline's workload, one full solve per step.
+``--case conv|assembly|solve`` runs one small case for ncu captures (no JSON line).
 """
 import argparse
 import json
@@ -28,15 +45,21 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+RTOL = 1e-10
+TRAIN_N = 256  # resolution the shipped heat network was trained on (heat_unet_n256.npz)
+
+# DRAM traffic per launch of the dominant kernels (dram__bytes_read.sum + dram__bytes_write.sum,
+# one ncu capture each; the commands are in the named profile summaries)
+NCU_TRAFFIC = {}
 
 
 def _peaks():
     try:
         with open(PEAKS) as fh:
             p = json.load(fh)
-        return float(p["hbm_gbs"]), "measured"
+        return float(p["hbm_gbs"]), float(p.get("bf16_tflops", 1941.6)), "measured"
     except Exception:
-        return 6800.0, "fallback"
+        return 6800.0, 1900.0, "fallback"
 
 
 class Clocks:
@@ -47,7 +70,6 @@ class Clocks:
         self.path = os.path.join(tempfile.gettempdir(), f"agx_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -80,275 +102,483 @@ class Clocks:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "error": str(e)}
 
 
-def _solve_once(w, static, newton_rtol, x0=None, profile_ctx=None):
-    from autopdex_gb300 import solver
-    st = dict(w.settings)
-    st = w.steps[0](st)
-    sol, info = solver.solver(w.dofs if x0 is None else x0, st, static, newton_tol=0.0, newton_rtol=newton_rtol,
-                              maxiter=30)
-    return sol, info
-
-
-def gpu_arm(args):
+# ---- helpers -------------------------------------------------------------------------------
+def _sync():
     import torch
+    torch.cuda.synchronize()
+
+
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def _flat(d):
+    a = next(iter(d.values())) if isinstance(d, dict) else d
+    if hasattr(a, "detach"):
+        a = a.detach().cpu().numpy()
+    return np.asarray(a, dtype=np.float64).reshape(-1)
+
+
+def _info():
+    from autopdex_gb300 import solver
+    li = solver.last_info
+    return {"newton": int(li.iterations), "krylov": int(li.krylov_iterations), "res0": float(li.res0),
+            "res": float(li.res_norm), "residual_ratio": (li.res_norm / li.res0) if li.res0 else 0.0,
+            "diverged": bool(li.diverged)}
+
+
+def _timed(fn):
+    """CUDA-event time (s) of fn() on torch's current stream (the library's stream)."""
+    a, b = _events()
+    _sync()
+    a.record()
+    out = fn()
+    b.record()
+    _sync()
+    return a.elapsed_time(b) / 1e3, out
+
+
+def _profile(prob, fn):
+    """Per-category kernel times (ms) and launch counts of fn() with the library's events on
+    (CUDA graphs are not used while profiling)."""
     import ctypes as C
-    from autopdex_gb300 import configs, solver, _native as N
-    from autopdex_gb300._problem import get_problem
-
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    n = args.size
-    w = configs.neo_hooke_cube(n=n, n_steps=10)
-    mixed = dict(w.static_settings, precision="mixed", solver="pcg")
-    plain = dict(w.static_settings, precision="float64", solver="pcg")
-    rtol = 1e-10
-    kw = dict(krylov_tol=args.krylov_tol)
-
-    # device-resident inputs: dofs and prescribed values already on the GPU
-    st = w.steps[0](dict(w.settings))
-    prob = get_problem(w.dofs, st, mixed)
-    dev = prob.device
-    x0_host = np.zeros((w.n_dofs // 3, 3))
-    x0_host[:, 0] = w.raw["stretch"] / w.raw["n_steps"] * w.raw["coords"][:, 0]
-    x0_host = x0_host.reshape(-1)
-    g_dev = torch.as_tensor(np.asarray(st["dirichlet conditions"], dtype=np.float64).reshape(-1), device=dev)
-    st_dev = dict(st)
-    st_dev["dirichlet conditions"] = g_dev.reshape(-1, 3)
-    x0_dev = torch.as_tensor(x0_host.reshape(-1, 3), device=dev)
-
-    def run_dev(static, **over):
-        k = dict(kw, **over)
-        return solver.solver(x0_dev, st_dev, static, newton_tol=0.0, newton_rtol=rtol, maxiter=30, **k)
-
-    for _ in range(args.warmup):
-        run_dev(mixed)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    lib = N.load()
-    l0 = C.c_int64()
-    prob._call("agx_launch_count", C.byref(l0))
+    from autopdex_gb300 import _native as N
     prob._call("agx_profile", 1)
-    stream = torch.cuda.current_stream()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    infos = []
-    with Clocks() as clk:
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(args.steps):
-            sol, info = run_dev(mixed)
-            infos.append((info, solver.last_info.krylov_iterations))
-        e1.record(stream)
-        torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    t_ms = e0.elapsed_time(e1)
-    ms = (C.c_double * N.AGX_PROF_CATEGORIES)()
-    cnt = (C.c_int64 * N.AGX_PROF_CATEGORIES)()
-    prob._call("agx_profile_read", ms, cnt)
-    prob._call("agx_profile", 0)
-    l1 = C.c_int64()
-    prob._call("agx_launch_count", C.byref(l1))
-    if dist:
-        from autopdex_gb300 import replicas
-        t_ms = replicas.max_over_ranks(t_ms, device=dev)
-    per_step_s = t_ms / 1e3 / args.steps
-
-    # verify the solution of the last timed step: float64 residual ratio
-    res0 = solver.last_info.res0
-    res_end = solver.last_info.res_norm
-
-    # plain float64 Jacobi-PCG on the same step, beside the headline: (a) with the same inner
-    # tolerance schedule as the mixed path, (b) with inner solves to 1e-11 (direct-solve accuracy)
-    def timed(static, **over):
-        run_dev(static, **over)
-        torch.cuda.synchronize()
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        _, inf = run_dev(static, **over)
-        b.record(stream)
-        torch.cuda.synchronize()
-        return a.elapsed_time(b) / 1e3, inf, solver.last_info.krylov_iterations
-    if args.only_mixed:
-        plain_s, info_p, plain_kry = float("nan"), (0, 0.0, False), 0
-        tight_s, info_t, tight_kry = float("nan"), (0, 0.0, False), 0
-    else:
-        plain_s, info_p, plain_kry = timed(plain)
-        tight_s, info_t, tight_kry = timed(plain, krylov_tol=1e-11)
-
-    # end to end through the public API with host buffers (H2D of the inputs, D2H of the result)
-    def run_host():
-        s = dict(st)
-        return solver.solver(x0_host.reshape(-1, 3), s, mixed, newton_tol=0.0, newton_rtol=rtol, maxiter=30, **kw)
-    if not args.only_mixed:
-        run_host()
-    torch.cuda.synchronize()
-    k_e2e = 0 if args.only_mixed else max(1, min(args.steps, 3))
-    t0 = time.perf_counter()
-    for _ in range(k_e2e):
-        out_host, _ = run_host()
-    torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / max(1, k_e2e)
-
-    # roofline of the dominant kernel (largest category)
-    cats = {"tangent_assembly": N.AGX_PROF_TANGENT, "residual_assembly": N.AGX_PROF_RESIDUAL,
-            "spmv": N.AGX_PROF_SPMV, "krylov_vector": N.AGX_PROF_VECTOR}
-    shares = {k: ms[v] for k, v in cats.items()}
-    launches = {k: int(cnt[v]) for k, v in cats.items()}
-    b = 3
-    nnzb = prob.nnzb
-    n_nodes = w.n_dofs // 3
-    # fused product: matrix planes + columns + rowptr; reads z and p_old, writes p_new and q
-    spmv_bytes = nnzb * (b * b * 4 + 4) + (n_nodes + 1) * 4 + 4 * w.n_dofs * 4
-    spmv_avg_ms = ms[N.AGX_PROF_SPMV] / max(1, cnt[N.AGX_PROF_SPMV])
-    peak, peak_kind = _peaks()
-    achieved = spmv_bytes / (spmv_avg_ms * 1e-3) / 1e9
-    traffic = None
-    tr_path = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tr_path):
-        try:
-            traffic = json.load(open(tr_path)).get("spmv_f32_bsr3_64cube_bytes_per_launch")
-        except Exception:
-            traffic = None
-    # element tangent pass: algorithmic bytes (coords, dofs, conn, scatter map, float32 values)
-    n_e = n ** 3
-    asm_bytes = n_nodes * 3 * 8 + w.n_dofs * 8 + n_e * 8 * 4 + n_e * 64 * 4 + nnzb * 9 * 4
-    asm_avg_ms = ms[N.AGX_PROF_TANGENT] / max(1, cnt[N.AGX_PROF_TANGENT])
-    # The 3-D neo-Hooke tangent is bound by arithmetic, not bytes: an analytic count of the
-    # float32 kernel's flops, per lane (8 per element) and Gauss point (8): Jacobian by group
-    # sums, its inverse and the gradients ~100, shape functions ~15, F, F^-1 and F^-T g ~110,
-    # the 8 rows of 3 x 3 tangent entries ~83 each -> ~890; against the measured FP32 rate.
-    asm_flops = n_e * 8 * 8 * (100 + 15 + 110 + 8 * 83)
-    fp32_peak_tflops = 69.8  # FMA-chain probe on this GPU (2 flops per FMA)
-
-    line = {
-        "metric": "time_to_1e-10_relative_fp64_residual (64^3 neo-Hooke cube, load step 1 of 10)",
-        "value": per_step_s,
-        "unit": "s",
-        "n_gpus": world,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": per_step_s * 1e3,
-        "higher_is_better": False,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f32 tangent/SpMV + f64 residual",
-        "data": "synthetic (structured meshes of the workloads; no dataset)",
-        "config": {"workload": f"neo_hooke_cube_{n}^3_hex8_load_step_1", "n_dofs": w.n_dofs, "nnz": nnzb * 9,
-                   "newton_rtol": rtol, "krylov": "jacobi-pcg f32 (rtol %.0e)" % args.krylov_tol,
-                   "l2": "working set > 129 MB L2 (no flush needed)", "parallelism": "replicas" if world > 1 else "1 gpu",
-                   "krylov_chunks": "CUDA graphs of 32 iterations", "spmv_lanes_per_row": "autotuned"},
-        "plain_fp64_pcg_s": plain_s,
-        "speedup_mixed_vs_plain_fp64": plain_s / per_step_s,
-        "plain_fp64_pcg_tight_s": tight_s,
-        "newton_iterations": int(infos[-1][0][0]),
-        "newton_iterations_plain_fp64": int(info_p[0]),
-        "newton_iterations_plain_fp64_tight": int(info_t[0]),
-        "krylov_iterations_mixed": int(infos[-1][1]),
-        "krylov_iterations_plain_fp64": int(plain_kry),
-        "krylov_iterations_plain_fp64_tight": int(tight_kry),
-        "converged": bool(not infos[-1][0][2]) and (res_end <= rtol * res0 * 1.0000001),
-        "final_residual_ratio": res_end / res0 if res0 else None,
-        "kernel_ms_per_step": {k: v / args.steps for k, v in shares.items()},
-        "kernel_launches_per_step": {k: v / args.steps for k, v in launches.items()},
-        "roofline": {"bound": "hbm", "kernel": f"spmv_dot_kernel<float,3,{getattr(prob, 'spmv_tpr', 8)}> "
-                                                "(BSR 3x3 SpMV, direction update, dot)",
-                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": traffic, "algorithmic_bytes": spmv_bytes,
-                     "avg_launch_ms": spmv_avg_ms},
-        "assembly": {"kernel": "element_kernel<HEX8,NEO_HOOKE,float> (tangent pass)",
-                     "algorithmic_bytes": asm_bytes, "avg_launch_ms": asm_avg_ms,
-                     "achieved_gbs": asm_bytes / (asm_avg_ms * 1e-3) / 1e9 if asm_avg_ms else None,
-                     "flops_estimate": asm_flops,
-                     "achieved_tflops": asm_flops / (asm_avg_ms * 1e-3) / 1e12 if asm_avg_ms else None,
-                     "fp32_peak_tflops": fp32_peak_tflops,
-                     "frac_fp32_peak": asm_flops / (asm_avg_ms * 1e-3) / 1e12 / fp32_peak_tflops if asm_avg_ms else None},
-        "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 2 * w.n_dofs * 8,
-                "d2h_bytes_per_step": w.n_dofs * 8},
-        "gpu_launches": int(l1.value - l0.value),
-        "clocks": clk.summary(),
-    }
-    if rank == 0 and not args.only_mixed:
-        try:
-            line["assembly_hbm"] = assembly_roofline()
-            line["assembly_hbm_2048"] = assembly_roofline(n=2048)  # values (151 MB) larger than L2
-        except Exception as e:  # noqa: BLE001 -- reported, the headline stands
-            line["assembly_hbm"] = {"error": str(e)[:200]}
-    if rank == 0 and not args.only_mixed and not args.no_learned:
-        try:
-            line["heat_learned"] = heat_learned(n=args.learned_n)
-        except Exception as e:  # noqa: BLE001 -- reported, the headline stands
-            line["heat_learned"] = {"error": str(e)[:200]}
-    if rank == 0 and args.more_workloads:
-        try:
-            line["other_workloads"] = other_workloads()
-        except Exception as e:  # noqa: BLE001 -- reported, the headline stands
-            line["other_workloads"] = {"error": str(e)[:300]}
-    if rank == 0 and not args.no_cpu_baseline and not args.only_mixed:
-        try:
-            line["cpu_baseline"] = cpu_baseline(n, int(info_t[0]), int(tight_kry), budget_s=args.cpu_budget)
-        except Exception as e:  # noqa: BLE001 -- reported, the headline stands
-            line["cpu_baseline"] = {"error": str(e)[:300]}
-    if dist:
-        dist.destroy_process_group()
-    if rank == 0:
-        print(json.dumps(line))
+    try:
+        fn()
+        _sync()
+        ms = (C.c_double * N.AGX_PROF_CATEGORIES)()
+        cnt = (C.c_int64 * N.AGX_PROF_CATEGORIES)()
+        prob._call("agx_profile_read", ms, cnt)
+    finally:
+        prob._call("agx_profile", 0)
+    names = {N.AGX_PROF_TANGENT: "tangent_assembly", N.AGX_PROF_RESIDUAL: "residual_assembly",
+             N.AGX_PROF_SPMV: "krylov_product", N.AGX_PROF_VECTOR: "krylov_vector",
+             N.AGX_PROF_PRECOND: "network", N.AGX_PROF_FACTOR: "factorization", N.AGX_PROF_SMOOTH: "smoothing_product"}
+    return {v: float(ms[k]) for k, v in names.items()}, {v: int(cnt[k]) for k, v in names.items()}
 
 
-TRAIN_N = 256  # resolution the shipped network was trained on (heat_unet_n256.npz)
+def _launches(prob):
+    import ctypes as C
+    v = C.c_int64()
+    prob._call("agx_launch_count", C.byref(v))
+    return int(v.value)
 
 
-def heat_learned(n=1024, seed=10000, rtol=1e-10):
-    """Heat conduction with k = exp(GRF) on n x n Q1 quads: time to a 1e-10 relative float64 residual for
-    plain float64 Jacobi-PCG, mixed Jacobi-PCG and the learned preconditioner in mixed FCG."""
+def _flush_buffer():
+    import torch
+    return torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+
+# ---- the headline: 1024^2 heat, learned + mixed against plain float64 -------------------------
+def _heat_variants():
+    return [("plain_fp64_pcg", dict(precision="float64", solver="pcg"), dict(krylov_tol=1e-11)),
+            ("mixed_pcg", dict(precision="mixed", solver="pcg"), dict(krylov_tol=1e-5)),
+            ("learned_mixed_fcg", dict(precision="mixed", solver="fcg", **{"type of preconditioner": "learned"}),
+             dict(krylov_tol=1e-4))]
+
+
+def _heat_learned_setup(w, n):
+    from autopdex_gb300 import learned, solver
+    net = learned.UNet.load(os.path.join(learned.WEIGHTS_DIR, "heat_unet_n256.npz"))
+    factor = max(1, n // TRAIN_N)
+    pc = learned.GridPreconditioner(net, n, n, w.settings["conductivity"], factor=factor)
+    solver.set_learned_preconditioner(None, pc)
+    return net, pc, factor
+
+
+def headline(args, rank):
     import torch
     from autopdex_gb300 import configs, learned, solver
-    path = os.path.join(learned.WEIGHTS_DIR, "heat_unet_n256.npz")
-    if not os.path.exists(path):
-        return {"skipped": "no trained weights"}
-    net = learned.UNet.load(path)
-    out = {"workload": f"heat_grf_{n}x{n}_q1 (seed {seed})", "weights": os.path.basename(path),
-           "network_grid": f"{n // max(1, n // TRAIN_N) + 1}^2 nodes (coarsening {max(1, n // TRAIN_N)})"}
-    variants = [("plain_fp64_pcg", dict(precision="float64", solver="pcg"), dict(krylov_tol=1e-11)),
-                ("mixed_pcg", dict(precision="mixed", solver="pcg"), dict(krylov_tol=1e-5)),
-                ("learned_mixed_fcg", dict(precision="mixed", solver="fcg", **{"type of preconditioner": "learned"}),
-                 dict(krylov_tol=1e-4))]
-    factor = max(1, n // TRAIN_N)
-    for name, st, kw in variants:
-        w = configs.heat_grf(n=n, seed=seed)
-        static = dict(w.static_settings, **st)
-        if name.startswith("learned"):
-            solver.set_learned_preconditioner(None, learned.GridPreconditioner(net, n, n, w.settings["conductivity"],
-                                                                                  factor=factor))
-        solver.solver(w.dofs, w.settings, static, newton_tol=0.0, newton_rtol=rtol, maxiter=30,
-                      krylov_maxiter=400000, **kw)  # warm-up (context, graphs)
-        torch.cuda.synchronize()
+    from autopdex_gb300._problem import get_problem
+    n = args.size
+    w = configs.heat_grf(n=n, seed=10000)
+    net, pc, factor = _heat_learned_setup(w, n)
+    name, st, kw = _heat_variants()[2]
+    static = dict(w.static_settings, **st)
+    kw = dict(kw, newton_tol=0.0, newton_rtol=RTOL, maxiter=30, krylov_maxiter=400000)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    x0 = torch.zeros(w.n_dofs, dtype=torch.float64, device=dev)
+    st_dev = dict(w.settings)
+    st_dev["dirichlet conditions"] = {"T": torch.zeros(w.n_dofs, dtype=torch.float64, device=dev)}
+    dofs_dev = {"T": x0}
+
+    def run():
+        return solver.solver(dofs_dev, st_dev, static, **kw)
+    for _ in range(args.warmup):
+        run()
+    prob = get_problem(dofs_dev, st_dev, static)
+    flush = _flush_buffer()
+    _sync()
+    if args.dist:
+        args.dist.barrier()
+    l0 = _launches(prob)
+    stream = torch.cuda.current_stream()
+    ev = [_events() for _ in range(args.steps)]
+    infos = []
+    with Clocks() as clk:
+        _sync()
+        for a, b in ev:
+            flush.fill_(1)  # inputs from HBM: the 256 MB write evicts the problem from L2
+            a.record(stream)
+            sol, info = run()
+            b.record(stream)
+            infos.append(_info())
+        _sync()
+    l1 = _launches(prob)
+    if args.dist:
+        args.dist.barrier()
+    t_ms = sum(a.elapsed_time(b) for a, b in ev)
+    if args.dist:
+        from autopdex_gb300 import replicas
+        t_ms = replicas.max_over_ranks(t_ms, device=dev)
+    per_step = t_ms / 1e3 / args.steps
+    out = {"s": per_step, "info": infos[-1], "launches_per_step": (l1 - l0) / args.steps, "clocks": clk.summary(),
+           "prob": prob, "solution": sol, "w": w, "net": net, "factor": factor, "static": static, "kw": kw,
+           "run": run}
+    # the comparison of the metric: plain float64 Jacobi-PCG (and mixed Jacobi-PCG) on the same problem
+    cmp = {}
+    for vname, vst, vkw in _heat_variants()[:2]:
+        vstatic = dict(w.static_settings, **vst)
+        vkw = dict(vkw, newton_tol=0.0, newton_rtol=RTOL, maxiter=30, krylov_maxiter=400000)
+        solver.solver(w.dofs, w.settings, vstatic, **vkw)
+        flush.fill_(1)
+        s, _ = _timed(lambda: solver.solver(w.dofs, w.settings, vstatic, **vkw))
+        cmp[vname] = dict(s=s, **_info())
+    cmp["learned_mixed_fcg"] = dict(s=per_step, **infos[-1])
+    cmp["speedup_learned_mixed_vs_plain_fp64"] = cmp["plain_fp64_pcg"]["s"] / per_step
+    out["comparison"] = cmp
+    del flush
+    return out
+
+
+def headline_e2e(h, steps):
+    """The headline solve through solver.solver with host arrays: H2D of the DOFs and the
+    prescribed values, D2H of the solution, inside the timed region."""
+    from autopdex_gb300 import solver
+    w = h["w"]
+    static, kw = h["static"], h["kw"]
+    dofs = {"T": np.zeros(w.n_dofs)}
+    solver.solver(dofs, w.settings, static, **kw)
+    t0 = time.perf_counter()
+    k = max(1, min(steps, 3))
+    for _ in range(k):
+        sol, _ = solver.solver(dofs, w.settings, static, **kw)
+        assert isinstance(sol["T"], np.ndarray)
+    _sync()
+    s = (time.perf_counter() - t0) / k
+    return {"value": s, "unit": "s", "h2d_bytes_per_step": 2 * w.n_dofs * 8, "d2h_bytes_per_step": w.n_dofs * 8}
+
+
+def _network_flops(hp, wp):
+    """Tensor-core FLOPs of one U-Net forward pass on an hp x wp padded grid."""
+    from autopdex_gb300 import learned
+    level = {"e0": 0, "e1": 1, "e2": 2, "b3": 3, "d2": 2, "d1": 1, "d0": 0, "ou": 0}
+    tot = 0
+    for name, c1, c2, co, relu in learned.LAYERS:
+        lv = level[name[:2]]
+        h, w_ = hp // learned.POOL ** lv, wp // learned.POOL ** lv
+        tot += 2 * 9 * (c1 + c2) * co * h * w_
+    return tot
+
+
+def headline_roofline(h):
+    """Per-category shares of the headline solve and the roofline of its dominant kernel."""
+    from autopdex_gb300 import learned
+    prob = h["prob"]
+    ms, cnt = _profile(prob, h["run"])
+    tot = sum(ms.values())
+    shares = {k: (v / tot if tot else 0.0) for k, v in ms.items()}
+    hbm, bf16, kind = _peaks()
+    n_nodes, n, ndof = prob.n_nodes, prob.n_dofs, prob.ndof
+    nnzb = prob.nnzb
+    s = 4  # float32 products
+    # algorithmic bytes per launch: values and columns of every stored block, row pointers, and
+    # the vectors (fused Krylov product: z, p_old read, p_new, q written; plain product: x, y)
+    fused = nnzb * (ndof * ndof * s + 4) + 4 * (n_nodes + 1) + 4 * n * s
+    plain = nnzb * (ndof * ndof * s + 4) + 4 * (n_nodes + 1) + 2 * n * s
+    hc = h["w"].raw["n"] // h["factor"] + 1
+    flops = _network_flops(learned.padded(hc), learned.padded(hc))
+    cand = {"smoothing_product": ("hbm", plain, "spmv_kernel<float,1,tpr> (two-level smoothing and K y products)"),
+            "krylov_product": ("hbm", fused, "spmv_dot_kernel<float,1,tpr> (FCG product with direction update and dot)"),
+            "network": ("tensor", flops, "U-Net forward: 15 conv3x3_tc launches (tcgen05, BF16) + grid transfers")}
+    dom = max(cand, key=lambda k: ms.get(k, 0.0))
+    bound, work, kname = cand[dom]
+    avg_ms = ms[dom] / max(1, cnt[dom])
+    if bound == "hbm":
+        ach = work / (avg_ms * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel": kname, "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                "peak_source": kind, "algorithmic_bytes": work, "avg_launch_ms": avg_ms,
+                "traffic": NCU_TRAFFIC.get(kname)}
+    else:
+        ach = work / (avg_ms * 1e-3) / 1e12
+        roof = {"bound": "tensor", "kernel": kname, "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
+                "frac": ach / bf16, "peak_source": kind, "flops_per_application": work, "avg_application_ms": avg_ms,
+                "traffic": NCU_TRAFFIC.get(kname)}
+    others = {}
+    for k, (b_, wk, kn) in cand.items():
+        if k == dom or not cnt.get(k):
+            continue
+        a_ms = ms[k] / cnt[k]
+        if b_ == "hbm":
+            others[k] = {"kernel": kn, "avg_launch_ms": a_ms, "achieved_gbs": wk / (a_ms * 1e-3) / 1e9,
+                         "frac": wk / (a_ms * 1e-3) / 1e9 / hbm}
+        else:
+            others[k] = {"kernel": kn, "avg_application_ms": a_ms, "achieved_tflops": wk / (a_ms * 1e-3) / 1e12,
+                         "frac": wk / (a_ms * 1e-3) / 1e12 / bf16}
+    roof["other_kernels"] = others
+    return roof, {"ms": ms, "launches": cnt, "shares": shares}
+
+
+# ---- oracle errors and the CPU path (the checker; oracle/ is used only here) ------------------
+def _oracle_residual(w, u, settings=None, accurate=False):
+    """Float64 residual of workload w at DOFs u by the oracle's C restatement."""
+    from oracle import corc
+    r = w.raw
+    st = settings if settings is not None else w.settings
+    kind, coords = r["kind"], r["coords"]
+    n = coords.shape[0]
+    if kind == "poisson":
+        Re, _ = corc.q1_elements("poisson", r["conns"][0], coords, u, [20.0, 10.0, 1.0, 0.5], tangent=False)
+        return corc.scatter(r["conns"][0], 1, Re, n)
+    if kind == "heat":
+        Re, _ = corc.q1_elements("heat", r["conns"][0], coords, u, [1.0], elem_field=r["k"], tangent=False)
+        return corc.scatter(r["conns"][0], 1, Re, n)
+    if kind == "neo_hooke_3d":
+        Re, _ = corc.q1_elements("neo_hooke", r["conns"][0], coords, u, [r["E"], r["nu"]], accurate=accurate,
+                                 tangent=False)
+        return corc.scatter(r["conns"][0], 3, Re, 3 * n)
+    if kind == "cook":
+        Re, _ = corc.q1_elements("neo_hooke", r["conns"][0], coords, u, [r["E"], r["nu"]], accurate=accurate,
+                                 tangent=False)
+        R = corc.scatter(r["conns"][0], 2, Re, 2 * n)
+        Rl = corc.neumann_lines(r["conns"][1], coords, (0.0, float(st["load multiplier"])))
+        return R + corc.scatter(r["conns"][1], 2, Rl, 2 * n)
+    if kind == "heat_be":
+        Tn = _flat(st["dofs n"])
+        Re, _ = corc.q1_elements("heat_be", r["conns"][0], coords, u, [1.0, 0.5, 1.0, float(st["time increment"])],
+                                 node_field=Tn, tangent=False)
+        return corc.scatter(r["conns"][0], 1, Re, n)
+    raise ValueError(kind)
+
+
+def oracle_errors(w, u_gpu, res0, settings=None, u_oracle=None, scale=1.0, seed=0):
+    """Errors against the float64 oracle: residual parity at a random non-converged state
+    (||R_gpu - R_oracle|| / ||R_oracle||), the true float64 residual of the GPU solution
+    evaluated by the oracle relative to the load step's first residual, and, when the oracle
+    solved too, ||u_gpu - u_oracle||_inf."""
+    from autopdex_gb300 import assembler
+    st = settings if settings is not None else w.settings
+    free = ~np.asarray(w.raw["dirichlet"], dtype=bool).reshape(-1)
+    rng = np.random.default_rng(seed)
+    ur = rng.uniform(-scale, scale, w.n_dofs)
+    shape = np.shape(next(iter(w.dofs.values()))) if isinstance(w.dofs, dict) else np.shape(w.dofs)
+    ur_d = {next(iter(w.dofs)): ur.reshape(shape)} if isinstance(w.dofs, dict) else ur.reshape(shape)
+    R_gpu = _flat(assembler.assemble_residual(ur_d, st, w.static_settings))
+    acc = w.raw["kind"] in ("cook", "neo_hooke_3d")
+    R_or = _oracle_residual(w, ur, st, accurate=acc)
+    out = {"residual_parity": float(np.linalg.norm(R_gpu - R_or) / np.linalg.norm(R_or)),
+           "residual_parity_state": f"uniform random DOFs in [-{scale:g}, {scale:g}]"}
+    R_true = _oracle_residual(w, _flat(u_gpu), st, accurate=acc)
+    out["true_residual_ratio"] = float(np.linalg.norm(R_true[free]) / res0) if res0 else None
+    if acc:
+        R_ref = _oracle_residual(w, _flat(u_gpu), st, accurate=False)
+        out["true_residual_ratio_reference_evaluation"] = float(np.linalg.norm(R_ref[free]) / res0) if res0 else None
+    if u_oracle is not None:
+        out["max_abs_u_minus_oracle"] = float(np.abs(_flat(u_gpu) - _flat(u_oracle)).max())
+        out["max_abs_u_oracle"] = float(np.abs(_flat(u_oracle)).max())
+    return out
+
+
+def cpu_solve(w, rtol=RTOL, direct=False, maxiter=2000000):
+    """The CPU path of one linear(ized) solve from zero: C elements, SciPy COO -> CSR with the
+    Dirichlet rows and columns deleted (scipy_assembling, solver.py:1180-1222), then spsolve
+    (direct, solver.py:1520) or the C Jacobi-PCG to rtol; returns the solution and timings."""
+    import scipy.sparse as sps
+    import scipy.sparse.linalg as spla
+    from oracle import corc
+    r = w.raw
+    coords, conn = r["coords"], r["conns"][0]
+    n = coords.shape[0]
+    free = ~np.asarray(r["dirichlet"], dtype=bool)
+    u0 = np.zeros(n)
+    t0 = time.perf_counter()
+    if r["kind"] == "heat":
+        Re, Ke = corc.q1_elements("heat", conn, coords, u0, [1.0], elem_field=r["k"])
+    else:
+        Re, Ke = corc.q1_elements("poisson", conn, coords, u0, [20.0, 10.0, 1.0, 0.5])
+    R = corc.scatter(conn, 1, Re, n)
+    t1 = time.perf_counter()
+    m = conn.shape[1]
+    A = sps.coo_matrix((Ke.ravel(), (np.repeat(conn, m, axis=1).ravel(), np.tile(conn, (1, m)).ravel())),
+                       shape=(n, n)).tocsr()
+    A = A[:, free][free].tocsr()
+    del Ke
+    t2 = time.perf_counter()
+    b = -R[free]
+    if direct:
+        x = spla.spsolve(A.tocsc(), b)
+        its = 0
+    else:
+        x, rr, its = corc.pcg_csr_tol(A, b, rtol, maxiter)
+    t3 = time.perf_counter()
+    u = np.zeros(n)
+    u[free] = x
+    rel = float(np.linalg.norm(A @ x - b) / np.linalg.norm(b))
+    return u, {"s": t3 - t0, "elements_s": t1 - t0, "coo_to_csr_s": t2 - t1, "solve_s": t3 - t2, "iterations": its,
+               "relative_residual": rel, "threads": corc.threads()}
+
+
+# ---- sub-records -------------------------------------------------------------------------------
+def rec_poisson(n=200, cpu=True):
+    from autopdex_gb300 import configs, solver
+    w = configs.poisson(n=n, solver="lapack")
+    kw = dict(newton_tol=1e-10)
+    solver.solver(w.dofs, w.settings, w.static_settings, **kw)
+    s, (sol, info) = _timed(lambda: solver.solver(w.dofs, w.settings, w.static_settings, **kw))
+    out = {"workload": f"poisson_{n}x{n}_q1 (one Newton step, direct solve)", "gpu_direct": dict(s=s, **_info())}
+    wp = configs.poisson(n=n, solver="pcg")
+    solver.solver(wp.dofs, wp.settings, wp.static_settings, newton_tol=1e-10, krylov_tol=1e-13)
+    s2, _ = _timed(lambda: solver.solver(wp.dofs, wp.settings, wp.static_settings, newton_tol=1e-10,
+                                          krylov_tol=1e-13))
+    out["gpu_plain_fp64_pcg_1e-13"] = dict(s=s2, **_info())
+    res0 = out["gpu_direct"]["res0"]
+    u_or = None
+    if cpu:
+        u_or, c = cpu_solve(w, direct=True)
+        out["cpu_baseline"] = dict(c, kind="port", sample="full problem: C elements, SciPy COO->CSR with Dirichlet "
+                                   "deletion, SciPy spsolve (single-threaded SuperLU)")
+    out["oracle_error"] = oracle_errors(w, sol, res0, u_oracle=u_or)
+    return out
+
+
+def rec_neo_hooke_cube(n=64, steps=10):
+    import torch
+    from autopdex_gb300 import configs, solver
+    out = {"workload": f"neo_hooke_cube_{n}^3_hex8, load steps 1..{steps} of 10 (u_x = 0.03 k on x = 1), Newton to "
+                       f"1e-10 of each step's first residual"}
+    for name, prec, ktol in (("mixed_pcg", "mixed", 1e-4), ("plain_fp64_pcg", "float64", 1e-4)):
+        w = configs.neo_hooke_cube(n=n, n_steps=10, precision=prec)
+        dev = torch.device("cuda", torch.cuda.current_device())
+        # start of load step 1 from the linear lifting of the prescribed values (from u = 0 the
+        # first element layer is stretched threefold at h = 1/64 and undamped Newton diverges)
+        x0 = np.zeros((w.n_dofs // 3, 3))
+        x0[:, 0] = w.raw["stretch"] / w.raw["n_steps"] * w.raw["coords"][:, 0]
+        kw = dict(newton_tol=0.0, newton_rtol=RTOL, maxiter=30, krylov_tol=ktol)
+        # warm-up: context, autotuning, graphs
+        st = w.steps[0](dict(w.settings))
+        solver.solver(torch.as_tensor(x0, device=dev), st, w.static_settings, **kw)
+        per = []
+
+        lift = torch.as_tensor(x0, device=dev)
+
+        def all_steps():
+            x = torch.zeros_like(lift)
+            settings = dict(w.settings)
+            for k in range(steps):
+                # each step starts from the previous solution plus the linear lifting of the
+                # prescribed increment (u_x += 0.03 x), consistent with the new boundary values
+                x = x + lift
+                settings = w.steps[k](settings)
+                settings["dirichlet conditions"] = torch.as_tensor(np.asarray(settings["dirichlet conditions"]),
+                                                                   device=dev)
+                x, _ = solver.solver(x, settings, w.static_settings, **kw)
+                per.append(_info())
+            return x, settings
+        s, (x, settings) = _timed(all_steps)
+        out[name] = {"s": s, "newton": sum(p["newton"] for p in per), "krylov": sum(p["krylov"] for p in per),
+                     "max_residual_ratio": max(p["residual_ratio"] for p in per),
+                     "diverged": any(p["diverged"] for p in per)}
+        if name == "mixed_pcg":
+            st_np = dict(settings)
+            st_np["dirichlet conditions"] = np.asarray(settings["dirichlet conditions"].cpu())
+            out["oracle_error"] = oracle_errors(w, x, per[-1]["res0"], settings=st_np, scale=0.003)
+    out["speedup_mixed_vs_plain_fp64"] = out["plain_fp64_pcg"]["s"] / out["mixed_pcg"]["s"]
+    return out
+
+
+def rec_cook(n=512, steps=1, plain_limit_s=120.0):
+    from autopdex_gb300 import configs, solver
+    out = {"workload": f"cook_membrane_{n}x{n}_q1 (nu = 0.4999), load steps 1..{steps} of 20"}
+    rt = 1e-8
+    out["newton_rtol"] = rt
+    for name, sol_name, prec, ktol in (("direct_fp64", "lapack", "float64", 1e-13),
+                                       ("plain_fp64_pcg", "pcg", "float64", 1e-4)):
+        w = configs.cook_membrane(n=n, solver=sol_name, precision=prec)
+        kw = dict(newton_tol=0.0, newton_rtol=rt, maxiter=12, krylov_tol=ktol)
+        if name == "plain_fp64_pcg":
+            kw["krylov_maxiter"] = 200000
+        x = w.dofs
+        settings = dict(w.settings)
+        per = []
         t0 = time.perf_counter()
-        sol, info = solver.solver(w.dofs, w.settings, static, newton_tol=0.0, newton_rtol=rtol, maxiter=30,
-                                  krylov_maxiter=400000, **kw)
-        torch.cuda.synchronize()
-        li = solver.last_info
-        out[name] = {"s": time.perf_counter() - t0, "newton": int(info[0]), "krylov": int(li.krylov_iterations),
-                     "residual_ratio": li.res_norm / li.res0 if li.res0 else None, "diverged": bool(info[2])}
-    out["speedup_learned_vs_plain_fp64"] = out["plain_fp64_pcg"]["s"] / out["learned_mixed_fcg"]["s"]
+        for k in range(steps):
+            settings = w.steps[k](settings)
+            s, (x, info) = _timed(lambda: solver.solver(x, settings, w.static_settings, **kw))
+            per.append(dict(s=s, **_info()))
+            if time.perf_counter() - t0 > plain_limit_s:
+                break
+        out[name] = {"s": sum(p["s"] for p in per), "steps_run": len(per), "per_step": per}
+        if name == "direct_fp64":
+            out["oracle_error"] = oracle_errors(w, x, per[-1]["res0"], settings=settings, scale=1e-5)
+    return out
+
+
+def rec_heat(h):
+    """The headline problem's record: the three variants and the oracle's errors."""
+    w = h["w"]
+    out = {"workload": f"heat_grf_{w.raw['n']}x{w.raw['n']}_q1 (seed 10000), time to {RTOL:g}",
+           "network_grid": f"{w.raw['n'] // h['factor'] + 1}^2 nodes (coarsening {h['factor']})"}
+    out.update(h["comparison"])
+    return out
+
+
+def rec_heat_be(n=128, steps=10, plain_steps=3):
+    import torch
+    from autopdex_gb300 import configs, solver
+    out = {"workload": f"heat_be_{n}^3_hex8 (k = 1 + 0.5 T^2, dt = 1e-3), time steps 1..{steps} of 100"}
+    for name, sol_name, prec, ktol, nsteps in (("mixed_pcg", "pcg", "mixed", 1e-5, steps),
+                                               ("plain_fp64_bicgstab", "bicgstab", "float64", 1e-11, plain_steps)):
+        w = configs.heat_transient(n=n, solver=sol_name, precision=prec)
+        dev = torch.device("cuda", torch.cuda.current_device())
+        T0 = torch.as_tensor(w.raw["T0"], device=dev)
+        kw = dict(newton_tol=0.0, newton_rtol=RTOL, maxiter=30, krylov_tol=ktol)
+        settings = dict(w.settings)
+        settings["dofs n"] = {"T": T0.clone()}
+        settings["dirichlet conditions"] = {"T": torch.zeros_like(T0)}
+        solver.solver({"T": T0.clone()}, settings, w.static_settings, **kw)  # context, tuning, graphs
+        per = []
+        first = {}
+
+        def run():
+            T = T0.clone()
+            for k in range(nsteps):
+                settings["dofs n"] = {"T": T}
+                Tn, _ = solver.solver({"T": T}, settings, w.static_settings, **kw)
+                per.append(_info())
+                if k == 0:
+                    first["T1"] = Tn["T"].clone()
+                T = Tn["T"]
+            return T
+        s, T = _timed(run)
+        out[name] = {"s_per_step": s / nsteps, "steps": nsteps, "newton": sum(p["newton"] for p in per),
+                     "krylov": sum(p["krylov"] for p in per),
+                     "max_residual_ratio": max(p["residual_ratio"] for p in per),
+                     "sum_T_squared": float((T * T).sum())}
+        if name == "mixed_pcg":
+            st = dict(w.settings)
+            st["dofs n"] = {"T": w.raw["T0"]}
+            out["oracle_error_first_step"] = oracle_errors(w, first["T1"], per[0]["res0"], settings=st, scale=1.0)
+    out["speedup_mixed_vs_plain_fp64"] = out["plain_fp64_bicgstab"]["s_per_step"] / out["mixed_pcg"]["s_per_step"]
     return out
 
 
 def assembly_roofline(n=1024, reps=20):
-    """Float32 tangent assembly of the 1024^2 random-conductivity heat mesh (an HBM-bound
-    assembly: a scalar potential on Q1 quads), timed with CUDA events per agx_assemble call.
-
-    Algorithmic bytes: coordinates + DOFs + connectivity +
-    values written once (n_nodes dim 8 + n_dofs 8 + n_e nen 4 + nnz 4); the row kernel of
-    structured grids moves coordinates, conductivities, row pointers and values."""
+    """Float32 tangent assembly of the n^2 random-conductivity heat mesh, timed with CUDA events
+    per agx_assemble call after a 256 MB buffer write (inputs from HBM).  Algorithmic bytes:
+    coordinates + DOFs + connectivity + values written once (n_nodes dim 8 + n_dofs 8 + n_e nen 4
+    + nnz 4)."""
     import ctypes as C
     import torch
     from autopdex_gb300 import configs, _native as N
@@ -359,32 +589,27 @@ def assembly_roofline(n=1024, reps=20):
     x = torch.zeros(prob.n_dofs, dtype=torch.float64, device=prob.device)
     for _ in range(3):
         prob._call("agx_assemble", C.c_void_p(x.data_ptr()), None, N.AGX_F32)
-    # The mesh's arrays and values (about 60 MB) fit in the 129 MB L2: every timed call
-    # follows a write of a 256 MB buffer, so that its inputs come from HBM.
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=prob.device)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
-    for a, b in ev:  # per call, the library's own timing off
+    flush = _flush_buffer()
+    ev = [_events() for _ in range(reps)]
+    for a, b in ev:
         flush.fill_(1)
         a.record()
         prob._call("agx_assemble", C.c_void_p(x.data_ptr()), None, N.AGX_F32)
         b.record()
-    torch.cuda.synchronize()
+    _sync()
     call_ms = sum(a.elapsed_time(b) for a, b in ev)
-    prob._call("agx_profile", 1)
-    for _ in range(reps):  # per kernel: the library's events around each row-kernel launch
-        flush.fill_(1)
-        prob._call("agx_assemble", C.c_void_p(x.data_ptr()), None, N.AGX_F32)
-    torch.cuda.synchronize()
-    ms = (C.c_double * N.AGX_PROF_CATEGORIES)()
-    cnt = (C.c_int64 * N.AGX_PROF_CATEGORIES)()
-    prob._call("agx_profile_read", ms, cnt)
-    prob._call("agx_profile", 0)
+
+    def kern():
+        for _ in range(reps):
+            flush.fill_(1)
+            prob._call("agx_assemble", C.c_void_p(x.data_ptr()), None, N.AGX_F32)
+    ms, cnt = _profile(prob, kern)
     del flush
     n_e = n * n
     nbytes = prob.n_nodes * 2 * 8 + prob.n_dofs * 8 + n_e * 4 * 4 + prob.nnzb * 4
     call_s = call_ms / 1e3 / reps
-    kern_s = ms[N.AGX_PROF_TANGENT] / 1e3 / max(1, cnt[N.AGX_PROF_TANGENT])
-    peak, kind = _peaks()
+    kern_s = ms["tangent_assembly"] / 1e3 / max(1, cnt["tangent_assembly"])
+    peak, _, kind = _peaks()
     return {"workload": f"heat_grf_{n}x{n}_q1 float32 tangent", "kernel": "grid_tangent_kernel<HEAT_POTENTIAL,float>",
             "algorithmic_bytes": nbytes, "call_us": call_s * 1e6, "kernel_us": kern_s * 1e6,
             "achieved_gbs_call": nbytes / call_s / 1e9, "achieved_gbs_kernel": nbytes / kern_s / 1e9,
@@ -392,151 +617,168 @@ def assembly_roofline(n=1024, reps=20):
             "peak_source": kind, "l2": "256 MB buffer written before every timed call"}
 
 
-def _timed_solve(w, static, step=None, x0=None, rtol=1e-10, **kw):
-    """One solver.solver call (warm context: a first call builds it), CUDA-synchronised wall
-    time, with the Newton and Krylov counts and the final float64 residual ratio."""
+def cpu_baseline_headline(h, budget_s=120.0):
+    """The CPU path on the full headline problem (one solve to 1e-10 with Jacobi-PCG), and the
+    headline's errors against it."""
+    w = h["w"]
+    u_or, c = cpu_solve(w, rtol=RTOL)
+    err = oracle_errors(w, h["solution"], h["info"]["res0"], u_oracle=u_or)
+    base = {"value": c["s"], "unit": "s", "cores": c["threads"], "kind": "port",
+            "sample": (f"the full {w.raw['n']}^2 problem: C elements ({c['elements_s']:.2f} s), SciPy COO->CSR with "
+                       f"Dirichlet deletion ({c['coo_to_csr_s']:.2f} s), C OpenMP Jacobi-PCG to {RTOL:g} "
+                       f"({c['iterations']} iterations, {c['solve_s']:.2f} s)"),
+            "relative_residual": c["relative_residual"]}
+    return base, err
+
+
+# ---- arms ----------------------------------------------------------------------------------------
+def gpu_arm(args):
     import torch
-    from autopdex_gb300 import solver
-    st = dict(w.settings)
-    if step is not None:
-        st = step(st)
-    dofs = w.dofs if x0 is None else x0
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    sol, info = solver.solver(dofs, st, static, newton_tol=0.0, newton_rtol=rtol, maxiter=30, **kw)
-    torch.cuda.synchronize()
-    li = solver.last_info
-    return sol, {"s": time.perf_counter() - t0, "newton": int(info[0]), "krylov": int(li.krylov_iterations),
-                 "residual_ratio": li.res_norm / li.res0 if li.res0 else None, "diverged": bool(info[2])}
-
-
-def other_workloads(cook_n=128, cook_rtol=1e-6, heat3d_n=128, heat3d_steps=2):
-    """The 200^2 Poisson, Cook membrane and 3-D backward-Euler heat workloads beside the headline:
-    plain float64 against mixed precision where the
-    method allows it (BiCGStab, for the non-symmetric backward-Euler tangent, runs in float64).
-
-    Cook's membrane (nu = 0.4999) is run at cook_n^2 to a relative Newton residual of cook_rtol:
-    with Jacobi-PCG the float64 Newton residual of this nearly incompressible problem stalls
-    near 4.5e-7 of the first one already at 128^2 (measured: 31 Newton iterations and 1.8 M CG
-    iterations without getting below it), so 1e-10 is out of reach for the plain method."""
-    from autopdex_gb300 import configs
-    out = {}
-    # 200^2 Poisson, one Newton step with the direct-solver name ('lapack')
-    w = configs.poisson(n=200, solver="lapack")
-    _timed_solve(w, w.static_settings)
-    _, out["poisson_200_fp64_direct"] = _timed_solve(w, w.static_settings)
-    # Cook membrane, load step 1 of 20
-    res = {}
-    for name, prec, ktol in (("plain_fp64_pcg", "float64", 1e-8), ("mixed_pcg", "mixed", 1e-5)):
-        w = configs.cook_membrane(n=cook_n, precision=prec)
-        _timed_solve(w, w.static_settings, step=w.steps[0], rtol=cook_rtol, krylov_tol=ktol, krylov_maxiter=400000)
-        _, res[name] = _timed_solve(w, w.static_settings, step=w.steps[0], rtol=cook_rtol, krylov_tol=ktol,
-                                    krylov_maxiter=400000)
-    res["speedup_mixed_vs_plain_fp64"] = res["plain_fp64_pcg"]["s"] / res["mixed_pcg"]["s"]
-    out[f"cook_{cook_n}_load_step_1_rtol_{cook_rtol:g}"] = res
-    # 3-D nonlinear backward-Euler heat, the first time steps: float64 BiCGStab (the tangent has
-    # a small non-symmetric k'(T) part) against mixed Jacobi-PCG (float32 CG on the
-    # mass-dominated tangent inside the float64 Newton loop, which the float64 residual judges)
-    import numpy as np
-    res = {}
-    for name, sol_name, prec, ktol in (("plain_fp64_bicgstab", "bicgstab", "float64", 1e-11),
-                                       ("mixed_pcg", "pcg", "mixed", 1e-5)):
-        w = configs.heat_transient(n=heat3d_n, solver=sol_name, precision=prec)
-        T = np.asarray(w.raw["T0"], dtype=np.float64)
-        steps = []
-        for k in range(heat3d_steps + 1):
-            w.settings["dofs n"] = {"T": T.copy()}
-            sol, r = _timed_solve(w, w.static_settings, x0={"T": T.copy()}, krylov_tol=ktol)
-            T = np.asarray(sol["T"])
-            if k:
-                steps.append(r)  # the first call builds the context and is not counted
-        res[name] = {"s_per_step": sum(r["s"] for r in steps) / len(steps), "per_step": steps,
-                     "sum_T_squared": float(np.sum(T * T))}
-    res["speedup_mixed_vs_plain_fp64"] = res["plain_fp64_bicgstab"]["s_per_step"] / res["mixed_pcg"]["s_per_step"]
-    out[f"heat_be_{heat3d_n}^3_steps_1_to_{heat3d_steps}"] = res
-    return out
-
-
-def cpu_baseline(n, newton_iters, cg_iters, budget_s=20.0):
-    """CPU oracle on a bounded sample of the workload, scaled to one load step.
-
-    The oracle's C restatement (oracle/c/orc.c: closed-form float64 neo-Hooke brick and
-    Jacobi-PCG on CSR, OpenMP over all host cores) on the 32^3 cube: (a) residual and tangent
-    cost per element; (b) COO -> CSR with Dirichlet rows and columns deleted, as
-    scipy_assembling does (solver.py:1180-1222, SciPy, single-threaded as there), per stored
-    entry; (c) Jacobi-PCG cost per iteration per stored entry -- the reference's 'cg' +
-    'jacobi' algorithm on the assembled matrix.  Scaled with the Newton and CG iteration
-    counts of the float64 GPU path on the full problem:
-    t = newton_iters (2 n_e t_res + n_e t_tan + nnz t_csr) + cg_iters nnz t_iter."""
-    import scipy.sparse as sps
-    from autopdex_gb300 import configs
-    from oracle import corc
-
-    threads = corc.threads()
-    ns = 32
-    w = configs.neo_hooke_cube(n=ns, n_steps=10)
-    coords, conn = w.raw["coords"], w.raw["conns"][0]
-    n_e = conn.shape[0]
-    u = np.random.default_rng(0).uniform(-1e-3, 1e-3, coords.shape)
-    corc.neo_hooke_hex8(conn[:256], coords, u, w.raw["E"], w.raw["nu"])  # threads up, library loaded
-    t0 = time.perf_counter()
-    corc.neo_hooke_hex8(conn, coords, u, w.raw["E"], w.raw["nu"], tangent=False)
-    t_res = (time.perf_counter() - t0) / n_e
-    t0 = time.perf_counter()
-    _, K_e = corc.neo_hooke_hex8(conn, coords, u, w.raw["E"], w.raw["nu"])
-    t_tan = (time.perf_counter() - t0) / n_e
-    edofs = (conn[:, :, None] * 3 + np.arange(3)).reshape(n_e, 24)
-    free = ~np.asarray(w.raw["dirichlet"], dtype=bool)
-    t0 = time.perf_counter()
-    A = sps.coo_matrix((K_e.ravel(), (np.repeat(edofs, 24, axis=1).ravel(), np.tile(edofs, (1, 24)).ravel())),
-                       shape=(free.size, free.size)).tocsr()
-    A = A[free][:, free].tocsr()
-    t_csr = (time.perf_counter() - t0) / A.nnz
-    del K_e
-    b = np.random.default_rng(1).standard_normal(A.shape[0])
-    corc.pcg_csr(A, b, 3)
-    iters = 100
-    t0 = time.perf_counter()
-    corc.pcg_csr(A, b, iters)
-    t_iter = (time.perf_counter() - t0) / iters / A.nnz
-    nnz = 243 * (n + 1) ** 3  # stored entries of the full problem: 27 node blocks of 3 x 3 per node (upper bound)
-    n_e_full = n ** 3
-    est = newton_iters * (2 * n_e_full * t_res + n_e_full * t_tan + nnz * t_csr) + cg_iters * nnz * t_iter
-    return {"value": est, "unit": "s", "cores": threads, "kind": "port",
-            "sample": (f"oracle C restatement on the {ns}^3 cube ({threads} threads): residual {t_res * 1e6:.2f} and "
-                       f"tangent {t_tan * 1e6:.2f} us per element, COO->CSR with Dirichlet deletion (SciPy) "
-                       f"{t_csr * 1e9:.1f} ns and Jacobi-PCG {t_iter * 1e9:.2f} ns per stored entry and iteration; "
-                       f"scaled to {n}^3 with the float64 GPU path's {newton_iters} Newton and {cg_iters} CG "
-                       f"iterations")}
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    args.dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        args.dist = dist
+    h = headline(args, rank)
+    n = args.size
+    line = {
+        "metric": f"time_to_{RTOL:g}_relative_fp64_residual (learned+mixed vs plain FP64 Jacobi-PCG; "
+                  f"{n}^2 random-conductivity heat, the learned-preconditioner workload)",
+        "value": h["s"], "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": h["s"] * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 FCG + bf16 network + f64 residual/refinement",
+        "data": "synthetic (seeded Gaussian random field conductivity; no dataset)",
+        "config": {"workload": f"heat_grf_{n}x{n}_q1_seed10000", "n_dofs": h["w"].n_dofs, "newton_rtol": RTOL,
+                   "krylov": "flexible CG (float32) with the U-Net two-level preconditioner, inner rtol 1e-4",
+                   "network_grid": f"{n // h['factor'] + 1}^2 (coarsening {h['factor']})",
+                   "l2": "256 MB buffer written before every timed step", "krylov_chunks": "CUDA graphs",
+                   "parallelism": "replicas" if world > 1 else "1 gpu"},
+        "newton_iterations": h["info"]["newton"], "krylov_iterations": h["info"]["krylov"],
+        "final_residual_ratio": h["info"]["residual_ratio"],
+        "converged": (not h["info"]["diverged"]) and h["info"]["residual_ratio"] <= RTOL * 1.0000001,
+        "plain_fp64_pcg_s": h["comparison"]["plain_fp64_pcg"]["s"],
+        "speedup_learned_mixed_vs_plain_fp64": h["comparison"]["speedup_learned_mixed_vs_plain_fp64"],
+        "gpu_launches": int(round(h["launches_per_step"] * args.steps)),
+        "clocks": h["clocks"],
+    }
+    try:
+        line["e2e"] = headline_e2e(h, args.steps)
+    except Exception as e:  # noqa: BLE001 -- reported, the headline stands
+        line["e2e"] = {"error": str(e)[:200]}
+    try:
+        line["roofline"], line["kernel_ms_per_step"] = headline_roofline(h)
+    except Exception as e:  # noqa: BLE001
+        line["roofline"] = {"error": str(e)[:200]}
+    configs_out = {}
+    if rank == 0 and not args.only_headline:
+        configs_out["heat_1024"] = rec_heat(h)
+        for key, fn in (("poisson_200", lambda: rec_poisson(cpu=not args.no_cpu_baseline)),
+                        ("neo_hooke_64cube", rec_neo_hooke_cube),
+                        ("cook_512", lambda: rec_cook(steps=args.cook_steps)),
+                        ("heat_be_128cube", rec_heat_be)):
+            try:
+                configs_out[key] = fn()
+            except Exception as e:  # noqa: BLE001 -- reported, the headline stands
+                configs_out[key] = {"error": str(e)[:300]}
+        try:
+            line["assembly_hbm"] = assembly_roofline()
+            line["assembly_hbm_2048"] = assembly_roofline(n=2048)  # values (151 MB) larger than L2
+        except Exception as e:  # noqa: BLE001
+            line["assembly_hbm"] = {"error": str(e)[:200]}
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            line["cpu_baseline"], err = cpu_baseline_headline(h)
+            if "heat_1024" in configs_out:
+                configs_out["heat_1024"]["oracle_error"] = err
+            line["oracle_error"] = err
+        except Exception as e:  # noqa: BLE001
+            line["cpu_baseline"] = {"error": str(e)[:300]}
+    if configs_out:
+        line["configs"] = configs_out
+    if args.dist:
+        args.dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line, default=float))
 
 
 def reference_arm(args):
+    """The CPU path of the headline workload (one full solve to 1e-10 per step) on all host
+    cores: the oracle's C restatement, since the reference is JAX code and no JAX exists."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    from autopdex_gb300 import configs
     n = args.size
-    # iteration counts of the float64 path on the 64^3 load step, measured on the GPU arm
-    newton_iters, cg_iters = args.ref_newton_iters, args.ref_cg_iters
-    vals = []
+    w = configs.heat_grf(n=n, seed=10000)
     for _ in range(args.warmup):
-        cpu_baseline(n, newton_iters, cg_iters)
+        cpu_solve(w)
+    vals, last = [], None
     t0 = time.perf_counter()
-    last = None
     for _ in range(args.steps):
-        last = cpu_baseline(n, newton_iters, cg_iters)
-        vals.append(last["value"])
+        _, last = cpu_solve(w)
+        vals.append(last["s"])
     wall = time.perf_counter() - t0
     v = float(np.median(vals))
+    sample = (f"full {n}^2 problem per step: C elements, SciPy COO->CSR with Dirichlet deletion, C OpenMP "
+              f"Jacobi-PCG to {RTOL:g} ({last['iterations']} iterations)")
     line = {"impl": "reference",
-            "metric": "time_to_1e-10_relative_fp64_residual (64^3 neo-Hooke cube, load step 1 of 10)",
+            "metric": f"time_to_{RTOL:g}_relative_fp64_residual (learned+mixed vs plain FP64 Jacobi-PCG; "
+                      f"{n}^2 random-conductivity heat, the learned-preconditioner workload)",
             "value": v, "unit": "s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"neo_hooke_cube_{n}^3_hex8_load_step_1"},
-            "cpu_baseline": {"value": v, "unit": "s", "cores": last["cores"], "kind": last["kind"],
-                             "sample": last["sample"]},
+            "config": {"workload": f"heat_grf_{n}x{n}_q1_seed10000"},
+            "cpu_baseline": {"value": v, "unit": "s", "cores": last["threads"], "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+# ---- small cases for ncu captures (no JSON line) ----------------------------------------------
+def case(args):
+    import ctypes as C
+    import torch
+    from autopdex_gb300 import configs, learned, solver, _native as N
+    from autopdex_gb300._problem import get_problem
+    if args.case == "conv":
+        net = learned.UNet(seed=0)
+        _, c1, c2, co, relu = next(l for l in learned.LAYERS if l[0] == args.layer)
+        g = torch.Generator(device="cuda").manual_seed(0)
+        x1 = torch.randn(1, args.size, args.size, c1, device="cuda", generator=g).to(torch.bfloat16)
+        x2 = torch.randn(1, args.size, args.size, c2, device="cuda", generator=g).to(torch.bfloat16) if c2 else None
+        for _ in range(args.reps):
+            net._conv(args.layer, x1, x2, 1, args.size, args.size)
+        _sync()
+        net.check()
+        print(f"conv {args.layer} on {args.size}^2: {args.reps} launches")
+        return
+    make = {"heat": lambda: configs.heat_grf(n=args.size, seed=10000, precision=args.precision, solver=args.solver),
+            "poisson": lambda: configs.poisson(n=args.size, precision=args.precision, solver=args.solver),
+            "neo_hooke": lambda: configs.neo_hooke_cube(n=args.size, precision=args.precision, solver=args.solver),
+            "cook": lambda: configs.cook_membrane(n=args.size, precision=args.precision, solver=args.solver)}
+    w = make[args.workload]()
+    if args.case == "assembly":
+        prob = get_problem(w.dofs, w.settings, w.static_settings)
+        prob.update_models(w.settings)
+        x = torch.zeros(prob.n_dofs, dtype=torch.float64, device=prob.device)
+        dt = N.AGX_F32 if args.precision == "mixed" else N.AGX_F64
+        for _ in range(args.reps):
+            prob._call("agx_assemble", C.c_void_p(x.data_ptr()), None, dt)
+        _sync()
+        print(f"assembly {w.name}: {args.reps} calls")
+        return
+    static = dict(w.static_settings)
+    if args.learned:
+        _heat_learned_setup(w, args.size)
+        static["type of preconditioner"] = "learned"
+    settings = w.steps[0](dict(w.settings)) if w.steps else w.settings
+    kw = dict(newton_tol=0.0, newton_rtol=RTOL, maxiter=30, krylov_tol=args.krylov_tol, krylov_maxiter=400000)
+    solver.solver(w.dofs, settings, static, **kw)
+    _sync()
+    print(f"solve {w.name}: {json.dumps(_info())}")
 
 
 def main():
@@ -545,22 +787,27 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--size", type=int, default=64)
-    ap.add_argument("--krylov-tol", type=float, default=1e-4)
-    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only-mixed", action="store_true", help="time the mixed path only (profiling runs)")
-    ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner heat section")
-    ap.add_argument("--learned-n", type=int, default=1024)
-    ap.add_argument("--more-workloads", action="store_true", help="also time the Poisson, Cook and 3-D transient heat workloads")
-    ap.add_argument("--ref-newton-iters", type=int, default=4)
-    ap.add_argument("--ref-cg-iters", type=int, default=3000)
+    ap.add_argument("--only-headline", action="store_true", help="time the headline only (profiling runs)")
+    ap.add_argument("--cook-steps", type=int, default=1)
+    ap.add_argument("--case", choices=["conv", "assembly", "solve"], help="one small case for ncu captures")
+    ap.add_argument("--workload", default="heat", choices=["heat", "poisson", "neo_hooke", "cook"])
+    ap.add_argument("--precision", default="mixed")
+    ap.add_argument("--solver", default="pcg")
+    ap.add_argument("--learned", action="store_true")
+    ap.add_argument("--krylov-tol", type=float, default=1e-4)
+    ap.add_argument("--layer", default="e0b")
+    ap.add_argument("--reps", type=int, default=3)
     args = ap.parse_args()
-    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+    if args.case:
+        case(args)
+        return
     if args.impl == "reference":
         reference_arm(args)
-    else:
-        gpu_arm(args)
+        return
+    args.warmup = max(args.warmup, 3)
+    gpu_arm(args)
 
 
 if __name__ == "__main__":

@@ -237,8 +237,9 @@ int agx_set_preconditioner_mode(agx_context* ctx, int mode, double omega, int sw
 #define AGX_PROF_RESIDUAL 1  /* float64 residual-only element passes */
 #define AGX_PROF_SPMV 2      /* sparse products of the Krylov iterations */
 #define AGX_PROF_VECTOR 3    /* Krylov vector updates with their reductions */
-#define AGX_PROF_PRECOND 4   /* preconditioner applications */
+#define AGX_PROF_PRECOND 4   /* the registered preconditioner callback (the network) */
 #define AGX_PROF_FACTOR 5    /* direct factorizations */
+#define AGX_PROF_SMOOTH 6    /* products of the two-level preconditioner's smoothing and step */
 #define AGX_PROF_CATEGORIES 8
 int agx_profile(agx_context* ctx, int enable);
 int agx_profile_read(agx_context* ctx, double* ms, int64_t* launches);

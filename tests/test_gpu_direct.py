@@ -33,7 +33,9 @@ def test_direct_solve_matches_spsolve(case):
     from autopdex_gb300._problem import get_problem
     w = {"poisson": lambda: configs.poisson(n=30), "cook": lambda: configs.cook_membrane(n=12, n_steps=2),
          "neo_hooke_3d": lambda: configs.neo_hooke_cube(n=4, n_steps=2)}[case]()
-    scale = {"poisson": 1.0, "cook": 0.05, "neo_hooke_3d": 0.02}[case]
+    # small random states: with lam / mu = 5000 (Cook, nu = 0.4999) larger ones make the tangent
+    # indefinite (pressure stiffness of a far-from-equilibrium state), and Cholesky rightly fails
+    scale = {"poisson": 1.0, "cook": 1e-5, "neo_hooke_3d": 0.005}[case]
     rng = np.random.default_rng(11)
     u = rng.uniform(-scale, scale, w.n_dofs)
     if case == "cook":
@@ -48,17 +50,22 @@ def test_direct_solve_matches_spsolve(case):
     b_dev = torch.as_tensor(b, device=prob.device)
     x = torch.empty_like(b_dev)
     opts = N.SolveOpts()
-    opts.method, opts.rtol, opts.atol, opts.maxiter, opts.check_every = N.AGX_CHOL_BAND, 1e-13, 0.0, 10, 1
+    # the membrane's condition number (~1e8 at nu = 0.4999) bounds the attainable float64
+    # relative residual near 1e-11 and the agreement of two backward-stable solvers near 1e-8
+    rtol, xtol = {"poisson": (1e-13, 1e-11), "cook": (1e-10, 1e-7), "neo_hooke_3d": (1e-13, 1e-11)}[case]
+    opts.method, opts.rtol, opts.atol, opts.maxiter, opts.check_every = N.AGX_CHOL_BAND, rtol, 0.0, 10, 1
     info = N.SolveInfo()
     rc = prob._call("agx_solve", N.C.c_void_p(b_dev.data_ptr()), N.C.c_void_p(x.data_ptr()), N.C.byref(opts),
                     N.C.byref(info))
-    assert rc == N.AGX_OK and info.status == N.AGX_OK and info.rel_residual <= 1e-13
+    assert rc == N.AGX_OK and info.status == N.AGX_OK and info.rel_residual <= rtol, (rc, info.rel_residual)
     op = oracle_problem(w)
     _, coo = newton.assemble(op.sets, u, op.coords, oracle_settings(w), op.n_dofs)
     A = newton.scipy_assembling(coo, op.n_dofs, free)
     ref = spla.spsolve(A.tocsc(), b[free])
     got = x.cpu().numpy()
-    assert np.abs(got[free] - ref).max() <= 1e-11 * np.abs(ref).max()
+    rel_sp = np.linalg.norm(A @ ref - b[free]) / np.linalg.norm(b[free])
+    assert info.rel_residual <= max(rtol, 10.0 * rel_sp)
+    assert np.abs(got[free] - ref).max() <= xtol * np.abs(ref).max()
     assert np.all(got[~free] == 0.0)
 
 
@@ -84,3 +91,26 @@ def test_cook_load_step_direct_matches_oracle():
     assert not div and res <= 1e-8
     ref, info, _ = newton.damped_newton(oracle_problem(w), np.zeros(w.n_dofs), oracle_settings(w), 1e-8)
     assert np.abs(_flat(sol) - ref).max() <= 1e-8 * max(1.0, np.abs(ref).max())
+
+
+def test_indefinite_tangent_reports_breakdown():
+    """A far-from-equilibrium state of the nearly incompressible membrane has an indefinite
+    tangent: the factorization reports AGX_DIVERGED (no exception, no garbage solution
+    claimed as converged)."""
+    import torch
+    from autopdex_gb300 import _native as N
+    from autopdex_gb300._problem import get_problem
+    w = configs.cook_membrane(n=12, n_steps=2)
+    u = np.random.default_rng(11).uniform(-0.05, 0.05, w.n_dofs)
+    prob = get_problem(w.dofs, w.settings, w.static_settings)
+    prob.update_models(w.settings)
+    x_dev = torch.as_tensor(u, device=prob.device)
+    prob._call("agx_assemble", N.C.c_void_p(x_dev.data_ptr()), None, N.AGX_F64)
+    b = torch.ones(w.n_dofs, dtype=torch.float64, device=prob.device)
+    x = torch.empty_like(b)
+    opts = N.SolveOpts()
+    opts.method, opts.rtol, opts.atol, opts.maxiter, opts.check_every = N.AGX_CHOL_BAND, 1e-13, 0.0, 10, 1
+    info = N.SolveInfo()
+    rc = prob._call("agx_solve", N.C.c_void_p(b.data_ptr()), N.C.c_void_p(x.data_ptr()), N.C.byref(opts),
+                    N.C.byref(info))
+    assert rc == N.AGX_DIVERGED and info.status == N.AGX_DIVERGED
