@@ -22,7 +22,7 @@ AGX_MODEL_NEO_HOOKE = 2
 AGX_MODEL_NEUMANN = 3
 AGX_MODEL_HEAT_BE = 4
 AGX_F64, AGX_F32 = 0, 1
-AGX_PCG, AGX_PCG_MIXED, AGX_BICGSTAB, AGX_FCG_MIXED, AGX_CHOL_BAND = 0, 1, 2, 3, 4
+AGX_PCG, AGX_PCG_MIXED, AGX_BICGSTAB, AGX_FCG_MIXED, AGX_CHOL_BAND, AGX_FCG_F64 = 0, 1, 2, 3, 4, 5
 
 AGX_PROF_TANGENT, AGX_PROF_RESIDUAL, AGX_PROF_SPMV, AGX_PROF_VECTOR, AGX_PROF_PRECOND = 0, 1, 2, 3, 4
 AGX_PROF_FACTOR, AGX_PROF_SMOOTH = 5, 6
@@ -102,6 +102,11 @@ _SIGNATURES = {
     "agx_nn_restrict": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, _P, _P]),
     "agx_nn_prolong": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P]),
     "agx_nn_vector_from_grid": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P]),
+    "agx_nn_grid_from_field": (C.c_int, [_P, C.c_int, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P,
+                                         _P, _P]),
+    "agx_nn_field_from_grid": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P]),
+    "agx_nn_restrict_field": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P]),
+    "agx_nn_prolong_field": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P]),
 }
 
 _lib = None

@@ -64,6 +64,7 @@ void free_device(agx_context* ctx) {
   release(ctx->d_band);
   release(ctx->d_band_err);
   release(ctx->d_band_l11);
+  release(ctx->d_band_rdiag);
   for (double** p : {&ctx->d_R, &ctx->d_b, &ctx->d_dx, &ctx->d_r, &ctx->d_z, &ctx->d_p, &ctx->d_q, &ctx->d_s,
                      &ctx->d_t, &ctx->d_rhat, &ctx->d_v})
     release(*p);
@@ -544,8 +545,8 @@ int agx_newton(agx_context* ctx, double* dofs, const double* dvals, const agx_ne
   if (!dofs || !dvals || !opts) return agx_fail(ctx, AGX_ERR_ARG, "null argument");
   const int tdt = opts->tangent_dtype;
   const int kry = opts->krylov.method;
-  if ((kry == AGX_PCG || kry == AGX_BICGSTAB || kry == AGX_CHOL_BAND) && tdt != AGX_F64)
-    return agx_fail(ctx, AGX_ERR_ARG, "PCG, BiCGStab and the banded Cholesky solve need a float64 tangent");
+  if ((kry == AGX_PCG || kry == AGX_BICGSTAB || kry == AGX_CHOL_BAND || kry == AGX_FCG_F64) && tdt != AGX_F64)
+    return agx_fail(ctx, AGX_ERR_ARG, "PCG, BiCGStab, float64 FCG and the banded Cholesky solve need a float64 tangent");
   if ((kry == AGX_PCG_MIXED || kry == AGX_FCG_MIXED) && tdt != AGX_F32)
     return agx_fail(ctx, AGX_ERR_ARG, "mixed methods need a float32 tangent");
   agx_newton_info out{};
@@ -593,7 +594,9 @@ int agx_newton(agx_context* ctx, double* dofs, const double* dvals, const agx_ne
       if (nonfinite > 0 || !std::isfinite(res)) div = true;
       next_step = !div;
     } else {
-      printf("Warning: Newton scheme could not converge!\n");
+      // the reference prints this warning (solver.py:926-927); a library writes it to stderr so
+      // that it cannot interleave with a caller's output on stdout
+      fprintf(stderr, "Warning: Newton scheme could not converge!\n");
       next_step = false;
       div = true;
     }

@@ -135,7 +135,7 @@ struct agx_context {
     int tpr = 0;                   // lanes per row of the captured products
     std::vector<cudaEvent_t> ev[AGX_PROF_CATEGORIES];  // event pairs recorded by each replay
   };
-  graph_rec graphs[2];
+  graph_rec graphs[3];  // Jacobi-PCG float64, float32 methods, flexible CG float64
   graph_rec* capturing = nullptr;  // set while a chunk is being captured
   bool use_graphs = true;
   // the legacy default stream cannot be captured: graphs then run on this private stream,
@@ -155,6 +155,7 @@ struct agx_context {
   int precond_capturable = 0;  // the callback only enqueues work on the stream it is given
   int64_t precond_gen = 0;     // bumped whenever the callback or its mode changes
   int spmv_tpr[2] = {0, 0};  // lanes per block row of the Krylov product, float64 / float32 (0: default)
+  int64_t f32_copy_gen = -1;  // tangent generation whose float32 copy (values, inverse diagonal) is current
 
   // banded Cholesky factor of the float64 tangent (AGX_CHOL_BAND): lower band stored by
   // columns, entry (j + k, j) at d_band[j (band_w + 1) + k], k = 0 .. band_w
@@ -162,6 +163,7 @@ struct agx_context {
   double* d_band = nullptr;     // n_dofs * (band_w + 1)
   int* d_band_err = nullptr;    // first column whose pivot was not positive (+1), 0 if none
   double* d_band_l11 = nullptr; // factored diagonal block of the current panel (scratch)
+  double* d_band_rdiag = nullptr;  // reciprocals of the factor's diagonal (n_dofs)
   int64_t band_gen = -1;        // tangent generation the factor belongs to
   double band_sign = 1.0;       // the factor is of band_sign * K (-1 for negative definite tangents)
   size_t band_max_bytes = (size_t)24 << 30;  // largest factor this context allocates

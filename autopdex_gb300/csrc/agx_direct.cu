@@ -32,10 +32,24 @@ namespace {
 
 constexpr int NB = 32;   // panel width
 constexpr int TM = 64;   // update tile
-constexpr int PF_THREADS = 128;
+constexpr int PF_THREADS = 64;  // rows of the block below the diagonal block per CTA
 constexpr int SOLVE_THREADS = 1024;
 
 __host__ __device__ __forceinline__ int64_t imin(int64_t a, int64_t b) { return a < b ? a : b; }
+
+// 1 / sqrt(d) for a positive float64 pivot: a float32 estimate refined by two steps of the
+// Newton-Raphson iteration y <- y (3 - d y^2) / 2 for the reciprocal square root (each step
+// roughly squares the relative error: ~1e-7 -> ~1e-14 -> rounding level).  GB300 runs float64 at
+// 1/64 of its float32 rate, and the pivots of a band factorization form a sequential chain, so
+// this replaces a float64 square root and a float64 division per column.  Outside the float32
+// range the float64 square root is used instead.
+__device__ __forceinline__ double pivot_rsqrt(double d) {
+  if (!(d > 1e-30 && d < 1e30)) return 1.0 / sqrt(d);
+  double y = (double)rsqrtf((float)d);
+  y = y * (1.5 - 0.5 * d * y * y);
+  y = y * (1.5 - 0.5 * d * y * y);
+  return y;
+}
 
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
@@ -87,8 +101,9 @@ __global__ void diag_signs(int64_t n_dofs, int ndof, int64_t nnzb, const int32_t
 // Factor of the diagonal block of panel j0 (nbp columns) and the rows below it.
 __global__ void __launch_bounds__(PF_THREADS)
 panel_factor(double* __restrict__ band, int64_t n, int64_t w, int64_t j0, int nbp, double* __restrict__ l11,
-             int* __restrict__ err) {
+             double* __restrict__ rdiag, int* __restrict__ err) {
   __shared__ double L[NB][NB + 1];
+  __shared__ double rinv[NB];  // reciprocals of the pivots L_qq
   const int64_t ld = w + 1;
   for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
     const int i = idx / NB, q = idx % NB;
@@ -102,11 +117,13 @@ panel_factor(double* __restrict__ band, int64_t n, int64_t w, int64_t j0, int nb
         if (blockIdx.x == 0) atomicCAS(err, 0, (int)(j0 + q + 1));
         d = 1.0;
       }
-      L[q][q] = sqrt(d);
+      const double y = pivot_rsqrt(d);
+      L[q][q] = d * y;
+      rinv[q] = y;
     }
     __syncthreads();
-    const double piv = L[q][q];
-    for (int i = q + 1 + threadIdx.x; i < nbp; i += blockDim.x) L[i][q] /= piv;
+    const double ri = rinv[q];
+    for (int i = q + 1 + threadIdx.x; i < nbp; i += blockDim.x) L[i][q] *= ri;
     __syncthreads();
     const int m = nbp - q - 1;
     for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
@@ -115,8 +132,10 @@ panel_factor(double* __restrict__ band, int64_t n, int64_t w, int64_t j0, int nb
     }
     __syncthreads();
   }
-  if (blockIdx.x == 0)
+  if (blockIdx.x == 0) {
     for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) l11[idx] = L[idx / NB][idx % NB];
+    if (threadIdx.x < nbp) rdiag[j0 + threadIdx.x] = rinv[threadIdx.x];
+  }
   // one row of L21 per thread: x L11^T = a  (rows r = j0 + nbp + R, R < w)
   const int64_t R = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t r = j0 + nbp + R;
@@ -133,7 +152,7 @@ panel_factor(double* __restrict__ band, int64_t n, int64_t w, int64_t j0, int nb
       double v = x[q];
 #pragma unroll
       for (int p = 0; p < q; ++p) v -= x[p] * L[q][p];
-      x[q] = v / L[q][q];
+      x[q] = v * rinv[q];
     }
   }
 #pragma unroll
@@ -193,7 +212,8 @@ syrk_update(double* __restrict__ band, int64_t n, int64_t w, int64_t j0, int nbp
 }
 
 // v <- L^-1 v (one CTA)
-__global__ void __launch_bounds__(SOLVE_THREADS) band_forward(const double* __restrict__ band, int64_t n, int64_t w,
+__global__ void __launch_bounds__(SOLVE_THREADS) band_forward(const double* __restrict__ band,
+                                                              const double* __restrict__ rdiag, int64_t n, int64_t w,
                                                               double* __restrict__ v) {
   __shared__ double L[NB][NB + 1];
   __shared__ double y[NB];
@@ -209,7 +229,7 @@ __global__ void __launch_bounds__(SOLVE_THREADS) band_forward(const double* __re
     if (threadIdx.x < 32) {
       double yi = lane < nbp ? v[j0 + lane] : 0.0;
       for (int q = 0; q < nbp; ++q) {
-        if (lane == q) yi /= L[q][q];
+        if (lane == q) yi *= rdiag[j0 + q];
         const double yq = __shfl_sync(0xffffffffu, yi, q);
         if (lane > q && lane < nbp) yi -= L[lane][q] * yq;
       }
@@ -234,7 +254,8 @@ __global__ void __launch_bounds__(SOLVE_THREADS) band_forward(const double* __re
 }
 
 // v <- L^-T v (one CTA)
-__global__ void __launch_bounds__(SOLVE_THREADS) band_backward(const double* __restrict__ band, int64_t n, int64_t w,
+__global__ void __launch_bounds__(SOLVE_THREADS) band_backward(const double* __restrict__ band,
+                                                               const double* __restrict__ rdiag, int64_t n, int64_t w,
                                                                double* __restrict__ v) {
   __shared__ double L[NB][NB + 1];
   __shared__ double s[NB];
@@ -260,7 +281,7 @@ __global__ void __launch_bounds__(SOLVE_THREADS) band_backward(const double* __r
     if (threadIdx.x < 32) {
       double xi = lane < nbp ? v[j0 + lane] - s[lane] : 0.0;
       for (int q = nbp - 1; q >= 0; --q) {
-        if (lane == q) xi /= L[q][q];
+        if (lane == q) xi *= rdiag[j0 + q];
         const double xq = __shfl_sync(0xffffffffu, xi, q);
         if (lane < q) xi -= L[q][lane] * xq;
       }
@@ -306,8 +327,8 @@ int band_width(agx_context* ctx) {
 }
 
 void forward_backward(agx_context* ctx, double* v) {
-  band_forward<<<1, SOLVE_THREADS, 0, ctx->stream>>>(ctx->d_band, ctx->n_dofs, ctx->band_w, v);
-  band_backward<<<1, SOLVE_THREADS, 0, ctx->stream>>>(ctx->d_band, ctx->n_dofs, ctx->band_w, v);
+  band_forward<<<1, SOLVE_THREADS, 0, ctx->stream>>>(ctx->d_band, ctx->d_band_rdiag, ctx->n_dofs, ctx->band_w, v);
+  band_backward<<<1, SOLVE_THREADS, 0, ctx->stream>>>(ctx->d_band, ctx->d_band_rdiag, ctx->n_dofs, ctx->band_w, v);
   ctx->n_launches += 2;
 }
 
@@ -351,7 +372,7 @@ int band_factor(agx_context* ctx) {
   for (int64_t j0 = 0; j0 < n; j0 += NB) {
     const int nbp = (int)imin(NB, n - j0);
     panel_factor<<<pf_grid, PF_THREADS, 0, ctx->stream>>>(ctx->d_band, n, w, j0, nbp, ctx->d_band_l11,
-                                                          ctx->d_band_err);
+                                                          ctx->d_band_rdiag, ctx->d_band_err);
     syrk_update<<<sy_grid, 256, 0, ctx->stream>>>(ctx->d_band, n, w, j0, nbp, ctx->d_band_l11);
     ctx->n_launches += 2;
   }
@@ -383,6 +404,7 @@ int agx_band_solve_impl(agx_context* ctx, const double* b, double* x, const agx_
     AGX_CUDA(ctx, cudaMalloc(&ctx->d_band, (size_t)bytes));
     AGX_CUDA(ctx, cudaMalloc(&ctx->d_band_err, sizeof(int)));
     AGX_CUDA(ctx, cudaMalloc(&ctx->d_band_l11, sizeof(double) * NB * NB));
+    AGX_CUDA(ctx, cudaMalloc(&ctx->d_band_rdiag, sizeof(double) * n));
   }
   if (ctx->band_gen != ctx->tangent_gen) {
     agx_prof_scope ps(ctx, AGX_PROF_FACTOR);

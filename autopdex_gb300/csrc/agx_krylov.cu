@@ -665,6 +665,30 @@ bicg_init(int64_t n, const double* __restrict__ b, double* __restrict__ x, doubl
   }
 }
 
+// ---- float64 flexible CG with a float32 preconditioner ---------------------------------
+// f_r = r / ||b|| (float32), and back: z = f_z ||b||
+__global__ void __launch_bounds__(AGX_BLOCK) to_f32_scaled(int64_t n, const double* __restrict__ r,
+                                                           float* __restrict__ f, const agx_krylov_scalars* sc) {
+  if (sc->converged) return;
+  const double s = sc->extra[0];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    f[i] = (float)(r[i] * s);
+}
+
+__global__ void __launch_bounds__(AGX_BLOCK) from_f32_scaled(int64_t n, const float* __restrict__ f,
+                                                             double* __restrict__ z, const agx_krylov_scalars* sc) {
+  if (sc->converged) return;
+  const double s = sc->extra[1];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    z[i] = (double)f[i] * s;
+}
+
+// float32 copy of a float64 array (tangent values, inverse diagonal)
+__global__ void copy_to_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
 // ---- conversions and helpers ---------------------------------------------------------
 template <typename T>
 __global__ void to_double_scaled(int64_t n, const T* __restrict__ x, double* __restrict__ out,
@@ -1138,6 +1162,21 @@ int apply_registered_preconditioner(agx_context* ctx) {
   return 0;
 }
 
+// float32 copy of the float64 tangent (values and inverse diagonal) for the float32
+// preconditioner of the float64 flexible CG, made once per assembled tangent
+int ensure_f32_copy(agx_context* ctx) {
+  if (ctx->tangent_valid != AGX_F64)
+    return agx_fail(ctx, AGX_ERR_STATE, "float64 flexible CG needs a float64 tangent (assemble first)");
+  if (ctx->f32_copy_gen == ctx->tangent_gen) return AGX_OK;
+  const int64_t nv = ctx->nnzb * ctx->ndof * ctx->ndof;
+  copy_to_f32<<<agx_grid(ctx, nv), AGX_BLOCK, 0, ctx->stream>>>(nv, ctx->d_vals64, ctx->d_vals32);
+  copy_to_f32<<<agx_grid(ctx, ctx->n_dofs), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dofs, ctx->d_dinv64, ctx->d_dinv32);
+  AGX_CHECK_LAUNCH(ctx);
+  ctx->n_launches += 2;
+  ctx->f32_copy_gen = ctx->tangent_gen;
+  return AGX_OK;
+}
+
 // Gershgorin bound for the Chebyshev smoother, recomputed once per float32 tangent (host
 // synchronisation; called before any capture)
 int update_chebyshev_bound(agx_context* ctx) {
@@ -1269,6 +1308,74 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
     }
     to_double_scaled<float><<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, x, sc, 1);
     ctx->n_launches += 1;
+  } else if (method == AGX_FCG_F64) {
+    if (int rc = ensure_f32_copy(ctx)) return rc;
+    const bool flexible = ctx->precond != nullptr;
+    bool precond_failed = false;
+    double* pbuf[2] = {ctx->d_p, ctx->d_s};
+    int cur = 0;
+    pcg_init_kernel<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, rhs, ctx->d_dinv64, x, ctx->d_r, ctx->d_z, pbuf[0],
+                                                             sc, ctx->d_partials, ctx->d_counter, 0, flexible ? 0 : 1);
+    // z = M r: the float32 preconditioner on r / ||b|| (Jacobi in float64 without a callback)
+    auto precond = [&]() {
+      if (!flexible) {
+        agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
+        jacobi_apply<double><<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv64, ctx->d_r, ctx->d_z, sc);
+        ctx->n_launches += 1;
+        return;
+      }
+      {
+        agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
+        to_f32_scaled<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_r, ctx->f_r, sc);
+      }
+      if (apply_registered_preconditioner(ctx) != 0) precond_failed = true;
+      {
+        agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
+        from_f32_scaled<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_z, ctx->d_z, sc);
+      }
+      ctx->n_launches += 2;
+    };
+    if (flexible) {
+      if (int rc = update_chebyshev_bound(ctx)) return rc;
+      precond();
+      if (precond_failed) return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");
+    }
+    fcg_direction_dots<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_r, ctx->d_z, ctx->d_q, sc, ctx->d_partials,
+                                                                ctx->d_counter);
+    ctx->n_launches += 1;
+    auto chunk = [&](int kn) {
+      for (int k = 0; k < kn; ++k) {
+        double* pnew = pbuf[cur ^ 1];
+        launch_spmv_dot<double>(ctx, ctx->d_vals64, ctx->d_z, pbuf[cur], pnew, ctx->d_q, (const double*)ctx->d_r, 0);
+        {
+          agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
+          fcg_update_kernel<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, x, ctx->d_r, pnew, ctx->d_q, sc,
+                                                                     ctx->d_partials, ctx->d_counter);
+        }
+        precond();
+        {
+          agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
+          fcg_direction_dots<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_r, ctx->d_z, ctx->d_q, sc,
+                                                                      ctx->d_partials, ctx->d_counter);
+        }
+        cur ^= 1;
+      }
+    };
+    while (true) {
+      const int kn = std::min(every, maxiter - it_done);
+      ctx->n_launches += 3 * kn;
+      if (flexible && !ctx->precond_capturable) {
+        chunk(kn);
+        AGX_CHECK_LAUNCH(ctx);
+      } else if (int rc = run_chunk(ctx, 2, x, every, kn, chunk, flexible ? ctx->precond_gen : -1)) {
+        return rc;
+      }
+      if (precond_failed) return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");
+      int rc = read_scalars(ctx);
+      if (rc) return rc;
+      it_done = ctx->h_scal->iters;
+      if (ctx->h_scal->converged || it_done >= maxiter) break;
+    }
   } else if (method == AGX_BICGSTAB) {
     bicg_init<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, rhs, x, ctx->d_r, ctx->d_rhat, ctx->d_p, ctx->d_v, sc);
     while (true) {

@@ -20,6 +20,7 @@
 #include <cudaTypedefs.h>
 
 #include "agx_common.cuh"
+#include "../../include/autopdex_gb300_nn.h"
 
 namespace {
 
@@ -545,9 +546,12 @@ __global__ void bias_grad_kernel(const __nv_bfloat16* __restrict__ g, int64_t P,
 // node vector (float, n_nodes = Hn x Wn, node i*Wn + j) -> NHWC C = 16 image (Hp x Wp) with
 // channel 0 = s * r, channel 1 = aux (per-node feature), other channels 0; s = 1/rms(r) read
 // from scale[0] (null: 1).  One image per call (B = 1).
-__global__ void grid_from_vector_kernel(const float* __restrict__ r, const float* __restrict__ aux,
-                                        const float* __restrict__ scale, int Hn, int Wn, int Hp, int Wp,
-                                        __nv_bfloat16* __restrict__ img) {
+// node field (Hn x Wn nodes, nd interleaved components: r[node nd + c]) -> NHWC 16-channel
+// image Hp x Wp: channels 0 .. nd-1 the field (times scale[0] when given), channels
+// nd .. nd+naux-1 the per-node features aux[node naux + a], zeros elsewhere
+__global__ void grid_from_field_kernel(const float* __restrict__ r, int nd, const float* __restrict__ aux, int naux,
+                                       const float* __restrict__ scale, int Hn, int Wn, int Hp, int Wp,
+                                       __nv_bfloat16* __restrict__ img) {
   const int64_t total = (int64_t)Hp * Wp;
   const float s = scale ? scale[0] : 1.0f;
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < total; p += (int64_t)gridDim.x * blockDim.x) {
@@ -557,8 +561,9 @@ __global__ void grid_from_vector_kernel(const float* __restrict__ r, const float
     for (int c = 0; c < 16; ++c) h[c] = __float2bfloat16(0.0f);
     if (i < Hn && j < Wn) {
       const int64_t node = (int64_t)i * Wn + j;
-      h[0] = __float2bfloat16(s * r[node]);
-      if (aux) h[1] = __float2bfloat16(aux[node]);
+      for (int c = 0; c < nd; ++c) h[c] = __float2bfloat16(s * r[node * nd + c]);
+      if (aux)
+        for (int a = 0; a < naux; ++a) h[nd + a] = __float2bfloat16(aux[node * naux + a]);
     }
     uint4* dst = reinterpret_cast<uint4*>(img + p * 16);
     dst[0] = reinterpret_cast<uint4*>(h)[0];
@@ -566,14 +571,15 @@ __global__ void grid_from_vector_kernel(const float* __restrict__ r, const float
   }
 }
 
-// channel 0 of an NHWC image with C channels -> node vector
-__global__ void vector_from_grid_kernel(const __nv_bfloat16* __restrict__ img, int C, int Hn, int Wn, int Wp,
-                                        float* __restrict__ z) {
-  const int64_t total = (int64_t)Hn * Wn;
-  for (int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; node < total;
-       node += (int64_t)gridDim.x * blockDim.x) {
+// channels 0 .. nd-1 of an NHWC image with C channels -> node field z[node nd + c]
+__global__ void field_from_grid_kernel(const __nv_bfloat16* __restrict__ img, int C, int nd, int Hn, int Wn, int Wp,
+                                       float* __restrict__ z) {
+  const int64_t total = (int64_t)Hn * Wn * nd;
+  for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d < total; d += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t node = d / nd;
+    const int c = (int)(d - node * nd);
     const int i = (int)(node / Wn), j = (int)(node % Wn);
-    z[node] = __bfloat162float(img[((int64_t)i * Wp + j) * C]);
+    z[d] = __bfloat162float(img[((int64_t)i * Wp + j) * C + c]);
   }
 }
 
@@ -597,31 +603,37 @@ __global__ void inv_rms_kernel(const float* __restrict__ r, int64_t n, float* __
 // Prolongation: fine(i, j) = sum over the (up to 4) surrounding coarse nodes of
 // w(i - f I) w(j - f J) coarse(I, J), w(d) = 1 - |d| / f.  Restriction is its transpose,
 // evaluated as a gather over the (2f - 1)^2 fine nodes around each coarse node.
-__global__ void prolong_kernel(const float* __restrict__ c, int Hc, int Wc, int f, float* __restrict__ out) {
+__global__ void prolong_kernel(const float* __restrict__ c, int nd, int Hc, int Wc, int f, float* __restrict__ out) {
   const int Wf = (Wc - 1) * f + 1;
-  const int64_t total = (int64_t)((Hc - 1) * f + 1) * Wf;
+  const int64_t total = (int64_t)((Hc - 1) * f + 1) * Wf * nd;
   const float inv = 1.0f / (float)f;
-  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < total; p += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d < total; d += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = d / nd;
+    const int k = (int)(d - p * nd);
     const int i = (int)(p / Wf), j = (int)(p - (int64_t)(p / Wf) * Wf);
     const int I = i / f, J = j / f;
     const float ti = (float)(i - I * f) * inv, tj = (float)(j - J * f) * inv;
     const int I1 = I + 1 < Hc ? I + 1 : I, J1 = J + 1 < Wc ? J + 1 : J;
-    const float v00 = c[(int64_t)I * Wc + J], v01 = c[(int64_t)I * Wc + J1];
-    const float v10 = c[(int64_t)I1 * Wc + J], v11 = c[(int64_t)I1 * Wc + J1];
-    out[p] = (1.0f - ti) * ((1.0f - tj) * v00 + tj * v01) + ti * ((1.0f - tj) * v10 + tj * v11);
+    const float v00 = c[((int64_t)I * Wc + J) * nd + k], v01 = c[((int64_t)I * Wc + J1) * nd + k];
+    const float v10 = c[((int64_t)I1 * Wc + J) * nd + k], v11 = c[((int64_t)I1 * Wc + J1) * nd + k];
+    out[d] = (1.0f - ti) * ((1.0f - tj) * v00 + tj * v01) + ti * ((1.0f - tj) * v10 + tj * v11);
   }
 }
 
-__global__ void restrict_kernel(const float* __restrict__ fine, const unsigned char* __restrict__ fixed, int Hc, int Wc,
-                                int f, float* __restrict__ out) {
+// coarse = P^T fine per component; `fixed` (optional) flags fine DOFs (node nd + component):
+// a coarse component whose fine DOF at the same node is fixed is zero
+__global__ void restrict_kernel(const float* __restrict__ fine, const unsigned char* __restrict__ fixed, int nd, int Hc,
+                                int Wc, int f, float* __restrict__ out) {
   const int Hf = (Hc - 1) * f + 1, Wf = (Wc - 1) * f + 1;
-  const int64_t total = (int64_t)Hc * Wc;
+  const int64_t total = (int64_t)Hc * Wc * nd;
   const float inv = 1.0f / (float)f;
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d < total; d += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = d / nd;
+    const int k = (int)(d - q * nd);
     const int I = (int)(q / Wc), J = (int)(q - (int64_t)(q / Wc) * Wc);
     const int ci = I * f, cj = J * f;
     float acc = 0.0f;
-    if (!(fixed && fixed[(int64_t)ci * Wf + cj])) {
+    if (!(fixed && fixed[((int64_t)ci * Wf + cj) * nd + k])) {
       for (int di = -(f - 1); di <= f - 1; ++di) {
         const int i = ci + di;
         if (i < 0 || i >= Hf) continue;
@@ -630,12 +642,12 @@ __global__ void restrict_kernel(const float* __restrict__ fine, const unsigned c
         for (int dj = -(f - 1); dj <= f - 1; ++dj) {
           const int j = cj + dj;
           if (j < 0 || j >= Wf) continue;
-          row += (1.0f - (float)abs(dj) * inv) * fine[(int64_t)i * Wf + j];
+          row += (1.0f - (float)abs(dj) * inv) * fine[((int64_t)i * Wf + j) * nd + k];
         }
         acc += wi * row;
       }
     }
-    out[q] = acc;
+    out[d] = acc;
   }
 }
 
@@ -818,30 +830,53 @@ int agx_nn_bias_grad(const void* g, int64_t P, int C, float* db, void* stream) {
 
 int agx_nn_grid_from_vector(const float* r, const float* aux, int Hn, int Wn, int Hp, int Wp, int normalize,
                             float* scale, void* img, void* stream) {
+  return agx_nn_grid_from_field(r, 1, aux, aux ? 1 : 0, Hn, Wn, Hp, Wp, normalize, scale, img, stream);
+}
+
+int agx_nn_grid_from_field(const float* r, int nd, const float* aux, int naux, int Hn, int Wn, int Hp, int Wp,
+                           int normalize, float* scale, void* img, void* stream) {
+  if (!r || !img || nd < 1 || nd > 3 || naux < 0 || nd + naux > 16 || (naux > 0 && !aux) || Hn > Hp || Wn > Wp ||
+      (normalize && !scale))
+    return AGX_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
-  if (normalize) inv_rms_kernel<<<1, 1024, 0, s>>>(r, (int64_t)Hn * Wn, scale);
-  grid_from_vector_kernel<<<grid1((int64_t)Hp * Wp), 256, 0, s>>>(r, aux, normalize ? scale : nullptr, Hn, Wn, Hp, Wp,
-                                                                  (__nv_bfloat16*)img);
+  if (normalize) inv_rms_kernel<<<1, 1024, 0, s>>>(r, (int64_t)Hn * Wn * nd, scale);
+  grid_from_field_kernel<<<grid1((int64_t)Hp * Wp), 256, 0, s>>>(r, nd, naux > 0 ? aux : nullptr, naux,
+                                                                 normalize ? scale : nullptr, Hn, Wn, Hp, Wp,
+                                                                 (__nv_bfloat16*)img);
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
 }
 
 int agx_nn_restrict(const float* fine, const unsigned char* fixed, int Hc, int Wc, int f, float* coarse,
                     void* stream) {
-  if (!fine || !coarse || Hc < 2 || Wc < 2 || f < 1 || f > 64) return AGX_ERR_ARG;
-  restrict_kernel<<<grid1((int64_t)Hc * Wc), 256, 0, (cudaStream_t)stream>>>(fine, fixed, Hc, Wc, f, coarse);
+  return agx_nn_restrict_field(fine, fixed, 1, Hc, Wc, f, coarse, stream);
+}
+
+int agx_nn_restrict_field(const float* fine, const unsigned char* fixed, int nd, int Hc, int Wc, int f, float* coarse,
+                          void* stream) {
+  if (!fine || !coarse || nd < 1 || nd > 3 || Hc < 2 || Wc < 2 || f < 1 || f > 64) return AGX_ERR_ARG;
+  restrict_kernel<<<grid1((int64_t)Hc * Wc * nd), 256, 0, (cudaStream_t)stream>>>(fine, fixed, nd, Hc, Wc, f, coarse);
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
 }
 
 int agx_nn_prolong(const float* coarse, int Hc, int Wc, int f, float* fine, void* stream) {
-  if (!fine || !coarse || Hc < 2 || Wc < 2 || f < 1 || f > 64) return AGX_ERR_ARG;
-  prolong_kernel<<<grid1((int64_t)((Hc - 1) * f + 1) * ((Wc - 1) * f + 1)), 256, 0, (cudaStream_t)stream>>>(
-      coarse, Hc, Wc, f, fine);
+  return agx_nn_prolong_field(coarse, 1, Hc, Wc, f, fine, stream);
+}
+
+int agx_nn_prolong_field(const float* coarse, int nd, int Hc, int Wc, int f, float* fine, void* stream) {
+  if (!fine || !coarse || nd < 1 || nd > 3 || Hc < 2 || Wc < 2 || f < 1 || f > 64) return AGX_ERR_ARG;
+  prolong_kernel<<<grid1((int64_t)((Hc - 1) * f + 1) * ((Wc - 1) * f + 1) * nd), 256, 0, (cudaStream_t)stream>>>(
+      coarse, nd, Hc, Wc, f, fine);
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
 }
 
 int agx_nn_vector_from_grid(const void* img, int C, int Hn, int Wn, int Wp, float* z, void* stream) {
-  vector_from_grid_kernel<<<grid1((int64_t)Hn * Wn), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)img, C,
-                                                                                    Hn, Wn, Wp, z);
+  return agx_nn_field_from_grid(img, C, 1, Hn, Wn, Wp, z, stream);
+}
+
+int agx_nn_field_from_grid(const void* img, int C, int nd, int Hn, int Wn, int Wp, float* z, void* stream) {
+  if (!img || !z || nd < 1 || nd > C || Wn > Wp) return AGX_ERR_ARG;
+  field_from_grid_kernel<<<grid1((int64_t)Hn * Wn * nd), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)img, C,
+                                                                                        nd, Hn, Wn, Wp, z);
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
 }
 

@@ -47,9 +47,15 @@ def padded(n):
 
 
 class UNet:
-    def __init__(self, device="cuda", seed=0, params=None):
+    """``n_in``: input channels in use (the field's components plus auxiliary features; the
+    rest of the 16 are padding and their weights stay zero)."""
+
+    def __init__(self, device="cuda", seed=0, params=None, n_in=2):
         self.lib = N.load()
         self.device = torch.device(device)
+        if params is not None and "meta.n_in" in params:
+            n_in = int(np.asarray(params["meta.n_in"]))
+        self.n_in = n_in
         g = torch.Generator().manual_seed(seed)
         self.w, self.b = {}, {}
         for name, c1, c2, co, relu in LAYERS:
@@ -57,19 +63,20 @@ class UNet:
             std = math.sqrt(2.0 / (9 * cin)) if relu else math.sqrt(1.0 / (9 * cin))
             w = torch.randn(co, cin, 3, 3, generator=g) * std
             if name == "e0a":
-                w[:, 2:] = 0.0  # channels 2..15 of the input are padding
+                w[:, n_in:] = 0.0  # channels n_in..15 of the input are padding
             self.w[name] = w.to(self.device)
             self.b[name] = torch.zeros(co, device=self.device)
         if params is not None:
             self.load_state(params)
         self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self.launches = 0  # kernels this network has launched (forward and backward passes)
         self._s, self._arena = None, None
         self.pack()
 
     # ---- parameters -------------------------------------------------------------------
     def state(self):
         return {f"{k}.w": v.detach().cpu().numpy() for k, v in self.w.items()} | \
-               {f"{k}.b": v.detach().cpu().numpy() for k, v in self.b.items()}
+               {f"{k}.b": v.detach().cpu().numpy() for k, v in self.b.items()} | {"meta.n_in": np.int64(self.n_in)}
 
     def load_state(self, st):
         for k in self.w:
@@ -126,6 +133,7 @@ class UNet:
         rc = self.lib.agx_nn_conv3x3(_p(x1), _p(x2), c1, c2, _p(self.img_f[name]), _p(self.b[name]), _p(out), None,
                                      co, co, relu, B, H, W, _p(self.err), self._stream())
         self._ok("agx_nn_conv3x3", rc)
+        self.launches += 1
         return out
 
     def _pool(self, x, B, H, W, c, key):
@@ -134,6 +142,7 @@ class UNet:
         while f < POOL:
             out = self._act(B, H // (2 * f), W // (2 * f), c, f"{key}.{f}")
             self._ok("agx_nn_pool2", self.lib.agx_nn_pool2(_p(x), _p(out), B, H // f, W // f, c, 0, self._stream()))
+            self.launches += 1
             x, f = out, 2 * f
         return x
 
@@ -144,6 +153,7 @@ class UNet:
             out = self._act(B, 2 * f * H, 2 * f * W, c, f"{key}.{f}")
             self._ok("agx_nn_upsample2", self.lib.agx_nn_upsample2(_p(x), _p(out), B, f * H, f * W, c, 0,
                                                                    self._stream()))
+            self.launches += 1
             x, f = out, 2 * f
         return x
 
@@ -281,15 +291,20 @@ def node_log_conductivity(k_elem, nx, ny):
     return (s / c).reshape(-1).astype(np.float32)
 
 
-def to_image(lib, r, aux, Hn, Wn, normalize=True, out=None, scale=None, stream=None):
+def to_image(lib, r, aux, Hn, Wn, normalize=True, out=None, scale=None, stream=None, nd=1, naux=None):
+    """Network input image of a node field r (nd components per node, node-major) and the
+    per-node auxiliary features aux (naux per node; 1 when not given)."""
     Hp, Wp = padded(Hn), padded(Wn)
     dev = r.device
     img = out if out is not None else torch.empty((1, Hp, Wp, C_IN), dtype=torch.bfloat16, device=dev)
     sc = scale if scale is not None else torch.empty(1, dtype=torch.float32, device=dev)
     st = stream or C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
-    rc = lib.agx_nn_grid_from_vector(_p(r), _p(aux), Hn, Wn, Hp, Wp, 1 if normalize else 0, _p(sc), _p(img), st)
+    if naux is None:
+        naux = 0 if aux is None else 1
+    rc = lib.agx_nn_grid_from_field(_p(r), nd, _p(aux), naux, Hn, Wn, Hp, Wp, 1 if normalize else 0, _p(sc),
+                                    _p(img), st)
     if rc != 0:
-        raise RuntimeError("agx_nn_grid_from_vector failed")
+        raise RuntimeError("agx_nn_grid_from_field failed")
     return img, sc
 
 
@@ -306,9 +321,10 @@ class TrainingSet:
     (float32, on the GPU), its error energy s = (r1, e1) / rms(r1)^2, and the index of its
     problem, whose float32 tangent values (the library's layout) are kept for K y."""
 
-    def __init__(self, n, prob, r1, s, pid, aux, values, free):
+    def __init__(self, n, prob, r1, s, pid, aux, values, free, nd=1, naux=1):
         self.n, self.prob = n, prob
         self.r1, self.s, self.pid, self.aux, self.values, self.free = r1, s, pid, aux, values, free
+        self.nd, self.naux = nd, naux
 
     def __len__(self):
         return self.r1.shape[0]
@@ -388,6 +404,130 @@ def make_training_set(n_problems, n=256, rhs_per_problem=2, seed0=0, iterates=IT
     return TrainingSet(n, prob, r1s, ss, pid, auxs, values, free)
 
 
+def node_features(coords):
+    """Per-node features of a membrane's node grid for the network: the coordinates centred and
+    scaled to [-1, 1] by the largest extent (n_nodes, 2)."""
+    c = np.asarray(coords, dtype=np.float64)
+    c = (c - c.mean(0)) / (np.abs(c - c.mean(0)).max() + 1e-300)
+    return c.astype(np.float32)
+
+
+def _direct(prob, rhs, x):
+    """x = K^-1 rhs with the banded Cholesky factor of the assembled float64 tangent."""
+    opts = N.SolveOpts()
+    opts.method, opts.rtol, opts.atol, opts.maxiter, opts.check_every = N.AGX_CHOL_BAND, 1e-6, 0.0, 1, 1
+    info = N.SolveInfo()
+    rc = prob.lib.agx_solve(prob.ctx, C.c_void_p(rhs.data_ptr()), C.c_void_p(x.data_ptr()), C.byref(opts),
+                            C.byref(info))
+    if rc < 0:
+        N.check(prob.ctx, "agx_solve", rc)
+    if info.status == N.AGX_DIVERGED:
+        raise RuntimeError("the banded Cholesky factorization met a non-positive pivot")
+    return info
+
+
+def chebyshev_presmooth(prob, r, dinv, lmax, degree, frac):
+    """Residual left by the degree-`degree` Chebyshev smoother for D^-1 K on [frac lmax, lmax]
+    started from z = 0 (the pre-smoothing of preconditioner mode 3), in float64."""
+    lmin = frac * lmax
+    theta, delta = 0.5 * (lmax + lmin), 0.5 * (lmax - lmin)
+    sigma = theta / delta
+    rho = 1.0 / sigma
+    d = dinv * r / theta
+    z = d.clone()
+    t = torch.empty_like(r)
+    for _ in range(1, degree):
+        prob._call("agx_spmv", N.AGX_F64, C.c_void_p(z.data_ptr()), C.c_void_p(t.data_ptr()))
+        rc = r - t
+        rn = 1.0 / (2.0 * sigma - rho)
+        d = rn * rho * d + (2.0 * rn / delta) * dinv * rc
+        z = z + d
+        rho = rn
+    prob._call("agx_spmv", N.AGX_F64, C.c_void_p(z.data_ptr()), C.c_void_p(t.data_ptr()))
+    return r - t
+
+
+def gershgorin_lmax(prob):
+    """max over rows of sum_j |K_ij| / |K_ii| of the assembled float64 tangent (the bound the
+    Chebyshev smoother of the native FCG uses)."""
+    b = prob.ndof
+    rp = torch.empty(prob.n_nodes + 1, dtype=torch.int32, device=prob.device)
+    col = torch.empty(prob.nnzb, dtype=torch.int32, device=prob.device)
+    vals = torch.empty((prob.nnzb, b, b), dtype=torch.float64, device=prob.device)
+    prob._call("agx_copy_matrix", N.AGX_F64, C.c_void_p(rp.data_ptr()), C.c_void_p(col.data_ptr()),
+               C.c_void_p(vals.data_ptr()))
+    row_of = torch.repeat_interleave(torch.arange(prob.n_nodes, device=prob.device), (rp[1:] - rp[:-1]).long())
+    absrow = torch.zeros((prob.n_nodes, b), dtype=torch.float64, device=prob.device)
+    absrow.index_add_(0, row_of, vals.abs().sum(2))
+    diag = vals[row_of == col.long()].diagonal(dim1=1, dim2=2).reshape(prob.n_nodes, b)
+    return float((absrow / diag.abs().clamp_min(1e-300)).max())
+
+
+def make_membrane_training_set(n=128, load_steps=(0, 5, 10, 15, 20), rhs_per_state=400, seed=0, degree=3,
+                               frac=1.0 / 30.0, verbose=False):
+    """Samples for the two-level preconditioner of the nearly incompressible Cook membrane
+    (plane-strain neo-Hooke, nu = 0.4999; the 512^2 membrane workload's geometry at n x n):
+    for the tangents at the converged states of the given load steps (0: the undeformed
+    state) and random smooth-plus-rough vector right-hand sides r, the residual r1 that the
+    Chebyshev pre-smoothing of the native FCG leaves and its error energy s = (r1, K^-1 r1),
+    K^-1 by the banded Cholesky factor of the float64 tangent.  Stored per sample: r1 / rms,
+    s / rms^2 and the state index (whose float32 tangent serves K y in training)."""
+    from . import configs, solver
+    from ._problem import get_problem
+    w = configs.cook_membrane(n=n, solver="lapack")
+    prob = get_problem(w.dofs, w.settings, w.static_settings)
+    dev = prob.device
+    nd = prob.ndof
+    mask = torch.as_tensor(prob.mask.astype(bool), device=dev)
+    free = (~mask).float()
+    rng = np.random.default_rng(seed + 4242)
+    aux = torch.as_tensor(node_features(w.raw["coords"]).reshape(-1), device=dev)
+    states = [np.zeros(w.n_dofs)] if 0 in load_steps else []
+    u = np.zeros(w.n_dofs)
+    settings = dict(w.settings)
+    for k in range(1, max(load_steps) + 1):
+        settings = w.steps[k - 1](settings)
+        sol, info = solver.solver(u.reshape(-1, nd), settings, w.static_settings, newton_tol=0.0, newton_rtol=1e-7,
+                                  maxiter=12)
+        u = np.asarray(sol).reshape(-1)
+        if k in load_steps:
+            states.append(u.copy())
+    nv = prob.nnzb * nd * nd
+    S = len(states) * rhs_per_state
+    values = torch.empty((len(states), nv), dtype=torch.float32, device=dev)
+    r1s = torch.empty((S, prob.n_dofs), dtype=torch.float32, device=dev)
+    ss = torch.empty(S, dtype=torch.float32, device=dev)
+    pid = torch.empty(S, dtype=torch.int64)
+    e1 = torch.empty(prob.n_dofs, dtype=torch.float64, device=dev)
+    dinv = torch.empty_like(e1)
+    ones = torch.ones_like(e1)
+    m = n + 1
+    j_out = 0
+    for i, us in enumerate(states):
+        x = torch.as_tensor(us, device=dev)
+        prob.update_models(settings)
+        prob._call("agx_assemble", C.c_void_p(x.data_ptr()), None, N.AGX_F32)
+        prob._call("agx_copy_values", N.AGX_F32, C.c_void_p(values[i].data_ptr()))
+        prob._call("agx_assemble", C.c_void_p(x.data_ptr()), None, N.AGX_F64)
+        prob._call("agx_jacobi", N.AGX_F64, C.c_void_p(ones.data_ptr()), C.c_void_p(dinv.data_ptr()))
+        lmax = gershgorin_lmax(prob)
+        for j in range(rhs_per_state):
+            r = torch.stack([_random_rhs(rng, m, dev) for _ in range(nd)], 1).reshape(-1)
+            r = torch.where(mask, torch.zeros_like(r), r)
+            r1 = chebyshev_presmooth(prob, r, dinv, lmax, degree, frac)
+            r1 = torch.where(mask, torch.zeros_like(r1), r1)
+            _direct(prob, r1, e1)
+            rms = r1.pow(2).mean().sqrt().clamp_min(1e-300)
+            r1s[j_out] = (r1 / rms).float()
+            ss[j_out] = float((r1 @ e1) / (rms * rms))
+            pid[j_out] = i
+            j_out += 1
+        if verbose:
+            print(f"state {i}: {rhs_per_state} samples, lmax {lmax:.3g}", flush=True)
+    auxs = aux.reshape(1, -1).expand(len(states), -1).contiguous()
+    return TrainingSet(n, prob, r1s, ss, pid, auxs, values, free, nd=nd, naux=2)
+
+
 def _random_rhs(rng, m, device):
     """Smooth-plus-rough random field on an m x m node grid."""
     f = np.zeros((m, m))
@@ -449,15 +589,16 @@ def train(net, ts, steps=3000, batch=16, lr=2e-3, seed=0, verbose=False):
         idx = torch.randint(0, len(ts), (batch,), generator=gen)
         pids = ts.pid[idx].tolist()
         for b, (i, pi) in enumerate(zip(idx.tolist(), pids)):
-            to_image(lib, ts.r1[i], ts.aux[pi], Hn, Wn, True, out=x[b:b + 1], scale=sc[b:b + 1], stream=stream)
+            to_image(lib, ts.r1[i], ts.aux[pi], Hn, Wn, True, out=x[b:b + 1], scale=sc[b:b + 1], stream=stream,
+                     nd=ts.nd, naux=ts.naux)
         out, acts = net.forward(x, keep=True)
-        y = (out[..., 0].float()[:, :Hn, :Wn].reshape(batch, -1) * ts.free).contiguous()
+        y = (out[..., :ts.nd].float()[:, :Hn, :Wn].reshape(batch, -1) * ts.free).contiguous()
         for b, pi in enumerate(pids):
             prob._call("agx_spmv_values", N.AGX_F32, C.c_void_p(ts.values[pi].data_ptr()),
                        C.c_void_p(y[b].data_ptr()), C.c_void_p(Ky[b].data_ptr()))
         r1 = ts.r1[idx.to(net.device)]
         loss, grad = energy_loss(r1, y, Ky, ts.s[idx.to(net.device)])
-        g[:, :Hn, :Wn, 0] = (grad * ts.free / batch).reshape(batch, Hn, Wn)
+        g[:, :Hn, :Wn, :ts.nd] = (grad * ts.free / batch).reshape(batch, Hn, Wn, ts.nd)
         # the backward pass is linear in g: run it on g / max|g| (bf16-friendly) and rescale
         gmax = float(g.abs().max().clamp_min(1e-30))
         gw, gb = net.backward((g / gmax).to(torch.bfloat16), acts)
@@ -469,7 +610,7 @@ def train(net, ts, steps=3000, batch=16, lr=2e-3, seed=0, verbose=False):
         sched.step()
         opt.zero_grad(set_to_none=True)
         with torch.no_grad():
-            net.w["e0a"][:, 2:] = 0.0
+            net.w["e0a"][:, net.n_in:] = 0.0
         net.pack()
         losses.append(float(loss.mean()))
         if verbose and step % 100 == 0:
@@ -489,7 +630,9 @@ def coarse_log_conductivity(k_elem, nx, ny, f):
 
 class GridPreconditioner:
     """The network as the coarse solver of a two-level preconditioner on the node grid of an
-    nx x ny structured quad mesh (scalar field).
+    nx x ny structured quad mesh, for a field of ``nd`` components per node (1: heat, the
+    network's features the coarse log-conductivity; 2: a plane displacement field, features
+    given as ``aux``).
 
     FCG applies it in a symmetric two-level form: smoothing (damped Jacobi, mode 2, as in
     training, or Chebyshev, mode 3), y = P net(P^T r) with the energy-optimal step, and
@@ -498,10 +641,12 @@ class GridPreconditioner:
     (factor n) x (factor n) problems on its own resolution.  All buffers are allocated here and the callback only
     enqueues kernels on the stream it is given, so FCG captures it into CUDA graphs."""
 
-    def __init__(self, net, nx, ny, k_elem, factor=1, mode=None, omega=None, sweeps=None, fixed=None):
+    def __init__(self, net, nx, ny, k_elem=None, factor=1, mode=None, omega=None, sweeps=None, fixed=None, nd=1,
+                 aux=None):
         if nx % factor or ny % factor:
             raise ValueError("the grid must be divisible by the coarsening factor")
         self.net = net
+        self.nd = nd
         # smoothing around the network, measured on the 1024^2 heat workload to a 1e-10
         # residual: on a coarsened grid (factor 4) the degree-3 Chebyshev smoother on
         # [lmax/30, lmax] (mode 3: 0.070 s; damped Jacobi, mode 2, best at 5 sweeps: 0.093 s);
@@ -517,11 +662,17 @@ class GridPreconditioner:
         self.Hn, self.Wn = nx // factor + 1, ny // factor + 1
         self.Hp, self.Wp = padded(self.Hn), padded(self.Wn)
         dev = net.device
-        self.aux = torch.as_tensor(coarse_log_conductivity(k_elem, nx, ny, factor), device=dev)
+        # per-node features of the network's grid: the coarse log-conductivity (heat), or the
+        # caller's (Hn Wn, naux) array
+        if aux is None:
+            aux = coarse_log_conductivity(k_elem, nx, ny, factor)
+        aux = np.asarray(aux, dtype=np.float32).reshape(self.Hn * self.Wn, -1)
+        self.naux = aux.shape[1]
+        self.aux = torch.as_tensor(np.ascontiguousarray(aux), device=dev)
         self.img = torch.zeros((1, self.Hp, self.Wp, C_IN), dtype=torch.bfloat16, device=dev)
         self.scale = torch.empty(1, dtype=torch.float32, device=dev)
-        self.rc = torch.zeros(self.Hn * self.Wn, dtype=torch.float32, device=dev)
-        self.yc = torch.zeros(self.Hn * self.Wn, dtype=torch.float32, device=dev)
+        self.rc = torch.zeros(self.Hn * self.Wn * nd, dtype=torch.float32, device=dev)
+        self.yc = torch.zeros(self.Hn * self.Wn * nd, dtype=torch.float32, device=dev)
         self.fixed = None if fixed is None else torch.as_tensor(np.asarray(fixed, dtype=np.uint8), device=dev)
         self.arena = {}
         self.applications = 0
@@ -532,23 +683,26 @@ class GridPreconditioner:
         lib = self.net.lib
         st = C.c_void_p(stream)
         f = self.factor
+        nd = self.nd
         if f > 1:
             fixed = _p(self.fixed)
-            rc = lib.agx_nn_restrict(C.c_void_p(r_ptr), fixed, self.Hn, self.Wn, f, _p(self.rc), st)
+            rc = lib.agx_nn_restrict_field(C.c_void_p(r_ptr), fixed, nd, self.Hn, self.Wn, f, _p(self.rc), st)
             if rc != 0:
                 return rc
             src = self.rc.data_ptr()
         else:
             src = r_ptr
-        rc = lib.agx_nn_grid_from_vector(C.c_void_p(src), _p(self.aux), self.Hn, self.Wn, self.Hp, self.Wp, 1,
-                                         _p(self.scale), _p(self.img), st)
+        rc = lib.agx_nn_grid_from_field(C.c_void_p(src), nd, _p(self.aux), self.naux, self.Hn, self.Wn, self.Hp,
+                                        self.Wp, 1, _p(self.scale), _p(self.img), st)
         if rc != 0:
             return rc
         out = self.net.forward(self.img, stream=st, arena=self.arena)
         dst = self.yc.data_ptr() if f > 1 else z_ptr
-        rc = lib.agx_nn_vector_from_grid(_p(out), C_OUT, self.Hn, self.Wn, self.Wp, C.c_void_p(dst), st)
+        rc = lib.agx_nn_field_from_grid(_p(out), C_OUT, nd, self.Hn, self.Wn, self.Wp, C.c_void_p(dst), st)
         if rc == 0 and f > 1:
-            rc = lib.agx_nn_prolong(_p(self.yc), self.Hn, self.Wn, f, C.c_void_p(z_ptr), st)
+            rc = lib.agx_nn_prolong_field(_p(self.yc), nd, self.Hn, self.Wn, f, C.c_void_p(z_ptr), st)
+        # grid transfers: (restrict,) 1/rms, image, field (, prolong)
+        self.net.launches += 3 + (2 if f > 1 else 0)
         self.applications += 1
         return rc
 
@@ -562,7 +716,7 @@ class GridPreconditioner:
         prob.learned = self
 
     def callback(self, prob):
-        if prob.n_dofs != (self.nx + 1) * (self.ny + 1):
+        if prob.n_dofs != (self.nx + 1) * (self.ny + 1) * self.nd:
             raise ValueError("the learned preconditioner was built for another grid")
         if self.factor > 1 and self.fixed is None:
             self.fixed = torch.as_tensor(prob.mask.astype(np.uint8), device=self.net.device)

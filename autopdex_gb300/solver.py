@@ -18,7 +18,9 @@ Keys read from ``static_settings`` (besides AutoPDEx's own):
 * ``'precision'``: ``'float64'`` (default) or ``'mixed'`` (float32 tangent and Krylov
   iterations inside the float64 Newton / refinement loop).
 * ``'type of preconditioner'``: ``'jacobi'`` (default) or ``'learned'`` (the network set with
-  :func:`set_learned_preconditioner`; Jacobi when none is set).
+  :func:`set_learned_preconditioner`; Jacobi when none is set): flexible CG in float32 with
+  ``'precision': 'mixed'``, in float64 with the preconditioner in float32 / bf16 with
+  ``'precision': 'float64'``.
 
 Extra keyword arguments: ``newton_tol``, ``maxiter`` (Newton), ``newton_rtol`` (stop also at
 ``||R|| <= newton_rtol ||R_0||``), ``krylov_tol``, ``krylov_maxiter``, ``reuse_tangent``.
@@ -52,21 +54,26 @@ def _method(static_settings, kwargs):
             raise NotImplementedError("BiCGStab runs in float64 only")
         method = N.AGX_BICGSTAB
     elif name == "fcg":
-        method = N.AGX_FCG_MIXED
+        method = N.AGX_FCG_F64 if precision == "float64" else N.AGX_FCG_MIXED
     else:
         raise NotImplementedError(f"solver {name!r} is not available in the gb300 backend")
     if precond == "learned":
-        method = N.AGX_FCG_MIXED
+        # float32 FCG for 'mixed'; float64 FCG with the float32 / bf16 preconditioner for
+        # 'float64' (tangents whose conditioning float32 Krylov vectors cannot resolve)
+        method = N.AGX_FCG_F64 if precision == "float64" else N.AGX_FCG_MIXED
     elif precond != "jacobi":
         raise NotImplementedError(f"preconditioner {precond!r} is not available in the gb300 backend")
     mixed = method in (N.AGX_PCG_MIXED, N.AGX_FCG_MIXED)
-    default_tol = 1e-13 if direct else (1e-5 if mixed else 1e-11)
+    default_tol = 1e-13 if direct else (1e-5 if mixed else (1e-4 if method == N.AGX_FCG_F64 else 1e-11))
     opts = N.SolveOpts()
     opts.method = method
     opts.rtol = float(kwargs.get("krylov_tol", default_tol))
     opts.atol = float(kwargs.get("krylov_atol", 0.0))
     opts.maxiter = int(kwargs.get("krylov_maxiter", 100000))
-    opts.check_every = int(kwargs.get("krylov_check_every", 32))
+    # iterations between host checks of convergence (one CUDA graph replay each); the learned
+    # preconditioner converges in tens of iterations, so its chunks are shorter (a replay past
+    # convergence still runs the network)
+    opts.check_every = int(kwargs.get("krylov_check_every", 8 if precond == "learned" else 32))
     return opts, (N.AGX_F32 if mixed else N.AGX_F64)
 
 
@@ -129,7 +136,7 @@ def solve_damped_newton(dofs, settings, static_settings, newton_tol=1e-8, dampin
     prob.update_models(settings)
     opts = N.NewtonOpts()
     kopts, tdt = _method(static_settings, kwargs)
-    if kopts.method == N.AGX_FCG_MIXED:
+    if kopts.method in (N.AGX_FCG_MIXED, N.AGX_FCG_F64):
         _attach_learned(prob, static_settings)
     opts.newton_tol = float(newton_tol)
     opts.newton_rtol = float(kwargs.get("newton_rtol", 0.0))
@@ -163,7 +170,7 @@ def solve_linear(dofs, settings, static_settings, **kwargs):
     prob = get_problem(dofs, settings, static_settings)
     prob.update_models(settings)
     kopts, tdt = _method(static_settings, kwargs)
-    if kopts.method == N.AGX_FCG_MIXED:
+    if kopts.method in (N.AGX_FCG_MIXED, N.AGX_FCG_F64):
         _attach_learned(prob, static_settings)
     x = prob.to_device(dofs).clone()
     cond = settings.get("dirichlet conditions")

@@ -2,11 +2,16 @@
 
     python -m autopdex_gb300.train_preconditioner --n 256 --problems 2000 --steps 6000 \
         --out autopdex_gb300/weights/heat_unet_n256.npz
+    python -m autopdex_gb300.train_preconditioner --problem membrane --n 128 --steps 3000 \
+        --out autopdex_gb300/weights/membrane_unet_n128.npz
 
-Training pairs (residual, error) come from the iterates of the plain float64 Jacobi-PCG solver
-on heat-conduction problems -div(k grad T) = b with k = exp(Gaussian random field) seeded
+heat: training pairs (residual, error) come from the iterates of the plain float64 Jacobi-PCG
+solver on heat-conduction problems -div(k grad T) = b with k = exp(Gaussian random field) seeded
 0 .. problems-1 (length 0.05, std 1, the 1024 x 1024 heat workload's family at n x n), one
 constant and one random right-hand side each.
+membrane: the nearly incompressible Cook membrane (the 512 x 512 membrane workload's geometry
+at n x n), tangents at converged load states, random vector right-hand sides after the
+Chebyshev pre-smoothing of the native FCG, error energies from the banded Cholesky factor.
 """
 import argparse
 import json
@@ -26,12 +31,21 @@ def main():
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--out", default=os.path.join(learned.WEIGHTS_DIR, "heat_unet_n256.npz"))
+    ap.add_argument("--problem", default="heat", choices=["heat", "membrane"])
+    ap.add_argument("--rhs-per-state", type=int, default=400)
+    ap.add_argument("--out", default=None)
     args = ap.parse_args()
+    if args.out is None:
+        args.out = os.path.join(learned.WEIGHTS_DIR, f"{args.problem}_unet_n{args.n}.npz")
     t0 = time.time()
-    ts = learned.make_training_set(args.problems, n=args.n, seed0=args.seed, verbose=True)
+    if args.problem == "heat":
+        ts = learned.make_training_set(args.problems, n=args.n, seed0=args.seed, verbose=True)
+        net = learned.UNet(seed=args.seed)
+    else:
+        ts = learned.make_membrane_training_set(n=args.n, rhs_per_state=args.rhs_per_state, seed=args.seed,
+                                                verbose=True)
+        net = learned.UNet(seed=args.seed, n_in=ts.nd + ts.naux)
     t1 = time.time()
-    net = learned.UNet(seed=args.seed)
     losses = learned.train(net, ts, steps=args.steps, batch=args.batch, lr=args.lr, verbose=True)
     torch.cuda.synchronize()
     t2 = time.time()
@@ -42,8 +56,9 @@ def main():
             "loss_first50": round(sum(losses[:50]) / 50, 4), "loss_last50": round(sum(losses[-50:]) / 50, 4),
             "loss_per_100_steps": [round(sum(losses[i:i + 100]) / len(losses[i:i + 100]), 4)
                                    for i in range(0, len(losses), 100)],
-            "command": f"python -m autopdex_gb300.train_preconditioner --n {args.n} --problems {args.problems} "
-                       f"--steps {args.steps}"}
+            "problem": args.problem,
+            "command": f"python -m autopdex_gb300.train_preconditioner --problem {args.problem} --n {args.n} "
+                       f"--problems {args.problems} --rhs-per-state {args.rhs_per_state} --steps {args.steps}"}
     with open(os.path.splitext(args.out)[0] + ".json", "w") as fh:
         json.dump(meta, fh, indent=1)
     print(f"data {t1 - t0:.1f} s ({len(ts)} pairs), training {t2 - t1:.1f} s, "

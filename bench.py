@@ -213,7 +213,7 @@ def headline(args, rank):
     _sync()
     if args.dist:
         args.dist.barrier()
-    l0 = _launches(prob)
+    l0 = _launches(prob) + net.launches
     stream = torch.cuda.current_stream()
     ev = [_events() for _ in range(args.steps)]
     infos = []
@@ -226,7 +226,7 @@ def headline(args, rank):
             b.record(stream)
             infos.append(_info())
         _sync()
-    l1 = _launches(prob)
+    l1 = _launches(prob) + net.launches  # the library's kernels and the network's (conv, pool, transfers)
     if args.dist:
         args.dist.barrier()
     t_ms = sum(a.elapsed_time(b) for a, b in ev)
@@ -501,7 +501,10 @@ def rec_neo_hooke_cube(n=64, steps=10):
 def rec_cook(n=512, steps=1, plain_limit_s=120.0):
     from autopdex_gb300 import configs, solver
     out = {"workload": f"cook_membrane_{n}x{n}_q1 (nu = 0.4999), load steps 1..{steps} of 20"}
-    rt = 1e-8
+    # the float64 residual of this nearly incompressible membrane stalls near 4e-8 of a load
+    # step's first residual at 512^2 (rounding of the displacements, amplified by lam / mu =
+    # 5000, not the solver: the direct solve stalls there too), so the Newton tolerance is 1e-7
+    rt = 1e-7
     out["newton_rtol"] = rt
     for name, sol_name, prec, ktol in (("direct_fp64", "lapack", "float64", 1e-13),
                                        ("plain_fp64_pcg", "pcg", "float64", 1e-4)):
@@ -776,9 +779,10 @@ def case(args):
         static["type of preconditioner"] = "learned"
     settings = w.steps[0](dict(w.settings)) if w.steps else w.settings
     kw = dict(newton_tol=0.0, newton_rtol=RTOL, maxiter=30, krylov_tol=args.krylov_tol, krylov_maxiter=400000)
-    solver.solver(w.dofs, settings, static, **kw)
+    for _ in range(args.reps):
+        solver.solver(w.dofs, settings, static, **kw)
     _sync()
-    print(f"solve {w.name}: {json.dumps(_info())}")
+    print(f"solve {w.name}: {args.reps} solves, last {json.dumps(_info())}")
 
 
 def main():

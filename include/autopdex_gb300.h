@@ -88,6 +88,12 @@ extern "C" {
 #define AGX_BICGSTAB 2   /* Jacobi-BiCGStab in float64, for non-symmetric tangents */
 #define AGX_FCG_MIXED 3  /* flexible CG in float32 with the registered preconditioner
                             (agx_set_preconditioner), Jacobi when none is registered */
+#define AGX_FCG_F64 5    /* flexible CG in float64 (vectors, products with the float64 tangent)
+                            with the registered preconditioner applied in float32 on the
+                            residual scaled by 1 / ||b|| (its two-level smoothing on a float32
+                            copy of the tangent, the callback's network in bf16); Jacobi when
+                            none is registered.  For tangents whose conditioning float32 Krylov
+                            vectors cannot resolve (nearly incompressible solids). */
 #define AGX_CHOL_BAND 4  /* direct: banded Cholesky of the float64 tangent with float64
                             refinement to rtol (the 'lapack' / 'umfpack' spsolve of
                             linear_solve_scipy, solver.py:1493-1539) for symmetric definite
@@ -102,7 +108,8 @@ typedef struct agx_context agx_context;
 typedef int (*agx_precond_fn)(void* user, const float* r, float* z, int64_t n, void* stream);
 
 typedef struct {
-  int method;          /* AGX_PCG, AGX_PCG_MIXED, AGX_BICGSTAB, AGX_FCG_MIXED, AGX_CHOL_BAND */
+  int method;          /* AGX_PCG, AGX_PCG_MIXED, AGX_BICGSTAB, AGX_FCG_MIXED, AGX_CHOL_BAND,
+                          AGX_FCG_F64 */
   double rtol;         /* stop when ||r|| <= rtol ||b|| (jax.scipy cg semantics, solver.py:1116) */
   double atol;         /* ... or ||r|| <= atol */
   int maxiter;

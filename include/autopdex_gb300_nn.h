@@ -54,6 +54,18 @@ int agx_nn_restrict(const float* fine, const unsigned char* fixed, int Hc, int W
 int agx_nn_prolong(const float* coarse, int Hc, int Wc, int f, float* fine, void* stream);
 /* channel 0 of an NHWC image with C channels -> node vector */
 int agx_nn_vector_from_grid(const void* img, int C, int Hn, int Wn, int Wp, float* z, void* stream);
+/* The same transfers for a node field of nd (1 .. 3) components stored node-major
+   (r[node nd + c], the DOF numbering of an (n_nodes, nd) array): agx_nn_grid_from_field writes
+   channels 0 .. nd-1 (scaled to unit rms over all components when normalize) and naux
+   per-node features aux[node naux + a] into channels nd .. nd+naux-1 (nd + naux <= 16);
+   agx_nn_field_from_grid reads channels 0 .. nd-1; agx_nn_restrict_field /
+   agx_nn_prolong_field transfer every component bilinearly, `fixed` flagging fine DOFs. */
+int agx_nn_grid_from_field(const float* r, int nd, const float* aux, int naux, int Hn, int Wn, int Hp, int Wp,
+                           int normalize, float* scale, void* img, void* stream);
+int agx_nn_field_from_grid(const void* img, int C, int nd, int Hn, int Wn, int Wp, float* z, void* stream);
+int agx_nn_restrict_field(const float* fine, const unsigned char* fixed, int nd, int Hc, int Wc, int f, float* coarse,
+                          void* stream);
+int agx_nn_prolong_field(const float* coarse, int nd, int Hc, int Wc, int f, float* fine, void* stream);
 
 #ifdef __cplusplus
 }
