@@ -503,9 +503,14 @@ int agx_autotune(agx_context* ctx, int* spmv_tpr, float* spmv_ms) {
 int agx_set_tuning(agx_context* ctx, int dtype, int spmv_tpr) {
   if (!ctx) return AGX_ERR_ARG;
   if (dtype != AGX_F64 && dtype != AGX_F32) return agx_fail(ctx, AGX_ERR_ARG, "dtype must be AGX_F64 or AGX_F32");
-  if (spmv_tpr != 0 && spmv_tpr != 1 && spmv_tpr != 2 && spmv_tpr != 4 && spmv_tpr != 8 && spmv_tpr != 16)
-    return agx_fail(ctx, AGX_ERR_ARG, "lanes per row must be 0, 1, 2, 4, 8 or 16");
-  if (ctx->ndof == 3 && spmv_tpr != 0 && spmv_tpr < 4)
+  const int lanes = spmv_tpr & 255, unroll4 = spmv_tpr >> 8;
+  const bool plain_ok = unroll4 == 0 && (lanes == 0 || lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8 ||
+                                          lanes == 16);
+  const bool unroll_ok = unroll4 == 1 && (lanes == 2 || lanes == 4 || lanes == 8);
+  if (!plain_ok && !unroll_ok)
+    return agx_fail(ctx, AGX_ERR_ARG, "lanes per row must be 0, 1, 2, 4, 8 or 16 (2, 4 or 8 with 256 added for four "
+                                      "blocks per lane and trip)");
+  if (ctx->ndof == 3 && spmv_tpr != 0 && lanes < 4)
     return agx_fail(ctx, AGX_ERR_ARG, "3 DOFs per node need 4 or more lanes per row");
   ctx->spmv_tpr[dtype == AGX_F32 ? 1 : 0] = spmv_tpr;
   return AGX_OK;

@@ -135,41 +135,50 @@ __device__ __forceinline__ bool bad(double x) { return !isfinite(x) || x == 0.0;
 // the TPR lanes of a row (consecutive k) read each entry plane with contiguous loads.
 // y = A x for the node-block CSR with TPR lanes per block row; with `dir` the operand is
 // formed on the fly as x = z + beta p_old (the CG direction update folded into the product).
-template <typename T, int NDOF, int TPR, bool DIR>
+// U (2 or 4) blocks per lane and trip: all U blocks' columns and value planes are requested
+// before any gather or FMA, so each lane keeps U blocks of loads in flight (the product is bound
+// by bytes in flight per SM, not by traffic); matrix data is streamed (evict-first) so that the
+// gathered vectors stay in L2.
+template <typename T, int NDOF, int TPR, bool DIR, int U = 2>
 __device__ __forceinline__ void bsr_row(int64_t row, int sub, const int32_t* __restrict__ rowptr,
                                         const int32_t* __restrict__ col, const T* __restrict__ vals, int64_t nnzb,
                                         const T* __restrict__ x, const T* __restrict__ pold, T beta, T (&y)[NDOF]) {
 #pragma unroll
   for (int i = 0; i < NDOF; ++i) y[i] = 0;
   const int beg = rowptr[row], end = rowptr[row + 1];
-  // two blocks per lane and trip: both blocks' columns and value planes are requested before
-  // any gather or FMA, so each lane keeps twice the loads in flight; matrix data is streamed
-  // (evict-first) so that the gathered vectors stay in L2
-  for (int k = beg + sub; k < end; k += 2 * TPR) {
-    const int k2 = k + TPR;
-    const bool two = k2 < end;
-    const int64_t c1 = __ldcs(col + k);
-    const int64_t c2 = two ? __ldcs(col + k2) : c1;
-    T v1[NDOF * NDOF], v2[NDOF * NDOF];
+  for (int k = beg + sub; k < end; k += U * TPR) {
+    int64_t c[U];
+    bool ok[U];
 #pragma unroll
-    for (int e = 0; e < NDOF * NDOF; ++e) {
-      v1[e] = __ldcs(vals + (int64_t)e * nnzb + k);
-      v2[e] = two ? __ldcs(vals + (int64_t)e * nnzb + k2) : T(0);
+    for (int u = 0; u < U; ++u) {
+      const int kk = k + u * TPR;
+      ok[u] = kk < end;
+      c[u] = ok[u] ? __ldcs(col + kk) : 0;
     }
-    T x1[NDOF], x2[NDOF];
+    T v[U][NDOF * NDOF];
 #pragma unroll
-    for (int j = 0; j < NDOF; ++j) {
-      x1[j] = x[c1 * NDOF + j];
-      x2[j] = two ? x[c2 * NDOF + j] : T(0);
-      if constexpr (DIR) {
-        x1[j] += beta * pold[c1 * NDOF + j];
-        if (two) x2[j] += beta * pold[c2 * NDOF + j];
+    for (int e = 0; e < NDOF * NDOF; ++e)
+#pragma unroll
+      for (int u = 0; u < U; ++u) v[u][e] = ok[u] ? __ldcs(vals + (int64_t)e * nnzb + k + u * TPR) : T(0);
+    T xs[U][NDOF];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int j = 0; j < NDOF; ++j) {
+        xs[u][j] = ok[u] ? x[c[u] * NDOF + j] : T(0);
+        if constexpr (DIR) {
+          if (ok[u]) xs[u][j] += beta * pold[c[u] * NDOF + j];
+        }
       }
-    }
 #pragma unroll
     for (int i = 0; i < NDOF; ++i)
 #pragma unroll
-      for (int j = 0; j < NDOF; ++j) y[i] += v1[i * NDOF + j] * x1[j] + v2[i * NDOF + j] * x2[j];
+      for (int j = 0; j < NDOF; ++j) {
+        T t = 0;
+#pragma unroll
+        for (int u = 0; u < U; ++u) t += v[u][i * NDOF + j] * xs[u][j];
+        y[i] += t;
+      }
   }
 #pragma unroll
   for (int o = TPR / 2; o >= 1; o >>= 1)
@@ -177,7 +186,7 @@ __device__ __forceinline__ void bsr_row(int64_t row, int sub, const int32_t* __r
     for (int i = 0; i < NDOF; ++i) y[i] += __shfl_xor_sync(0xffffffffu, y[i], o);
 }
 
-template <typename T, int NDOF, int TPR>
+template <typename T, int NDOF, int TPR, int U = 2>
 __global__ void __launch_bounds__(AGX_BLOCK) spmv_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr,
                                                          const int32_t* __restrict__ col, const T* __restrict__ vals,
                                                          int64_t nnzb, const T* __restrict__ x, T* __restrict__ y) {
@@ -186,8 +195,8 @@ __global__ void __launch_bounds__(AGX_BLOCK) spmv_kernel(int64_t n_rows, const i
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = L / TPR;
     T yr[NDOF];
-    bsr_row<T, NDOF, TPR, false>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, x, nullptr, T(0),
-                                 yr);
+    bsr_row<T, NDOF, TPR, false, U>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, x, nullptr,
+                                    T(0), yr);
     if (row < n_rows && sub == 0) {
 #pragma unroll
       for (int i = 0; i < NDOF; ++i) y[row * NDOF + i] = yr[i];
@@ -197,7 +206,7 @@ __global__ void __launch_bounds__(AGX_BLOCK) spmv_kernel(int64_t n_rows, const i
 
 // p_new = z + beta p_old (own rows), q = A p_new, alpha = rz / (p_new, q).  beta = 0 on the
 // first iteration (p_old = 0), which makes p_new = z.
-template <typename T, int NDOF, int TPR>
+template <typename T, int NDOF, int TPR, int U = 2>
 __global__ void __launch_bounds__(AGX_BLOCK)
 spmv_dot_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                 const T* __restrict__ vals, int64_t nnzb, const T* __restrict__ z, const T* __restrict__ pold,
@@ -211,7 +220,8 @@ spmv_dot_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = L / TPR;
     T yr[NDOF];
-    bsr_row<T, NDOF, TPR, true>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, z, pold, beta, yr);
+    bsr_row<T, NDOF, TPR, true, U>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, z, pold, beta,
+                                   yr);
     if (row < n_rows && sub == 0) {
 #pragma unroll
       for (int i = 0; i < NDOF; ++i) {
@@ -759,17 +769,20 @@ int resident_grid(agx_context* ctx, K kernel) {
 }
 
 // returns the grid (the number of block partials written when block_partials is set)
-template <typename T, int ND, int TP>
+template <typename T, int ND, int TP, int U = 2>
 int spmv_dot_variant(agx_context* ctx, const T* vals, const T* z, const T* pold, T* pnew, T* q, const T* rflex,
                      int block_partials) {
   static int g_cache = 0;
-  if (!g_cache) g_cache = resident_grid(ctx, spmv_dot_kernel<T, ND, TP>);
-  spmv_dot_kernel<T, ND, TP><<<g_cache, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_nodes, ctx->d_rowptr, ctx->d_col, vals,
-                                                                     ctx->nnzb, z, pold, pnew, q, ctx->d_scal,
-                                                                     ctx->d_partials, ctx->d_counter, rflex,
-                                                                     block_partials);
+  if (!g_cache) g_cache = resident_grid(ctx, spmv_dot_kernel<T, ND, TP, U>);
+  spmv_dot_kernel<T, ND, TP, U><<<g_cache, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_nodes, ctx->d_rowptr, ctx->d_col,
+                                                                        vals, ctx->nnzb, z, pold, pnew, q, ctx->d_scal,
+                                                                        ctx->d_partials, ctx->d_counter, rflex,
+                                                                        block_partials);
   return g_cache;
 }
+
+// a product variant: lanes per block row, plus SPMV_UNROLL4 for four blocks per lane and trip
+constexpr int SPMV_UNROLL4 = 256;
 
 // default lanes per block row when the autotuner has not chosen one
 int default_tpr(const agx_context* ctx) { return ctx->ndof == 1 ? (ctx->dim == 3 ? 8 : 4) : (ctx->ndof == 2 ? 4 : 8); }
@@ -782,6 +795,9 @@ int spmv_dot_nd(agx_context* ctx, int tpr, const T* vals, const T* z, const T* p
     case 2: return spmv_dot_variant<T, ND, 2>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
     case 4: return spmv_dot_variant<T, ND, 4>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
     case 16: return spmv_dot_variant<T, ND, 16>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
+    case 2 | SPMV_UNROLL4: return spmv_dot_variant<T, ND, 2, 4>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
+    case 4 | SPMV_UNROLL4: return spmv_dot_variant<T, ND, 4, 4>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
+    case 8 | SPMV_UNROLL4: return spmv_dot_variant<T, ND, 8, 4>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
     default: return spmv_dot_variant<T, ND, 8>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
   }
 }
@@ -843,7 +859,7 @@ int run_chunk(agx_context* ctx, int slot, const void* x, int every, int kn, F&& 
     AGX_CUDA(ctx, cudaEventCreateWithFlags(&ctx->graph_ev[1], cudaEventDisableTiming));
   }
   const cudaStream_t gs = legacy ? ctx->graph_stream : work;
-  if (!gr.exec || gr.key_x != x || gr.every != every || gr.prof != ctx->prof_on || gr.tpr != ctx->spmv_tpr[0] * 64 + ctx->spmv_tpr[1] ||
+  if (!gr.exec || gr.key_x != x || gr.every != every || gr.prof != ctx->prof_on || gr.tpr != ctx->spmv_tpr[0] * 4096 + ctx->spmv_tpr[1] ||
       gr.pc_key != pc_key) {
     if (gr.exec) cudaGraphExecDestroy(gr.exec);
     gr.exec = nullptr;
@@ -866,7 +882,7 @@ int run_chunk(agx_context* ctx, int slot, const void* x, int every, int kn, F&& 
     gr.key_x = x;
     gr.every = every;
     gr.prof = ctx->prof_on;
-    gr.tpr = ctx->spmv_tpr[0] * 64 + ctx->spmv_tpr[1];
+    gr.tpr = ctx->spmv_tpr[0] * 4096 + ctx->spmv_tpr[1];
     gr.pc_key = pc_key;
   }
   if (legacy) {
@@ -945,7 +961,7 @@ int agx_autotune_spmv(agx_context* ctx, int* chosen, float* best_ms) {
   if (ctx->tangent_valid != AGX_F32 && ctx->tangent_valid != AGX_F64)
     return agx_fail(ctx, AGX_ERR_STATE, "autotune needs an assembled tangent");
   const bool f32 = ctx->tangent_valid == AGX_F32;
-  const int cands[5] = {1, 2, 4, 8, 16};
+  const int cands[8] = {1, 2, 4, 8, 16, 2 | SPMV_UNROLL4, 4 | SPMV_UNROLL4, 8 | SPMV_UNROLL4};
   cudaEvent_t e0, e1;
   AGX_CUDA(ctx, cudaEventCreate(&e0));
   AGX_CUDA(ctx, cudaEventCreate(&e1));
@@ -958,7 +974,7 @@ int agx_autotune_spmv(agx_context* ctx, int* chosen, float* best_ms) {
   float best = 1e30f;
   int pick = default_tpr(ctx);
   for (int c : cands) {
-    if (ctx->ndof == 3 && c < 4) continue;
+    if (ctx->ndof == 3 && (c & (SPMV_UNROLL4 - 1)) < 4) continue;
     auto run = [&]() {
       cudaMemsetAsync(ctx->d_scal, 0, sizeof(agx_krylov_scalars), ctx->stream);
       if (f32) {
@@ -1021,6 +1037,9 @@ void spmv_nd(agx_context* ctx, int tpr, int g, const T* v, const T* x, T* y) {
     case 2: spmv_kernel<T, ND, 2><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
     case 4: spmv_kernel<T, ND, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
     case 16: spmv_kernel<T, ND, 16><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
+    case 2 | SPMV_UNROLL4: spmv_kernel<T, ND, 2, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
+    case 4 | SPMV_UNROLL4: spmv_kernel<T, ND, 4, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
+    case 8 | SPMV_UNROLL4: spmv_kernel<T, ND, 8, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
     default: spmv_kernel<T, ND, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
   }
 }
@@ -1030,7 +1049,7 @@ int agx_spmv_values_impl(agx_context* ctx, int dtype, const void* values, const 
   const int64_t nr = ctx->n_nodes;
   const int tuned = ctx->spmv_tpr[dtype == AGX_F32 ? 1 : 0];
   const int tpr = tuned > 0 ? tuned : default_tpr(ctx);
-  const int g = agx_grid(ctx, nr * tpr, 8);
+  const int g = agx_grid(ctx, nr * (tpr & (SPMV_UNROLL4 - 1)), 8);
   auto go = [&](auto tag) {
     using T = decltype(tag);
     const T* v = (const T*)values;

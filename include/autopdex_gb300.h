@@ -266,9 +266,10 @@ int agx_profile_read(agx_context* ctx, double* ms, int64_t* launches);
 int agx_pcg_noalloc(const int32_t* rowptr, const int32_t* col, const double* vals, int64_t n_nodes, int ndof,
                     const double* rhs, double* x, double rtol, int maxiter, void* cuda_stream,
                     agx_solve_info* info, char* errbuf, int errbuf_len);
-/* Autotuner: times every lanes-per-block-row variant (1, 2, 4, 8, 16) of the Krylov product
-   on the last assembled tangent (CUDA events), keeps the fastest for that tangent's
-   precision and reports it. */
+/* Autotuner: times every variant of the Krylov product -- lanes per block row 1, 2, 4, 8, 16
+   with two blocks per lane and trip, and 2, 4, 8 lanes with four blocks (code lanes + 256) --
+   on the last assembled tangent (CUDA events), keeps the fastest for that tangent's precision
+   and reports its code. */
 int agx_autotune(agx_context* ctx, int* spmv_tpr, float* spmv_ms);
 /* Applies a tuning decision for the float64 (AGX_F64) or float32 (AGX_F32) product, e.g. from
    the autotuner's cache; 0 restores the default. */

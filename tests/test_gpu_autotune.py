@@ -1,5 +1,6 @@
-"""The autotuner's SpMV variants (1, 2, 4, 8 or 16 lanes per block row) solve identically, the
-autotuner picks one of them per precision, and invalid tuning values are rejected."""
+"""The autotuner's SpMV variants (1, 2, 4, 8 or 16 lanes per block row with two blocks per lane
+and trip; 2, 4 or 8 lanes with four blocks, code lanes + 256) solve identically, the autotuner
+picks one of them per precision, and invalid tuning values are rejected."""
 import ctypes as C
 
 import numpy as np
@@ -11,6 +12,8 @@ from autopdex_gb300 import configs
 from autopdex_gb300._problem import get_problem
 
 pytestmark = pytest.mark.gpu
+
+VARIANTS = (1, 2, 4, 8, 16, 2 + 256, 4 + 256, 8 + 256)
 
 
 def _solve(prob, rhs, method):
@@ -34,7 +37,7 @@ def test_variants_agree_and_autotuner_picks_one(dtype):
     rhs = torch.where(mask, torch.zeros_like(x0), torch.ones_like(x0))
     method = N.AGX_PCG if dtype == N.AGX_F64 else N.AGX_PCG_MIXED
     sols = {}
-    for tpr in (1, 2, 4, 8, 16):
+    for tpr in VARIANTS:
         prob._call("agx_set_tuning", dtype, tpr)
         sols[tpr] = _solve(prob, rhs, method)
     ref, its = sols[4]
@@ -45,7 +48,7 @@ def test_variants_agree_and_autotuner_picks_one(dtype):
     tpr = C.c_int()
     ms = C.c_float()
     prob._call("agx_autotune", C.byref(tpr), C.byref(ms))
-    assert tpr.value in (1, 2, 4, 8, 16) and ms.value > 0.0
+    assert tpr.value in VARIANTS and ms.value > 0.0
     prob._call("agx_set_tuning", dtype, 0)
 
 
@@ -56,6 +59,9 @@ def test_invalid_tuning_is_rejected():
     assert lib.agx_set_tuning(prob.ctx, N.AGX_F32, 3) != N.AGX_OK
     assert lib.agx_set_tuning(prob.ctx, N.AGX_F32, 2) != N.AGX_OK  # 3 DOFs per node need >= 4 lanes
     assert lib.agx_set_tuning(prob.ctx, 7, 4) != N.AGX_OK
+    assert lib.agx_set_tuning(prob.ctx, N.AGX_F32, 16 + 256) != N.AGX_OK  # no four-block variant with 16 lanes
+    assert lib.agx_set_tuning(prob.ctx, N.AGX_F32, 2 + 256) != N.AGX_OK  # 3 DOFs per node need >= 4 lanes
+    assert lib.agx_set_tuning(prob.ctx, N.AGX_F32, 8 + 256) == N.AGX_OK
     assert lib.agx_set_tuning(prob.ctx, N.AGX_F64, 8) == N.AGX_OK
 
 
