@@ -581,6 +581,15 @@ int agx_newton(agx_context* ctx, double* dofs, const double* dvals, const agx_ne
     rc = agx_krylov_impl(ctx, ctx->d_b, ctx->d_dx, &opts->krylov, &si);
     if (rc) return rc;
     out.krylov_iterations += si.iterations;
+    if (kry == AGX_CHOL_BAND && si.status == AGX_DIVERGED) {
+      // the tangent is not definite: no Newton step exists from this factorization; stop with
+      // the diverged flag (the reference's LU would take an indefinite step)
+      out.iterations = itt + 1;
+      out.res_norm = res;
+      out.diverged = 1;
+      if (info) *info = out;
+      return AGX_OK;
+    }
     // damped update of the free DOFs, prescribed DOFs set (solver.py:879-892)
     agx_launch_newton_update(ctx, dofs, ctx->d_dx, dvals, opts->damping);
     // residual for the convergence test (solver.py:898-903); reused as next iteration's rhs

@@ -410,7 +410,8 @@ int agx_band_solve_impl(agx_context* ctx, const double* b, double* x, const agx_
     agx_prof_scope ps(ctx, AGX_PROF_FACTOR);
     const int rc = band_factor(ctx);
     if (rc < 0) return rc;
-    if (rc > 0) {  // not positive definite: reported like a Krylov breakdown
+    if (rc > 0) {  // not positive definite: reported like a Krylov breakdown, with x = 0
+      AGX_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
       if (info) {
         info->iterations = 0;
         info->rel_residual = NAN;

@@ -321,8 +321,8 @@ class TrainingSet:
     (float32, on the GPU), its error energy s = (r1, e1) / rms(r1)^2, and the index of its
     problem, whose float32 tangent values (the library's layout) are kept for K y."""
 
-    def __init__(self, n, prob, r1, s, pid, aux, values, free, nd=1, naux=1):
-        self.n, self.prob = n, prob
+    def __init__(self, n, prob, r1, s, pid, aux, values, free, nd=1, naux=1, factor=1):
+        self.n, self.prob, self.factor = n, prob, factor
         self.r1, self.s, self.pid, self.aux, self.values, self.free = r1, s, pid, aux, values, free
         self.nd, self.naux = nd, naux
 
@@ -464,14 +464,16 @@ def gershgorin_lmax(prob):
 
 
 def make_membrane_training_set(n=128, load_steps=(0, 5, 10, 15, 20), rhs_per_state=400, seed=0, degree=3,
-                               frac=1.0 / 30.0, verbose=False):
+                               frac=1.0 / 30.0, factor=1, verbose=False):
     """Samples for the two-level preconditioner of the nearly incompressible Cook membrane
     (plane-strain neo-Hooke, nu = 0.4999; the 512^2 membrane workload's geometry at n x n):
     for the tangents at the converged states of the given load steps (0: the undeformed
     state) and random smooth-plus-rough vector right-hand sides r, the residual r1 that the
     Chebyshev pre-smoothing of the native FCG leaves and its error energy s = (r1, K^-1 r1),
     K^-1 by the banded Cholesky factor of the float64 tangent.  Stored per sample: r1 / rms,
-    s / rms^2 and the state index (whose float32 tangent serves K y in training)."""
+    s / rms^2 and the state index (whose float32 tangent serves K y in training).  With
+    ``factor`` f the network is trained on the (n / f + 1)^2 grid through the bilinear transfers,
+    the form in which it serves finer meshes."""
     from . import configs, solver
     from ._problem import get_problem
     w = configs.cook_membrane(n=n, solver="lapack")
@@ -481,7 +483,8 @@ def make_membrane_training_set(n=128, load_steps=(0, 5, 10, 15, 20), rhs_per_sta
     mask = torch.as_tensor(prob.mask.astype(bool), device=dev)
     free = (~mask).float()
     rng = np.random.default_rng(seed + 4242)
-    aux = torch.as_tensor(node_features(w.raw["coords"]).reshape(-1), device=dev)
+    wc = w if factor == 1 else configs.cook_membrane(n=n // factor)
+    aux = torch.as_tensor(node_features(wc.raw["coords"]).reshape(-1), device=dev)
     states = [np.zeros(w.n_dofs)] if 0 in load_steps else []
     u = np.zeros(w.n_dofs)
     settings = dict(w.settings)
@@ -525,7 +528,7 @@ def make_membrane_training_set(n=128, load_steps=(0, 5, 10, 15, 20), rhs_per_sta
         if verbose:
             print(f"state {i}: {rhs_per_state} samples, lmax {lmax:.3g}", flush=True)
     auxs = aux.reshape(1, -1).expand(len(states), -1).contiguous()
-    return TrainingSet(n, prob, r1s, ss, pid, auxs, values, free, nd=nd, naux=2)
+    return TrainingSet(n, prob, r1s, ss, pid, auxs, values, free, nd=nd, naux=2, factor=factor)
 
 
 def _random_rhs(rng, m, device):
@@ -570,11 +573,22 @@ def energy_loss(r1, y, Ky, s):
 
 def train(net, ts, steps=3000, batch=16, lr=2e-3, seed=0, verbose=False):
     """Adam with a cosine learning-rate schedule on :func:`energy_loss`; every product K y
-    runs through agx_spmv_values with the stored tangent of the sample's problem."""
+    runs through agx_spmv_values with the stored tangent of the sample's problem.
+
+    With ``ts.factor`` f > 1 the network works on the grid coarsened by f, as
+    :class:`GridPreconditioner` applies it: input P^T r1 (Dirichlet nodes zeroed), output
+    y = P y_c on the sample's grid, and the gradient P^T dL/dy for the network."""
     lib = net.lib
     prob = ts.prob
-    Hn = Wn = ts.n + 1
+    f = getattr(ts, "factor", 1)
+    Hf = ts.n + 1
+    Hn = Wn = ts.n // f + 1
     Hp, Wp = padded(Hn), padded(Wn)
+    nd = ts.nd
+    fixed = torch.as_tensor(prob.mask.astype(np.uint8), device=net.device) if f > 1 else None
+    rc_buf = torch.empty((batch, Hn * Wn * nd), dtype=torch.float32, device=net.device)
+    y_fine = torch.empty((batch, Hf * Hf * nd), dtype=torch.float32, device=net.device)
+    gc_buf = torch.empty((batch, Hn * Wn * nd), dtype=torch.float32, device=net.device)
     params = net.parameters()
     opt = torch.optim.Adam(params, lr=lr)
     sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, steps)
@@ -589,16 +603,37 @@ def train(net, ts, steps=3000, batch=16, lr=2e-3, seed=0, verbose=False):
         idx = torch.randint(0, len(ts), (batch,), generator=gen)
         pids = ts.pid[idx].tolist()
         for b, (i, pi) in enumerate(zip(idx.tolist(), pids)):
-            to_image(lib, ts.r1[i], ts.aux[pi], Hn, Wn, True, out=x[b:b + 1], scale=sc[b:b + 1], stream=stream,
-                     nd=ts.nd, naux=ts.naux)
+            src = ts.r1[i]
+            if f > 1:
+                rc = lib.agx_nn_restrict_field(_p(ts.r1[i]), _p(fixed), nd, Hn, Wn, f, _p(rc_buf[b]), stream)
+                if rc != 0:
+                    raise RuntimeError("agx_nn_restrict_field failed")
+                src = rc_buf[b]
+            to_image(lib, src, ts.aux[pi], Hn, Wn, True, out=x[b:b + 1], scale=sc[b:b + 1], stream=stream,
+                     nd=nd, naux=ts.naux)
         out, acts = net.forward(x, keep=True)
-        y = (out[..., :ts.nd].float()[:, :Hn, :Wn].reshape(batch, -1) * ts.free).contiguous()
+        yc = out[..., :nd].float()[:, :Hn, :Wn].reshape(batch, -1).contiguous()
+        if f > 1:
+            for b in range(batch):
+                rc = lib.agx_nn_prolong_field(_p(yc[b]), nd, Hn, Wn, f, _p(y_fine[b]), stream)
+                if rc != 0:
+                    raise RuntimeError("agx_nn_prolong_field failed")
+            y = (y_fine * ts.free).contiguous()
+        else:
+            y = (yc * ts.free).contiguous()
         for b, pi in enumerate(pids):
             prob._call("agx_spmv_values", N.AGX_F32, C.c_void_p(ts.values[pi].data_ptr()),
                        C.c_void_p(y[b].data_ptr()), C.c_void_p(Ky[b].data_ptr()))
         r1 = ts.r1[idx.to(net.device)]
         loss, grad = energy_loss(r1, y, Ky, ts.s[idx.to(net.device)])
-        g[:, :Hn, :Wn, :ts.nd] = (grad * ts.free / batch).reshape(batch, Hn, Wn, ts.nd)
+        gy = (grad * ts.free / batch).contiguous()
+        if f > 1:  # y = P y_c: dL/dy_c = P^T dL/dy
+            for b in range(batch):
+                rc = lib.agx_nn_restrict_field(_p(gy[b]), None, nd, Hn, Wn, f, _p(gc_buf[b]), stream)
+                if rc != 0:
+                    raise RuntimeError("agx_nn_restrict_field failed")
+            gy = gc_buf
+        g[:, :Hn, :Wn, :nd] = gy.reshape(batch, Hn, Wn, nd)
         # the backward pass is linear in g: run it on g / max|g| (bf16-friendly) and rescale
         gmax = float(g.abs().max().clamp_min(1e-30))
         gw, gb = net.backward((g / gmax).to(torch.bfloat16), acts)

@@ -185,6 +185,9 @@ def solve_linear(dofs, settings, static_settings, **kwargs):
     rhs = -R
     prob._call("agx_solve", N.C.c_void_p(rhs.data_ptr()), N.C.c_void_p(dx.data_ptr()), N.C.byref(kopts),
                N.C.byref(info))
+    if kopts.method == N.AGX_CHOL_BAND and info.status == N.AGX_DIVERGED:
+        raise RuntimeError("the direct solve found the tangent not positive (or negative) definite at these DOFs; "
+                           "use an iterative solver ('bicgstab') for indefinite tangents")
     out = torch.where(m, g, dx)
     return _out_like(out, dofs, prob.key)
 

@@ -33,6 +33,8 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--problem", default="heat", choices=["heat", "membrane"])
     ap.add_argument("--rhs-per-state", type=int, default=400)
+    ap.add_argument("--factor", type=int, default=1, help="membrane: train the network on the grid coarsened by this")
+    ap.add_argument("--degree", type=int, default=3, help="membrane: Chebyshev pre-smoothing degree")
     ap.add_argument("--out", default=None)
     args = ap.parse_args()
     if args.out is None:
@@ -43,7 +45,7 @@ def main():
         net = learned.UNet(seed=args.seed)
     else:
         ts = learned.make_membrane_training_set(n=args.n, rhs_per_state=args.rhs_per_state, seed=args.seed,
-                                                verbose=True)
+                                                factor=args.factor, degree=args.degree, verbose=True)
         net = learned.UNet(seed=args.seed, n_in=ts.nd + ts.naux)
     t1 = time.time()
     losses = learned.train(net, ts, steps=args.steps, batch=args.batch, lr=args.lr, verbose=True)
@@ -58,7 +60,8 @@ def main():
                                    for i in range(0, len(losses), 100)],
             "problem": args.problem,
             "command": f"python -m autopdex_gb300.train_preconditioner --problem {args.problem} --n {args.n} "
-                       f"--problems {args.problems} --rhs-per-state {args.rhs_per_state} --steps {args.steps}"}
+                       f"--problems {args.problems} --rhs-per-state {args.rhs_per_state} --factor {args.factor} "
+                       f"--degree {args.degree} --steps {args.steps}"}
     with open(os.path.splitext(args.out)[0] + ".json", "w") as fh:
         json.dump(meta, fh, indent=1)
     print(f"data {t1 - t0:.1f} s ({len(ts)} pairs), training {t2 - t1:.1f} s, "

@@ -114,3 +114,14 @@ def test_indefinite_tangent_reports_breakdown():
     rc = prob._call("agx_solve", N.C.c_void_p(b.data_ptr()), N.C.c_void_p(x.data_ptr()), N.C.byref(opts),
                     N.C.byref(info))
     assert rc == N.AGX_DIVERGED and info.status == N.AGX_DIVERGED
+
+
+def test_newton_with_direct_solve_stops_on_indefinite_tangent():
+    """From a far-from-equilibrium start the membrane's tangent is indefinite: Newton with a
+    direct-solver name stops with the diverged flag instead of stepping with a failed factor."""
+    from autopdex_gb300 import solver
+    w = configs.cook_membrane(n=12, n_steps=2, solver="lapack")
+    w.settings = w.steps[0](w.settings)
+    u0 = np.random.default_rng(11).uniform(-0.05, 0.05, w.n_dofs).reshape(-1, 2)
+    sol, (it, res, div) = solver.solver(u0, w.settings, w.static_settings, newton_tol=1e-8)
+    assert div and it == 1

@@ -50,7 +50,10 @@ def test_solver_type_linear_matches_oracle(case):
     if w.steps:
         w.settings = w.steps[-1](w.settings)
     static = dict(w.static_settings, **{"solver type": "linear", "solver": "lapack"})
-    u0 = np.random.default_rng(3).uniform(-scale, scale, w.n_dofs) * (0.0 if case == "poisson" else 0.2)
+    # small states for the nearly incompressible membrane: far from equilibrium its tangent is
+    # indefinite (lam / mu = 5000) and the direct solve, a Cholesky factorization, refuses it
+    u0 = np.random.default_rng(3).uniform(-scale, scale, w.n_dofs) * {"poisson": 0.0, "neo_hooke_3d": 0.2,
+                                                                       "cook": 2e-4}[case]
     sol, info = solver.solver(_like(w, u0), w.settings, static, krylov_tol=1e-13)
     assert info is None
     prob = oracle_problem(w)
