@@ -352,17 +352,23 @@ struct ModelTraits {
   static constexpr int SLOTS = 1 + SDIM + (MODEL == AGX_MODEL_NEO_HOOKE ? SDIM : 0);  // N, g, h
 };
 
-// One kernel per (element type, model, arithmetic type, what to compute).
-template <int ET, int MODEL, typename T, bool DO_R, bool DO_K>
+// One kernel per (element type, model, arithmetic type, what to compute).  CB > 0: the
+// tangent columns of nodes b0 .. b0 + CB - 1 only (a lane holds CB x NDOF x NDOF accumulators
+// instead of NEN x NDOF x NDOF: the 27-node brick's neo-Hooke tangent row, 243 entries, is
+// assembled in passes over column chunks, each recomputing the element's Gauss points).
+template <int ET, int MODEL, typename T, bool DO_R, bool DO_K, int CB = 0>
 __global__ void __launch_bounds__(AGX_BLOCK)
 element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* __restrict__ epos,
                const T* __restrict__ coords, const double* __restrict__ dofs,
                const T* __restrict__ elem_field, const double* __restrict__ node_field,
                const uint8_t* __restrict__ dmask_node, ModelParams mp, double* __restrict__ R,
                T* __restrict__ vals, int64_t nnzb, const double* __restrict__ geo, double* __restrict__ geo_out,
-               int ng, const QuadTable qt) {
+               int ng, const QuadTable qt, int b0 = 0) {
   using ET_ = ElemTraits<ET>;
   constexpr int RDIM = ET_::RDIM, NEN = ET_::NEN, GROUP = ET_::GROUP;
+  constexpr int NCOL = (CB > 0 && CB < NEN) ? CB : NEN;  // tangent column nodes of this pass
+  constexpr bool CHUNKED = NCOL < NEN;
+  const int c0 = CHUNKED ? b0 : 0;
   // integration points per element: the simplex set's table, or the ng-point Gauss rule per direction
   const int NQ = is_simplex<ET>() ? qt.n : (RDIM == 1 ? ng : (RDIM == 2 ? ng * ng : ng * ng * ng));
   constexpr int SDIM = space_dim<ET>();
@@ -406,10 +412,10 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
     double Ra[NDOF];
 #pragma unroll
     for (int c = 0; c < NDOF; ++c) Ra[c] = 0.0;
-    T K[DO_K ? NEN : 1][DO_K ? NDOF : 1][DO_K ? NDOF : 1];
+    T K[DO_K ? NCOL : 1][DO_K ? NDOF : 1][DO_K ? NDOF : 1];
     if constexpr (DO_K) {
 #pragma unroll
-      for (int b = 0; b < NEN; ++b)
+      for (int b = 0; b < NCOL; ++b)
 #pragma unroll
         for (int i = 0; i < NDOF; ++i)
 #pragma unroll
@@ -528,14 +534,16 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
             for (int d = 0; d < SDIM; ++d) slab[warp][lane][1 + d] = ga[d];
             __syncwarp();
 #pragma unroll
-            for (int b = 0; b < NEN; ++b) {
+            for (int bb = 0; bb < NCOL; ++bb) {
+              const int b = c0 + bb;
+              if (CHUNKED && b >= NEN) break;
               const T Nb = slab[warp][gbase + b][0];
               T gg = 0;
 #pragma unroll
               for (int d = 0; d < SDIM; ++d) gg += ga[d] * slab[warp][gbase + b][1 + d];
               T kab = kq * gg;
               if constexpr (MODEL == AGX_MODEL_HEAT_BE) kab += mass * Na * Nb + dkq * Nb * gug;
-              K[b][0][0] += wdet * kab;
+              K[bb][0][0] += wdet * kab;
             }
           }
         } else if constexpr (MODEL == AGX_MODEL_NEO_HOOKE) {
@@ -575,7 +583,9 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
             __syncwarp();
             const T lj2 = lam * Jdet * Jdet;
 #pragma unroll
-            for (int b = 0; b < NEN; ++b) {
+            for (int bb = 0; bb < NCOL; ++bb) {
+              const int b = c0 + bb;
+              if (CHUNKED && b >= NEN) break;
               T gb[SDIM], hb[SDIM];
 #pragma unroll
               for (int d = 0; d < SDIM; ++d) {
@@ -589,7 +599,7 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
               for (int i = 0; i < SDIM; ++i)
 #pragma unroll
                 for (int k = 0; k < SDIM; ++k)
-                  K[b][i][k] += wdet * ((i == k ? mu * gg : T(0)) - c * hb[i] * ha[k] + lj2 * ha[i] * hb[k]);
+                  K[bb][i][k] += wdet * ((i == k ? mu * gg : T(0)) - c * hb[i] * ha[k] + lj2 * ha[i] * hb[k]);
             }
           }
         }
@@ -606,7 +616,9 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
     }
     if constexpr (DO_K && MT::HAS_K) {
 #pragma unroll
-      for (int b = 0; b < NEN; ++b) {
+      for (int bb = 0; bb < NCOL; ++bb) {
+        const int b = c0 + bb;
+        if (CHUNKED && b >= NEN) break;
         const unsigned dmb = __shfl_sync(0xffffffffu, dma, gbase + b);
         if (valid && act) {
           // entry-major value planes: entry (i, j) of block pos at vals[(i ndof + j) nnzb + pos]
@@ -616,7 +628,7 @@ element_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const int32_t* 
 #pragma unroll
             for (int j = 0; j < NDOF; ++j)
               if (!((dma >> i) & 1u) && !((dmb >> j) & 1u))
-                atomicAdd(blk + (int64_t)(i * NDOF + j) * nnzb, K[b][i][j]);
+                atomicAdd(blk + (int64_t)(i * NDOF + j) * nnzb, K[bb][i][j]);
         }
       }
     }
@@ -1059,10 +1071,27 @@ void launch_element(agx_context* ctx, agx_element_set& s, const double* dofs, do
     for (int d = 0; d < 3; ++d) qt.x[q][d] = s.qp[q][d];
     qt.w[q] = s.qw[q];
   }
-  element_kernel<ET, MODEL, T, DO_R, DO_K><<<grid, AGX_BLOCK, 0, ctx->stream>>>(
-      s.n_elem, s.d_conn, s.d_epos, coords_of<T>(ctx), dofs, elem_field_of<T>(s), s.d_node_field, ctx->d_dmask_node,
-      mp, R, vals, ctx->nnzb, geo, geo_out, s.ngauss, qt);
-  ctx->n_launches += 1;
+  if constexpr (ET == AGX_HEX27 && MODEL == AGX_MODEL_NEO_HOOKE && DO_K) {
+    // 27 nodes x 3 DOFs: the tangent row in column chunks (9 nodes in float32, 5 in float64), the
+    // residual with the first chunk
+    constexpr int CBk = std::is_same<T, double>::value ? 5 : 9;
+    for (int b0 = 0; b0 < 27; b0 += CBk) {
+      if (b0 == 0)
+        element_kernel<ET, MODEL, T, DO_R, true, CBk><<<grid, AGX_BLOCK, 0, ctx->stream>>>(
+            s.n_elem, s.d_conn, s.d_epos, coords_of<T>(ctx), dofs, elem_field_of<T>(s), s.d_node_field,
+            ctx->d_dmask_node, mp, R, vals, ctx->nnzb, geo, geo_out, s.ngauss, qt, b0);
+      else
+        element_kernel<ET, MODEL, T, false, true, CBk><<<grid, AGX_BLOCK, 0, ctx->stream>>>(
+            s.n_elem, s.d_conn, s.d_epos, coords_of<T>(ctx), dofs, elem_field_of<T>(s), s.d_node_field,
+            ctx->d_dmask_node, mp, nullptr, vals, ctx->nnzb, geo, nullptr, s.ngauss, qt, b0);
+      ctx->n_launches += 1;
+    }
+  } else {
+    element_kernel<ET, MODEL, T, DO_R, DO_K><<<grid, AGX_BLOCK, 0, ctx->stream>>>(
+        s.n_elem, s.d_conn, s.d_epos, coords_of<T>(ctx), dofs, elem_field_of<T>(s), s.d_node_field,
+        ctx->d_dmask_node, mp, R, vals, ctx->nnzb, geo, geo_out, s.ngauss, qt);
+    ctx->n_launches += 1;
+  }
 }
 
 // dispatch on (element type, model) for one pass kind
@@ -1115,6 +1144,7 @@ int dispatch(agx_context* ctx, agx_element_set& s, const double* dofs, double* R
   AGX_CASE(AGX_TET10, AGX_MODEL_NEO_HOOKE)
   AGX_CASE(AGX_HEX27, AGX_MODEL_POISSON_SINCOS)
   AGX_CASE(AGX_HEX27, AGX_MODEL_HEAT_POTENTIAL)
+  AGX_CASE(AGX_HEX27, AGX_MODEL_NEO_HOOKE)
 #undef AGX_CASE
   return agx_fail(ctx, AGX_ERR_UNSUPPORTED, "element type %d with model %d is not supported", s.elem_type, s.model);
 }

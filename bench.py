@@ -531,32 +531,46 @@ def rec_neo_hooke_cube(n=64, steps=10):
 
 
 def rec_cook(n=512, steps=1, plain_limit_s=120.0):
-    from autopdex_gb300 import configs, solver
+    """Cook's membrane: float64 Newton with the direct (banded Cholesky) solve, with plain
+    float64 Jacobi-PCG, and, when trained weights exist, with the learned preconditioner in
+    float64 flexible CG (the float32 / bf16 two-level preconditioner inside float64 vectors)."""
+    from autopdex_gb300 import configs, learned, solver
     out = {"workload": f"cook_membrane_{n}x{n}_q1 (nu = 0.4999), load steps 1..{steps} of 20"}
     # the float64 residual of this nearly incompressible membrane stalls near 4e-8 of a load
     # step's first residual at 512^2 (rounding of the displacements, amplified by lam / mu =
     # 5000, not the solver: the direct solve stalls there too), so the Newton tolerance is 1e-7
     rt = 1e-7
     out["newton_rtol"] = rt
-    for name, sol_name, prec, ktol in (("direct_fp64", "lapack", "float64", 1e-13),
-                                       ("plain_fp64_pcg", "pcg", "float64", 1e-4)):
-        w = configs.cook_membrane(n=n, solver=sol_name, precision=prec)
-        kw = dict(newton_tol=0.0, newton_rtol=rt, maxiter=12, krylov_tol=ktol)
-        if name == "plain_fp64_pcg":
-            kw["krylov_maxiter"] = 200000
+    variants = [("direct_fp64", dict(solver="lapack"), 1e-13), ("plain_fp64_pcg", dict(solver="pcg"), 1e-4)]
+    wpath = os.path.join(learned.WEIGHTS_DIR, "membrane_unet_n256.npz")
+    if os.path.exists(wpath):
+        variants.append(("learned_fp64_fcg", dict(solver="fcg", **{"type of preconditioner": "learned"}), 1e-4))
+    for name, st, ktol in variants:
+        w = configs.cook_membrane(n=n)
+        static = dict(w.static_settings, precision="float64", **st)
+        kw = dict(newton_tol=0.0, newton_rtol=rt, maxiter=12, krylov_tol=ktol, krylov_maxiter=200000)
+        if name.startswith("learned"):
+            net = learned.UNet.load(wpath)
+            factor = n // 128
+            coarse = configs.cook_membrane(n=n // factor)
+            solver.set_learned_preconditioner(None, learned.GridPreconditioner(
+                net, n, n, factor=factor, nd=2, aux=learned.node_features(coarse.raw["coords"])))
+            out["network"] = {"weights": os.path.basename(wpath), "grid": f"{n // factor + 1}^2 (coarsening {factor})"}
         x = w.dofs
         settings = dict(w.settings)
         per = []
         t0 = time.perf_counter()
         for k in range(steps):
             settings = w.steps[k](settings)
-            s, (x, info) = _timed(lambda: solver.solver(x, settings, w.static_settings, **kw))
+            s, (x, info) = _timed(lambda: solver.solver(x, settings, static, **kw))
             per.append(dict(s=s, **_info()))
             if time.perf_counter() - t0 > plain_limit_s:
                 break
         out[name] = {"s": sum(p["s"] for p in per), "steps_run": len(per), "per_step": per}
         if name == "direct_fp64":
             out["oracle_error"] = oracle_errors(w, x, per[-1]["res0"], settings=settings, scale=1e-5)
+    if "learned_fp64_fcg" in out and out["learned_fp64_fcg"]["steps_run"] == out["plain_fp64_pcg"]["steps_run"]:
+        out["speedup_learned_vs_plain_fp64"] = out["plain_fp64_pcg"]["s"] / out["learned_fp64_fcg"]["s"]
     return out
 
 
