@@ -825,10 +825,15 @@ def case(args):
         static["type of preconditioner"] = "learned"
     settings = w.steps[0](dict(w.settings)) if w.steps else w.settings
     kw = dict(newton_tol=0.0, newton_rtol=RTOL, maxiter=30, krylov_tol=args.krylov_tol, krylov_maxiter=400000)
+    solver.solver(w.dofs, settings, static, **kw)  # context, autotuning, graphs
+    if args.tpr:  # a product variant instead of the autotuner's pick (lanes per row, +256: four blocks per trip)
+        prob = get_problem(w.dofs, settings, static)
+        dt = N.AGX_F32 if args.precision == "mixed" else N.AGX_F64
+        prob._call("agx_set_tuning", dt, int(args.tpr))
     for _ in range(args.reps):
         solver.solver(w.dofs, settings, static, **kw)
     _sync()
-    print(f"solve {w.name}: {args.reps} solves, last {json.dumps(_info())}")
+    print(f"solve {w.name}: {args.reps} solves after a warm-up solve, last {json.dumps(_info())}")
 
 
 def main():
@@ -849,6 +854,7 @@ def main():
     ap.add_argument("--krylov-tol", type=float, default=1e-4)
     ap.add_argument("--layer", default="e0b")
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--tpr", type=int, default=0, help="solve case: SpMV variant code instead of the autotuner's")
     args = ap.parse_args()
     if args.case:
         case(args)
