@@ -504,30 +504,6 @@ gershgorin_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int3
   }
 }
 
-// rc -= t
-__global__ void __launch_bounds__(AGX_BLOCK)
-tl_residual(int64_t n, float* __restrict__ rc, const float* __restrict__ t, const agx_krylov_scalars* sc) {
-  if (sc->converged) return;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    rc[i] -= t[i];
-}
-
-// c = (rc, y) / (y, K y) with t = K y; c = 0 when the denominator vanishes
-__global__ void __launch_bounds__(AGX_BLOCK)
-tl_step(int64_t n, const float* __restrict__ r1, const float* __restrict__ y, const float* __restrict__ t,
-        agx_krylov_scalars* sc, double* partials, unsigned* counter) {
-  if (sc->converged) return;
-  float a_t = 0, b_t = 0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    a_t += r1[i] * y[i];
-    b_t += y[i] * t[i];
-  }
-  double acc[2] = {(double)a_t, (double)b_t};
-  double tot[2];
-  if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0)
-    sc->extra[2] = (isfinite(tot[0]) && isfinite(tot[1]) && tot[1] != 0.0) ? tot[0] / tot[1] : 0.0;
-}
-
 // z += c y; rc -= c t (t = K y): rc stays r - K z
 __global__ void __launch_bounds__(AGX_BLOCK)
 tl_combine(int64_t n, float* __restrict__ z, const float* __restrict__ y, float* __restrict__ rc,
@@ -537,6 +513,75 @@ tl_combine(int64_t n, float* __restrict__ z, const float* __restrict__ y, float*
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     z[i] += c * y[i];
     rc[i] -= c * t[i];
+  }
+}
+
+// ---- the two-level application's products with their element-wise work fused in ---------
+// One kernel per smoothing step: the product t = K x for the lane group's rows, then, for the
+// same rows, the step's element-wise update -- no separate sweep kernel and no t vector.
+//   TL_SWEEP  rc -= t; d = a x + b D^-1 rc (into dnew: x, the previous increment, is still
+//             being gathered by other rows); z += d
+//   TL_RESID  rc -= t                     (the residual after the last pre-smoothing step)
+//   TL_STEP   t written; block sums of (rc, y) and (y, t) -> c = (rc, y) / (y, K y)
+enum { TL_SWEEP = 0, TL_RESID = 1, TL_STEP = 2 };
+
+template <int NDOF, int TPR, int U, int EPI>
+__global__ void __launch_bounds__(AGX_BLOCK)
+tl_spmv(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+        const float* __restrict__ vals, int64_t nnzb, const float* __restrict__ x, float* __restrict__ rc,
+        const float* __restrict__ dinv, float a, float b, float* __restrict__ dnew, float* __restrict__ z,
+        float* __restrict__ tout, agx_krylov_scalars* sc, double* partials, unsigned* counter) {
+  if (sc->converged) return;
+  const int sub = threadIdx.x % TPR;
+  const int64_t total = ((n_rows * TPR + 31) / 32) * 32;
+  float acc_a = 0.0f, acc_b = 0.0f;
+  for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = L / TPR;
+    float yr[NDOF];
+    bsr_row<float, NDOF, TPR, false, U>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, x, nullptr,
+                                        0.0f, yr);
+    if (row < n_rows && sub == 0) {
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i) {
+        const int64_t d = row * NDOF + i;
+        const float t = yr[i];
+        if constexpr (EPI == TL_SWEEP) {
+          const float r = rc[d] - t;
+          rc[d] = r;
+          const float dn = (a != 0.0f ? a * x[d] : 0.0f) + b * dinv[d] * r;
+          dnew[d] = dn;
+          z[d] += dn;
+        } else if constexpr (EPI == TL_RESID) {
+          rc[d] -= t;
+        } else {
+          tout[d] = t;
+          acc_a += rc[d] * x[d];
+          acc_b += x[d] * t;
+        }
+      }
+    }
+  }
+  if constexpr (EPI == TL_STEP) {
+    double acc[2] = {(double)acc_a, (double)acc_b};
+    double tot[2];
+    if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0)
+      sc->extra[2] = (isfinite(tot[0]) && isfinite(tot[1]) && tot[1] != 0.0) ? tot[0] / tot[1] : 0.0;
+  }
+}
+
+// z += c y; rc -= c t; then the first post-smoothing step: d = b D^-1 rc into dz, z += d
+__global__ void __launch_bounds__(AGX_BLOCK)
+tl_combine_sweep(int64_t n, float* __restrict__ z, const float* __restrict__ y, float* __restrict__ rc,
+                 const float* __restrict__ t, const float* __restrict__ dinv, float b, float* __restrict__ dz,
+                 const agx_krylov_scalars* sc) {
+  if (sc->converged) return;
+  const float c = (float)sc->extra[2];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float r = rc[i] - c * t[i];
+    rc[i] = r;
+    const float d = b * dinv[i] * r;
+    dz[i] = d;
+    z[i] = (z[i] + c * y[i]) + d;
   }
 }
 
@@ -1099,6 +1144,43 @@ int agx_residual_norm(agx_context* ctx, const double* R, double* norm2, double* 
 }
 
 // z = M(r) on the float32 Krylov vectors (f_r -> f_z) for the flexible method
+template <int ND, int EPI>
+void tl_spmv_nd(agx_context* ctx, int code, int g, const float* x, float* rc, float a, float b, float* dnew,
+                float* tout) {
+  auto* sc = ctx->d_scal;
+  const int64_t nr = ctx->n_nodes;
+#define AGX_TL(TP_, U_)                                                                                           \
+  tl_spmv<ND, TP_, U_, EPI><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, ctx->d_vals32,     \
+                                                               ctx->nnzb, x, rc, ctx->d_dinv32, a, b, dnew,       \
+                                                               ctx->f_z, tout, sc, ctx->d_partials, ctx->d_counter)
+  switch (code) {
+    case 1: AGX_TL(1, 2); break;
+    case 2: AGX_TL(2, 2); break;
+    case 4: AGX_TL(4, 2); break;
+    case 16: AGX_TL(16, 2); break;
+    case 2 | SPMV_UNROLL4: AGX_TL(2, 4); break;
+    case 4 | SPMV_UNROLL4: AGX_TL(4, 4); break;
+    case 8 | SPMV_UNROLL4: AGX_TL(8, 4); break;
+    default: AGX_TL(8, 2); break;
+  }
+#undef AGX_TL
+}
+
+// t = K x with the step's element-wise work (TL_SWEEP / TL_RESID / TL_STEP), the float32 tangent,
+// the autotuner's product variant for float32
+template <int EPI>
+void launch_tl_spmv(agx_context* ctx, const float* x, float* rc, float a, float b, float* dnew, float* tout) {
+  agx_prof_scope ps(ctx, AGX_PROF_SMOOTH);
+  const int tuned = ctx->spmv_tpr[1];
+  const int code = tuned > 0 ? tuned : default_tpr(ctx);
+  // a reducing kernel writes one partial per block: its grid stays within the partials buffer
+  const int g = EPI == TL_STEP ? ctx->red_blocks : agx_grid(ctx, ctx->n_nodes * (code & (SPMV_UNROLL4 - 1)), 8);
+  if (ctx->ndof == 1) tl_spmv_nd<1, EPI>(ctx, code, g, x, rc, a, b, dnew, tout);
+  else if (ctx->ndof == 2) tl_spmv_nd<2, EPI>(ctx, code, g, x, rc, a, b, dnew, tout);
+  else tl_spmv_nd<3, EPI>(ctx, code, g, x, rc, a, b, dnew, tout);
+  ctx->n_launches += 1;
+}
+
 int apply_registered_preconditioner(agx_context* ctx) {
   const int64_t n = ctx->n_dofs;
   const int gv = agx_grid(ctx, n);
@@ -1136,47 +1218,46 @@ int apply_registered_preconditioner(agx_context* ctx) {
       cb[k] = (float)ctx->precond_omega;
     }
   }
-  float *rc = ctx->f_w2, *t = ctx->f_w1, *y = ctx->f_w3, *dz = ctx->f_w4;
-  // profiling categories: the products under AGX_PROF_SMOOTH, the element-wise kernels under
-  // AGX_PROF_VECTOR, the registered callback (the network) under AGX_PROF_PRECOND
-  auto smooth_product = [&](const float* in, float* out) {
-    agx_prof_scope pp(ctx, AGX_PROF_SMOOTH);
-    agx_spmv_impl(ctx, AGX_F32, in, out);
-  };
-  for (int s = 0; s < nu; ++s) {
-    {
-      agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
-      tl_sweep<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv32, cb[s], ca[s], s == 0 ? ctx->f_r : rc, rc,
-                                                  s == 0 ? nullptr : t, ctx->f_z, dz, s == 0, sc);
-    }
-    smooth_product(dz, t);
-  }
+  // rc the running residual r - K z, y the network's output, dA / dB the increments of
+  // consecutive smoothing steps (a step reads the previous one while writing its own), t = K y.
+  // Profiling categories: the products (with their fused element-wise work) under
+  // AGX_PROF_SMOOTH, the element-wise kernels under AGX_PROF_VECTOR, the registered callback
+  // (the network) under AGX_PROF_PRECOND.
+  float *rc = ctx->f_w2, *y = ctx->f_w3, *dA = ctx->f_w4, *dB = ctx->f_w1, *t = ctx->f_w1;
   {
-    agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
-    tl_residual<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, rc, t, sc);
+    agx_prof_scope pv(ctx, AGX_PROF_VECTOR);  // first step from z = 0: rc = r, d = b0 D^-1 r, z = d
+    tl_sweep<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv32, cb[0], ca[0], ctx->f_r, rc, nullptr, ctx->f_z, dA,
+                                                1, sc);
+    ctx->n_launches += 1;
   }
+  for (int s = 1; s < nu; ++s) {
+    launch_tl_spmv<TL_SWEEP>(ctx, dA, rc, ca[s], cb[s], dB, nullptr);
+    std::swap(dA, dB);
+  }
+  launch_tl_spmv<TL_RESID>(ctx, dA, rc, 0.0f, 0.0f, nullptr, nullptr);
   {
     agx_prof_scope pn(ctx, AGX_PROF_PRECOND);
     if (ctx->precond(ctx->precond_user, rc, y, n, ctx->stream) != 0) return -1;
     zero_prescribed<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir, ctx->d_dir_dofs, y);
+    ctx->n_launches += 1;
   }
-  smooth_product(y, t);
+  launch_tl_spmv<TL_STEP>(ctx, y, rc, 0.0f, 0.0f, nullptr, t);
+  if (ctx->precond_mode < 2) {
+    agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
+    tl_combine<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_z, y, rc, t, sc);
+    ctx->n_launches += 1;
+    return 0;
+  }
+  // z += c y, rc -= c t and the first post-smoothing step in one kernel; then the others
+  float *pA = ctx->f_w4, *pB = ctx->f_w1;  // t (in f_w1) is consumed by the combined kernel
   {
     agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
-    tl_step<<<ctx->vec_blocks, AGX_BLOCK, 0, ctx->stream>>>(n, rc, y, t, sc, ctx->d_partials, ctx->d_counter);
-    tl_combine<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_z, y, rc, t, sc);
+    tl_combine_sweep<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_z, y, rc, t, ctx->d_dinv32, cb[0], pA, sc);
+    ctx->n_launches += 1;
   }
-  ctx->n_launches += 2 * nu + 5;
-  if (ctx->precond_mode >= 2) {
-    for (int s = 0; s < nu; ++s) {
-      {
-        agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
-        tl_sweep<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv32, cb[s], ca[s], rc, rc, s == 0 ? nullptr : t,
-                                                    ctx->f_z, dz, 0, sc);
-      }
-      if (s + 1 < nu) smooth_product(dz, t);
-    }
-    ctx->n_launches += 2 * nu - 1;
+  for (int s = 1; s < nu; ++s) {
+    launch_tl_spmv<TL_SWEEP>(ctx, pA, rc, ca[s], cb[s], pB, nullptr);
+    std::swap(pA, pB);
   }
   return 0;
 }
