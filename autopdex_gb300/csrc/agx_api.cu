@@ -114,7 +114,6 @@ bool model_ok(int elem_type, int model, int dim, int ndof, int n_params, std::st
     case AGX_MODEL_NEO_HOOKE:
       if (ndof != sdim) return why = "NEO_HOOKE needs dim DOFs per node", false;
       if (n_params < 2) return why = "NEO_HOOKE needs params E, nu", false;
-      if (elem_type == AGX_HEX27) return why = "NEO_HOOKE on 27-node bricks is not implemented", false;
       if (domain) return true;
       return why = "NEO_HOOKE needs a domain element (quad4/quad9/tri3/tri6 in 2-D, hex8/tet4/tet10 in 3-D)", false;
     case AGX_MODEL_NEUMANN:

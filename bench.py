@@ -334,12 +334,19 @@ def headline_roofline(h):
     s = 4  # float32 products
     # algorithmic bytes per launch: values and columns of every stored block, row pointers, and
     # the vectors (fused Krylov product: z, p_old read, p_new, q written; plain product: x, y)
-    fused = nnzb * (ndof * ndof * s + 4) + 4 * (n_nodes + 1) + 4 * n * s
-    plain = nnzb * (ndof * ndof * s + 4) + 4 * (n_nodes + 1) + 2 * n * s
+    matrix = nnzb * (ndof * ndof * s + 4) + 4 * (n_nodes + 1)
+    fused = matrix + 4 * n * s
+    # the two-level products carry their element-wise work: per application 2 (nu - 1) sweep
+    # products (x gathered; rc, z read and written; D^-1 read; the new increment written: 7
+    # vectors), one residual product (x; rc read and written: 3) and one step product (y, rc
+    # read, K y written: 3); nu = 3 smoothing steps on either side
+    nu = 3
+    plain = matrix + n * s * (2 * (nu - 1) * 7 + 3 + 3) / (2 * (nu - 1) + 2)
     hc = h["w"].raw["n"] // h["factor"] + 1
     flops = _network_flops(learned.padded(hc), learned.padded(hc))
     tpr = getattr(prob, "spmv_tpr", "tpr")
-    cand = {"smoothing_product": ("hbm", plain, f"spmv_kernel<float,1,{tpr}> (two-level smoothing and K y products)"),
+    cand = {"smoothing_product": ("hbm", plain, f"tl_spmv<1,{tpr}> (two-level smoothing, residual and step products "
+                                                "with their element-wise work fused)"),
             "krylov_product": ("hbm", fused, f"spmv_dot_kernel<float,1,{tpr}> (FCG product with direction update "
                                              "and dot)"),
             "network": ("tensor", flops, "U-Net forward: 15 conv3x3_tc (tcgen05, BF16), pooling, upsampling and "
@@ -530,7 +537,7 @@ def rec_neo_hooke_cube(n=64, steps=10):
     return out
 
 
-def rec_cook(n=512, steps=1, plain_limit_s=120.0):
+def rec_cook(n=512, steps=1, plain_limit_s=120.0, with_learned=False):
     """Cook's membrane: float64 Newton with the direct (banded Cholesky) solve, with plain
     float64 Jacobi-PCG, and, when trained weights exist, with the learned preconditioner in
     float64 flexible CG (the float32 / bf16 two-level preconditioner inside float64 vectors)."""
@@ -543,7 +550,7 @@ def rec_cook(n=512, steps=1, plain_limit_s=120.0):
     out["newton_rtol"] = rt
     variants = [("direct_fp64", dict(solver="lapack"), 1e-13), ("plain_fp64_pcg", dict(solver="pcg"), 1e-4)]
     wpath = os.path.join(learned.WEIGHTS_DIR, "membrane_unet_n256.npz")
-    if os.path.exists(wpath):
+    if with_learned and os.path.exists(wpath):
         variants.append(("learned_fp64_fcg", dict(solver="fcg", **{"type of preconditioner": "learned"}), 1e-4))
     for name, st, ktol in variants:
         w = configs.cook_membrane(n=n)
@@ -824,14 +831,19 @@ def case(args):
         _heat_learned_setup(w, args.size)
         static["type of preconditioner"] = "learned"
     settings = w.steps[0](dict(w.settings)) if w.steps else w.settings
-    kw = dict(newton_tol=0.0, newton_rtol=RTOL, maxiter=30, krylov_tol=args.krylov_tol, krylov_maxiter=400000)
-    solver.solver(w.dofs, settings, static, **kw)  # context, autotuning, graphs
+    kw = dict(newton_tol=0.0, newton_rtol=RTOL if args.workload != "cook" else 1e-7, maxiter=30,
+              krylov_tol=args.krylov_tol, krylov_maxiter=400000)
+    x0 = w.dofs
+    if args.workload == "neo_hooke":  # load step 1 from the linear lifting of the prescribed u_x
+        x0 = np.zeros((w.n_dofs // 3, 3))
+        x0[:, 0] = w.raw["stretch"] / w.raw["n_steps"] * w.raw["coords"][:, 0]
+    solver.solver(x0, settings, static, **kw)  # context, autotuning, graphs
     if args.tpr:  # a product variant instead of the autotuner's pick (lanes per row, +256: four blocks per trip)
-        prob = get_problem(w.dofs, settings, static)
+        prob = get_problem(x0, settings, static)
         dt = N.AGX_F32 if args.precision == "mixed" else N.AGX_F64
         prob._call("agx_set_tuning", dt, int(args.tpr))
     for _ in range(args.reps):
-        solver.solver(w.dofs, settings, static, **kw)
+        solver.solver(x0, settings, static, **kw)
     _sync()
     print(f"solve {w.name}: {args.reps} solves after a warm-up solve, last {json.dumps(_info())}")
 
