@@ -83,6 +83,8 @@ _SIGNATURES = {
     "agx_profile_read": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     "agx_autotune": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
     "agx_set_tuning": (C.c_int, [_P, C.c_int, C.c_int]),
+    "agx_grid_pattern": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "agx_set_pdl": (C.c_int, [C.c_int]),
     "agx_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
 "agx_pcg_noalloc": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int, _P, _P, C.c_double, C.c_int, _P,
                                 C.POINTER(SolveInfo), C.c_char_p, C.c_int]),
@@ -95,6 +97,13 @@ _SIGNATURES = {
     "agx_nn_unpack_wgrad": (C.c_int, [_P, C.c_int, C.c_int, _P, _P]),
     "agx_nn_pool2": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
     "agx_nn_upsample2": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
+    "agx_nn_pool": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
+    "agx_nn_restrict_image_work": (C.c_int, []),
+    "agx_nn_set_halo_loader": (C.c_int, [C.c_int]),
+    "agx_nn_restrict_image": (C.c_int, [_P, _P, C.c_int, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                        _P, _P, _P, _P, _P]),
+    "agx_nn_prolong_image": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, _P]),
+    "agx_nn_upsample": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
     "agx_nn_relu_backward": (C.c_int, [_P, _P, C.c_int64, _P]),
     "agx_nn_add": (C.c_int, [_P, _P, C.c_int64, _P]),
     "agx_nn_bias_grad": (C.c_int, [_P, C.c_int64, C.c_int, _P, _P]),

@@ -213,17 +213,19 @@ class Problem:
         import json
         from . import build as _b
         path = os.path.join(_b.LIBDIR, "autotune.json")
+        gny = C.c_int()
+        self._call("agx_grid_pattern", C.byref(gny))
         key = f"{torch.cuda.get_device_name(self.device)}|{'f32' if dtype == N.AGX_F32 else 'f64'}|" \
-              f"ndof={self.ndof}|dim={self.dim}|nnzb=2^{int(np.log2(max(1, self.nnzb)))}"
+              f"ndof={self.ndof}|dim={self.dim}|nnzb=2^{int(np.log2(max(1, self.nnzb)))}" \
+              f"{'|grid' if gny.value > 0 else ''}"
         cache = {}
         try:
             with open(path) as fh:
                 cache = json.load(fh)
         except (OSError, ValueError):
             cache = {}
-        if key in cache:
+        if key in cache and self.lib.agx_set_tuning(self.ctx, dtype, int(cache[key]["spmv_tpr"])) == N.AGX_OK:
             tpr_v = int(cache[key]["spmv_tpr"])
-            self._call("agx_set_tuning", dtype, tpr_v)
         else:
             self._call("agx_assemble", C.c_void_p(dofs_dev.data_ptr()), None, dtype)
             tpr = C.c_int()

@@ -132,6 +132,8 @@ bool model_ok(int elem_type, int model, int dim, int ndof, int n_params, std::st
 
 }  // namespace
 
+bool g_agx_pdl = true;  // agx_set_pdl
+
 extern "C" {
 
 int agx_create(agx_context** out, void* stream) {
@@ -502,16 +504,34 @@ int agx_autotune(agx_context* ctx, int* spmv_tpr, float* spmv_ms) {
 int agx_set_tuning(agx_context* ctx, int dtype, int spmv_tpr) {
   if (!ctx) return AGX_ERR_ARG;
   if (dtype != AGX_F64 && dtype != AGX_F32) return agx_fail(ctx, AGX_ERR_ARG, "dtype must be AGX_F64 or AGX_F32");
-  const int lanes = spmv_tpr & 255, unroll4 = spmv_tpr >> 8;
+  if (spmv_tpr == SPMV_GRID) {
+    if (ctx->pattern_grid_ny <= 0)
+      return agx_fail(ctx, AGX_ERR_ARG, "the grid product (512) needs the pattern of a structured QUAD4 grid with 1 "
+                                        "or 2 DOFs per node");
+    ctx->spmv_tpr[dtype == AGX_F32 ? 1 : 0] = spmv_tpr;
+    return AGX_OK;
+  }
+  const int lanes = spmv_tpr & (SPMV_UNROLL4 - 1), unroll4 = spmv_tpr / SPMV_UNROLL4;
   const bool plain_ok = unroll4 == 0 && (lanes == 0 || lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8 ||
                                           lanes == 16);
   const bool unroll_ok = unroll4 == 1 && (lanes == 2 || lanes == 4 || lanes == 8);
   if (!plain_ok && !unroll_ok)
     return agx_fail(ctx, AGX_ERR_ARG, "lanes per row must be 0, 1, 2, 4, 8 or 16 (2, 4 or 8 with 256 added for four "
-                                      "blocks per lane and trip)");
+                                      "blocks per lane and trip; 512 the structured grid's product)");
   if (ctx->ndof == 3 && spmv_tpr != 0 && lanes < 4)
     return agx_fail(ctx, AGX_ERR_ARG, "3 DOFs per node need 4 or more lanes per row");
   ctx->spmv_tpr[dtype == AGX_F32 ? 1 : 0] = spmv_tpr;
+  return AGX_OK;
+}
+
+int agx_set_pdl(int enable) {
+  g_agx_pdl = enable != 0;
+  return AGX_OK;
+}
+
+int agx_grid_pattern(const agx_context* ctx, int* ny) {
+  if (!ctx || !ny) return AGX_ERR_ARG;
+  *ny = ctx->pattern_grid_ny;
   return AGX_OK;
 }
 

@@ -59,6 +59,13 @@ struct agx_krylov_scalars {
   int pad[2];
 };
 
+// Krylov product variant codes: lanes per block row (1, 2, 4, 8, 16), plus SPMV_UNROLL4 for
+// four blocks per lane and trip (2, 4, 8 lanes); SPMV_GRID the structured grid's index-free
+// product (one lane per row, 1 or 2 DOFs per node)
+constexpr int SPMV_UNROLL4 = 256;
+constexpr int SPMV_GRID = 512;
+inline int spmv_lanes(int code) { return code == SPMV_GRID ? 1 : (code & (SPMV_UNROLL4 - 1)); }
+
 struct agx_context {
   cudaStream_t stream = nullptr;
   std::string err;
@@ -105,6 +112,10 @@ struct agx_context {
   float *f_x = nullptr, *f_r = nullptr, *f_z = nullptr, *f_p = nullptr, *f_q = nullptr, *f_rold = nullptr;
   float *f_w1 = nullptr, *f_w2 = nullptr, *f_w3 = nullptr, *f_w4 = nullptr;  // two-level preconditioner work
 
+  // > 0: the pattern is the in-range 3 x 3 stencil of a structured nx x ny QUAD4 grid with
+  // ny = pattern_grid_ny (the index-free product SPMV_GRID applies)
+  int pattern_grid_ny = 0;
+
   // reductions
   int red_blocks = 0;   // largest grid of a reducing kernel (8 per SM)
   int vec_blocks = 0;   // grid of the reducing vector kernels (2 per SM: short reduction tails)
@@ -133,6 +144,8 @@ struct agx_context {
     int every = 0;
     bool prof = false;             // captured with timing events
     int tpr = 0;                   // lanes per row of the captured products
+    int64_t kernels = 0;           // kernel nodes of the graph (the callback's included)
+    bool pdl = false;              // captured with programmatic dependent launch
     std::vector<cudaEvent_t> ev[AGX_PROF_CATEGORIES];  // event pairs recorded by each replay
   };
   graph_rec graphs[3];  // Jacobi-PCG float64, float32 methods, flexible CG float64
@@ -173,6 +186,36 @@ struct agx_context {
 // error handling: every entry point returns an int status and records a message
 // ------------------------------------------------------------------------------------
 int agx_fail(agx_context* ctx, int code, const char* fmt, ...);
+
+// Programmatic dependent launch.  The kernels of the Krylov iterations and of the learned
+// preconditioner begin with agx_pdl_entry(): griddepcontrol.wait returns once the grid before
+// them in the stream has completed and its writes are visible, then launch_dependents lets the
+// next grid launch.  agx_launch_pdl launches with programmatic stream serialization, so the next
+// kernel's blocks are scheduled while this one runs instead of after it (the launch latency of a
+// chain of short dependent kernels is hidden).  Only kernels that begin with the entry may be
+// launched this way; without the attribute the entry costs nothing.  agx_set_pdl(0) turns the
+// attribute off process-wide.
+extern bool g_agx_pdl;
+__device__ __forceinline__ void agx_pdl_entry() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t agx_launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                                  Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = g_agx_pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
 
 #define AGX_CUDA(ctx, call)                                                          \
   do {                                                                               \

@@ -186,17 +186,80 @@ __device__ __forceinline__ void bsr_row(int64_t row, int sub, const int32_t* __r
     for (int i = 0; i < NDOF; ++i) y[i] += __shfl_xor_sync(0xffffffffu, y[i], o);
 }
 
+// The same product for the tangent of a structured nx x ny QUAD4 grid (node p = i (ny + 1) + j,
+// every pattern row the in-range 3 x 3 stencil of its node, checked when the pattern is built):
+// row p's blocks are its stencil neighbours in (di, dj) order starting at
+//   rowptr(p) = S(i) (3 ny + 1) + r_i S(j),  S(m) = 3 m - [m > 0],  r_i = [i > 0] + 1 + [i < nx]
+// (S(m) blocks in the rows or columns before m, 3 ny + 1 in a full row of nodes), so one lane per
+// row reads only its values and the gathered vector: no row pointer, no column index.
+template <typename T, int NDOF, bool DIR>
+__device__ __forceinline__ void grid_row(int64_t row, int ny, int64_t n_rows, const T* __restrict__ vals,
+                                         int64_t nnzb, const T* __restrict__ x, const T* __restrict__ pold, T beta,
+                                         T (&y)[NDOF]) {
+  const int64_t ny1 = (int64_t)ny + 1, nx = n_rows / ny1 - 1;
+  const int64_t i = row / ny1;
+  const int j = (int)(row - i * ny1);
+  const int ri = (i > 0) + 1 + (i < nx);
+  const int64_t k0 = (3 * i - (i > 0)) * (3 * (int64_t)ny + 1) + (int64_t)ri * (3 * j - (j > 0));
+  bool ok[9];
+  int m[9];
+  int cnt = 0;
+#pragma unroll
+  for (int t = 0; t < 9; ++t) {
+    const int di = t / 3 - 1, dj = t % 3 - 1;
+    ok[t] = (di >= 0 || i > 0) && (di <= 0 || i < nx) && (dj >= 0 || j > 0) && (dj <= 0 || j < ny);
+    m[t] = cnt;
+    cnt += ok[t] ? 1 : 0;
+  }
+  T v[9][NDOF * NDOF];
+#pragma unroll
+  for (int e = 0; e < NDOF * NDOF; ++e)
+#pragma unroll
+    for (int t = 0; t < 9; ++t) v[t][e] = ok[t] ? __ldcs(vals + (int64_t)e * nnzb + k0 + m[t]) : T(0);
+#pragma unroll
+  for (int q = 0; q < NDOF; ++q) y[q] = 0;
+#pragma unroll
+  for (int t = 0; t < 9; ++t) {
+    const int64_t c = row + (int64_t)(t / 3 - 1) * ny1 + (t % 3 - 1);
+#pragma unroll
+    for (int jj = 0; jj < NDOF; ++jj) {
+      T xv = ok[t] ? x[c * NDOF + jj] : T(0);
+      if constexpr (DIR) {
+        if (ok[t]) xv += beta * pold[c * NDOF + jj];
+      }
+#pragma unroll
+      for (int q = 0; q < NDOF; ++q) y[q] += v[t][q * NDOF + jj] * xv;
+    }
+  }
+}
+
+// A product row in the tangent's storage: U > 0 the node-block CSR with TPR lanes per row,
+// U == 0 the structured grid's stencil (one lane per row, gny = ny)
+template <typename T, int NDOF, int TPR, bool DIR, int U>
+__device__ __forceinline__ void tangent_row(int64_t row, int sub, const int32_t* __restrict__ rowptr,
+                                            const int32_t* __restrict__ col, const T* __restrict__ vals,
+                                            int64_t nnzb, int64_t n_rows, int gny, const T* __restrict__ x,
+                                            const T* __restrict__ pold, T beta, T (&y)[NDOF]) {
+  if constexpr (U == 0) {
+    static_assert(TPR == 1, "the grid product has one lane per row");
+    grid_row<T, NDOF, DIR>(row, gny, n_rows, vals, nnzb, x, pold, beta, y);
+  } else {
+    bsr_row<T, NDOF, TPR, DIR, U>(row, sub, rowptr, col, vals, nnzb, x, pold, beta, y);
+  }
+}
+
 template <typename T, int NDOF, int TPR, int U = 2>
 __global__ void __launch_bounds__(AGX_BLOCK) spmv_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr,
                                                          const int32_t* __restrict__ col, const T* __restrict__ vals,
-                                                         int64_t nnzb, const T* __restrict__ x, T* __restrict__ y) {
+                                                         int64_t nnzb, int gny, const T* __restrict__ x,
+                                                         T* __restrict__ y) {
   const int sub = threadIdx.x % TPR;
   const int64_t total = ((n_rows * TPR + 31) / 32) * 32;
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = L / TPR;
     T yr[NDOF];
-    bsr_row<T, NDOF, TPR, false, U>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, x, nullptr,
-                                    T(0), yr);
+    tangent_row<T, NDOF, TPR, false, U>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, n_rows, gny,
+                                        x, nullptr, T(0), yr);
     if (row < n_rows && sub == 0) {
 #pragma unroll
       for (int i = 0; i < NDOF; ++i) y[row * NDOF + i] = yr[i];
@@ -204,14 +267,15 @@ __global__ void __launch_bounds__(AGX_BLOCK) spmv_kernel(int64_t n_rows, const i
   }
 }
 
-// p_new = z + beta p_old (own rows), q = A p_new, alpha = rz / (p_new, q).  beta = 0 on the
-// first iteration (p_old = 0), which makes p_new = z.
+// p_new = z + beta p_old (own rows), q = A p_new, block partials of (p_new, q) for the step
+// alpha = rz / (p_new, q).  beta = 0 on the first iteration (p_old = 0), which makes p_new = z.
 template <typename T, int NDOF, int TPR, int U = 2>
 __global__ void __launch_bounds__(AGX_BLOCK)
 spmv_dot_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-                const T* __restrict__ vals, int64_t nnzb, const T* __restrict__ z, const T* __restrict__ pold,
-                T* __restrict__ pnew, T* __restrict__ q, agx_krylov_scalars* sc, double* partials, unsigned* counter,
-                const T* __restrict__ rflex, int block_partials) {
+                const T* __restrict__ vals, int64_t nnzb, int gny, const T* __restrict__ z,
+                const T* __restrict__ pold, T* __restrict__ pnew, T* __restrict__ q, agx_krylov_scalars* sc,
+                double* __restrict__ partials, const T* __restrict__ rflex) {
+  agx_pdl_entry();
   if (sc->converged) return;
   const T beta = (T)sc->beta;
   const int sub = threadIdx.x % TPR;
@@ -220,8 +284,8 @@ spmv_dot_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = L / TPR;
     T yr[NDOF];
-    bsr_row<T, NDOF, TPR, true, U>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, z, pold, beta,
-                                   yr);
+    tangent_row<T, NDOF, TPR, true, U>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, n_rows, gny, z,
+                                       pold, beta, yr);
     if (row < n_rows && sub == 0) {
 #pragma unroll
       for (int i = 0; i < NDOF; ++i) {
@@ -234,26 +298,14 @@ spmv_dot_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_
       }
     }
   }
+  // block partials of (p, A p) -- and of (p, r) for the flexible method -- for pcg_finish_pq
+  // (Jacobi-PCG) or fcg_finish_pq (flexible CG)
   double acc[2] = {(double)acc_t, (double)accr_t};
-  if (block_partials) {  // Jacobi-PCG: pcg_finish_pq sums them
+  if (rflex) {
+    write_block_partials<2>(acc, partials);
+  } else {
     const double acc1[1] = {acc[0]};
     write_block_partials<1>(acc1, partials);
-    return;
-  }
-  double tot[2];
-  if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
-    sc->pq = tot[0];
-    // flexible CG: the step is the exact line minimiser (p, r) / (p, A p), which differs from
-    // (r, z) / (p, A p) once the preconditioner varies from one iteration to the next
-    if (rflex) sc->rz = tot[1];
-    // Only a zero or non-finite (p, Ap) is a breakdown: the tangents of clockwise-numbered
-    // quads (mesher.py:88-94 numbers quads clockwise, so det J < 0) are negative definite,
-    // and CG with a Jacobi preconditioner of the same sign runs as on (-K, -D).
-    if (bad(tot[0])) {
-      sc->converged = 2;
-    } else {
-      sc->alpha = sc->rz / tot[0];
-    }
   }
 }
 
@@ -320,6 +372,7 @@ __global__ void __launch_bounds__(AGX_BLOCK)
 pcg_update_kernel(int64_t n, T* __restrict__ x, T* __restrict__ r, T* __restrict__ z, const T* __restrict__ p,
                   const T* __restrict__ q, const T* __restrict__ dinv, agx_krylov_scalars* sc,
                   double* __restrict__ partials) {
+  agx_pdl_entry();
   if (sc->converged) return;
   constexpr int V = 16 / sizeof(T);
   using W = vec16<T>;
@@ -365,6 +418,7 @@ pcg_update_kernel(int64_t n, T* __restrict__ x, T* __restrict__ r, T* __restrict
 // one block: alpha = (r, z) / (p, A p) from the product's block partials
 __global__ void __launch_bounds__(AGX_BLOCK)
 pcg_finish_pq(agx_krylov_scalars* sc, const double* __restrict__ parts, int np) {
+  agx_pdl_entry();
   if (sc->converged) return;
   double t[1];
   sum_block_partials<1>(parts, np, t);
@@ -381,6 +435,7 @@ pcg_finish_pq(agx_krylov_scalars* sc, const double* __restrict__ parts, int np) 
 // one block: the update's (r, z) and (r, r): iteration count, convergence test, beta
 __global__ void __launch_bounds__(AGX_BLOCK)
 pcg_finish_rz(agx_krylov_scalars* sc, const double* __restrict__ parts, int np) {
+  agx_pdl_entry();
   if (sc->converged) return;
   double t[2];
   sum_block_partials<2>(parts, np, t);
@@ -401,44 +456,122 @@ pcg_finish_rz(agx_krylov_scalars* sc, const double* __restrict__ parts, int np) 
 }
 
 // ---- flexible CG (Notay FCG(1)): beta = -(z_new, q) / (p, q) ----------------------------
+// The update and direction kernels write block partials (16-byte accesses when every vector is
+// aligned, a scalar loop otherwise); one-block kernels after them finish the sums and set the
+// step scalars, as in the Jacobi-PCG iteration.
+
+// x += a p; r -= a q; block partials of (r, r) for fcg_finish_update
 template <typename T>
 __global__ void __launch_bounds__(AGX_BLOCK)
 fcg_update_kernel(int64_t n, T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p, const T* __restrict__ q,
-                  agx_krylov_scalars* sc, double* partials, unsigned* counter) {
+                  agx_krylov_scalars* sc, double* __restrict__ partials) {
+  agx_pdl_entry();
   if (sc->converged) return;
+  constexpr int V = 16 / sizeof(T);
+  using W = vec16<T>;
   const T a = (T)sc->alpha;
-  double acc[1] = {0.0};
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  T rr_t = 0;
+  const bool aligned = ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(r) |
+                         reinterpret_cast<uintptr_t>(p) | reinterpret_cast<uintptr_t>(q)) & 15u) == 0;
+  const int64_t nv = aligned ? n / V : 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nv; k += stride) {
+    W xv = reinterpret_cast<const W*>(x)[k], rv = reinterpret_cast<const W*>(r)[k];
+    const W pv = reinterpret_cast<const W*>(p)[k], qv = reinterpret_cast<const W*>(q)[k];
+#pragma unroll
+    for (int u = 0; u < V; ++u) {
+      xv.v[u] += a * pv.v[u];
+      const T ri = rv.v[u] - a * qv.v[u];
+      rv.v[u] = ri;
+      rr_t += ri * ri;
+    }
+    reinterpret_cast<W*>(x)[k] = xv;
+    reinterpret_cast<W*>(r)[k] = rv;
+  }
+  for (int64_t i = nv * V + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     x[i] += a * p[i];
     const T ri = r[i] - a * q[i];
     r[i] = ri;
-    acc[0] += (double)ri * (double)ri;
+    rr_t += ri * ri;
   }
-  double tot[1];
-  if (reduce_last_block<1>(acc, partials, counter, tot) && threadIdx.x == 0) {
+  const double acc[1] = {(double)rr_t};
+  write_block_partials<1>(acc, partials);
+}
+
+// one block: iteration count, (r, r) and the convergence test
+__global__ void __launch_bounds__(AGX_BLOCK)
+fcg_finish_update(agx_krylov_scalars* sc, const double* __restrict__ parts, int np) {
+  agx_pdl_entry();
+  if (sc->converged) return;
+  double t[1];
+  sum_block_partials<1>(parts, np, t);
+  if (threadIdx.x == 0) {
     sc->iters += 1;
-    sc->rr = tot[0];
-    if (!isfinite(tot[0])) sc->converged = 2;
-    else if (tot[0] <= sc->rr_stop) sc->converged = 1;
+    sc->rr = t[0];
+    if (!isfinite(t[0])) sc->converged = 2;
+    else if (t[0] <= sc->rr_stop) sc->converged = 1;
   }
 }
 
-// after z = M r: rz = (r, z), beta = -(z, q)/(p, q)   (first=1: only rz, p = z)
+// after z = M r: block partials of (r, z) and (z, q) for fcg_finish_direction
 template <typename T>
 __global__ void __launch_bounds__(AGX_BLOCK)
 fcg_direction_dots(int64_t n, const T* __restrict__ r, const T* __restrict__ z, const T* __restrict__ q,
-                   agx_krylov_scalars* sc, double* partials, unsigned* counter) {
+                   agx_krylov_scalars* sc, double* __restrict__ partials) {
+  agx_pdl_entry();
   if (sc->converged) return;
-  double acc[2] = {0.0, 0.0};
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    acc[0] += (double)r[i] * (double)z[i];
-    acc[1] += (double)z[i] * (double)q[i];
+  constexpr int V = 16 / sizeof(T);
+  using W = vec16<T>;
+  T rz_t = 0, zq_t = 0;
+  const bool aligned = ((reinterpret_cast<uintptr_t>(r) | reinterpret_cast<uintptr_t>(z) |
+                         reinterpret_cast<uintptr_t>(q)) & 15u) == 0;
+  const int64_t nv = aligned ? n / V : 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nv; k += stride) {
+    const W rv = reinterpret_cast<const W*>(r)[k], zv = reinterpret_cast<const W*>(z)[k];
+    const W qv = reinterpret_cast<const W*>(q)[k];
+#pragma unroll
+    for (int u = 0; u < V; ++u) {
+      rz_t += rv.v[u] * zv.v[u];
+      zq_t += zv.v[u] * qv.v[u];
+    }
   }
-  double tot[2];
-  if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
-    sc->rz = tot[0];
-    sc->beta = sc->iters == 0 ? 0.0 : -tot[1] / sc->pq;
-    if (bad(tot[0])) sc->converged = 2;
+  for (int64_t i = nv * V + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    rz_t += r[i] * z[i];
+    zq_t += z[i] * q[i];
+  }
+  const double acc[2] = {(double)rz_t, (double)zq_t};
+  write_block_partials<2>(acc, partials);
+}
+
+// one block: rz = (r, z), beta = -(z, q) / (p, q) (0 on the first direction)
+__global__ void __launch_bounds__(AGX_BLOCK)
+fcg_finish_direction(agx_krylov_scalars* sc, const double* __restrict__ parts, int np) {
+  agx_pdl_entry();
+  if (sc->converged) return;
+  double t[2];
+  sum_block_partials<2>(parts, np, t);
+  if (threadIdx.x == 0) {
+    sc->rz = t[0];
+    sc->beta = sc->iters == 0 ? 0.0 : -t[1] / sc->pq;
+    if (bad(t[0])) sc->converged = 2;
+  }
+}
+
+// one block: (p, A p) and the flexible step's (p, r) from spmv_dot_kernel's partials: the
+// step is the exact line minimiser (p, r) / (p, A p), which differs from (r, z) / (p, A p)
+// once the preconditioner varies from one iteration to the next
+__global__ void __launch_bounds__(AGX_BLOCK)
+fcg_finish_pq(agx_krylov_scalars* sc, const double* __restrict__ parts, int np) {
+  agx_pdl_entry();
+  if (sc->converged) return;
+  double t[2];
+  sum_block_partials<2>(parts, np, t);
+  if (threadIdx.x == 0) {
+    sc->pq = t[0];
+    sc->rz = t[1];
+    if (bad(t[0])) sc->converged = 2;
+    else sc->alpha = t[1] / t[0];
   }
 }
 
@@ -452,6 +585,7 @@ template <typename T>
 __global__ void __launch_bounds__(AGX_BLOCK)
 jacobi_apply(int64_t n, const T* __restrict__ dinv, const T* __restrict__ r, T* __restrict__ z,
              const agx_krylov_scalars* sc) {
+  agx_pdl_entry();
   if (sc->converged) return;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     z[i] = dinv[i] * r[i];
@@ -465,6 +599,7 @@ __global__ void __launch_bounds__(AGX_BLOCK)
 tl_sweep(int64_t n, const float* __restrict__ dinv, float b, float a, const float* rin, float* rc,
          const float* __restrict__ t, float* __restrict__ z, float* __restrict__ dz, int first,
          const agx_krylov_scalars* sc) {
+  agx_pdl_entry();
   if (sc->converged) return;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float v = t ? rin[i] - t[i] : rin[i];
@@ -508,6 +643,7 @@ gershgorin_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int3
 __global__ void __launch_bounds__(AGX_BLOCK)
 tl_combine(int64_t n, float* __restrict__ z, const float* __restrict__ y, float* __restrict__ rc,
            const float* __restrict__ t, const agx_krylov_scalars* sc) {
+  agx_pdl_entry();
   if (sc->converged) return;
   const float c = (float)sc->extra[2];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -522,15 +658,16 @@ tl_combine(int64_t n, float* __restrict__ z, const float* __restrict__ y, float*
 //   TL_SWEEP  rc -= t; d = a x + b D^-1 rc (into dnew: x, the previous increment, is still
 //             being gathered by other rows); z += d
 //   TL_RESID  rc -= t                     (the residual after the last pre-smoothing step)
-//   TL_STEP   t written; block sums of (rc, y) and (y, t) -> c = (rc, y) / (y, K y)
+//   TL_STEP   t written; block partials of (rc, y) and (y, t) for tl_finish_step
 enum { TL_SWEEP = 0, TL_RESID = 1, TL_STEP = 2 };
 
 template <int NDOF, int TPR, int U, int EPI>
 __global__ void __launch_bounds__(AGX_BLOCK)
 tl_spmv(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-        const float* __restrict__ vals, int64_t nnzb, const float* __restrict__ x, float* __restrict__ rc,
+        const float* __restrict__ vals, int64_t nnzb, int gny, const float* __restrict__ x, float* __restrict__ rc,
         const float* __restrict__ dinv, float a, float b, float* __restrict__ dnew, float* __restrict__ z,
-        float* __restrict__ tout, agx_krylov_scalars* sc, double* partials, unsigned* counter) {
+        float* __restrict__ tout, agx_krylov_scalars* sc, double* __restrict__ partials) {
+  agx_pdl_entry();
   if (sc->converged) return;
   const int sub = threadIdx.x % TPR;
   const int64_t total = ((n_rows * TPR + 31) / 32) * 32;
@@ -538,8 +675,8 @@ tl_spmv(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __res
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = L / TPR;
     float yr[NDOF];
-    bsr_row<float, NDOF, TPR, false, U>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, x, nullptr,
-                                        0.0f, yr);
+    tangent_row<float, NDOF, TPR, false, U>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, n_rows,
+                                            gny, x, nullptr, 0.0f, yr);
     if (row < n_rows && sub == 0) {
 #pragma unroll
       for (int i = 0; i < NDOF; ++i) {
@@ -562,11 +699,19 @@ tl_spmv(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __res
     }
   }
   if constexpr (EPI == TL_STEP) {
-    double acc[2] = {(double)acc_a, (double)acc_b};
-    double tot[2];
-    if (reduce_last_block<2>(acc, partials, counter, tot) && threadIdx.x == 0)
-      sc->extra[2] = (isfinite(tot[0]) && isfinite(tot[1]) && tot[1] != 0.0) ? tot[0] / tot[1] : 0.0;
+    const double acc[2] = {(double)acc_a, (double)acc_b};
+    write_block_partials<2>(acc, partials);  // tl_finish_step sums them
   }
+}
+
+// one block: the energy-optimal step c = (rc, y) / (y, K y) from TL_STEP's partials
+__global__ void __launch_bounds__(AGX_BLOCK)
+tl_finish_step(agx_krylov_scalars* sc, const double* __restrict__ parts, int np) {
+  agx_pdl_entry();
+  if (sc->converged) return;
+  double t[2];
+  sum_block_partials<2>(parts, np, t);
+  if (threadIdx.x == 0) sc->extra[2] = (isfinite(t[0]) && isfinite(t[1]) && t[1] != 0.0) ? t[0] / t[1] : 0.0;
 }
 
 // z += c y; rc -= c t; then the first post-smoothing step: d = b D^-1 rc into dz, z += d
@@ -574,6 +719,7 @@ __global__ void __launch_bounds__(AGX_BLOCK)
 tl_combine_sweep(int64_t n, float* __restrict__ z, const float* __restrict__ y, float* __restrict__ rc,
                  const float* __restrict__ t, const float* __restrict__ dinv, float b, float* __restrict__ dz,
                  const agx_krylov_scalars* sc) {
+  agx_pdl_entry();
   if (sc->converged) return;
   const float c = (float)sc->extra[2];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -724,6 +870,7 @@ bicg_init(int64_t n, const double* __restrict__ b, double* __restrict__ x, doubl
 // f_r = r / ||b|| (float32), and back: z = f_z ||b||
 __global__ void __launch_bounds__(AGX_BLOCK) to_f32_scaled(int64_t n, const double* __restrict__ r,
                                                            float* __restrict__ f, const agx_krylov_scalars* sc) {
+  agx_pdl_entry();
   if (sc->converged) return;
   const double s = sc->extra[0];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -732,6 +879,7 @@ __global__ void __launch_bounds__(AGX_BLOCK) to_f32_scaled(int64_t n, const doub
 
 __global__ void __launch_bounds__(AGX_BLOCK) from_f32_scaled(int64_t n, const float* __restrict__ f,
                                                              double* __restrict__ z, const agx_krylov_scalars* sc) {
+  agx_pdl_entry();
   if (sc->converged) return;
   const double s = sc->extra[1];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -793,6 +941,7 @@ __global__ void masked_scale_kernel(int64_t n, const double* __restrict__ src, d
 
 template <typename T>
 __global__ void zero_prescribed(int64_t n_dir, const int32_t* __restrict__ dir, T* __restrict__ v) {
+  agx_pdl_entry();
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n_dir; k += (int64_t)gridDim.x * blockDim.x)
     v[dir[k]] = T(0);
 }
@@ -813,50 +962,49 @@ int resident_grid(agx_context* ctx, K kernel) {
   return g < ctx->red_blocks ? g : ctx->red_blocks;
 }
 
-// returns the grid (the number of block partials written when block_partials is set)
+// returns the grid (the number of block partials written)
 template <typename T, int ND, int TP, int U = 2>
-int spmv_dot_variant(agx_context* ctx, const T* vals, const T* z, const T* pold, T* pnew, T* q, const T* rflex,
-                     int block_partials) {
+int spmv_dot_variant(agx_context* ctx, const T* vals, const T* z, const T* pold, T* pnew, T* q, const T* rflex) {
   static int g_cache = 0;
   if (!g_cache) g_cache = resident_grid(ctx, spmv_dot_kernel<T, ND, TP, U>);
-  spmv_dot_kernel<T, ND, TP, U><<<g_cache, AGX_BLOCK, 0, ctx->stream>>>(ctx->n_nodes, ctx->d_rowptr, ctx->d_col,
-                                                                        vals, ctx->nnzb, z, pold, pnew, q, ctx->d_scal,
-                                                                        ctx->d_partials, ctx->d_counter, rflex,
-                                                                        block_partials);
+  agx_launch_pdl(spmv_dot_kernel<T, ND, TP, U>, g_cache, AGX_BLOCK, 0, ctx->stream, ctx->n_nodes, ctx->d_rowptr, ctx->d_col,
+                                                                        vals, ctx->nnzb, ctx->pattern_grid_ny, z, pold,
+                                                                        pnew, q, ctx->d_scal, ctx->d_partials, rflex);
   return g_cache;
 }
 
-// a product variant: lanes per block row, plus SPMV_UNROLL4 for four blocks per lane and trip
-constexpr int SPMV_UNROLL4 = 256;
 
 // default lanes per block row when the autotuner has not chosen one
 int default_tpr(const agx_context* ctx) { return ctx->ndof == 1 ? (ctx->dim == 3 ? 8 : 4) : (ctx->ndof == 2 ? 4 : 8); }
 
 template <typename T, int ND>
 int spmv_dot_nd(agx_context* ctx, int tpr, const T* vals, const T* z, const T* pold, T* pnew, T* q,
-                const T* rflex, int block_partials = 0) {
+                const T* rflex) {
   switch (tpr) {
-    case 1: return spmv_dot_variant<T, ND, 1>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
-    case 2: return spmv_dot_variant<T, ND, 2>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
-    case 4: return spmv_dot_variant<T, ND, 4>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
-    case 16: return spmv_dot_variant<T, ND, 16>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
-    case 2 | SPMV_UNROLL4: return spmv_dot_variant<T, ND, 2, 4>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
-    case 4 | SPMV_UNROLL4: return spmv_dot_variant<T, ND, 4, 4>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
-    case 8 | SPMV_UNROLL4: return spmv_dot_variant<T, ND, 8, 4>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
-    default: return spmv_dot_variant<T, ND, 8>(ctx, vals, z, pold, pnew, q, rflex, block_partials);
+    case 1: return spmv_dot_variant<T, ND, 1>(ctx, vals, z, pold, pnew, q, rflex);
+    case 2: return spmv_dot_variant<T, ND, 2>(ctx, vals, z, pold, pnew, q, rflex);
+    case 4: return spmv_dot_variant<T, ND, 4>(ctx, vals, z, pold, pnew, q, rflex);
+    case 16: return spmv_dot_variant<T, ND, 16>(ctx, vals, z, pold, pnew, q, rflex);
+    case 2 | SPMV_UNROLL4: return spmv_dot_variant<T, ND, 2, 4>(ctx, vals, z, pold, pnew, q, rflex);
+    case 4 | SPMV_UNROLL4: return spmv_dot_variant<T, ND, 4, 4>(ctx, vals, z, pold, pnew, q, rflex);
+    case 8 | SPMV_UNROLL4: return spmv_dot_variant<T, ND, 8, 4>(ctx, vals, z, pold, pnew, q, rflex);
+    case SPMV_GRID:
+      if constexpr (ND <= 2) return spmv_dot_variant<T, ND, 1, 0>(ctx, vals, z, pold, pnew, q, rflex);
+      [[fallthrough]];
+    default: return spmv_dot_variant<T, ND, 8>(ctx, vals, z, pold, pnew, q, rflex);
   }
 }
 
 // rflex (flexible CG only): the residual whose dot with the new direction gives the step
 template <typename T>
 int launch_spmv_dot(agx_context* ctx, const T* vals, const T* z, const T* pold, T* pnew, T* q,
-                    const T* rflex = nullptr, int block_partials = 0) {
+                    const T* rflex = nullptr) {
   agx_prof_scope ps(ctx, AGX_PROF_SPMV);
   const int tuned = ctx->spmv_tpr[std::is_same<T, float>::value ? 1 : 0];
   const int tpr = tuned > 0 ? tuned : default_tpr(ctx);
-  if (ctx->ndof == 1) return spmv_dot_nd<T, 1>(ctx, tpr, vals, z, pold, pnew, q, rflex, block_partials);
-  if (ctx->ndof == 2) return spmv_dot_nd<T, 2>(ctx, tpr, vals, z, pold, pnew, q, rflex, block_partials);
-  return spmv_dot_nd<T, 3>(ctx, tpr, vals, z, pold, pnew, q, rflex, block_partials);
+  if (ctx->ndof == 1) return spmv_dot_nd<T, 1>(ctx, tpr, vals, z, pold, pnew, q, rflex);
+  if (ctx->ndof == 2) return spmv_dot_nd<T, 2>(ctx, tpr, vals, z, pold, pnew, q, rflex);
+  return spmv_dot_nd<T, 3>(ctx, tpr, vals, z, pold, pnew, q, rflex);
 }
 
 template <int NDOF, int TPR>
@@ -886,9 +1034,12 @@ void launch_bicg_spmv(agx_context* ctx, int which, double* a, double* b, double*
 
 // Issues kn iterations through `chunk`: full chunks of an even length replay a CUDA graph
 // captured at the first use (keyed by the output vector; re-captured when it changes), the
-// remainder is launched directly.
+// remainder is launched directly.  `counted`: the launches the caller has already added to
+// the context's count for this chunk; a replay replaces them by the graph's kernel nodes,
+// which include a registered preconditioner's own kernels.
 template <class F>
-int run_chunk(agx_context* ctx, int slot, const void* x, int every, int kn, F&& chunk, int64_t pc_key = -1) {
+int run_chunk(agx_context* ctx, int slot, const void* x, int every, int kn, F&& chunk, int64_t counted,
+              int64_t pc_key = -1) {
   auto& gr = ctx->graphs[slot];
   // events recorded by graph nodes cannot be timed: profiling runs launch directly
   if (!ctx->use_graphs || ctx->prof_on || kn != every || every % 2 != 0) {
@@ -904,8 +1055,8 @@ int run_chunk(agx_context* ctx, int slot, const void* x, int every, int kn, F&& 
     AGX_CUDA(ctx, cudaEventCreateWithFlags(&ctx->graph_ev[1], cudaEventDisableTiming));
   }
   const cudaStream_t gs = legacy ? ctx->graph_stream : work;
-  if (!gr.exec || gr.key_x != x || gr.every != every || gr.prof != ctx->prof_on || gr.tpr != ctx->spmv_tpr[0] * 4096 + ctx->spmv_tpr[1] ||
-      gr.pc_key != pc_key) {
+  if (!gr.exec || gr.key_x != x || gr.every != every || gr.prof != ctx->prof_on ||
+      gr.tpr != ctx->spmv_tpr[0] * 4096 + ctx->spmv_tpr[1] || gr.pc_key != pc_key || gr.pdl != g_agx_pdl) {
     if (gr.exec) cudaGraphExecDestroy(gr.exec);
     gr.exec = nullptr;
     for (auto& v : gr.ev) {
@@ -913,14 +1064,26 @@ int run_chunk(agx_context* ctx, int slot, const void* x, int every, int kn, F&& 
       v.clear();
     }
     cudaGraph_t graph = nullptr;
+    const int64_t launches_before = ctx->n_launches;
     AGX_CUDA(ctx, cudaStreamBeginCapture(gs, cudaStreamCaptureModeThreadLocal));
     ctx->capturing = &gr;
     ctx->stream = gs;  // the chunk's launches go to the capturing stream
     chunk(every);
     ctx->stream = work;
     ctx->capturing = nullptr;
+    ctx->n_launches = launches_before;  // captured, not launched: the replay below counts them
     cudaError_t e = cudaStreamEndCapture(gs, &graph);
     if (e != cudaSuccess) return agx_fail(ctx, AGX_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    size_t nn = 0;
+    gr.kernels = 0;
+    if (cudaGraphGetNodes(graph, nullptr, &nn) == cudaSuccess && nn > 0) {
+      std::vector<cudaGraphNode_t> nodes(nn);
+      if (cudaGraphGetNodes(graph, nodes.data(), &nn) == cudaSuccess)
+        for (size_t i = 0; i < nn; ++i) {
+          cudaGraphNodeType t;
+          if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++gr.kernels;
+        }
+    }
     e = cudaGraphInstantiate(&gr.exec, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return agx_fail(ctx, AGX_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
@@ -929,6 +1092,7 @@ int run_chunk(agx_context* ctx, int slot, const void* x, int every, int kn, F&& 
     gr.prof = ctx->prof_on;
     gr.tpr = ctx->spmv_tpr[0] * 4096 + ctx->spmv_tpr[1];
     gr.pc_key = pc_key;
+    gr.pdl = g_agx_pdl;
   }
   if (legacy) {
     AGX_CUDA(ctx, cudaEventRecord(ctx->graph_ev[0], work));
@@ -939,6 +1103,7 @@ int run_chunk(agx_context* ctx, int slot, const void* x, int every, int kn, F&& 
   } else {
     AGX_CUDA(ctx, cudaGraphLaunch(gr.exec, work));
   }
+  ctx->n_launches += gr.kernels - counted;
   if (gr.prof) {
     // the replay re-recorded the graph's events: add their times once the chunk is done
     AGX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1006,7 +1171,8 @@ int agx_autotune_spmv(agx_context* ctx, int* chosen, float* best_ms) {
   if (ctx->tangent_valid != AGX_F32 && ctx->tangent_valid != AGX_F64)
     return agx_fail(ctx, AGX_ERR_STATE, "autotune needs an assembled tangent");
   const bool f32 = ctx->tangent_valid == AGX_F32;
-  const int cands[8] = {1, 2, 4, 8, 16, 2 | SPMV_UNROLL4, 4 | SPMV_UNROLL4, 8 | SPMV_UNROLL4};
+  std::vector<int> cands = {1, 2, 4, 8, 16, 2 | SPMV_UNROLL4, 4 | SPMV_UNROLL4, 8 | SPMV_UNROLL4};
+  if (ctx->pattern_grid_ny > 0) cands.push_back(SPMV_GRID);
   cudaEvent_t e0, e1;
   AGX_CUDA(ctx, cudaEventCreate(&e0));
   AGX_CUDA(ctx, cudaEventCreate(&e1));
@@ -1019,7 +1185,7 @@ int agx_autotune_spmv(agx_context* ctx, int* chosen, float* best_ms) {
   float best = 1e30f;
   int pick = default_tpr(ctx);
   for (int c : cands) {
-    if (ctx->ndof == 3 && (c & (SPMV_UNROLL4 - 1)) < 4) continue;
+    if (ctx->ndof == 3 && spmv_lanes(c) < 4) continue;
     auto run = [&]() {
       cudaMemsetAsync(ctx->d_scal, 0, sizeof(agx_krylov_scalars), ctx->stream);
       if (f32) {
@@ -1077,15 +1243,22 @@ void agx_launch_jacobi(agx_context* ctx, int dtype, const void* r, void* z) {
 template <typename T, int ND>
 void spmv_nd(agx_context* ctx, int tpr, int g, const T* v, const T* x, T* y) {
   const int64_t nr = ctx->n_nodes;
+  const int gny = ctx->pattern_grid_ny;
   switch (tpr) {
-    case 1: spmv_kernel<T, ND, 1><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
-    case 2: spmv_kernel<T, ND, 2><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
-    case 4: spmv_kernel<T, ND, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
-    case 16: spmv_kernel<T, ND, 16><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
-    case 2 | SPMV_UNROLL4: spmv_kernel<T, ND, 2, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
-    case 4 | SPMV_UNROLL4: spmv_kernel<T, ND, 4, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
-    case 8 | SPMV_UNROLL4: spmv_kernel<T, ND, 8, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
-    default: spmv_kernel<T, ND, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, x, y); break;
+    case 1: spmv_kernel<T, ND, 1><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, gny, x, y); break;
+    case 2: spmv_kernel<T, ND, 2><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, gny, x, y); break;
+    case 4: spmv_kernel<T, ND, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, gny, x, y); break;
+    case 16: spmv_kernel<T, ND, 16><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, gny, x, y); break;
+    case 2 | SPMV_UNROLL4: spmv_kernel<T, ND, 2, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, gny, x, y); break;
+    case 4 | SPMV_UNROLL4: spmv_kernel<T, ND, 4, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, gny, x, y); break;
+    case 8 | SPMV_UNROLL4: spmv_kernel<T, ND, 8, 4><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, gny, x, y); break;
+    case SPMV_GRID:
+      if constexpr (ND <= 2) {
+        spmv_kernel<T, ND, 1, 0><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, gny, x, y);
+        break;
+      }
+      [[fallthrough]];
+    default: spmv_kernel<T, ND, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, gny, x, y); break;
   }
 }
 
@@ -1094,7 +1267,7 @@ int agx_spmv_values_impl(agx_context* ctx, int dtype, const void* values, const 
   const int64_t nr = ctx->n_nodes;
   const int tuned = ctx->spmv_tpr[dtype == AGX_F32 ? 1 : 0];
   const int tpr = tuned > 0 ? tuned : default_tpr(ctx);
-  const int g = agx_grid(ctx, nr * (tpr & (SPMV_UNROLL4 - 1)), 8);
+  const int g = agx_grid(ctx, nr * spmv_lanes(tpr), 8);
   auto go = [&](auto tag) {
     using T = decltype(tag);
     const T* v = (const T*)values;
@@ -1150,9 +1323,10 @@ void tl_spmv_nd(agx_context* ctx, int code, int g, const float* x, float* rc, fl
   auto* sc = ctx->d_scal;
   const int64_t nr = ctx->n_nodes;
 #define AGX_TL(TP_, U_)                                                                                           \
-  tl_spmv<ND, TP_, U_, EPI><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, ctx->d_vals32,     \
-                                                               ctx->nnzb, x, rc, ctx->d_dinv32, a, b, dnew,       \
-                                                               ctx->f_z, tout, sc, ctx->d_partials, ctx->d_counter)
+  agx_launch_pdl(tl_spmv<ND, TP_, U_, EPI>, g, AGX_BLOCK, 0, ctx->stream, nr, ctx->d_rowptr, ctx->d_col, ctx->d_vals32,     \
+                                                               ctx->nnzb, ctx->pattern_grid_ny, x, rc,            \
+                                                               ctx->d_dinv32, a, b, dnew, ctx->f_z, tout, sc,     \
+                                                               ctx->d_partials)
   switch (code) {
     case 1: AGX_TL(1, 2); break;
     case 2: AGX_TL(2, 2); break;
@@ -1161,6 +1335,12 @@ void tl_spmv_nd(agx_context* ctx, int code, int g, const float* x, float* rc, fl
     case 2 | SPMV_UNROLL4: AGX_TL(2, 4); break;
     case 4 | SPMV_UNROLL4: AGX_TL(4, 4); break;
     case 8 | SPMV_UNROLL4: AGX_TL(8, 4); break;
+    case SPMV_GRID:
+      if constexpr (ND <= 2) {
+        AGX_TL(1, 0);
+        break;
+      }
+      [[fallthrough]];
     default: AGX_TL(8, 2); break;
   }
 #undef AGX_TL
@@ -1174,7 +1354,7 @@ void launch_tl_spmv(agx_context* ctx, const float* x, float* rc, float a, float 
   const int tuned = ctx->spmv_tpr[1];
   const int code = tuned > 0 ? tuned : default_tpr(ctx);
   // a reducing kernel writes one partial per block: its grid stays within the partials buffer
-  const int g = EPI == TL_STEP ? ctx->red_blocks : agx_grid(ctx, ctx->n_nodes * (code & (SPMV_UNROLL4 - 1)), 8);
+  const int g = EPI == TL_STEP ? ctx->red_blocks : agx_grid(ctx, ctx->n_nodes * spmv_lanes(code), 8);
   if (ctx->ndof == 1) tl_spmv_nd<1, EPI>(ctx, code, g, x, rc, a, b, dnew, tout);
   else if (ctx->ndof == 2) tl_spmv_nd<2, EPI>(ctx, code, g, x, rc, a, b, dnew, tout);
   else tl_spmv_nd<3, EPI>(ctx, code, g, x, rc, a, b, dnew, tout);
@@ -1188,7 +1368,7 @@ int apply_registered_preconditioner(agx_context* ctx) {
   if (ctx->precond_mode == 0) {
     agx_prof_scope pn(ctx, AGX_PROF_PRECOND);
     if (ctx->precond(ctx->precond_user, ctx->f_r, ctx->f_z, n, ctx->stream) != 0) return -1;
-    zero_prescribed<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir, ctx->d_dir_dofs,
+    agx_launch_pdl(zero_prescribed<float>, agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream, ctx->n_dir, ctx->d_dir_dofs,
                                                                                    ctx->f_z);
     ctx->n_launches += 1;
     return 0;
@@ -1226,7 +1406,7 @@ int apply_registered_preconditioner(agx_context* ctx) {
   float *rc = ctx->f_w2, *y = ctx->f_w3, *dA = ctx->f_w4, *dB = ctx->f_w1, *t = ctx->f_w1;
   {
     agx_prof_scope pv(ctx, AGX_PROF_VECTOR);  // first step from z = 0: rc = r, d = b0 D^-1 r, z = d
-    tl_sweep<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv32, cb[0], ca[0], ctx->f_r, rc, nullptr, ctx->f_z, dA,
+    agx_launch_pdl(tl_sweep, gv, AGX_BLOCK, 0, ctx->stream, n, ctx->d_dinv32, cb[0], ca[0], ctx->f_r, rc, nullptr, ctx->f_z, dA,
                                                 1, sc);
     ctx->n_launches += 1;
   }
@@ -1238,13 +1418,15 @@ int apply_registered_preconditioner(agx_context* ctx) {
   {
     agx_prof_scope pn(ctx, AGX_PROF_PRECOND);
     if (ctx->precond(ctx->precond_user, rc, y, n, ctx->stream) != 0) return -1;
-    zero_prescribed<float><<<agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream>>>(ctx->n_dir, ctx->d_dir_dofs, y);
+    agx_launch_pdl(zero_prescribed<float>, agx_grid(ctx, ctx->n_dir), AGX_BLOCK, 0, ctx->stream, ctx->n_dir, ctx->d_dir_dofs, y);
     ctx->n_launches += 1;
   }
   launch_tl_spmv<TL_STEP>(ctx, y, rc, 0.0f, 0.0f, nullptr, t);
+  agx_launch_pdl(tl_finish_step, 1, AGX_BLOCK, 0, ctx->stream, sc, ctx->d_partials, ctx->red_blocks);
+  ctx->n_launches += 1;
   if (ctx->precond_mode < 2) {
     agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
-    tl_combine<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_z, y, rc, t, sc);
+    agx_launch_pdl(tl_combine, gv, AGX_BLOCK, 0, ctx->stream, n, ctx->f_z, y, rc, t, sc);
     ctx->n_launches += 1;
     return 0;
   }
@@ -1252,7 +1434,7 @@ int apply_registered_preconditioner(agx_context* ctx) {
   float *pA = ctx->f_w4, *pB = ctx->f_w1;  // t (in f_w1) is consumed by the combined kernel
   {
     agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
-    tl_combine_sweep<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_z, y, rc, t, ctx->d_dinv32, cb[0], pA, sc);
+    agx_launch_pdl(tl_combine_sweep, gv, AGX_BLOCK, 0, ctx->stream, n, ctx->f_z, y, rc, t, ctx->d_dinv32, cb[0], pA, sc);
     ctx->n_launches += 1;
   }
   for (int s = 1; s < nu; ++s) {
@@ -1333,19 +1515,19 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
     auto chunk = [&](int kn) {
       for (int k = 0; k < kn; ++k) {
         double* pnew = pbuf[cur ^ 1];
-        const int ns = launch_spmv_dot<double>(ctx, ctx->d_vals64, ctx->d_z, pbuf[cur], pnew, ctx->d_q, nullptr, 1);
-        pcg_finish_pq<<<1, AGX_BLOCK, 0, ctx->stream>>>(sc, ctx->d_partials, ns);
+        const int ns = launch_spmv_dot<double>(ctx, ctx->d_vals64, ctx->d_z, pbuf[cur], pnew, ctx->d_q);
+        agx_launch_pdl(pcg_finish_pq, 1, AGX_BLOCK, 0, ctx->stream, sc, ctx->d_partials, ns);
         agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
-        pcg_update_kernel<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, x, ctx->d_r, ctx->d_z, pnew, ctx->d_q,
+        agx_launch_pdl(pcg_update_kernel<double>, g, AGX_BLOCK, 0, ctx->stream, n, x, ctx->d_r, ctx->d_z, pnew, ctx->d_q,
                                                                    ctx->d_dinv64, sc, ctx->d_partials);
-        pcg_finish_rz<<<1, AGX_BLOCK, 0, ctx->stream>>>(sc, ctx->d_partials, g);
+        agx_launch_pdl(pcg_finish_rz, 1, AGX_BLOCK, 0, ctx->stream, sc, ctx->d_partials, g);
         cur ^= 1;
       }
     };
     while (true) {
       const int kn = std::min(every, maxiter - it_done);
       ctx->n_launches += 4 * kn;
-      if (int rc = run_chunk(ctx, 0, x, every, kn, chunk)) return rc;
+      if (int rc = run_chunk(ctx, 0, x, every, kn, chunk, 4 * kn)) return rc;
       int rc = read_scalars(ctx);
       if (rc) return rc;
       it_done = ctx->h_scal->iters;
@@ -1363,30 +1545,34 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
       if (int rc = update_chebyshev_bound(ctx)) return rc;
       if (apply_registered_preconditioner(ctx) != 0)
         return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");
-      fcg_direction_dots<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_r, ctx->f_z, ctx->f_q, sc, ctx->d_partials,
-                                                                 ctx->d_counter);
-      ctx->n_launches += 2;
+      agx_launch_pdl(fcg_direction_dots<float>, g, AGX_BLOCK, 0, ctx->stream, n, ctx->f_r, ctx->f_z, ctx->f_q, sc, ctx->d_partials);
+      agx_launch_pdl(fcg_finish_direction, 1, AGX_BLOCK, 0, ctx->stream, sc, ctx->d_partials, g);
+      ctx->n_launches += 3;
     }
     auto chunk = [&](int kn) {
       for (int k = 0; k < kn; ++k) {
         float* pnew = pbuf[cur ^ 1];
         const int ns = launch_spmv_dot<float>(ctx, ctx->d_vals32, ctx->f_z, pbuf[cur], pnew, ctx->f_q,
-                                              flexible ? (const float*)ctx->f_r : nullptr, flexible ? 0 : 1);
+                                              flexible ? (const float*)ctx->f_r : nullptr);
         if (!flexible) {
-          pcg_finish_pq<<<1, AGX_BLOCK, 0, ctx->stream>>>(sc, ctx->d_partials, ns);
+          agx_launch_pdl(pcg_finish_pq, 1, AGX_BLOCK, 0, ctx->stream, sc, ctx->d_partials, ns);
           agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
-          pcg_update_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, ctx->f_r, ctx->f_z, pnew,
+          agx_launch_pdl(pcg_update_kernel<float>, g, AGX_BLOCK, 0, ctx->stream, n, ctx->f_x, ctx->f_r, ctx->f_z, pnew,
                                                                     ctx->f_q, ctx->d_dinv32, sc, ctx->d_partials);
-          pcg_finish_rz<<<1, AGX_BLOCK, 0, ctx->stream>>>(sc, ctx->d_partials, g);
+          agx_launch_pdl(pcg_finish_rz, 1, AGX_BLOCK, 0, ctx->stream, sc, ctx->d_partials, g);
         } else {
+          agx_launch_pdl(fcg_finish_pq, 1, AGX_BLOCK, 0, ctx->stream, sc, ctx->d_partials, ns);
           {
             agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
-            fcg_update_kernel<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_x, ctx->f_r, pnew, ctx->f_q, sc,
-                                                                      ctx->d_partials, ctx->d_counter);
+            agx_launch_pdl(fcg_update_kernel<float>, g, AGX_BLOCK, 0, ctx->stream, n, ctx->f_x, ctx->f_r, pnew, ctx->f_q, sc,
+                                                                      ctx->d_partials);
+            agx_launch_pdl(fcg_finish_update, 1, AGX_BLOCK, 0, ctx->stream, sc, ctx->d_partials, g);
           }
           if (apply_registered_preconditioner(ctx) != 0) precond_failed = true;
-          fcg_direction_dots<float><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_r, ctx->f_z, ctx->f_q, sc,
-                                                                     ctx->d_partials, ctx->d_counter);
+          agx_launch_pdl(fcg_direction_dots<float>, g, AGX_BLOCK, 0, ctx->stream, n, ctx->f_r, ctx->f_z, ctx->f_q, sc,
+                                                                     ctx->d_partials);
+          agx_launch_pdl(fcg_finish_direction, 1, AGX_BLOCK, 0, ctx->stream, sc, ctx->d_partials, g);
+          ctx->n_launches += 2;  // the flexible iteration's two extra finishers
         }
         cur ^= 1;
       }
@@ -1397,7 +1583,7 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
       if (flexible && !ctx->precond_capturable) {
         chunk(kn);  // a preconditioner that may synchronise or allocate: no graph
         AGX_CHECK_LAUNCH(ctx);
-      } else if (int rc = run_chunk(ctx, 1, ctx->f_x, every, kn, chunk, flexible ? ctx->precond_gen : -1)) {
+      } else if (int rc = run_chunk(ctx, 1, ctx->f_x, every, kn, chunk, 4 * kn, flexible ? ctx->precond_gen : -1)) {
         return rc;
       }
       if (precond_failed) return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");
@@ -1420,18 +1606,18 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
     auto precond = [&]() {
       if (!flexible) {
         agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
-        jacobi_apply<double><<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_dinv64, ctx->d_r, ctx->d_z, sc);
+        agx_launch_pdl(jacobi_apply<double>, gv, AGX_BLOCK, 0, ctx->stream, n, ctx->d_dinv64, ctx->d_r, ctx->d_z, sc);
         ctx->n_launches += 1;
         return;
       }
       {
         agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
-        to_f32_scaled<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_r, ctx->f_r, sc);
+        agx_launch_pdl(to_f32_scaled, gv, AGX_BLOCK, 0, ctx->stream, n, ctx->d_r, ctx->f_r, sc);
       }
       if (apply_registered_preconditioner(ctx) != 0) precond_failed = true;
       {
         agx_prof_scope pv(ctx, AGX_PROF_VECTOR);
-        from_f32_scaled<<<gv, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->f_z, ctx->d_z, sc);
+        agx_launch_pdl(from_f32_scaled, gv, AGX_BLOCK, 0, ctx->stream, n, ctx->f_z, ctx->d_z, sc);
       }
       ctx->n_launches += 2;
     };
@@ -1440,24 +1626,29 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
       precond();
       if (precond_failed) return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");
     }
-    fcg_direction_dots<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_r, ctx->d_z, ctx->d_q, sc, ctx->d_partials,
-                                                                ctx->d_counter);
-    ctx->n_launches += 1;
+    agx_launch_pdl(fcg_direction_dots<double>, g, AGX_BLOCK, 0, ctx->stream, n, ctx->d_r, ctx->d_z, ctx->d_q, sc, ctx->d_partials);
+    agx_launch_pdl(fcg_finish_direction, 1, AGX_BLOCK, 0, ctx->stream, sc, ctx->d_partials, g);
+    ctx->n_launches += 2;
     auto chunk = [&](int kn) {
       for (int k = 0; k < kn; ++k) {
         double* pnew = pbuf[cur ^ 1];
-        launch_spmv_dot<double>(ctx, ctx->d_vals64, ctx->d_z, pbuf[cur], pnew, ctx->d_q, (const double*)ctx->d_r, 0);
+        const int ns =
+            launch_spmv_dot<double>(ctx, ctx->d_vals64, ctx->d_z, pbuf[cur], pnew, ctx->d_q, (const double*)ctx->d_r);
+        agx_launch_pdl(fcg_finish_pq, 1, AGX_BLOCK, 0, ctx->stream, sc, ctx->d_partials, ns);
         {
           agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
-          fcg_update_kernel<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, x, ctx->d_r, pnew, ctx->d_q, sc,
-                                                                     ctx->d_partials, ctx->d_counter);
+          agx_launch_pdl(fcg_update_kernel<double>, g, AGX_BLOCK, 0, ctx->stream, n, x, ctx->d_r, pnew, ctx->d_q, sc,
+                                                                     ctx->d_partials);
+          agx_launch_pdl(fcg_finish_update, 1, AGX_BLOCK, 0, ctx->stream, sc, ctx->d_partials, g);
         }
         precond();
         {
           agx_prof_scope ps(ctx, AGX_PROF_VECTOR);
-          fcg_direction_dots<double><<<g, AGX_BLOCK, 0, ctx->stream>>>(n, ctx->d_r, ctx->d_z, ctx->d_q, sc,
-                                                                      ctx->d_partials, ctx->d_counter);
+          agx_launch_pdl(fcg_direction_dots<double>, g, AGX_BLOCK, 0, ctx->stream, n, ctx->d_r, ctx->d_z, ctx->d_q, sc,
+                                                                      ctx->d_partials);
+          agx_launch_pdl(fcg_finish_direction, 1, AGX_BLOCK, 0, ctx->stream, sc, ctx->d_partials, g);
         }
+        ctx->n_launches += 3;  // the three finishers
         cur ^= 1;
       }
     };
@@ -1467,7 +1658,7 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
       if (flexible && !ctx->precond_capturable) {
         chunk(kn);
         AGX_CHECK_LAUNCH(ctx);
-      } else if (int rc = run_chunk(ctx, 2, x, every, kn, chunk, flexible ? ctx->precond_gen : -1)) {
+      } else if (int rc = run_chunk(ctx, 2, x, every, kn, chunk, 3 * kn, flexible ? ctx->precond_gen : -1)) {
         return rc;
       }
       if (precond_failed) return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");

@@ -15,6 +15,8 @@
 //
 // Every wait is bounded: a CTA whose MMA does not complete in time records an error flag
 // and still releases its TMEM.
+#include <algorithm>
+#include <cooperative_groups.h>
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -23,6 +25,8 @@
 #include "../../include/autopdex_gb300_nn.h"
 
 namespace {
+
+namespace cg = cooperative_groups;
 
 constexpr int kTile = 128;        // output pixels per CTA (MMA M)
 constexpr int kWaitLimit = 1 << 22;
@@ -119,8 +123,9 @@ struct ConvArgs {
 // pixels x 16 channels -- is a no-swizzle K-major view starting at halo pixel
 // ((dy + 1) * 130 + dx + 1) of plane 2 kc: 8-pixel core matrices 128 bytes apart (SBO) and
 // channel chunks one plane apart (LBO), so the nine taps are nine descriptors over one copy of
-// the input instead of a nine-fold gather.  The packed weights stay in shared memory for the
-// CTA's lifetime.  Halos cycle through kStages buffers filled kStages - 1 tiles ahead (one
+// the input instead of a nine-fold gather.  The packed weights arrive in one bulk copy issued
+// with the first halos and stay in shared memory for the CTA's lifetime; the bias sits in
+// shared memory too.  Halos cycle through kStages buffers filled kStages - 1 tiles ahead (one
 // mbarrier each, completed by the copies' transaction bytes), and the accumulator alternates
 // between two TMEM column ranges, so the MMAs of tile k run while the four warps drain tile
 // k - 1 through tcgen05.ld, and the copies of tiles k + 1 .. k + kStages - 1 are in flight.
@@ -148,6 +153,14 @@ __device__ __forceinline__ void tma_load4(uint32_t dst, const CUtensorMap* map, 
       : "memory");
 }
 
+// one thread: a contiguous global -> shared copy of `bytes` (both ends 16-byte aligned, bytes
+// a multiple of 16), completing on `bar`
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
 // one thread: the CIN / 8 plane copies of a tile's halo, completing on `bar`
 template <int C1, int C2>
 __device__ __forceinline__ void issue_halo(const ConvMaps& m, const ConvArgs& a, int64_t tile, int tiles_x,
@@ -167,8 +180,8 @@ __device__ __forceinline__ void issue_halo(const ConvMaps& m, const ConvArgs& a,
 }
 
 template <int COUT, int EPI>
-__device__ __forceinline__ void conv_epilogue(const ConvArgs& a, uint32_t tacc, int64_t tile, int tiles_x, int tid,
-                                              int warp) {
+__device__ __forceinline__ void conv_epilogue(const ConvArgs& a, const float* sbias, uint32_t tacc, int64_t tile,
+                                              int tiles_x, int tid, int warp) {
   float acc[COUT];
 #pragma unroll
   for (int c = 0; c < COUT; c += 16) tmem_ld16(tacc + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, acc + c);
@@ -178,7 +191,7 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, uint32_t tacc, 
   const int64_t p = row * a.W + x;
 #pragma unroll
   for (int c = 0; c < COUT; ++c) {
-    float v = acc[c] + (a.bias ? a.bias[c] : 0.0f);
+    float v = acc[c] + sbias[c];
     if (EPI == 1) v = fmaxf(v, 0.0f);
     acc[c] = v;
   }
@@ -195,19 +208,59 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, uint32_t tacc, 
   }
 }
 
-template <int C1, int C2, int COUT, int EPI>
+// Halo loaders.  kLoadTma (the default): one tensor copy per 8-channel plane by thread 0,
+// completing on the buffer's mbarrier.  kLoadAsync: the CTA's 128 threads copy the halo's 16-byte
+// pixel chunks with cp.async (consecutive lanes take consecutive chunks of the NHWC rows, so a
+// warp reads whole 64-byte pixels, 512 contiguous bytes; padding and pixels past the image edge
+// are zero-filled), one commit group per tile, made visible to the tensor cores by a proxy fence
+// and the iteration's barrier.  Measured on the U-Net's 320^2 levels the tensor copies are
+// 15-30 % faster; both fill shared memory identically.
+constexpr int kLoadAsync = 0, kLoadTma = 1;
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// all threads: the halo of `tile` into the plane layout at `halo` (one commit group follows)
+template <int C1, int C2>
+__device__ __forceinline__ void copy_halo_async(const ConvArgs& a, int64_t tile, int tiles_x, uint32_t halo, int tid) {
+  constexpr int NCH = (C1 + C2) / 8, NCH1 = C1 / 8;
+  const int64_t row = tile / tiles_x;  // b * H + y
+  const int x0 = (int)(tile - row * tiles_x) * kTile;
+  const int b = (int)(row / a.H), y = (int)(row - (int64_t)b * a.H);
+  for (int u = tid; u < NCH * kHaloPx; u += kTile) {
+    const int c = u % NCH, hp = u / NCH;
+    const int r = hp / kHaloW, px = hp - r * kHaloW;
+    const int yy = y - 1 + r, xx = x0 - 1 + px;
+    const bool in = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+    const int64_t pix = in ? ((int64_t)b * a.H + yy) * a.W + xx : 0;
+    const __nv_bfloat16* src = c < NCH1 ? a.in1 + pix * C1 + 8 * c : a.in2 + pix * C2 + 8 * (c - NCH1);
+    cp_async16(halo + (uint32_t)(c * kPlaneBytes + hp * 16), src, in ? 16u : 0u);
+  }
+}
+
+template <int C1, int C2, int COUT, int EPI, int LD>
 __global__ void __launch_bounds__(kTile) conv3x3_tc(const __grid_constant__ ConvMaps maps, ConvArgs a) {
+  agx_pdl_entry();
   constexpr int CIN = C1 + C2, K = 9 * CIN, NG = COUT / 8, NCH = CIN / 8;
   constexpr int B_BYTES = K * COUT * 2;
   constexpr int HALO_BYTES = NCH * kPlaneBytes;
   constexpr int NCOLS = tmem_cols(2 * COUT);  // two accumulators
   static_assert(CIN % 16 == 0 && COUT % 16 == 0, "channel counts must be multiples of 16");
   static_assert(B_BYTES % 1024 == 0 && HALO_BYTES % 128 == 0, "shared-memory carve-up");
+  static_assert(kStages >= 2, "the cp.async ring waits for all but kStages - 2 groups");
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* sB = smem;
   __shared__ uint32_t tmem_slot;
   __shared__ __align__(8) uint64_t full_bar[kStages];
   __shared__ __align__(8) uint64_t mma_bar[2];
+  __shared__ __align__(8) uint64_t w_bar;
+  __shared__ float sbias[COUT];
   const int tid = threadIdx.x, warp = tid >> 5;
   const int tiles_x = (a.W + kTile - 1) / kTile;
   const int64_t ntiles = (int64_t)a.B * a.H * tiles_x;
@@ -217,35 +270,64 @@ __global__ void __launch_bounds__(kTile) conv3x3_tc(const __grid_constant__ Conv
   const uint32_t halo_base = b0 + B_BYTES;
   const uint32_t fbar0 = (uint32_t)__cvta_generic_to_shared(&full_bar[0]);
   const uint32_t mbar0 = (uint32_t)__cvta_generic_to_shared(&mma_bar[0]);
+  const uint32_t wbar = (uint32_t)__cvta_generic_to_shared(&w_bar);
   if (tid == 0) {
+    if constexpr (LD == kLoadTma) {
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&maps.in1)) : "memory");
+      if constexpr (C2 > 0)
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&maps.in2)) : "memory");
 #pragma unroll
-    for (int s = 0; s < kStages; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(fbar0 + 8u * s));
+      for (int s = 0; s < kStages; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(fbar0 + 8u * s));
+    }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar0));
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar0 + 8u));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(wbar));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    // prologue: the first kStages halos of this CTA, one per buffer
-    for (int j = 0; j < kStages && j < my_tiles; ++j)
-      issue_halo<C1, C2>(maps, a, first + j * stride, tiles_x, halo_base + (uint32_t)(j * HALO_BYTES), fbar0 + 8u * j);
+    // the packed weights (already in core-matrix order) in one bulk copy, in flight together
+    // with the first kStages halos
+    if (my_tiles > 0) {
+      mbar_expect(wbar, (uint32_t)B_BYTES);
+      bulk_load(b0, a.wpk, (uint32_t)B_BYTES, wbar);
+    }
+    if constexpr (LD == kLoadTma)
+      for (int j = 0; j < kStages && j < my_tiles; ++j)
+        issue_halo<C1, C2>(maps, a, first + j * stride, tiles_x, halo_base + (uint32_t)(j * HALO_BYTES),
+                           fbar0 + 8u * j);
   }
-  // packed weights: already in core-matrix order (generic-proxy stores, fenced for the MMAs)
-  for (int i = tid; i < B_BYTES / 16; i += kTile)
-    reinterpret_cast<uint4*>(sB)[i] = reinterpret_cast<const uint4*>(a.wpk)[i];
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if constexpr (LD == kLoadAsync) {
+    // the first kStages halos, one commit group per buffer (empty groups past the last tile)
+    for (int j = 0; j < kStages; ++j) {
+      if (j < my_tiles)
+        copy_halo_async<C1, C2>(a, first + j * stride, tiles_x, halo_base + (uint32_t)(j * HALO_BYTES), tid);
+      cp_async_commit();
+    }
+  }
+  if (tid < COUT) sbias[tid] = a.bias ? a.bias[tid] : 0.0f;
   if (warp == 0) tmem_alloc<NCOLS>(&tmem_slot);
+  if constexpr (LD == kLoadAsync) {
+    // tile 0 complete and visible to the tensor cores (generic-proxy writes, then the
+    // proxy fence, then the barrier before the MMAs are issued)
+    cp_async_wait<kStages - 1>();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_slot;
   const uint32_t id = idesc_bf16(kTile, COUT);
   int ok = 1;
-  int64_t issued = kStages < my_tiles ? kStages : my_tiles;  // halos issued so far (thread 0's count)
-  int64_t consumed = 0;                                       // halos waited for by thread 0
+  int64_t issued = kStages < my_tiles ? kStages : my_tiles;  // TMA halos issued so far (thread 0's count)
+  int64_t consumed = 0;                                       // TMA halos waited for by thread 0
+  bool weights = my_tiles == 0;                               // weight copy waited for (thread 0)
   for (int64_t k = 0; k <= my_tiles && ok; ++k) {
     // (1) MMAs of tile k into accumulator k % 2 (its previous use, tile k - 2, was drained
     //     before the barrier that closed the last iteration)
     if (k < my_tiles && tid == 0) {
       const int st = (int)(k % kStages);
-      if (!mbar_wait(fbar0 + 8u * st, (uint32_t)((k / kStages) & 1))) {
+      if (!weights && mbar_wait(wbar, 0u)) weights = true;
+      bool have = weights;
+      if constexpr (LD == kLoadTma) have = have && mbar_wait(fbar0 + 8u * st, (uint32_t)((k / kStages) & 1));
+      if (!have) {
         atomicExch(a.err, 1);
         ok = 0;
       } else {
@@ -271,8 +353,8 @@ __global__ void __launch_bounds__(kTile) conv3x3_tc(const __grid_constant__ Conv
                      : "memory");
       }
     }
-    // (2) drain tile k - 1: its MMAs done also frees its halo buffer, refilled with tile k + 2
-    //     (= issued: the prologue filled every buffer)
+    // (2) drain tile k - 1: its MMAs done also frees its halo buffer, refilled with tile
+    //     k - 1 + kStages (the prologue filled every buffer)
     if (k >= 1) {
       const int64_t j = k - 1;
       const int done = mbar_wait(mbar0 + 8u * (uint32_t)(j & 1), (uint32_t)((j >> 1) & 1));
@@ -281,23 +363,42 @@ __global__ void __launch_bounds__(kTile) conv3x3_tc(const __grid_constant__ Conv
         ok = 0;
       } else {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (tid == 0 && issued < my_tiles) {
-          const int st = (int)(issued % kStages);
-          issue_halo<C1, C2>(maps, a, first + issued * stride, tiles_x, halo_base + (uint32_t)(st * HALO_BYTES),
-                             fbar0 + 8u * st);
-          ++issued;
+        if constexpr (LD == kLoadTma) {
+          if (tid == 0 && issued < my_tiles) {
+            const int st = (int)(issued % kStages);
+            issue_halo<C1, C2>(maps, a, first + issued * stride, tiles_x, halo_base + (uint32_t)(st * HALO_BYTES),
+                               fbar0 + 8u * st);
+            ++issued;
+          }
+        } else {
+          const int64_t nt = j + kStages;
+          if (nt < my_tiles)
+            copy_halo_async<C1, C2>(a, first + nt * stride, tiles_x,
+                                    halo_base + (uint32_t)((nt % kStages) * HALO_BYTES), tid);
+          cp_async_commit();
         }
-        conv_epilogue<COUT, EPI>(a, tmem + (uint32_t)((j & 1) * COUT), first + j * stride, tiles_x, tid, warp);
+        conv_epilogue<COUT, EPI>(a, sbias, tmem + (uint32_t)((j & 1) * COUT), first + j * stride, tiles_x, tid,
+                                 warp);
       }
+    }
+    if constexpr (LD == kLoadAsync) {
+      // tile k + 1 complete (all groups but the kStages - 2 newest) and visible to the MMAs
+      cp_async_wait<kStages - 2>();
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     ok = __syncthreads_and(ok);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   }
-  // copies issued but never waited for (only after an error): wait for them (bounded) before
-  // leaving; each is the latest use of its buffer, so its phase parity identifies it
-  if (tid == 0)
-    for (int64_t j = consumed; j < issued; ++j) mbar_wait(fbar0 + 8u * (uint32_t)(j % kStages), (uint32_t)((j / kStages) & 1));
+  // copies issued but never waited for (only after an error): wait for them (bounded for the
+  // tensor copies; each is the latest use of its buffer, so its phase parity identifies it)
+  if constexpr (LD == kLoadAsync) asm volatile("cp.async.wait_all;" ::: "memory");
+  if (tid == 0) {
+    if constexpr (LD == kLoadTma)
+      for (int64_t j = consumed; j < issued; ++j)
+        mbar_wait(fbar0 + 8u * (uint32_t)(j % kStages), (uint32_t)((j / kStages) & 1));
+    if (!weights) mbar_wait(wbar, 0u);
+  }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) tmem_free<NCOLS>(tmem);
@@ -495,6 +596,84 @@ __global__ void avgpool2_kernel(const __nv_bfloat16* __restrict__ in, __nv_bfloa
   }
 }
 
+// f x f block transfers between a fine NHWC image (H x W) and a coarse one (H / f x W / f),
+// eight channels (16 bytes) per thread, float sums rounded to bf16 once:
+//   block_sum:   coarse = scale * (sum over the f x f block of fine)   (pooling, adjoint of upsampling)
+//   block_bcast: fine   = scale * coarse of its block                  (upsampling, adjoint of pooling)
+__device__ __forceinline__ void bf16x8_acc(const uint4& v, float* a) {
+  const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const float2 f = __bfloat1622float2(h[u]);
+    a[2 * u] += f.x;
+    a[2 * u + 1] += f.y;
+  }
+}
+
+__device__ __forceinline__ uint4 bf16x8_pack(const float* a, float scale) {
+  uint4 v;
+  __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(&v);
+#pragma unroll
+  for (int u = 0; u < 4; ++u) h[u] = __floats2bfloat162_rn(scale * a[2 * u], scale * a[2 * u + 1]);
+  return v;
+}
+
+// F: the block size as a template constant (the f x f loads unrolled and in flight together),
+// 0 for a runtime f; C8 = 4 (32 channels) is the U-Net's hidden width
+template <int F>
+__global__ void block_sum_kernel(const uint4* __restrict__ fine, uint4* __restrict__ coarse, int B, int H, int W,
+                                 int C8, int f_rt, float scale) {
+  agx_pdl_entry();
+  const int f = F > 0 ? F : f_rt;
+  const int Ho = H / f, Wo = W / f;
+  const int64_t total = (int64_t)B * Ho * Wo * C8;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C8);
+    const int64_t pix = i / C8;
+    const int xo = (int)(pix % Wo), yo = (int)((pix / Wo) % Ho), b = (int)(pix / ((int64_t)Wo * Ho));
+    float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if constexpr (F > 0) {
+      uint4 v[F * F];
+#pragma unroll
+      for (int dy = 0; dy < F; ++dy) {
+        const uint4* row = fine + (((int64_t)b * H + (int64_t)F * yo + dy) * W + (int64_t)F * xo) * C8 + c;
+#pragma unroll
+        for (int dx = 0; dx < F; ++dx) v[dy * F + dx] = __ldg(row + (int64_t)dx * C8);
+      }
+#pragma unroll
+      for (int u = 0; u < F * F; ++u) bf16x8_acc(v[u], a);
+    } else {
+      for (int dy = 0; dy < f; ++dy) {
+        const uint4* row = fine + (((int64_t)b * H + (int64_t)f * yo + dy) * W + (int64_t)f * xo) * C8 + c;
+        for (int dx = 0; dx < f; ++dx) bf16x8_acc(__ldg(row + (int64_t)dx * C8), a);
+      }
+    }
+    coarse[i] = bf16x8_pack(a, scale);
+  }
+}
+
+template <int F>
+__global__ void block_bcast_kernel(const uint4* __restrict__ coarse, uint4* __restrict__ fine, int B, int H, int W,
+                                   int C8, int f_rt, float scale) {
+  agx_pdl_entry();
+  const int f = F > 0 ? F : f_rt;
+  const int Ho = H / f, Wo = W / f;
+  const int64_t total = (int64_t)B * H * W * C8;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C8);
+    const int64_t pix = i / C8;
+    const int x = (int)(pix % W), y = (int)((pix / W) % H), b = (int)(pix / ((int64_t)W * H));
+    const uint4 v = __ldg(coarse + (((int64_t)b * Ho + y / f) * Wo + x / f) * C8 + c);
+    if (scale == 1.0f) {
+      fine[i] = v;
+    } else {
+      float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      bf16x8_acc(v, a);
+      fine[i] = bf16x8_pack(a, scale);
+    }
+  }
+}
+
 // nearest 2x upsampling and its adjoint (sum over the 2x2 block)
 __global__ void upsample2_kernel(const __nv_bfloat16* __restrict__ in, __nv_bfloat16* __restrict__ out, int B, int H,
                                  int W, int C, int backward) {
@@ -552,6 +731,7 @@ __global__ void bias_grad_kernel(const __nv_bfloat16* __restrict__ g, int64_t P,
 __global__ void grid_from_field_kernel(const float* __restrict__ r, int nd, const float* __restrict__ aux, int naux,
                                        const float* __restrict__ scale, int Hn, int Wn, int Hp, int Wp,
                                        __nv_bfloat16* __restrict__ img) {
+  agx_pdl_entry();
   const int64_t total = (int64_t)Hp * Wp;
   const float s = scale ? scale[0] : 1.0f;
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < total; p += (int64_t)gridDim.x * blockDim.x) {
@@ -574,6 +754,7 @@ __global__ void grid_from_field_kernel(const float* __restrict__ r, int nd, cons
 // channels 0 .. nd-1 of an NHWC image with C channels -> node field z[node nd + c]
 __global__ void field_from_grid_kernel(const __nv_bfloat16* __restrict__ img, int C, int nd, int Hn, int Wn, int Wp,
                                        float* __restrict__ z) {
+  agx_pdl_entry();
   const int64_t total = (int64_t)Hn * Wn * nd;
   for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d < total; d += (int64_t)gridDim.x * blockDim.x) {
     const int64_t node = d / nd;
@@ -584,18 +765,51 @@ __global__ void field_from_grid_kernel(const __nv_bfloat16* __restrict__ img, in
 }
 
 // 1 / rms of a float vector (single block)
-__global__ void inv_rms_kernel(const float* __restrict__ r, int64_t n, float* __restrict__ out) {
+// 1 / rms of r over a cluster of kRmsCluster CTAs: float4 loads (when r is 16-byte aligned),
+// float partial sums per thread, float64 within and across the CTAs, the CTA totals read by
+// rank 0 through distributed shared memory (no global workspace, no atomics)
+constexpr int kRmsCluster = 8;
+__global__ void __cluster_dims__(kRmsCluster, 1, 1) __launch_bounds__(1024)
+    inv_rms_kernel(const float* __restrict__ r, int64_t n, float* __restrict__ out) {
+  cg::cluster_group cluster = cg::this_cluster();
   __shared__ double sh[32];
-  double s = 0.0;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += (double)r[i] * (double)r[i];
-  for (int o = 16; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __shared__ double total;
+  const int rank = (int)cluster.block_rank();
+  const int64_t t0 = (int64_t)rank * blockDim.x + threadIdx.x, nt = (int64_t)kRmsCluster * blockDim.x;
+  float s0 = 0.f, s1 = 0.f;
+  int64_t tail = 0;
+  if ((reinterpret_cast<uintptr_t>(r) & 15u) == 0) {
+    const float4* r4 = reinterpret_cast<const float4*>(r);
+    const int64_t n4 = n >> 2;
+    int64_t i = t0;
+    for (; i + 3 * nt < n4; i += 4 * nt) {  // four independent 16-byte loads in flight per thread
+      const float4 a = __ldg(r4 + i), b = __ldg(r4 + i + nt), c = __ldg(r4 + i + 2 * nt), d = __ldg(r4 + i + 3 * nt);
+      s0 += (a.x * a.x + a.y * a.y) + (a.z * a.z + a.w * a.w) + (b.x * b.x + b.y * b.y) + (b.z * b.z + b.w * b.w);
+      s1 += (c.x * c.x + c.y * c.y) + (c.z * c.z + c.w * c.w) + (d.x * d.x + d.y * d.y) + (d.z * d.z + d.w * d.w);
+    }
+    for (; i < n4; i += nt) {
+      const float4 a = __ldg(r4 + i);
+      s0 += (a.x * a.x + a.y * a.y) + (a.z * a.z + a.w * a.w);
+    }
+    tail = n4 << 2;
+  }
+  for (int64_t i = tail + t0; i < n; i += nt) s1 += r[i] * r[i];
+  double d = (double)s0 + (double)s1;
+  for (int o = 16; o >= 1; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = d;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {
+    d = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+    for (int o = 16; o >= 1; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if (threadIdx.x == 0) total = d;
+  }
+  cluster.sync();
+  if (rank == 0 && threadIdx.x == 0) {
     double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+    for (int q = 0; q < kRmsCluster; ++q) t += *cluster.map_shared_rank(&total, q);
     out[0] = t > 0.0 ? (float)(1.0 / sqrt(t / (double)n)) : 1.0f;
   }
+  cluster.sync();  // the other CTAs' shared memory stays valid until rank 0 has read it
 }
 
 // Bilinear transfer between a structured coarse node grid Hc x Wc and the fine grid
@@ -651,6 +865,150 @@ __global__ void restrict_kernel(const float* __restrict__ fine, const unsigned c
   }
 }
 
+// ---- the coarse-grid network's transfers, fused ------------------------------------------
+// restrict_sq_kernel: coarse = P^T fine as restrict_kernel, with the block size F of the
+// transfer a template constant (the (2F - 1)^2 taps unrolled, so a thread's loads are all in
+// flight together; F = 0: runtime f), 32-bit index arithmetic, and one float64 partial sum of
+// squares of the block's outputs in partials[blockIdx.x].  image_from_coarse_kernel: every
+// block first adds the np partials itself (fixed order), so 1 / rms needs no launch of its own,
+// then writes (coarse / rms, aux) into the image as grid_from_field_kernel does.
+// prolong_image_kernel: fine = P applied to channels 0 .. nd-1 of the network's output image
+// (the coarse field is never written out), zero at fixed DOFs.
+constexpr int kRestrictBlocks = 1024;  // largest grid of restrict_sq_kernel (partials it writes)
+
+template <int F>
+__global__ void __launch_bounds__(256)
+restrict_sq_kernel(const float* __restrict__ fine, const unsigned char* __restrict__ fixed, int nd, int Hc, int Wc,
+                   int f_rt, float* __restrict__ out, double* __restrict__ partials) {
+  agx_pdl_entry();
+  const int f = F > 0 ? F : f_rt;
+  const int Hf = (Hc - 1) * f + 1, Wf = (Wc - 1) * f + 1;
+  const int total = Hc * Wc * nd;
+  const float inv = 1.0f / (float)f;
+  float sq = 0.0f;
+  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < total; d += gridDim.x * blockDim.x) {
+    const int q = d / nd, k = d - q * nd;
+    const int I = q / Wc, J = q - I * Wc;
+    const int ci = I * f, cj = J * f;
+    float acc = 0.0f;
+    if (!(fixed && fixed[((int64_t)ci * Wf + cj) * nd + k])) {
+      if constexpr (F > 0) {
+#pragma unroll
+        for (int di = -(F - 1); di <= F - 1; ++di) {
+          const int i = ci + di;
+          const float wi = (i >= 0 && i < Hf) ? 1.0f - (float)(di < 0 ? -di : di) * inv : 0.0f;
+          const int ii = i < 0 ? 0 : (i >= Hf ? Hf - 1 : i);
+          float row = 0.0f;
+#pragma unroll
+          for (int dj = -(F - 1); dj <= F - 1; ++dj) {
+            const int j = cj + dj;
+            const float wj = (j >= 0 && j < Wf) ? 1.0f - (float)(dj < 0 ? -dj : dj) * inv : 0.0f;
+            const int jj = j < 0 ? 0 : (j >= Wf ? Wf - 1 : j);
+            row += wj * __ldg(fine + ((int64_t)ii * Wf + jj) * nd + k);
+          }
+          acc += wi * row;
+        }
+      } else {
+        for (int di = -(f - 1); di <= f - 1; ++di) {
+          const int i = ci + di;
+          if (i < 0 || i >= Hf) continue;
+          const float wi = 1.0f - (float)abs(di) * inv;
+          float row = 0.0f;
+          for (int dj = -(f - 1); dj <= f - 1; ++dj) {
+            const int j = cj + dj;
+            if (j < 0 || j >= Wf) continue;
+            row += (1.0f - (float)abs(dj) * inv) * fine[((int64_t)i * Wf + j) * nd + k];
+          }
+          acc += wi * row;
+        }
+      }
+    }
+    out[d] = acc;
+    sq += acc * acc;
+  }
+  __shared__ double sh[8];
+  double v = (double)sq;
+  for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+    partials[blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+image_from_coarse_kernel(const float* __restrict__ r, int nd, const float* __restrict__ aux, int naux,
+                         const double* __restrict__ partials, int np, int64_t n, float* __restrict__ scale, int Hn,
+                         int Wn, int Hp, int Wp, __nv_bfloat16* __restrict__ img) {
+  agx_pdl_entry();
+  __shared__ double sh[8];
+  __shared__ float s_sh;
+  double v = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) v += partials[i];
+  for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+    const float sc = t > 0.0 ? (float)(1.0 / sqrt(t / (double)n)) : 1.0f;
+    s_sh = sc;
+    if (blockIdx.x == 0) scale[0] = sc;
+  }
+  __syncthreads();
+  const float s = s_sh;
+  const int total = Hp * Wp;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+    const int i = p / Wp, j = p - i * Wp;
+    __align__(16) __nv_bfloat16 h[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) h[c] = __float2bfloat16(0.0f);
+    if (i < Hn && j < Wn) {
+      const int64_t node = (int64_t)i * Wn + j;
+      for (int c = 0; c < nd; ++c) h[c] = __float2bfloat16(s * r[node * nd + c]);
+      if (aux)
+        for (int a = 0; a < naux; ++a) h[nd + a] = __float2bfloat16(aux[node * naux + a]);
+    }
+    uint4* dst = reinterpret_cast<uint4*>(img + (int64_t)p * 16);
+    dst[0] = reinterpret_cast<uint4*>(h)[0];
+    dst[1] = reinterpret_cast<uint4*>(h)[1];
+  }
+}
+
+// one fine row per blockIdx.y; F as in restrict_sq_kernel
+template <int F>
+__global__ void __launch_bounds__(256)
+prolong_image_kernel(const __nv_bfloat16* __restrict__ img, int C, int nd, int Hc, int Wc, int Wp, int f_rt,
+                     const unsigned char* __restrict__ fixed, float* __restrict__ out) {
+  agx_pdl_entry();
+  const int f = F > 0 ? F : f_rt;
+  const int Wf = (Wc - 1) * f + 1;
+  const int i = blockIdx.y;
+  const int I = i / f;
+  const float inv = 1.0f / (float)f;
+  const float ti = (float)(i - I * f) * inv;
+  const int I1 = I + 1 < Hc ? I + 1 : I;
+  const int row_len = Wf * nd;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < row_len; t += gridDim.x * blockDim.x) {
+    const int j = t / nd, k = t - j * nd;
+    const int64_t d = (int64_t)i * row_len + t;
+    float v = 0.0f;
+    if (!(fixed && fixed[d])) {
+      const int J = j / f;
+      const float tj = (float)(j - J * f) * inv;
+      const int J1 = J + 1 < Wc ? J + 1 : J;
+      const float v00 = __bfloat162float(img[((int64_t)I * Wp + J) * C + k]);
+      const float v01 = __bfloat162float(img[((int64_t)I * Wp + J1) * C + k]);
+      const float v10 = __bfloat162float(img[((int64_t)I1 * Wp + J) * C + k]);
+      const float v11 = __bfloat162float(img[((int64_t)I1 * Wp + J1) * C + k]);
+      v = (1.0f - ti) * ((1.0f - tj) * v00 + tj * v01) + ti * ((1.0f - tj) * v10 + tj * v11);
+    }
+    out[d] = v;
+  }
+}
+
 int sm_count() {
   static int n = 0;
   if (!n) {
@@ -688,15 +1046,17 @@ int make_halo_map(CUtensorMap* m, const void* base, int C, int B, int H, int W) 
   return r == CUDA_SUCCESS ? AGX_OK : AGX_ERR_ARG;
 }
 
-template <int C1, int C2, int COUT, int EPI>
-int launch_conv(const ConvArgs& a, cudaStream_t s) {
+int g_halo_loader = kLoadTma;  // agx_nn_set_halo_loader
+
+template <int C1, int C2, int COUT, int EPI, int LD>
+int launch_conv_as(const ConvArgs& a, cudaStream_t s) {
   constexpr int CIN = C1 + C2;
   constexpr int smem = 9 * CIN * COUT * 2 + kStages * (CIN / 8) * kPlaneBytes;
   static int per_sm = 0;
   if (!per_sm) {
-    if (cudaFuncSetAttribute(conv3x3_tc<C1, C2, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+    if (cudaFuncSetAttribute(conv3x3_tc<C1, C2, COUT, EPI, LD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
             cudaSuccess ||
-        cudaFuncSetAttribute(conv3x3_tc<C1, C2, COUT, EPI>, cudaFuncAttributePreferredSharedMemoryCarveout,
+        cudaFuncSetAttribute(conv3x3_tc<C1, C2, COUT, EPI, LD>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              cudaSharedmemCarveoutMaxShared) != cudaSuccess)
       return AGX_ERR_CUDA;
     // resident CTAs per SM from the shared-memory budget (at most 8: TMEM holds 512 columns)
@@ -708,18 +1068,28 @@ int launch_conv(const ConvArgs& a, cudaStream_t s) {
     const int tmem_cap = 512 / tmem_cols(2 * COUT);
     per_sm = per_sm < 1 ? 1 : (per_sm > tmem_cap ? tmem_cap : per_sm);
   }
-  ConvMaps maps;
-  if (int rc = make_halo_map(&maps.in1, a.in1, C1, a.B, a.H, a.W)) return rc;
-  if (C2 > 0) {
-    if (int rc = make_halo_map(&maps.in2, a.in2, C2, a.B, a.H, a.W)) return rc;
-  } else {
-    maps.in2 = maps.in1;
+  ConvMaps maps{};
+  if constexpr (LD == kLoadTma) {
+    if (int rc = make_halo_map(&maps.in1, a.in1, C1, a.B, a.H, a.W)) return rc;
+    if (C2 > 0) {
+      if (int rc = make_halo_map(&maps.in2, a.in2, C2, a.B, a.H, a.W)) return rc;
+    } else {
+      maps.in2 = maps.in1;
+    }
+  } else if ((reinterpret_cast<uintptr_t>(a.in1) | reinterpret_cast<uintptr_t>(a.in2)) & 15u) {
+    return AGX_ERR_ARG;  // 16-byte pixel chunks
   }
   const int64_t tiles = (int64_t)a.B * a.H * ((a.W + kTile - 1) / kTile);
   const int64_t cap = (int64_t)per_sm * sm_count();
   const int grid = (int)(tiles < cap ? tiles : cap);
-  conv3x3_tc<C1, C2, COUT, EPI><<<grid, kTile, smem, s>>>(maps, a);
+  agx_launch_pdl(conv3x3_tc<C1, C2, COUT, EPI, LD>, grid, kTile, smem, s, maps, a);
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+template <int C1, int C2, int COUT, int EPI>
+int launch_conv(const ConvArgs& a, cudaStream_t s) {
+  return g_halo_loader == kLoadTma ? launch_conv_as<C1, C2, COUT, EPI, kLoadTma>(a, s)
+                                   : launch_conv_as<C1, C2, COUT, EPI, kLoadAsync>(a, s);
 }
 
 template <int C1, int C2, int COUT>
@@ -746,6 +1116,26 @@ int grid1(int64_t n) {
   return (int)(g < 152 * 8 ? (g < 1 ? 1 : g) : 152 * 8);
 }
 
+// fine (H x W) -> coarse block sums times `scale`, and coarse -> fine broadcasts times `scale`
+void launch_block_sum(const void* fine, void* coarse, int B, int H, int W, int C, int f, float scale, cudaStream_t s) {
+  const int g = grid1((int64_t)B * (H / f) * (W / f) * (C / 8));
+  const uint4* in = (const uint4*)fine;
+  uint4* out = (uint4*)coarse;
+  if (f == 2) agx_launch_pdl(block_sum_kernel<2>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale);
+  else if (f == 4) agx_launch_pdl(block_sum_kernel<4>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale);
+  else agx_launch_pdl(block_sum_kernel<0>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale);
+}
+
+void launch_block_bcast(const void* coarse, void* fine, int B, int H, int W, int C, int f, float scale,
+                        cudaStream_t s) {
+  const int g = grid1((int64_t)B * H * W * (C / 8));
+  const uint4* in = (const uint4*)coarse;
+  uint4* out = (uint4*)fine;
+  if (f == 2) agx_launch_pdl(block_bcast_kernel<2>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale);
+  else if (f == 4) agx_launch_pdl(block_bcast_kernel<4>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale);
+  else agx_launch_pdl(block_bcast_kernel<0>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale);
+}
+
 }  // namespace
 
 extern "C" {
@@ -757,6 +1147,7 @@ int agx_nn_conv3x3(const void* in1, const void* in2, int c1, int c2, const void*
   cudaStream_t s = (cudaStream_t)stream;
   if (!in1 || !wpk || !out1 || !err || B <= 0 || H <= 0 || W <= 0) return AGX_ERR_ARG;
   if (split <= 0 || split > cout || split % 8 || (split < cout && !out2)) return AGX_ERR_ARG;
+  if (reinterpret_cast<uintptr_t>(wpk) & 15u) return AGX_ERR_ARG;  // one bulk copy into shared memory
 #define AGX_CONV(C1_, C2_, CO_, R_)                                                         \
   if (c1 == C1_ && c2 == C2_ && cout == CO_ && relu == R_) return launch_conv<C1_, C2_, CO_, R_>(a, s);
   AGX_CONV(16, 0, 32, 1)
@@ -770,6 +1161,12 @@ int agx_nn_conv3x3(const void* in1, const void* in2, int c1, int c2, const void*
   AGX_CONV(16, 0, 32, 0)
 #undef AGX_CONV
   return AGX_ERR_UNSUPPORTED;
+}
+
+int agx_nn_set_halo_loader(int loader) {
+  if (loader != kLoadAsync && loader != kLoadTma) return AGX_ERR_ARG;
+  g_halo_loader = loader;
+  return AGX_OK;
 }
 
 int agx_nn_wgrad3x3(const void* in1, const void* in2, int c1, int c2, const void* dout, int cout, float* dw_rows,
@@ -807,6 +1204,29 @@ int agx_nn_pool2(const void* in, void* out, int B, int H, int W, int C, int back
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
 }
 
+int agx_nn_pool(const void* in, void* out, int B, int H, int W, int C, int f, int backward, void* stream) {
+  if (!in || !out || B <= 0 || f < 1 || f > 64 || H % f || W % f || C % 8 ||
+      ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u))
+    return AGX_ERR_ARG;
+  const float inv = 1.0f / (float)(f * f);
+  if (!backward)
+    launch_block_sum(in, out, B, H, W, C, f, inv, (cudaStream_t)stream);
+  else
+    launch_block_bcast(in, out, B, H, W, C, f, inv, (cudaStream_t)stream);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+int agx_nn_upsample(const void* in, void* out, int B, int H, int W, int C, int f, int backward, void* stream) {
+  if (!in || !out || B <= 0 || f < 1 || f > 64 || C % 8 ||
+      ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u))
+    return AGX_ERR_ARG;
+  if (!backward)
+    launch_block_bcast(in, out, B, H * f, W * f, C, f, 1.0f, (cudaStream_t)stream);
+  else
+    launch_block_sum(in, out, B, H * f, W * f, C, f, 1.0f, (cudaStream_t)stream);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
 int agx_nn_upsample2(const void* in, void* out, int B, int H, int W, int C, int backward, void* stream) {
   upsample2_kernel<<<grid1((int64_t)B * H * W * C), 256, 0, (cudaStream_t)stream>>>(
       (const __nv_bfloat16*)in, (__nv_bfloat16*)out, B, H, W, C, backward);
@@ -839,10 +1259,51 @@ int agx_nn_grid_from_field(const float* r, int nd, const float* aux, int naux, i
       (normalize && !scale))
     return AGX_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
-  if (normalize) inv_rms_kernel<<<1, 1024, 0, s>>>(r, (int64_t)Hn * Wn * nd, scale);
-  grid_from_field_kernel<<<grid1((int64_t)Hp * Wp), 256, 0, s>>>(r, nd, naux > 0 ? aux : nullptr, naux,
+  if (normalize) inv_rms_kernel<<<kRmsCluster, 1024, 0, s>>>(r, (int64_t)Hn * Wn * nd, scale);
+  agx_launch_pdl(grid_from_field_kernel, grid1((int64_t)Hp * Wp), 256, 0, s, r, nd, naux > 0 ? aux : nullptr, naux,
                                                                  normalize ? scale : nullptr, Hn, Wn, Hp, Wp,
                                                                  (__nv_bfloat16*)img);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+int agx_nn_restrict_image_work(void) { return kRestrictBlocks; }
+
+int agx_nn_restrict_image(const float* fine, const unsigned char* fixed, int nd, const float* aux, int naux, int Hc,
+                          int Wc, int f, int Hp, int Wp, float* coarse, double* work, float* scale, void* img,
+                          void* stream) {
+  if (!fine || !coarse || !work || !scale || !img || nd < 1 || nd > 3 || naux < 0 || nd + naux > 16 ||
+      (naux > 0 && !aux) || Hc < 2 || Wc < 2 || f < 1 || f > 64 || Hc > Hp || Wc > Wp ||
+      (int64_t)Hc * Wc * nd >= (1LL << 31) || (int64_t)Hp * Wp >= (1LL << 31))
+    return AGX_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t total = (int64_t)Hc * Wc * nd;
+  const int nb = (int)std::min<int64_t>(kRestrictBlocks, (total + 255) / 256);
+  switch (f) {
+    case 2: agx_launch_pdl(restrict_sq_kernel<2>, nb, 256, 0, s, fine, fixed, nd, Hc, Wc, f, coarse, work); break;
+    case 4: agx_launch_pdl(restrict_sq_kernel<4>, nb, 256, 0, s, fine, fixed, nd, Hc, Wc, f, coarse, work); break;
+    case 8: agx_launch_pdl(restrict_sq_kernel<8>, nb, 256, 0, s, fine, fixed, nd, Hc, Wc, f, coarse, work); break;
+    default: agx_launch_pdl(restrict_sq_kernel<0>, nb, 256, 0, s, fine, fixed, nd, Hc, Wc, f, coarse, work); break;
+  }
+  agx_launch_pdl(image_from_coarse_kernel, grid1((int64_t)Hp * Wp), 256, 0, s, coarse, nd, naux > 0 ? aux : nullptr, naux, work,
+                                                                    nb, total, scale, Hc, Wc, Hp, Wp,
+                                                                    (__nv_bfloat16*)img);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+int agx_nn_prolong_image(const void* img, int C, int nd, int Hc, int Wc, int Wp, int f, const unsigned char* fixed,
+                         float* fine, void* stream) {
+  if (!img || !fine || nd < 1 || nd > C || Hc < 2 || Wc < 2 || Wc > Wp || f < 1 || f > 64) return AGX_ERR_ARG;
+  const int64_t Hf = (int64_t)(Hc - 1) * f + 1, row = ((int64_t)(Wc - 1) * f + 1) * nd;
+  if (Hf > 65535 || Hf * row >= (1LL << 31)) return AGX_ERR_ARG;
+  const dim3 grid((unsigned)((row + 255) / 256), (unsigned)Hf);
+  cudaStream_t s = (cudaStream_t)stream;
+  const __nv_bfloat16* im = (const __nv_bfloat16*)img;
+  switch (f) {
+    case 2: agx_launch_pdl(prolong_image_kernel<2>, grid, 256, 0, s, im, C, nd, Hc, Wc, Wp, f, fixed, fine); break;
+    case 4: agx_launch_pdl(prolong_image_kernel<4>, grid, 256, 0, s, im, C, nd, Hc, Wc, Wp, f, fixed, fine); break;
+    case 8: agx_launch_pdl(prolong_image_kernel<8>, grid, 256, 0, s, im, C, nd, Hc, Wc, Wp, f, fixed, fine); break;
+    default: agx_launch_pdl(prolong_image_kernel<0>, grid, 256, 0, s, im, C, nd, Hc, Wc, Wp, f, fixed, fine); break;
+  }
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
 }
 
@@ -875,7 +1336,7 @@ int agx_nn_vector_from_grid(const void* img, int C, int Hn, int Wn, int Wp, floa
 
 int agx_nn_field_from_grid(const void* img, int C, int nd, int Hn, int Wn, int Wp, float* z, void* stream) {
   if (!img || !z || nd < 1 || nd > C || Wn > Wp) return AGX_ERR_ARG;
-  field_from_grid_kernel<<<grid1((int64_t)Hn * Wn * nd), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)img, C,
+  agx_launch_pdl(field_from_grid_kernel, grid1((int64_t)Hn * Wn * nd), 256, 0, (cudaStream_t)stream, (const __nv_bfloat16*)img, C,
                                                                                         nd, Hn, Wn, Wp, z);
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
 }

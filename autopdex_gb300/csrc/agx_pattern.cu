@@ -152,7 +152,12 @@ int agx_build_pattern(agx_context* ctx) {
         }
     });
   }
-  for (auto& s : ctx->sets) detect_structured_grid(ctx, s, rowptr);
+  ctx->pattern_grid_ny = 0;
+  for (auto& s : ctx->sets) {
+    detect_structured_grid(ctx, s, rowptr);
+    // the row lengths matched the grid's stencil: every other set's entries lie inside it
+    if (s.grid_nx > 0 && ctx->ndof <= 2) ctx->pattern_grid_ny = s.grid_ny;
+  }
   // upload
   const int bs = ctx->ndof * ctx->ndof;
   AGX_CUDA(ctx, cudaMalloc(&ctx->d_rowptr, sizeof(int32_t) * (nn + 1)));

@@ -137,25 +137,18 @@ class UNet:
         return out
 
     def _pool(self, x, B, H, W, c, key):
-        """POOL x POOL average pooling as repeated 2 x 2 pooling."""
-        f = 1
-        while f < POOL:
-            out = self._act(B, H // (2 * f), W // (2 * f), c, f"{key}.{f}")
-            self._ok("agx_nn_pool2", self.lib.agx_nn_pool2(_p(x), _p(out), B, H // f, W // f, c, 0, self._stream()))
-            self.launches += 1
-            x, f = out, 2 * f
-        return x
+        """POOL x POOL average pooling in one launch."""
+        out = self._act(B, H // POOL, W // POOL, c, f"{key}.{POOL}")
+        self._ok("agx_nn_pool", self.lib.agx_nn_pool(_p(x), _p(out), B, H, W, c, POOL, 0, self._stream()))
+        self.launches += 1
+        return out
 
     def _up(self, x, B, H, W, c, key):
-        """Nearest POOL x upsampling of an H x W image as repeated 2 x upsampling."""
-        f = 1
-        while f < POOL:
-            out = self._act(B, 2 * f * H, 2 * f * W, c, f"{key}.{f}")
-            self._ok("agx_nn_upsample2", self.lib.agx_nn_upsample2(_p(x), _p(out), B, f * H, f * W, c, 0,
-                                                                   self._stream()))
-            self.launches += 1
-            x, f = out, 2 * f
-        return x
+        """Nearest POOL x upsampling of an H x W image in one launch."""
+        out = self._act(B, POOL * H, POOL * W, c, f"{key}.{POOL}")
+        self._ok("agx_nn_upsample", self.lib.agx_nn_upsample(_p(x), _p(out), B, H, W, c, POOL, 0, self._stream()))
+        self.launches += 1
+        return out
 
     # ---- forward / backward -------------------------------------------------------------
     def forward(self, x, keep=False, stream=None, arena=None):
@@ -227,21 +220,15 @@ class UNet:
         self.gb = {k: torch.zeros_like(v) for k, v in self.b.items()}
 
         def upb(g, h, w):  # adjoint of upsampling to (h, w) -> coarse (h / POOL, w / POOL)
-            f = 2
-            while f <= POOL:
-                out = self._act(B, h // f, w // f, C_HID)
-                self._ok("agx_nn_upsample2", self.lib.agx_nn_upsample2(_p(g), _p(out), B, h // f, w // f, C_HID, 1,
-                                                                       s))
-                g, f = out, 2 * f
-            return g
+            out = self._act(B, h // POOL, w // POOL, C_HID)
+            self._ok("agx_nn_upsample", self.lib.agx_nn_upsample(_p(g), _p(out), B, h // POOL, w // POOL, C_HID,
+                                                                 POOL, 1, s))
+            return out
 
         def poolb(g, h, w):  # adjoint of pooling from (h, w): coarse (h / POOL, w / POOL) -> (h, w)
-            f = POOL // 2
-            while f >= 1:
-                out = self._act(B, h // f, w // f, C_HID)
-                self._ok("agx_nn_pool2", self.lib.agx_nn_pool2(_p(g), _p(out), B, h // f, w // f, C_HID, 1, s))
-                g, f = out, f // 2
-            return g
+            out = self._act(B, h, w, C_HID)
+            self._ok("agx_nn_pool", self.lib.agx_nn_pool(_p(g), _p(out), B, h, w, C_HID, POOL, 1, s))
+            return out
 
         def add(x, y):
             self._ok("agx_nn_add", self.lib.agx_nn_add(_p(x), _p(y), x.numel(), s))
@@ -708,6 +695,7 @@ class GridPreconditioner:
         self.scale = torch.empty(1, dtype=torch.float32, device=dev)
         self.rc = torch.zeros(self.Hn * self.Wn * nd, dtype=torch.float32, device=dev)
         self.yc = torch.zeros(self.Hn * self.Wn * nd, dtype=torch.float32, device=dev)
+        self.work = torch.zeros(net.lib.agx_nn_restrict_image_work(), dtype=torch.float64, device=dev)
         self.fixed = None if fixed is None else torch.as_tensor(np.asarray(fixed, dtype=np.uint8), device=dev)
         self.arena = {}
         self.applications = 0
@@ -720,24 +708,25 @@ class GridPreconditioner:
         f = self.factor
         nd = self.nd
         if f > 1:
-            fixed = _p(self.fixed)
-            rc = lib.agx_nn_restrict_field(C.c_void_p(r_ptr), fixed, nd, self.Hn, self.Wn, f, _p(self.rc), st)
+            # restriction, 1 / rms and the input image in two launches; the output prolonged
+            # straight from the network's image, zero at the prescribed DOFs
+            rc = lib.agx_nn_restrict_image(C.c_void_p(r_ptr), _p(self.fixed), nd, _p(self.aux), self.naux, self.Hn,
+                                           self.Wn, f, self.Hp, self.Wp, _p(self.rc), _p(self.work), _p(self.scale),
+                                           _p(self.img), st)
             if rc != 0:
                 return rc
-            src = self.rc.data_ptr()
+            out = self.net.forward(self.img, stream=st, arena=self.arena)
+            rc = lib.agx_nn_prolong_image(_p(out), C_OUT, nd, self.Hn, self.Wn, self.Wp, f, _p(self.fixed),
+                                          C.c_void_p(z_ptr), st)
+            self.net.launches += 3
         else:
-            src = r_ptr
-        rc = lib.agx_nn_grid_from_field(C.c_void_p(src), nd, _p(self.aux), self.naux, self.Hn, self.Wn, self.Hp,
-                                        self.Wp, 1, _p(self.scale), _p(self.img), st)
-        if rc != 0:
-            return rc
-        out = self.net.forward(self.img, stream=st, arena=self.arena)
-        dst = self.yc.data_ptr() if f > 1 else z_ptr
-        rc = lib.agx_nn_field_from_grid(_p(out), C_OUT, nd, self.Hn, self.Wn, self.Wp, C.c_void_p(dst), st)
-        if rc == 0 and f > 1:
-            rc = lib.agx_nn_prolong_field(_p(self.yc), nd, self.Hn, self.Wn, f, C.c_void_p(z_ptr), st)
-        # grid transfers: (restrict,) 1/rms, image, field (, prolong)
-        self.net.launches += 3 + (2 if f > 1 else 0)
+            rc = lib.agx_nn_grid_from_field(C.c_void_p(r_ptr), nd, _p(self.aux), self.naux, self.Hn, self.Wn,
+                                            self.Hp, self.Wp, 1, _p(self.scale), _p(self.img), st)
+            if rc != 0:
+                return rc
+            out = self.net.forward(self.img, stream=st, arena=self.arena)
+            rc = lib.agx_nn_field_from_grid(_p(out), C_OUT, nd, self.Hn, self.Wn, self.Wp, C.c_void_p(z_ptr), st)
+            self.net.launches += 3  # 1 / rms, image, field
         self.applications += 1
         return rc
 

@@ -23,6 +23,11 @@ extern "C" {
 int agx_nn_conv3x3(const void* in1, const void* in2, int c1, int c2, const void* wpk, const float* bias,
                    void* out1, void* out2, int split, int cout, int relu, int B, int H, int W, int* err,
                    void* stream);
+/* How agx_nn_conv3x3 stages its input halos in shared memory: 0 cp.async by all threads of the
+   CTA, 16-byte pixel chunks with zero fill at the image edge (in1 and in2 then 16-byte
+   aligned); 1 (the default, the faster one measured) one tensor-memory-access copy per
+   8-channel plane.  Both give identical results.  Process-wide; affects later launches only. */
+int agx_nn_set_halo_loader(int loader);
 /* dw_rows[(tap * (c1 + c2) + ci) * cout + co] += sum over pixels of in(p + tap)[ci] * dout(p)[co] */
 int agx_nn_wgrad3x3(const void* in1, const void* in2, int c1, int c2, const void* dout, int cout, float* dw_rows,
                     int B, int H, int W, int* err, void* stream);
@@ -34,6 +39,13 @@ int agx_nn_unpack_wgrad(const float* dw_rows, int cout, int cin, float* dw, void
 int agx_nn_pool2(const void* in, void* out, int B, int H, int W, int C, int backward, void* stream);
 /* nearest 2x upsampling (backward = 0) or its adjoint; H, W: coarse size */
 int agx_nn_upsample2(const void* in, void* out, int B, int H, int W, int C, int backward, void* stream);
+/* f x f average pooling (backward = 0: out = block means) or its adjoint (backward = 1: every
+   pixel of a block gets the coarse value / f^2); H, W: full size, multiples of f.  C a multiple
+   of 8, in and out 16-byte aligned; sums in float, rounded to bf16 once. */
+int agx_nn_pool(const void* in, void* out, int B, int H, int W, int C, int f, int backward, void* stream);
+/* nearest f x upsampling (backward = 0) or its adjoint (backward = 1: block sums); H, W: coarse
+   size.  Same channel and alignment rules as agx_nn_pool. */
+int agx_nn_upsample(const void* in, void* out, int B, int H, int W, int C, int f, int backward, void* stream);
 /* g *= (y > 0) */
 int agx_nn_relu_backward(void* g, const void* y, int64_t n, void* stream);
 /* a += b */
@@ -66,6 +78,20 @@ int agx_nn_field_from_grid(const void* img, int C, int nd, int Hn, int Wn, int W
 int agx_nn_restrict_field(const float* fine, const unsigned char* fixed, int nd, int Hc, int Wc, int f, float* coarse,
                           void* stream);
 int agx_nn_prolong_field(const float* coarse, int nd, int Hc, int Wc, int f, float* fine, void* stream);
+/* The coarse-grid network's transfers in fewer launches.  agx_nn_restrict_image: coarse =
+   P^T fine (as agx_nn_restrict_field) and the network's input image of (coarse / rms, aux) with
+   1 / rms in scale[0] (as agx_nn_grid_from_field with normalize = 1) in two launches: the
+   restriction leaves per-block sums of squares in `work` (agx_nn_restrict_image_work() doubles)
+   and every block of the image kernel adds them up itself.  agx_nn_prolong_image: fine = P
+   applied to channels 0 .. nd-1 of an NHWC image with C channels (the network's output; the
+   coarse field is not written out), zero at the DOFs flagged in `fixed` (optional).  Grids
+   below 2^31 entries; the fine grid at most 65535 rows. */
+int agx_nn_restrict_image_work(void);
+int agx_nn_restrict_image(const float* fine, const unsigned char* fixed, int nd, const float* aux, int naux, int Hc,
+                          int Wc, int f, int Hp, int Wp, float* coarse, double* work, float* scale, void* img,
+                          void* stream);
+int agx_nn_prolong_image(const void* img, int C, int nd, int Hc, int Wc, int Wp, int f, const unsigned char* fixed,
+                         float* fine, void* stream);
 
 #ifdef __cplusplus
 }

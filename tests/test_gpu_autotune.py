@@ -1,6 +1,11 @@
 """The autotuner's SpMV variants (1, 2, 4, 8 or 16 lanes per block row with two blocks per lane
-and trip; 2, 4 or 8 lanes with four blocks, code lanes + 256) solve identically, the autotuner
-picks one of them per precision, and invalid tuning values are rejected."""
+and trip; 2, 4 or 8 lanes with four blocks, code lanes + 256; on a structured QUAD4 grid the
+index-free grid product, code 512) solve identically, the autotuner picks one of them per
+precision, and invalid tuning values are rejected.
+
+Tolerances, written where used: float64 products of one variant against SciPy's CSR product of
+the same matrix <= 1e-13 of max |y| (summation order differs); solutions of the variants within
+1e-8 (float64 PCG to 1e-10) or 1e-3 (float32 PCG to 1e-5) of each other."""
 import ctypes as C
 
 import numpy as np
@@ -13,7 +18,7 @@ from autopdex_gb300._problem import get_problem
 
 pytestmark = pytest.mark.gpu
 
-VARIANTS = (1, 2, 4, 8, 16, 2 + 256, 4 + 256, 8 + 256)
+VARIANTS = (1, 2, 4, 8, 16, 2 + 256, 4 + 256, 8 + 256, 512)  # 512: the heat problems' structured grid
 
 
 def _solve(prob, rhs, method):
@@ -63,6 +68,41 @@ def test_invalid_tuning_is_rejected():
     assert lib.agx_set_tuning(prob.ctx, N.AGX_F32, 2 + 256) != N.AGX_OK  # 3 DOFs per node need >= 4 lanes
     assert lib.agx_set_tuning(prob.ctx, N.AGX_F32, 8 + 256) == N.AGX_OK
     assert lib.agx_set_tuning(prob.ctx, N.AGX_F64, 8) == N.AGX_OK
+    assert lib.agx_set_tuning(prob.ctx, N.AGX_F64, 512) != N.AGX_OK  # hexahedra: no grid product
+
+
+@pytest.mark.parametrize("case", ["heat", "cook"])
+def test_grid_product_matches_scipy(case):
+    """agx_spmv with the grid product (code 512) on a structured QUAD4 grid -- one DOF per node
+    (heat) and two (the Cook membrane's skewed grid) -- against SciPy's product of the copied
+    CSR matrix, float64 and float32 tangents."""
+    import scipy.sparse as sps
+    w = configs.heat_grf(n=37, seed=3) if case == "heat" else configs.cook_membrane(n=23, n_steps=2)
+    if case == "cook":
+        w.settings["load multiplier"] = 0.03
+    prob = get_problem(w.dofs, w.settings, w.static_settings)
+    prob.update_models(w.settings)
+    rng = np.random.default_rng(4)
+    u = torch.as_tensor(rng.uniform(-1e-3, 1e-3, prob.n_dofs), device=prob.device)
+    nd = prob.ndof
+    for dtype, tdt, tol in ((N.AGX_F64, torch.float64, 1e-13), (N.AGX_F32, torch.float32, 2e-6)):
+        prob._call("agx_assemble", C.c_void_p(u.data_ptr()), None, dtype)
+        nn = prob.n_dofs // nd
+        rowptr = torch.empty(nn + 1, dtype=torch.int32, device=prob.device)
+        col = torch.empty(prob.nnzb, dtype=torch.int32, device=prob.device)
+        vals = torch.empty(prob.nnzb * nd * nd, dtype=tdt, device=prob.device)
+        prob._call("agx_copy_matrix", dtype, C.c_void_p(rowptr.data_ptr()), C.c_void_p(col.data_ptr()),
+                   C.c_void_p(vals.data_ptr()))
+        blocks = vals.double().cpu().numpy().reshape(-1, nd, nd)  # row-major blocks
+        A = sps.bsr_matrix((blocks, col.cpu().numpy(), rowptr.cpu().numpy()), shape=(prob.n_dofs, prob.n_dofs))
+        x = torch.as_tensor(rng.standard_normal(prob.n_dofs), device=prob.device).to(tdt)
+        ref = A @ x.double().cpu().numpy()
+        for code in (512, 4):
+            prob._call("agx_set_tuning", dtype, code)
+            y = torch.empty_like(x)
+            prob._call("agx_spmv", dtype, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()))
+            assert np.abs(y.double().cpu().numpy() - ref).max() <= tol * np.abs(ref).max(), (case, dtype, code)
+        prob._call("agx_set_tuning", dtype, 0)
 
 
 def test_autotuner_times_real_products():
@@ -78,5 +118,5 @@ def test_autotuner_times_real_products():
         tpr = C.c_int()
         ms = C.c_float()
         prob._call("agx_autotune", C.byref(tpr), C.byref(ms))
-        matrix_bytes = prob.nnzb * (s + 4)
+        matrix_bytes = prob.nnzb * (s + (0 if tpr.value == 512 else 4))  # the grid product reads no indices
         assert ms.value * 1e-3 >= matrix_bytes / 8e12, (dtype, tpr.value, ms.value)
