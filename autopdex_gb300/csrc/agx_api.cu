@@ -59,6 +59,7 @@ void free_device(agx_context* ctx) {
   release(ctx->d_diagpos);
   release(ctx->d_vals64);
   release(ctx->d_vals32);
+  release(ctx->d_vals16);
   release(ctx->d_dinv64);
   release(ctx->d_dinv32);
   release(ctx->d_band);
@@ -541,11 +542,13 @@ int agx_set_preconditioner_mode(agx_context* ctx, int mode, double omega, int sw
     return agx_fail(ctx, AGX_ERR_ARG, mode == 3 ? "the Chebyshev interval fraction must lie in (0, 1)"
                                                : "Jacobi damping must lie in (0, 1]");
   if (sweeps < 1 || sweeps > 16) return agx_fail(ctx, AGX_ERR_ARG, "smoothing sweeps must lie in 1 .. 16");
-  if (flags & ~AGX_PRECOND_CAPTURABLE) return agx_fail(ctx, AGX_ERR_ARG, "unknown preconditioner flags");
+  if (flags & ~(AGX_PRECOND_CAPTURABLE | AGX_PRECOND_BF16_SMOOTHING))
+    return agx_fail(ctx, AGX_ERR_ARG, "unknown preconditioner flags");
   ctx->precond_mode = mode;
   ctx->precond_omega = omega;
   ctx->precond_sweeps = sweeps;
   ctx->precond_capturable = (flags & AGX_PRECOND_CAPTURABLE) != 0;
+  ctx->precond_bf16 = (flags & AGX_PRECOND_BF16_SMOOTHING) != 0;
   ctx->precond_gen += 1;
   return AGX_OK;
 }

@@ -9,6 +9,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "../../include/autopdex_gb300.h"
 
 #define AGX_MAX_PARAMS 16
@@ -166,6 +168,9 @@ struct agx_context {
   int64_t cheb_gen = -1;       // tangent generation the bound belongs to
   int64_t tangent_gen = 0;     // bumped by every tangent assembly
   int precond_capturable = 0;  // the callback only enqueues work on the stream it is given
+  int precond_bf16 = 0;        // two-level products on a bf16 copy of the float32 values
+  __nv_bfloat16* d_vals16 = nullptr;
+  int64_t bf16_copy_gen = -1;  // tangent generation whose bf16 copy is current
   int64_t precond_gen = 0;     // bumped whenever the callback or its mode changes
   int spmv_tpr[2] = {0, 0};  // lanes per block row of the Krylov product, float64 / float32 (0: default)
   int64_t f32_copy_gen = -1;  // tangent generation whose float32 copy (values, inverse diagonal) is current

@@ -139,9 +139,16 @@ __device__ __forceinline__ bool bad(double x) { return !isfinite(x) || x == 0.0;
 // before any gather or FMA, so each lane keeps U blocks of loads in flight (the product is bound
 // by bytes in flight per SM, not by traffic); matrix data is streamed (evict-first) so that the
 // gathered vectors stay in L2.
-template <typename T, int NDOF, int TPR, bool DIR, int U = 2>
+// a stored value (float, double or the bf16 smoothing copy) in the product's precision, streamed
+template <typename T, typename VT>
+__device__ __forceinline__ T load_val(const VT* p) {
+  if constexpr (std::is_same<VT, __nv_bfloat16>::value) return (T)__bfloat162float(__ldcs(p));
+  else return (T)__ldcs(p);
+}
+
+template <typename T, int NDOF, int TPR, bool DIR, int U = 2, typename VT = T>
 __device__ __forceinline__ void bsr_row(int64_t row, int sub, const int32_t* __restrict__ rowptr,
-                                        const int32_t* __restrict__ col, const T* __restrict__ vals, int64_t nnzb,
+                                        const int32_t* __restrict__ col, const VT* __restrict__ vals, int64_t nnzb,
                                         const T* __restrict__ x, const T* __restrict__ pold, T beta, T (&y)[NDOF]) {
 #pragma unroll
   for (int i = 0; i < NDOF; ++i) y[i] = 0;
@@ -159,7 +166,7 @@ __device__ __forceinline__ void bsr_row(int64_t row, int sub, const int32_t* __r
 #pragma unroll
     for (int e = 0; e < NDOF * NDOF; ++e)
 #pragma unroll
-      for (int u = 0; u < U; ++u) v[u][e] = ok[u] ? __ldcs(vals + (int64_t)e * nnzb + k + u * TPR) : T(0);
+      for (int u = 0; u < U; ++u) v[u][e] = ok[u] ? load_val<T>(vals + (int64_t)e * nnzb + k + u * TPR) : T(0);
     T xs[U][NDOF];
 #pragma unroll
     for (int u = 0; u < U; ++u)
@@ -192,15 +199,16 @@ __device__ __forceinline__ void bsr_row(int64_t row, int sub, const int32_t* __r
 //   rowptr(p) = S(i) (3 ny + 1) + r_i S(j),  S(m) = 3 m - [m > 0],  r_i = [i > 0] + 1 + [i < nx]
 // (S(m) blocks in the rows or columns before m, 3 ny + 1 in a full row of nodes), so one lane per
 // row reads only its values and the gathered vector: no row pointer, no column index.
-template <typename T, int NDOF, bool DIR>
-__device__ __forceinline__ void grid_row(int64_t row, int ny, int64_t n_rows, const T* __restrict__ vals,
+template <typename T, int NDOF, bool DIR, typename VT = T>
+__device__ __forceinline__ void grid_row(int64_t row, int ny, int64_t n_rows, const VT* __restrict__ vals,
                                          int64_t nnzb, const T* __restrict__ x, const T* __restrict__ pold, T beta,
                                          T (&y)[NDOF]) {
-  const int64_t ny1 = (int64_t)ny + 1, nx = n_rows / ny1 - 1;
-  const int64_t i = row / ny1;
-  const int j = (int)(row - i * ny1);
+  // node counts below 2^31 (the pattern's int32 offsets): 32-bit division
+  const uint32_t ny1 = (uint32_t)ny + 1u, nx = (uint32_t)n_rows / ny1 - 1u;
+  const uint32_t i = (uint32_t)row / ny1;
+  const int j = (int)((uint32_t)row - i * ny1);
   const int ri = (i > 0) + 1 + (i < nx);
-  const int64_t k0 = (3 * i - (i > 0)) * (3 * (int64_t)ny + 1) + (int64_t)ri * (3 * j - (j > 0));
+  const int64_t k0 = (int64_t)(3 * i - (i > 0)) * (3 * (int64_t)ny + 1) + (int64_t)ri * (3 * j - (j > 0));
   bool ok[9];
   int m[9];
   int cnt = 0;
@@ -215,12 +223,12 @@ __device__ __forceinline__ void grid_row(int64_t row, int ny, int64_t n_rows, co
 #pragma unroll
   for (int e = 0; e < NDOF * NDOF; ++e)
 #pragma unroll
-    for (int t = 0; t < 9; ++t) v[t][e] = ok[t] ? __ldcs(vals + (int64_t)e * nnzb + k0 + m[t]) : T(0);
+    for (int t = 0; t < 9; ++t) v[t][e] = ok[t] ? load_val<T>(vals + (int64_t)e * nnzb + k0 + m[t]) : T(0);
 #pragma unroll
   for (int q = 0; q < NDOF; ++q) y[q] = 0;
 #pragma unroll
   for (int t = 0; t < 9; ++t) {
-    const int64_t c = row + (int64_t)(t / 3 - 1) * ny1 + (t % 3 - 1);
+    const int64_t c = row + (int64_t)(t / 3 - 1) * (int64_t)ny1 + (t % 3 - 1);
 #pragma unroll
     for (int jj = 0; jj < NDOF; ++jj) {
       T xv = ok[t] ? x[c * NDOF + jj] : T(0);
@@ -235,16 +243,16 @@ __device__ __forceinline__ void grid_row(int64_t row, int ny, int64_t n_rows, co
 
 // A product row in the tangent's storage: U > 0 the node-block CSR with TPR lanes per row,
 // U == 0 the structured grid's stencil (one lane per row, gny = ny)
-template <typename T, int NDOF, int TPR, bool DIR, int U>
+template <typename T, int NDOF, int TPR, bool DIR, int U, typename VT = T>
 __device__ __forceinline__ void tangent_row(int64_t row, int sub, const int32_t* __restrict__ rowptr,
-                                            const int32_t* __restrict__ col, const T* __restrict__ vals,
+                                            const int32_t* __restrict__ col, const VT* __restrict__ vals,
                                             int64_t nnzb, int64_t n_rows, int gny, const T* __restrict__ x,
                                             const T* __restrict__ pold, T beta, T (&y)[NDOF]) {
   if constexpr (U == 0) {
     static_assert(TPR == 1, "the grid product has one lane per row");
-    grid_row<T, NDOF, DIR>(row, gny, n_rows, vals, nnzb, x, pold, beta, y);
+    grid_row<T, NDOF, DIR, VT>(row, gny, n_rows, vals, nnzb, x, pold, beta, y);
   } else {
-    bsr_row<T, NDOF, TPR, DIR, U>(row, sub, rowptr, col, vals, nnzb, x, pold, beta, y);
+    bsr_row<T, NDOF, TPR, DIR, U, VT>(row, sub, rowptr, col, vals, nnzb, x, pold, beta, y);
   }
 }
 
@@ -661,10 +669,10 @@ tl_combine(int64_t n, float* __restrict__ z, const float* __restrict__ y, float*
 //   TL_STEP   t written; block partials of (rc, y) and (y, t) for tl_finish_step
 enum { TL_SWEEP = 0, TL_RESID = 1, TL_STEP = 2 };
 
-template <int NDOF, int TPR, int U, int EPI>
+template <int NDOF, int TPR, int U, int EPI, typename VT = float>
 __global__ void __launch_bounds__(AGX_BLOCK)
 tl_spmv(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-        const float* __restrict__ vals, int64_t nnzb, int gny, const float* __restrict__ x, float* __restrict__ rc,
+        const VT* __restrict__ vals, int64_t nnzb, int gny, const float* __restrict__ x, float* __restrict__ rc,
         const float* __restrict__ dinv, float a, float b, float* __restrict__ dnew, float* __restrict__ z,
         float* __restrict__ tout, agx_krylov_scalars* sc, double* __restrict__ partials) {
   agx_pdl_entry();
@@ -675,8 +683,8 @@ tl_spmv(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __res
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = L / TPR;
     float yr[NDOF];
-    tangent_row<float, NDOF, TPR, false, U>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, n_rows,
-                                            gny, x, nullptr, 0.0f, yr);
+    tangent_row<float, NDOF, TPR, false, U, VT>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb,
+                                                n_rows, gny, x, nullptr, 0.0f, yr);
     if (row < n_rows && sub == 0) {
 #pragma unroll
       for (int i = 0; i < NDOF; ++i) {
@@ -1316,17 +1324,17 @@ int agx_residual_norm(agx_context* ctx, const double* R, double* norm2, double* 
   return AGX_OK;
 }
 
-// z = M(r) on the float32 Krylov vectors (f_r -> f_z) for the flexible method
-template <int ND, int EPI>
-void tl_spmv_nd(agx_context* ctx, int code, int g, const float* x, float* rc, float a, float b, float* dnew,
-                float* tout) {
+// z = M(r) on the float32 Krylov vectors (f_r -> f_z) for the flexible method; VT the stored
+// values the products read (float, or the bf16 smoothing copy)
+template <int ND, int EPI, typename VT>
+void tl_spmv_nd(agx_context* ctx, int code, int g, const VT* vals, const float* x, float* rc, float a, float b,
+                float* dnew, float* tout) {
   auto* sc = ctx->d_scal;
   const int64_t nr = ctx->n_nodes;
-#define AGX_TL(TP_, U_)                                                                                           \
-  agx_launch_pdl(tl_spmv<ND, TP_, U_, EPI>, g, AGX_BLOCK, 0, ctx->stream, nr, ctx->d_rowptr, ctx->d_col, ctx->d_vals32,     \
-                                                               ctx->nnzb, ctx->pattern_grid_ny, x, rc,            \
-                                                               ctx->d_dinv32, a, b, dnew, ctx->f_z, tout, sc,     \
-                                                               ctx->d_partials)
+#define AGX_TL(TP_, U_)                                                                                         \
+  agx_launch_pdl(tl_spmv<ND, TP_, U_, EPI, VT>, g, AGX_BLOCK, 0, ctx->stream, nr, ctx->d_rowptr, ctx->d_col, \
+                 vals, ctx->nnzb, ctx->pattern_grid_ny, x, rc, ctx->d_dinv32, a, b, dnew, ctx->f_z, tout, sc,   \
+                 ctx->d_partials)
   switch (code) {
     case 1: AGX_TL(1, 2); break;
     case 2: AGX_TL(2, 2); break;
@@ -1355,9 +1363,14 @@ void launch_tl_spmv(agx_context* ctx, const float* x, float* rc, float a, float 
   const int code = tuned > 0 ? tuned : default_tpr(ctx);
   // a reducing kernel writes one partial per block: its grid stays within the partials buffer
   const int g = EPI == TL_STEP ? ctx->red_blocks : agx_grid(ctx, ctx->n_nodes * spmv_lanes(code), 8);
-  if (ctx->ndof == 1) tl_spmv_nd<1, EPI>(ctx, code, g, x, rc, a, b, dnew, tout);
-  else if (ctx->ndof == 2) tl_spmv_nd<2, EPI>(ctx, code, g, x, rc, a, b, dnew, tout);
-  else tl_spmv_nd<3, EPI>(ctx, code, g, x, rc, a, b, dnew, tout);
+  auto go = [&](auto* vals) {
+    using VT = std::remove_const_t<std::remove_pointer_t<decltype(vals)>>;
+    if (ctx->ndof == 1) tl_spmv_nd<1, EPI, VT>(ctx, code, g, vals, x, rc, a, b, dnew, tout);
+    else if (ctx->ndof == 2) tl_spmv_nd<2, EPI, VT>(ctx, code, g, vals, x, rc, a, b, dnew, tout);
+    else tl_spmv_nd<3, EPI, VT>(ctx, code, g, vals, x, rc, a, b, dnew, tout);
+  };
+  if (ctx->precond_bf16) go(ctx->d_vals16);
+  else go(ctx->d_vals32);
   ctx->n_launches += 1;
 }
 
@@ -1442,6 +1455,24 @@ int apply_registered_preconditioner(agx_context* ctx) {
     std::swap(pA, pB);
   }
   return 0;
+}
+
+// bf16 copy of the float32 tangent's values for the two-level products
+// (AGX_PRECOND_BF16_SMOOTHING), made once per assembled tangent (before any capture)
+__global__ void copy_to_bf16(int64_t n, const float* __restrict__ src, __nv_bfloat16* __restrict__ dst) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = __float2bfloat16(src[i]);
+}
+
+int ensure_bf16_copy(agx_context* ctx) {
+  if (!ctx->precond_bf16 || ctx->precond_mode == 0 || ctx->bf16_copy_gen == ctx->tangent_gen) return AGX_OK;
+  const int64_t nv = ctx->nnzb * ctx->ndof * ctx->ndof;
+  if (!ctx->d_vals16) AGX_CUDA(ctx, cudaMalloc(&ctx->d_vals16, sizeof(__nv_bfloat16) * std::max<int64_t>(1, nv)));
+  copy_to_bf16<<<agx_grid(ctx, nv), AGX_BLOCK, 0, ctx->stream>>>(nv, ctx->d_vals32, ctx->d_vals16);
+  AGX_CHECK_LAUNCH(ctx);
+  ctx->n_launches += 1;
+  ctx->bf16_copy_gen = ctx->tangent_gen;
+  return AGX_OK;
 }
 
 // float32 copy of the float64 tangent (values and inverse diagonal) for the float32
@@ -1543,6 +1574,7 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
                                                             flexible ? 0 : 1);
     if (flexible) {
       if (int rc = update_chebyshev_bound(ctx)) return rc;
+      if (int rc = ensure_bf16_copy(ctx)) return rc;
       if (apply_registered_preconditioner(ctx) != 0)
         return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");
       agx_launch_pdl(fcg_direction_dots<float>, g, AGX_BLOCK, 0, ctx->stream, n, ctx->f_r, ctx->f_z, ctx->f_q, sc, ctx->d_partials);
@@ -1623,6 +1655,7 @@ int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_so
     };
     if (flexible) {
       if (int rc = update_chebyshev_bound(ctx)) return rc;
+      if (int rc = ensure_bf16_copy(ctx)) return rc;
       precond();
       if (precond_failed) return agx_fail(ctx, AGX_ERR_ARG, "preconditioner callback failed");
     }

@@ -664,11 +664,14 @@ class GridPreconditioner:
     enqueues kernels on the stream it is given, so FCG captures it into CUDA graphs."""
 
     def __init__(self, net, nx, ny, k_elem=None, factor=1, mode=None, omega=None, sweeps=None, fixed=None, nd=1,
-                 aux=None):
+                 aux=None, bf16_smoothing=False):
         if nx % factor or ny % factor:
             raise ValueError("the grid must be divisible by the coarsening factor")
         self.net = net
         self.nd = nd
+        # the smoothing, residual and step products on a bf16 copy of the tangent's values
+        # (AGX_PRECOND_BF16_SMOOTHING)
+        self.bf16_smoothing = bool(bf16_smoothing)
         # smoothing around the network, measured on the 1024^2 heat workload to a 1e-10
         # residual: on a coarsened grid (factor 4) the degree-3 Chebyshev smoother on
         # [lmax/30, lmax] (mode 3: 0.070 s; damped Jacobi, mode 2, best at 5 sweeps: 0.093 s);
@@ -735,8 +738,8 @@ class GridPreconditioner:
         cb = self.callback(prob)
         prob._precond_cb = cb
         prob._call("agx_set_preconditioner", cb, None)
-        prob._call("agx_set_preconditioner_mode", int(self.mode), float(self.omega), int(self.sweeps),
-                   N.AGX_PRECOND_CAPTURABLE)
+        flags = N.AGX_PRECOND_CAPTURABLE | (N.AGX_PRECOND_BF16_SMOOTHING if self.bf16_smoothing else 0)
+        prob._call("agx_set_preconditioner_mode", int(self.mode), float(self.omega), int(self.sweeps), flags)
         prob.learned = self
 
     def callback(self, prob):

@@ -179,11 +179,15 @@ def _heat_variants():
              dict(krylov_tol=1e-4))]
 
 
+BF16_SMOOTHING = False  # --bf16-smoothing: the two-level products on a bf16 copy of the values
+
+
 def _heat_learned_setup(w, n):
     from autopdex_gb300 import learned, solver
     net = learned.UNet.load(os.path.join(learned.WEIGHTS_DIR, "heat_unet_n256.npz"))
     factor = max(1, n // TRAIN_N)
-    pc = learned.GridPreconditioner(net, n, n, w.settings["conductivity"], factor=factor)
+    pc = learned.GridPreconditioner(net, n, n, w.settings["conductivity"], factor=factor,
+                                    bf16_smoothing=BF16_SMOOTHING)
     solver.set_learned_preconditioner(None, pc)
     return net, pc, factor
 
@@ -333,8 +337,11 @@ def headline_roofline(h):
     nnzb = prob.nnzb
     s = 4  # float32 products
     # algorithmic bytes per launch: values and columns of every stored block, row pointers, and
-    # the vectors (fused Krylov product: z, p_old read, p_new, q written; plain product: x, y)
-    matrix = nnzb * (ndof * ndof * s + 4) + 4 * (n_nodes + 1)
+    # the vectors (fused Krylov product: z, p_old read, p_new, q written; plain product: x, y);
+    # the structured grid's product (code 512) reads no row pointers or column indices
+    tpr = getattr(prob, "spmv_tpr", 0)
+    grid = tpr == 512
+    matrix = nnzb * ndof * ndof * s if grid else nnzb * (ndof * ndof * s + 4) + 4 * (n_nodes + 1)
     fused = matrix + 4 * n * s
     # the two-level products carry their element-wise work: per application 2 (nu - 1) sweep
     # products (x gathered; rc, z read and written; D^-1 read; the new increment written: 7
@@ -344,10 +351,10 @@ def headline_roofline(h):
     plain = matrix + n * s * (2 * (nu - 1) * 7 + 3 + 3) / (2 * (nu - 1) + 2)
     hc = h["w"].raw["n"] // h["factor"] + 1
     flops = _network_flops(learned.padded(hc), learned.padded(hc))
-    tpr = getattr(prob, "spmv_tpr", "tpr")
-    cand = {"smoothing_product": ("hbm", plain, f"tl_spmv<1,{tpr}> (two-level smoothing, residual and step products "
+    var = "grid" if grid else f"bsr, {tpr} lanes per row"
+    cand = {"smoothing_product": ("hbm", plain, f"tl_spmv<1,{var}> (two-level smoothing, residual and step products "
                                                 "with their element-wise work fused)"),
-            "krylov_product": ("hbm", fused, f"spmv_dot_kernel<float,1,{tpr}> (FCG product with direction update "
+            "krylov_product": ("hbm", fused, f"spmv_dot_kernel<float,1,{var}> (FCG product with direction update "
                                              "and dot)"),
             "network": ("tensor", flops, "U-Net forward: 15 conv3x3_tc (tcgen05, BF16), pooling, upsampling and "
                                          "grid transfers, replayed from a CUDA graph")}
@@ -801,15 +808,23 @@ def case(args):
     from autopdex_gb300._problem import get_problem
     if args.case == "conv":
         net = learned.UNet(seed=0)
+        if args.halo_loader >= 0:
+            assert net.lib.agx_nn_set_halo_loader(args.halo_loader) == 0
         _, c1, c2, co, relu = next(l for l in learned.LAYERS if l[0] == args.layer)
         g = torch.Generator(device="cuda").manual_seed(0)
         x1 = torch.randn(1, args.size, args.size, c1, device="cuda", generator=g).to(torch.bfloat16)
         x2 = torch.randn(1, args.size, args.size, c2, device="cuda", generator=g).to(torch.bfloat16) if c2 else None
+        net._conv(args.layer, x1, x2, 1, args.size, args.size)  # warm-up (attributes, first launch)
+        _sync()
+        a, b = _events()
+        a.record()
         for _ in range(args.reps):
             net._conv(args.layer, x1, x2, 1, args.size, args.size)
+        b.record()
         _sync()
         net.check()
-        print(f"conv {args.layer} on {args.size}^2: {args.reps} launches")
+        print(f"conv {args.layer} on {args.size}^2: {args.reps} launches after one warm-up launch, "
+              f"{a.elapsed_time(b) * 1e3 / max(1, args.reps):.2f} us per launch (CUDA events, back to back)")
         return
     make = {"heat": lambda: configs.heat_grf(n=args.size, seed=10000, precision=args.precision, solver=args.solver),
             "poisson": lambda: configs.poisson(n=args.size, precision=args.precision, solver=args.solver),
@@ -867,7 +882,12 @@ def main():
     ap.add_argument("--layer", default="e0b")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--tpr", type=int, default=0, help="solve case: SpMV variant code instead of the autotuner's")
+    ap.add_argument("--bf16-smoothing", action="store_true",
+                    help="the learned preconditioner's smoothing products on a bf16 copy of the tangent values")
+    ap.add_argument("--halo-loader", type=int, default=-1, help="conv case: agx_nn_set_halo_loader mode")
     args = ap.parse_args()
+    global BF16_SMOOTHING
+    BF16_SMOOTHING = args.bf16_smoothing
     if args.case:
         case(args)
         return

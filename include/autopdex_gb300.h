@@ -233,8 +233,13 @@ int agx_set_preconditioner(agx_context* ctx, agx_precond_fn fn, void* user);
    flags: AGX_PRECOND_CAPTURABLE declares that the callback only enqueues device work on the
    stream it is given (no synchronisation, allocation or host reads), so that FCG captures
    its iterations, callback included, into CUDA graphs and replays them; the callback's
-   buffers must then stay valid until the preconditioner is replaced. */
+   buffers must then stay valid until the preconditioner is replaced.
+   AGX_PRECOND_BF16_SMOOTHING (modes 1-3): the smoothing, residual and step products of the
+   two-level application read a bf16 copy of the float32 tangent's values (made once per
+   assembled tangent; float32 vectors and accumulation), which halves their value traffic; the
+   Krylov product itself keeps the float32 values. */
 #define AGX_PRECOND_CAPTURABLE 1
+#define AGX_PRECOND_BF16_SMOOTHING 2
 int agx_set_preconditioner_mode(agx_context* ctx, int mode, double omega, int sweeps, int flags);
 /* Kernel timing.  While enabled, the library brackets its kernel launches with CUDA events
    on its stream and accumulates the elapsed time per category; agx_profile_read

@@ -23,10 +23,12 @@ extern "C" {
 int agx_nn_conv3x3(const void* in1, const void* in2, int c1, int c2, const void* wpk, const float* bias,
                    void* out1, void* out2, int split, int cout, int relu, int B, int H, int W, int* err,
                    void* stream);
-/* How agx_nn_conv3x3 stages its input halos in shared memory: 0 cp.async by all threads of the
-   CTA, 16-byte pixel chunks with zero fill at the image edge (in1 and in2 then 16-byte
-   aligned); 1 (the default, the faster one measured) one tensor-memory-access copy per
-   8-channel plane.  Both give identical results.  Process-wide; affects later launches only. */
+/* How agx_nn_conv3x3 feeds its tensor cores: 0 cp.async halo copies by all threads of the CTA
+   (16-byte pixel chunks, zero fill at the image edge; in1 and in2 then 16-byte aligned) and one
+   loop with a CTA barrier per tile; 1 one tensor-memory-access copy per 8-channel plane in the
+   same loop; 2 the tensor copies in a warp-specialised kernel (a copy warp, an MMA warp and four
+   epilogue warps on mbarrier rings); 3 (the default) 2 for two-input layers of at least 128^2
+   pixels, else 1.  All give identical results.  Process-wide; affects later launches only. */
 int agx_nn_set_halo_loader(int loader);
 /* dw_rows[(tap * (c1 + c2) + ci) * cout + co] += sum over pixels of in(p + tap)[ci] * dout(p)[co] */
 int agx_nn_wgrad3x3(const void* in1, const void* in2, int c1, int c2, const void* dout, int cout, float* dw_rows,
