@@ -16,7 +16,8 @@
 // factors the NB x NB diagonal block in shared memory (every CTA, redundantly; CTA 0 leaves the
 // result in a scratch block) and solves one row of the w x NB block below per thread
 // (L21 = A21 L11^-T); syrk_update then subtracts L21 L21^T from the w x w lower triangle that
-// follows, in 64 x 64 tiles, and copies the diagonal block from the scratch into the band.
+// follows, in 16 x 16 to 64 x 64 tiles (whichever leaves the busiest SM the least float64 work),
+// and copies the diagonal block from the scratch into the band.
 // Work: about n w^2 float64 flops (0.56 TFLOP for the 512^2 membrane).
 // Solves: one CTA walks blocks of NB rows -- forward substitution with column updates of the
 // rows below, backward substitution with per-column dot products of the rows below -- and the
@@ -31,7 +32,6 @@
 namespace {
 
 constexpr int NB = 32;   // panel width
-constexpr int TM = 64;   // update tile
 constexpr int PF_THREADS = 64;  // rows of the block below the diagonal block per CTA
 constexpr int SOLVE_THREADS = 1024;
 
@@ -103,8 +103,9 @@ __global__ void __launch_bounds__(PF_THREADS)
 panel_factor(double* __restrict__ band, int64_t n, int64_t w, int64_t j0, int nbp, double* __restrict__ l11,
              double* __restrict__ rdiag, int* __restrict__ err) {
   __shared__ double L[NB][NB + 1];
-  __shared__ double rinv[NB];  // reciprocals of the pivots L_qq
+  __shared__ double rinv[NB];  // reciprocals of the pivots L_qq (0 past a partial last panel)
   const int64_t ld = w + 1;
+  if (threadIdx.x < NB) rinv[threadIdx.x] = 0.0;
   for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
     const int i = idx / NB, q = idx % NB;
     L[i][q] = (q <= i && i < nbp && (int64_t)(i - q) <= w) ? band[(j0 + q) * ld + (i - q)] : 0.0;
@@ -146,14 +147,16 @@ panel_factor(double* __restrict__ band, int64_t n, int64_t w, int64_t j0, int nb
     const int64_t off = nbp + R - q;
     x[q] = (q < nbp && off <= w) ? band[(j0 + q) * ld + off] : 0.0;
   }
+  // right-looking: once x_q is final it updates every later x_p; each x_p subtracts the same
+  // terms in the same order (q = 0 .. p-1) as a row-by-row solve would, but consecutive FMAs
+  // go to different accumulators, so the float64 latency overlaps instead of forming one
+  // chain of NB (NB - 1) / 2 dependent FMAs.  Columns past a partial last panel are zero in
+  // x and L and have rinv = 0, so the loop needs no bound.
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
-    if (q < nbp) {
-      double v = x[q];
+    x[q] *= rinv[q];
 #pragma unroll
-      for (int p = 0; p < q; ++p) v -= x[p] * L[q][p];
-      x[q] = v * rinv[q];
-    }
+    for (int p = q + 1; p < NB; ++p) x[p] -= x[q] * L[p][q];
   }
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
@@ -162,10 +165,14 @@ panel_factor(double* __restrict__ band, int64_t n, int64_t w, int64_t j0, int nb
   }
 }
 
-// A22 -= L21 L21^T on the w x w lower triangle after panel j0; CTA 0 also stores the factored
-// diagonal block (kept in l11 by panel_factor so that no CTA of that kernel read it half-written)
+// A22 -= L21 L21^T on the w x w lower triangle after panel j0, in TM x TM tiles (TM = 16, 32 or
+// 64: the largest that still gives every SM a tile, since the update is bound by each SM's float64
+// rate); CTA 0 also stores the factored diagonal block (kept in l11 by panel_factor so that no CTA
+// of that kernel read it half-written)
+template <int TM>
 __global__ void __launch_bounds__(256)
 syrk_update(double* __restrict__ band, int64_t n, int64_t w, int64_t j0, int nbp, const double* __restrict__ l11) {
+  constexpr int R = TM / 16;  // a thread's R x R accumulators
   const int64_t ld = w + 1;
   if (blockIdx.x == 0)
     for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
@@ -188,26 +195,26 @@ syrk_update(double* __restrict__ band, int64_t n, int64_t w, int64_t j0, int nbp
   }
   __syncthreads();
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  double acc[4][4] = {};
+  double acc[R][R] = {};
 #pragma unroll 8
   for (int q = 0; q < NB; ++q) {
-    double a[4], bb[4];
+    double a[R], bb[R];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < R; ++u) {
       a[u] = Xa[q][tx + 16 * u];
       bb[u] = Xb[q][ty + 16 * u];
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+    for (int u = 0; u < R; ++u)
 #pragma unroll
-      for (int v = 0; v < 4; ++v) acc[u][v] += a[u] * bb[v];
+      for (int v = 0; v < R; ++v) acc[u][v] += a[u] * bb[v];
   }
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < R; ++u)
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const int64_t R = ti * TM + tx + 16 * u, Cc = tj * TM + ty + 16 * v;
-      if (R < w && Cc <= R && j0 + nbp + R < n) band[(j0 + nbp + Cc) * ld + (R - Cc)] -= acc[u][v];
+    for (int v = 0; v < R; ++v) {
+      const int64_t Rr = ti * TM + tx + 16 * u, Cc = tj * TM + ty + 16 * v;
+      if (Rr < w && Cc <= Rr && j0 + nbp + Rr < n) band[(j0 + nbp + Cc) * ld + (Rr - Cc)] -= acc[u][v];
     }
 }
 
@@ -227,9 +234,12 @@ __global__ void __launch_bounds__(SOLVE_THREADS) band_forward(const double* __re
     }
     __syncthreads();
     if (threadIdx.x < 32) {
+      // the block's pivot reciprocals in registers before the sequential chain (a global load
+      // inside it would put one memory latency on every step)
+      const double rd = lane < nbp ? rdiag[j0 + lane] : 1.0;
       double yi = lane < nbp ? v[j0 + lane] : 0.0;
       for (int q = 0; q < nbp; ++q) {
-        if (lane == q) yi *= rdiag[j0 + q];
+        if (lane == q) yi *= rd;
         const double yq = __shfl_sync(0xffffffffu, yi, q);
         if (lane > q && lane < nbp) yi -= L[lane][q] * yq;
       }
@@ -242,12 +252,13 @@ __global__ void __launch_bounds__(SOLVE_THREADS) band_forward(const double* __re
     for (int64_t R = threadIdx.x; R < w; R += blockDim.x) {
       const int64_t r = j0 + nbp + R;
       if (r >= n) break;
-      double s = 0.0;
-      for (int q = 0; q < nbp; ++q) {
+      double s4[4] = {0.0, 0.0, 0.0, 0.0};  // four partial sums: short float64 dependency chains
+#pragma unroll
+      for (int q = 0; q < NB; ++q) {
         const int64_t off = nbp + R - q;
-        if (off <= w) s += band[(j0 + q) * ld + off] * y[q];
+        if (q < nbp && off <= w) s4[q & 3] += band[(j0 + q) * ld + off] * y[q];
       }
-      v[r] -= s;
+      v[r] -= (s4[0] + s4[1]) + (s4[2] + s4[3]);
     }
     __syncthreads();
   }
@@ -279,9 +290,10 @@ __global__ void __launch_bounds__(SOLVE_THREADS) band_backward(const double* __r
     }
     __syncthreads();
     if (threadIdx.x < 32) {
+      const double rd = lane < nbp ? rdiag[j0 + lane] : 1.0;
       double xi = lane < nbp ? v[j0 + lane] - s[lane] : 0.0;
       for (int q = nbp - 1; q >= 0; --q) {
-        if (lane == q) xi *= rdiag[j0 + q];
+        if (lane == q) xi *= rd;
         const double xq = __shfl_sync(0xffffffffu, xi, q);
         if (lane < q) xi -= L[q][lane] * xq;
       }
@@ -367,13 +379,28 @@ int band_factor(agx_context* ctx) {
   }
   AGX_CHECK_LAUNCH(ctx);
   const int pf_grid = (int)std::max<int64_t>(1, (w + PF_THREADS - 1) / PF_THREADS);
-  const int64_t nt = (w + TM - 1) / TM;
-  const int sy_grid = (int)std::max<int64_t>(1, nt * (nt + 1) / 2);
+  auto tiles = [&](int tm) {
+    const int64_t nt = (w + tm - 1) / tm;
+    return (int)std::max<int64_t>(1, nt * (nt + 1) / 2);
+  };
+  // the tile size with the least float64 work on the busiest SM: ceil(tiles / SMs) tiles of tm^3
+  int tm = 64;
+  double best = 1e300;
+  for (int t : {64, 32, 16}) {
+    const double cost = std::ceil((double)tiles(t) / ctx->sm_count) * (double)t * t * t;
+    if (cost < best * 0.999) {
+      best = cost;
+      tm = t;
+    }
+  }
+  const int sy_grid = tiles(tm);
   for (int64_t j0 = 0; j0 < n; j0 += NB) {
     const int nbp = (int)imin(NB, n - j0);
     panel_factor<<<pf_grid, PF_THREADS, 0, ctx->stream>>>(ctx->d_band, n, w, j0, nbp, ctx->d_band_l11,
                                                           ctx->d_band_rdiag, ctx->d_band_err);
-    syrk_update<<<sy_grid, 256, 0, ctx->stream>>>(ctx->d_band, n, w, j0, nbp, ctx->d_band_l11);
+    if (tm == 64) syrk_update<64><<<sy_grid, 256, 0, ctx->stream>>>(ctx->d_band, n, w, j0, nbp, ctx->d_band_l11);
+    else if (tm == 32) syrk_update<32><<<sy_grid, 256, 0, ctx->stream>>>(ctx->d_band, n, w, j0, nbp, ctx->d_band_l11);
+    else syrk_update<16><<<sy_grid, 256, 0, ctx->stream>>>(ctx->d_band, n, w, j0, nbp, ctx->d_band_l11);
     ctx->n_launches += 2;
   }
   AGX_CHECK_LAUNCH(ctx);
