@@ -13,6 +13,7 @@ AGX_OK = 0
 AGX_NOT_CONVERGED = 1
 AGX_PRECOND_CAPTURABLE = 1
 AGX_PRECOND_BF16_SMOOTHING = 2
+AGX_NN_CONST_WEIGHTS = 2
 AGX_DIVERGED = 2
 
 AGX_QUAD4, AGX_HEX8, AGX_LINE2, AGX_QUAD9, AGX_LINE3 = 0, 1, 2, 3, 4

@@ -111,6 +111,7 @@ struct ConvArgs {
   int split;                 // S
   int B, H, W;
   int* err;
+  int const_weights;         // weights and bias not written by the kernel just before this one
 };
 
 // out = epi(conv3x3(concat(in1, in2)) + bias); EPI 0: identity, 1: ReLU.
@@ -246,7 +247,6 @@ __device__ __forceinline__ void copy_halo_async(const ConvArgs& a, int64_t tile,
 
 template <int C1, int C2, int COUT, int EPI, int LD>
 __global__ void __launch_bounds__(kTile) conv3x3_tc(const __grid_constant__ ConvMaps maps, ConvArgs a) {
-  agx_pdl_entry();
   constexpr int CIN = C1 + C2, K = 9 * CIN, NG = COUT / 8, NCH = CIN / 8;
   constexpr int B_BYTES = K * COUT * 2;
   constexpr int HALO_BYTES = NCH * kPlaneBytes;
@@ -283,9 +283,20 @@ __global__ void __launch_bounds__(kTile) conv3x3_tc(const __grid_constant__ Conv
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar0 + 8u));
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(wbar));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    // constant weights: their bulk copy overlaps the tail of the kernel before this one
+    if (a.const_weights && my_tiles > 0) {
+      mbar_expect(wbar, (uint32_t)B_BYTES);
+      bulk_load(b0, a.wpk, (uint32_t)B_BYTES, wbar);
+    }
+  }
+  if (a.const_weights && tid < COUT) sbias[tid] = a.bias ? a.bias[tid] : 0.0f;
+  if (warp == 0) tmem_alloc<NCOLS>(&tmem_slot);
+  // the previous kernel's outputs are visible from here on (programmatic dependent launch)
+  agx_pdl_entry();
+  if (tid == 0) {
     // the packed weights (already in core-matrix order) in one bulk copy, in flight together
     // with the first kStages halos
-    if (my_tiles > 0) {
+    if (!a.const_weights && my_tiles > 0) {
       mbar_expect(wbar, (uint32_t)B_BYTES);
       bulk_load(b0, a.wpk, (uint32_t)B_BYTES, wbar);
     }
@@ -302,8 +313,7 @@ __global__ void __launch_bounds__(kTile) conv3x3_tc(const __grid_constant__ Conv
       cp_async_commit();
     }
   }
-  if (tid < COUT) sbias[tid] = a.bias ? a.bias[tid] : 0.0f;
-  if (warp == 0) tmem_alloc<NCOLS>(&tmem_slot);
+  if (!a.const_weights && tid < COUT) sbias[tid] = a.bias ? a.bias[tid] : 0.0f;
   if constexpr (LD == kLoadAsync) {
     // tile 0 complete and visible to the tensor cores (generic-proxy writes, then the
     // proxy fence, then the barrier before the MMAs are issued)
@@ -437,7 +447,6 @@ __device__ __forceinline__ int mbar_wait_or_abort(uint32_t addr, uint32_t phase,
 
 template <int C1, int C2, int COUT, int EPI>
 __global__ void __launch_bounds__(kWsThreads) conv3x3_ws(const __grid_constant__ ConvMaps maps, ConvArgs a) {
-  agx_pdl_entry();
   constexpr int CIN = C1 + C2, K = 9 * CIN, NG = COUT / 8, NCH = CIN / 8;
   constexpr int B_BYTES = K * COUT * 2;
   constexpr int HALO_BYTES = NCH * kPlaneBytes;
@@ -476,9 +485,17 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_ws(const __grid_constant__
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_flag = 0;
     copies_issued = tiles_consumed = mmas_issued = tiles_drained = 0;
+    // constant weights: their bulk copy overlaps the tail of the kernel before this one
+    if (a.const_weights && my_tiles > 0) {
+      mbar_expect(wbar, (uint32_t)B_BYTES);
+      bulk_load(b0, a.wpk, (uint32_t)B_BYTES, wbar);
+    }
   }
-  if (tid < COUT) sbias[tid] = a.bias ? a.bias[tid] : 0.0f;
+  if (a.const_weights && tid < COUT) sbias[tid] = a.bias ? a.bias[tid] : 0.0f;
   if (warp == 0) tmem_alloc<NCOLS>(&tmem_slot);
+  // the previous kernel's outputs are visible from here on (programmatic dependent launch)
+  agx_pdl_entry();
+  if (!a.const_weights && tid < COUT) sbias[tid] = a.bias ? a.bias[tid] : 0.0f;
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -487,7 +504,7 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_ws(const __grid_constant__
     // ---- producer: the weights once, then the halos through the ring
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&maps.in1)) : "memory");
     if constexpr (C2 > 0) asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&maps.in2)) : "memory");
-    if (my_tiles > 0) {
+    if (!a.const_weights && my_tiles > 0) {
       mbar_expect(wbar, (uint32_t)B_BYTES);
       bulk_load(b0, a.wpk, (uint32_t)B_BYTES, wbar);
     }
@@ -1348,8 +1365,11 @@ extern "C" {
 
 int agx_nn_conv3x3(const void* in1, const void* in2, int c1, int c2, const void* wpk, const float* bias, void* out1,
                    void* out2, int split, int cout, int relu, int B, int H, int W, int* err, void* stream) {
+  if (relu & ~(1 | AGX_NN_CONST_WEIGHTS)) return AGX_ERR_ARG;
+  const int const_weights = (relu & AGX_NN_CONST_WEIGHTS) ? 1 : 0;
+  relu &= 1;
   ConvArgs a{(const __nv_bfloat16*)in1, (const __nv_bfloat16*)in2, (const __nv_bfloat16*)wpk, bias,
-             (__nv_bfloat16*)out1, (__nv_bfloat16*)out2, split, B, H, W, err};
+             (__nv_bfloat16*)out1, (__nv_bfloat16*)out2, split, B, H, W, err, const_weights};
   cudaStream_t s = (cudaStream_t)stream;
   if (!in1 || !wpk || !out1 || !err || B <= 0 || H <= 0 || W <= 0) return AGX_ERR_ARG;
   if (split <= 0 || split > cout || split % 8 || (split < cout && !out2)) return AGX_ERR_ARG;

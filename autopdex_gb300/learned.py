@@ -95,6 +95,9 @@ class UNet:
 
     def pack(self):
         """bf16 operand images of every layer (forward and input-gradient)."""
+        # convolutions may prefetch weights ahead of their predecessor (AGX_NN_CONST_WEIGHTS)
+        # only once a synchronisation has followed the packing (GridPreconditioner sets it)
+        self.const_weights = False
         s = self._stream()
         self.img_f, self.img_b = {}, {}
         for name, c1, c2, co, relu in LAYERS:
@@ -130,8 +133,9 @@ class UNet:
     def _conv(self, name, x1, x2, B, H, W):
         _, c1, c2, co, relu = next(l for l in LAYERS if l[0] == name)
         out = self._act(B, H, W, co, name)
+        flags = relu | (N.AGX_NN_CONST_WEIGHTS if self.const_weights and self._arena is not None else 0)
         rc = self.lib.agx_nn_conv3x3(_p(x1), _p(x2), c1, c2, _p(self.img_f[name]), _p(self.b[name]), _p(out), None,
-                                     co, co, relu, B, H, W, _p(self.err), self._stream())
+                                     co, co, flags, B, H, W, _p(self.err), self._stream())
         self._ok("agx_nn_conv3x3", rc)
         self.launches += 1
         return out
@@ -704,6 +708,7 @@ class GridPreconditioner:
         self.applications = 0
         net.forward(self.img, arena=self.arena)  # allocate the activations once
         torch.cuda.synchronize(dev)
+        net.const_weights = True  # packed and synchronised: later forward passes may prefetch them
 
     def apply_ptr(self, r_ptr, z_ptr, n, stream):
         lib = self.net.lib

@@ -72,6 +72,15 @@ def test_conv_halo_loaders_agree_on_many_tiles(c1, c2):
     torch.cuda.synchronize()
     assert int(err.item()) == 0
     assert torch.equal(outs[0], outs[1]) and torch.equal(outs[0], outs[2])
+    # AGX_NN_CONST_WEIGHTS (weights copied before the programmatic-launch wait): same result;
+    # unknown flag bits are refused
+    out = torch.empty_like(outs[0])
+    assert lib.agx_nn_conv3x3(_ptr(x1d), _ptr(x2d), c1, c2, _ptr(imgf), _ptr(bd), _ptr(out), None, co, co,
+                              1 | N.AGX_NN_CONST_WEIGHTS, B, H, W, _ptr(err), s) == 0
+    assert lib.agx_nn_conv3x3(_ptr(x1d), _ptr(x2d), c1, c2, _ptr(imgf), _ptr(bd), _ptr(out), None, co, co, 1 | 4,
+                              B, H, W, _ptr(err), s) != 0
+    torch.cuda.synchronize()
+    assert torch.equal(outs[0], out)
     xin = torch.cat([x1, x2], -1) if c2 else x1
     ref = onn.conv(xin, w, b.float().double(), 1)
     assert (outs[0].double().cpu() - ref).abs().max() <= 1e-2 * ref.abs().max()
