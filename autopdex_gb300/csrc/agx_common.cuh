@@ -42,6 +42,10 @@ struct agx_element_set {
   // in-range 3 x 3 node stencils; 0 when the set is not such a grid
   int grid_nx = 0, grid_ny = 0;
   bool grid_affine = false;  // every element of the grid is a parallelogram (float64 coordinates)
+  // every element is the same parallelogram (edge vectors equal to 1e-14 of the element size):
+  // grid_m = (M00, M01, M11, det J) of the constant Jacobian J, M = adj(J) adj(J)^T / det J
+  bool grid_uniform = false;
+  double grid_m[4] = {0.0, 0.0, 0.0, 0.0};
 };
 
 // Scalars of one Krylov solve, kept in device memory so that iterations need no host

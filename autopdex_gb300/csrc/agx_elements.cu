@@ -1094,10 +1094,75 @@ void launch_element(agx_context* ctx, agx_element_set& s, const double* dofs, do
   }
 }
 
-// dispatch on (element type, model) for one pass kind
+// ---- float64 residual of the heat potential on a uniform structured quad grid ---------------
+// Every element is the same parallelogram, so its 2 x 2 Gauss-point stiffness per unit
+// coefficient is one 4 x 4 matrix K0 = M00 C00 + M01 C01 + M11 C11 (C.. the point sums of the
+// reference derivative products, M from the constant Jacobian, both as quad_stiffness forms
+// them) and every element's load vector is the source times det J (the four shape functions
+// sum to 1 at each point).  One lane per node adds the four adjacent elements' rows:
+// R_p = sum_e k_e (K0 T_e)_a - f det J, with a the node's place in element e -- one write per
+// node, no atomics, no geometry cache (the element kernel reads ~380 bytes of cached
+// gradients per element).
+__global__ void __launch_bounds__(AGX_BLOCK)
+grid_heat_residual(int nx, int ny, const double* __restrict__ kfield, double src, const double* __restrict__ T,
+                   double M00, double M01, double M11, double det, double* __restrict__ R) {
+  double K0[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      double c00 = 0, c01 = 0, c11 = 0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const double xq = gauss_point(q & 1), yq = gauss_point((q >> 1) & 1);
+        const double fa0 = (1.0 + node_sign<AGX_QUAD4>(a, 0) * xq) * 0.5;
+        const double fa1 = (1.0 + node_sign<AGX_QUAD4>(a, 1) * yq) * 0.5;
+        const double fb0 = (1.0 + node_sign<AGX_QUAD4>(b, 0) * xq) * 0.5;
+        const double fb1 = (1.0 + node_sign<AGX_QUAD4>(b, 1) * yq) * 0.5;
+        const double da0 = node_sign<AGX_QUAD4>(a, 0) * 0.5 * fa1, da1 = node_sign<AGX_QUAD4>(a, 1) * 0.5 * fa0;
+        const double db0 = node_sign<AGX_QUAD4>(b, 0) * 0.5 * fb1, db1 = node_sign<AGX_QUAD4>(b, 1) * 0.5 * fb0;
+        c00 += da0 * db0;
+        c01 += da0 * db1 + da1 * db0;
+        c11 += da1 * db1;
+      }
+      K0[a][b] = M00 * c00 + M01 * c01 + M11 * c11;
+    }
+  const int W = ny + 1;
+  const int64_t n = (int64_t)(nx + 1) * W;
+  const double load = src * det;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(p / W), j = (int)(p - (int64_t)i * W);
+    double acc = 0.0;
+    // the element (ei, ej) = (i - di, j - dj) holds node p at local (di, dj): mesher order
+    // (0, 0) -> 0, (0, 1) -> 1, (1, 1) -> 2, (1, 0) -> 3
+#pragma unroll
+    for (int di = 0; di < 2; ++di)
+#pragma unroll
+      for (int dj = 0; dj < 2; ++dj) {
+        const int ei = i - di, ej = j - dj;
+        if (ei < 0 || ei >= nx || ej < 0 || ej >= ny) continue;
+        const int a = di == 0 ? (dj == 0 ? 0 : 1) : (dj == 0 ? 3 : 2);
+        const int64_t n0 = (int64_t)ei * W + ej;
+        const double t0 = T[n0], t1 = T[n0 + 1], t2 = T[n0 + W + 1], t3 = T[n0 + W];
+        const double ke = kfield ? kfield[(int64_t)ei * ny + ej] : 1.0;
+        acc += ke * (K0[a][0] * t0 + K0[a][1] * t1 + K0[a][2] * t2 + K0[a][3] * t3) - load;
+      }
+    R[p] += acc;
+  }
+}
+
+// dispatch on (element type, model) for one pass kind// dispatch on (element type, model) for one pass kind
 template <typename T, bool DO_R, bool DO_K>
 int dispatch(agx_context* ctx, agx_element_set& s, const double* dofs, double* R, T* vals) {
   if constexpr (std::is_same<T, double>::value && DO_R && !DO_K) {
+    if (s.model == AGX_MODEL_HEAT_POTENTIAL && s.elem_type == AGX_QUAD4 && s.grid_nx > 0 && s.grid_uniform &&
+        s.ngauss == 2 && ctx->ndof == 1) {
+      grid_heat_residual<<<agx_grid(ctx, (int64_t)(s.grid_nx + 1) * (s.grid_ny + 1)), AGX_BLOCK, 0, ctx->stream>>>(
+          s.grid_nx, s.grid_ny, s.d_elem_field, s.params[0], dofs, s.grid_m[0], s.grid_m[1], s.grid_m[2], s.grid_m[3],
+          R);
+      ctx->n_launches += 1;
+      return AGX_OK;
+    }
     if (s.model == AGX_MODEL_NEO_HOOKE && s.d_geo && s.ngauss == 2 &&
         (s.elem_type == AGX_HEX8 || s.elem_type == AGX_QUAD4)) {
       ModelParams mp;

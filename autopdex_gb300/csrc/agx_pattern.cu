@@ -72,6 +72,37 @@ void detect_structured_grid(agx_context* ctx, agx_element_set& s, const std::vec
         std::fabs(x2[0] - x0[0]) + std::fabs(x2[1] - x0[1]) + std::fabs(x1[0] - x3[0]) + std::fabs(x1[1] - x3[1]);
     s.grid_affine = std::fabs(ex) + std::fabs(ey) <= scale * 1e-13;
   }
+  // one parallelogram for the whole grid: the element matrices differ only by their coefficient
+  s.grid_uniform = false;
+  if (s.grid_affine) {
+    auto edges = [&](int64_t e, double* v) {
+      const int32_t* n = c + e * 4;
+      const double* x0 = X + 2 * (int64_t)n[0];
+      const double* x1 = X + 2 * (int64_t)n[1];
+      const double* x3 = X + 2 * (int64_t)n[3];
+      v[0] = x1[0] - x0[0], v[1] = x1[1] - x0[1], v[2] = x3[0] - x0[0], v[3] = x3[1] - x0[1];
+    };
+    double r[4];
+    edges(0, r);
+    const double size = std::fabs(r[0]) + std::fabs(r[1]) + std::fabs(r[2]) + std::fabs(r[3]);
+    bool uni = size > 0.0;
+    for (int64_t e = 1; e < s.n_elem && uni; ++e) {
+      double v[4];
+      edges(e, v);
+      uni = std::fabs(v[0] - r[0]) + std::fabs(v[1] - r[1]) + std::fabs(v[2] - r[2]) + std::fabs(v[3] - r[3]) <=
+            size * 1e-14;
+    }
+    if (uni) {
+      // J = (1/2) [x1 - x0 | x3 - x0] (mesher's node order), as the element kernels form it
+      const double J00 = 0.5 * r[0], J01 = 0.5 * r[2], J10 = 0.5 * r[1], J11 = 0.5 * r[3];
+      const double det = J00 * J11 - J01 * J10;
+      s.grid_uniform = det != 0.0;
+      s.grid_m[0] = (J11 * J11 + J01 * J01) / det;
+      s.grid_m[1] = -(J11 * J10 + J01 * J00) / det;
+      s.grid_m[2] = (J10 * J10 + J00 * J00) / det;
+      s.grid_m[3] = det;
+    }
+  }
 }
 
 }  // namespace
