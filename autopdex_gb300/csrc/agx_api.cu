@@ -505,10 +505,10 @@ int agx_autotune(agx_context* ctx, int* spmv_tpr, float* spmv_ms) {
 int agx_set_tuning(agx_context* ctx, int dtype, int spmv_tpr) {
   if (!ctx) return AGX_ERR_ARG;
   if (dtype != AGX_F64 && dtype != AGX_F32) return agx_fail(ctx, AGX_ERR_ARG, "dtype must be AGX_F64 or AGX_F32");
-  if (spmv_tpr == SPMV_GRID) {
+  if (spmv_is_grid(spmv_tpr)) {
     if (ctx->pattern_grid_ny <= 0)
-      return agx_fail(ctx, AGX_ERR_ARG, "the grid product (512) needs the pattern of a structured QUAD4 grid with 1 "
-                                        "or 2 DOFs per node");
+      return agx_fail(ctx, AGX_ERR_ARG, "the grid products (512, 1024) need the pattern of a structured QUAD4 grid "
+                                        "with 1 or 2 DOFs per node");
     ctx->spmv_tpr[dtype == AGX_F32 ? 1 : 0] = spmv_tpr;
     return AGX_OK;
   }
@@ -518,7 +518,7 @@ int agx_set_tuning(agx_context* ctx, int dtype, int spmv_tpr) {
   const bool unroll_ok = unroll4 == 1 && (lanes == 2 || lanes == 4 || lanes == 8);
   if (!plain_ok && !unroll_ok)
     return agx_fail(ctx, AGX_ERR_ARG, "lanes per row must be 0, 1, 2, 4, 8 or 16 (2, 4 or 8 with 256 added for four "
-                                      "blocks per lane and trip; 512 the structured grid's product)");
+                                      "blocks per lane and trip; 512 / 1024 the structured grid's product with one / two rows per lane)");
   if (ctx->ndof == 3 && spmv_tpr != 0 && lanes < 4)
     return agx_fail(ctx, AGX_ERR_ARG, "3 DOFs per node need 4 or more lanes per row");
   ctx->spmv_tpr[dtype == AGX_F32 ? 1 : 0] = spmv_tpr;

@@ -67,10 +67,14 @@ struct agx_krylov_scalars {
 
 // Krylov product variant codes: lanes per block row (1, 2, 4, 8, 16), plus SPMV_UNROLL4 for
 // four blocks per lane and trip (2, 4, 8 lanes); SPMV_GRID the structured grid's index-free
-// product (one lane per row, 1 or 2 DOFs per node)
+// product (one lane per row, 1 or 2 DOFs per node), SPMV_GRID2 the same with two rows per lane
 constexpr int SPMV_UNROLL4 = 256;
 constexpr int SPMV_GRID = 512;
-inline int spmv_lanes(int code) { return code == SPMV_GRID ? 1 : (code & (SPMV_UNROLL4 - 1)); }
+constexpr int SPMV_GRID2 = 1024;  // the grid product with two rows per lane
+inline int spmv_lanes(int code) {
+  return (code == SPMV_GRID || code == SPMV_GRID2) ? 1 : (code & (SPMV_UNROLL4 - 1));
+}
+inline bool spmv_is_grid(int code) { return code == SPMV_GRID || code == SPMV_GRID2; }
 
 struct agx_context {
   cudaStream_t stream = nullptr;

@@ -242,13 +242,14 @@ __device__ __forceinline__ void grid_row(int64_t row, int ny, int64_t n_rows, co
 }
 
 // A product row in the tangent's storage: U > 0 the node-block CSR with TPR lanes per row,
-// U == 0 the structured grid's stencil (one lane per row, gny = ny)
+// U <= 0 the structured grid's stencil (one lane per row, gny = ny; U == -2: the kernels give
+// each lane two consecutive rows, whose loads are then in flight together)
 template <typename T, int NDOF, int TPR, bool DIR, int U, typename VT = T>
 __device__ __forceinline__ void tangent_row(int64_t row, int sub, const int32_t* __restrict__ rowptr,
                                             const int32_t* __restrict__ col, const VT* __restrict__ vals,
                                             int64_t nnzb, int64_t n_rows, int gny, const T* __restrict__ x,
                                             const T* __restrict__ pold, T beta, T (&y)[NDOF]) {
-  if constexpr (U == 0) {
+  if constexpr (U <= 0) {  // 0: one row per lane, -2: two rows per lane (the kernels' loops)
     static_assert(TPR == 1, "the grid product has one lane per row");
     grid_row<T, NDOF, DIR, VT>(row, gny, n_rows, vals, nnzb, x, pold, beta, y);
   } else {
@@ -261,16 +262,25 @@ __global__ void __launch_bounds__(AGX_BLOCK) spmv_kernel(int64_t n_rows, const i
                                                          const int32_t* __restrict__ col, const T* __restrict__ vals,
                                                          int64_t nnzb, int gny, const T* __restrict__ x,
                                                          T* __restrict__ y) {
+  constexpr int RPT = U == -2 ? 2 : 1;  // rows per lane
   const int sub = threadIdx.x % TPR;
-  const int64_t total = ((n_rows * TPR + 31) / 32) * 32;
+  const int64_t total = (((n_rows + RPT - 1) / RPT * TPR + 31) / 32) * 32;
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t row = L / TPR;
-    T yr[NDOF];
-    tangent_row<T, NDOF, TPR, false, U>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, n_rows, gny,
-                                        x, nullptr, T(0), yr);
-    if (row < n_rows && sub == 0) {
+    const int64_t r0 = (L / TPR) * RPT;
+    T yr[RPT][NDOF];
 #pragma unroll
-      for (int i = 0; i < NDOF; ++i) y[row * NDOF + i] = yr[i];
+    for (int rr = 0; rr < RPT; ++rr) {
+      const int64_t row = r0 + rr;
+      tangent_row<T, NDOF, TPR, false, U>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, n_rows,
+                                          gny, x, nullptr, T(0), yr[rr]);
+    }
+#pragma unroll
+    for (int rr = 0; rr < RPT; ++rr) {
+      const int64_t row = r0 + rr;
+      if (row < n_rows && sub == 0) {
+#pragma unroll
+        for (int i = 0; i < NDOF; ++i) y[row * NDOF + i] = yr[rr][i];
+      }
     }
   }
 }
@@ -286,23 +296,32 @@ spmv_dot_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_
   agx_pdl_entry();
   if (sc->converged) return;
   const T beta = (T)sc->beta;
+  constexpr int RPT = U == -2 ? 2 : 1;  // rows per lane
   const int sub = threadIdx.x % TPR;
-  const int64_t total = ((n_rows * TPR + 31) / 32) * 32;
+  const int64_t total = (((n_rows + RPT - 1) / RPT * TPR + 31) / 32) * 32;
   T acc_t = 0, accr_t = 0;  // per-thread partials in T (a few rows), block and grid sums in float64
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t row = L / TPR;
-    T yr[NDOF];
-    tangent_row<T, NDOF, TPR, true, U>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, n_rows, gny, z,
-                                       pold, beta, yr);
-    if (row < n_rows && sub == 0) {
+    const int64_t r0 = (L / TPR) * RPT;
+    T yr[RPT][NDOF];
 #pragma unroll
-      for (int i = 0; i < NDOF; ++i) {
-        const int64_t d = row * NDOF + i;
-        const T pn = z[d] + beta * pold[d];
-        pnew[d] = pn;
-        q[d] = yr[i];
-        acc_t += yr[i] * pn;
-        if (rflex) accr_t += rflex[d] * pn;
+    for (int rr = 0; rr < RPT; ++rr) {
+      const int64_t row = r0 + rr;
+      tangent_row<T, NDOF, TPR, true, U>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb, n_rows, gny,
+                                         z, pold, beta, yr[rr]);
+    }
+#pragma unroll
+    for (int rr = 0; rr < RPT; ++rr) {
+      const int64_t row = r0 + rr;
+      if (row < n_rows && sub == 0) {
+#pragma unroll
+        for (int i = 0; i < NDOF; ++i) {
+          const int64_t d = row * NDOF + i;
+          const T pn = z[d] + beta * pold[d];
+          pnew[d] = pn;
+          q[d] = yr[rr][i];
+          acc_t += yr[rr][i] * pn;
+          if (rflex) accr_t += rflex[d] * pn;
+        }
       }
     }
   }
@@ -677,31 +696,40 @@ tl_spmv(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __res
         float* __restrict__ tout, agx_krylov_scalars* sc, double* __restrict__ partials) {
   agx_pdl_entry();
   if (sc->converged) return;
+  constexpr int RPT = U == -2 ? 2 : 1;  // rows per lane
   const int sub = threadIdx.x % TPR;
-  const int64_t total = ((n_rows * TPR + 31) / 32) * 32;
+  const int64_t total = (((n_rows + RPT - 1) / RPT * TPR + 31) / 32) * 32;
   float acc_a = 0.0f, acc_b = 0.0f;
   for (int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t row = L / TPR;
-    float yr[NDOF];
-    tangent_row<float, NDOF, TPR, false, U, VT>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb,
-                                                n_rows, gny, x, nullptr, 0.0f, yr);
-    if (row < n_rows && sub == 0) {
+    const int64_t r0 = (L / TPR) * RPT;
+    float yr[RPT][NDOF];
 #pragma unroll
-      for (int i = 0; i < NDOF; ++i) {
-        const int64_t d = row * NDOF + i;
-        const float t = yr[i];
-        if constexpr (EPI == TL_SWEEP) {
-          const float r = rc[d] - t;
-          rc[d] = r;
-          const float dn = (a != 0.0f ? a * x[d] : 0.0f) + b * dinv[d] * r;
-          dnew[d] = dn;
-          z[d] += dn;
-        } else if constexpr (EPI == TL_RESID) {
-          rc[d] -= t;
-        } else {
-          tout[d] = t;
-          acc_a += rc[d] * x[d];
-          acc_b += x[d] * t;
+    for (int rr = 0; rr < RPT; ++rr) {
+      const int64_t row = r0 + rr;
+      tangent_row<float, NDOF, TPR, false, U, VT>(row < n_rows ? row : n_rows - 1, sub, rowptr, col, vals, nnzb,
+                                                  n_rows, gny, x, nullptr, 0.0f, yr[rr]);
+    }
+#pragma unroll
+    for (int rr = 0; rr < RPT; ++rr) {
+      const int64_t row = r0 + rr;
+      if (row < n_rows && sub == 0) {
+#pragma unroll
+        for (int i = 0; i < NDOF; ++i) {
+          const int64_t d = row * NDOF + i;
+          const float t = yr[rr][i];
+          if constexpr (EPI == TL_SWEEP) {
+            const float r = rc[d] - t;
+            rc[d] = r;
+            const float dn = (a != 0.0f ? a * x[d] : 0.0f) + b * dinv[d] * r;
+            dnew[d] = dn;
+            z[d] += dn;
+          } else if constexpr (EPI == TL_RESID) {
+            rc[d] -= t;
+          } else {
+            tout[d] = t;
+            acc_a += rc[d] * x[d];
+            acc_b += x[d] * t;
+          }
         }
       }
     }
@@ -999,6 +1027,9 @@ int spmv_dot_nd(agx_context* ctx, int tpr, const T* vals, const T* z, const T* p
     case SPMV_GRID:
       if constexpr (ND <= 2) return spmv_dot_variant<T, ND, 1, 0>(ctx, vals, z, pold, pnew, q, rflex);
       [[fallthrough]];
+    case SPMV_GRID2:
+      if constexpr (ND <= 2) return spmv_dot_variant<T, ND, 1, -2>(ctx, vals, z, pold, pnew, q, rflex);
+      [[fallthrough]];
     default: return spmv_dot_variant<T, ND, 8>(ctx, vals, z, pold, pnew, q, rflex);
   }
 }
@@ -1180,7 +1211,10 @@ int agx_autotune_spmv(agx_context* ctx, int* chosen, float* best_ms) {
     return agx_fail(ctx, AGX_ERR_STATE, "autotune needs an assembled tangent");
   const bool f32 = ctx->tangent_valid == AGX_F32;
   std::vector<int> cands = {1, 2, 4, 8, 16, 2 | SPMV_UNROLL4, 4 | SPMV_UNROLL4, 8 | SPMV_UNROLL4};
-  if (ctx->pattern_grid_ny > 0) cands.push_back(SPMV_GRID);
+  if (ctx->pattern_grid_ny > 0) {
+    cands.push_back(SPMV_GRID);
+    cands.push_back(SPMV_GRID2);
+  }
   cudaEvent_t e0, e1;
   AGX_CUDA(ctx, cudaEventCreate(&e0));
   AGX_CUDA(ctx, cudaEventCreate(&e1));
@@ -1266,6 +1300,12 @@ void spmv_nd(agx_context* ctx, int tpr, int g, const T* v, const T* x, T* y) {
         break;
       }
       [[fallthrough]];
+    case SPMV_GRID2:
+      if constexpr (ND <= 2) {
+        spmv_kernel<T, ND, 1, -2><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, gny, x, y);
+        break;
+      }
+      [[fallthrough]];
     default: spmv_kernel<T, ND, 8><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, gny, x, y); break;
   }
 }
@@ -1346,6 +1386,12 @@ void tl_spmv_nd(agx_context* ctx, int code, int g, const VT* vals, const float* 
     case SPMV_GRID:
       if constexpr (ND <= 2) {
         AGX_TL(1, 0);
+        break;
+      }
+      [[fallthrough]];
+    case SPMV_GRID2:
+      if constexpr (ND <= 2) {
+        AGX_TL(1, -2);
         break;
       }
       [[fallthrough]];

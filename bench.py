@@ -340,7 +340,7 @@ def headline_roofline(h):
     # the vectors (fused Krylov product: z, p_old read, p_new, q written; plain product: x, y);
     # the structured grid's product (code 512) reads no row pointers or column indices
     tpr = getattr(prob, "spmv_tpr", 0)
-    grid = tpr == 512
+    grid = tpr in (512, 1024)
     matrix = nnzb * ndof * ndof * s if grid else nnzb * (ndof * ndof * s + 4) + 4 * (n_nodes + 1)
     fused = matrix + 4 * n * s
     # the two-level products carry their element-wise work: per application 2 (nu - 1) sweep
@@ -351,7 +351,7 @@ def headline_roofline(h):
     plain = matrix + n * s * (2 * (nu - 1) * 7 + 3 + 3) / (2 * (nu - 1) + 2)
     hc = h["w"].raw["n"] // h["factor"] + 1
     flops = _network_flops(learned.padded(hc), learned.padded(hc))
-    var = "grid" if grid else f"bsr, {tpr} lanes per row"
+    var = ("grid, 2 rows per lane" if tpr == 1024 else "grid") if grid else f"bsr, {tpr} lanes per row"
     cand = {"smoothing_product": ("hbm", plain, f"tl_spmv<1,{var}> (two-level smoothing, residual and step products "
                                                 "with their element-wise work fused)"),
             "krylov_product": ("hbm", fused, f"spmv_dot_kernel<float,1,{var}> (FCG product with direction update "

@@ -275,8 +275,8 @@ int agx_pcg_noalloc(const int32_t* rowptr, const int32_t* col, const double* val
    with two blocks per lane and trip, 2, 4, 8 lanes with four blocks (code lanes + 256), and,
    when the pattern is the 3 x 3 stencil of a structured QUAD4 grid with 1 or 2 DOFs per node,
    the grid product that computes each row's block offsets and columns instead of reading them
-   (code 512) -- on the last assembled tangent (CUDA events), keeps the fastest for that
-   tangent's precision and reports its code. */
+   (code 512; 1024 with two rows per lane) -- on the last assembled tangent (CUDA events),
+   keeps the fastest for that tangent's precision and reports its code. */
 int agx_autotune(agx_context* ctx, int* spmv_tpr, float* spmv_ms);
 /* Applies a tuning decision for the float64 (AGX_F64) or float32 (AGX_F32) product, e.g. from
    the autotuner's cache; 0 restores the default. */
@@ -286,8 +286,8 @@ int agx_set_tuning(agx_context* ctx, int dtype, int spmv_tpr);
    before it and then lets the next one launch, so the next kernel's blocks are scheduled while
    the current one runs.  0 launches them plainly (same results). */
 int agx_set_pdl(int enable);
-/* ny of the structured QUAD4 grid whose 3 x 3 stencil the pattern is (the grid product, code
-   512, applies), else 0; for keys of a tuning cache. */
+/* ny of the structured QUAD4 grid whose 3 x 3 stencil the pattern is (the grid products,
+   codes 512 and 1024, apply), else 0; for keys of a tuning cache. */
 int agx_grid_pattern(const agx_context* ctx, int* ny);
 /* Number of kernels this context has launched since it was created. */
 int agx_launch_count(const agx_context* ctx, int64_t* launches);

@@ -1,6 +1,6 @@
 """The autotuner's SpMV variants (1, 2, 4, 8 or 16 lanes per block row with two blocks per lane
 and trip; 2, 4 or 8 lanes with four blocks, code lanes + 256; on a structured QUAD4 grid the
-index-free grid product, code 512) solve identically, the autotuner picks one of them per
+index-free grid product, code 512, or with two rows per lane, 1024) solve identically, the autotuner picks one of them per
 precision, and invalid tuning values are rejected.
 
 Tolerances, written where used: float64 products of one variant against SciPy's CSR product of
@@ -18,7 +18,7 @@ from autopdex_gb300._problem import get_problem
 
 pytestmark = pytest.mark.gpu
 
-VARIANTS = (1, 2, 4, 8, 16, 2 + 256, 4 + 256, 8 + 256, 512)  # 512: the heat problems' structured grid
+VARIANTS = (1, 2, 4, 8, 16, 2 + 256, 4 + 256, 8 + 256, 512, 1024)  # 512, 1024: the structured grid's products
 
 
 def _solve(prob, rhs, method):
@@ -97,7 +97,7 @@ def test_grid_product_matches_scipy(case):
         A = sps.bsr_matrix((blocks, col.cpu().numpy(), rowptr.cpu().numpy()), shape=(prob.n_dofs, prob.n_dofs))
         x = torch.as_tensor(rng.standard_normal(prob.n_dofs), device=prob.device).to(tdt)
         ref = A @ x.double().cpu().numpy()
-        for code in (512, 4):
+        for code in (512, 1024, 4):
             prob._call("agx_set_tuning", dtype, code)
             y = torch.empty_like(x)
             prob._call("agx_spmv", dtype, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()))
@@ -118,5 +118,5 @@ def test_autotuner_times_real_products():
         tpr = C.c_int()
         ms = C.c_float()
         prob._call("agx_autotune", C.byref(tpr), C.byref(ms))
-        matrix_bytes = prob.nnzb * (s + (0 if tpr.value == 512 else 4))  # the grid product reads no indices
+        matrix_bytes = prob.nnzb * (s + (0 if tpr.value in (512, 1024) else 4))  # the grid products read no indices
         assert ms.value * 1e-3 >= matrix_bytes / 8e12, (dtype, tpr.value, ms.value)
