@@ -176,7 +176,7 @@ def _heat_variants():
     return [("plain_fp64_pcg", dict(precision="float64", solver="pcg"), dict(krylov_tol=1e-11)),
             ("mixed_pcg", dict(precision="mixed", solver="pcg"), dict(krylov_tol=1e-5)),
             ("learned_mixed_fcg", dict(precision="mixed", solver="fcg", **{"type of preconditioner": "learned"}),
-             dict(krylov_tol=1e-4))]
+             dict(krylov_tol=1e-3))]
 
 
 BF16_SMOOTHING = False  # --bf16-smoothing: the two-level products on a bf16 copy of the values
@@ -716,7 +716,7 @@ def gpu_arm(args):
         "dtype": "f32 FCG + bf16 network + f64 residual/refinement",
         "data": "synthetic (seeded Gaussian random field conductivity; no dataset)",
         "config": {"workload": f"heat_grf_{n}x{n}_q1_seed10000", "n_dofs": h["w"].n_dofs, "newton_rtol": RTOL,
-                   "krylov": "flexible CG (float32) with the U-Net two-level preconditioner, inner rtol 1e-4",
+                   "krylov": "flexible CG (float32) with the U-Net two-level preconditioner, inner rtol 1e-3",
                    "network_grid": f"{n // h['factor'] + 1}^2 (coarsening {h['factor']})",
                    "l2": "256 MB buffer written before every timed step", "krylov_chunks": "CUDA graphs",
                    "parallelism": "replicas" if world > 1 else "1 gpu"},
