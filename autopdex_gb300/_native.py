@@ -87,6 +87,8 @@ _SIGNATURES = {
     "agx_set_tuning": (C.c_int, [_P, C.c_int, C.c_int]),
     "agx_grid_pattern": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "agx_set_pdl": (C.c_int, [C.c_int]),
+    "agx_solve_flag": (C.c_int, [_P, C.POINTER(_P)]),
+    "agx_nn_set_skip_flag": (C.c_int, [_P]),
     "agx_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
 "agx_pcg_noalloc": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int, _P, _P, C.c_double, C.c_int, _P,
                                 C.POINTER(SolveInfo), C.c_char_p, C.c_int]),

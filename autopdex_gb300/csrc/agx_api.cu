@@ -530,6 +530,13 @@ int agx_set_pdl(int enable) {
   return AGX_OK;
 }
 
+int agx_solve_flag(agx_context* ctx, const int** flag) {
+  if (!ctx || !flag) return AGX_ERR_ARG;
+  if (!ctx->d_scal) return agx_fail(ctx, AGX_ERR_STATE, "no solve state before agx_finalize");
+  *flag = &ctx->d_scal->converged;
+  return AGX_OK;
+}
+
 int agx_grid_pattern(const agx_context* ctx, int* ny) {
   if (!ctx || !ny) return AGX_ERR_ARG;
   *ny = ctx->pattern_grid_ny;

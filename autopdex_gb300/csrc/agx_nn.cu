@@ -28,6 +28,12 @@ namespace {
 
 namespace cg = cooperative_groups;
 
+// agx_nn_set_skip_flag: a device int that the inference kernels read after their
+// programmatic-launch wait; nonzero makes them return at once (passed to every launch, so a
+// captured graph keeps it)
+const int* g_nn_skip = nullptr;
+__device__ __forceinline__ bool nn_skip(const int* skip) { return skip && __ldcg(skip) != 0; }
+
 constexpr int kTile = 128;        // output pixels per CTA (MMA M)
 constexpr int kWaitLimit = 1 << 22;
 
@@ -112,6 +118,7 @@ struct ConvArgs {
   int B, H, W;
   int* err;
   int const_weights;         // weights and bias not written by the kernel just before this one
+  const int* skip;           // nonzero there: return at once (the solve using the network has converged)
 };
 
 // out = epi(conv3x3(concat(in1, in2)) + bias); EPI 0: identity, 1: ReLU.
@@ -293,6 +300,14 @@ __global__ void __launch_bounds__(kTile) conv3x3_tc(const __grid_constant__ Conv
   if (warp == 0) tmem_alloc<NCOLS>(&tmem_slot);
   // the previous kernel's outputs are visible from here on (programmatic dependent launch)
   agx_pdl_entry();
+  if (nn_skip(a.skip)) {  // release what the prologue took: the weight copy in flight, TMEM
+    if (tid == 0 && a.const_weights && my_tiles > 0) mbar_wait(wbar, 0u);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 0) tmem_free<NCOLS>(tmem_slot);
+    return;
+  }
   if (tid == 0) {
     // the packed weights (already in core-matrix order) in one bulk copy, in flight together
     // with the first kStages halos
@@ -495,6 +510,14 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_ws(const __grid_constant__
   if (warp == 0) tmem_alloc<NCOLS>(&tmem_slot);
   // the previous kernel's outputs are visible from here on (programmatic dependent launch)
   agx_pdl_entry();
+  if (nn_skip(a.skip)) {  // release what the prologue took: the weight copy in flight, TMEM
+    if (tid == 0 && a.const_weights && my_tiles > 0) mbar_wait(wbar, 0u);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 0) tmem_free<NCOLS>(tmem_slot);
+    return;
+  }
   if (!a.const_weights && tid < COUT) sbias[tid] = a.bias ? a.bias[tid] : 0.0f;
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -836,8 +859,9 @@ __device__ __forceinline__ uint4 bf16x8_pack(const float* a, float scale) {
 // 0 for a runtime f; C8 = 4 (32 channels) is the U-Net's hidden width
 template <int F>
 __global__ void block_sum_kernel(const uint4* __restrict__ fine, uint4* __restrict__ coarse, int B, int H, int W,
-                                 int C8, int f_rt, float scale) {
+                                 int C8, int f_rt, float scale, const int* skip) {
   agx_pdl_entry();
+  if (nn_skip(skip)) return;
   const int f = F > 0 ? F : f_rt;
   const int Ho = H / f, Wo = W / f;
   const int64_t total = (int64_t)B * Ho * Wo * C8;
@@ -868,8 +892,9 @@ __global__ void block_sum_kernel(const uint4* __restrict__ fine, uint4* __restri
 
 template <int F>
 __global__ void block_bcast_kernel(const uint4* __restrict__ coarse, uint4* __restrict__ fine, int B, int H, int W,
-                                   int C8, int f_rt, float scale) {
+                                   int C8, int f_rt, float scale, const int* skip) {
   agx_pdl_entry();
+  if (nn_skip(skip)) return;
   const int f = F > 0 ? F : f_rt;
   const int Ho = H / f, Wo = W / f;
   const int64_t total = (int64_t)B * H * W * C8;
@@ -944,8 +969,9 @@ __global__ void bias_grad_kernel(const __nv_bfloat16* __restrict__ g, int64_t P,
 // nd .. nd+naux-1 the per-node features aux[node naux + a], zeros elsewhere
 __global__ void grid_from_field_kernel(const float* __restrict__ r, int nd, const float* __restrict__ aux, int naux,
                                        const float* __restrict__ scale, int Hn, int Wn, int Hp, int Wp,
-                                       __nv_bfloat16* __restrict__ img) {
+                                       __nv_bfloat16* __restrict__ img, const int* skip) {
   agx_pdl_entry();
+  if (nn_skip(skip)) return;
   const int64_t total = (int64_t)Hp * Wp;
   const float s = scale ? scale[0] : 1.0f;
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < total; p += (int64_t)gridDim.x * blockDim.x) {
@@ -967,8 +993,9 @@ __global__ void grid_from_field_kernel(const float* __restrict__ r, int nd, cons
 
 // channels 0 .. nd-1 of an NHWC image with C channels -> node field z[node nd + c]
 __global__ void field_from_grid_kernel(const __nv_bfloat16* __restrict__ img, int C, int nd, int Hn, int Wn, int Wp,
-                                       float* __restrict__ z) {
+                                       float* __restrict__ z, const int* skip) {
   agx_pdl_entry();
+  if (nn_skip(skip)) return;
   const int64_t total = (int64_t)Hn * Wn * nd;
   for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d < total; d += (int64_t)gridDim.x * blockDim.x) {
     const int64_t node = d / nd;
@@ -1093,8 +1120,9 @@ constexpr int kRestrictBlocks = 1024;  // largest grid of restrict_sq_kernel (pa
 template <int F>
 __global__ void __launch_bounds__(256)
 restrict_sq_kernel(const float* __restrict__ fine, const unsigned char* __restrict__ fixed, int nd, int Hc, int Wc,
-                   int f_rt, float* __restrict__ out, double* __restrict__ partials) {
+                   int f_rt, float* __restrict__ out, double* __restrict__ partials, const int* skip) {
   agx_pdl_entry();
+  if (nn_skip(skip)) return;
   const int f = F > 0 ? F : f_rt;
   const int Hf = (Hc - 1) * f + 1, Wf = (Wc - 1) * f + 1;
   const int total = Hc * Wc * nd;
@@ -1155,8 +1183,9 @@ restrict_sq_kernel(const float* __restrict__ fine, const unsigned char* __restri
 __global__ void __launch_bounds__(256)
 image_from_coarse_kernel(const float* __restrict__ r, int nd, const float* __restrict__ aux, int naux,
                          const double* __restrict__ partials, int np, int64_t n, float* __restrict__ scale, int Hn,
-                         int Wn, int Hp, int Wp, __nv_bfloat16* __restrict__ img) {
+                         int Wn, int Hp, int Wp, __nv_bfloat16* __restrict__ img, const int* skip) {
   agx_pdl_entry();
+  if (nn_skip(skip)) return;
   __shared__ double sh[8];
   __shared__ float s_sh;
   double v = 0.0;
@@ -1195,8 +1224,9 @@ image_from_coarse_kernel(const float* __restrict__ r, int nd, const float* __res
 template <int F>
 __global__ void __launch_bounds__(256)
 prolong_image_kernel(const __nv_bfloat16* __restrict__ img, int C, int nd, int Hc, int Wc, int Wp, int f_rt,
-                     const unsigned char* __restrict__ fixed, float* __restrict__ out) {
+                     const unsigned char* __restrict__ fixed, float* __restrict__ out, const int* skip) {
   agx_pdl_entry();
+  if (nn_skip(skip)) return;
   const int f = F > 0 ? F : f_rt;
   const int Wf = (Wc - 1) * f + 1;
   const int i = blockIdx.y;
@@ -1344,9 +1374,9 @@ void launch_block_sum(const void* fine, void* coarse, int B, int H, int W, int C
   const int g = grid1((int64_t)B * (H / f) * (W / f) * (C / 8));
   const uint4* in = (const uint4*)fine;
   uint4* out = (uint4*)coarse;
-  if (f == 2) agx_launch_pdl(block_sum_kernel<2>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale);
-  else if (f == 4) agx_launch_pdl(block_sum_kernel<4>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale);
-  else agx_launch_pdl(block_sum_kernel<0>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale);
+  if (f == 2) agx_launch_pdl(block_sum_kernel<2>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale, g_nn_skip);
+  else if (f == 4) agx_launch_pdl(block_sum_kernel<4>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale, g_nn_skip);
+  else agx_launch_pdl(block_sum_kernel<0>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale, g_nn_skip);
 }
 
 void launch_block_bcast(const void* coarse, void* fine, int B, int H, int W, int C, int f, float scale,
@@ -1354,9 +1384,9 @@ void launch_block_bcast(const void* coarse, void* fine, int B, int H, int W, int
   const int g = grid1((int64_t)B * H * W * (C / 8));
   const uint4* in = (const uint4*)coarse;
   uint4* out = (uint4*)fine;
-  if (f == 2) agx_launch_pdl(block_bcast_kernel<2>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale);
-  else if (f == 4) agx_launch_pdl(block_bcast_kernel<4>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale);
-  else agx_launch_pdl(block_bcast_kernel<0>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale);
+  if (f == 2) agx_launch_pdl(block_bcast_kernel<2>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale, g_nn_skip);
+  else if (f == 4) agx_launch_pdl(block_bcast_kernel<4>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale, g_nn_skip);
+  else agx_launch_pdl(block_bcast_kernel<0>, g, 256, 0, s, in, out, B, H, W, C / 8, f, scale, g_nn_skip);
 }
 
 }  // namespace
@@ -1369,7 +1399,7 @@ int agx_nn_conv3x3(const void* in1, const void* in2, int c1, int c2, const void*
   const int const_weights = (relu & AGX_NN_CONST_WEIGHTS) ? 1 : 0;
   relu &= 1;
   ConvArgs a{(const __nv_bfloat16*)in1, (const __nv_bfloat16*)in2, (const __nv_bfloat16*)wpk, bias,
-             (__nv_bfloat16*)out1, (__nv_bfloat16*)out2, split, B, H, W, err, const_weights};
+             (__nv_bfloat16*)out1, (__nv_bfloat16*)out2, split, B, H, W, err, const_weights, g_nn_skip};
   cudaStream_t s = (cudaStream_t)stream;
   if (!in1 || !wpk || !out1 || !err || B <= 0 || H <= 0 || W <= 0) return AGX_ERR_ARG;
   if (split <= 0 || split > cout || split % 8 || (split < cout && !out2)) return AGX_ERR_ARG;
@@ -1387,6 +1417,11 @@ int agx_nn_conv3x3(const void* in1, const void* in2, int c1, int c2, const void*
   AGX_CONV(16, 0, 32, 0)
 #undef AGX_CONV
   return AGX_ERR_UNSUPPORTED;
+}
+
+int agx_nn_set_skip_flag(const int* flag) {
+  g_nn_skip = flag;
+  return AGX_OK;
 }
 
 int agx_nn_set_halo_loader(int loader) {
@@ -1487,8 +1522,7 @@ int agx_nn_grid_from_field(const float* r, int nd, const float* aux, int naux, i
   cudaStream_t s = (cudaStream_t)stream;
   if (normalize) inv_rms_kernel<<<kRmsCluster, 1024, 0, s>>>(r, (int64_t)Hn * Wn * nd, scale);
   agx_launch_pdl(grid_from_field_kernel, grid1((int64_t)Hp * Wp), 256, 0, s, r, nd, naux > 0 ? aux : nullptr, naux,
-                                                                 normalize ? scale : nullptr, Hn, Wn, Hp, Wp,
-                                                                 (__nv_bfloat16*)img);
+                 normalize ? scale : nullptr, Hn, Wn, Hp, Wp, (__nv_bfloat16*)img, g_nn_skip);
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
 }
 
@@ -1505,14 +1539,13 @@ int agx_nn_restrict_image(const float* fine, const unsigned char* fixed, int nd,
   const int64_t total = (int64_t)Hc * Wc * nd;
   const int nb = (int)std::min<int64_t>(kRestrictBlocks, (total + 255) / 256);
   switch (f) {
-    case 2: agx_launch_pdl(restrict_sq_kernel<2>, nb, 256, 0, s, fine, fixed, nd, Hc, Wc, f, coarse, work); break;
-    case 4: agx_launch_pdl(restrict_sq_kernel<4>, nb, 256, 0, s, fine, fixed, nd, Hc, Wc, f, coarse, work); break;
-    case 8: agx_launch_pdl(restrict_sq_kernel<8>, nb, 256, 0, s, fine, fixed, nd, Hc, Wc, f, coarse, work); break;
-    default: agx_launch_pdl(restrict_sq_kernel<0>, nb, 256, 0, s, fine, fixed, nd, Hc, Wc, f, coarse, work); break;
+    case 2: agx_launch_pdl(restrict_sq_kernel<2>, nb, 256, 0, s, fine, fixed, nd, Hc, Wc, f, coarse, work, g_nn_skip); break;
+    case 4: agx_launch_pdl(restrict_sq_kernel<4>, nb, 256, 0, s, fine, fixed, nd, Hc, Wc, f, coarse, work, g_nn_skip); break;
+    case 8: agx_launch_pdl(restrict_sq_kernel<8>, nb, 256, 0, s, fine, fixed, nd, Hc, Wc, f, coarse, work, g_nn_skip); break;
+    default: agx_launch_pdl(restrict_sq_kernel<0>, nb, 256, 0, s, fine, fixed, nd, Hc, Wc, f, coarse, work, g_nn_skip); break;
   }
-  agx_launch_pdl(image_from_coarse_kernel, grid1((int64_t)Hp * Wp), 256, 0, s, coarse, nd, naux > 0 ? aux : nullptr, naux, work,
-                                                                    nb, total, scale, Hc, Wc, Hp, Wp,
-                                                                    (__nv_bfloat16*)img);
+  agx_launch_pdl(image_from_coarse_kernel, grid1((int64_t)Hp * Wp), 256, 0, s, coarse, nd, naux > 0 ? aux : nullptr,
+                 naux, work, nb, total, scale, Hc, Wc, Hp, Wp, (__nv_bfloat16*)img, g_nn_skip);
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
 }
 
@@ -1525,10 +1558,10 @@ int agx_nn_prolong_image(const void* img, int C, int nd, int Hc, int Wc, int Wp,
   cudaStream_t s = (cudaStream_t)stream;
   const __nv_bfloat16* im = (const __nv_bfloat16*)img;
   switch (f) {
-    case 2: agx_launch_pdl(prolong_image_kernel<2>, grid, 256, 0, s, im, C, nd, Hc, Wc, Wp, f, fixed, fine); break;
-    case 4: agx_launch_pdl(prolong_image_kernel<4>, grid, 256, 0, s, im, C, nd, Hc, Wc, Wp, f, fixed, fine); break;
-    case 8: agx_launch_pdl(prolong_image_kernel<8>, grid, 256, 0, s, im, C, nd, Hc, Wc, Wp, f, fixed, fine); break;
-    default: agx_launch_pdl(prolong_image_kernel<0>, grid, 256, 0, s, im, C, nd, Hc, Wc, Wp, f, fixed, fine); break;
+    case 2: agx_launch_pdl(prolong_image_kernel<2>, grid, 256, 0, s, im, C, nd, Hc, Wc, Wp, f, fixed, fine, g_nn_skip); break;
+    case 4: agx_launch_pdl(prolong_image_kernel<4>, grid, 256, 0, s, im, C, nd, Hc, Wc, Wp, f, fixed, fine, g_nn_skip); break;
+    case 8: agx_launch_pdl(prolong_image_kernel<8>, grid, 256, 0, s, im, C, nd, Hc, Wc, Wp, f, fixed, fine, g_nn_skip); break;
+    default: agx_launch_pdl(prolong_image_kernel<0>, grid, 256, 0, s, im, C, nd, Hc, Wc, Wp, f, fixed, fine, g_nn_skip); break;
   }
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
 }
@@ -1562,8 +1595,8 @@ int agx_nn_vector_from_grid(const void* img, int C, int Hn, int Wn, int Wp, floa
 
 int agx_nn_field_from_grid(const void* img, int C, int nd, int Hn, int Wn, int Wp, float* z, void* stream) {
   if (!img || !z || nd < 1 || nd > C || Wn > Wp) return AGX_ERR_ARG;
-  agx_launch_pdl(field_from_grid_kernel, grid1((int64_t)Hn * Wn * nd), 256, 0, (cudaStream_t)stream, (const __nv_bfloat16*)img, C,
-                                                                                        nd, Hn, Wn, Wp, z);
+  agx_launch_pdl(field_from_grid_kernel, grid1((int64_t)Hn * Wn * nd), 256, 0, (cudaStream_t)stream,
+                 (const __nv_bfloat16*)img, C, nd, Hn, Wn, Wp, z, g_nn_skip);
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
 }
 

@@ -706,12 +706,22 @@ class GridPreconditioner:
         self.fixed = None if fixed is None else torch.as_tensor(np.asarray(fixed, dtype=np.uint8), device=dev)
         self.arena = {}
         self.applications = 0
+        self.skip_flag = None  # the solve's converged flag once attached to a problem
         net.forward(self.img, arena=self.arena)  # allocate the activations once
         torch.cuda.synchronize(dev)
         net.const_weights = True  # packed and synchronised: later forward passes may prefetch them
 
     def apply_ptr(self, r_ptr, z_ptr, n, stream):
         lib = self.net.lib
+        # the network's kernels return at once when the solve has converged (iterations a
+        # captured chunk runs past convergence)
+        lib.agx_nn_set_skip_flag(self.skip_flag)
+        try:
+            return self._apply(lib, r_ptr, z_ptr, stream)
+        finally:
+            lib.agx_nn_set_skip_flag(None)
+
+    def _apply(self, lib, r_ptr, z_ptr, stream):
         st = C.c_void_p(stream)
         f = self.factor
         nd = self.nd
@@ -752,6 +762,9 @@ class GridPreconditioner:
             raise ValueError("the learned preconditioner was built for another grid")
         if self.factor > 1 and self.fixed is None:
             self.fixed = torch.as_tensor(prob.mask.astype(np.uint8), device=self.net.device)
+        flag = C.c_void_p()
+        prob._call("agx_solve_flag", C.byref(flag))
+        self.skip_flag = flag
 
         def fn(user, r, z, n, stream):
             try:

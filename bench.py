@@ -296,6 +296,17 @@ def network_application_ms(pc, n_dofs, reps=30):
     dev = pc.net.device
     r = torch.randn(n_dofs, dtype=torch.float32, device=dev)
     z = torch.empty_like(r)
+    # outside a solve: the network must not skip on the last solve's converged flag
+    skip, pc.skip_flag = pc.skip_flag, None
+    try:
+        return _network_application_ms(pc, r, z, n_dofs, reps)
+    finally:
+        pc.skip_flag = skip
+
+
+def _network_application_ms(pc, r, z, n_dofs, reps):
+    import torch
+    dev = pc.net.device
     s = torch.cuda.Stream(device=dev)
     s.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(s):

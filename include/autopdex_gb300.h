@@ -286,6 +286,10 @@ int agx_set_tuning(agx_context* ctx, int dtype, int spmv_tpr);
    before it and then lets the next one launch, so the next kernel's blocks are scheduled while
    the current one runs.  0 launches them plainly (same results). */
 int agx_set_pdl(int enable);
+/* Device address of the current Krylov solve's status (an int: 0 while iterating, 1
+   converged, 2 broken down), written by the library's kernels between iterations; a
+   registered preconditioner's kernels may read it to skip work the solve no longer needs. */
+int agx_solve_flag(agx_context* ctx, const int** flag);
 /* ny of the structured QUAD4 grid whose 3 x 3 stencil the pattern is (the grid products,
    codes 512 and 1024, apply), else 0; for keys of a tuning cache. */
 int agx_grid_pattern(const agx_context* ctx, int* ny);

@@ -33,6 +33,13 @@ int agx_nn_conv3x3(const void* in1, const void* in2, int c1, int c2, const void*
    epilogue warps on mbarrier rings); 3 (the default) 2 for two-input layers of at least 128^2
    pixels, else 1.  All give identical results.  Process-wide; affects later launches only. */
 int agx_nn_set_halo_loader(int loader);
+/* A device int that the inference kernels launched from now on (convolutions, pooling,
+   upsampling, the grid transfers and images) read after waiting for their predecessor: nonzero
+   makes them return at once.  A preconditioner passes the solve's converged flag
+   (agx_solve_flag), so that iterations a captured CUDA-graph chunk runs past convergence skip
+   the network; NULL (the default) turns it off.  Process-wide; launches keep the pointer they
+   were given, graph captures included. */
+int agx_nn_set_skip_flag(const int* flag);
 /* dw_rows[(tap * (c1 + c2) + ci) * cout + co] += sum over pixels of in(p + tap)[ci] * dout(p)[co] */
 int agx_nn_wgrad3x3(const void* in1, const void* in2, int c1, int c2, const void* dout, int cout, float* dw_rows,
                     int B, int H, int W, int* err, void* stream);
