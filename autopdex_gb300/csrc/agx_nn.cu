@@ -1341,8 +1341,8 @@ int launch_conv(const ConvArgs& a, cudaStream_t s) {
   const bool ws = g_halo_loader == kLoadTmaWs ||
                   (g_halo_loader == kLoadAuto && C2 > 0 && (int64_t)a.H * a.W >= 128 * 128);
   if (ws) return launch_conv_as<C1, C2, COUT, EPI, kLoadTmaWs>(a, s);
-  return g_halo_loader == kLoadTma ? launch_conv_as<C1, C2, COUT, EPI, kLoadTma>(a, s)
-                                   : launch_conv_as<C1, C2, COUT, EPI, kLoadAsync>(a, s);
+  return g_halo_loader == kLoadAsync ? launch_conv_as<C1, C2, COUT, EPI, kLoadAsync>(a, s)
+                                     : launch_conv_as<C1, C2, COUT, EPI, kLoadTma>(a, s);
 }
 
 template <int C1, int C2, int COUT>
