@@ -15,6 +15,7 @@ AGX_PRECOND_CAPTURABLE = 1
 AGX_PRECOND_BF16_SMOOTHING = 2
 AGX_NN_CONST_WEIGHTS = 2
 AGX_DIVERGED = 2
+AGX_ERR_ARG, AGX_ERR_CUDA, AGX_ERR_UNSUPPORTED, AGX_ERR_STATE = -1, -2, -3, -5
 
 AGX_QUAD4, AGX_HEX8, AGX_LINE2, AGX_QUAD9, AGX_LINE3 = 0, 1, 2, 3, 4
 AGX_TRI3, AGX_TRI6, AGX_TET4, AGX_TET10, AGX_HEX27 = 5, 6, 7, 8, 9
@@ -103,6 +104,20 @@ _SIGNATURES = {
     "agx_nn_upsample2": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
     "agx_nn_pool": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
     "agx_nn_restrict_image_work": (C.c_int, []),
+    "agx_nn_conv3x3x3": (C.c_int, [_P, _P, C.c_int, C.c_int, _P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int,
+                                   C.c_int, C.c_int, C.c_int, _P, _P]),
+    "agx_nn_wgrad3x3x3": (C.c_int, [_P, _P, C.c_int, C.c_int, _P, C.c_int, _P, C.c_int, C.c_int, C.c_int, C.c_int,
+                                    _P, _P]),
+    "agx_nn_pack_weights3d": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P]),
+    "agx_nn_unpack_wgrad3d": (C.c_int, [_P, C.c_int, C.c_int, _P, _P]),
+    "agx_nn_pool3d": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
+    "agx_nn_upsample3d": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
+    "agx_nn_restrict_image3d_work": (C.c_int, []),
+    "agx_nn_restrict_image3d": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P,
+                                          _P, _P, _P, _P]),
+    "agx_nn_restrict3d": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P]),
+    "agx_nn_prolong_image3d": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P,
+                                         _P]),
     "agx_nn_set_halo_loader": (C.c_int, [C.c_int]),
     "agx_nn_restrict_image": (C.c_int, [_P, _P, C.c_int, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                         _P, _P, _P, _P, _P]),

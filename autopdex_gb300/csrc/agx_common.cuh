@@ -46,6 +46,14 @@ struct agx_element_set {
   // grid_m = (M00, M01, M11, det J) of the constant Jacobian J, M = adj(J) adj(J)^T / det J
   bool grid_uniform = false;
   double grid_m[4] = {0.0, 0.0, 0.0, 0.0};
+  // structured HEX8 brick grid of the mesher's numbering (brick_n = nx, ny, nz; 0 when the set
+  // is not one) whose pattern rows are exactly the in-range 27-node stencils; brick_uniform:
+  // every node on one lattice x0 + i e1 + j e2 + k e3, so J = [e1 | e2 | e3] / 2 everywhere,
+  // brick_m = (J^T J)^-1 as M00 M01 M02 M11 M12 M22, brick_det = det J
+  int brick_n[3] = {0, 0, 0};
+  bool brick_uniform = false;
+  double brick_m[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  double brick_det = 0.0;
 };
 
 // Scalars of one Krylov solve, kept in device memory so that iterations need no host
@@ -243,6 +251,11 @@ inline cudaError_t agx_launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 bloc
 // internal entry points shared across translation units
 int agx_build_pattern(agx_context* ctx);
 int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, int tangent_dtype);
+// uniform structured brick grids with the backward-Euler heat model (agx_brick.cu)
+bool agx_brick_heat_be(const agx_context* ctx, const agx_element_set& s);
+void agx_launch_brick_residual(agx_context* ctx, const agx_element_set& s, const double* dofs, double* R);
+void agx_launch_brick_tangent(agx_context* ctx, const agx_element_set& s, const double* dofs, float* vals,
+                              float* dinv);
 int agx_krylov_impl(agx_context* ctx, const double* rhs, double* x, const agx_solve_opts* opts,
                     agx_solve_info* info);
 int agx_residual_norm(agx_context* ctx, const double* R, double* norm2, double* nonfinite);

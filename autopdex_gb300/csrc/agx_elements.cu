@@ -1155,6 +1155,10 @@ grid_heat_residual(int nx, int ny, const double* __restrict__ kfield, double src
 template <typename T, bool DO_R, bool DO_K>
 int dispatch(agx_context* ctx, agx_element_set& s, const double* dofs, double* R, T* vals) {
   if constexpr (std::is_same<T, double>::value && DO_R && !DO_K) {
+    if (agx_brick_heat_be(ctx, s)) {
+      agx_launch_brick_residual(ctx, s, dofs, R);
+      return AGX_OK;
+    }
     if (s.model == AGX_MODEL_HEAT_POTENTIAL && s.elem_type == AGX_QUAD4 && s.grid_nx > 0 && s.grid_uniform &&
         s.ngauss == 2 && ctx->ndof == 1) {
       grid_heat_residual<<<agx_grid(ctx, (int64_t)(s.grid_nx + 1) * (s.grid_ny + 1)), AGX_BLOCK, 0, ctx->stream>>>(
@@ -1256,6 +1260,18 @@ static agx_element_set* grid_tangent_set(agx_context* ctx) {
   return with_k == 1 ? hit : nullptr;
 }
 
+// the uniform brick set whose float32 tangent the brick row kernel writes on its own, or null
+static agx_element_set* brick_tangent_set(agx_context* ctx) {
+  agx_element_set* hit = nullptr;
+  int with_k = 0;
+  for (auto& s : ctx->sets) {
+    if (s.model == AGX_MODEL_NEUMANN) continue;
+    ++with_k;
+    if (agx_brick_heat_be(ctx, s)) hit = &s;
+  }
+  return with_k == 1 ? hit : nullptr;
+}
+
 template <int MODEL, typename T, bool AFFINE>
 static void launch_grid_tangent_as(agx_context* ctx, agx_element_set& s, T* vals, T* dinv) {
   // one wave: the resident blocks of every SM (occupancy calculator), never more warps than
@@ -1302,11 +1318,13 @@ int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, in
         s.nqp < 1)
       return agx_fail(ctx, AGX_ERR_STATE, "simplex set without integration points (agx_set_quadrature_points)");
   agx_element_set* gset = tangent_dtype >= 0 ? grid_tangent_set(ctx) : nullptr;
+  // the uniform brick grid's row kernel (float32 tangents; float64 ones keep the element pass)
+  agx_element_set* bset = (!gset && tangent_dtype == AGX_F32) ? brick_tangent_set(ctx) : nullptr;
   if (residual || tangent_dtype == AGX_F64)
     for (auto& s : ctx->sets)
       if (int rc = build_geometry(ctx, s)) return rc;
   if (residual) AGX_CUDA(ctx, cudaMemsetAsync(residual, 0, sizeof(double) * ctx->n_dofs, ctx->stream));
-  if (gset) {
+  if (gset || bset) {
     // every entry of every row is written by the row kernel: no zeroing, no diagonal pass
   } else if (tangent_dtype == AGX_F64) {
     AGX_CUDA(ctx, cudaMemsetAsync(ctx->d_vals64, 0, sizeof(double) * ctx->nnzb * bs, ctx->stream));
@@ -1333,7 +1351,16 @@ int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, in
         agx_prof_scope ps(ctx, AGX_PROF_RESIDUAL);
         rc = dispatch<double, true, false>(ctx, s, dofs, residual, (double*)nullptr);
       }
-    } else if (gset && s.model != AGX_MODEL_NEUMANN) {
+    } else if (bset == &s) {
+      {
+        agx_prof_scope ps(ctx, AGX_PROF_TANGENT);
+        agx_launch_brick_tangent(ctx, s, dofs, ctx->d_vals32, ctx->d_dinv32);
+      }
+      if (residual) {
+        agx_prof_scope ps(ctx, AGX_PROF_RESIDUAL);
+        rc = dispatch<double, true, false>(ctx, s, dofs, residual, (double*)nullptr);
+      }
+    } else if ((gset || bset) && s.model != AGX_MODEL_NEUMANN) {
       rc = AGX_ERR_STATE;  // unreachable: the row kernel serves the only set with a tangent
     } else if (tangent_dtype == AGX_F64) {
       agx_prof_scope ps(ctx, AGX_PROF_TANGENT);
@@ -1356,8 +1383,8 @@ int agx_assemble_impl(agx_context* ctx, const double* dofs, double* residual, in
     if (rc != AGX_OK) return rc;
     AGX_CHECK_LAUNCH(ctx);
   }
-  if (tangent_dtype >= 0 && !gset) ctx->n_launches += (ctx->n_dir > 0 ? 2 : 1);  // Dirichlet diagonal + inverse diagonal
-  if (gset) {
+  if (tangent_dtype >= 0 && !gset && !bset) ctx->n_launches += (ctx->n_dir > 0 ? 2 : 1);  // Dirichlet diagonal + inverse diagonal
+  if (gset || bset) {
     ctx->tangent_valid = tangent_dtype;  // the row kernel wrote the inverse diagonal
   } else if (tangent_dtype == AGX_F64) {
     inverse_diagonal<double><<<agx_grid(ctx, ctx->n_dofs), AGX_BLOCK, 0, ctx->stream>>>(

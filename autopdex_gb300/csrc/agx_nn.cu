@@ -22,90 +22,17 @@
 #include <cudaTypedefs.h>
 
 #include "agx_common.cuh"
+#include "agx_tc.cuh"
 #include "../../include/autopdex_gb300_nn.h"
-
-namespace {
-
-namespace cg = cooperative_groups;
 
 // agx_nn_set_skip_flag: a device int that the inference kernels read after their
 // programmatic-launch wait; nonzero makes them return at once (passed to every launch, so a
 // captured graph keeps it)
 const int* g_nn_skip = nullptr;
-__device__ __forceinline__ bool nn_skip(const int* skip) { return skip && __ldcg(skip) != 0; }
 
-constexpr int kTile = 128;        // output pixels per CTA (MMA M)
-constexpr int kWaitLimit = 1 << 22;
+namespace {
 
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  // tcgen05 shared-memory matrix descriptor, no swizzle: start >> 4 (bits 0-13), leading
-  // byte offset >> 4 (16-29: distance of core matrices along K), stride byte offset >> 4
-  // (32-45: distance of 8-row groups along M/N), descriptor version 1 (bits 46-47)
-  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFF);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
-  d |= (uint64_t)1 << 46;
-  return d;
-}
-
-__device__ __forceinline__ uint32_t idesc_bf16(int M, int N) {
-  // kind::f16 instruction descriptor: f32 accumulator (bits 4-5 = 1), A and B bf16 (bits 7-9,
-  // 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
-      "l"(da), "l"(db), "r"(idesc), "r"(acc)
-      : "memory");
-}
-
-__device__ __forceinline__ int mbar_wait(uint32_t addr, uint32_t phase) {
-  for (int it = 0; it < kWaitLimit; ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\tselp.u32 %0, 1, 0, q;\n\t}\n"
-        : "=r"(ok)
-        : "r"(addr), "r"(phase)
-        : "memory");
-    if (ok) return 1;
-  }
-  return 0;
-}
-
-// 32 lanes x 16 consecutive f32 columns of TMEM per call (thread = lane = row)
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
-}
-
-template <int NCOLS>
-__device__ __forceinline__ void tmem_alloc(uint32_t* slot) {
-  const uint32_t s = (uint32_t)__cvta_generic_to_shared(slot);
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s), "n"(NCOLS) : "memory");
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-
-template <int NCOLS>
-__device__ __forceinline__ void tmem_free(uint32_t tmem) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(NCOLS) : "memory");
-}
-
-__host__ __device__ constexpr int tmem_cols(int n) { return n <= 32 ? 32 : (n <= 64 ? 64 : 128); }
-
-// byte offset of element (row, k) in a K-major no-swizzle operand with `rgroups` 8-row groups
-__device__ __forceinline__ uint32_t core_off(int row, int k, int rgroups) {
-  return (uint32_t)((((k >> 3) * rgroups + (row >> 3)) * 8 + (row & 7)) * 16 + (k & 7) * 2);
-}
+namespace cg = cooperative_groups;
 
 struct ConvArgs {
   const __nv_bfloat16* in1;  // NHWC, C1 channels
@@ -148,10 +75,6 @@ struct ConvMaps {
   CUtensorMap in2;  // {C2, W, H, B}, unused when C2 == 0
 };
 
-__device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
 __device__ __forceinline__ void tma_load4(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
                                           uint32_t bar) {
   asm volatile(
@@ -159,14 +82,6 @@ __device__ __forceinline__ void tma_load4(uint32_t dst, const CUtensorMap* map, 
       "[%6];" ::"r"(dst),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
       : "memory");
-}
-
-// one thread: a contiguous global -> shared copy of `bytes` (both ends 16-byte aligned, bytes
-// a multiple of 16), completing on `bar`
-__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(src), "r"(bytes), "r"(bar)
-               : "memory");
 }
 
 // one thread: the CIN / 8 plane copies of a tile's halo, completing on `bar`
@@ -642,20 +557,22 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_ws(const __grid_constant__
 }
 
 struct WgradArgs {
-  const __nv_bfloat16* in1;  // forward inputs, NHWC, C1 (+ C2) channels
+  const __nv_bfloat16* in1;  // forward inputs, NHWC (NDHWC for 27 taps), C1 (+ C2) channels
   const __nv_bfloat16* in2;
   const __nv_bfloat16* dout; // gradient of the pre-activation output, NHWC, COUT channels
-  float* dw;                 // (9 CIN) x COUT, f32, accumulated with atomics
-  int B, H, W;
+  float* dw;                 // (TAPS CIN) x COUT, f32, accumulated with atomics
+  int B, D, H, W;            // D = 1 for the 2-D convolution
   int64_t pix_per_cta;       // pixels reduced by one CTA (multiple of 16)
   int* err;
 };
 
 // dW[k, co] += sum_p A[k, p] dOut[p, co], A[t CIN + ci, p] = in[p + tap_t, ci]; one CTA per
 // (128-row slice of k, pixel chunk); the pixel chunk is consumed in sub-chunks of PCH pixels.
-template <int C1, int C2, int COUT, int PCH>
+// TAPS = 9: 3x3 taps t = 3 dy + dx of a 2-D image; TAPS = 27: 3x3x3 taps t = 9 dz + 3 dy + dx
+// of a 3-D one (offsets dz - 1, dy - 1, dx - 1).
+template <int C1, int C2, int COUT, int PCH, int TAPS>
 __global__ void __launch_bounds__(kTile) wgrad_tc(WgradArgs a) {
-  constexpr int CIN = C1 + C2, KW = 9 * CIN;
+  constexpr int CIN = C1 + C2, KW = TAPS * CIN;
   constexpr int A_BYTES = kTile * PCH * 2;   // 128 rows x PCH pixels
   constexpr int NCOLS = tmem_cols(COUT);
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -665,7 +582,7 @@ __global__ void __launch_bounds__(kTile) wgrad_tc(WgradArgs a) {
   __shared__ __align__(8) uint64_t mbar;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int row0 = blockIdx.y * kTile;       // first k row of this CTA
-  const int64_t HW = (int64_t)a.H * a.W, P = HW * a.B;
+  const int64_t HW = (int64_t)a.H * a.W, P = HW * a.D * a.B;
   const int64_t pbeg = (int64_t)blockIdx.x * a.pix_per_cta;
   const int64_t pend = pbeg + a.pix_per_cta < P ? pbeg + a.pix_per_cta : P;
   const uint32_t mbar_addr = (uint32_t)__cvta_generic_to_shared(&mbar);
@@ -692,12 +609,14 @@ __global__ void __launch_bounds__(kTile) wgrad_tc(WgradArgs a) {
         const int64_t pp = c0 + pg * 8 + u;
         uint4 v = make_uint4(0, 0, 0, 0);
         if (rowok && pp < pend) {
-          const int bb = (int)(pp / HW);
-          const int64_t rem = pp - (int64_t)bb * HW;
+          const int64_t bz = pp / HW;  // b D + z
+          const int64_t rem = pp - bz * HW;
           const int y = (int)(rem / a.W), x = (int)(rem - (int64_t)y * a.W);
-          const int yy = y + t / 3 - 1, xx = x + t % 3 - 1;
-          if (yy >= 0 && yy < a.H && xx >= 0 && xx < a.W) {
-            const int64_t q = ((int64_t)bb * a.H + yy) * a.W + xx;
+          const int dz = TAPS == 27 ? t / 9 - 1 : 0;
+          const int z = (int)(bz % a.D), zz = z + dz;
+          const int yy = y + (t / 3) % 3 - 1, xx = x + t % 3 - 1;
+          if (zz >= 0 && zz < a.D && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W) {
+            const int64_t q = ((bz + dz) * a.H + yy) * a.W + xx;
             if (ci < C1)
               v = *reinterpret_cast<const uint4*>(a.in1 + q * C1 + ci);
             else
@@ -777,14 +696,14 @@ __global__ void __launch_bounds__(kTile) wgrad_tc(WgradArgs a) {
 }
 
 // ---- small kernels ----------------------------------------------------------------------
-// Packs f32 weights W[co][ci][3][3] into the B image of the forward conv (rows co,
-// k = tap CIN + ci) or of the input-gradient conv (rows ci, k = tap' COUT + co with the taps
-// flipped, tap' = 8 - tap).
-__global__ void pack_weights_kernel(const float* __restrict__ w, int cout, int cin, int mode,
+// Packs f32 weights W[co][ci][taps] (taps = 9: [3][3]; 27: [3][3][3]) into the B image of the
+// forward conv (rows co, k = tap CIN + ci) or of the input-gradient conv (rows ci,
+// k = tap' COUT + co with the taps flipped, tap' = taps - 1 - tap: the offsets are symmetric).
+__global__ void pack_weights_kernel(const float* __restrict__ w, int cout, int cin, int taps, int mode,
                                     __nv_bfloat16* __restrict__ img) {
-  const int total = cout * cin * 9;
+  const int total = cout * cin * taps;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-    const int co = i / (cin * 9), rem = i % (cin * 9), ci = rem / 9, t = rem % 9;
+    const int co = i / (cin * taps), rem = i % (cin * taps), ci = rem / taps, t = rem % taps;
     int row, k, rows;
     if (mode == 0) {
       row = co;
@@ -792,7 +711,7 @@ __global__ void pack_weights_kernel(const float* __restrict__ w, int cout, int c
       rows = cout;
     } else {
       row = ci;
-      k = (8 - t) * cout + co;
+      k = (taps - 1 - t) * cout + co;
       rows = cin;
     }
     const int off = (((k >> 3) * (rows / 8) + (row >> 3)) * 8 + (row & 7)) * 8 + (k & 7);
@@ -800,11 +719,12 @@ __global__ void pack_weights_kernel(const float* __restrict__ w, int cout, int c
   }
 }
 
-// dW rows (tap CIN + ci) x cout -> torch layout [co][ci][3][3]
-__global__ void unpack_wgrad_kernel(const float* __restrict__ dwk, int cout, int cin, float* __restrict__ dw) {
-  const int total = cout * cin * 9;
+// dW rows (tap CIN + ci) x cout -> torch layout [co][ci][taps]
+__global__ void unpack_wgrad_kernel(const float* __restrict__ dwk, int cout, int cin, int taps,
+                                    float* __restrict__ dw) {
+  const int total = cout * cin * taps;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-    const int co = i / (cin * 9), rem = i % (cin * 9), ci = rem / 9, t = rem % 9;
+    const int co = i / (cin * taps), rem = i % (cin * taps), ci = rem / taps, t = rem % taps;
     dw[i] = dwk[(t * cin + ci) * cout + co];
   }
 }
@@ -1253,29 +1173,6 @@ prolong_image_kernel(const __nv_bfloat16* __restrict__ img, int C, int nd, int H
   }
 }
 
-int sm_count() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
-  return n;
-}
-
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }
-  return fn;
-}
-
 // NHWC bf16 tensor {C, W, H, B} with the halo box {8, 130, 3, 1}
 int make_halo_map(CUtensorMap* m, const void* base, int C, int B, int H, int W) {
   auto fn = encode_fn();
@@ -1345,22 +1242,22 @@ int launch_conv(const ConvArgs& a, cudaStream_t s) {
                                      : launch_conv_as<C1, C2, COUT, EPI, kLoadTma>(a, s);
 }
 
-template <int C1, int C2, int COUT>
+template <int C1, int C2, int COUT, int TAPS = 9>
 int launch_wgrad(const WgradArgs& a0, cudaStream_t s) {
   constexpr int CIN = C1 + C2, PCH = 256;
   const int smem = kTile * PCH * 2 + COUT * PCH * 2;
   static bool attr = false;
   if (!attr) {
-    if (cudaFuncSetAttribute(wgrad_tc<C1, C2, COUT, PCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
-        cudaSuccess)
+    if (cudaFuncSetAttribute(wgrad_tc<C1, C2, COUT, PCH, TAPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess)
       return AGX_ERR_CUDA;
     attr = true;
   }
   WgradArgs a = a0;
-  const int64_t P = (int64_t)a.B * a.H * a.W;
+  const int64_t P = (int64_t)a.B * a.D * a.H * a.W;
   a.pix_per_cta = 2048;
-  const dim3 grid((unsigned)((P + a.pix_per_cta - 1) / a.pix_per_cta), (unsigned)((9 * CIN + kTile - 1) / kTile));
-  wgrad_tc<C1, C2, COUT, PCH><<<grid, kTile, smem, s>>>(a);
+  const dim3 grid((unsigned)((P + a.pix_per_cta - 1) / a.pix_per_cta), (unsigned)((TAPS * CIN + kTile - 1) / kTile));
+  wgrad_tc<C1, C2, COUT, PCH, TAPS><<<grid, kTile, smem, s>>>(a);
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
 }
 
@@ -1433,8 +1330,8 @@ int agx_nn_set_halo_loader(int loader) {
 int agx_nn_wgrad3x3(const void* in1, const void* in2, int c1, int c2, const void* dout, int cout, float* dw_rows,
                     int B, int H, int W, int* err, void* stream) {
   if (!in1 || !dout || !dw_rows || !err || B <= 0 || H <= 0 || W <= 0) return AGX_ERR_ARG;
-  WgradArgs a{(const __nv_bfloat16*)in1, (const __nv_bfloat16*)in2, (const __nv_bfloat16*)dout, dw_rows, B, H, W, 0,
-              err};
+  WgradArgs a{(const __nv_bfloat16*)in1, (const __nv_bfloat16*)in2, (const __nv_bfloat16*)dout, dw_rows, B, 1, H, W,
+              0, err};
   cudaStream_t s = (cudaStream_t)stream;
 #define AGX_WG(C1_, C2_, CO_) \
   if (c1 == C1_ && c2 == C2_ && cout == CO_) return launch_wgrad<C1_, C2_, CO_>(a, s);
@@ -1446,15 +1343,40 @@ int agx_nn_wgrad3x3(const void* in1, const void* in2, int c1, int c2, const void
   return AGX_ERR_UNSUPPORTED;
 }
 
+int agx_nn_wgrad3x3x3(const void* in1, const void* in2, int c1, int c2, const void* dout, int cout, float* dw_rows,
+                      int B, int D, int H, int W, int* err, void* stream) {
+  if (!in1 || !dout || !dw_rows || !err || B <= 0 || D <= 0 || H <= 0 || W <= 0 || (c2 > 0 && !in2))
+    return AGX_ERR_ARG;
+  WgradArgs a{(const __nv_bfloat16*)in1, (const __nv_bfloat16*)in2, (const __nv_bfloat16*)dout, dw_rows, B, D, H, W,
+              0, err};
+  cudaStream_t s = (cudaStream_t)stream;
+  if (c1 == 16 && c2 == 0 && cout == 16) return launch_wgrad<16, 0, 16, 27>(a, s);
+  if (c1 == 16 && c2 == 16 && cout == 16) return launch_wgrad<16, 16, 16, 27>(a, s);
+  return AGX_ERR_UNSUPPORTED;
+}
+
 int agx_nn_pack_weights(const float* w, int cout, int cin, int mode, void* img, void* stream) {
   if (!w || !img || cout % 8 || cin % 8) return AGX_ERR_ARG;
-  pack_weights_kernel<<<grid1((int64_t)cout * cin * 9), 256, 0, (cudaStream_t)stream>>>(w, cout, cin, mode,
+  pack_weights_kernel<<<grid1((int64_t)cout * cin * 9), 256, 0, (cudaStream_t)stream>>>(w, cout, cin, 9, mode,
                                                                                        (__nv_bfloat16*)img);
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
 }
 
 int agx_nn_unpack_wgrad(const float* dw_rows, int cout, int cin, float* dw, void* stream) {
-  unpack_wgrad_kernel<<<grid1((int64_t)cout * cin * 9), 256, 0, (cudaStream_t)stream>>>(dw_rows, cout, cin, dw);
+  unpack_wgrad_kernel<<<grid1((int64_t)cout * cin * 9), 256, 0, (cudaStream_t)stream>>>(dw_rows, cout, cin, 9, dw);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+int agx_nn_pack_weights3d(const float* w, int cout, int cin, int mode, void* img, void* stream) {
+  if (!w || !img || cout % 8 || cin % 8) return AGX_ERR_ARG;
+  pack_weights_kernel<<<grid1((int64_t)cout * cin * 27), 256, 0, (cudaStream_t)stream>>>(w, cout, cin, 27, mode,
+                                                                                        (__nv_bfloat16*)img);
+  return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
+}
+
+int agx_nn_unpack_wgrad3d(const float* dw_rows, int cout, int cin, float* dw, void* stream) {
+  if (!dw_rows || !dw) return AGX_ERR_ARG;
+  unpack_wgrad_kernel<<<grid1((int64_t)cout * cin * 27), 256, 0, (cudaStream_t)stream>>>(dw_rows, cout, cin, 27, dw);
   return cudaGetLastError() == cudaSuccess ? AGX_OK : AGX_ERR_CUDA;
 }
 

@@ -8,6 +8,7 @@
 // element and local node pair (a, b) the position of block (conn[a], conn[b]) is stored,
 // so that assembly adds element blocks straight into their final slots.
 #include <algorithm>
+#include <cmath>
 #include <thread>
 
 #include "agx_common.cuh"
@@ -105,6 +106,91 @@ void detect_structured_grid(agx_context* ctx, agx_element_set& s, const std::vec
   }
 }
 
+// A HEX8 set that is the mesher's structured nx x ny x nz brick grid over all nodes (element
+// (i ny + j) nz + k with local nodes (i,j,k), (i+1,j,k), (i+1,j+1,k), (i,j+1,k), then the same
+// at k + 1; node (i, j, k) = (i (ny + 1) + j)(nz + 1) + k), every pattern row the in-range
+// 27-node stencil; uniform when every node is x0 + i e1 + j e2 + k e3 (to 1e-13 of the grid's
+// extent): then J = [e1 | e2 | e3] / 2 for every element.
+void detect_structured_brick(agx_context* ctx, agx_element_set& s, const std::vector<int32_t>& rowptr) {
+  s.brick_n[0] = s.brick_n[1] = s.brick_n[2] = 0;
+  s.brick_uniform = false;
+  if (s.elem_type != AGX_HEX8 || ctx->dim != 3 || s.n_elem < 1) return;
+  const int32_t* c = s.h_conn.data();
+  if (c[0] != 0 || c[4] != 1) return;
+  const int64_t nz = (int64_t)c[3] - 1;
+  if (nz < 1 || c[1] % (nz + 1)) return;
+  const int64_t ny = (int64_t)c[1] / (nz + 1) - 1;
+  if (ny < 1 || s.n_elem % (ny * nz)) return;
+  const int64_t nx = s.n_elem / (ny * nz);
+  const int64_t sa = (ny + 1) * (nz + 1), sb = nz + 1;
+  if ((nx + 1) * sa != ctx->n_nodes) return;
+  bool ok = true;
+  parallel_for(nx, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e && ok; ++i)
+      for (int64_t j = 0; j < ny; ++j)
+        for (int64_t k = 0; k < nz; ++k) {
+          const int32_t* el = c + ((i * ny + j) * nz + k) * 8;
+          const int64_t n0 = i * sa + j * sb + k;
+          if (el[0] != n0 || el[1] != n0 + sa || el[2] != n0 + sa + sb || el[3] != n0 + sb || el[4] != n0 + 1 ||
+              el[5] != n0 + sa + 1 || el[6] != n0 + sa + sb + 1 || el[7] != n0 + sb + 1) {
+            ok = false;
+            return;
+          }
+        }
+  });
+  if (!ok) return;
+  for (int64_t i = 0; i <= nx && ok; ++i)
+    for (int64_t j = 0; j <= ny && ok; ++j)
+      for (int64_t k = 0; k <= nz; ++k) {
+        const int64_t len = ((i > 0) + 1 + (i < nx)) * ((j > 0) + 1 + (j < ny)) * ((k > 0) + 1 + (k < nz));
+        const int64_t p = i * sa + j * sb + k;
+        if (rowptr[p + 1] - rowptr[p] != len) {
+          ok = false;
+          break;
+        }
+      }
+  if (!ok) return;
+  s.brick_n[0] = (int)nx, s.brick_n[1] = (int)ny, s.brick_n[2] = (int)nz;
+  const double* X = ctx->h_coords.data();
+  double e[3][3], ext = 0.0;
+  for (int d = 0; d < 3; ++d) {
+    e[0][d] = X[3 * sa + d] - X[d];
+    e[1][d] = X[3 * sb + d] - X[d];
+    e[2][d] = X[3 * 1 + d] - X[d];
+    ext += std::fabs(e[0][d]) * nx + std::fabs(e[1][d]) * ny + std::fabs(e[2][d]) * nz;
+  }
+  bool uni = ext > 0.0;
+  for (int64_t i = 0; i <= nx && uni; ++i)
+    for (int64_t j = 0; j <= ny && uni; ++j)
+      for (int64_t k = 0; k <= nz; ++k) {
+        const double* x = X + 3 * (i * sa + j * sb + k);
+        double dev = 0.0;
+        for (int d = 0; d < 3; ++d) dev += std::fabs(x[d] - (X[d] + i * e[0][d] + j * e[1][d] + k * e[2][d]));
+        if (dev > 1e-13 * ext) {
+          uni = false;
+          break;
+        }
+      }
+  if (!uni) return;
+  // J[d][m] = e_m[d] / 2; (J^T J)^-1 by the adjugate of the Gram matrix
+  double G[3][3];
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) G[a][b] = 0.25 * (e[a][0] * e[b][0] + e[a][1] * e[b][1] + e[a][2] * e[b][2]);
+  const double det = 0.125 * (e[0][0] * (e[1][1] * e[2][2] - e[2][1] * e[1][2]) -
+                              e[1][0] * (e[0][1] * e[2][2] - e[2][1] * e[0][2]) +
+                              e[2][0] * (e[0][1] * e[1][2] - e[1][1] * e[0][2]));
+  const double g = det * det;  // det(J^T J)
+  if (!(g > 0.0)) return;
+  s.brick_m[0] = (G[1][1] * G[2][2] - G[1][2] * G[2][1]) / g;
+  s.brick_m[1] = (G[0][2] * G[2][1] - G[0][1] * G[2][2]) / g;
+  s.brick_m[2] = (G[0][1] * G[1][2] - G[0][2] * G[1][1]) / g;
+  s.brick_m[3] = (G[0][0] * G[2][2] - G[0][2] * G[2][0]) / g;
+  s.brick_m[4] = (G[0][2] * G[1][0] - G[0][0] * G[1][2]) / g;
+  s.brick_m[5] = (G[0][0] * G[1][1] - G[0][1] * G[1][0]) / g;
+  s.brick_det = det;
+  s.brick_uniform = true;
+}
+
 }  // namespace
 
 int agx_build_pattern(agx_context* ctx) {
@@ -186,6 +272,7 @@ int agx_build_pattern(agx_context* ctx) {
   ctx->pattern_grid_ny = 0;
   for (auto& s : ctx->sets) {
     detect_structured_grid(ctx, s, rowptr);
+    detect_structured_brick(ctx, s, rowptr);
     // the row lengths matched the grid's stencil: every other set's entries lie inside it
     if (s.grid_nx > 0 && ctx->ndof <= 2) ctx->pattern_grid_ny = s.grid_ny;
   }

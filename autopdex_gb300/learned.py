@@ -48,7 +48,15 @@ def padded(n):
 
 class UNet:
     """``n_in``: input channels in use (the field's components plus auxiliary features; the
-    rest of the 16 are padding and their weights stay zero)."""
+    rest of the 16 are padding and their weights stay zero).
+
+    The class describes the 2-D network (NHWC tensors, 3x3 convolutions, POOL x POOL pooling);
+    :class:`UNet3D` changes the class attributes below for the 3-D one."""
+
+    dims = 2          # spatial dimensions of the tensors
+    layers = LAYERS
+    pool = POOL
+    hid = C_HID
 
     def __init__(self, device="cuda", seed=0, params=None, n_in=2):
         self.lib = N.load()
@@ -58,10 +66,11 @@ class UNet:
         self.n_in = n_in
         g = torch.Generator().manual_seed(seed)
         self.w, self.b = {}, {}
-        for name, c1, c2, co, relu in LAYERS:
+        taps = 3 ** self.dims
+        for name, c1, c2, co, relu in self.layers:
             cin = c1 + c2
-            std = math.sqrt(2.0 / (9 * cin)) if relu else math.sqrt(1.0 / (9 * cin))
-            w = torch.randn(co, cin, 3, 3, generator=g) * std
+            std = math.sqrt(2.0 / (taps * cin)) if relu else math.sqrt(1.0 / (taps * cin))
+            w = torch.randn(co, cin, *(3,) * self.dims, generator=g) * std
             if name == "e0a":
                 w[:, n_in:] = 0.0  # channels n_in..15 of the input are padding
             self.w[name] = w.to(self.device)
@@ -91,7 +100,10 @@ class UNet:
         return cls(device=device, params=dict(np.load(path)))
 
     def parameters(self):
-        return [self.w[k] for k, *_ in LAYERS] + [self.b[k] for k, *_ in LAYERS]
+        return [self.w[k] for k, *_ in self.layers] + [self.b[k] for k, *_ in self.layers]
+
+    def _layer(self, name):
+        return next(l for l in self.layers if l[0] == name)
 
     def pack(self):
         """bf16 operand images of every layer (forward and input-gradient)."""
@@ -99,14 +111,17 @@ class UNet:
         # only once a synchronisation has followed the packing (GridPreconditioner sets it)
         self.const_weights = False
         s = self._stream()
+        fn = "agx_nn_pack_weights" if self.dims == 2 else "agx_nn_pack_weights3d"
+        pack = getattr(self.lib, fn)
+        taps = 3 ** self.dims
         self.img_f, self.img_b = {}, {}
-        for name, c1, c2, co, relu in LAYERS:
+        for name, c1, c2, co, relu in self.layers:
             cin = c1 + c2
             w = self.w[name].contiguous()
-            f = torch.empty(co * cin * 9, dtype=torch.bfloat16, device=self.device)
-            bimg = torch.empty(co * cin * 9, dtype=torch.bfloat16, device=self.device)
-            self._ok("agx_nn_pack_weights", self.lib.agx_nn_pack_weights(_p(w), co, cin, 0, _p(f), s))
-            self._ok("agx_nn_pack_weights", self.lib.agx_nn_pack_weights(_p(w), co, cin, 1, _p(bimg), s))
+            f = torch.empty(co * cin * taps, dtype=torch.bfloat16, device=self.device)
+            bimg = torch.empty(co * cin * taps, dtype=torch.bfloat16, device=self.device)
+            self._ok(fn, pack(_p(w), co, cin, 0, _p(f), s))
+            self._ok(fn, pack(_p(w), co, cin, 1, _p(bimg), s))
             self.img_f[name], self.img_b[name] = f, bimg
 
     # ---- helpers ------------------------------------------------------------------------
@@ -120,43 +135,59 @@ class UNet:
         if rc != 0:
             raise RuntimeError(f"{fn} failed with status {rc}")
 
-    def _act(self, B, H, W, c, key=None):
-        """Activation buffer: from the arena when one is active (allocated on first use)."""
+    def _act(self, B, S, c, key=None):
+        """Activation buffer (B, *S, c): from the arena when one is active (allocated on first use)."""
+        shape = (B, *S, c)
         if self._arena is not None and key is not None:
             t = self._arena.get(key)
-            if t is None or t.shape != (B, H, W, c):
-                t = torch.empty((B, H, W, c), dtype=torch.bfloat16, device=self.device)
+            if t is None or tuple(t.shape) != shape:
+                t = torch.empty(shape, dtype=torch.bfloat16, device=self.device)
                 self._arena[key] = t
             return t
-        return torch.empty((B, H, W, c), dtype=torch.bfloat16, device=self.device)
+        return torch.empty(shape, dtype=torch.bfloat16, device=self.device)
 
-    def _conv(self, name, x1, x2, B, H, W):
-        _, c1, c2, co, relu = next(l for l in LAYERS if l[0] == name)
-        out = self._act(B, H, W, co, name)
+    def _convolve(self, x1, x2, c1, c2, wimg, bias, out1, out2, split, cout, flags, B, S, s):
+        if self.dims == 2:
+            return self.lib.agx_nn_conv3x3(_p(x1), _p(x2), c1, c2, _p(wimg), _p(bias), _p(out1), _p(out2), split, cout,
+                                           flags, B, *S, _p(self.err), s)
+        return self.lib.agx_nn_conv3x3x3(_p(x1), _p(x2), c1, c2, _p(wimg), _p(bias), _p(out1), _p(out2), split, cout,
+                                         flags, B, *S, _p(self.err), s)
+
+    def _conv(self, name, x1, x2, B, S):
+        _, c1, c2, co, relu = self._layer(name)
+        out = self._act(B, S, co, name)
         flags = relu | (N.AGX_NN_CONST_WEIGHTS if self.const_weights and self._arena is not None else 0)
-        rc = self.lib.agx_nn_conv3x3(_p(x1), _p(x2), c1, c2, _p(self.img_f[name]), _p(self.b[name]), _p(out), None,
-                                     co, co, flags, B, H, W, _p(self.err), self._stream())
-        self._ok("agx_nn_conv3x3", rc)
+        rc = self._convolve(x1, x2, c1, c2, self.img_f[name], self.b[name], out, None, co, co, flags, B, S,
+                            self._stream())
+        self._ok("convolution", rc)
         self.launches += 1
         return out
 
-    def _pool(self, x, B, H, W, c, key):
-        """POOL x POOL average pooling in one launch."""
-        out = self._act(B, H // POOL, W // POOL, c, f"{key}.{POOL}")
-        self._ok("agx_nn_pool", self.lib.agx_nn_pool(_p(x), _p(out), B, H, W, c, POOL, 0, self._stream()))
+    def _transfer(self, up, x, out, B, S, c, backward, s):
+        """Pooling (up False) or upsampling (up True) of x at spatial size S, one launch."""
+        if self.dims == 2:
+            fn = self.lib.agx_nn_upsample if up else self.lib.agx_nn_pool
+        else:
+            fn = self.lib.agx_nn_upsample3d if up else self.lib.agx_nn_pool3d
+        self._ok("pooling" if not up else "upsampling", fn(_p(x), _p(out), B, *S, c, self.pool, backward, s))
+
+    def _pool(self, x, B, S, c, key):
+        """Average pooling by self.pool in every dimension, one launch."""
+        out = self._act(B, tuple(v // self.pool for v in S), c, f"{key}.{self.pool}")
+        self._transfer(False, x, out, B, S, c, 0, self._stream())
         self.launches += 1
         return out
 
-    def _up(self, x, B, H, W, c, key):
-        """Nearest POOL x upsampling of an H x W image in one launch."""
-        out = self._act(B, POOL * H, POOL * W, c, f"{key}.{POOL}")
-        self._ok("agx_nn_upsample", self.lib.agx_nn_upsample(_p(x), _p(out), B, H, W, c, POOL, 0, self._stream()))
+    def _up(self, x, B, S, c, key):
+        """Nearest upsampling by self.pool of an image of spatial size S, one launch."""
+        out = self._act(B, tuple(self.pool * v for v in S), c, f"{key}.{self.pool}")
+        self._transfer(True, x, out, B, S, c, 0, self._stream())
         self.launches += 1
         return out
 
     # ---- forward / backward -------------------------------------------------------------
     def forward(self, x, keep=False, stream=None, arena=None):
-        """x: (B, H, W, 16) bf16 with H, W multiples of POOL^3 -> (B, H, W, 16) bf16.
+        """x: (B, *S, 16) bf16 with every extent of S a multiple of pool^3 -> (B, *S, 16) bf16.
 
         ``stream``: launch on this CUDA stream (a c_void_p) instead of torch's current one;
         ``arena``: a dict of activation buffers reused across calls (no allocation once warm)."""
@@ -166,106 +197,139 @@ class UNet:
         finally:
             self._s, self._arena = None, None
 
+    def _level(self, S0, k):
+        return tuple(v // self.pool ** k for v in S0)
+
     def _forward(self, x, keep):
-        B, H, W, _ = x.shape
-        q1, q2, q3 = POOL, POOL ** 2, POOL ** 3
+        B, S0 = x.shape[0], tuple(x.shape[1:-1])
+        L = [self._level(S0, k) for k in range(4)]
+        h = self.hid
         a = {"x": x}
-        a["e0a"] = self._conv("e0a", x, None, B, H, W)
-        a["e0b"] = self._conv("e0b", a["e0a"], None, B, H, W)
-        a["p0"] = self._pool(a["e0b"], B, H, W, C_HID, "p0")
-        a["e1a"] = self._conv("e1a", a["p0"], None, B, H // q1, W // q1)
-        a["e1b"] = self._conv("e1b", a["e1a"], None, B, H // q1, W // q1)
-        a["p1"] = self._pool(a["e1b"], B, H // q1, W // q1, C_HID, "p1")
-        a["e2a"] = self._conv("e2a", a["p1"], None, B, H // q2, W // q2)
-        a["e2b"] = self._conv("e2b", a["e2a"], None, B, H // q2, W // q2)
-        a["p2"] = self._pool(a["e2b"], B, H // q2, W // q2, C_HID, "p2")
-        a["b3a"] = self._conv("b3a", a["p2"], None, B, H // q3, W // q3)
-        a["b3b"] = self._conv("b3b", a["b3a"], None, B, H // q3, W // q3)
-        a["u2"] = self._up(a["b3b"], B, H // q3, W // q3, C_HID, "u2")
-        a["d2a"] = self._conv("d2a", a["u2"], a["e2b"], B, H // q2, W // q2)
-        a["d2b"] = self._conv("d2b", a["d2a"], None, B, H // q2, W // q2)
-        a["u1"] = self._up(a["d2b"], B, H // q2, W // q2, C_HID, "u1")
-        a["d1a"] = self._conv("d1a", a["u1"], a["e1b"], B, H // q1, W // q1)
-        a["d1b"] = self._conv("d1b", a["d1a"], None, B, H // q1, W // q1)
-        a["u0"] = self._up(a["d1b"], B, H // q1, W // q1, C_HID, "u0")
-        a["d0a"] = self._conv("d0a", a["u0"], a["e0b"], B, H, W)
-        a["d0b"] = self._conv("d0b", a["d0a"], None, B, H, W)
-        out = self._conv("out", a["d0b"], None, B, H, W)
+        a["e0a"] = self._conv("e0a", x, None, B, L[0])
+        a["e0b"] = self._conv("e0b", a["e0a"], None, B, L[0])
+        a["p0"] = self._pool(a["e0b"], B, L[0], h, "p0")
+        a["e1a"] = self._conv("e1a", a["p0"], None, B, L[1])
+        a["e1b"] = self._conv("e1b", a["e1a"], None, B, L[1])
+        a["p1"] = self._pool(a["e1b"], B, L[1], h, "p1")
+        a["e2a"] = self._conv("e2a", a["p1"], None, B, L[2])
+        a["e2b"] = self._conv("e2b", a["e2a"], None, B, L[2])
+        a["p2"] = self._pool(a["e2b"], B, L[2], h, "p2")
+        a["b3a"] = self._conv("b3a", a["p2"], None, B, L[3])
+        a["b3b"] = self._conv("b3b", a["b3a"], None, B, L[3])
+        a["u2"] = self._up(a["b3b"], B, L[3], h, "u2")
+        a["d2a"] = self._conv("d2a", a["u2"], a["e2b"], B, L[2])
+        a["d2b"] = self._conv("d2b", a["d2a"], None, B, L[2])
+        a["u1"] = self._up(a["d2b"], B, L[2], h, "u1")
+        a["d1a"] = self._conv("d1a", a["u1"], a["e1b"], B, L[1])
+        a["d1b"] = self._conv("d1b", a["d1a"], None, B, L[1])
+        a["u0"] = self._up(a["d1b"], B, L[1], h, "u0")
+        a["d0a"] = self._conv("d0a", a["u0"], a["e0b"], B, L[0])
+        a["d0b"] = self._conv("d0b", a["d0a"], None, B, L[0])
+        out = self._conv("out", a["d0b"], None, B, L[0])
         return (out, a) if keep else out
 
-    def _layer_backward(self, name, g, x1, x2, y, B, H, W, need_input_grad=True):
+    def _layer_backward(self, name, g, x1, x2, y, B, S, need_input_grad=True):
         """g: gradient w.r.t. the layer output y (modified in place by the ReLU mask)."""
-        _, c1, c2, co, relu = next(l for l in LAYERS if l[0] == name)
+        _, c1, c2, co, relu = self._layer(name)
         s = self._stream()
         if relu:
             self._ok("agx_nn_relu_backward", self.lib.agx_nn_relu_backward(_p(g), _p(y), g.numel(), s))
-        P = B * H * W
+        P = B * math.prod(S)
         self._ok("agx_nn_bias_grad", self.lib.agx_nn_bias_grad(_p(g), P, co, _p(self.gb[name]), s))
-        rows = torch.zeros(9 * (c1 + c2) * co, dtype=torch.float32, device=self.device)
-        self._ok("agx_nn_wgrad3x3", self.lib.agx_nn_wgrad3x3(_p(x1), _p(x2), c1, c2, _p(g), co, _p(rows), B, H, W,
-                                                           _p(self.err), s))
+        taps = 3 ** self.dims
+        rows = torch.zeros(taps * (c1 + c2) * co, dtype=torch.float32, device=self.device)
         dw = torch.empty_like(self.w[name])
-        self._ok("agx_nn_unpack_wgrad", self.lib.agx_nn_unpack_wgrad(_p(rows), co, c1 + c2, _p(dw), s))
+        if self.dims == 2:
+            rc = self.lib.agx_nn_wgrad3x3(_p(x1), _p(x2), c1, c2, _p(g), co, _p(rows), B, *S, _p(self.err), s)
+            self._ok("agx_nn_wgrad3x3", rc)
+            self._ok("agx_nn_unpack_wgrad", self.lib.agx_nn_unpack_wgrad(_p(rows), co, c1 + c2, _p(dw), s))
+        else:
+            rc = self.lib.agx_nn_wgrad3x3x3(_p(x1), _p(x2), c1, c2, _p(g), co, _p(rows), B, *S, _p(self.err), s)
+            self._ok("agx_nn_wgrad3x3x3", rc)
+            self._ok("agx_nn_unpack_wgrad3d", self.lib.agx_nn_unpack_wgrad3d(_p(rows), co, c1 + c2, _p(dw), s))
         self.gw[name] += dw
         if not need_input_grad:
             return None, None
-        d1 = self._act(B, H, W, c1)
-        d2 = self._act(B, H, W, c2) if c2 else None
-        rc = self.lib.agx_nn_conv3x3(_p(g), None, co, 0, _p(self.img_b[name]), None, _p(d1), _p(d2), c1, c1 + c2, 0,
-                                     B, H, W, _p(self.err), s)
-        self._ok("agx_nn_conv3x3 (input gradient)", rc)
+        d1 = self._act(B, S, c1)
+        d2 = self._act(B, S, c2) if c2 else None
+        rc = self._convolve(g, None, co, 0, self.img_b[name], None, d1, d2, c1, c1 + c2, 0, B, S, s)
+        self._ok("convolution (input gradient)", rc)
         return d1, d2
 
     def backward(self, gout, a):
         """Accumulates parameter gradients into self.gw / self.gb for d(loss)/d(out) = gout."""
-        B, H, W, _ = gout.shape
+        B, S0 = gout.shape[0], tuple(gout.shape[1:-1])
+        L = [self._level(S0, k) for k in range(4)]
+        h = self.hid
         s = self._stream()
         self.gw = {k: torch.zeros_like(v) for k, v in self.w.items()}
         self.gb = {k: torch.zeros_like(v) for k, v in self.b.items()}
 
-        def upb(g, h, w):  # adjoint of upsampling to (h, w) -> coarse (h / POOL, w / POOL)
-            out = self._act(B, h // POOL, w // POOL, C_HID)
-            self._ok("agx_nn_upsample", self.lib.agx_nn_upsample(_p(g), _p(out), B, h // POOL, w // POOL, C_HID,
-                                                                 POOL, 1, s))
+        def upb(g, k):  # adjoint of the upsampling from level k + 1 to level k: -> level k + 1
+            out = self._act(B, L[k + 1], h)
+            self._transfer(True, g, out, B, L[k + 1], h, 1, s)
             return out
 
-        def poolb(g, h, w):  # adjoint of pooling from (h, w): coarse (h / POOL, w / POOL) -> (h, w)
-            out = self._act(B, h, w, C_HID)
-            self._ok("agx_nn_pool", self.lib.agx_nn_pool(_p(g), _p(out), B, h, w, C_HID, POOL, 1, s))
+        def poolb(g, k):  # adjoint of the pooling from level k to level k + 1: -> level k
+            out = self._act(B, L[k], h)
+            self._transfer(False, g, out, B, L[k], h, 1, s)
             return out
 
         def add(x, y):
             self._ok("agx_nn_add", self.lib.agx_nn_add(_p(x), _p(y), x.numel(), s))
             return x
 
-        q1, q2, q3 = POOL, POOL ** 2, POOL ** 3
         g = gout.clone()
-        g, _ = self._layer_backward("out", g, a["d0b"], None, None, B, H, W)
-        g, _ = self._layer_backward("d0b", g, a["d0a"], None, a["d0b"], B, H, W)
-        g_u0, g_s0 = self._layer_backward("d0a", g, a["u0"], a["e0b"], a["d0a"], B, H, W)
-        g = upb(g_u0, H, W)
-        g, _ = self._layer_backward("d1b", g, a["d1a"], None, a["d1b"], B, H // q1, W // q1)
-        g_u1, g_s1 = self._layer_backward("d1a", g, a["u1"], a["e1b"], a["d1a"], B, H // q1, W // q1)
-        g = upb(g_u1, H // q1, W // q1)
-        g, _ = self._layer_backward("d2b", g, a["d2a"], None, a["d2b"], B, H // q2, W // q2)
-        g_u2, g_s2 = self._layer_backward("d2a", g, a["u2"], a["e2b"], a["d2a"], B, H // q2, W // q2)
-        g = upb(g_u2, H // q2, W // q2)
-        g, _ = self._layer_backward("b3b", g, a["b3a"], None, a["b3b"], B, H // q3, W // q3)
-        g, _ = self._layer_backward("b3a", g, a["p2"], None, a["b3a"], B, H // q3, W // q3)
-        g = add(poolb(g, H // q2, W // q2), g_s2)
-        g, _ = self._layer_backward("e2b", g, a["e2a"], None, a["e2b"], B, H // q2, W // q2)
-        g, _ = self._layer_backward("e2a", g, a["p1"], None, a["e2a"], B, H // q2, W // q2)
-        g = add(poolb(g, H // q1, W // q1), g_s1)
-        g, _ = self._layer_backward("e1b", g, a["e1a"], None, a["e1b"], B, H // q1, W // q1)
-        g, _ = self._layer_backward("e1a", g, a["p0"], None, a["e1a"], B, H // q1, W // q1)
-        g = add(poolb(g, H, W), g_s0)
-        g, _ = self._layer_backward("e0b", g, a["e0a"], None, a["e0b"], B, H, W)
-        self._layer_backward("e0a", g, a["x"], None, a["e0a"], B, H, W, need_input_grad=False)
+        g, _ = self._layer_backward("out", g, a["d0b"], None, None, B, L[0])
+        g, _ = self._layer_backward("d0b", g, a["d0a"], None, a["d0b"], B, L[0])
+        g_u0, g_s0 = self._layer_backward("d0a", g, a["u0"], a["e0b"], a["d0a"], B, L[0])
+        g = upb(g_u0, 0)
+        g, _ = self._layer_backward("d1b", g, a["d1a"], None, a["d1b"], B, L[1])
+        g_u1, g_s1 = self._layer_backward("d1a", g, a["u1"], a["e1b"], a["d1a"], B, L[1])
+        g = upb(g_u1, 1)
+        g, _ = self._layer_backward("d2b", g, a["d2a"], None, a["d2b"], B, L[2])
+        g_u2, g_s2 = self._layer_backward("d2a", g, a["u2"], a["e2b"], a["d2a"], B, L[2])
+        g = upb(g_u2, 2)
+        g, _ = self._layer_backward("b3b", g, a["b3a"], None, a["b3b"], B, L[3])
+        g, _ = self._layer_backward("b3a", g, a["p2"], None, a["b3a"], B, L[3])
+        g = add(poolb(g, 2), g_s2)
+        g, _ = self._layer_backward("e2b", g, a["e2a"], None, a["e2b"], B, L[2])
+        g, _ = self._layer_backward("e2a", g, a["p1"], None, a["e2a"], B, L[2])
+        g = add(poolb(g, 1), g_s1)
+        g, _ = self._layer_backward("e1b", g, a["e1a"], None, a["e1b"], B, L[1])
+        g, _ = self._layer_backward("e1a", g, a["p0"], None, a["e1a"], B, L[1])
+        g = add(poolb(g, 0), g_s0)
+        g, _ = self._layer_backward("e0b", g, a["e0a"], None, a["e0b"], B, L[0])
+        self._layer_backward("e0a", g, a["x"], None, a["e0a"], B, L[0], need_input_grad=False)
         return self.gw, self.gb
 
     def check(self):
         if int(self.err.item()) != 0:
             raise RuntimeError("a tensor-core kernel timed out waiting for its MMA")
+
+
+# The 3-D network: 16 channels at every level, 3x3x3 convolutions, 2 x 2 x 2 average pooling
+# (the coarsest level of a 40^3 grid is 5^3), the same encoder-decoder graph as the 2-D one
+LAYERS3 = [("e0a", 16, 0, 16, 1), ("e0b", 16, 0, 16, 1), ("e1a", 16, 0, 16, 1), ("e1b", 16, 0, 16, 1),
+           ("e2a", 16, 0, 16, 1), ("e2b", 16, 0, 16, 1), ("b3a", 16, 0, 16, 1), ("b3b", 16, 0, 16, 1),
+           ("d2a", 16, 16, 16, 1), ("d2b", 16, 0, 16, 1), ("d1a", 16, 16, 16, 1), ("d1b", 16, 0, 16, 1),
+           ("d0a", 16, 16, 16, 1), ("d0b", 16, 0, 16, 1), ("out", 16, 0, 16, 0)]
+POOL3 = 2
+
+
+class UNet3D(UNet):
+    """The 3-D U-Net on NDHWC tensors (include/autopdex_gb300_nn.h, the 3-D part)."""
+
+    dims = 3
+    layers = LAYERS3
+    pool = POOL3
+    hid = 16
+
+
+def padded3(n):
+    """Grid extent padded to a multiple of POOL3^3 (three poolings)."""
+    m = POOL3 ** 3
+    return (n + m - 1) // m * m
 
 
 # ---- grids, features, data ---------------------------------------------------------------
@@ -628,7 +692,7 @@ def train(net, ts, steps=3000, batch=16, lr=2e-3, seed=0, verbose=False):
         # the backward pass is linear in g: run it on g / max|g| (bf16-friendly) and rescale
         gmax = float(g.abs().max().clamp_min(1e-30))
         gw, gb = net.backward((g / gmax).to(torch.bfloat16), acts)
-        for name, *_ in LAYERS:
+        for name, *_ in net.layers:
             net.w[name].grad = gw[name] * gmax
             net.b[name].grad = gb[name] * gmax
         if bool(torch.stack([torch.isfinite(t.grad).all() for t in params]).all()):
@@ -757,8 +821,11 @@ class GridPreconditioner:
         prob._call("agx_set_preconditioner_mode", int(self.mode), float(self.omega), int(self.sweeps), flags)
         prob.learned = self
 
+    def _grid_dofs(self):
+        return (self.nx + 1) * (self.ny + 1) * self.nd
+
     def callback(self, prob):
-        if prob.n_dofs != (self.nx + 1) * (self.ny + 1) * self.nd:
+        if prob.n_dofs != self._grid_dofs():
             raise ValueError("the learned preconditioner was built for another grid")
         if self.factor > 1 and self.fixed is None:
             self.fixed = torch.as_tensor(prob.mask.astype(np.uint8), device=self.net.device)
@@ -772,3 +839,199 @@ class GridPreconditioner:
             except Exception:  # noqa: BLE001 -- report through the status code
                 return -1
         return N.PRECOND_FN(fn)
+
+
+# ---- the 3-D variant: structured brick meshes -------------------------------------------------
+class BrickPreconditioner(GridPreconditioner):
+    """The 3-D network as the coarse solver of the two-level preconditioner on the node grid of
+    an n x n x n structured brick mesh (scalar field, ``mesher.structured_mesh`` node order).
+
+    The network works on the grid coarsened by ``factor`` (trilinear P), padded to a multiple
+    of 8 voxels a side; its input channels are the restricted residual / rms and a 0/1
+    indicator of the coarse grid inside the padding.  Smoothing (Chebyshev by default), the
+    energy-optimal step and the capture into CUDA graphs are those of
+    :class:`GridPreconditioner`."""
+
+    def __init__(self, net, n, factor=4, mode=3, omega=None, sweeps=None, fixed=None):
+        if n % factor:
+            raise ValueError("the grid must be divisible by the coarsening factor")
+        if getattr(net, "dims", 2) != 3:
+            raise ValueError("BrickPreconditioner needs a UNet3D")
+        self.net, self.nd, self.bf16_smoothing = net, 1, False
+        self.mode = mode
+        self.omega = omega if omega is not None else (OMEGA if mode != 3 else 1.0 / 30.0)
+        self.sweeps = sweeps if sweeps is not None else (2 if mode != 3 else 3)
+        self.factor, self.n = factor, n
+        self.nc = n // factor + 1
+        self.npad = padded3(self.nc)
+        dev = net.device
+        self.img = torch.zeros((1, self.npad, self.npad, self.npad, C_IN), dtype=torch.bfloat16, device=dev)
+        self.scale = torch.empty(1, dtype=torch.float32, device=dev)
+        self.rc = torch.zeros(self.nc ** 3, dtype=torch.float32, device=dev)
+        self.work = torch.zeros(net.lib.agx_nn_restrict_image3d_work(), dtype=torch.float64, device=dev)
+        self.fixed = None if fixed is None else torch.as_tensor(np.asarray(fixed, dtype=np.uint8), device=dev)
+        self.arena = {}
+        self.applications = 0
+        self.skip_flag = None
+        net.forward(self.img, arena=self.arena)
+        torch.cuda.synchronize(dev)
+        net.const_weights = True
+
+    def _grid_dofs(self):
+        return (self.n + 1) ** 3
+
+    def _apply(self, lib, r_ptr, z_ptr, stream):
+        st = C.c_void_p(stream)
+        nc, npad, f = self.nc, self.npad, self.factor
+        rc = lib.agx_nn_restrict_image3d(C.c_void_p(r_ptr), _p(self.fixed), nc, nc, nc, f, npad, npad, npad,
+                                         _p(self.rc), _p(self.work), _p(self.scale), _p(self.img), st)
+        if rc != 0:
+            return rc
+        out = self.net.forward(self.img, stream=st, arena=self.arena)
+        rc = lib.agx_nn_prolong_image3d(_p(out), C_OUT, nc, nc, nc, npad, npad, f, _p(self.fixed), C.c_void_p(z_ptr),
+                                        st)
+        self.net.launches += 3
+        self.applications += 1
+        return rc
+
+
+ITERATES3 = (0, 2, 5, 10, 20, 40)
+
+
+def _random_rhs3(rng, m, device):
+    """Smooth-plus-rough random field on an m x m x m node grid."""
+    f = np.zeros((m, m, m))
+    for scale in (4, 16):
+        c = rng.standard_normal((scale, scale, scale))
+        k = m // scale + 1
+        f += np.kron(c, np.ones((k, k, k)))[:m, :m, :m] / math.sqrt(scale)
+    f += 0.1 * rng.standard_normal((m, m, m))
+    return torch.as_tensor(f.reshape(-1), dtype=torch.float64, device=device)
+
+
+def make_brick_training_set(n=128, states=2, rhs_per_state=4, seed0=0, iterates=ITERATES3, krylov_tol=1e-10,
+                            omega=OMEGA, factor=4, verbose=False):
+    """Samples of the 128^3 backward-Euler heat workload's family: for ``states`` seeded random
+    temperature fields T (the tangent of the first Newton step of a time step from T, with
+    k = 1 + 0.5 T^2) and right-hand sides (the Newton residual at T, then smooth-plus-rough
+    random fields), the iterates of the plain float64 Jacobi-PCG solver give (residual, error)
+    pairs as in :func:`make_training_set`."""
+    from . import configs
+    from ._problem import get_problem
+    w = configs.heat_transient(n=n, seed=seed0)
+    prob = get_problem(w.dofs, w.settings, w.static_settings)
+    dev = prob.device
+    mask = torch.as_tensor(prob.mask.astype(bool), device=dev)
+    free = (~mask).float()
+    rng = np.random.default_rng(seed0 + 4321)
+    nv = prob.nnzb * prob.ndof * prob.ndof
+    values = torch.empty((states, nv), dtype=torch.float32, device=dev)
+    S = states * rhs_per_state * len(iterates)
+    r1s = torch.empty((S, prob.n_dofs), dtype=torch.float32, device=dev)
+    ss = torch.empty(S, dtype=torch.float32, device=dev)
+    pid = torch.empty(S, dtype=torch.int64)
+    t = torch.empty(prob.n_dofs, dtype=torch.float64, device=dev)
+    xs, xk, z, res = (torch.empty_like(t) for _ in range(4))
+    j_out = 0
+    for i in range(states):
+        T = torch.as_tensor(rng.uniform(0.0, 1.0, prob.n_dofs), device=dev)
+        T[mask] = 0.0
+        w.settings["dofs n"] = {"T": T.cpu().numpy()}
+        prob.update_models(w.settings)
+        prob._call("agx_assemble", C.c_void_p(T.data_ptr()), C.c_void_p(res.data_ptr()), N.AGX_F64)
+        for j in range(rhs_per_state):
+            b = -res.clone() if j == 0 else _random_rhs3(rng, n + 1, dev)
+            b = torch.where(mask, torch.zeros_like(b), b)
+            info = _solve(prob, b, xs, krylov_tol, 200000)
+            for it in iterates:
+                if it == 0:
+                    xk.zero_()
+                else:
+                    _solve(prob, b, xk, 0.0, it)
+                prob._call("agx_spmv", N.AGX_F64, C.c_void_p(xk.data_ptr()), C.c_void_p(t.data_ptr()))
+                r = b - t
+                prob._call("agx_jacobi", N.AGX_F64, C.c_void_p(r.data_ptr()), C.c_void_p(z.data_ptr()))
+                z.mul_(omega)
+                prob._call("agx_spmv", N.AGX_F64, C.c_void_p(z.data_ptr()), C.c_void_p(t.data_ptr()))
+                r1 = r - t
+                e1 = (xs - xk) - z
+                r1[mask] = 0.0
+                e1[mask] = 0.0
+                rms = r1.pow(2).mean().sqrt().clamp_min(1e-300)
+                r1s[j_out] = (r1 / rms).float()
+                ss[j_out] = float((r1 @ e1) / (rms * rms))
+                pid[j_out] = i
+                j_out += 1
+            if verbose:
+                print(f"state {i} rhs {j}: {info.iterations} CG iterations to {krylov_tol:g}", flush=True)
+        prob._call("agx_assemble", C.c_void_p(T.data_ptr()), None, N.AGX_F32)
+        prob._call("agx_copy_values", N.AGX_F32, C.c_void_p(values[i].data_ptr()))
+    return TrainingSet(n, prob, r1s, ss, pid, None, values, free, nd=1, naux=0, factor=factor)
+
+
+def train3d(net, ts, steps=1000, batch=4, lr=2e-3, seed=0, verbose=False):
+    """:func:`train` for the 3-D network: input image restrict_image3d(P^T r1) (as the
+    preconditioner builds it), y = P (output channel 0), dL/d(output) = P^T dL/dy."""
+    lib = net.lib
+    prob = ts.prob
+    f = ts.factor
+    nc = ts.n // f + 1
+    npad = padded3(nc)
+    fixed = torch.as_tensor(prob.mask.astype(np.uint8), device=net.device)
+    dev = net.device
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    x = torch.zeros((batch, npad, npad, npad, C_IN), dtype=torch.bfloat16, device=dev)
+    rc = torch.empty((batch, nc ** 3), dtype=torch.float32, device=dev)
+    work = torch.empty(lib.agx_nn_restrict_image3d_work(), dtype=torch.float64, device=dev)
+    sc = torch.empty(batch, dtype=torch.float32, device=dev)
+    y = torch.empty((batch, prob.n_dofs), dtype=torch.float32, device=dev)
+    Ky = torch.empty_like(y)
+    gc = torch.empty((batch, nc ** 3), dtype=torch.float32, device=dev)
+    g = torch.zeros((batch, npad, npad, npad, C_OUT), dtype=torch.float32, device=dev)
+    params = net.parameters()
+    opt = torch.optim.Adam(params, lr=lr)
+    sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, steps)
+    gen = torch.Generator().manual_seed(seed)
+    losses = []
+
+    def ok(name, rcode):
+        if rcode != 0:
+            raise RuntimeError(f"{name} failed with status {rcode}")
+    for step in range(steps):
+        idx = torch.randint(0, len(ts), (batch,), generator=gen)
+        pids = ts.pid[idx].tolist()
+        for b, i in enumerate(idx.tolist()):
+            ok("agx_nn_restrict_image3d",
+               lib.agx_nn_restrict_image3d(_p(ts.r1[i]), _p(fixed), nc, nc, nc, f, npad, npad, npad, _p(rc[b]),
+                                           _p(work), _p(sc[b:b + 1]), _p(x[b:b + 1]), stream))
+        out, acts = net.forward(x, keep=True)
+        for b in range(batch):
+            ok("agx_nn_prolong_image3d",
+               lib.agx_nn_prolong_image3d(_p(out[b:b + 1]), C_OUT, nc, nc, nc, npad, npad, f, _p(fixed), _p(y[b]),
+                                          stream))
+        for b, pi in enumerate(pids):
+            prob._call("agx_spmv_values", N.AGX_F32, C.c_void_p(ts.values[pi].data_ptr()),
+                       C.c_void_p(y[b].data_ptr()), C.c_void_p(Ky[b].data_ptr()))
+        r1 = ts.r1[idx.to(dev)]
+        loss, grad = energy_loss(r1, y, Ky, ts.s[idx.to(dev)])
+        gy = (grad * ts.free / batch).contiguous()
+        for b in range(batch):  # y = P y_c, zero at fixed nodes: dL/dy_c = P^T (dL/dy masked)
+            ok("agx_nn_restrict3d", lib.agx_nn_restrict3d(_p(gy[b]), None, nc, nc, nc, f, _p(gc[b]), stream))
+        g[:, :nc, :nc, :nc, 0] = gc.reshape(batch, nc, nc, nc)
+        gmax = float(g.abs().max().clamp_min(1e-30))
+        gw, gb = net.backward((g / gmax).to(torch.bfloat16), acts)
+        for name, *_ in net.layers:
+            net.w[name].grad = gw[name] * gmax
+            net.b[name].grad = gb[name] * gmax
+        if bool(torch.stack([torch.isfinite(t.grad).all() for t in params]).all()):
+            opt.step()
+        sched.step()
+        opt.zero_grad(set_to_none=True)
+        with torch.no_grad():
+            net.w["e0a"][:, net.n_in:] = 0.0
+        net.pack()
+        losses.append(float(loss.mean()))
+        if verbose and step % 100 == 0:
+            print(f"step {step}: loss {np.mean(losses[-50:]):.4f}", flush=True)
+    net.check()
+    return losses

@@ -4,6 +4,8 @@
         --out autopdex_gb300/weights/heat_unet_n256.npz
     python -m autopdex_gb300.train_preconditioner --problem membrane --n 128 --steps 3000 \
         --out autopdex_gb300/weights/membrane_unet_n128.npz
+    python -m autopdex_gb300.train_preconditioner --problem brick --n 128 --problems 2 \
+        --rhs-per-state 4 --factor 4 --steps 1500 --batch 4
 
 heat: training pairs (residual, error) come from the iterates of the plain float64 Jacobi-PCG
 solver on heat-conduction problems -div(k grad T) = b with k = exp(Gaussian random field) seeded
@@ -12,6 +14,10 @@ constant and one random right-hand side each.
 membrane: the nearly incompressible Cook membrane (the 512 x 512 membrane workload's geometry
 at n x n), tangents at converged load states, random vector right-hand sides after the
 Chebyshev pre-smoothing of the native FCG, error energies from the banded Cholesky factor.
+brick: the 3-D network (UNet3D) on the 128^3 backward-Euler heat workload's family: tangents
+of the first Newton step from seeded random temperature fields, right-hand sides the Newton
+residual and random fields, pairs from the plain float64 Jacobi-PCG iterates; the network
+works on the grid coarsened by --factor.
 """
 import argparse
 import json
@@ -31,7 +37,7 @@ def main():
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--problem", default="heat", choices=["heat", "membrane"])
+    ap.add_argument("--problem", default="heat", choices=["heat", "membrane", "brick"])
     ap.add_argument("--rhs-per-state", type=int, default=400)
     ap.add_argument("--factor", type=int, default=1, help="membrane: train the network on the grid coarsened by this")
     ap.add_argument("--degree", type=int, default=3, help="membrane: Chebyshev pre-smoothing degree")
@@ -43,12 +49,17 @@ def main():
     if args.problem == "heat":
         ts = learned.make_training_set(args.problems, n=args.n, seed0=args.seed, verbose=True)
         net = learned.UNet(seed=args.seed)
+    elif args.problem == "brick":
+        ts = learned.make_brick_training_set(n=args.n, states=args.problems, rhs_per_state=args.rhs_per_state,
+                                             seed0=args.seed, factor=args.factor, verbose=True)
+        net = learned.UNet3D(seed=args.seed)
     else:
         ts = learned.make_membrane_training_set(n=args.n, rhs_per_state=args.rhs_per_state, seed=args.seed,
                                                 factor=args.factor, degree=args.degree, verbose=True)
         net = learned.UNet(seed=args.seed, n_in=ts.nd + ts.naux)
     t1 = time.time()
-    losses = learned.train(net, ts, steps=args.steps, batch=args.batch, lr=args.lr, verbose=True)
+    fit = learned.train3d if args.problem == "brick" else learned.train
+    losses = fit(net, ts, steps=args.steps, batch=args.batch, lr=args.lr, verbose=True)
     torch.cuda.synchronize()
     t2 = time.time()
     os.makedirs(os.path.dirname(args.out), exist_ok=True)

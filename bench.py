@@ -610,18 +610,31 @@ def rec_heat(h):
 
 def rec_heat_be(n=128, steps=10, plain_steps=3):
     import torch
-    from autopdex_gb300 import configs, solver
+    from autopdex_gb300 import configs, learned, solver
     out = {"workload": f"heat_be_{n}^3_hex8 (k = 1 + 0.5 T^2, dt = 1e-3), time steps 1..{steps} of 100"}
-    for name, sol_name, prec, ktol, nsteps in (("mixed_pcg", "pcg", "mixed", 1e-5, steps),
-                                               ("plain_fp64_bicgstab", "bicgstab", "float64", 1e-11, plain_steps)):
-        w = configs.heat_transient(n=n, solver=sol_name, precision=prec)
+    variants = [("mixed_pcg", dict(solver="pcg", precision="mixed"), 1e-5, steps),
+                ("plain_fp64_bicgstab", dict(solver="bicgstab", precision="float64"), 1e-11, plain_steps)]
+    wpath = os.path.join(learned.WEIGHTS_DIR, f"brick_unet_n{n}.npz")
+    if os.path.exists(wpath):
+        variants.insert(1, ("learned_mixed_fcg", dict(solver="fcg", precision="mixed",
+                                                      **{"type of preconditioner": "learned"}), 1e-3, steps))
+    for name, st, ktol, nsteps in variants:
+        w = configs.heat_transient(n=n)
+        static = dict(w.static_settings, **st)
+        pc = None
+        if name.startswith("learned"):
+            net = learned.UNet3D.load(wpath)
+            pc = learned.BrickPreconditioner(net, n, factor=4)
+            solver.set_learned_preconditioner(None, pc)
+            out["network"] = {"weights": os.path.basename(wpath), "grid": f"{pc.nc}^3 nodes (coarsening 4), "
+                              f"image {pc.npad}^3"}
         dev = torch.device("cuda", torch.cuda.current_device())
         T0 = torch.as_tensor(w.raw["T0"], device=dev)
         kw = dict(newton_tol=0.0, newton_rtol=RTOL, maxiter=30, krylov_tol=ktol)
         settings = dict(w.settings)
         settings["dofs n"] = {"T": T0.clone()}
         settings["dirichlet conditions"] = {"T": torch.zeros_like(T0)}
-        solver.solver({"T": T0.clone()}, settings, w.static_settings, **kw)  # context, tuning, graphs
+        solver.solver({"T": T0.clone()}, settings, static, **kw)  # context, tuning, graphs
         per = []
         first = {}
 
@@ -629,38 +642,61 @@ def rec_heat_be(n=128, steps=10, plain_steps=3):
             T = T0.clone()
             for k in range(nsteps):
                 settings["dofs n"] = {"T": T}
-                Tn, _ = solver.solver({"T": T}, settings, w.static_settings, **kw)
+                Tn, _ = solver.solver({"T": T}, settings, static, **kw)
                 per.append(_info())
                 if k == 0:
                     first["T1"] = Tn["T"].clone()
                 T = Tn["T"]
             return T
+        if pc is not None:
+            pc.applications = 0
         s, T = _timed(run)
+        if pc is not None:
+            solver.set_learned_preconditioner(None, None)
         out[name] = {"s_per_step": s / nsteps, "steps": nsteps, "newton": sum(p["newton"] for p in per),
                      "krylov": sum(p["krylov"] for p in per),
                      "max_residual_ratio": max(p["residual_ratio"] for p in per),
                      "sum_T_squared": float((T * T).sum())}
+        if pc is not None:
+            out[name]["network_applications"] = pc.applications
         if name == "mixed_pcg":
-            st = dict(w.settings)
-            st["dofs n"] = {"T": w.raw["T0"]}
-            out["oracle_error_first_step"] = oracle_errors(w, first["T1"], per[0]["res0"], settings=st, scale=1.0)
-    out["speedup_mixed_vs_plain_fp64"] = out["plain_fp64_bicgstab"]["s_per_step"] / out["mixed_pcg"]["s_per_step"]
+            st0 = dict(w.settings)
+            st0["dofs n"] = {"T": w.raw["T0"]}
+            out["oracle_error_first_step"] = oracle_errors(w, first["T1"], per[0]["res0"], settings=st0, scale=1.0)
+    base = out["plain_fp64_bicgstab"]["s_per_step"]
+    out["speedup_mixed_vs_plain_fp64"] = base / out["mixed_pcg"]["s_per_step"]
+    if "learned_mixed_fcg" in out:
+        out["speedup_learned_vs_plain_fp64"] = base / out["learned_mixed_fcg"]["s_per_step"]
+    try:
+        out["assembly_hbm"] = assembly_roofline(workload="heat_be", n=n)
+    except Exception as e:  # noqa: BLE001 -- the record keeps the solve numbers
+        out["assembly_hbm"] = {"error": str(e)[:200]}
     return out
 
 
-def assembly_roofline(n=1024, reps=20):
-    """Float32 tangent assembly of the n^2 random-conductivity heat mesh, timed with CUDA events
-    per agx_assemble call after a 256 MB buffer write (inputs from HBM).  Algorithmic bytes:
-    coordinates + DOFs + connectivity + values written once (n_nodes dim 8 + n_dofs 8 + n_e nen 4
-    + nnz 4)."""
+def assembly_roofline(n=1024, reps=20, workload="heat_grf"):
+    """Float32 tangent assembly, timed with CUDA events per agx_assemble call after a 256 MB
+    buffer write (inputs from HBM): of the n^2 random-conductivity heat mesh (``heat_grf``,
+    the structured-grid kernel) or of the n^3 backward-Euler brick mesh (``heat_be``, the
+    element kernel with its scatter into the tangent's slots).  Algorithmic bytes: coordinates
+    + DOFs (+ the previous time step's DOFs) + connectivity + values written once (n_nodes dim 8
+    + n_dofs 8 (x 2) + n_e nen 4 + nnz 4)."""
     import ctypes as C
     import torch
     from autopdex_gb300 import configs, _native as N
     from autopdex_gb300._problem import get_problem
-    w = configs.heat_grf(n=n, seed=0)
+    if workload == "heat_be":
+        w = configs.heat_transient(n=n)
+        dim, nen, n_e, kernel = 3, 8, n ** 3, "element_kernel<HEAT_BE, float> (scatter into the slot map)"
+    else:
+        w = configs.heat_grf(n=n, seed=0)
+        dim, nen, n_e, kernel = 2, 4, n * n, "grid_tangent_kernel<HEAT_POTENTIAL,float>"
     prob = get_problem(w.dofs, w.settings, w.static_settings)
     prob.update_models(w.settings)
-    x = torch.zeros(prob.n_dofs, dtype=torch.float64, device=prob.device)
+    if workload == "heat_be":
+        x = torch.as_tensor(w.raw["T0"], dtype=torch.float64, device=prob.device)
+    else:
+        x = torch.zeros(prob.n_dofs, dtype=torch.float64, device=prob.device)
     for _ in range(3):
         prob._call("agx_assemble", C.c_void_p(x.data_ptr()), None, N.AGX_F32)
     flush = _flush_buffer()
@@ -679,12 +715,13 @@ def assembly_roofline(n=1024, reps=20):
             prob._call("agx_assemble", C.c_void_p(x.data_ptr()), None, N.AGX_F32)
     ms, cnt = _profile(prob, kern)
     del flush
-    n_e = n * n
-    nbytes = prob.n_nodes * 2 * 8 + prob.n_dofs * 8 + n_e * 4 * 4 + prob.nnzb * 4
+    nbytes = prob.n_nodes * dim * 8 + prob.n_dofs * 8 * (2 if workload == "heat_be" else 1) + n_e * nen * 4 + \
+        prob.nnzb * prob.ndof * prob.ndof * 4
     call_s = call_ms / 1e3 / reps
     kern_s = ms["tangent_assembly"] / 1e3 / max(1, cnt["tangent_assembly"])
     peak, _, kind = _peaks()
-    return {"workload": f"heat_grf_{n}x{n}_q1 float32 tangent", "kernel": "grid_tangent_kernel<HEAT_POTENTIAL,float>",
+    name = f"heat_be_{n}^3_hex8" if workload == "heat_be" else f"heat_grf_{n}x{n}_q1"
+    return {"workload": f"{name} float32 tangent", "kernel": kernel,
             "algorithmic_bytes": nbytes, "call_us": call_s * 1e6, "kernel_us": kern_s * 1e6,
             "achieved_gbs_call": nbytes / call_s / 1e9, "achieved_gbs_kernel": nbytes / kern_s / 1e9,
             "peak_gbs": peak, "frac_call": nbytes / call_s / 1e9 / peak, "frac_kernel": nbytes / kern_s / 1e9 / peak,
@@ -825,12 +862,12 @@ def case(args):
         g = torch.Generator(device="cuda").manual_seed(0)
         x1 = torch.randn(1, args.size, args.size, c1, device="cuda", generator=g).to(torch.bfloat16)
         x2 = torch.randn(1, args.size, args.size, c2, device="cuda", generator=g).to(torch.bfloat16) if c2 else None
-        net._conv(args.layer, x1, x2, 1, args.size, args.size)  # warm-up (attributes, first launch)
+        net._conv(args.layer, x1, x2, 1, (args.size, args.size))  # warm-up (attributes, first launch)
         _sync()
         a, b = _events()
         a.record()
         for _ in range(args.reps):
-            net._conv(args.layer, x1, x2, 1, args.size, args.size)
+            net._conv(args.layer, x1, x2, 1, (args.size, args.size))
         b.record()
         _sync()
         net.check()

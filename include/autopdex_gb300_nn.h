@@ -105,6 +105,44 @@ int agx_nn_restrict_image(const float* fine, const unsigned char* fixed, int nd,
 int agx_nn_prolong_image(const void* img, int C, int nd, int Hc, int Wc, int Wp, int f, const unsigned char* fixed,
                          float* fine, void* stream);
 
+/* ---- the 3-D network (structured brick meshes) -----------------------------------------
+   Tensors are NDHWC bf16 (batch, z, y, x, channel).  agx_nn_conv3x3x3: 3x3x3 convolution,
+   stride 1, zero padding 1, of concat(in1 [c1 channels], in2 [c2]) with the weight image of
+   agx_nn_pack_weights3d (mode 0: forward; mode 1: the input-gradient image, whose output
+   splits into out1 [split channels] and out2 [cout - split]); relu as agx_nn_conv3x3
+   (bit 0 ReLU, AGX_NN_CONST_WEIGHTS).  Supported (c1, c2, cout): (16, 0, 16) with and without
+   ReLU, (16, 16, 16) with ReLU, (16, 0, 32) without (the input gradient of a concatenating
+   layer).  Tensors 16-byte aligned.  agx_nn_wgrad3x3x3 accumulates dW rows (27 (c1 + c2)) x cout
+   as agx_nn_wgrad3x3 does, for (16, 0, 16) and (16, 16, 16); agx_nn_unpack_wgrad3d turns them
+   into the [cout][cin][3][3][3] layout.  Taps are t = 9 dz + 3 dy + dx. */
+int agx_nn_conv3x3x3(const void* in1, const void* in2, int c1, int c2, const void* wpk, const float* bias, void* out1,
+                     void* out2, int split, int cout, int relu, int B, int D, int H, int W, int* err, void* stream);
+int agx_nn_wgrad3x3x3(const void* in1, const void* in2, int c1, int c2, const void* dout, int cout, float* dw_rows,
+                      int B, int D, int H, int W, int* err, void* stream);
+int agx_nn_pack_weights3d(const float* w, int cout, int cin, int mode, void* img, void* stream);
+int agx_nn_unpack_wgrad3d(const float* dw_rows, int cout, int cin, float* dw, void* stream);
+/* f x f x f average pooling (backward = 0; D, H, W: full size, multiples of f) or its adjoint
+   (backward = 1: every voxel of a block gets coarse / f^3); nearest f x upsampling (backward = 0;
+   D, H, W: coarse size) or its adjoint (block sums).  C a multiple of 8, 16-byte aligned. */
+int agx_nn_pool3d(const void* in, void* out, int B, int D, int H, int W, int C, int f, int backward, void* stream);
+int agx_nn_upsample3d(const void* in, void* out, int B, int D, int H, int W, int C, int f, int backward, void* stream);
+/* Transfers between the scalar node field of a structured brick mesh -- ((Dc-1) f + 1) x
+   ((Hc-1) f + 1) x ((Wc-1) f + 1) nodes, node (i, j, k) at (i Hf + j) Wf + k -- and the
+   network's coarse grid of Dc x Hc x Wc nodes, coarse node (I, J, K) on fine node (f I, f J, f K);
+   P is trilinear interpolation.  agx_nn_restrict_image3d: coarse = P^T fine (zero where the
+   fine node under it is flagged in `fixed`, optional) and the input image (Dp x Hp x Wp voxels,
+   16 channels: coarse / rms, then 1 inside the coarse grid) with 1 / rms in scale[0], in two
+   launches (`work`: agx_nn_restrict_image3d_work() doubles).  agx_nn_restrict3d: coarse = P^T
+   fine alone.  agx_nn_prolong_image3d: fine = P applied to channel 0 of an image with C
+   channels, zero at flagged nodes. */
+int agx_nn_restrict_image3d_work(void);
+int agx_nn_restrict_image3d(const float* fine, const unsigned char* fixed, int Dc, int Hc, int Wc, int f, int Dp,
+                            int Hp, int Wp, float* coarse, double* work, float* scale, void* img, void* stream);
+int agx_nn_restrict3d(const float* fine, const unsigned char* fixed, int Dc, int Hc, int Wc, int f, float* coarse,
+                      void* stream);
+int agx_nn_prolong_image3d(const void* img, int C, int Dc, int Hc, int Wc, int Hp, int Wp, int f,
+                           const unsigned char* fixed, float* fine, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -222,3 +222,56 @@ def test_dlpack_inputs_match_numpy_path():
     assert isinstance(sol, torch.Tensor) and sol.is_cuda and tuple(sol.shape) == np.shape(w.dofs)
     assert np.abs(sol.cpu().numpy() - np.asarray(ref)).max() <= 1e-12 * max(1.0, np.abs(ref).max())
     assert torch.count_nonzero(d0) == 0
+
+
+def _sheared_brick_heat_be(shape=(6, 5, 4), seed=3):
+    """The 128^3 backward-Euler heat workload's model (configs.heat_transient) on a sheared,
+    non-cubic brick grid: a parallelepiped lattice, so the assembly takes the uniform brick
+    grid's kernels with a full (non-diagonal) Jacobian."""
+    from autopdex_gb300 import mesher, models, seeder, spaces
+    from autopdex_gb300.configs import Workload
+    e1, e2, e3 = np.array([1.2, 0.1, 0.0]), np.array([0.3, 0.9, 0.2]), np.array([0.1, 0.2, 0.8])
+    verts = np.array([0 * e1, e1, e1 + e2, e2, e3, e1 + e3, e1 + e2 + e3, e2 + e3])
+    coords, elems = mesher.structured_mesh(shape, verts, "brick")
+    nx, ny, nz = shape
+    idx = np.arange(coords.shape[0])
+    i, j, k = idx // ((ny + 1) * (nz + 1)), (idx // (nz + 1)) % (ny + 1), idx % (nz + 1)
+    bnd = (i == 0) | (i == nx) | (j == 0) | (j == ny) | (k == 0) | (k == nz)
+    rng = np.random.default_rng(seed)
+    T0 = rng.uniform(0.0, 1.0, coords.shape[0])
+    T0[bnd] = 0.0
+    dt = 1e-3
+    integrand = models.heat_backward_euler_integrand(1.0, 0.5, 1.0, "time increment", "dofs n")
+    model = models.mixed_reference_domain_residual(integrand, {"T": spaces.fem_iso_line_quad_brick},
+                                                   *seeder.gauss_legendre_nd(3, 2), "T")
+    static = {"assembling mode": ("user residual",), "solution structure": ("nodal imposition",),
+              "model": (model,), "solver type": "newton", "solver backend": "gb300", "solver": "pcg",
+              "precision": "mixed", "verbose": -1}
+    settings = {"connectivity": ({"T": elems},), "dirichlet dofs": {"T": bnd}, "node coordinates": {"T": coords},
+                "dirichlet conditions": {"T": np.zeros(coords.shape[0])}, "dofs n": {"T": T0.copy()},
+                "time increment": dt}
+    raw = dict(coords=coords, conns=[elems], dirichlet=bnd, values=np.zeros(coords.shape[0]), T0=T0, dt=dt,
+               kind="heat_be", n_steps=1)
+    return Workload("heat_be_sheared_brick", {"T": T0.copy()}, settings, static, raw)
+
+
+def test_sheared_brick_grid_residual_and_float32_tangent_match_oracle():
+    """The uniform brick grid's float64 residual (sum-factorised) and float32 row-gathered
+    tangent against the oracle at random DOFs; tolerances as above (1e-12 and 2e-6)."""
+    from autopdex_gb300 import assembler
+    w = _sheared_brick_heat_be()
+    u = _random_dofs(w, 1.0, seed=5)
+    R_gpu = _flat(assembler.assemble_residual(_like(w, u), w.settings, w.static_settings))
+    prob = oracle_problem(w)
+    R_or, coo = newton.assemble(prob.sets, u, prob.coords, oracle_settings(w), prob.n_dofs)
+    assert np.linalg.norm(R_gpu - R_or) <= 1e-12 * np.linalg.norm(R_or)
+    K = assembler.assemble_tangent(_like(w, u), w.settings, w.static_settings, dtype="float32").to_scipy()
+    K_or = newton.scipy_assembling(coo, prob.n_dofs, None)
+    assert abs(K - K_or).max() <= 2e-6 * abs(K_or).max()
+    Kd = assembler.assemble_tangent(_like(w, u), w.settings, w.static_settings, dtype="float32",
+                                    eliminate_dirichlet=True).to_scipy()
+    free = ~prob.dirichlet
+    K_red = newton.scipy_assembling(coo, prob.n_dofs, free)
+    assert abs(Kd[free][:, free] - K_red).max() <= 2e-6 * abs(K_red).max()
+    assert np.array_equal(Kd[prob.dirichlet].toarray(),
+                          scipy.sparse.eye(prob.n_dofs, format="csr")[prob.dirichlet].toarray())
