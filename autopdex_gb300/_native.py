@@ -87,6 +87,7 @@ _SIGNATURES = {
     "agx_autotune": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
     "agx_set_tuning": (C.c_int, [_P, C.c_int, C.c_int]),
     "agx_grid_pattern": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "agx_brick_pattern": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "agx_set_pdl": (C.c_int, [C.c_int]),
     "agx_solve_flag": (C.c_int, [_P, C.POINTER(_P)]),
     "agx_nn_set_skip_flag": (C.c_int, [_P]),

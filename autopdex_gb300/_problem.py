@@ -213,11 +213,12 @@ class Problem:
         import json
         from . import build as _b
         path = os.path.join(_b.LIBDIR, "autotune.json")
-        gny = C.c_int()
+        gny, brick = C.c_int(), C.c_int()
         self._call("agx_grid_pattern", C.byref(gny))
+        self._call("agx_brick_pattern", C.byref(brick))
         key = f"{torch.cuda.get_device_name(self.device)}|{'f32' if dtype == N.AGX_F32 else 'f64'}|" \
               f"ndof={self.ndof}|dim={self.dim}|nnzb=2^{int(np.log2(max(1, self.nnzb)))}" \
-              f"{'|grid' if gny.value > 0 else ''}"
+              f"{'|grid' if gny.value > 0 else ''}{'|brick' if brick.value > 0 else ''}"
         cache = {}
         try:
             with open(path) as fh:

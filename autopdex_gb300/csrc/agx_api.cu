@@ -505,6 +505,13 @@ int agx_autotune(agx_context* ctx, int* spmv_tpr, float* spmv_ms) {
 int agx_set_tuning(agx_context* ctx, int dtype, int spmv_tpr) {
   if (!ctx) return AGX_ERR_ARG;
   if (dtype != AGX_F64 && dtype != AGX_F32) return agx_fail(ctx, AGX_ERR_ARG, "dtype must be AGX_F64 or AGX_F32");
+  if (spmv_tpr == SPMV_BRICK) {
+    if (ctx->pattern_brick <= 0)
+      return agx_fail(ctx, AGX_ERR_ARG, "the brick product (2048) needs the pattern of a structured HEX8 grid "
+                                        "with 1 to 3 DOFs per node");
+    ctx->spmv_tpr[dtype == AGX_F32 ? 1 : 0] = spmv_tpr;
+    return AGX_OK;
+  }
   if (spmv_is_grid(spmv_tpr)) {
     if (ctx->pattern_grid_ny <= 0)
       return agx_fail(ctx, AGX_ERR_ARG, "the grid products (512, 1024) need the pattern of a structured QUAD4 grid "
@@ -540,6 +547,12 @@ int agx_solve_flag(agx_context* ctx, const int** flag) {
 int agx_grid_pattern(const agx_context* ctx, int* ny) {
   if (!ctx || !ny) return AGX_ERR_ARG;
   *ny = ctx->pattern_grid_ny;
+  return AGX_OK;
+}
+
+int agx_brick_pattern(const agx_context* ctx, int* code) {
+  if (!ctx || !code) return AGX_ERR_ARG;
+  *code = ctx->pattern_brick;
   return AGX_OK;
 }
 

@@ -79,8 +79,9 @@ struct agx_krylov_scalars {
 constexpr int SPMV_UNROLL4 = 256;
 constexpr int SPMV_GRID = 512;
 constexpr int SPMV_GRID2 = 1024;  // the grid product with two rows per lane
+constexpr int SPMV_BRICK = 2048;  // the structured brick grid's index-free 27-node product
 inline int spmv_lanes(int code) {
-  return (code == SPMV_GRID || code == SPMV_GRID2) ? 1 : (code & (SPMV_UNROLL4 - 1));
+  return (code == SPMV_GRID || code == SPMV_GRID2 || code == SPMV_BRICK) ? 1 : (code & (SPMV_UNROLL4 - 1));
 }
 inline bool spmv_is_grid(int code) { return code == SPMV_GRID || code == SPMV_GRID2; }
 
@@ -133,6 +134,11 @@ struct agx_context {
   // > 0: the pattern is the in-range 3 x 3 stencil of a structured nx x ny QUAD4 grid with
   // ny = pattern_grid_ny (the index-free product SPMV_GRID applies)
   int pattern_grid_ny = 0;
+  // pattern of a structured nx x ny x nz brick grid (27-node stencils, 1 to 3 DOFs per node):
+  // (ny << 16) | nz, 0 otherwise (the index-free product SPMV_BRICK applies)
+  int pattern_brick = 0;
+  // the grid argument of the product kernels: pattern_grid_ny or pattern_brick
+  int pattern_stencil = 0;
 
   // reductions
   int red_blocks = 0;   // largest grid of a reducing kernel (8 per SM)

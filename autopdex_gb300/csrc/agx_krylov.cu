@@ -241,15 +241,113 @@ __device__ __forceinline__ void grid_row(int64_t row, int ny, int64_t n_rows, co
   }
 }
 
+// The same for the tangent of a structured nx x ny x nz brick grid (node p = (i (ny + 1) + j)
+// (nz + 1) + k, every pattern row the in-range 27-node stencil): the blocks before row p are
+//   S(i) (3 ny + 1)(3 nz + 1) + r_i S(j) (3 nz + 1) + r_i r_j S(k)
+// with S and r as above per direction, and row p's blocks are its in-range neighbours in
+// (di, dj, dk) order.  code = (ny << 16) | nz.  Scalar fields load all 27 values at once; block
+// fields one plane of 9 neighbours at a time (register pressure).
+template <typename T, int NDOF, bool DIR, typename VT = T>
+__device__ __forceinline__ void brick_row(int64_t row, int code, int64_t n_rows, const VT* __restrict__ vals,
+                                          int64_t nnzb, const T* __restrict__ x, const T* __restrict__ pold, T beta,
+                                          T (&y)[NDOF]) {
+  const uint32_t ny = (uint32_t)code >> 16, nz = (uint32_t)code & 0xFFFFu;
+  const uint32_t NZ = nz + 1u, plane = (ny + 1u) * NZ;
+  const uint32_t nx = (uint32_t)n_rows / plane - 1u;
+  const uint32_t i = (uint32_t)row / plane, rem = (uint32_t)row - i * plane;
+  const uint32_t j = rem / NZ, k = rem - j * NZ;
+  const int ri = (i > 0) + 1 + (i < nx), rj = (j > 0) + 1 + (j < ny);
+  const int64_t k0 = (int64_t)(3 * i - (i > 0)) * (3 * (int64_t)ny + 1) * (3 * (int64_t)nz + 1) +
+                     (int64_t)ri * (3 * j - (j > 0)) * (3 * (int64_t)nz + 1) + (int64_t)(ri * rj) * (3 * k - (k > 0));
+  bool ok[27];
+  int m[27];
+  int cnt = 0;
+#pragma unroll
+  for (int t = 0; t < 27; ++t) {
+    const int di = t / 9 - 1, dj = (t / 3) % 3 - 1, dk = t % 3 - 1;
+    ok[t] = (di >= 0 || i > 0) && (di <= 0 || i < nx) && (dj >= 0 || j > 0) && (dj <= 0 || j < ny) &&
+            (dk >= 0 || k > 0) && (dk <= 0 || k < nz);
+    m[t] = cnt;
+    cnt += ok[t] ? 1 : 0;
+  }
+#pragma unroll
+  for (int q = 0; q < NDOF; ++q) y[q] = 0;
+  if constexpr (NDOF == 1 && sizeof(VT) <= 4) {
+    // The warp's 32 consecutive rows (every kernel's lanes hold consecutive rows, the tail
+    // clamped to the last row) own one contiguous range of at most 32 x 27 values: loaded
+    // coalesced, 27 loads in flight per lane, into the warp's slice of shared memory, from which
+    // each lane reads its row (a stride of 27 words: no bank conflicts).
+    __shared__ VT stage[AGX_BLOCK / 32][32 * 27];
+    VT* sw = stage[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int64_t base = __shfl_sync(0xffffffffu, k0, 0);
+    const int total = (int)(__shfl_sync(0xffffffffu, k0 + cnt, 31) - base);
+    VT r[27];
+#pragma unroll
+    for (int u = 0; u < 27; ++u) {
+      const int sidx = lane + 32 * u;
+      r[u] = sidx < total ? __ldcs(vals + base + sidx) : VT(0);
+    }
+    __syncwarp();  // the previous row's reads of the slice are done
+#pragma unroll
+    for (int u = 0; u < 27; ++u) {
+      const int sidx = lane + 32 * u;
+      if (sidx < total) sw[sidx] = r[u];
+    }
+    __syncwarp();
+    const VT* my = sw + (k0 - base);
+#pragma unroll
+    for (int t = 0; t < 27; ++t) {
+      if (!ok[t]) continue;
+      const int64_t c = row + (int64_t)(t / 9 - 1) * plane + (int64_t)((t / 3) % 3 - 1) * NZ + (t % 3 - 1);
+      T xv = x[c];
+      if constexpr (DIR) xv += beta * pold[c];
+      T v;
+      if constexpr (std::is_same<VT, __nv_bfloat16>::value) v = (T)__bfloat162float(my[m[t]]);
+      else v = (T)my[m[t]];
+      y[0] += v * xv;
+    }
+    return;
+  }
+  constexpr int CH = NDOF == 1 ? 27 : 9;  // neighbours whose values are in flight together
+#pragma unroll
+  for (int t0 = 0; t0 < 27; t0 += CH) {
+    T v[CH][NDOF * NDOF];
+#pragma unroll
+    for (int e = 0; e < NDOF * NDOF; ++e)
+#pragma unroll
+      for (int u = 0; u < CH; ++u)
+        v[u][e] = ok[t0 + u] ? load_val<T>(vals + (int64_t)e * nnzb + k0 + m[t0 + u]) : T(0);
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int t = t0 + u;
+      const int64_t c = row + (int64_t)(t / 9 - 1) * plane + (int64_t)((t / 3) % 3 - 1) * NZ + (t % 3 - 1);
+#pragma unroll
+      for (int jj = 0; jj < NDOF; ++jj) {
+        T xv = ok[t] ? x[c * NDOF + jj] : T(0);
+        if constexpr (DIR) {
+          if (ok[t]) xv += beta * pold[c * NDOF + jj];
+        }
+#pragma unroll
+        for (int q = 0; q < NDOF; ++q) y[q] += v[u][q * NDOF + jj] * xv;
+      }
+    }
+  }
+}
+
 // A product row in the tangent's storage: U > 0 the node-block CSR with TPR lanes per row,
 // U <= 0 the structured grid's stencil (one lane per row, gny = ny; U == -2: the kernels give
-// each lane two consecutive rows, whose loads are then in flight together)
+// each lane two consecutive rows, whose loads are then in flight together; U == -3: the brick
+// grid's stencil, gny = its packed code)
 template <typename T, int NDOF, int TPR, bool DIR, int U, typename VT = T>
 __device__ __forceinline__ void tangent_row(int64_t row, int sub, const int32_t* __restrict__ rowptr,
                                             const int32_t* __restrict__ col, const VT* __restrict__ vals,
                                             int64_t nnzb, int64_t n_rows, int gny, const T* __restrict__ x,
                                             const T* __restrict__ pold, T beta, T (&y)[NDOF]) {
-  if constexpr (U <= 0) {  // 0: one row per lane, -2: two rows per lane (the kernels' loops)
+  if constexpr (U == -3) {
+    static_assert(TPR == 1, "the brick product has one lane per row");
+    brick_row<T, NDOF, DIR, VT>(row, gny, n_rows, vals, nnzb, x, pold, beta, y);
+  } else if constexpr (U <= 0) {  // 0: one row per lane, -2: two rows per lane (the kernels' loops)
     static_assert(TPR == 1, "the grid product has one lane per row");
     grid_row<T, NDOF, DIR, VT>(row, gny, n_rows, vals, nnzb, x, pold, beta, y);
   } else {
@@ -1004,7 +1102,7 @@ int spmv_dot_variant(agx_context* ctx, const T* vals, const T* z, const T* pold,
   static int g_cache = 0;
   if (!g_cache) g_cache = resident_grid(ctx, spmv_dot_kernel<T, ND, TP, U>);
   agx_launch_pdl(spmv_dot_kernel<T, ND, TP, U>, g_cache, AGX_BLOCK, 0, ctx->stream, ctx->n_nodes, ctx->d_rowptr, ctx->d_col,
-                                                                        vals, ctx->nnzb, ctx->pattern_grid_ny, z, pold,
+                                                                        vals, ctx->nnzb, ctx->pattern_stencil, z, pold,
                                                                         pnew, q, ctx->d_scal, ctx->d_partials, rflex);
   return g_cache;
 }
@@ -1029,6 +1127,9 @@ int spmv_dot_nd(agx_context* ctx, int tpr, const T* vals, const T* z, const T* p
       [[fallthrough]];
     case SPMV_GRID2:
       if constexpr (ND <= 2) return spmv_dot_variant<T, ND, 1, -2>(ctx, vals, z, pold, pnew, q, rflex);
+      [[fallthrough]];
+    case SPMV_BRICK:
+      if (tpr == SPMV_BRICK) return spmv_dot_variant<T, ND, 1, -3>(ctx, vals, z, pold, pnew, q, rflex);
       [[fallthrough]];
     default: return spmv_dot_variant<T, ND, 8>(ctx, vals, z, pold, pnew, q, rflex);
   }
@@ -1215,6 +1316,7 @@ int agx_autotune_spmv(agx_context* ctx, int* chosen, float* best_ms) {
     cands.push_back(SPMV_GRID);
     cands.push_back(SPMV_GRID2);
   }
+  if (ctx->pattern_brick > 0) cands.push_back(SPMV_BRICK);
   cudaEvent_t e0, e1;
   AGX_CUDA(ctx, cudaEventCreate(&e0));
   AGX_CUDA(ctx, cudaEventCreate(&e1));
@@ -1227,7 +1329,7 @@ int agx_autotune_spmv(agx_context* ctx, int* chosen, float* best_ms) {
   float best = 1e30f;
   int pick = default_tpr(ctx);
   for (int c : cands) {
-    if (ctx->ndof == 3 && spmv_lanes(c) < 4) continue;
+    if (ctx->ndof == 3 && spmv_lanes(c) < 4 && c != SPMV_BRICK) continue;
     auto run = [&]() {
       cudaMemsetAsync(ctx->d_scal, 0, sizeof(agx_krylov_scalars), ctx->stream);
       if (f32) {
@@ -1285,7 +1387,7 @@ void agx_launch_jacobi(agx_context* ctx, int dtype, const void* r, void* z) {
 template <typename T, int ND>
 void spmv_nd(agx_context* ctx, int tpr, int g, const T* v, const T* x, T* y) {
   const int64_t nr = ctx->n_nodes;
-  const int gny = ctx->pattern_grid_ny;
+  const int gny = ctx->pattern_stencil;
   switch (tpr) {
     case 1: spmv_kernel<T, ND, 1><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, gny, x, y); break;
     case 2: spmv_kernel<T, ND, 2><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, gny, x, y); break;
@@ -1303,6 +1405,12 @@ void spmv_nd(agx_context* ctx, int tpr, int g, const T* v, const T* x, T* y) {
     case SPMV_GRID2:
       if constexpr (ND <= 2) {
         spmv_kernel<T, ND, 1, -2><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, gny, x, y);
+        break;
+      }
+      [[fallthrough]];
+    case SPMV_BRICK:
+      if (tpr == SPMV_BRICK) {
+        spmv_kernel<T, ND, 1, -3><<<g, AGX_BLOCK, 0, ctx->stream>>>(nr, ctx->d_rowptr, ctx->d_col, v, ctx->nnzb, gny, x, y);
         break;
       }
       [[fallthrough]];
@@ -1373,7 +1481,7 @@ void tl_spmv_nd(agx_context* ctx, int code, int g, const VT* vals, const float* 
   const int64_t nr = ctx->n_nodes;
 #define AGX_TL(TP_, U_)                                                                                         \
   agx_launch_pdl(tl_spmv<ND, TP_, U_, EPI, VT>, g, AGX_BLOCK, 0, ctx->stream, nr, ctx->d_rowptr, ctx->d_col, \
-                 vals, ctx->nnzb, ctx->pattern_grid_ny, x, rc, ctx->d_dinv32, a, b, dnew, ctx->f_z, tout, sc,   \
+                 vals, ctx->nnzb, ctx->pattern_stencil, x, rc, ctx->d_dinv32, a, b, dnew, ctx->f_z, tout, sc,   \
                  ctx->d_partials)
   switch (code) {
     case 1: AGX_TL(1, 2); break;
@@ -1392,6 +1500,12 @@ void tl_spmv_nd(agx_context* ctx, int code, int g, const VT* vals, const float* 
     case SPMV_GRID2:
       if constexpr (ND <= 2) {
         AGX_TL(1, -2);
+        break;
+      }
+      [[fallthrough]];
+    case SPMV_BRICK:
+      if (code == SPMV_BRICK) {
+        AGX_TL(1, -3);
         break;
       }
       [[fallthrough]];

@@ -270,12 +270,16 @@ int agx_build_pattern(agx_context* ctx) {
     });
   }
   ctx->pattern_grid_ny = 0;
+  ctx->pattern_brick = 0;
   for (auto& s : ctx->sets) {
     detect_structured_grid(ctx, s, rowptr);
     detect_structured_brick(ctx, s, rowptr);
     // the row lengths matched the grid's stencil: every other set's entries lie inside it
     if (s.grid_nx > 0 && ctx->ndof <= 2) ctx->pattern_grid_ny = s.grid_ny;
+    if (s.brick_n[0] > 0 && ctx->ndof <= 3 && s.brick_n[1] < 32768 && s.brick_n[2] < 65536)
+      ctx->pattern_brick = (s.brick_n[1] << 16) | s.brick_n[2];
   }
+  ctx->pattern_stencil = ctx->pattern_grid_ny > 0 ? ctx->pattern_grid_ny : ctx->pattern_brick;
   // upload
   const int bs = ctx->ndof * ctx->ndof;
   AGX_CUDA(ctx, cudaMalloc(&ctx->d_rowptr, sizeof(int32_t) * (nn + 1)));

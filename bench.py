@@ -351,7 +351,7 @@ def headline_roofline(h):
     # the vectors (fused Krylov product: z, p_old read, p_new, q written; plain product: x, y);
     # the structured grid's product (code 512) reads no row pointers or column indices
     tpr = getattr(prob, "spmv_tpr", 0)
-    grid = tpr in (512, 1024)
+    grid = tpr in (512, 1024, 2048)
     matrix = nnzb * ndof * ndof * s if grid else nnzb * (ndof * ndof * s + 4) + 4 * (n_nodes + 1)
     fused = matrix + 4 * n * s
     # the two-level products carry their element-wise work: per application 2 (nu - 1) sweep

@@ -275,7 +275,9 @@ int agx_pcg_noalloc(const int32_t* rowptr, const int32_t* col, const double* val
    with two blocks per lane and trip, 2, 4, 8 lanes with four blocks (code lanes + 256), and,
    when the pattern is the 3 x 3 stencil of a structured QUAD4 grid with 1 or 2 DOFs per node,
    the grid product that computes each row's block offsets and columns instead of reading them
-   (code 512; 1024 with two rows per lane) -- on the last assembled tangent (CUDA events),
+   (code 512; 1024 with two rows per lane), and when it is the 27-node stencil of a structured
+   HEX8 grid with 1 to 3 DOFs per node the brick product of the same kind (code 2048) -- on
+   the last assembled tangent (CUDA events),
    keeps the fastest for that tangent's precision and reports its code. */
 int agx_autotune(agx_context* ctx, int* spmv_tpr, float* spmv_ms);
 /* Applies a tuning decision for the float64 (AGX_F64) or float32 (AGX_F32) product, e.g. from
@@ -293,6 +295,9 @@ int agx_solve_flag(agx_context* ctx, const int** flag);
 /* ny of the structured QUAD4 grid whose 3 x 3 stencil the pattern is (the grid products,
    codes 512 and 1024, apply), else 0; for keys of a tuning cache. */
 int agx_grid_pattern(const agx_context* ctx, int* ny);
+/* (ny << 16) | nz of the structured HEX8 grid whose 27-node stencil the pattern is (the brick
+   product, code 2048, applies), else 0; for keys of a tuning cache. */
+int agx_brick_pattern(const agx_context* ctx, int* code);
 /* Number of kernels this context has launched since it was created. */
 int agx_launch_count(const agx_context* ctx, int64_t* launches);
 /* Sizes for the host layer: n_dofs, nnzb, ndof. */

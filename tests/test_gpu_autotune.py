@@ -69,6 +69,10 @@ def test_invalid_tuning_is_rejected():
     assert lib.agx_set_tuning(prob.ctx, N.AGX_F32, 8 + 256) == N.AGX_OK
     assert lib.agx_set_tuning(prob.ctx, N.AGX_F64, 8) == N.AGX_OK
     assert lib.agx_set_tuning(prob.ctx, N.AGX_F64, 512) != N.AGX_OK  # hexahedra: no grid product
+    assert lib.agx_set_tuning(prob.ctx, N.AGX_F64, 2048) == N.AGX_OK  # a structured brick grid
+    w2 = configs.heat_grf(n=8, seed=1)
+    prob2 = get_problem(w2.dofs, w2.settings, w2.static_settings)
+    assert prob2.lib.agx_set_tuning(prob2.ctx, N.AGX_F32, 2048) != N.AGX_OK  # quads: no brick product
 
 
 @pytest.mark.parametrize("case", ["heat", "cook"])
@@ -118,5 +122,59 @@ def test_autotuner_times_real_products():
         tpr = C.c_int()
         ms = C.c_float()
         prob._call("agx_autotune", C.byref(tpr), C.byref(ms))
-        matrix_bytes = prob.nnzb * (s + (0 if tpr.value in (512, 1024) else 4))  # the grid products read no indices
+        matrix_bytes = prob.nnzb * (s + (0 if tpr.value in (512, 1024, 2048) else 4))  # the grid products read no indices
         assert ms.value * 1e-3 >= matrix_bytes / 8e12, (dtype, tpr.value, ms.value)
+
+
+@pytest.mark.parametrize("case", ["heat_be", "neo_hooke", "sheared"])
+def test_brick_product_matches_scipy(case):
+    """agx_spmv with the brick product (code 2048) on structured HEX8 grids -- one DOF per node
+    (the backward-Euler heat workload, non-cubic 9 x 7 x 5 and a sheared lattice) and three (the
+    neo-Hooke cube) -- against SciPy's product of the copied matrix, float64 and float32
+    tangents; the fused Krylov product of the variant solves like the default one."""
+    import scipy.sparse as sps
+    if case == "neo_hooke":
+        w = configs.neo_hooke_cube(n=6, n_steps=2)
+    elif case == "heat_be":
+        w = configs.heat_transient(n=8, n_steps=1)
+    else:
+        from test_gpu_parity import _sheared_brick_heat_be
+        w = _sheared_brick_heat_be(shape=(9, 7, 5))
+    prob = get_problem(w.dofs, w.settings, w.static_settings)
+    prob.update_models(w.settings)
+    code = C.c_int()
+    prob._call("agx_brick_pattern", C.byref(code))
+    assert code.value > 0
+    rng = np.random.default_rng(6)
+    u = torch.as_tensor(rng.uniform(-1e-3, 1e-3, prob.n_dofs), device=prob.device)
+    nd = prob.ndof
+    for dtype, tdt, tol in ((N.AGX_F64, torch.float64, 1e-13), (N.AGX_F32, torch.float32, 2e-6)):
+        prob._call("agx_assemble", C.c_void_p(u.data_ptr()), None, dtype)
+        nn = prob.n_dofs // nd
+        rowptr = torch.empty(nn + 1, dtype=torch.int32, device=prob.device)
+        col = torch.empty(prob.nnzb, dtype=torch.int32, device=prob.device)
+        vals = torch.empty(prob.nnzb * nd * nd, dtype=tdt, device=prob.device)
+        prob._call("agx_copy_matrix", dtype, C.c_void_p(rowptr.data_ptr()), C.c_void_p(col.data_ptr()),
+                   C.c_void_p(vals.data_ptr()))
+        blocks = vals.double().cpu().numpy().reshape(-1, nd, nd)
+        A = sps.bsr_matrix((blocks, col.cpu().numpy(), rowptr.cpu().numpy()), shape=(prob.n_dofs, prob.n_dofs))
+        x = torch.as_tensor(rng.standard_normal(prob.n_dofs), device=prob.device).to(tdt)
+        ref = A @ x.double().cpu().numpy()
+        for c in (2048, 8):
+            prob._call("agx_set_tuning", dtype, c)
+            y = torch.empty_like(x)
+            prob._call("agx_spmv", dtype, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()))
+            assert np.abs(y.double().cpu().numpy() - ref).max() <= tol * np.abs(ref).max(), (case, dtype, c)
+        if case != "neo_hooke":  # at T = 0 the heat tangent is SPD: the fused product inside PCG
+            zero = torch.zeros_like(u)
+            prob._call("agx_assemble", C.c_void_p(zero.data_ptr()), None, dtype)
+            mask = torch.as_tensor(prob.mask.astype(bool), device=prob.device)
+            rhs = torch.where(mask, torch.zeros_like(u), torch.ones_like(u))
+            method = N.AGX_PCG if dtype == N.AGX_F64 else N.AGX_PCG_MIXED
+            sols = {}
+            for c in (2048, 8):
+                prob._call("agx_set_tuning", dtype, c)
+                sols[c] = _solve(prob, rhs, method)
+            tol_s = 1e-8 if dtype == N.AGX_F64 else 1e-3
+            assert np.abs(sols[2048][0] - sols[8][0]).max() <= tol_s * np.abs(sols[8][0]).max()
+        prob._call("agx_set_tuning", dtype, 0)
