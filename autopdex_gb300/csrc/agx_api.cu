@@ -70,7 +70,7 @@ void free_device(agx_context* ctx) {
                      &ctx->d_t, &ctx->d_rhat, &ctx->d_v})
     release(*p);
   for (float** p : {&ctx->f_x, &ctx->f_r, &ctx->f_z, &ctx->f_p, &ctx->f_q, &ctx->f_rold, &ctx->f_w1, &ctx->f_w2,
-                    &ctx->f_w3, &ctx->f_w4})
+                    &ctx->f_w3, &ctx->f_w4, &ctx->f_dofs32})
     release(*p);
   release(ctx->d_partials);
   release(ctx->d_counter);
@@ -260,7 +260,7 @@ int agx_finalize(agx_context* ctx) {
                      &ctx->d_t, &ctx->d_rhat, &ctx->d_v, &ctx->d_dinv64})
     if (int rc = alloc(ctx, p, n)) return rc;
   for (float** p : {&ctx->f_x, &ctx->f_r, &ctx->f_z, &ctx->f_p, &ctx->f_q, &ctx->f_rold, &ctx->d_dinv32, &ctx->f_w1,
-                    &ctx->f_w2, &ctx->f_w3, &ctx->f_w4})
+                    &ctx->f_w2, &ctx->f_w3, &ctx->f_w4, &ctx->f_dofs32})
     if (int rc = alloc(ctx, p, n)) return rc;
   ctx->red_blocks = ctx->sm_count * 8;  // one resident wave of 256-thread blocks
   ctx->vec_blocks = ctx->sm_count * 4;  // reducing vector kernels (16-byte accesses)

@@ -18,7 +18,8 @@
 // float64 operations of the per-point evaluation, which is what bounds this pass on a GPU
 // whose float64 rate is a fraction of its float32 rate.
 //
-// brick_heat_be_tangent (float32): one thread per node row, atomic-free.  The row of node
+// brick_heat_be_tangent (float32): one thread per node row, atomic-free, on a float32 copy of
+// the DOFs.  The row of node
 // (I, J, K) gathers the matrices of its up to 8 elements (each recomputed from the element's
 // nodal values) into the 27-entry stencil, deletes prescribed columns (identity row at a
 // prescribed node), writes 1 / diagonal, and the 128 rows of a block leave through shared
@@ -200,8 +201,15 @@ brick_heat_be_residual(int nx, int ny, int nz, const double* __restrict__ u, con
 
 constexpr int kRowBlock = 128;  // node rows per block of the tangent kernel
 
+__global__ void __launch_bounds__(256) dofs_to_float(int64_t n, const double* __restrict__ u, float* __restrict__ f) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    f[i] = (float)u[i];
+}
+
+// u: the DOFs rounded to float32 once (a float64 load and conversion per use would run on the
+// float64 pipe: 64 per row)
 __global__ void __launch_bounds__(kRowBlock)
-brick_heat_be_tangent(int nx, int ny, int nz, const double* __restrict__ u, BrickParams bp,
+brick_heat_be_tangent(int nx, int ny, int nz, const float* __restrict__ u, BrickParams bp,
                       const uint8_t* __restrict__ dmask, const int32_t* __restrict__ rowptr, float* __restrict__ vals,
                       float* __restrict__ dinv) {
   __shared__ float stage[kRowBlock * 27];
@@ -237,7 +245,7 @@ brick_heat_be_tangent(int nx, int ny, int nz, const double* __restrict__ u, Bric
 #pragma unroll
             for (int b = 0; b < 2; ++b)
 #pragma unroll
-              for (int c = 0; c < 2; ++c) t[a][b][c] = (float)__ldg(u + n0 + a * sa + b * sb + c);
+              for (int c = 0; c < 2; ++c) t[a][b][c] = __ldg(u + n0 + a * sa + b * sb + c);
           float Tq[2][2][2], gx[2][2], gy[2][2], gz[2][2];
           interp(t, Tq);
           rgrad(t, gx, gy, gz);
@@ -349,7 +357,9 @@ void agx_launch_brick_residual(agx_context* ctx, const agx_element_set& s, const
 void agx_launch_brick_tangent(agx_context* ctx, const agx_element_set& s, const double* dofs, float* vals,
                               float* dinv) {
   const int64_t n = ctx->n_nodes;
+  dofs_to_float<<<agx_grid(ctx, n), 256, 0, ctx->stream>>>(n, dofs, ctx->f_dofs32);
   brick_heat_be_tangent<<<(unsigned)((n + kRowBlock - 1) / kRowBlock), kRowBlock, 0, ctx->stream>>>(
-      s.brick_n[0], s.brick_n[1], s.brick_n[2], dofs, brick_params(s), ctx->d_dmask_node, ctx->d_rowptr, vals, dinv);
-  ctx->n_launches += 1;
+      s.brick_n[0], s.brick_n[1], s.brick_n[2], ctx->f_dofs32, brick_params(s), ctx->d_dmask_node, ctx->d_rowptr,
+      vals, dinv);
+  ctx->n_launches += 2;
 }

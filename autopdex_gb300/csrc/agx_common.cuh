@@ -130,6 +130,7 @@ struct agx_context {
   // single-precision Krylov vectors (mixed precision inner solve)
   float *f_x = nullptr, *f_r = nullptr, *f_z = nullptr, *f_p = nullptr, *f_q = nullptr, *f_rold = nullptr;
   float *f_w1 = nullptr, *f_w2 = nullptr, *f_w3 = nullptr, *f_w4 = nullptr;  // two-level preconditioner work
+  float* f_dofs32 = nullptr;  // float32 copy of the DOFs (the brick grid's float32 tangent reads it)
 
   // > 0: the pattern is the in-range 3 x 3 stencil of a structured nx x ny QUAD4 grid with
   // ny = pattern_grid_ny (the index-free product SPMV_GRID applies)

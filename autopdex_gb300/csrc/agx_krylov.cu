@@ -355,8 +355,13 @@ __device__ __forceinline__ void tangent_row(int64_t row, int sub, const int32_t*
   }
 }
 
+// the brick product's staged scalar rows: three blocks per SM (registers capped), since the
+// product is bound by the latency of its two dependent load rounds
+template <int U, int NDOF, int VBYTES>
+constexpr int brick_min_blocks() { return (U == -3 && NDOF == 1 && VBYTES <= 4) ? 3 : 0; }  // 0: no bound
+
 template <typename T, int NDOF, int TPR, int U = 2>
-__global__ void __launch_bounds__(AGX_BLOCK) spmv_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr,
+__global__ void __launch_bounds__(AGX_BLOCK, brick_min_blocks<U, NDOF, sizeof(T)>()) spmv_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr,
                                                          const int32_t* __restrict__ col, const T* __restrict__ vals,
                                                          int64_t nnzb, int gny, const T* __restrict__ x,
                                                          T* __restrict__ y) {
@@ -386,7 +391,7 @@ __global__ void __launch_bounds__(AGX_BLOCK) spmv_kernel(int64_t n_rows, const i
 // p_new = z + beta p_old (own rows), q = A p_new, block partials of (p_new, q) for the step
 // alpha = rz / (p_new, q).  beta = 0 on the first iteration (p_old = 0), which makes p_new = z.
 template <typename T, int NDOF, int TPR, int U = 2>
-__global__ void __launch_bounds__(AGX_BLOCK)
+__global__ void __launch_bounds__(AGX_BLOCK, brick_min_blocks<U, NDOF, sizeof(T)>())
 spmv_dot_kernel(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                 const T* __restrict__ vals, int64_t nnzb, int gny, const T* __restrict__ z,
                 const T* __restrict__ pold, T* __restrict__ pnew, T* __restrict__ q, agx_krylov_scalars* sc,
@@ -787,7 +792,7 @@ tl_combine(int64_t n, float* __restrict__ z, const float* __restrict__ y, float*
 enum { TL_SWEEP = 0, TL_RESID = 1, TL_STEP = 2 };
 
 template <int NDOF, int TPR, int U, int EPI, typename VT = float>
-__global__ void __launch_bounds__(AGX_BLOCK)
+__global__ void __launch_bounds__(AGX_BLOCK, brick_min_blocks<U, NDOF, sizeof(VT)>())
 tl_spmv(int64_t n_rows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
         const VT* __restrict__ vals, int64_t nnzb, int gny, const float* __restrict__ x, float* __restrict__ rc,
         const float* __restrict__ dinv, float a, float b, float* __restrict__ dnew, float* __restrict__ z,

@@ -608,7 +608,11 @@ def rec_heat(h):
     return out
 
 
-def rec_heat_be(n=128, steps=10, plain_steps=3):
+def rec_heat_be(n=128, steps=100, plain_steps=3):
+    """The 128^3 backward-Euler heat workload: all 100 time steps with mixed Jacobi-PCG and with
+    the learned (3-D network) + mixed flexible CG, the first plain_steps with float64 BiCGStab;
+    Newton to a 1e-10 float64 residual ratio in every step; and the float32 tangent assembly's
+    roofline."""
     import torch
     from autopdex_gb300 import configs, learned, solver
     out = {"workload": f"heat_be_{n}^3_hex8 (k = 1 + 0.5 T^2, dt = 1e-3), time steps 1..{steps} of 100"}
@@ -616,8 +620,10 @@ def rec_heat_be(n=128, steps=10, plain_steps=3):
                 ("plain_fp64_bicgstab", dict(solver="bicgstab", precision="float64"), 1e-11, plain_steps)]
     wpath = os.path.join(learned.WEIGHTS_DIR, f"brick_unet_n{n}.npz")
     if os.path.exists(wpath):
+        # inner tolerance 1e-4 (measured over 5 steps: 1e-3 / 1e-4 / 1e-5 -> 20 / 16 / 16 Newton
+        # steps, 35.5 / 29.4 / 32.2 ms per time step)
         variants.insert(1, ("learned_mixed_fcg", dict(solver="fcg", precision="mixed",
-                                                      **{"type of preconditioner": "learned"}), 1e-3, steps))
+                                                      **{"type of preconditioner": "learned"}), 1e-4, steps))
     for name, st, ktol, nsteps in variants:
         w = configs.heat_transient(n=n)
         static = dict(w.static_settings, **st)
@@ -637,6 +643,7 @@ def rec_heat_be(n=128, steps=10, plain_steps=3):
         solver.solver({"T": T0.clone()}, settings, static, **kw)  # context, tuning, graphs
         per = []
         first = {}
+        start, mid = _events()
 
         def run():
             T = T0.clone()
@@ -646,15 +653,19 @@ def rec_heat_be(n=128, steps=10, plain_steps=3):
                 per.append(_info())
                 if k == 0:
                     first["T1"] = Tn["T"].clone()
+                if k == plain_steps - 1:
+                    mid.record()
                 T = Tn["T"]
             return T
         if pc is not None:
             pc.applications = 0
+        start.record()
         s, T = _timed(run)
         if pc is not None:
             solver.set_learned_preconditioner(None, None)
-        out[name] = {"s_per_step": s / nsteps, "steps": nsteps, "newton": sum(p["newton"] for p in per),
-                     "krylov": sum(p["krylov"] for p in per),
+        out[name] = {"s_per_step": s / nsteps, "steps": nsteps,
+                     f"s_per_step_first_{plain_steps}": start.elapsed_time(mid) / 1e3 / plain_steps,
+                     "newton": sum(p["newton"] for p in per), "krylov": sum(p["krylov"] for p in per),
                      "max_residual_ratio": max(p["residual_ratio"] for p in per),
                      "sum_T_squared": float((T * T).sum())}
         if pc is not None:
@@ -663,10 +674,12 @@ def rec_heat_be(n=128, steps=10, plain_steps=3):
             st0 = dict(w.settings)
             st0["dofs n"] = {"T": w.raw["T0"]}
             out["oracle_error_first_step"] = oracle_errors(w, first["T1"], per[0]["res0"], settings=st0, scale=1.0)
-    base = out["plain_fp64_bicgstab"]["s_per_step"]
-    out["speedup_mixed_vs_plain_fp64"] = base / out["mixed_pcg"]["s_per_step"]
+    # over the same time steps (the first plain_steps: the later ones need fewer iterations)
+    key = f"s_per_step_first_{plain_steps}"
+    base = out["plain_fp64_bicgstab"][key]
+    out["speedup_mixed_vs_plain_fp64"] = base / out["mixed_pcg"][key]
     if "learned_mixed_fcg" in out:
-        out["speedup_learned_vs_plain_fp64"] = base / out["learned_mixed_fcg"]["s_per_step"]
+        out["speedup_learned_vs_plain_fp64"] = base / out["learned_mixed_fcg"][key]
     try:
         out["assembly_hbm"] = assembly_roofline(workload="heat_be", n=n)
     except Exception as e:  # noqa: BLE001 -- the record keeps the solve numbers
