@@ -1321,7 +1321,9 @@ int agx_autotune_spmv(agx_context* ctx, int* chosen, float* best_ms) {
     cands.push_back(SPMV_GRID);
     cands.push_back(SPMV_GRID2);
   }
-  if (ctx->pattern_brick > 0) cands.push_back(SPMV_BRICK);
+  // the brick product stages scalar rows only; for node blocks its unstaged form (a thread's 9
+  // blocks of 3 x 3 in registers) lost to the BSR variants inside the 64^3 neo-Hooke solve
+  if (ctx->pattern_brick > 0 && ctx->ndof == 1) cands.push_back(SPMV_BRICK);
   cudaEvent_t e0, e1;
   AGX_CUDA(ctx, cudaEventCreate(&e0));
   AGX_CUDA(ctx, cudaEventCreate(&e1));
