@@ -17,6 +17,12 @@ AGX_NN_CONST_WEIGHTS = 2
 AGX_DIVERGED = 2
 AGX_ERR_ARG, AGX_ERR_CUDA, AGX_ERR_UNSUPPORTED, AGX_ERR_STATE = -1, -2, -3, -5
 
+
+def AGX_NN_LOADER(l):
+    """Per-launch halo loader flag of agx_nn_conv3x3 (0 cp.async, 1 tensor copies, 2 warp-specialised)."""
+    return (int(l) + 1) << 4
+
+
 AGX_QUAD4, AGX_HEX8, AGX_LINE2, AGX_QUAD9, AGX_LINE3 = 0, 1, 2, 3, 4
 AGX_TRI3, AGX_TRI6, AGX_TET4, AGX_TET10, AGX_HEX27 = 5, 6, 7, 8, 9
 AGX_MODEL_POISSON_SINCOS = 0

@@ -1232,14 +1232,13 @@ int launch_conv_as(const ConvArgs& a, cudaStream_t s) {
 }
 
 template <int C1, int C2, int COUT, int EPI>
-int launch_conv(const ConvArgs& a, cudaStream_t s) {
+int launch_conv(const ConvArgs& a, cudaStream_t s, int loader) {
   // measured (320^2 U-Net levels): the warp-specialised kernel 18 % faster on the two-input
   // layers, within a few percent either way on the others
-  const bool ws = g_halo_loader == kLoadTmaWs ||
-                  (g_halo_loader == kLoadAuto && C2 > 0 && (int64_t)a.H * a.W >= 128 * 128);
+  const bool ws = loader == kLoadTmaWs || (loader == kLoadAuto && C2 > 0 && (int64_t)a.H * a.W >= 128 * 128);
   if (ws) return launch_conv_as<C1, C2, COUT, EPI, kLoadTmaWs>(a, s);
-  return g_halo_loader == kLoadAsync ? launch_conv_as<C1, C2, COUT, EPI, kLoadAsync>(a, s)
-                                     : launch_conv_as<C1, C2, COUT, EPI, kLoadTma>(a, s);
+  return loader == kLoadAsync ? launch_conv_as<C1, C2, COUT, EPI, kLoadAsync>(a, s)
+                              : launch_conv_as<C1, C2, COUT, EPI, kLoadTma>(a, s);
 }
 
 template <int C1, int C2, int COUT, int TAPS = 9>
@@ -1292,8 +1291,10 @@ extern "C" {
 
 int agx_nn_conv3x3(const void* in1, const void* in2, int c1, int c2, const void* wpk, const float* bias, void* out1,
                    void* out2, int split, int cout, int relu, int B, int H, int W, int* err, void* stream) {
-  if (relu & ~(1 | AGX_NN_CONST_WEIGHTS)) return AGX_ERR_ARG;
+  if (relu & ~(1 | AGX_NN_CONST_WEIGHTS | (3 << 4))) return AGX_ERR_ARG;
   const int const_weights = (relu & AGX_NN_CONST_WEIGHTS) ? 1 : 0;
+  const int pick = (relu >> 4) & 3;  // AGX_NN_LOADER(l) = (l + 1) << 4; 0: the process-wide choice
+  const int loader = pick ? pick - 1 : g_halo_loader;
   relu &= 1;
   ConvArgs a{(const __nv_bfloat16*)in1, (const __nv_bfloat16*)in2, (const __nv_bfloat16*)wpk, bias,
              (__nv_bfloat16*)out1, (__nv_bfloat16*)out2, split, B, H, W, err, const_weights, g_nn_skip};
@@ -1302,7 +1303,7 @@ int agx_nn_conv3x3(const void* in1, const void* in2, int c1, int c2, const void*
   if (split <= 0 || split > cout || split % 8 || (split < cout && !out2)) return AGX_ERR_ARG;
   if (reinterpret_cast<uintptr_t>(wpk) & 15u) return AGX_ERR_ARG;  // one bulk copy into shared memory
 #define AGX_CONV(C1_, C2_, CO_, R_)                                                         \
-  if (c1 == C1_ && c2 == C2_ && cout == CO_ && relu == R_) return launch_conv<C1_, C2_, CO_, R_>(a, s);
+  if (c1 == C1_ && c2 == C2_ && cout == CO_ && relu == R_) return launch_conv<C1_, C2_, CO_, R_>(a, s, loader);
   AGX_CONV(16, 0, 32, 1)
   AGX_CONV(32, 0, 32, 1)
   AGX_CONV(32, 32, 32, 1)

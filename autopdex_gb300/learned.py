@@ -80,6 +80,7 @@ class UNet:
         self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.launches = 0  # kernels this network has launched (forward and backward passes)
         self._s, self._arena = None, None
+        self.loader = {}  # layer name -> halo loader of its forward convolution (autotune)
         self.pack()
 
     # ---- parameters -------------------------------------------------------------------
@@ -153,10 +154,13 @@ class UNet:
         return self.lib.agx_nn_conv3x3x3(_p(x1), _p(x2), c1, c2, _p(wimg), _p(bias), _p(out1), _p(out2), split, cout,
                                          flags, B, *S, _p(self.err), s)
 
-    def _conv(self, name, x1, x2, B, S):
+    def _conv(self, name, x1, x2, B, S, loader=None):
         _, c1, c2, co, relu = self._layer(name)
         out = self._act(B, S, co, name)
         flags = relu | (N.AGX_NN_CONST_WEIGHTS if self.const_weights and self._arena is not None else 0)
+        lo = self.loader.get(name) if loader is None else loader
+        if lo is not None:
+            flags |= N.AGX_NN_LOADER(lo)
         rc = self._convolve(x1, x2, c1, c2, self.img_f[name], self.b[name], out, None, co, co, flags, B, S,
                             self._stream())
         self._ok("convolution", rc)
@@ -306,6 +310,72 @@ class UNet:
     def check(self):
         if int(self.err.item()) != 0:
             raise RuntimeError("a tensor-core kernel timed out waiting for its MMA")
+
+    def autotune(self, x, reps=50, loaders=(0, 1, 2), gain=0.01):
+        """Chooses each layer's halo loader (agx_nn_conv3x3's kernel variant: cp.async loop,
+        tensor-copy loop, warp-specialised; identical outputs) by what the preconditioner runs: the
+        whole forward pass captured into a CUDA graph (programmatic launches overlapping as in the
+        FCG graphs) and replayed reps times under CUDA events.  Coordinate descent from the
+        default choice (warm-up first): for every layer in turn each variant is tried with the
+        others fixed and kept when the pass gets faster by more than `gain`.  Returns
+        {"us_per_pass": (before, after), layer: (loader, {loader: us per pass})}.  2-D networks
+        only (the 3-D convolution has one variant)."""
+        if self.dims != 2:
+            return {}
+        B, S0 = x.shape[0], tuple(x.shape[1:-1])
+        assign = {}
+        for name, c1, c2, co, relu in self.layers:
+            lv = {"e0": 0, "e1": 1, "e2": 2, "b3": 3, "d2": 2, "d1": 1, "d0": 0, "ou": 0}[name[:2]]
+            H, W = self._level(S0, lv)
+            assign[name] = 2 if (c2 > 0 and H * W >= 128 * 128) else 1  # the process-wide default
+        stream = torch.cuda.Stream(self.device)
+        sp = C.c_void_p(stream.cuda_stream)
+        arena = {}
+        saved_cw, saved_loader = self.const_weights, dict(self.loader)
+
+        def pass_us(trial):
+            self.loader = dict(trial)
+            with torch.cuda.stream(stream):
+                self.forward(x, stream=sp, arena=arena)  # first launches and activations outside the capture
+            stream.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=stream):
+                self.forward(x, stream=sp, arena=arena)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                for _ in range(3):
+                    g.replay()
+                e0.record()
+                for _ in range(reps):
+                    g.replay()
+                e1.record()
+            e1.synchronize()
+            return e0.elapsed_time(e1) * 1e3 / reps
+
+        chosen = {}
+        try:
+            self.const_weights = False
+            best = pass_us(assign)
+            first = best
+            for name, *_ in self.layers:
+                times = {assign[name]: best}
+                for lo in loaders:
+                    if lo == assign[name]:
+                        continue
+                    t = pass_us(dict(assign, **{name: lo}))
+                    times[lo] = t
+                    if t < best * (1.0 - gain):
+                        best, assign[name] = t, lo
+                chosen[name] = (assign[name], times)
+        except Exception:
+            self.loader = saved_loader
+            raise
+        finally:
+            self.const_weights = saved_cw
+        self.loader = dict(assign)
+        self.check()
+        chosen["us_per_pass"] = (first, best)
+        return chosen
 
 
 # The 3-D network: 16 channels at every level, 3x3x3 convolutions, 2 x 2 x 2 average pooling
@@ -732,7 +802,7 @@ class GridPreconditioner:
     enqueues kernels on the stream it is given, so FCG captures it into CUDA graphs."""
 
     def __init__(self, net, nx, ny, k_elem=None, factor=1, mode=None, omega=None, sweeps=None, fixed=None, nd=1,
-                 aux=None, bf16_smoothing=False):
+                 aux=None, bf16_smoothing=False, autotune=True):
         if nx % factor or ny % factor:
             raise ValueError("the grid must be divisible by the coarsening factor")
         self.net = net
@@ -771,6 +841,8 @@ class GridPreconditioner:
         self.arena = {}
         self.applications = 0
         self.skip_flag = None  # the solve's converged flag once attached to a problem
+        # every layer's convolution variant timed on this grid's shapes (before FCG captures them)
+        self.loaders = net.autotune(self.img) if autotune else {}
         net.forward(self.img, arena=self.arena)  # allocate the activations once
         torch.cuda.synchronize(dev)
         net.const_weights = True  # packed and synchronised: later forward passes may prefetch them

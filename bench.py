@@ -240,6 +240,8 @@ def headline(args, rank):
     per_step = t_ms / 1e3 / args.steps
     out = {"s": per_step, "info": infos[-1], "launches_per_step": (l1 - l0) / args.steps, "clocks": clk.summary(),
            "prob": prob, "solution": sol, "w": w, "net": net, "factor": factor, "static": static, "kw": kw,
+           "conv_variants": {k: (v[0] if k != "us_per_pass" else [round(t, 1) for t in v])
+                             for k, v in pc.loaders.items()},
            "run": run}
     # the comparison of the metric: plain float64 Jacobi-PCG (and mixed Jacobi-PCG) on the same problem
     cmp = {}
@@ -782,6 +784,7 @@ def gpu_arm(args):
                    "krylov": "flexible CG (float32) with the U-Net two-level preconditioner, inner rtol 1e-3",
                    "network_grid": f"{n // h['factor'] + 1}^2 (coarsening {h['factor']})",
                    "l2": "256 MB buffer written before every timed step", "krylov_chunks": "CUDA graphs",
+                   "conv_variants": h["conv_variants"],
                    "parallelism": "replicas" if world > 1 else "1 gpu"},
         "newton_iterations": h["info"]["newton"], "krylov_iterations": h["info"]["krylov"],
         "final_residual_ratio": h["info"]["residual_ratio"],

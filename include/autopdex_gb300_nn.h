@@ -19,10 +19,12 @@ extern "C" {
 /* out = act(conv3x3(concat(in1[c1], in2[c2])) + bias), cout output channels written as
    out1 (channels [0, split)) and out2 (channels [split, cout)); relu: 0 or 1, plus
    AGX_NN_CONST_WEIGHTS when wpk and bias were not written by the kernel launched just before
-   this one on the stream (their copy then overlaps that kernel's tail).  Packed
-   weights from agx_nn_pack_weights (mode 0), or the input-gradient image (mode 1) with
-   in1 = output gradient, no bias and relu = 0. */
+   this one on the stream (their copy then overlaps that kernel's tail), plus AGX_NN_LOADER(l)
+   to choose this launch's halo loader (l as agx_nn_set_halo_loader, 0 .. 2; without it the
+   process-wide choice applies).  Packed weights from agx_nn_pack_weights (mode 0), or the
+   input-gradient image (mode 1) with in1 = output gradient, no bias and relu = 0. */
 #define AGX_NN_CONST_WEIGHTS 2
+#define AGX_NN_LOADER(l) (((l) + 1) << 4)
 int agx_nn_conv3x3(const void* in1, const void* in2, int c1, int c2, const void* wpk, const float* bias,
                    void* out1, void* out2, int split, int cout, int relu, int B, int H, int W, int* err,
                    void* stream);

@@ -429,3 +429,26 @@ def test_trained_network_reduces_fcg_iterations():
         # the weight gradient sums with float atomics, so the trained network and its count vary
         # from run to run (16-19 of 87 at 64, 23-28 of 77 at 128 observed)
         assert its["two_level_with_network"] < 0.4 * its["two_level_without_network"], results
+
+
+def test_network_autotuner_picks_a_variant_per_layer_and_keeps_outputs():
+    """UNet.autotune (coordinate descent over every layer's three convolution variants, each
+    candidate network timed as a replayed CUDA graph) ends no slower than it started, keeps one
+    variant per layer, and -- the variants giving identical outputs -- leaves the network's
+    output bit-identical."""
+    from autopdex_gb300 import learned
+    net = learned.UNet(seed=4)
+    g = torch.Generator().manual_seed(9)
+    x = torch.zeros(1, 320, 320, 16, dtype=torch.float64)
+    x[..., :2] = torch.randn(1, 320, 320, 2, generator=g, dtype=torch.float64)
+    xd = x.to(torch.bfloat16).cuda()
+    before = net.forward(xd).clone()
+    chosen = net.autotune(xd)
+    after = net.forward(xd)
+    torch.cuda.synchronize()
+    net.check()
+    t0, t1 = chosen.pop("us_per_pass")
+    assert 0 < t1 <= t0
+    assert set(chosen) == {name for name, *_ in learned.LAYERS}
+    assert all(lo in (0, 1, 2) and all(t > 0 for t in times.values()) for lo, times in chosen.values())
+    assert torch.equal(before, after)
