@@ -13,10 +13,11 @@
 //
 // brick_heat_be_residual (float64): one thread per element.  Values and reference gradients
 // at the 8 Gauss points by sum factorisation (one 1-D contraction per direction), the flux
-// det k(T) M grad_xi T and the mass term det rho_c / dt (T - T_n), and the transposed
-// contractions back to the 8 nodes, added to R with reductions.  About a third of the
-// float64 operations of the per-point evaluation, which is what bounds this pass on a GPU
-// whose float64 rate is a fraction of its float32 rate.
+// det k(T) M grad_xi T and its transposed contractions back to the 8 nodes; the mass term
+// det rho_c / dt (T - T_n), linear, as the 1-D Gauss mass matrix applied per direction; added
+// to R with reductions.  About a quarter of the float64 operations of the per-point
+// evaluation, which is what bounds this pass on a GPU whose float64 rate is a fraction of its
+// float32 rate.
 //
 // brick_heat_be_tangent (float32): one thread per node row, atomic-free, on a float32 copy of
 // the DOFs.  The row of node
@@ -101,12 +102,59 @@ __device__ __forceinline__ void rgrad(const T (&f)[2][2][2], T (&gx)[2][2], T (&
   two(dz, gz);
 }
 
+// transposed contractions: out[a][b][c] = sum_pqr B(p,a) B(q,b) B(r,c) F[p][q][r], and
+// S[u][v] = sum_st B(s,u) B(t,v) H[s][t]
+template <typename T>
+__device__ __forceinline__ void tinterp(const T (&F)[2][2][2], T (&out)[2][2][2]) {
+  T c1[2][2][2], c2[2][2][2];
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+      for (int r = 0; r < 2; ++r) c1[a][q][r] = bv<T>(0, a) * F[0][q][r] + bv<T>(1, a) * F[1][q][r];
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+      for (int r = 0; r < 2; ++r) c2[a][b][r] = bv<T>(0, b) * c1[a][0][r] + bv<T>(1, b) * c1[a][1][r];
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) out[a][b][c] = bv<T>(0, c) * c2[a][b][0] + bv<T>(1, c) * c2[a][b][1];
+}
+
+template <typename T>
+__device__ __forceinline__ void back2(const T (&H)[2][2], T (&S)[2][2]) {
+  T a[2][2];
+#pragma unroll
+  for (int u = 0; u < 2; ++u)
+#pragma unroll
+    for (int t = 0; t < 2; ++t) a[u][t] = bv<T>(0, u) * H[0][t] + bv<T>(1, u) * H[1][t];
+#pragma unroll
+  for (int u = 0; u < 2; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) S[u][v] = bv<T>(0, v) * a[u][0] + bv<T>(1, v) * a[u][1];
+}
+
+// the 1-D Gauss mass matrix B^T B = [[2, 1], [1, 2]] / 3
+__device__ __forceinline__ constexpr float m1(int i, int j) { return i == j ? 2.0f / 3.0f : 1.0f / 3.0f; }
+
+// DIAG: J^T J diagonal (an axis-aligned lattice), so M grad_xi T needs 3 products, not 9
+template <bool DIAG>
 __global__ void __launch_bounds__(256)
 brick_heat_be_residual(int nx, int ny, int nz, const double* __restrict__ u, const double* __restrict__ un,
                        BrickParams bp, double* __restrict__ R) {
   const int64_t n_e = (int64_t)nx * ny * nz;
   const int64_t sa = (int64_t)(ny + 1) * (nz + 1), sb = nz + 1;
   const double M00 = bp.M[0], M01 = bp.M[1], M02 = bp.M[2], M11 = bp.M[3], M12 = bp.M[4], M22 = bp.M[5];
+  const double k0d = bp.det * bp.k0, k2d = bp.det * bp.k2;
+  // the mass term is linear: det mass (M1 x M1 x M1) (T - T_n) with the 1-D Gauss mass matrix
+  // M1 = B^T B = [[2, 1], [1, 2]] / 3, applied as (x_c + x_0 + x_1) per direction and 1/27 at the end
+  const double mdet = bp.det * bp.mass / 27.0;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n_e; e += (int64_t)gridDim.x * blockDim.x) {
     const int k = (int)(e % nz);
     const int64_t ij = e / nz;
@@ -123,12 +171,36 @@ brick_heat_be_residual(int nx, int ny, int nz, const double* __restrict__ u, con
           t[a][b][c] = u[idx];
           d[a][b][c] = t[a][b][c] - un[idx];
         }
-    double Tq[2][2][2], Dq[2][2][2], gx[2][2], gy[2][2], gz[2][2];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int b = 0; b < 2; ++b) {
+        const double s2 = d[a][b][0] + d[a][b][1];
+        d[a][b][0] += s2;
+        d[a][b][1] += s2;
+      }
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const double s2 = d[a][0][c] + d[a][1][c];
+        d[a][0][c] += s2;
+        d[a][1][c] += s2;
+      }
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const double s2 = d[0][b][c] + d[1][b][c];
+        d[0][b][c] += s2;
+        d[1][b][c] += s2;
+      }
+    double Tq[2][2][2], gx[2][2], gy[2][2], gz[2][2];
     interp(t, Tq);
-    interp(d, Dq);
     rgrad(t, gx, gy, gz);
-    // per Gauss point: c = det mass (T - T_n), h = det k M grad_xi T; their partial sums
-    double c[2][2][2], Hx[2][2], Hy[2][2], Hz[2][2];
+    // per Gauss point the flux h = det k M grad_xi T, summed over the point coordinate that its
+    // test-function contraction does not need
+    double Hx[2][2], Hy[2][2], Hz[2][2];
 #pragma unroll
     for (int a = 0; a < 2; ++a)
 #pragma unroll
@@ -140,48 +212,19 @@ brick_heat_be_residual(int nx, int ny, int nz, const double* __restrict__ u, con
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
           const double T0 = Tq[p][q][r];
-          const double kd = bp.det * (bp.k0 + bp.k2 * T0 * T0);
+          const double kd = k0d + k2d * T0 * T0;
           const double g0 = gx[q][r], g1 = gy[p][r], g2 = gz[p][q];
-          Hx[q][r] += kd * (M00 * g0 + M01 * g1 + M02 * g2);
-          Hy[p][r] += kd * (M01 * g0 + M11 * g1 + M12 * g2);
-          Hz[p][q] += kd * (M02 * g0 + M12 * g1 + M22 * g2);
-          c[p][q][r] = bp.det * bp.mass * Dq[p][q][r];
+          if constexpr (DIAG) {
+            Hx[q][r] += kd * (M00 * g0);
+            Hy[p][r] += kd * (M11 * g1);
+            Hz[p][q] += kd * (M22 * g2);
+          } else {
+            Hx[q][r] += kd * (M00 * g0 + M01 * g1 + M02 * g2);
+            Hy[p][r] += kd * (M01 * g0 + M11 * g1 + M12 * g2);
+            Hz[p][q] += kd * (M02 * g0 + M12 * g1 + M22 * g2);
+          }
         }
-    // R[a][b][c] = sum B(p,a) B(q,b) B(r,c) c + D(a) Sx[b][c] + D(b) Sy[a][c] + D(c) Sz[a][b]
-    double Rn[2][2][2];
-    {
-      double c1[2][2][2], c2[2][2][2];
-#pragma unroll
-      for (int a = 0; a < 2; ++a)
-#pragma unroll
-        for (int q = 0; q < 2; ++q)
-#pragma unroll
-          for (int r = 0; r < 2; ++r) c1[a][q][r] = bv<double>(0, a) * c[0][q][r] + bv<double>(1, a) * c[1][q][r];
-#pragma unroll
-      for (int a = 0; a < 2; ++a)
-#pragma unroll
-        for (int b = 0; b < 2; ++b)
-#pragma unroll
-          for (int r = 0; r < 2; ++r) c2[a][b][r] = bv<double>(0, b) * c1[a][0][r] + bv<double>(1, b) * c1[a][1][r];
-#pragma unroll
-      for (int a = 0; a < 2; ++a)
-#pragma unroll
-        for (int b = 0; b < 2; ++b)
-#pragma unroll
-          for (int cc = 0; cc < 2; ++cc)
-            Rn[a][b][cc] = bv<double>(0, cc) * c2[a][b][0] + bv<double>(1, cc) * c2[a][b][1];
-    }
-    auto back2 = [](const double (&H)[2][2], double (&S)[2][2]) {  // S[u][v] = sum_st B(s,u) B(t,v) H[s][t]
-      double a[2][2];
-#pragma unroll
-      for (int uu = 0; uu < 2; ++uu)
-#pragma unroll
-        for (int tt = 0; tt < 2; ++tt) a[uu][tt] = bv<double>(0, uu) * H[0][tt] + bv<double>(1, uu) * H[1][tt];
-#pragma unroll
-      for (int uu = 0; uu < 2; ++uu)
-#pragma unroll
-        for (int vv = 0; vv < 2; ++vv) S[uu][vv] = bv<double>(0, vv) * a[uu][0] + bv<double>(1, vv) * a[uu][1];
-    };
+    // R[a][b][c] = mass part + D(a) Sx[b][c] + D(b) Sy[a][c] + D(c) Sz[a][b]
     double Sx[2][2], Sy[2][2], Sz[2][2];
     back2(Hx, Sx);  // [b][c]
     back2(Hy, Sy);  // [a][c]
@@ -192,7 +235,7 @@ brick_heat_be_residual(int nx, int ny, int nz, const double* __restrict__ u, con
       for (int b = 0; b < 2; ++b)
 #pragma unroll
         for (int cc = 0; cc < 2; ++cc) {
-          const double v = Rn[a][b][cc] + dv<double>(a) * Sx[b][cc] + dv<double>(b) * Sy[a][cc] +
+          const double v = mdet * d[a][b][cc] + dv<double>(a) * Sx[b][cc] + dv<double>(b) * Sy[a][cc] +
                            dv<double>(cc) * Sz[a][b];
           atomicAdd(R + n0 + a * sa + b * sb + cc, v);
         }
@@ -208,6 +251,7 @@ __global__ void __launch_bounds__(256) dofs_to_float(int64_t n, const double* __
 
 // u: the DOFs rounded to float32 once (a float64 load and conversion per use would run on the
 // float64 pipe: 64 per row)
+template <bool DIAG>
 __global__ void __launch_bounds__(kRowBlock)
 brick_heat_be_tangent(int nx, int ny, int nz, const float* __restrict__ u, BrickParams bp,
                       const uint8_t* __restrict__ dmask, const int32_t* __restrict__ rowptr, float* __restrict__ vals,
@@ -249,41 +293,56 @@ brick_heat_be_tangent(int nx, int ny, int nz, const float* __restrict__ u, Brick
           float Tq[2][2][2], gx[2][2], gy[2][2], gz[2][2];
           interp(t, Tq);
           rgrad(t, gx, gy, gz);
-          float row[8];  // K_ab of local node a = (di, dj, dk), b = (mi, mj, mk) as 4 mi + 2 mj + mk
+          // row a = (di, dj, dk) of the element matrix, column b = (mi, mj, mk):
+          //   sum_q [k_q (M grad_xi N_a).grad_xi N_b + det dk_q (M grad_xi N_a).grad_xi T N_b]
+          //   + det mass (M1 x M1 x M1)_ab,
+          // the Gauss sums as the test-function contractions of the residual: W collects
+          // k_q M grad_xi N_a per point coordinate pair, c the N_b coefficients
+          float Wx[2][2], Wy[2][2], Wz[2][2], c[2][2][2];
 #pragma unroll
-          for (int b = 0; b < 8; ++b) row[b] = 0.0f;
+          for (int u = 0; u < 2; ++u)
+#pragma unroll
+            for (int w2 = 0; w2 < 2; ++w2) Wx[u][w2] = Wy[u][w2] = Wz[u][w2] = 0.0f;
 #pragma unroll
           for (int pp = 0; pp < 2; ++pp)
 #pragma unroll
             for (int q = 0; q < 2; ++q)
 #pragma unroll
               for (int r = 0; r < 2; ++r) {
-                // reference gradient and value of N_a at this point (compile-time constants)
                 const float ga0 = dv<float>(di) * bv<float>(q, dj) * bv<float>(r, dk);
                 const float ga1 = bv<float>(pp, di) * dv<float>(dj) * bv<float>(r, dk);
                 const float ga2 = bv<float>(pp, di) * bv<float>(q, dj) * dv<float>(dk);
-                const float Na = bv<float>(pp, di) * bv<float>(q, dj) * bv<float>(r, dk);
-                const float m0 = M00 * ga0 + M01 * ga1 + M02 * ga2;  // M grad_xi N_a
-                const float m1 = M01 * ga0 + M11 * ga1 + M12 * ga2;
-                const float m2 = M02 * ga0 + M12 * ga1 + M22 * ga2;
+                float m0, m1_, m2;  // M grad_xi N_a
+                if constexpr (DIAG) {
+                  m0 = M00 * ga0, m1_ = M11 * ga1, m2 = M22 * ga2;
+                } else {
+                  m0 = M00 * ga0 + M01 * ga1 + M02 * ga2;
+                  m1_ = M01 * ga0 + M11 * ga1 + M12 * ga2;
+                  m2 = M02 * ga0 + M12 * ga1 + M22 * ga2;
+                }
                 const float T0 = Tq[pp][q][r];
                 const float kq = det * (k0 + k2 * T0 * T0);
-                const float sq = det * 2.0f * k2 * T0 * (m0 * gx[q][r] + m1 * gy[pp][r] + m2 * gz[pp][q]);
-                const float ma = det * mass * Na;
-#pragma unroll
-                for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-                  for (int mj = 0; mj < 2; ++mj)
-#pragma unroll
-                    for (int mk = 0; mk < 2; ++mk) {
-                      const float gb0 = dv<float>(mi) * bv<float>(q, mj) * bv<float>(r, mk);
-                      const float gb1 = bv<float>(pp, mi) * dv<float>(mj) * bv<float>(r, mk);
-                      const float gb2 = bv<float>(pp, mi) * bv<float>(q, mj) * dv<float>(mk);
-                      const float Nb = bv<float>(pp, mi) * bv<float>(q, mj) * bv<float>(r, mk);
-                      const float A = m0 * gb0 + m1 * gb1 + m2 * gb2;
-                      row[4 * mi + 2 * mj + mk] += kq * A + (ma + sq) * Nb;
-                    }
+                Wx[q][r] += kq * m0;
+                Wy[pp][r] += kq * m1_;
+                Wz[pp][q] += kq * m2;
+                c[pp][q][r] = det * 2.0f * k2 * T0 * (m0 * gx[q][r] + m1_ * gy[pp][r] + m2 * gz[pp][q]);
               }
+          float Kc[2][2][2], Sx[2][2], Sy[2][2], Sz[2][2];
+          tinterp(c, Kc);
+          back2(Wx, Sx);  // [mj][mk]
+          back2(Wy, Sy);  // [mi][mk]
+          back2(Wz, Sz);  // [mi][mj]
+          const float md = det * mass;
+          float row[8];
+#pragma unroll
+          for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+            for (int mj = 0; mj < 2; ++mj)
+#pragma unroll
+              for (int mk = 0; mk < 2; ++mk)
+                row[4 * mi + 2 * mj + mk] = Kc[mi][mj][mk] + dv<float>(mi) * Sx[mj][mk] + dv<float>(mj) * Sy[mi][mk] +
+                                            dv<float>(mk) * Sz[mi][mj] +
+                                            md * (m1(di, mi) * m1(dj, mj) * m1(dk, mk));
 #pragma unroll
           for (int mi = 0; mi < 2; ++mi)
 #pragma unroll
@@ -349,8 +408,13 @@ bool agx_brick_heat_be(const agx_context* ctx, const agx_element_set& s) {
 
 void agx_launch_brick_residual(agx_context* ctx, const agx_element_set& s, const double* dofs, double* R) {
   const int64_t n_e = (int64_t)s.brick_n[0] * s.brick_n[1] * s.brick_n[2];
-  brick_heat_be_residual<<<agx_grid(ctx, n_e), 256, 0, ctx->stream>>>(s.brick_n[0], s.brick_n[1], s.brick_n[2], dofs,
-                                                                       s.d_node_field, brick_params(s), R);
+  const bool diag = s.brick_m[1] == 0.0 && s.brick_m[2] == 0.0 && s.brick_m[4] == 0.0;
+  if (diag)
+    brick_heat_be_residual<true><<<agx_grid(ctx, n_e), 256, 0, ctx->stream>>>(
+        s.brick_n[0], s.brick_n[1], s.brick_n[2], dofs, s.d_node_field, brick_params(s), R);
+  else
+    brick_heat_be_residual<false><<<agx_grid(ctx, n_e), 256, 0, ctx->stream>>>(
+        s.brick_n[0], s.brick_n[1], s.brick_n[2], dofs, s.d_node_field, brick_params(s), R);
   ctx->n_launches += 1;
 }
 
@@ -358,8 +422,14 @@ void agx_launch_brick_tangent(agx_context* ctx, const agx_element_set& s, const 
                               float* dinv) {
   const int64_t n = ctx->n_nodes;
   dofs_to_float<<<agx_grid(ctx, n), 256, 0, ctx->stream>>>(n, dofs, ctx->f_dofs32);
-  brick_heat_be_tangent<<<(unsigned)((n + kRowBlock - 1) / kRowBlock), kRowBlock, 0, ctx->stream>>>(
-      s.brick_n[0], s.brick_n[1], s.brick_n[2], ctx->f_dofs32, brick_params(s), ctx->d_dmask_node, ctx->d_rowptr,
-      vals, dinv);
+  const unsigned grid = (unsigned)((n + kRowBlock - 1) / kRowBlock);
+  if (s.brick_m[1] == 0.0 && s.brick_m[2] == 0.0 && s.brick_m[4] == 0.0)
+    brick_heat_be_tangent<true><<<grid, kRowBlock, 0, ctx->stream>>>(s.brick_n[0], s.brick_n[1], s.brick_n[2],
+                                                                     ctx->f_dofs32, brick_params(s), ctx->d_dmask_node,
+                                                                     ctx->d_rowptr, vals, dinv);
+  else
+    brick_heat_be_tangent<false><<<grid, kRowBlock, 0, ctx->stream>>>(s.brick_n[0], s.brick_n[1], s.brick_n[2],
+                                                                      ctx->f_dofs32, brick_params(s), ctx->d_dmask_node,
+                                                                      ctx->d_rowptr, vals, dinv);
   ctx->n_launches += 2;
 }
