@@ -895,7 +895,8 @@ def case(args):
     make = {"heat": lambda: configs.heat_grf(n=args.size, seed=10000, precision=args.precision, solver=args.solver),
             "poisson": lambda: configs.poisson(n=args.size, precision=args.precision, solver=args.solver),
             "neo_hooke": lambda: configs.neo_hooke_cube(n=args.size, precision=args.precision, solver=args.solver),
-            "cook": lambda: configs.cook_membrane(n=args.size, precision=args.precision, solver=args.solver)}
+            "cook": lambda: configs.cook_membrane(n=args.size, precision=args.precision, solver=args.solver),
+            "heat_be": lambda: configs.heat_transient(n=args.size, precision=args.precision, solver=args.solver)}
     w = make[args.workload]()
     if args.case == "assembly":
         prob = get_problem(w.dofs, w.settings, w.static_settings)
@@ -908,7 +909,11 @@ def case(args):
         print(f"assembly {w.name}: {args.reps} calls")
         return
     static = dict(w.static_settings)
-    if args.learned:
+    if args.learned and args.workload == "heat_be":  # the 3-D network on the brick grid coarsened by 4
+        net3 = learned.UNet3D.load(os.path.join(learned.WEIGHTS_DIR, f"brick_unet_n{args.size}.npz"))
+        solver.set_learned_preconditioner(None, learned.BrickPreconditioner(net3, args.size, factor=4))
+        static["type of preconditioner"] = "learned"
+    elif args.learned:
         _heat_learned_setup(w, args.size)
         static["type of preconditioner"] = "learned"
     settings = w.steps[0](dict(w.settings)) if w.steps else w.settings
@@ -927,6 +932,10 @@ def case(args):
         solver.solver(x0, settings, static, **kw)
     _sync()
     print(f"solve {w.name}: {args.reps} solves after a warm-up solve, last {json.dumps(_info())}")
+    if args.profile:  # one more solve with the library's per-category CUDA events (graphs off)
+        prob = get_problem(x0, settings, static)
+        ms, cnt = _profile(prob, lambda: solver.solver(x0, settings, static, **kw))
+        print("profile (ms, launches): " + json.dumps({k: [round(v, 3), cnt[k]] for k, v in ms.items() if cnt[k]}))
 
 
 def main():
@@ -940,7 +949,8 @@ def main():
     ap.add_argument("--only-headline", action="store_true", help="time the headline only (profiling runs)")
     ap.add_argument("--cook-steps", type=int, default=1)
     ap.add_argument("--case", choices=["conv", "assembly", "solve"], help="one small case for ncu captures")
-    ap.add_argument("--workload", default="heat", choices=["heat", "poisson", "neo_hooke", "cook"])
+    ap.add_argument("--workload", default="heat", choices=["heat", "poisson", "neo_hooke", "cook", "heat_be"])
+    ap.add_argument("--profile", action="store_true", help="solve case: per-category kernel times of one more solve")
     ap.add_argument("--precision", default="mixed")
     ap.add_argument("--solver", default="pcg")
     ap.add_argument("--learned", action="store_true")
