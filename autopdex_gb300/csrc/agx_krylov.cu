@@ -274,38 +274,75 @@ __device__ __forceinline__ void brick_row(int64_t row, int code, int64_t n_rows,
   for (int q = 0; q < NDOF; ++q) y[q] = 0;
   if constexpr (NDOF == 1 && sizeof(VT) <= 4) {
     // The warp's 32 consecutive rows (every kernel's lanes hold consecutive rows, the tail
-    // clamped to the last row) own one contiguous range of at most 32 x 27 values: loaded
-    // coalesced, 27 loads in flight per lane, into the warp's slice of shared memory, from which
-    // each lane reads its row (a stride of 27 words: no bank conflicts).
-    __shared__ VT stage[AGX_BLOCK / 32][32 * 27];
+    // clamped to the last row) own one contiguous range of at most 32 x 27 values: copied
+    // asynchronously in 16-byte chunks (cp.async, the last chunk zero-filled past the range) into
+    // the warp's slice of shared memory while each lane gathers its 27 vector entries (the fused
+    // product: through registers, below); then each lane reads its row from the slice (a stride
+    // of 27 words: no bank conflicts).
+    constexpr int EPC = 16 / (int)sizeof(VT);  // values per chunk
+    __shared__ __align__(16) VT stage[AGX_BLOCK / 32][32 * 27 + 16];
     VT* sw = stage[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const int64_t base = __shfl_sync(0xffffffffu, k0, 0);
-    const int total = (int)(__shfl_sync(0xffffffffu, k0 + cnt, 31) - base);
-    VT r[27];
+    const int64_t endk = __shfl_sync(0xffffffffu, k0 + cnt, 31);
+    const int64_t abase = base & ~(int64_t)(EPC - 1);  // 16-byte aligned start
+    const int nchunks = (int)((endk - abase + EPC - 1) / EPC);
+    if constexpr (DIR) {
+      // the fused product (direction update): its gather also reads the old direction, and the
+      // asynchronous form would spill; the values go through registers, 27 loads in flight
+      VT r[27];
 #pragma unroll
-    for (int u = 0; u < 27; ++u) {
-      const int sidx = lane + 32 * u;
-      r[u] = sidx < total ? __ldcs(vals + base + sidx) : VT(0);
+      for (int u = 0; u < 27; ++u) {
+        const int sidx = lane + 32 * u;
+        r[u] = sidx < (int)(endk - base) ? __ldcs(vals + base + sidx) : VT(0);
+      }
+      __syncwarp();  // the previous row's reads of the slice are done
+#pragma unroll
+      for (int u = 0; u < 27; ++u) {
+        const int sidx = lane + 32 * u;
+        if (sidx < (int)(endk - base)) sw[sidx] = r[u];
+      }
+      __syncwarp();
+      const VT* my = sw + (k0 - base);
+#pragma unroll
+      for (int t = 0; t < 27; ++t) {
+        if (!ok[t]) continue;
+        const int64_t c = row + (int64_t)(t / 9 - 1) * plane + (int64_t)((t / 3) % 3 - 1) * NZ + (t % 3 - 1);
+        const T xv = x[c] + beta * pold[c];
+        T v;
+        if constexpr (std::is_same<VT, __nv_bfloat16>::value) v = (T)__bfloat162float(my[m[t]]);
+        else v = (T)my[m[t]];
+        y[0] += v * xv;
+      }
+      return;
     }
     __syncwarp();  // the previous row's reads of the slice are done
-#pragma unroll
-    for (int u = 0; u < 27; ++u) {
-      const int sidx = lane + 32 * u;
-      if (sidx < total) sw[sidx] = r[u];
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sw);
+    for (int c = lane; c < nchunks; c += 32) {
+      const int64_t e0 = abase + (int64_t)c * EPC;
+      const int64_t rem = endk - e0;
+      const uint32_t bytes = rem >= EPC ? 16u : (uint32_t)rem * (uint32_t)sizeof(VT);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(sbase + (uint32_t)(c * 16)),
+                   "l"(vals + e0), "r"(bytes)
+                   : "memory");
     }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    T xv[27];
+#pragma unroll
+    for (int t = 0; t < 27; ++t) {
+      const int64_t c = row + (int64_t)(t / 9 - 1) * plane + (int64_t)((t / 3) % 3 - 1) * NZ + (t % 3 - 1);
+      xv[t] = ok[t] ? x[c] : T(0);
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
     __syncwarp();
-    const VT* my = sw + (k0 - base);
+    const VT* my = sw + (k0 - abase);
 #pragma unroll
     for (int t = 0; t < 27; ++t) {
       if (!ok[t]) continue;
-      const int64_t c = row + (int64_t)(t / 9 - 1) * plane + (int64_t)((t / 3) % 3 - 1) * NZ + (t % 3 - 1);
-      T xv = x[c];
-      if constexpr (DIR) xv += beta * pold[c];
       T v;
       if constexpr (std::is_same<VT, __nv_bfloat16>::value) v = (T)__bfloat162float(my[m[t]]);
       else v = (T)my[m[t]];
-      y[0] += v * xv;
+      y[0] += v * xv[t];
     }
     return;
   }
