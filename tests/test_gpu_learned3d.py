@@ -249,7 +249,8 @@ def test_trained_brick_network_cuts_krylov_iterations_at_128cube():
     """The committed 3-D network (trained on the 128^3 workload's family) inside mixed FCG on the
     first time step of the 128^3 backward-Euler heat workload: the step reaches the same
     solution as mixed Jacobi-PCG (1e-8 of its max; both Newton to a 1e-10 float64 residual
-    ratio) with under a third of its Krylov iterations (measured: 16 against 150)."""
+    ratio) with under a third of its Krylov iterations (measured with the default two damped
+    Jacobi sweeps: about a sixth)."""
     import os
     from autopdex_gb300 import learned, solver
     path = os.path.join(learned.WEIGHTS_DIR, "brick_unet_n128.npz")
