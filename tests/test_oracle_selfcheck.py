@@ -139,3 +139,38 @@ def test_potential_tangents_are_symmetric(kind):
     R, K = fun(*args)
     K = K.numpy().reshape(R.numel(), R.numel())
     assert np.abs(K - K.T).max() <= 1e-13 * np.abs(K).max()
+
+
+def test_brick_transfers_are_adjoint_and_interpolate_trilinear_fields():
+    """The oracle's 3-D transfers (the learned preconditioner's restriction and prolongation on
+    brick grids): restrict3 is the transpose of prolong3 (<P c, r> = <c, P^T r>), and prolong3
+    reproduces a trilinear field's nodal values exactly."""
+    from oracle import nn as onn
+    rng = np.random.default_rng(3)
+    for shape, f in (((3, 4, 5), 4), ((5, 5, 2), 2), ((2, 3, 2), 3)):
+        c = rng.standard_normal(shape)
+        fine = tuple((m - 1) * f + 1 for m in shape)
+        r = rng.standard_normal(fine)
+        assert abs((onn.prolong3(c, f) * r).sum() - (c * onn.restrict3(r, f, shape)).sum()) <= 1e-12 * np.abs(r).sum()
+        I, J, K = np.meshgrid(*(np.arange(m, dtype=float) for m in shape), indexing="ij")
+        lin = lambda x, y, z: 1.0 + 0.5 * x - 2.0 * y + 0.25 * z + 0.1 * x * y * z
+        fi, fj, fk = np.meshgrid(*(np.arange(m, dtype=float) / f for m in fine), indexing="ij")
+        assert np.abs(onn.prolong3(lin(I, J, K), f) - lin(fi, fj, fk)).max() <= 1e-12
+
+
+def test_unet3d_oracle_shapes_and_linearity_of_the_output_layer():
+    """The oracle's 3-D U-Net maps (B, D, H, W, 16) to (B, D, H, W, 16) for extents divisible by 8,
+    and its output layer (no ReLU) is affine in its input."""
+    from oracle import nn as onn
+    g = torch.Generator().manual_seed(1)
+    P = {n: (torch.randn(co, c1 + c2, 3, 3, 3, generator=g, dtype=torch.float64) * 0.1,
+             torch.randn(co, generator=g, dtype=torch.float64) * 0.1) for n, c1, c2, co, relu in onn.LAYERS3}
+    x = torch.randn(2, 8, 16, 8, 16, generator=g, dtype=torch.float64)
+    y = onn.unet3d(x, P)
+    assert y.shape == x.shape
+    w, b = P["out"]
+    a = torch.randn(1, 8, 8, 8, 16, generator=g, dtype=torch.float64)
+    c = torch.randn(1, 8, 8, 8, 16, generator=g, dtype=torch.float64)
+    lhs = onn.conv3d(a + c, w, b, 0)
+    rhs = onn.conv3d(a, w, b, 0) + onn.conv3d(c, w, torch.zeros_like(b), 0)
+    assert (lhs - rhs).abs().max() <= 1e-12 * lhs.abs().max()
