@@ -624,8 +624,9 @@ def rec_heat_be(n=128, steps=100, plain_steps=3):
                 ("plain_fp64_bicgstab", dict(solver="bicgstab", precision="float64"), 1e-11, plain_steps)]
     wpath = os.path.join(learned.WEIGHTS_DIR, f"brick_unet_n{n}.npz")
     if os.path.exists(wpath):
-        # inner tolerance 1e-4 (measured over 5 steps: 1e-3 / 1e-4 / 1e-5 -> 20 / 16 / 16 Newton
-        # steps, 35.5 / 29.4 / 32.2 ms per time step)
+        # inner tolerance 1e-4 (measured over 5 steps with Chebyshev smoothing: 1e-3 / 1e-4 / 1e-5
+        # -> 20 / 16 / 16 Newton steps, 35.5 / 29.4 / 32.2 ms per time step; over 10 steps with the
+        # damped Jacobi sweeps: 3e-5 / 1e-4 / 3e-4 / 1e-3 -> 20.6 / 19.8 / 20.0 / 19.7 ms)
         variants.insert(1, ("learned_mixed_fcg", dict(solver="fcg", precision="mixed",
                                                       **{"type of preconditioner": "learned"}), 1e-4, steps))
     for name, st, ktol, nsteps in variants:
