@@ -8,6 +8,7 @@
 // element and local node pair (a, b) the position of block (conn[a], conn[b]) is stored,
 // so that assembly adds element blocks straight into their final slots.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <thread>
 
@@ -124,21 +125,22 @@ void detect_structured_brick(agx_context* ctx, agx_element_set& s, const std::ve
   const int64_t nx = s.n_elem / (ny * nz);
   const int64_t sa = (ny + 1) * (nz + 1), sb = nz + 1;
   if ((nx + 1) * sa != ctx->n_nodes) return;
-  bool ok = true;
+  std::atomic<bool> conn_ok{true};  // written by the host threads of parallel_for
   parallel_for(nx, [&](int64_t b, int64_t e) {
-    for (int64_t i = b; i < e && ok; ++i)
+    for (int64_t i = b; i < e && conn_ok.load(std::memory_order_relaxed); ++i)
       for (int64_t j = 0; j < ny; ++j)
         for (int64_t k = 0; k < nz; ++k) {
           const int32_t* el = c + ((i * ny + j) * nz + k) * 8;
           const int64_t n0 = i * sa + j * sb + k;
           if (el[0] != n0 || el[1] != n0 + sa || el[2] != n0 + sa + sb || el[3] != n0 + sb || el[4] != n0 + 1 ||
               el[5] != n0 + sa + 1 || el[6] != n0 + sa + sb + 1 || el[7] != n0 + sb + 1) {
-            ok = false;
+            conn_ok.store(false, std::memory_order_relaxed);
             return;
           }
         }
   });
-  if (!ok) return;
+  if (!conn_ok.load()) return;
+  bool ok = true;
   for (int64_t i = 0; i <= nx && ok; ++i)
     for (int64_t j = 0; j <= ny && ok; ++j)
       for (int64_t k = 0; k <= nz; ++k) {
